@@ -1,0 +1,131 @@
+/*
+ * pasqual_gb300.h — C ABI of the GB300 (sm_103a) build of PASQUAL's hot path.
+ *
+ * Two layers, both plain C (pointers and sizes only):
+ *
+ *  1. pq_* — device-resident entry points.  Each one replaces one step of the reference's
+ *     construct_index()/construct_string_graph() and says which (file:line in the reference).
+ *     Host buffers are copied in and out; everything in between stays in GPU memory.
+ *
+ *  2. The reference's own entry points with the reference's own signatures and struct layouts
+ *     (construct_index, construct_string_graph, destroy_graph; src/index.h:63-68,
+ *     src/string_graph.h:139-142), exported by the same library so that the reference's main()
+ *     (src/test.c) and assemble() (src/assemble.c) link against it unchanged.  Those are declared
+ *     in pasqual_gb300_dropin.h.
+ *
+ * The library is built twice, like the reference (-D__INDEX_U32__ / -D__INDEX_U64__,
+ * src/common.h:31-44): libpasqual_gb300_u32.so (pq_idx = uint32_t) and
+ * libpasqual_gb300_u64.so (pq_idx = uint64_t, define PQ_IDX64 before including this header).
+ *
+ * Errors: every int-returning function returns PQ_OK (0) or a PQ_ERR_* code and keeps a message
+ * for pq_last_error().  Nothing calls exit(); the drop-in layer maps errors to the reference's
+ * ERROR_EXIT behaviour (message on stderr, exit status 0, src/common.h:87-94).
+ *
+ * Threading: a context is used from one host thread at a time; all its work is ordered on the
+ * CUDA stream given to pq_create (its own stream when NULL).
+ */
+#ifndef PASQUAL_GB300_H
+#define PASQUAL_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#ifdef PQ_IDX64
+typedef uint64_t pq_idx;
+#else
+typedef uint32_t pq_idx;
+#endif
+
+#define PQ_OK 0
+#define PQ_ERR_ARG 1
+#define PQ_ERR_CUDA 2
+#define PQ_ERR_NOMEM 3
+#define PQ_ERR_TOO_MANY_EDGES 4 /* a read has > 65535 edges on one side (src/string_graph.c:469-472) */
+#define PQ_ERR_STATE 5          /* a step was called before the one it depends on */
+#define PQ_ERR_CAPACITY 6       /* a read's interval table outgrew (2L)^2 (src/string_graph.c:542) */
+#define PQ_ERR_INTERNAL 7
+
+#if defined(__GNUC__)
+#define PQ_API __attribute__ ((visibility ("default")))
+#else
+#define PQ_API
+#endif
+
+typedef struct pq_ctx pq_ctx;
+
+/* Width of pq_idx in bytes (4 or 8): lets a loader check it bound the right build. */
+PQ_API int pq_idx_bytes (void);
+
+/* Create a context on CUDA device `device`; `cuda_stream` is a cudaStream_t or NULL. */
+PQ_API int pq_create (pq_ctx ** out, int device, void *cuda_stream);
+PQ_API void pq_destroy (pq_ctx * ctx);
+PQ_API const char *pq_last_error (const pq_ctx * ctx);
+
+/* Reads after import and de-duplication: num_reads * read_len base codes 1..4 (A,C,G,T), the
+ * layout of index_t.reads after import_singlereads (src/index.c:145-405).  min_overlap is the
+ * -t of the CLI, with SEQ_DEPTH(9) < min_overlap < read_len (src/test.c:306-311).
+ * from_device != 0: `reads` is a device pointer. */
+PQ_API int pq_set_reads (pq_ctx * ctx, const uint8_t * reads, pq_idx num_reads, int read_len,
+                  int min_overlap, int from_device);
+
+/* C[6], suffix_count[4], prefix_count[4] of index_t (src/index.c:336-346, 367-372). */
+PQ_API int pq_get_counts (pq_ctx * ctx, pq_idx C[6], pq_idx suffix_count[4], pq_idx prefix_count[4]);
+
+/* Suffix array of direction dir (0: the reads; 1: every read reversed), in the order the
+ * reference's sufsort produces single-threaded: read-bounded suffixes, end-of-read lowest, ties
+ * by text position.  Replaces transform_to_triplet[_reverse] + initial_sort + suf_sort over the
+ * five slots (src/sufsort.h:29-46, driven by src/index.c:558-585). */
+PQ_API int pq_sort (pq_ctx * ctx, int dir);
+/* Use a given suffix array instead of sorting (testing and external sorters). */
+PQ_API int pq_set_sa (pq_ctx * ctx, int dir, const pq_idx * sa, int from_device);
+PQ_API int pq_get_sa (pq_ctx * ctx, int dir, pq_idx * sa_host);
+
+/* FM-index of direction dir from its suffix array: BWT, occurrence blocks, reads_index and the
+ * k-mer seed table.  Replaces build_OCC + the occ prefix sum (src/index.c:26-142, 587-615). */
+PQ_API int pq_build_fm (pq_ctx * ctx, int dir);
+
+/* Both directions, sort + FM-index: the body of build_index (src/index.c:626-706). */
+PQ_API int pq_build_index (pq_ctx * ctx);
+
+/* Reference-layout copies of an FM-index (index_t.OCC_bitmap[5] back to back, each
+ * (n+64)/64 words; OCC_sample (n+64)/64*5 entries; reads_index num_reads entries). */
+PQ_API int pq_get_index_ref (pq_ctx * ctx, int dir, uint64_t * bitmap, pq_idx * sample,
+                      pq_idx * reads_index);
+
+/* Per-read seed intervals written into index_t.interval_start/end/depth (src/index.h:36-41):
+ * the exact SA interval of the read's last (dir 0) / first, reversed (dir 1) k bases. */
+PQ_API int pq_get_seeds (pq_ctx * ctx, int dir, pq_idx * start, pq_idx * size, uint16_t * depth);
+
+/* Seed depth k of the overlap search (1 <= k <= min(13, t)); default min(12, t). */
+PQ_API int pq_set_seed_k (pq_ctx * ctx, int k);
+
+/* Overlap search with transitive reduction for every read: find_intervals +
+ * extract_bw_edges + extract_fw_edges (src/string_graph.c:163-731) as driven by
+ * construct_string_graph (src/string_graph.c:800-830). */
+PQ_API int pq_overlaps (pq_ctx * ctx);
+
+/* Sizes of the last pq_overlaps result.  probes = rank probes issued (one 32-byte sector
+ * each); wide_reads = reads that needed the wide-scratch kernel. */
+PQ_API int pq_get_graph_sizes (pq_ctx * ctx, uint64_t * num_edges, uint64_t * probes,
+                        uint64_t * wide_reads);
+
+/* Copy the last pq_overlaps result to host arrays.  Per read: num_B, num_F (node_t.num_B/F),
+ * olp_B, olp_F (overlaps_B/F of src/string_graph.c:807-808), edge_off[num_reads+1].  Per edge,
+ * B edges then F edges of each read in the reference's DFS order: dest, overlap length, type
+ * (BF=0 FB=1 FF=2 BB=3) and the path_t.trans value (src/string_graph.c:940, 970). */
+PQ_API int pq_get_graph (pq_ctx * ctx, uint16_t * num_B, uint16_t * num_F, int32_t * olp_B,
+                  int32_t * olp_F, uint64_t * edge_off, pq_idx * dest, uint16_t * len,
+                  uint8_t * type, int32_t * trans);
+
+/* Time (ms, CUDA events on the context stream) of the last pq_sort/pq_build_fm/pq_overlaps. */
+PQ_API int pq_get_stage_ms (pq_ctx * ctx, float *sort_ms, float *fm_ms, float *search_ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,237 @@
+"""pasqual_gb300 — GB300 (sm_103a) build of PASQUAL's hot path behind a C ABI.
+
+The product is the CUDA library ``pasqual_gb300/_build/libpasqual_gb300_u{32,64}.so`` (C ABI
+declared in ``include/pasqual_gb300.h``).  This module is a thin ctypes host mirror of the
+reference's two entry points on the path:
+
+* :meth:`Pasqual.construct_index`        ~ ``construct_index`` (src/index.h:63-68) without the
+  FASTA import: reads in, both FM-indexes built on the GPU;
+* :meth:`Pasqual.construct_string_graph` ~ ``construct_string_graph`` (src/string_graph.h:139):
+  per-read irreducible edges in the reference's node order.
+
+There is no CPU fallback: if the CUDA library is missing or no GPU is present, these calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import build as _build
+
+__all__ = ["Pasqual", "Graph", "PQError", "load_library", "library_path", "EXPORTS"]
+
+PQ_ERRORS = {1: "PQ_ERR_ARG", 2: "PQ_ERR_CUDA", 3: "PQ_ERR_NOMEM", 4: "PQ_ERR_TOO_MANY_EDGES",
+             5: "PQ_ERR_STATE", 6: "PQ_ERR_CAPACITY", 7: "PQ_ERR_INTERNAL"}
+
+# Every entry point of include/pasqual_gb300.h (checked against the header by the tests).
+EXPORTS = ["pq_idx_bytes", "pq_create", "pq_destroy", "pq_last_error", "pq_set_reads",
+           "pq_get_counts", "pq_sort", "pq_set_sa", "pq_get_sa", "pq_build_fm", "pq_build_index",
+           "pq_get_index_ref", "pq_get_seeds", "pq_set_seed_k", "pq_overlaps",
+           "pq_get_graph_sizes", "pq_get_graph", "pq_get_stage_ms"]
+
+
+class PQError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__("%s: %s" % (PQ_ERRORS.get(code, "PQ_ERR_%d" % code), msg))
+        self.code = code
+
+
+def library_path(width: int = 32) -> str:
+    return _build.lib_path(width)
+
+
+_LIBS: dict = {}
+
+
+def load_library(width: int = 32) -> ct.CDLL:
+    """Load the CUDA library of one index width; raise if it was not built."""
+    if width in _LIBS:
+        return _LIBS[width]
+    path = library_path(width)
+    if not os.path.exists(path):
+        raise RuntimeError("pasqual_gb300 CUDA library not built: %s (run "
+                           "`python -c 'import __graft_entry__ as g; g.build()'`)" % path)
+    lib = ct.CDLL(path)
+    I = ct.c_uint64 if width == 64 else ct.c_uint32
+    vp, c_int = ct.c_void_p, ct.c_int
+    sig = {
+        "pq_idx_bytes": (c_int, []),
+        "pq_create": (c_int, [ct.POINTER(vp), c_int, vp]),
+        "pq_destroy": (None, [vp]),
+        "pq_last_error": (ct.c_char_p, [vp]),
+        "pq_set_reads": (c_int, [vp, vp, I, c_int, c_int, c_int]),
+        "pq_get_counts": (c_int, [vp, vp, vp, vp]),
+        "pq_sort": (c_int, [vp, c_int]),
+        "pq_set_sa": (c_int, [vp, c_int, vp, c_int]),
+        "pq_get_sa": (c_int, [vp, c_int, vp]),
+        "pq_build_fm": (c_int, [vp, c_int]),
+        "pq_build_index": (c_int, [vp]),
+        "pq_get_index_ref": (c_int, [vp, c_int, vp, vp, vp]),
+        "pq_get_seeds": (c_int, [vp, c_int, vp, vp, vp]),
+        "pq_set_seed_k": (c_int, [vp, c_int]),
+        "pq_overlaps": (c_int, [vp]),
+        "pq_get_graph_sizes": (c_int, [vp, vp, vp, vp]),
+        "pq_get_graph": (c_int, [vp] + [vp] * 9),
+        "pq_get_stage_ms": (c_int, [vp, vp, vp, vp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    if lib.pq_idx_bytes() * 8 != width:
+        raise RuntimeError("library %s has the wrong index width" % path)
+    _LIBS[width] = lib
+    return lib
+
+
+@dataclass
+class Graph:
+    """Overlap-search output: per read (num_B, num_F, olp_B, olp_F, edge_off) and per edge
+    (dest, length, etype, trans), B edges then F edges of each read, reference DFS order."""
+    num_B: np.ndarray
+    num_F: np.ndarray
+    olp_B: np.ndarray
+    olp_F: np.ndarray
+    edge_off: np.ndarray
+    dest: np.ndarray
+    length: np.ndarray
+    etype: np.ndarray
+    trans: np.ndarray
+    probes: int = 0
+    wide_reads: int = 0
+
+
+def _p(a: np.ndarray) -> ct.c_void_p:
+    return a.ctypes.data_as(ct.c_void_p)
+
+
+class Pasqual:
+    """One GPU context holding both FM-indexes of a read set (index width 32 or 64)."""
+
+    def __init__(self, width: int = 32, device: int = 0, stream: int | None = None):
+        self.width = width
+        self.lib = load_library(width)
+        self.dt = np.uint64 if width == 64 else np.uint32
+        h = ct.c_void_p()
+        rc = self.lib.pq_create(ct.byref(h), device, ct.c_void_p(stream) if stream else None)
+        if rc != 0:
+            raise PQError(rc, "pq_create failed (no CUDA device?)")
+        self.h = h
+        self.num_reads = 0
+        self.read_len = 0
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.pq_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _ck(self, rc: int, what: str) -> None:
+        if rc != 0:
+            msg = self.lib.pq_last_error(self.h)
+            raise PQError(rc, "%s: %s" % (what, msg.decode() if msg else ""))
+
+    # -- construct_index -------------------------------------------------------------------
+    def set_reads(self, reads: np.ndarray, min_overlap: int) -> None:
+        reads = np.ascontiguousarray(reads, dtype=np.uint8)
+        nr, L = reads.shape
+        self._ck(self.lib.pq_set_reads(self.h, _p(reads), nr, L, int(min_overlap), 0),
+                 "pq_set_reads")
+        self.num_reads, self.read_len = nr, L
+
+    def set_seed_k(self, k: int) -> None:
+        self._ck(self.lib.pq_set_seed_k(self.h, int(k)), "pq_set_seed_k")
+
+    def sort(self, direction: int) -> None:
+        self._ck(self.lib.pq_sort(self.h, direction), "pq_sort")
+
+    def set_sa(self, direction: int, sa: np.ndarray) -> None:
+        sa = np.ascontiguousarray(sa, dtype=self.dt)
+        self._ck(self.lib.pq_set_sa(self.h, direction, _p(sa), 0), "pq_set_sa")
+
+    def get_sa(self, direction: int) -> np.ndarray:
+        sa = np.empty(self.num_reads * self.read_len, self.dt)
+        self._ck(self.lib.pq_get_sa(self.h, direction, _p(sa)), "pq_get_sa")
+        return sa
+
+    def build_fm(self, direction: int) -> None:
+        self._ck(self.lib.pq_build_fm(self.h, direction), "pq_build_fm")
+
+    def build_index(self) -> None:
+        self._ck(self.lib.pq_build_index(self.h), "pq_build_index")
+
+    def construct_index(self, reads: np.ndarray, min_overlap: int) -> None:
+        """Reads (codes 1..4, [num_reads, read_len]) -> both FM-indexes on the GPU."""
+        self.set_reads(reads, min_overlap)
+        self.build_index()
+
+    def counts(self):
+        C = np.zeros(6, self.dt)
+        s = np.zeros(4, self.dt)
+        p = np.zeros(4, self.dt)
+        self._ck(self.lib.pq_get_counts(self.h, _p(C), _p(s), _p(p)), "pq_get_counts")
+        return C, s, p
+
+    def index_ref(self, direction: int):
+        """Reference-layout (OCC_bitmap[5] concatenated, OCC_sample, reads_index)."""
+        n = self.num_reads * self.read_len
+        rowlen = n // 64 + 1
+        bm = np.empty(5 * rowlen, np.uint64)
+        smp = np.empty(5 * rowlen, self.dt)
+        ri = np.empty(max(self.num_reads, 1), self.dt)
+        self._ck(self.lib.pq_get_index_ref(self.h, direction, _p(bm), _p(smp), _p(ri)),
+                 "pq_get_index_ref")
+        return bm, smp, ri[:self.num_reads]
+
+    def seeds(self, direction: int):
+        nr = max(self.num_reads, 1)
+        s = np.empty(nr, self.dt)
+        z = np.empty(nr, self.dt)
+        d = np.empty(nr, np.uint16)
+        self._ck(self.lib.pq_get_seeds(self.h, direction, _p(s), _p(z), _p(d)), "pq_get_seeds")
+        return s[:self.num_reads], z[:self.num_reads], d[:self.num_reads]
+
+    # -- construct_string_graph ------------------------------------------------------------
+    def overlaps(self) -> None:
+        self._ck(self.lib.pq_overlaps(self.h), "pq_overlaps")
+
+    def graph(self) -> Graph:
+        ne = ct.c_uint64()
+        pr = ct.c_uint64()
+        wr = ct.c_uint64()
+        self._ck(self.lib.pq_get_graph_sizes(self.h, ct.byref(ne), ct.byref(pr), ct.byref(wr)),
+                 "pq_get_graph_sizes")
+        nr, m = self.num_reads, ne.value
+        g = Graph(num_B=np.empty(nr, np.uint16), num_F=np.empty(nr, np.uint16),
+                  olp_B=np.empty(nr, np.int32), olp_F=np.empty(nr, np.int32),
+                  edge_off=np.empty(nr + 1, np.uint64), dest=np.empty(m, self.dt),
+                  length=np.empty(m, np.uint16), etype=np.empty(m, np.uint8),
+                  trans=np.empty(m, np.int32), probes=pr.value, wide_reads=wr.value)
+        self._ck(self.lib.pq_get_graph(self.h, _p(g.num_B), _p(g.num_F), _p(g.olp_B), _p(g.olp_F),
+                                       _p(g.edge_off), _p(g.dest), _p(g.length), _p(g.etype),
+                                       _p(g.trans)), "pq_get_graph")
+        return g
+
+    def construct_string_graph(self) -> Graph:
+        self.overlaps()
+        return self.graph()
+
+    def stage_ms(self):
+        a, b, c = ct.c_float(), ct.c_float(), ct.c_float()
+        self._ck(self.lib.pq_get_stage_ms(self.h, ct.byref(a), ct.byref(b), ct.byref(c)),
+                 "pq_get_stage_ms")
+        return a.value, b.value, c.value

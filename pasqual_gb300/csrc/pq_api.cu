@@ -1,0 +1,553 @@
+// pq_api.cu — the C ABI (include/pasqual_gb300.h): a context owning the device buffers of both
+// FM-indexes and the overlap-search output, and the entry points that sequence the kernels.
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <algorithm>
+
+#include "pq_index.cuh"
+#include "pq_sort.cuh"
+#include "../../include/pasqual_gb300.h"
+
+static_assert(sizeof(pq_idx) == sizeof(idx_t), "pq_idx and idx_t must agree");
+
+namespace {
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t want) {
+        if (want <= bytes && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&p, want ? want : 16);
+        if (e == cudaSuccess) bytes = want;
+        return e;
+    }
+    // grow keeping the first `keep` bytes
+    cudaError_t grow(size_t want, size_t keep, cudaStream_t st) {
+        if (want <= bytes && p) return cudaSuccess;
+        void* q = nullptr;
+        cudaError_t e = cudaMalloc(&q, want);
+        if (e != cudaSuccess) return e;
+        if (p && keep) cudaMemcpyAsync(q, p, std::min(keep, bytes), cudaMemcpyDeviceToDevice, st);
+        cudaStreamSynchronize(st);
+        if (p) cudaFree(p);
+        p = q;
+        bytes = want;
+        return cudaSuccess;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <class T> T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+}  // namespace
+
+struct pq_ctx {
+    int device = 0;
+    cudaStream_t st = nullptr;
+    bool own_stream = false;
+    std::string err;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    float ms_sort = 0, ms_fm = 0, ms_search = 0;
+
+    idx_t num_reads = 0;
+    int L = 0, t = 0;
+    int seed_k = 0;
+    DevBuf reads;
+    idx_t C[6] = {0}, sfx[4] = {0}, pfx[4] = {0};
+    bool have_reads = false;
+
+    // per direction
+    DevBuf sa[2], blk[2], sb[2], ri[2], kstart[2], kend[2];
+    bool sa_ok[2] = {false, false}, fm_ok[2] = {false, false};
+    int fm_k[2] = {0, 0};
+    DevBuf ktmp, sort_tmp, counts;
+
+    // overlap-search output
+    DevBuf nB, nF, oB, oF, status, esrc, e_dest, e_trans, e_len, e_type, ctrs, ovf_list;
+    DevBuf off, g_dest, g_len, g_type, g_trans, asm_tmp, wide;
+    bool graph_ok = false;
+    uint64_t num_edges = 0, probes = 0, wide_reads = 0;
+};
+
+static int fail(pq_ctx* c, int code, const std::string& msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+#define CK(call)                                                                                   \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess)                                                                     \
+            return fail(ctx, e_ == cudaErrorMemoryAllocation ? PQ_ERR_NOMEM : PQ_ERR_CUDA,        \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                      \
+    } while (0)
+
+static inline size_t n_rows(const pq_ctx* c) { return size_t(c->num_reads) * size_t(c->L); }
+static inline size_t n_blocks(const pq_ctx* c) { return n_rows(c) / 64 + 1; }
+static inline size_t n_supers(const pq_ctx* c) {
+    return (n_blocks(c) + kBlocksPerSuper - 1) / kBlocksPerSuper;
+}
+
+extern "C" {
+
+int pq_idx_bytes(void) { return int(sizeof(idx_t)); }
+
+int pq_create(pq_ctx** out, int device, void* cuda_stream) {
+    if (!out) return PQ_ERR_ARG;
+    *out = nullptr;
+    pq_ctx* ctx = new (std::nothrow) pq_ctx();
+    if (!ctx) return PQ_ERR_NOMEM;
+    ctx->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) {
+        delete ctx;
+        return PQ_ERR_CUDA;
+    }
+    if (cuda_stream) {
+        ctx->st = reinterpret_cast<cudaStream_t>(cuda_stream);
+    } else {
+        if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess) {
+            delete ctx;
+            return PQ_ERR_CUDA;
+        }
+        ctx->own_stream = true;
+    }
+    cudaEventCreate(&ctx->ev0);
+    cudaEventCreate(&ctx->ev1);
+    *out = ctx;
+    return PQ_OK;
+}
+
+void pq_destroy(pq_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->st);
+    DevBuf* bufs[] = {&ctx->reads, &ctx->ktmp, &ctx->sort_tmp, &ctx->counts, &ctx->nB, &ctx->nF, &ctx->oB,
+                      &ctx->oF, &ctx->status, &ctx->esrc, &ctx->e_dest, &ctx->e_trans, &ctx->e_len,
+                      &ctx->e_type, &ctx->ctrs, &ctx->ovf_list, &ctx->off, &ctx->g_dest, &ctx->g_len,
+                      &ctx->g_type, &ctx->g_trans, &ctx->asm_tmp, &ctx->wide};
+    for (DevBuf* b : bufs) b->release();
+    for (int d = 0; d < 2; ++d) {
+        ctx->sa[d].release();
+        ctx->blk[d].release();
+        ctx->sb[d].release();
+        ctx->ri[d].release();
+        ctx->kstart[d].release();
+        ctx->kend[d].release();
+    }
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->st);
+    delete ctx;
+}
+
+const char* pq_last_error(const pq_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+int pq_set_reads(pq_ctx* ctx, const uint8_t* reads, pq_idx num_reads, int read_len, int min_overlap,
+                 int from_device) {
+    if (!ctx) return PQ_ERR_ARG;
+    if (read_len <= 0 || read_len > 65535)
+        return fail(ctx, PQ_ERR_ARG, "invalid read length, valid range (0, 65535]");
+    if (min_overlap <= 9 || min_overlap >= read_len)
+        return fail(ctx, PQ_ERR_ARG, "invalid minimum overlap length, valid range (9, read_len)");
+    const unsigned __int128 n = (unsigned __int128)num_reads * (unsigned)read_len;
+    if (n >> (8 * sizeof(idx_t) - 1))
+        return fail(ctx, PQ_ERR_ARG, "num_reads * read_len does not fit the index width");
+    if (num_reads && !reads) return fail(ctx, PQ_ERR_ARG, "reads is NULL");
+    cudaSetDevice(ctx->device);
+    ctx->num_reads = num_reads;
+    ctx->L = read_len;
+    ctx->t = min_overlap;
+    if (!ctx->seed_k) ctx->seed_k = std::min(12, min_overlap);
+    ctx->seed_k = std::min(ctx->seed_k, min_overlap);
+    size_t bytes = size_t(num_reads) * read_len;
+    CK(ctx->reads.ensure(bytes + 64));
+    if (bytes)
+        CK(cudaMemcpyAsync(ctx->reads.p, reads, bytes, from_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                           ctx->st));
+    CK(ctx->counts.ensure(12 * sizeof(unsigned long long)));
+    CK(pq::read_counts(ctx->reads.as<uint8_t>(), num_reads, idx_t(read_len),
+                       ctx->counts.as<unsigned long long>(), ctx->st));
+    unsigned long long h[12];
+    CK(cudaMemcpyAsync(h, ctx->counts.p, sizeof h, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->C[0] = 0;
+    ctx->C[1] = 0;
+    ctx->C[2] = idx_t(h[0]);
+    ctx->C[3] = idx_t(h[0] + h[1]);
+    ctx->C[4] = idx_t(h[0] + h[1] + h[2]);
+    ctx->C[5] = idx_t(h[0] + h[1] + h[2] + h[3]);
+    for (int c = 0; c < 4; ++c) {
+        ctx->sfx[c] = idx_t(h[4 + c]);
+        ctx->pfx[c] = idx_t(h[8 + c]);
+    }
+    ctx->have_reads = true;
+    ctx->sa_ok[0] = ctx->sa_ok[1] = false;
+    ctx->fm_ok[0] = ctx->fm_ok[1] = false;
+    ctx->graph_ok = false;
+    return PQ_OK;
+}
+
+int pq_get_counts(pq_ctx* ctx, pq_idx C[6], pq_idx suffix_count[4], pq_idx prefix_count[4]) {
+    if (!ctx) return PQ_ERR_ARG;
+    if (!ctx->have_reads) return fail(ctx, PQ_ERR_STATE, "pq_set_reads first");
+    if (C) memcpy(C, ctx->C, sizeof ctx->C);
+    if (suffix_count) memcpy(suffix_count, ctx->sfx, sizeof ctx->sfx);
+    if (prefix_count) memcpy(prefix_count, ctx->pfx, sizeof ctx->pfx);
+    return PQ_OK;
+}
+
+int pq_sort(pq_ctx* ctx, int dir) {
+    if (!ctx || (dir != 0 && dir != 1)) return PQ_ERR_ARG;
+    if (!ctx->have_reads) return fail(ctx, PQ_ERR_STATE, "pq_set_reads first");
+    cudaSetDevice(ctx->device);
+    const size_t n = n_rows(ctx);
+    CK(ctx->sa[dir].ensure(n * sizeof(idx_t) + 64));
+    size_t tmp_bytes = pq::suffix_sort_tmp_bytes(n);
+    CK(ctx->sort_tmp.ensure(tmp_bytes));
+    CK(cudaEventRecord(ctx->ev0, ctx->st));
+    int rc = pq::suffix_sort(ctx->reads.as<uint8_t>(), ctx->num_reads, ctx->L, dir, ctx->sa[dir].as<idx_t>(),
+                             ctx->sort_tmp.p, tmp_bytes, ctx->st);
+    if (rc != 0) return fail(ctx, PQ_ERR_CUDA, std::string("suffix sort failed: ") + cudaGetErrorString(cudaGetLastError()));
+    CK(cudaEventRecord(ctx->ev1, ctx->st));
+    CK(cudaEventSynchronize(ctx->ev1));
+    cudaEventElapsedTime(&ctx->ms_sort, ctx->ev0, ctx->ev1);
+    ctx->sa_ok[dir] = true;
+    ctx->fm_ok[dir] = false;
+    ctx->graph_ok = false;
+    return PQ_OK;
+}
+
+int pq_set_sa(pq_ctx* ctx, int dir, const pq_idx* sa, int from_device) {
+    if (!ctx || (dir != 0 && dir != 1)) return PQ_ERR_ARG;
+    if (!ctx->have_reads) return fail(ctx, PQ_ERR_STATE, "pq_set_reads first");
+    cudaSetDevice(ctx->device);
+    const size_t n = n_rows(ctx);
+    CK(ctx->sa[dir].ensure(n * sizeof(idx_t) + 64));
+    if (n)
+        CK(cudaMemcpyAsync(ctx->sa[dir].p, sa, n * sizeof(idx_t),
+                           from_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->sa_ok[dir] = true;
+    ctx->fm_ok[dir] = false;
+    ctx->graph_ok = false;
+    return PQ_OK;
+}
+
+int pq_get_sa(pq_ctx* ctx, int dir, pq_idx* sa_host) {
+    if (!ctx || (dir != 0 && dir != 1) || !sa_host) return PQ_ERR_ARG;
+    if (!ctx->sa_ok[dir]) return fail(ctx, PQ_ERR_STATE, "no suffix array for this direction");
+    const size_t n = n_rows(ctx);
+    if (n) CK(cudaMemcpyAsync(sa_host, ctx->sa[dir].p, n * sizeof(idx_t), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return PQ_OK;
+}
+
+int pq_set_seed_k(pq_ctx* ctx, int k) {
+    if (!ctx) return PQ_ERR_ARG;
+    if (k < 1 || k > 13) return fail(ctx, PQ_ERR_ARG, "seed depth must be in [1, 13]");
+    if (ctx->have_reads && k > ctx->t) return fail(ctx, PQ_ERR_ARG, "seed depth must not exceed t");
+    ctx->seed_k = k;
+    return PQ_OK;
+}
+
+int pq_build_fm(pq_ctx* ctx, int dir) {
+    if (!ctx || (dir != 0 && dir != 1)) return PQ_ERR_ARG;
+    if (!ctx->sa_ok[dir]) return fail(ctx, PQ_ERR_STATE, "no suffix array for this direction");
+    cudaSetDevice(ctx->device);
+    const size_t n = n_rows(ctx);
+    CK(ctx->blk[dir].ensure(n_blocks(ctx) * sizeof(OccBlock)));
+    CK(ctx->sb[dir].ensure(n_supers(ctx) * 4 * sizeof(idx_t) + 64));
+    CK(ctx->ri[dir].ensure(size_t(ctx->num_reads) * sizeof(idx_t) + 64));
+    const int k = ctx->seed_k;
+    const size_t nk = size_t(1) << (2 * k);
+    CK(ctx->kstart[dir].ensure(nk * sizeof(idx_t)));
+    CK(ctx->kend[dir].ensure(nk * sizeof(idx_t)));
+    CK(ctx->ktmp.ensure(n * sizeof(uint32_t) + 64));
+    CK(cudaEventRecord(ctx->ev0, ctx->st));
+    CK(pq::build_occ(ctx->sa[dir].as<idx_t>(), ctx->reads.as<uint8_t>(), ctx->num_reads, idx_t(ctx->L), dir,
+                     ctx->blk[dir].as<OccBlock>(), ctx->sb[dir].as<idx_t>(), ctx->ri[dir].as<idx_t>(), ctx->st));
+    CK(pq::build_kmer_table(ctx->sa[dir].as<idx_t>(), ctx->reads.as<uint8_t>(), ctx->num_reads, idx_t(ctx->L), dir,
+                            k, ctx->ktmp.as<uint32_t>(), ctx->kstart[dir].as<idx_t>(), ctx->kend[dir].as<idx_t>(),
+                            ctx->st));
+    CK(cudaEventRecord(ctx->ev1, ctx->st));
+    CK(cudaEventSynchronize(ctx->ev1));
+    cudaEventElapsedTime(&ctx->ms_fm, ctx->ev0, ctx->ev1);
+    ctx->fm_ok[dir] = true;
+    ctx->fm_k[dir] = k;
+    ctx->graph_ok = false;
+    return PQ_OK;
+}
+
+int pq_build_index(pq_ctx* ctx) {
+    if (!ctx) return PQ_ERR_ARG;
+    float s = 0, f = 0;
+    for (int d = 0; d < 2; ++d) {
+        int rc = pq_sort(ctx, d);
+        if (rc) return rc;
+        s += ctx->ms_sort;
+        rc = pq_build_fm(ctx, d);
+        if (rc) return rc;
+        f += ctx->ms_fm;
+    }
+    ctx->ms_sort = s;
+    ctx->ms_fm = f;
+    return PQ_OK;
+}
+
+int pq_get_index_ref(pq_ctx* ctx, int dir, uint64_t* bitmap, pq_idx* sample, pq_idx* reads_index) {
+    if (!ctx || (dir != 0 && dir != 1)) return PQ_ERR_ARG;
+    if (!ctx->fm_ok[dir]) return fail(ctx, PQ_ERR_STATE, "no FM-index for this direction");
+    cudaSetDevice(ctx->device);
+    const size_t nblk = n_blocks(ctx);
+    if (bitmap || sample) {
+        DevBuf bm, smp;
+        CK(bm.ensure(nblk * 5 * sizeof(uint64_t)));
+        CK(smp.ensure(nblk * 5 * sizeof(idx_t)));
+        const idx_t* fix = dir == 0 ? ctx->sfx : ctx->pfx;
+        CK(pq::export_ref_layout(ctx->blk[dir].as<OccBlock>(), ctx->sb[dir].as<idx_t>(), ctx->num_reads,
+                                 idx_t(ctx->L), fix, bm.as<uint64_t>(), smp.as<idx_t>(), ctx->st));
+        if (bitmap) CK(cudaMemcpyAsync(bitmap, bm.p, nblk * 5 * sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx->st));
+        if (sample) CK(cudaMemcpyAsync(sample, smp.p, nblk * 5 * sizeof(idx_t), cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+        bm.release();
+        smp.release();
+    }
+    if (reads_index && ctx->num_reads)
+        CK(cudaMemcpyAsync(reads_index, ctx->ri[dir].p, size_t(ctx->num_reads) * sizeof(idx_t),
+                           cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return PQ_OK;
+}
+
+int pq_get_seeds(pq_ctx* ctx, int dir, pq_idx* start, pq_idx* size, uint16_t* depth) {
+    if (!ctx || (dir != 0 && dir != 1)) return PQ_ERR_ARG;
+    if (!ctx->fm_ok[dir]) return fail(ctx, PQ_ERR_STATE, "no FM-index for this direction");
+    cudaSetDevice(ctx->device);
+    const size_t nr = ctx->num_reads;
+    if (!nr) return PQ_OK;
+    DevBuf s, z;
+    CK(s.ensure(nr * sizeof(idx_t)));
+    CK(z.ensure(nr * sizeof(idx_t)));
+    CK(pq::read_seeds(ctx->reads.as<uint8_t>(), ctx->num_reads, ctx->L, dir, ctx->fm_k[dir],
+                      ctx->kstart[dir].as<idx_t>(), ctx->kend[dir].as<idx_t>(), s.as<idx_t>(), z.as<idx_t>(), ctx->st));
+    if (start) CK(cudaMemcpyAsync(start, s.p, nr * sizeof(idx_t), cudaMemcpyDeviceToHost, ctx->st));
+    if (size) CK(cudaMemcpyAsync(size, z.p, nr * sizeof(idx_t), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    if (depth)
+        for (size_t i = 0; i < nr; ++i) depth[i] = uint16_t(ctx->fm_k[dir]);
+    return PQ_OK;
+}
+
+int pq_overlaps(pq_ctx* ctx) {
+    if (!ctx) return PQ_ERR_ARG;
+    if (!ctx->fm_ok[0] || !ctx->fm_ok[1]) return fail(ctx, PQ_ERR_STATE, "build both FM-indexes first");
+    if (ctx->fm_k[0] != ctx->fm_k[1]) return fail(ctx, PQ_ERR_STATE, "seed tables of different depth");
+    cudaSetDevice(ctx->device);
+    const size_t nr = ctx->num_reads;
+    const size_t nrp = nr + 1;
+    CK(ctx->nB.ensure(nrp * 2));
+    CK(ctx->nF.ensure(nrp * 2));
+    CK(ctx->oB.ensure(nrp * 4));
+    CK(ctx->oF.ensure(nrp * 4));
+    CK(ctx->status.ensure(nrp));
+    CK(ctx->esrc.ensure(nrp * 8));
+    CK(ctx->ovf_list.ensure(nrp * sizeof(idx_t)));
+    CK(ctx->ctrs.ensure(64));
+    size_t ecap = std::max<size_t>(ctx->e_dest.bytes / sizeof(idx_t), nr * 6 + 4096);
+    CK(ctx->e_dest.ensure(ecap * sizeof(idx_t)));
+    CK(ctx->e_trans.ensure(ecap * 4));
+    CK(ctx->e_len.ensure(ecap * 2));
+    CK(ctx->e_type.ensure(ecap));
+
+    pq::SearchArgs A;
+    for (int d = 0; d < 2; ++d) {
+        FmView& f = A.fm[d];
+        f.blk = ctx->blk[d].as<OccBlock>();
+        f.sb = ctx->sb[d].as<idx_t>();
+        f.reads_index = ctx->ri[d].as<idx_t>();
+        f.kstart = ctx->kstart[d].as<idx_t>();
+        f.kend = ctx->kend[d].as<idx_t>();
+        const idx_t* fix = d == 0 ? ctx->sfx : ctx->pfx;
+        f.Cf[0] = ctx->C[0];
+        for (int c = 1; c <= 4; ++c) f.Cf[c] = ctx->C[c] + fix[c - 1];
+    }
+    A.reads = ctx->reads.as<uint8_t>();
+    A.num_reads = ctx->num_reads;
+    A.L = ctx->L;
+    A.t = ctx->t;
+    A.seed_k = ctx->fm_k[0];
+
+    unsigned long long* ctr = ctx->ctrs.as<unsigned long long>();   // [0] e_count [1] probes [2] ovf(u32)
+    pq::SearchOut O;
+    O.num_B = ctx->nB.as<uint16_t>();
+    O.num_F = ctx->nF.as<uint16_t>();
+    O.olp_B = ctx->oB.as<int32_t>();
+    O.olp_F = ctx->oF.as<int32_t>();
+    O.status = ctx->status.as<uint8_t>();
+    O.edge_src = ctx->esrc.as<unsigned long long>();
+    O.e_dest = ctx->e_dest.as<idx_t>();
+    O.e_trans = ctx->e_trans.as<int32_t>();
+    O.e_len = ctx->e_len.as<uint16_t>();
+    O.e_type = ctx->e_type.as<uint8_t>();
+    O.e_count = ctr + 0;
+    O.e_cap = ecap;
+    O.ovf_list = ctx->ovf_list.as<idx_t>();
+    O.ovf_count = reinterpret_cast<unsigned int*>(ctr + 2);
+    O.probes = ctr + 1;
+
+    CK(cudaMemsetAsync(ctr, 0, 64, ctx->st));
+    CK(cudaEventRecord(ctx->ev0, ctx->st));
+    int dev_sms = 152;
+    cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    if (nr) {
+        int blocks = int(std::min<size_t>((nr + 127) / 128, size_t(dev_sms) * 16));
+        CK(pq::search_fast(A, O, 128, blocks, ctx->st));
+    }
+    unsigned long long hc[3];
+    CK(cudaMemcpyAsync(hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    unsigned ovf = unsigned(hc[2] & 0xffffffffu);
+    ctx->wide_reads = ovf;
+    if (ovf) {
+        // wide tier over the overflow list; retried after growing the edge pool if needed
+        std::vector<idx_t> list(ovf);
+        CK(cudaMemcpyAsync(list.data(), ctx->ovf_list.p, ovf * sizeof(idx_t), cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+        const size_t slot_bytes = pq::wide_slot_bytes(ctx->L);
+        int slots = int(std::max<size_t>(1, std::min<size_t>({size_t(ovf), size_t(1024),
+                                                              (size_t(4) << 30) / slot_bytes})));
+        pq::WideScratch W;
+        W.stack_cap = size_t(2 * ctx->L) * size_t(2 * ctx->L);
+        W.frame_cap = size_t(ctx->L + 2);
+        W.edge_cap = size_t(2 * 65535 + 2);
+        W.slots = slots;
+        CK(ctx->wide.ensure(slot_bytes * slots + 1024));
+        const size_t st_bytes = W.stack_cap * slots * pq::kCandBytes;
+        const size_t fr_bytes = W.frame_cap * slots * pq::kFrameBytes;
+        W.stack = ctx->wide.p;
+        W.frames = static_cast<char*>(ctx->wide.p) + ((st_bytes + 255) & ~size_t(255));
+        W.edges = static_cast<char*>(W.frames) + ((fr_bytes + 255) & ~size_t(255));
+        DevBuf dlist;
+        for (int attempt = 0; attempt < 8 && !list.empty(); ++attempt) {
+            CK(dlist.ensure(list.size() * sizeof(idx_t)));
+            CK(cudaMemcpyAsync(dlist.p, list.data(), list.size() * sizeof(idx_t), cudaMemcpyHostToDevice, ctx->st));
+            CK(pq::search_wide(A, O, dlist.as<idx_t>(), unsigned(list.size()), W, ctx->st));
+            std::vector<uint8_t> stv(nr);
+            CK(cudaMemcpyAsync(stv.data(), ctx->status.p, nr, cudaMemcpyDeviceToHost, ctx->st));
+            CK(cudaMemcpyAsync(hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, ctx->st));
+            CK(cudaStreamSynchronize(ctx->st));
+            std::vector<idx_t> again;
+            for (idx_t r : list) {
+                uint8_t s = stv[r];
+                if (s == ERR_TOO_MANY) {
+                    dlist.release();
+                    return fail(ctx, PQ_ERR_TOO_MANY_EDGES, "assembly failed. Try a larger min overlap length.");
+                }
+                if (s == ERR_CAP) {
+                    dlist.release();
+                    return fail(ctx, PQ_ERR_CAPACITY, "interval table exceeded (2L)^2 entries for read " +
+                                                          std::to_string((unsigned long long)r));
+                }
+                if (s == OVF_POOL) again.push_back(r);
+                else if (s != OVF_NONE) {
+                    dlist.release();
+                    return fail(ctx, PQ_ERR_INTERNAL, "wide search left read unfinished");
+                }
+            }
+            if (again.empty()) { list.clear(); break; }
+            // grow the pool past everything reserved so far plus a full worst case per retried read
+            size_t need = size_t(hc[0]) + again.size() * size_t(2 * 65535 + 2);
+            size_t keep = std::min<size_t>(size_t(hc[0]), O.e_cap);
+            CK(ctx->e_dest.grow(need * sizeof(idx_t), keep * sizeof(idx_t), ctx->st));
+            CK(ctx->e_trans.grow(need * 4, keep * 4, ctx->st));
+            CK(ctx->e_len.grow(need * 2, keep * 2, ctx->st));
+            CK(ctx->e_type.grow(need, keep, ctx->st));
+            O.e_dest = ctx->e_dest.as<idx_t>();
+            O.e_trans = ctx->e_trans.as<int32_t>();
+            O.e_len = ctx->e_len.as<uint16_t>();
+            O.e_type = ctx->e_type.as<uint8_t>();
+            O.e_cap = need;
+            list.swap(again);
+        }
+        dlist.release();
+        if (!list.empty()) return fail(ctx, PQ_ERR_INTERNAL, "edge pool retries exhausted");
+    }
+    // CSR in read order
+    CK(ctx->off.ensure(nrp * 8));
+    unsigned long long total = 0;
+    size_t atb = pq::assemble_tmp_bytes(ctx->num_reads);
+    CK(ctx->asm_tmp.ensure(atb));
+    // size the CSR from the per-read counts
+    {
+        CK(pq::assemble_counts_total(O, ctx->num_reads, ctx->off.as<unsigned long long>(), ctx->asm_tmp.p, atb,
+                                     ctx->st));
+        CK(cudaMemcpyAsync(&total, ctx->off.as<unsigned long long>() + nr, 8, cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+    }
+    CK(ctx->g_dest.ensure((total + 1) * sizeof(idx_t)));
+    CK(ctx->g_len.ensure((total + 1) * 2));
+    CK(ctx->g_type.ensure(total + 1));
+    CK(ctx->g_trans.ensure((total + 1) * 4));
+    CK(pq::assemble_gather(O, ctx->num_reads, ctx->off.as<unsigned long long>(), ctx->g_dest.as<idx_t>(),
+                           ctx->g_len.as<uint16_t>(), ctx->g_type.as<uint8_t>(), ctx->g_trans.as<int32_t>(), ctx->st));
+    CK(cudaEventRecord(ctx->ev1, ctx->st));
+    CK(cudaMemcpyAsync(hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaEventSynchronize(ctx->ev1));
+    CK(cudaStreamSynchronize(ctx->st));
+    cudaEventElapsedTime(&ctx->ms_search, ctx->ev0, ctx->ev1);
+    ctx->num_edges = total;
+    ctx->probes = hc[1];
+    ctx->graph_ok = true;
+    return PQ_OK;
+}
+
+int pq_get_graph_sizes(pq_ctx* ctx, uint64_t* num_edges, uint64_t* probes, uint64_t* wide_reads) {
+    if (!ctx) return PQ_ERR_ARG;
+    if (!ctx->graph_ok) return fail(ctx, PQ_ERR_STATE, "pq_overlaps first");
+    if (num_edges) *num_edges = ctx->num_edges;
+    if (probes) *probes = ctx->probes;
+    if (wide_reads) *wide_reads = ctx->wide_reads;
+    return PQ_OK;
+}
+
+int pq_get_graph(pq_ctx* ctx, uint16_t* num_B, uint16_t* num_F, int32_t* olp_B, int32_t* olp_F, uint64_t* edge_off,
+                 pq_idx* dest, uint16_t* len, uint8_t* type, int32_t* trans) {
+    if (!ctx) return PQ_ERR_ARG;
+    if (!ctx->graph_ok) return fail(ctx, PQ_ERR_STATE, "pq_overlaps first");
+    const size_t nr = ctx->num_reads, ne = ctx->num_edges;
+    cudaStream_t s = ctx->st;
+    auto d2h = [&](void* h, const DevBuf& b, size_t bytes) -> cudaError_t {
+        if (!h || !bytes) return cudaSuccess;
+        return cudaMemcpyAsync(h, b.p, bytes, cudaMemcpyDeviceToHost, s);
+    };
+    CK(d2h(num_B, ctx->nB, nr * 2));
+    CK(d2h(num_F, ctx->nF, nr * 2));
+    CK(d2h(olp_B, ctx->oB, nr * 4));
+    CK(d2h(olp_F, ctx->oF, nr * 4));
+    CK(d2h(edge_off, ctx->off, (nr + 1) * 8));
+    CK(d2h(dest, ctx->g_dest, ne * sizeof(idx_t)));
+    CK(d2h(len, ctx->g_len, ne * 2));
+    CK(d2h(type, ctx->g_type, ne));
+    CK(d2h(trans, ctx->g_trans, ne * 4));
+    CK(cudaStreamSynchronize(s));
+    return PQ_OK;
+}
+
+int pq_get_stage_ms(pq_ctx* ctx, float* sort_ms, float* fm_ms, float* search_ms) {
+    if (!ctx) return PQ_ERR_ARG;
+    if (sort_ms) *sort_ms = ctx->ms_sort;
+    if (fm_ms) *fm_ms = ctx->ms_fm;
+    if (search_ms) *search_ms = ctx->ms_search;
+    return PQ_OK;
+}
+
+}  // extern "C"

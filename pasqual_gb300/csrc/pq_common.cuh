@@ -1,0 +1,70 @@
+// pq_common.cuh — shared types for the GB300 build of PASQUAL's hot path.
+//
+// Index width follows the reference's INDEX_LENGTH split (src/common.h:31-44): the library is
+// compiled twice, with and without -DPQ_IDX64, exactly as the reference builds
+// bin/pasqual_omp_u32 and _u64.
+#pragma once
+
+#include <cstdint>
+#include <cstddef>
+#include <cuda_runtime.h>
+
+#ifdef PQ_IDX64
+typedef uint64_t idx_t;
+#else
+typedef uint32_t idx_t;
+#endif
+
+// Base codes, as the reference stores them after import (src/index.c:282-303): $=0 A=1 C=2 G=3 T=4.
+// Edge types (src/string_graph.h:14-18).
+enum : int { PQ_BF = 0, PQ_FB = 1, PQ_FF = 2, PQ_BB = 3 };
+
+// ---------------------------------------------------------------------------------------------
+// Occurrence structure ("occ block"): one 32-byte sector covers 64 BWT rows, so one rank query is
+// one sector (plus an L2-resident superblock word).
+//
+//   lo, hi : bit j = low / high bit of the 2-bit base code (A=0..T=3) of row 64b+j
+//   dol    : bit j set <=> row 64b+j is a `$` row (read-start suffix); lo = hi = 0 there
+//   cnt[c] : # of base c+1 in rows [65536*(b/1024), 64b)  (relative to the superblock)
+//
+// Superblock (65536 rows): sb[4*s + c] = # of base c+1 in rows [0, 65536*s).
+// rank_c(pos) = sb + cnt + popc(match_c & below(pos));  rank_$(pos) = pos - sum_c rank_c(pos).
+// The reference's OCC(c, pos) (src/string_graph.c:11-23) equals fix[c] + rank_c(pos) for c >= 1
+// and rank_$(pos) for c = 0, where fix = suffix_count (forward) / prefix_count (backward).
+// ---------------------------------------------------------------------------------------------
+struct __align__(32) OccBlock {
+    uint64_t lo, hi, dol;
+    uint16_t cnt[4];
+};
+static_assert(sizeof(OccBlock) == 32, "occ block must be one 32-byte sector");
+
+constexpr int kBlockShift = 6;                    // 64 rows per block
+constexpr int kSuperShift = 16;                   // 65536 rows per superblock
+constexpr int kBlocksPerSuper = 1 << (kSuperShift - kBlockShift);
+
+// Device view of one FM-index direction.
+struct FmView {
+    const OccBlock* blk;      // n/64 + 1 blocks
+    const idx_t* sb;          // 4 per superblock
+    const idx_t* reads_index; // read id of the k-th `$` row
+    const idx_t* kstart;      // k-mer seed table: first row of each k-mer (or nullptr)
+    const idx_t* kend;        // last row (kend < kstart when the k-mer is absent)
+    idx_t Cf[5];              // Cf[0] = C[0]; Cf[c] = C[c] + fix[c]  (LF-mapping base)
+};
+
+// Status codes returned through the C ABI.
+enum : int {
+    PQ_OK = 0,
+    PQ_ERR_ARG = 1,
+    PQ_ERR_CUDA = 2,
+    PQ_ERR_NOMEM = 3,
+    PQ_ERR_TOO_MANY_EDGES = 4,   // a read has more than 65535 edges on one side
+    PQ_ERR_STATE = 5,
+    PQ_ERR_CAPACITY = 6,
+    PQ_ERR_INTERNAL = 7,
+};
+
+// Per-read overflow reasons recorded by the fast search kernel (the read is redone by the
+// wide-scratch kernel).
+enum : uint8_t { OVF_NONE = 0, OVF_STACK = 1, OVF_EDGES = 2, OVF_LEVELS = 3, OVF_POOL = 4,
+                 ERR_TOO_MANY = 16, ERR_CAP = 17 };

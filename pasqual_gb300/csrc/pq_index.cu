@@ -1,0 +1,341 @@
+// pq_index.cu — FM-index construction from a suffix array (both directions).
+//
+// Replaces the BWT/occurrence-table build of the reference: build_OCC (src/index.c:26-142), the
+// occ prefix sum (src/index.c:587-615), C[] and the prefix/suffix counts (src/index.c:336-372).
+// The reference fills five per-symbol bitmaps plus 5 counts per 64 rows; here one 32-byte occ
+// block per 64 rows holds everything a rank query needs (see pq_common.cuh), and the
+// reference-layout arrays are produced from it on demand for the drop-in host interface.
+#include "pq_index.cuh"
+#include "pq_sort.cuh"
+
+namespace pq {
+
+// Text character at position p (codes 1..4).  dir 1 = every read reversed in place, the text
+// transform_to_triplet_reverse sorts (src/sufsort.c:80-121).
+__device__ __forceinline__ int text_at(const uint8_t* __restrict__ reads, idx_t L, int dir, idx_t p) {
+    if (dir == 0) return reads[p];
+    idx_t r = p / L, off = p - r * L;
+    return reads[r * L + (L - 1 - off)];
+}
+
+// One warp per 64-row block: BWT symbol of each row (`$` for a read-start suffix, else the
+// preceding base), packed into lo/hi/dol masks with ballots; per-block symbol counts go into
+// cnt[] for the superblock pass.
+__global__ void k_bwt_blocks(const idx_t* __restrict__ sa, const uint8_t* __restrict__ reads,
+                             idx_t n, idx_t L, int dir, idx_t nblk, OccBlock* __restrict__ blk) {
+    const int lane = threadIdx.x & 31;
+    const size_t warp = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const size_t nwarps = (size_t(gridDim.x) * blockDim.x) >> 5;
+    for (size_t b = warp; b < nblk; b += nwarps) {
+        uint32_t lo2[2], hi2[2], dl2[2], va2[2];
+        #pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            size_t r = b * 64 + size_t(h) * 32 + lane;
+            int sym = -1;
+            if (r < n) {
+                idx_t p = sa[r];
+                idx_t off = p % L;
+                sym = off ? text_at(reads, L, dir, p - 1) : 0;
+            }
+            int code = sym > 0 ? sym - 1 : 0;
+            lo2[h] = __ballot_sync(0xffffffffu, code & 1);
+            hi2[h] = __ballot_sync(0xffffffffu, code >> 1);
+            dl2[h] = __ballot_sync(0xffffffffu, sym == 0);
+            va2[h] = __ballot_sync(0xffffffffu, sym >= 0);
+        }
+        if (lane == 0) {
+            OccBlock ob;
+            ob.lo = uint64_t(lo2[0]) | (uint64_t(lo2[1]) << 32);
+            ob.hi = uint64_t(hi2[0]) | (uint64_t(hi2[1]) << 32);
+            ob.dol = uint64_t(dl2[0]) | (uint64_t(dl2[1]) << 32);
+            uint64_t valid = uint64_t(va2[0]) | (uint64_t(va2[1]) << 32);
+            uint64_t base = valid & ~ob.dol;
+            ob.cnt[0] = (uint16_t)__popcll(base & ~ob.hi & ~ob.lo);
+            ob.cnt[1] = (uint16_t)__popcll(base & ~ob.hi & ob.lo);
+            ob.cnt[2] = (uint16_t)__popcll(base & ob.hi & ~ob.lo);
+            ob.cnt[3] = (uint16_t)__popcll(base & ob.hi & ob.lo);
+            blk[b] = ob;
+        }
+    }
+}
+
+// One CTA (256 threads x 4 blocks) per superblock: in-superblock exclusive prefix of the block
+// counts, written back as the blocks' relative counts; superblock totals to sbtot.
+__global__ void k_super_prefix(OccBlock* __restrict__ blk, idx_t nblk, idx_t* __restrict__ sbtot) {
+    __shared__ uint32_t warp_tot[8][4];
+    const size_t s = blockIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const size_t b0 = s * kBlocksPerSuper + size_t(tid) * 4;
+    uint32_t c[4][4];
+    uint32_t mine[4] = {0, 0, 0, 0};
+    #pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        size_t b = b0 + i;
+        #pragma unroll
+        for (int k = 0; k < 4; ++k) c[i][k] = 0;
+        if (b < nblk) {
+            uint2 w = *reinterpret_cast<const uint2*>(&blk[b].cnt[0]);
+            c[i][0] = w.x & 0xffff; c[i][1] = w.x >> 16; c[i][2] = w.y & 0xffff; c[i][3] = w.y >> 16;
+        }
+        #pragma unroll
+        for (int k = 0; k < 4; ++k) mine[k] += c[i][k];
+    }
+    // warp inclusive scan of the per-thread totals, per symbol
+    uint32_t incl[4];
+    #pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        uint32_t v = mine[k];
+        #pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v += y;
+        }
+        incl[k] = v;
+        if (lane == 31) warp_tot[wid][k] = v;
+    }
+    __syncthreads();
+    uint32_t run[4];
+    #pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        uint32_t before = 0;
+        for (int w = 0; w < wid; ++w) before += warp_tot[w][k];
+        run[k] = before + incl[k] - mine[k];
+    }
+    #pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        size_t b = b0 + i;
+        if (b < nblk) {
+            uint2 w;
+            w.x = run[0] | (run[1] << 16);
+            w.y = run[2] | (run[3] << 16);
+            *reinterpret_cast<uint2*>(&blk[b].cnt[0]) = w;
+        }
+        #pragma unroll
+        for (int k = 0; k < 4; ++k) run[k] += c[i][k];
+    }
+    if (tid == 255) {
+        #pragma unroll
+        for (int k = 0; k < 4; ++k) sbtot[s * 4 + k] = idx_t(run[k]);
+    }
+}
+
+// Single CTA: exclusive scan of superblock totals (in place), per symbol.
+__global__ void k_super_scan(idx_t* __restrict__ sb, size_t nsb) {
+    __shared__ idx_t carry[4];
+    __shared__ idx_t part[1024][4];
+    const int tid = threadIdx.x;
+    if (tid < 4) carry[tid] = 0;
+    __syncthreads();
+    for (size_t base = 0; base < nsb; base += 1024) {
+        size_t s = base + tid;
+        idx_t v[4];
+        #pragma unroll
+        for (int k = 0; k < 4; ++k) v[k] = s < nsb ? sb[s * 4 + k] : 0;
+        #pragma unroll
+        for (int k = 0; k < 4; ++k) part[tid][k] = v[k];
+        __syncthreads();
+        // Hillis-Steele inclusive scan over 1024 entries
+        for (int o = 1; o < 1024; o <<= 1) {
+            idx_t t[4];
+            #pragma unroll
+            for (int k = 0; k < 4; ++k) t[k] = tid >= o ? part[tid - o][k] : 0;
+            __syncthreads();
+            #pragma unroll
+            for (int k = 0; k < 4; ++k) part[tid][k] += t[k];
+            __syncthreads();
+        }
+        if (s < nsb) {
+            #pragma unroll
+            for (int k = 0; k < 4; ++k) sb[s * 4 + k] = carry[k] + part[tid][k] - v[k];
+        }
+        __syncthreads();
+        if (tid < 4) carry[tid] += part[1023][tid];
+        __syncthreads();
+    }
+}
+
+// reads_index (src/index.c:71-79): read id of every `$` row, in row order.
+__global__ void k_reads_index(const idx_t* __restrict__ sa, const OccBlock* __restrict__ blk,
+                              const idx_t* __restrict__ sb, idx_t n, idx_t L, idx_t nblk,
+                              idx_t* __restrict__ reads_index) {
+    const int lane = threadIdx.x & 31;
+    const size_t warp = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const size_t nwarps = (size_t(gridDim.x) * blockDim.x) >> 5;
+    for (size_t b = warp; b < nblk; b += nwarps) {
+        OccBlock ob = blk[b];
+        if (!ob.dol) continue;
+        const idx_t* s4 = sb + (b >> (kSuperShift - kBlockShift)) * 4;
+        idx_t row0 = idx_t(b * 64);
+        idx_t before = row0 - (s4[0] + s4[1] + s4[2] + s4[3] +
+                               idx_t(ob.cnt[0]) + ob.cnt[1] + ob.cnt[2] + ob.cnt[3]);
+        #pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            int j = h * 32 + lane;
+            if ((ob.dol >> j) & 1) {
+                uint64_t below = j ? (ob.dol & ((uint64_t(1) << j) - 1)) : 0;
+                idx_t k = before + idx_t(__popcll(below));
+                reads_index[k] = sa[row0 + j] / L;
+            }
+        }
+    }
+}
+
+// Read statistics: C[] (src/index.c:367-372), suffix_count / prefix_count (src/index.c:336-346).
+__global__ void k_read_counts(const uint8_t* __restrict__ reads, idx_t nr, idx_t L,
+                              unsigned long long* __restrict__ out /* base[4], sfx[4], pfx[4] */) {
+    __shared__ unsigned long long acc[12];
+    if (threadIdx.x < 12) acc[threadIdx.x] = 0;
+    __syncthreads();
+    unsigned long long loc[12] = {0};
+    const size_t stride = size_t(gridDim.x) * blockDim.x;
+    for (size_t r = size_t(blockIdx.x) * blockDim.x + threadIdx.x; r < nr; r += stride) {
+        const uint8_t* s = reads + r * L;
+        loc[4 + s[L - 1] - 1]++;
+        loc[8 + s[0] - 1]++;
+        for (idx_t j = 0; j < L; ++j) loc[s[j] - 1]++;
+    }
+    #pragma unroll
+    for (int k = 0; k < 12; ++k) if (loc[k]) atomicAdd(&acc[k], loc[k]);
+    __syncthreads();
+    if (threadIdx.x < 12 && acc[threadIdx.x]) atomicAdd(&out[threadIdx.x], acc[threadIdx.x]);
+}
+
+// k-mer seed table: rows whose suffix starts with a given k-mer are contiguous in a sorted SA;
+// record the first and last row of each.  code[r] = k-mer of row r or all-ones if the suffix is
+// shorter than k.
+__global__ void k_kmer_codes(const idx_t* __restrict__ sa, const uint8_t* __restrict__ reads,
+                             idx_t n, idx_t L, int dir, int k, uint32_t* __restrict__ code) {
+    const size_t stride = size_t(gridDim.x) * blockDim.x;
+    for (size_t r = size_t(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride) {
+        idx_t p = sa[r];
+        idx_t off = p % L;
+        uint32_t c = 0xffffffffu;
+        if (L - off >= idx_t(k)) {
+            c = 0;
+            for (int j = 0; j < k; ++j) c = (c << 2) | uint32_t(text_at(reads, L, dir, p + j) - 1);
+        }
+        code[r] = c;
+    }
+}
+
+__global__ void k_kmer_bounds(const uint32_t* __restrict__ code, idx_t n, idx_t* __restrict__ kstart,
+                              idx_t* __restrict__ kend) {
+    const size_t stride = size_t(gridDim.x) * blockDim.x;
+    for (size_t r = size_t(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride) {
+        uint32_t c = code[r];
+        if (c == 0xffffffffu) continue;
+        if (r == 0 || code[r - 1] != c) kstart[c] = idx_t(r);
+        if (r + 1 == n || code[r + 1] != c) kend[c] = idx_t(r);
+    }
+}
+
+__global__ void k_fill_idx(idx_t* __restrict__ a, size_t m, idx_t v) {
+    const size_t stride = size_t(gridDim.x) * blockDim.x;
+    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < m; i += stride) a[i] = v;
+}
+
+// Reference-layout export (src/index.h:26-30): bitmap[c] word b bit j+1 <=> BWT[64b+j] == c for
+// j <= 62, and sample[5b+c] = fix[c] + #c in BWT[0, 64b) (fix[0] = 0).
+__global__ void k_export_ref(const OccBlock* __restrict__ blk, const idx_t* __restrict__ sb,
+                             idx_t n, idx_t nblk, idx_t f1, idx_t f2, idx_t f3, idx_t f4,
+                             uint64_t* __restrict__ bitmap, idx_t* __restrict__ sample) {
+    const size_t stride = size_t(gridDim.x) * blockDim.x;
+    for (size_t b = size_t(blockIdx.x) * blockDim.x + threadIdx.x; b < nblk; b += stride) {
+        OccBlock ob = blk[b];
+        uint64_t valid = (size_t(n) >= (b + 1) * 64) ? ~uint64_t(0)
+                       : (size_t(n) > b * 64 ? ((uint64_t(1) << (size_t(n) - b * 64)) - 1) : 0);
+        uint64_t base = valid & ~ob.dol;
+        uint64_t m[5];
+        m[0] = ob.dol;
+        m[1] = base & ~ob.hi & ~ob.lo;
+        m[2] = base & ~ob.hi & ob.lo;
+        m[3] = base & ob.hi & ~ob.lo;
+        m[4] = base & ob.hi & ob.lo;
+        #pragma unroll
+        for (int c = 0; c < 5; ++c) bitmap[size_t(c) * nblk + b] = m[c] << 1;
+        const idx_t* s4 = sb + (b >> (kSuperShift - kBlockShift)) * 4;
+        idx_t r1 = s4[0] + ob.cnt[0], r2 = s4[1] + ob.cnt[1], r3 = s4[2] + ob.cnt[2], r4 = s4[3] + ob.cnt[3];
+        idx_t row0 = idx_t(b * 64);
+        sample[b * 5 + 0] = row0 - (r1 + r2 + r3 + r4);
+        sample[b * 5 + 1] = f1 + r1;
+        sample[b * 5 + 2] = f2 + r2;
+        sample[b * 5 + 3] = f3 + r3;
+        sample[b * 5 + 4] = f4 + r4;
+    }
+}
+
+// Per-read seeds (index_t.interval_start/end/depth, src/index.h:36-41): forward = the read's
+// last k bases, backward = its first k bases reversed; both exact SA intervals from the table.
+__global__ void k_read_seeds(const uint8_t* __restrict__ reads, idx_t nr, int L, int dir, int k,
+                             const idx_t* __restrict__ kstart, const idx_t* __restrict__ kend,
+                             idx_t* __restrict__ start, idx_t* __restrict__ size) {
+    const size_t stride = size_t(gridDim.x) * blockDim.x;
+    for (size_t r = size_t(blockIdx.x) * blockDim.x + threadIdx.x; r < nr; r += stride) {
+        const uint8_t* s = reads + r * size_t(L);
+        uint32_t code = 0;
+        for (int j = 0; j < k; ++j) {
+            int c = dir == 0 ? s[L - k + j] : s[k - 1 - j];
+            code = (code << 2) | uint32_t(c - 1);
+        }
+        start[r] = kstart[code];
+        size[r] = kend[code] - kstart[code] + 1;
+    }
+}
+
+static inline unsigned grid_for(size_t work, int threads, int per_sm = 8) {
+    size_t g = (work + threads - 1) / threads;
+    size_t cap = size_t(152) * per_sm * 4;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return unsigned(g);
+}
+
+cudaError_t build_occ(const idx_t* sa, const uint8_t* reads, idx_t num_reads, idx_t L, int dir,
+                      OccBlock* blk, idx_t* sb, idx_t* reads_index, cudaStream_t st) {
+    const size_t n = size_t(num_reads) * L;
+    const size_t nblk = n / 64 + 1;
+    const size_t nsb = (nblk + kBlocksPerSuper - 1) / kBlocksPerSuper;
+    k_bwt_blocks<<<grid_for(nblk * 32, 256), 256, 0, st>>>(sa, reads, idx_t(n), L, dir, idx_t(nblk), blk);
+    k_super_prefix<<<unsigned(nsb), 256, 0, st>>>(blk, idx_t(nblk), sb);
+    k_super_scan<<<1, 1024, 0, st>>>(sb, nsb);
+    k_reads_index<<<grid_for(nblk * 32, 256), 256, 0, st>>>(sa, blk, sb, idx_t(n), L, idx_t(nblk), reads_index);
+    return cudaGetLastError();
+}
+
+cudaError_t read_counts(const uint8_t* reads, idx_t num_reads, idx_t L, unsigned long long* out12,
+                        cudaStream_t st) {
+    cudaMemsetAsync(out12, 0, 12 * sizeof(unsigned long long), st);
+    if (num_reads) k_read_counts<<<grid_for(num_reads, 256), 256, 0, st>>>(reads, num_reads, L, out12);
+    return cudaGetLastError();
+}
+
+cudaError_t build_kmer_table(const idx_t* sa, const uint8_t* reads, idx_t num_reads, idx_t L, int dir,
+                             int k, uint32_t* code_tmp, idx_t* kstart, idx_t* kend, cudaStream_t st) {
+    const size_t n = size_t(num_reads) * L;
+    const size_t nk = size_t(1) << (2 * k);
+    k_fill_idx<<<grid_for(nk, 256), 256, 0, st>>>(kstart, nk, idx_t(1));
+    k_fill_idx<<<grid_for(nk, 256), 256, 0, st>>>(kend, nk, idx_t(0));
+    if (n) {
+        k_kmer_codes<<<grid_for(n, 256), 256, 0, st>>>(sa, reads, idx_t(n), L, dir, k, code_tmp);
+        k_kmer_bounds<<<grid_for(n, 256), 256, 0, st>>>(code_tmp, idx_t(n), kstart, kend);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t read_seeds(const uint8_t* reads, idx_t num_reads, int L, int dir, int k, const idx_t* kstart,
+                       const idx_t* kend, idx_t* start, idx_t* size, cudaStream_t st) {
+    if (num_reads)
+        k_read_seeds<<<grid_for(num_reads, 256), 256, 0, st>>>(reads, num_reads, L, dir, k, kstart, kend, start, size);
+    return cudaGetLastError();
+}
+
+cudaError_t export_ref_layout(const OccBlock* blk, const idx_t* sb, idx_t num_reads, idx_t L,
+                              const idx_t fix[4], uint64_t* bitmap, idx_t* sample, cudaStream_t st) {
+    const size_t n = size_t(num_reads) * L;
+    const size_t nblk = n / 64 + 1;
+    k_export_ref<<<grid_for(nblk, 256), 256, 0, st>>>(blk, sb, idx_t(n), idx_t(nblk), fix[0], fix[1],
+                                                      fix[2], fix[3], bitmap, sample);
+    return cudaGetLastError();
+}
+
+}  // namespace pq

@@ -1,0 +1,70 @@
+// pq_index.cuh — device-side index construction and search entry points (internal).
+#pragma once
+#include "pq_common.cuh"
+
+namespace pq {
+
+// FM-index build from a suffix array (pq_index.cu)
+cudaError_t build_occ(const idx_t* sa, const uint8_t* reads, idx_t num_reads, idx_t L, int dir,
+                      OccBlock* blk, idx_t* sb, idx_t* reads_index, cudaStream_t st);
+cudaError_t read_counts(const uint8_t* reads, idx_t num_reads, idx_t L, unsigned long long* out12,
+                        cudaStream_t st);
+cudaError_t build_kmer_table(const idx_t* sa, const uint8_t* reads, idx_t num_reads, idx_t L, int dir,
+                             int k, uint32_t* code_tmp, idx_t* kstart, idx_t* kend, cudaStream_t st);
+cudaError_t export_ref_layout(const OccBlock* blk, const idx_t* sb, idx_t num_reads, idx_t L,
+                              const idx_t fix[4], uint64_t* bitmap, idx_t* sample, cudaStream_t st);
+
+// Overlap search (pq_search.cu)
+struct SearchOut {
+    uint16_t* num_B;            // [num_reads]
+    uint16_t* num_F;
+    int32_t* olp_B;
+    int32_t* olp_F;
+    uint8_t* status;            // OVF_* / ERR_* per read (0 = done)
+    unsigned long long* edge_src;  // per read: offset into pool 1, or (1<<63 | offset) into pool 2
+    // edge pool (struct of arrays)
+    idx_t* e_dest;
+    int32_t* e_trans;
+    uint16_t* e_len;
+    uint8_t* e_type;
+    unsigned long long* e_count;   // atomic bump counter
+    unsigned long long e_cap;
+    idx_t* ovf_list;               // reads handed to the wide kernel
+    unsigned int* ovf_count;
+    unsigned long long* probes;    // total rank probes (one 32-byte sector each)
+};
+
+struct SearchArgs {
+    FmView fm[2];               // 0 forward, 1 backward
+    const uint8_t* reads;       // codes 1..4, forward orientation
+    idx_t num_reads;
+    int L;
+    int t;
+    int seed_k;                 // k-mer seed depth (0 = start at depth 1 from C[])
+};
+
+cudaError_t search_fast(const SearchArgs& a, const SearchOut& o, int threads_per_block, int blocks,
+                        cudaStream_t st);
+
+struct WideScratch {
+    void* stack;                // slots * stack_cap candidates
+    void* frames;               // slots * frame_cap
+    void* edges;                // slots * edge_cap
+    size_t stack_cap, frame_cap, edge_cap;
+    int slots;
+};
+size_t wide_slot_bytes(int L);
+cudaError_t search_wide(const SearchArgs& a, const SearchOut& o, const idx_t* list, unsigned count,
+                        const WideScratch& ws, cudaStream_t st);
+
+// Final CSR assembly: out_off = exclusive scan of num_B+num_F (out_off[num_reads] = total),
+// then the edges are gathered from the pool in read order.
+cudaError_t assemble_counts_total(const SearchOut& o, idx_t num_reads, unsigned long long* out_off,
+                                  void* scan_tmp, size_t scan_tmp_bytes, cudaStream_t st);
+cudaError_t assemble_gather(const SearchOut& o, idx_t num_reads, const unsigned long long* off,
+                            idx_t* dest, uint16_t* len, uint8_t* type, int32_t* trans, cudaStream_t st);
+size_t assemble_tmp_bytes(idx_t num_reads);
+extern const size_t kCandBytes;    // sizeof one stack entry of the search kernels
+extern const size_t kFrameBytes;   // sizeof one DFS frame
+
+}  // namespace pq

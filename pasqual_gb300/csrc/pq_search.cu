@@ -1,0 +1,599 @@
+// pq_search.cu — per-read overlap search with transitive reduction on the GPU.
+//
+// Replaces the body of construct_string_graph's per-read loop (src/string_graph.c:800-830):
+//   find_intervals   (src/string_graph.c:163-383)  four bidirectional backward searches
+//   extract_bw_edges (src/string_graph.c:560-731)  DFS irreducible-edge extraction, B side
+//   extract_fw_edges (src/string_graph.c:387-556)  the same for the F side
+// with the rank primitives OCCx/search_1/search_2/search_3 (src/string_graph.c:11-159) on the
+// one-sector occ blocks of pq_common.cuh.
+//
+// One thread searches one read.  The reference's recursion becomes an explicit stack: candidate
+// intervals of every open level live in a per-thread array laid out exactly as the reference's
+// I_fw/I_bw (a level's children directly after it), and one frame per level remembers which
+// extension base comes next.  The fast kernel keeps stack, frames and edge buffer in local
+// memory with fixed capacities; a read that outgrows any of them is recorded and redone by the
+// wide kernel, whose per-slot scratch has the reference's own bounds ((2L)^2 candidates,
+// 65535 edges per side), so every read completes with the reference's result.
+#include "pq_index.cuh"
+
+#include <algorithm>
+
+namespace pq {
+
+struct Cand {
+    idx_t ll, uu, remain;
+    uint16_t len;
+    uint8_t type;
+};
+struct Frame {
+    uint32_t pos;
+    uint16_t size;
+    uint16_t maxlen;
+    int32_t trans;
+    uint8_t next_a;
+};
+struct EdgeRec {
+    idx_t dest;
+    int32_t trans;
+    uint16_t len;
+    uint8_t type;
+};
+
+// ------------------------------------------------------------------------------ rank primitives
+
+__device__ __forceinline__ void ld_block(const OccBlock* p, uint64_t& lo, uint64_t& hi, uint64_t& dol,
+                                         uint32_t& c01, uint32_t& c23) {
+    const uint4* q = reinterpret_cast<const uint4*>(p);
+    uint4 a = __ldg(q);
+    uint4 b = __ldg(q + 1);
+    lo = uint64_t(a.x) | (uint64_t(a.y) << 32);
+    hi = uint64_t(a.z) | (uint64_t(a.w) << 32);
+    dol = uint64_t(b.x) | (uint64_t(b.y) << 32);
+    c01 = b.z;
+    c23 = b.w;
+}
+
+__device__ __forceinline__ uint64_t below(idx_t pos) {
+    return (uint64_t(1) << (pos & 63)) - 1;   // rows [64*(pos/64), pos) of the block
+}
+
+// match mask of base c (1..4) among non-$ rows
+__device__ __forceinline__ uint64_t match(uint64_t lo, uint64_t hi, uint64_t dol, int c) {
+    uint64_t code = uint64_t(c - 1);
+    uint64_t mlo = lo ^ ((code & 1) - 1);
+    uint64_t mhi = hi ^ ((code >> 1) - 1);
+    return mlo & mhi & ~dol;
+}
+
+__device__ __forceinline__ uint32_t rel_cnt(uint32_t c01, uint32_t c23, int c) {
+    uint32_t w = (c <= 2) ? c01 : c23;
+    return ((c & 1) ? w : (w >> 16)) & 0xffff;
+}
+
+// rank of base c (1..4) in BWT[0, pos), without the fix offset
+__device__ __forceinline__ idx_t rank_c(const FmView& f, int c, idx_t pos) {
+    uint64_t lo, hi, dol;
+    uint32_t c01, c23;
+    ld_block(f.blk + (pos >> kBlockShift), lo, hi, dol, c01, c23);
+    idx_t s = __ldg(f.sb + size_t(pos >> kSuperShift) * 4 + (c - 1));
+    return s + rel_cnt(c01, c23, c) + idx_t(__popcll(match(lo, hi, dol, c) & below(pos)));
+}
+
+// ranks of all four bases in BWT[0, pos)
+__device__ __forceinline__ void rank_all(const FmView& f, idx_t pos, idx_t r[4]) {
+    uint64_t lo, hi, dol;
+    uint32_t c01, c23;
+    ld_block(f.blk + (pos >> kBlockShift), lo, hi, dol, c01, c23);
+    const idx_t* s4 = f.sb + size_t(pos >> kSuperShift) * 4;
+    idx_t s0, s1, s2, s3;
+#ifdef PQ_IDX64
+    ulonglong2 a = __ldg(reinterpret_cast<const ulonglong2*>(s4));
+    ulonglong2 b = __ldg(reinterpret_cast<const ulonglong2*>(s4) + 1);
+    s0 = a.x; s1 = a.y; s2 = b.x; s3 = b.y;
+#else
+    uint4 a = __ldg(reinterpret_cast<const uint4*>(s4));
+    s0 = a.x; s1 = a.y; s2 = a.z; s3 = a.w;
+#endif
+    uint64_t m = below(pos) & ~dol;
+    r[0] = s0 + (c01 & 0xffff) + idx_t(__popcll(~hi & ~lo & m));
+    r[1] = s1 + (c01 >> 16) + idx_t(__popcll(~hi & lo & m));
+    r[2] = s2 + (c23 & 0xffff) + idx_t(__popcll(hi & ~lo & m));
+    r[3] = s3 + (c23 >> 16) + idx_t(__popcll(hi & lo & m));
+}
+
+// # of `$` rows in BWT[0, pos) (= the reference's OCC(0, pos))
+__device__ __forceinline__ idx_t rank_dollar(const FmView& f, idx_t pos) {
+    idx_t r[4];
+    rank_all(f, pos, r);
+    return pos - (r[0] + r[1] + r[2] + r[3]);
+}
+
+// search_1: LF-map the closed interval [l, u] by base c
+__device__ __forceinline__ void lf_step(const FmView& f, int c, idx_t& l, idx_t& u, uint32_t& probes) {
+    idx_t ol = rank_c(f, c, l);
+    idx_t ou = rank_c(f, c, u + 1);
+    probes += 2;
+    l = f.Cf[c] + ol;
+    u = f.Cf[c] + ou - 1;
+}
+
+// search_2: step on this index by c, keep the other index's interval [ll, uu] in sync.
+// #symbols < c in [l, u] ($ included) = (pos - sum_{k>=c} rank_k) differences; fixes cancel.
+__device__ __forceinline__ void bi_step(const FmView& f, int c, idx_t& l, idx_t& u, idx_t& ll, idx_t& uu,
+                                        uint32_t& probes) {
+    idx_t vl = l, vu = u + 1;
+    idx_t rl[4], ru[4];
+    rank_all(f, vl, rl);
+    rank_all(f, vu, ru);
+    probes += 2;
+    idx_t gel = 0, geu = 0;
+    #pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (k + 1 >= c) { gel += rl[k]; geu += ru[k]; }
+    }
+    idx_t less_l = vl - gel, less_u = vu - geu;
+    ll = ll + (less_u - less_l);
+    idx_t ol = rl[c - 1], ou = ru[c - 1];
+    l = f.Cf[c] + ol;
+    u = f.Cf[c] + ou - 1;
+    uu = ll + ou - ol - 1;
+}
+
+// search_3: (#$ in [l, u]) - 1, wrapping to all-ones at zero
+__device__ __forceinline__ idx_t dollars_m1(const FmView& f, idx_t l, idx_t u, uint32_t& probes) {
+    probes += 2;
+    return rank_dollar(f, u + 1) - rank_dollar(f, l) - 1;
+}
+
+// ------------------------------------------------------------------------------ per-read search
+
+struct ReadView {
+    const uint32_t* w;   // packed 2-bit codes (A=0..T=3), 16 per word, word i at w[i*stride]
+    int stride;
+    __device__ __forceinline__ int at(int i) const {   // code 1..4 of read position i
+        return int((w[(i >> 4) * stride] >> ((i & 15) * 2)) & 3) + 1;
+    }
+};
+
+__device__ __forceinline__ int complement(int c) { return 5 - c; }
+
+// pattern base at depth j (1-based) of each search kind (see oracle candidate_search)
+__device__ __forceinline__ int pattern_at(const ReadView& rd, int L, int kind, int j) {
+    switch (kind) {
+        case PQ_FB: return rd.at(L - j);
+        case PQ_FF: return complement(rd.at(L - j));
+        case PQ_BF: return rd.at(j - 1);
+        default: return complement(rd.at(j - 1));
+    }
+}
+
+// exact SA interval of pattern pat(hi) pat(hi-1) ... pat(lo) (text order) from the k-mer table
+__device__ __forceinline__ void kmer_seed(const FmView& f, const ReadView& rd, int L, int kind, int first,
+                                          int last, int step, idx_t& l, idx_t& u, uint32_t& probes) {
+    uint32_t code = 0;
+    for (int j = first;; j += step) {
+        code = (code << 2) | uint32_t(pattern_at(rd, L, kind, j) - 1);
+        if (j == last) break;
+    }
+    l = __ldg(f.kstart + code);
+    u = __ldg(f.kend + code);
+    probes += 1;
+}
+
+struct ReadResult {
+    int status;
+    int nB, nF;
+    int32_t olpB, olpF;
+    int ne;
+};
+
+// One of the four candidate searches of find_intervals; appends to stk[*cnt...].
+__device__ __forceinline__ int candidate_search(const SearchArgs& A, const ReadView& rd, int kind, Cand* stk,
+                                                int cap, int& cnt, int32_t& olp, uint32_t& probes) {
+    const int L = A.L, t = A.t;
+    const int ia = (kind == PQ_FB || kind == PQ_BB) ? 0 : 1;   // index walked
+    const FmView& FA = A.fm[ia];
+    const FmView& FB_ = A.fm[1 - ia];
+    const bool strict = (kind == PQ_FB || kind == PQ_BF);
+    idx_t l, u, ll = 0, uu = 0;
+    int d;
+    // seed: exact SA interval of pat(k)..pat(1) from the k-mer table (k = 1 reproduces the
+    // reference's depth-1 start at C[c]; any exact interval of depth <= t is equivalent)
+    const int k = A.seed_k;
+    kmer_seed(FA, rd, L, kind, k, 1, -1, l, u, probes);
+    d = k;
+#define LIVE(l, u) (strict ? ((l) < (u)) : ((l) <= (u)))
+    while (LIVE(l, u) && d < t) {
+        lf_step(FA, pattern_at(rd, L, kind, d + 1), l, u, probes);
+        d++;
+    }
+    if (LIVE(l, u)) {
+        // other index: pattern pat(1) pat(2) .. pat(d) (text order); seed with its last k bases
+        kmer_seed(FB_, rd, L, kind, d - k + 1, d, 1, ll, uu, probes);
+        for (int j = d - k; j >= 1; --j) lf_step(FB_, pattern_at(rd, L, kind, j), ll, uu, probes);
+    }
+    while (LIVE(l, u) && d < L) {
+        if (kind != PQ_BB || d >= t) {
+            idx_t tmp = dollars_m1(FA, l, u, probes);
+            if (cnt >= cap) return OVF_STACK;
+            Cand& c = stk[cnt++];
+            c.ll = ll;
+            c.uu = ll + tmp;
+            c.len = uint16_t(d);
+            c.type = uint8_t(kind);
+            c.remain = tmp + 1;
+            olp = int32_t(uint32_t(olp) + uint32_t(tmp + 1));
+        }
+        bi_step(FA, pattern_at(rd, L, kind, d + 1), l, u, ll, uu, probes);
+        d++;
+    }
+#undef LIVE
+    return OVF_NONE;
+}
+
+__device__ __forceinline__ int cand_index(int type) { return (type == PQ_FB || type == PQ_BB) ? 1 : 0; }
+
+// extract_fw_edges / extract_bw_edges as an explicit DFS over stk[0, n0).
+__device__ __forceinline__ int reduce_side(const SearchArgs& A, idx_t self, Cand* stk, int cap, int n0,
+                                           Frame* fr, int frcap, EdgeRec* eb, int ebcap, int& ne,
+                                           int& side_count, uint32_t& probes) {
+    const int L = A.L;
+    int level = 0;
+    fr[0].pos = 0;
+    fr[0].size = uint16_t(n0);
+    fr[0].maxlen = 0;
+    fr[0].trans = 0;
+    bool entering = true;
+    while (true) {
+        Frame& F = fr[level];
+        if (entering) {
+            entering = false;
+            F.next_a = 1;
+            if (int(F.maxlen) + level == L) {
+                bool flag = false;
+                for (int i = 0; i < F.size; ++i) {
+                    const Cand& c = stk[F.pos + i];
+                    if (int(c.len) + level != L) continue;
+                    const FmView& fo = A.fm[cand_index(c.type)];
+                    idx_t lll = fo.Cf[0] + rank_dollar(fo, c.ll);
+                    idx_t uuu = fo.Cf[0] + rank_dollar(fo, c.uu + 1) - 1;
+                    probes += 2;
+                    if (lll <= uuu) {
+                        for (idx_t kk = lll; kk < uuu + 1; ++kk) {
+                            idx_t r = __ldg(fo.reads_index + kk);
+                            flag = true;
+                            if (r != self) {
+                                if (side_count + 1 > 65535) return ERR_TOO_MANY;
+                                if (ne >= ebcap) return OVF_EDGES;
+                                EdgeRec& e = eb[ne++];
+                                e.dest = r;
+                                e.len = c.len;
+                                e.type = c.type;
+                                e.trans = F.trans;
+                                side_count++;
+                            }
+                        }
+                        break;
+                    }
+                }
+                if (flag) {
+                    if (level == 0) return OVF_NONE;
+                    --level;
+                    continue;
+                }
+            }
+        }
+        if (F.next_a > 4) {
+            if (level == 0) return OVF_NONE;
+            --level;
+            continue;
+        }
+        const int a = F.next_a++;
+        const uint32_t cpos = F.pos + F.size;
+        int cnt = 0, maxl = 0;
+        uint32_t tr = 0;
+        for (int i = 0; i < F.size; ++i) {
+            Cand& c = stk[F.pos + i];
+            if (c.remain == 0) continue;
+            const int o = cand_index(c.type);
+            const int ch = o == 0 ? complement(a) : a;
+            idx_t l2 = c.ll, u2 = c.uu;
+            lf_step(A.fm[o], ch, l2, u2, probes);
+            c.remain = c.remain - (u2 - l2 + 1);
+            if (l2 <= u2) {
+                if (int(cpos) + cnt >= cap) return OVF_STACK;
+                Cand& ch_ = stk[cpos + cnt++];
+                ch_.ll = l2;
+                ch_.uu = u2;
+                ch_.len = c.len;
+                ch_.type = c.type;
+                ch_.remain = u2 - l2 + 1;
+                tr += uint32_t(u2 - l2 + 1);
+                if (maxl < c.len) maxl = c.len;
+            }
+        }
+        if (cnt == 0) continue;
+        if (level + 1 >= frcap) return OVF_LEVELS;
+        ++level;
+        Frame& G = fr[level];
+        G.pos = cpos;
+        G.size = uint16_t(cnt);
+        G.maxlen = uint16_t(maxl);
+        G.trans = int32_t(tr);
+        entering = true;
+    }
+}
+
+__device__ __forceinline__ ReadResult search_read(const SearchArgs& A, idx_t self, const ReadView& rd, Cand* stk,
+                                                  int cap, Frame* fr, int frcap, EdgeRec* eb, int ebcap,
+                                                  uint32_t& probes) {
+    ReadResult R;
+    R.status = OVF_NONE;
+    R.nB = R.nF = 0;
+    R.olpB = R.olpF = 0;
+    R.ne = 0;
+    int n0 = 0, sc = 0;
+    // B side: B-F then B-B candidates, then extract_bw_edges
+    int s = candidate_search(A, rd, PQ_BF, stk, cap, n0, R.olpB, probes);
+    if (s == OVF_NONE) s = candidate_search(A, rd, PQ_BB, stk, cap, n0, R.olpB, probes);
+    if (s == OVF_NONE && R.olpB != 0) s = reduce_side(A, self, stk, cap, n0, fr, frcap, eb, ebcap, R.ne, sc, probes);
+    if (s != OVF_NONE) { R.status = s; return R; }
+    R.nB = sc;
+    // F side: F-B then F-F candidates, then extract_fw_edges
+    n0 = 0;
+    sc = 0;
+    s = candidate_search(A, rd, PQ_FB, stk, cap, n0, R.olpF, probes);
+    if (s == OVF_NONE) s = candidate_search(A, rd, PQ_FF, stk, cap, n0, R.olpF, probes);
+    if (s == OVF_NONE && R.olpF != 0) s = reduce_side(A, self, stk, cap, n0, fr, frcap, eb, ebcap, R.ne, sc, probes);
+    if (s != OVF_NONE) { R.status = s; return R; }
+    R.nF = sc;
+    return R;
+}
+
+__device__ __forceinline__ void load_read(const SearchArgs& A, idx_t r, uint32_t* w, int stride) {
+    const uint8_t* src = A.reads + size_t(r) * A.L;
+    const int words = (A.L + 15) >> 4;
+    for (int i = 0; i < words; ++i) {
+        uint32_t v = 0;
+        const int j0 = i * 16;
+        const int jn = min(16, A.L - j0);
+        for (int j = 0; j < jn; ++j) v |= uint32_t(src[j0 + j] - 1) << (2 * j);
+        w[i * stride] = v;
+    }
+}
+
+__device__ __forceinline__ void publish(const SearchOut& O, idx_t r, const ReadResult& R, const EdgeRec* eb) {
+    if (R.status != OVF_NONE) {
+        O.status[r] = uint8_t(R.status);
+        if (R.status != ERR_TOO_MANY) {
+            unsigned k = atomicAdd(O.ovf_count, 1u);
+            O.ovf_list[k] = r;
+        }
+        return;
+    }
+    unsigned long long base = 0;
+    if (R.ne) {
+        base = atomicAdd(O.e_count, (unsigned long long)R.ne);
+        if (base + R.ne > O.e_cap) {
+            O.status[r] = OVF_POOL;
+            unsigned k = atomicAdd(O.ovf_count, 1u);
+            O.ovf_list[k] = r;
+            return;
+        }
+        for (int i = 0; i < R.ne; ++i) {
+            O.e_dest[base + i] = eb[i].dest;
+            O.e_trans[base + i] = eb[i].trans;
+            O.e_len[base + i] = eb[i].len;
+            O.e_type[base + i] = eb[i].type;
+        }
+    }
+    O.status[r] = OVF_NONE;
+    O.num_B[r] = uint16_t(R.nB);
+    O.num_F[r] = uint16_t(R.nF);
+    O.olp_B[r] = R.olpB;
+    O.olp_F[r] = R.olpF;
+    O.edge_src[r] = base;
+}
+
+__device__ __forceinline__ void add_probes(const SearchOut& O, uint32_t probes) {
+    unsigned long long v = probes;
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(O.probes, v);
+}
+
+constexpr int kFastCap = 768;
+constexpr int kFastFrames = 128;
+constexpr int kFastEdges = 48;
+
+__global__ void __launch_bounds__(128) k_search_fast(SearchArgs A, SearchOut O) {
+    extern __shared__ uint32_t s_reads[];
+    Cand stk[kFastCap];
+    Frame fr[kFastFrames];
+    EdgeRec eb[kFastEdges];
+    uint32_t probes = 0;
+    const size_t stride = size_t(gridDim.x) * blockDim.x;
+    const size_t nwork = ((size_t(A.num_reads) + 31) / 32) * 32;   // whole warps for the probe reduction
+    for (size_t r = size_t(blockIdx.x) * blockDim.x + threadIdx.x; r < nwork; r += stride) {
+        if (r < A.num_reads) {
+            load_read(A, idx_t(r), s_reads + threadIdx.x, blockDim.x);
+            ReadView rd{s_reads + threadIdx.x, int(blockDim.x)};
+            ReadResult R = search_read(A, idx_t(r), rd, stk, kFastCap, fr, kFastFrames, eb, kFastEdges, probes);
+            publish(O, idx_t(r), R, eb);
+        }
+    }
+    add_probes(O, probes);
+}
+
+cudaError_t search_fast(const SearchArgs& a, const SearchOut& o, int threads_per_block, int blocks,
+                        cudaStream_t st) {
+    if (threads_per_block != 128) return cudaErrorInvalidValue;
+    const int words = (a.L + 15) / 16;
+    size_t smem = size_t(words) * threads_per_block * sizeof(uint32_t);
+    k_search_fast<<<blocks, threads_per_block, smem, st>>>(a, o);
+    return cudaGetLastError();
+}
+
+// Wide tier: the reference's own capacity bounds, scratch in global memory, one slot per thread.
+__global__ void __launch_bounds__(64) k_search_wide(SearchArgs A, SearchOut O, const idx_t* list, unsigned count,
+                                                    WideScratch W) {
+    extern __shared__ uint32_t s_reads[];
+    const unsigned slot = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t probes = 0;
+    if (slot < unsigned(W.slots)) {
+        Cand* stk = reinterpret_cast<Cand*>(W.stack) + size_t(slot) * W.stack_cap;
+        Frame* fr = reinterpret_cast<Frame*>(W.frames) + size_t(slot) * W.frame_cap;
+        EdgeRec* eb = reinterpret_cast<EdgeRec*>(W.edges) + size_t(slot) * W.edge_cap;
+        for (unsigned i = slot; i < count; i += unsigned(W.slots)) {
+            idx_t r = list[i];
+            load_read(A, r, s_reads + threadIdx.x, blockDim.x);
+            ReadView rd{s_reads + threadIdx.x, int(blockDim.x)};
+            ReadResult R = search_read(A, r, rd, stk, int(W.stack_cap), fr, int(W.frame_cap), eb, int(W.edge_cap),
+                                       probes);
+            if (R.status == OVF_STACK || R.status == OVF_LEVELS) R.status = ERR_CAP;
+            if (R.status == ERR_CAP || R.status == ERR_TOO_MANY || R.status == OVF_EDGES) {
+                O.status[r] = uint8_t(R.status == OVF_EDGES ? ERR_CAP : R.status);
+                continue;
+            }
+            // pool overflow is reported through status and the host grows the pool and retries
+            unsigned long long base = 0;
+            if (R.ne) {
+                base = atomicAdd(O.e_count, (unsigned long long)R.ne);
+                if (base + R.ne > O.e_cap) { O.status[r] = OVF_POOL; continue; }
+                for (int e = 0; e < R.ne; ++e) {
+                    O.e_dest[base + e] = eb[e].dest;
+                    O.e_trans[base + e] = eb[e].trans;
+                    O.e_len[base + e] = eb[e].len;
+                    O.e_type[base + e] = eb[e].type;
+                }
+            }
+            O.status[r] = OVF_NONE;
+            O.num_B[r] = uint16_t(R.nB);
+            O.num_F[r] = uint16_t(R.nF);
+            O.olp_B[r] = R.olpB;
+            O.olp_F[r] = R.olpF;
+            O.edge_src[r] = base;
+        }
+    }
+    if (probes) atomicAdd(O.probes, (unsigned long long)probes);
+}
+
+size_t wide_slot_bytes(int L) {
+    size_t cap = size_t(2 * L) * size_t(2 * L);
+    return cap * sizeof(Cand) + size_t(L + 2) * sizeof(Frame) + size_t(2 * 65535 + 2) * sizeof(EdgeRec);
+}
+
+cudaError_t search_wide(const SearchArgs& a, const SearchOut& o, const idx_t* list, unsigned count,
+                        const WideScratch& ws, cudaStream_t st) {
+    if (!count) return cudaSuccess;
+    const int tpb = 64;
+    const int words = (a.L + 15) / 16;
+    size_t smem = size_t(words) * tpb * sizeof(uint32_t);
+    int blocks = (ws.slots + tpb - 1) / tpb;
+    k_search_wide<<<blocks, tpb, smem, st>>>(a, o, list, count, ws);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------------ CSR assembly
+
+__global__ void k_edge_counts(const uint16_t* nB, const uint16_t* nF, idx_t n, unsigned long long* cnt) {
+    const size_t stride = size_t(gridDim.x) * blockDim.x;
+    for (size_t r = size_t(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride)
+        cnt[r] = (unsigned long long)nB[r] + nF[r];
+}
+
+// exclusive scan of 64-bit counts: tiles of 1024 per CTA (3 passes)
+__global__ void k_scan_tiles(const unsigned long long* in, size_t n, unsigned long long* out,
+                             unsigned long long* tile_sums) {
+    __shared__ unsigned long long warp_sum[32];
+    const size_t tile = blockIdx.x;
+    const size_t i = tile * 1024 + threadIdx.x;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    unsigned long long v = i < n ? in[i] : 0, x = v;
+    #pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sum[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        unsigned long long w = warp_sum[lane], z = w;
+        #pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned long long y = __shfl_up_sync(0xffffffffu, z, o);
+            if (lane >= o) z += y;
+        }
+        warp_sum[lane] = z - w;
+        if (lane == 31 && tile_sums) tile_sums[tile] = z;
+    }
+    __syncthreads();
+    if (i < n) out[i] = warp_sum[wid] + x - v;
+}
+
+__global__ void k_scan_add(unsigned long long* out, size_t n, const unsigned long long* tile_off) {
+    const size_t i = size_t(blockIdx.x) * 1024 + threadIdx.x;
+    if (i < n) out[i] += tile_off[blockIdx.x];
+}
+
+static void scan_u64(const unsigned long long* in, size_t n, unsigned long long* out, unsigned long long* tmp,
+                     cudaStream_t st) {
+    if (n == 0) return;
+    size_t tiles = (n + 1023) / 1024;
+    if (tiles == 1) {
+        k_scan_tiles<<<1, 1024, 0, st>>>(in, n, out, nullptr);
+        return;
+    }
+    unsigned long long* sums = tmp;
+    unsigned long long* sums_scan = tmp + tiles;
+    k_scan_tiles<<<unsigned(tiles), 1024, 0, st>>>(in, n, out, sums);
+    scan_u64(sums, tiles, sums_scan, tmp + 2 * tiles, st);
+    k_scan_add<<<unsigned(tiles), 1024, 0, st>>>(out, n, sums_scan);
+}
+
+size_t assemble_tmp_bytes(idx_t num_reads) {
+    size_t n = size_t(num_reads) + 1, total = n;   // counts
+    size_t t = (n + 1023) / 1024;
+    while (t > 1) { total += 2 * t; t = (t + 1023) / 1024; }
+    return (total + 64) * sizeof(unsigned long long);
+}
+
+__global__ void k_gather_edges(const SearchOut O, idx_t n, const unsigned long long* off, idx_t* dest,
+                               uint16_t* len, uint8_t* type, int32_t* trans) {
+    const size_t stride = size_t(gridDim.x) * blockDim.x;
+    for (size_t r = size_t(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride) {
+        unsigned long long o = off[r], m = off[r + 1] - o, s = O.edge_src[r];
+        for (unsigned long long j = 0; j < m; ++j) {
+            dest[o + j] = O.e_dest[s + j];
+            len[o + j] = O.e_len[s + j];
+            type[o + j] = O.e_type[s + j];
+            trans[o + j] = O.e_trans[s + j];
+        }
+    }
+}
+
+cudaError_t assemble_counts_total(const SearchOut& o, idx_t num_reads, unsigned long long* out_off, void* scan_tmp,
+                                  size_t scan_tmp_bytes, cudaStream_t st) {
+    const size_t n = size_t(num_reads);
+    if (scan_tmp_bytes < assemble_tmp_bytes(num_reads)) return cudaErrorInvalidValue;
+    unsigned long long* cnt = reinterpret_cast<unsigned long long*>(scan_tmp);
+    unsigned long long* tmp = cnt + n + 1;
+    cudaMemsetAsync(cnt, 0, (n + 1) * sizeof(unsigned long long), st);
+    unsigned g = unsigned(std::min<size_t>((n + 255) / 256 + 1, 152 * 32));
+    if (n) k_edge_counts<<<g, 256, 0, st>>>(o.num_B, o.num_F, idx_t(n), cnt);
+    scan_u64(cnt, n + 1, out_off, tmp, st);
+    return cudaGetLastError();
+}
+
+cudaError_t assemble_gather(const SearchOut& o, idx_t num_reads, const unsigned long long* off, idx_t* dest,
+                            uint16_t* len, uint8_t* type, int32_t* trans, cudaStream_t st) {
+    const size_t n = size_t(num_reads);
+    unsigned g = unsigned(std::min<size_t>((n + 255) / 256 + 1, 152 * 32));
+    if (n) k_gather_edges<<<g, 256, 0, st>>>(o, idx_t(n), off, dest, len, type, trans);
+    return cudaGetLastError();
+}
+
+const size_t kCandBytes = sizeof(Cand);
+const size_t kFrameBytes = sizeof(Frame);
+
+}  // namespace pq

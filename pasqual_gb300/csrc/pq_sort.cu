@@ -1,0 +1,477 @@
+// pq_sort.cu — suffix sort of the reads (forward) or of the reversed reads (backward).
+//
+// Replaces transform_to_triplet[_reverse], initial_sort and suf_sort (src/sufsort.c:80-614) as
+// driven by build_idx (src/index.c:558-585).  The reference sorts in 5 slots by an MSD counting
+// sort on 3-character "triplet" ranks with insertion sort for small buckets; its single-threaded
+// output order is: read-bounded suffix strings, end-of-read lowest, ties by text position.
+//
+// GB300 design: the text is packed 2 bits per base; every suffix gets a 64-bit key made of its
+// first 29 bases (padded with A) and the number of those bases that exist (0..29) -- comparing
+// (padded bases, length) is exactly the end-of-read-lowest order on the first 29 bases.  Keys
+// are radix sorted, each suffix's rank becomes the index of the first row of its group, and
+// prefix doubling sorts by (rank(p), rank(p+h) or "empty" past the read end) for
+// h = 29, 58, 116, ... until h covers the read length.  Every radix pass is stable and the
+// input starts in text order, so equal suffixes stay in text order: the canonical tie-break.
+#include "pq_sort.cuh"
+
+#include <algorithm>
+#include <vector>
+
+namespace pq {
+
+constexpr int kHead = 29;                 // bases per initial key
+constexpr int RS_THREADS = 256;
+constexpr int RS_IPT = 8;
+constexpr int RS_TILE = RS_THREADS * RS_IPT;
+constexpr int RS_WARPS = RS_THREADS / 32;
+constexpr int RS_MAX_CTAS = 152 * 4;
+
+__host__ __device__ __forceinline__ size_t zmin(size_t a, size_t b) { return a < b ? a : b; }
+
+static inline unsigned grid_for(size_t work, int threads, int per_sm = 8) {
+    size_t g = (work + threads - 1) / threads;
+    size_t cap = size_t(152) * per_sm * 4;
+    return unsigned(std::max<size_t>(1, std::min(g, cap)));
+}
+
+// ------------------------------------------------------------------------------ packed text
+
+__device__ __forceinline__ int text_code(const uint8_t* __restrict__ reads, idx_t L, int dir, size_t p) {
+    if (dir == 0) return reads[p];
+    size_t r = p / L, off = p - r * L;
+    return reads[r * L + (L - 1 - off)];
+}
+
+// 32 bases per word, first base in the top two bits (A=0 .. T=3)
+__global__ void k_pack_text(const uint8_t* __restrict__ reads, size_t n, idx_t L, int dir, size_t nwords,
+                            uint64_t* __restrict__ pk) {
+    const size_t stride = size_t(gridDim.x) * blockDim.x;
+    for (size_t w = size_t(blockIdx.x) * blockDim.x + threadIdx.x; w < nwords; w += stride) {
+        uint64_t v = 0;
+        for (int j = 0; j < 32; ++j) {
+            size_t p = w * 32 + j;
+            uint64_t c = p < n ? uint64_t(text_code(reads, L, dir, p) - 1) : 0;
+            v = (v << 2) | c;
+        }
+        pk[w] = v;
+    }
+}
+
+__device__ __forceinline__ uint64_t window(const uint64_t* __restrict__ pk, size_t p) {
+    size_t w = p >> 5;
+    int s = int(p & 31) * 2;
+    uint64_t a = pk[w];
+    uint64_t b = pk[w + 1];
+    return s ? ((a << s) | (b >> (64 - s))) : a;
+}
+
+__global__ void k_init_keys(const uint64_t* __restrict__ pk, size_t n, idx_t L, uint64_t* __restrict__ key,
+                            idx_t* __restrict__ val) {
+    const size_t stride = size_t(gridDim.x) * blockDim.x;
+    for (size_t p = size_t(blockIdx.x) * blockDim.x + threadIdx.x; p < n; p += stride) {
+        int m = int(L - idx_t(p % L));
+        int w = m < kHead ? m : kHead;
+        uint64_t x = window(pk, p);
+        uint64_t keep = ~uint64_t(0) << (64 - 2 * w);     // w >= 1
+        key[p] = (x & keep) | uint64_t(w);
+        val[p] = idx_t(p);
+    }
+}
+
+// ------------------------------------------------------------------------------ radix sort
+
+// Digit histograms of all 8 byte positions over the whole key array (order independent): a pass
+// whose digit is constant over all keys is the identity and is skipped.
+__global__ void k_digit_hist(const uint64_t* __restrict__ key, size_t n, unsigned long long* __restrict__ hist) {
+    __shared__ unsigned int h[8][256];
+    for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x) (&h[0][0])[i] = 0;
+    __syncthreads();
+    const size_t stride = size_t(gridDim.x) * blockDim.x;
+    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
+        uint64_t k = key[i];
+        #pragma unroll
+        for (int d = 0; d < 8; ++d) atomicAdd(&h[d][(k >> (8 * d)) & 255], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x)
+        if ((&h[0][0])[i]) atomicAdd(&hist[i], (unsigned long long)(&h[0][0])[i]);
+}
+
+__global__ void __launch_bounds__(RS_THREADS) k_rs_upsweep(const uint64_t* __restrict__ key, size_t n, int shift,
+                                                           size_t part, unsigned long long* __restrict__ cnt) {
+    __shared__ unsigned int h[RS_WARPS][256];
+    const int warp = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < RS_WARPS * 256; i += RS_THREADS) (&h[0][0])[i] = 0;
+    __syncthreads();
+    const size_t beg = size_t(blockIdx.x) * part;
+    const size_t end = zmin(n, beg + part);
+    for (size_t i = beg + threadIdx.x; i < end; i += RS_THREADS)
+        atomicAdd(&h[warp][(key[i] >> shift) & 255], 1u);
+    __syncthreads();
+    for (int d = threadIdx.x; d < 256; d += RS_THREADS) {
+        unsigned long long s = 0;
+        #pragma unroll
+        for (int w = 0; w < RS_WARPS; ++w) s += h[w][d];
+        cnt[size_t(d) * gridDim.x + blockIdx.x] = s;
+    }
+}
+
+// single-CTA exclusive scan of m 64-bit counts, in place
+__global__ void k_scan_small(unsigned long long* __restrict__ a, size_t m) {
+    __shared__ unsigned long long wsum[32];
+    __shared__ unsigned long long carry;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (size_t base = 0; base < m; base += 1024) {
+        size_t i = base + threadIdx.x;
+        unsigned long long v = i < m ? a[i] : 0, x = v;
+        #pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) wsum[wid] = x;
+        __syncthreads();
+        if (wid == 0) {
+            unsigned long long w = wsum[lane], z = w;
+            #pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                unsigned long long y = __shfl_up_sync(0xffffffffu, z, o);
+                if (lane >= o) z += y;
+            }
+            wsum[lane] = z - w;
+        }
+        __syncthreads();
+        unsigned long long c = carry;
+        if (i < m) a[i] = c + wsum[wid] + x - v;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry = c + wsum[wid] + x;
+        __syncthreads();
+    }
+}
+
+template <class V>
+__global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(const uint64_t* __restrict__ kin, const V* __restrict__ vin,
+                                                             uint64_t* __restrict__ kout, V* __restrict__ vout, size_t n,
+                                                             int shift, size_t part,
+                                                             const unsigned long long* __restrict__ offs) {
+    __shared__ uint64_t sk[RS_TILE];
+    __shared__ V sv[RS_TILE];
+    __shared__ unsigned int wcnt[RS_WARPS][256];
+    __shared__ unsigned int tcount[256];
+    __shared__ unsigned int dstart[256];
+    __shared__ unsigned long long base[256];
+    __shared__ unsigned int wtot[RS_WARPS];
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned lt_mask = (1u << lane) - 1;
+    for (int d = tid; d < 256; d += RS_THREADS) base[d] = offs[size_t(d) * gridDim.x + blockIdx.x];
+    const size_t beg = size_t(blockIdx.x) * part;
+    const size_t end = zmin(n, beg + part);
+    for (size_t t0 = beg; t0 < end; t0 += RS_TILE) {
+        for (int i = lane; i < 256; i += 32) wcnt[warp][i] = 0;
+        __syncwarp();
+        uint64_t k[RS_IPT];
+        V v[RS_IPT];
+        unsigned int lr[RS_IPT];
+        int dg[RS_IPT];
+        #pragma unroll
+        for (int r = 0; r < RS_IPT; ++r) {
+            size_t idx = t0 + size_t(warp) * 32 * RS_IPT + r * 32 + lane;
+            bool valid = idx < end;
+            k[r] = valid ? kin[idx] : 0;
+            v[r] = valid ? vin[idx] : V(0);
+            int d = valid ? int((k[r] >> shift) & 255) : -1;
+            dg[r] = d;
+            unsigned peers = __ballot_sync(0xffffffffu, valid);
+            #pragma unroll
+            for (int b = 0; b < 8; ++b) {
+                unsigned bits = __ballot_sync(0xffffffffu, (d >> b) & 1);
+                peers &= ((d >> b) & 1) ? bits : ~bits;
+            }
+            unsigned before = 0;
+            if (valid) before = wcnt[warp][d];
+            __syncwarp();
+            if (valid && (peers & lt_mask) == 0) wcnt[warp][d] = before + __popc(peers);
+            __syncwarp();
+            lr[r] = before + __popc(peers & lt_mask);
+        }
+        __syncthreads();
+        // per digit: warp prefixes and tile count
+        for (int d = tid; d < 256; d += RS_THREADS) {
+            unsigned run = 0;
+            #pragma unroll
+            for (int w = 0; w < RS_WARPS; ++w) {
+                unsigned c = wcnt[w][d];
+                wcnt[w][d] = run;
+                run += c;
+            }
+            tcount[d] = run;
+        }
+        __syncthreads();
+        // exclusive scan of tcount over the 256 digits (one per thread)
+        {
+            unsigned v0 = tcount[tid], x = v0;
+            #pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            if (lane == 31) wtot[warp] = x;
+            __syncthreads();
+            unsigned pre = 0;
+            for (int w = 0; w < warp; ++w) pre += wtot[w];
+            dstart[tid] = pre + x - v0;
+        }
+        __syncthreads();
+        #pragma unroll
+        for (int r = 0; r < RS_IPT; ++r) {
+            if (dg[r] >= 0) {
+                unsigned pos = dstart[dg[r]] + wcnt[warp][dg[r]] + lr[r];
+                sk[pos] = k[r];
+                sv[pos] = v[r];
+            }
+        }
+        __syncthreads();
+        const int cnt = int(zmin(size_t(RS_TILE), end - t0));
+        for (int j = tid; j < cnt; j += RS_THREADS) {
+            uint64_t key = sk[j];
+            int d = int((key >> shift) & 255);
+            unsigned long long g = base[d] + (unsigned)(j - dstart[d]);
+            kout[g] = key;
+            vout[g] = sv[j];
+        }
+        __syncthreads();
+        for (int d = tid; d < 256; d += RS_THREADS) base[d] += tcount[d];
+        __syncthreads();
+    }
+}
+
+size_t radix_tmp_bytes(size_t n) {
+    (void)n;
+    return (size_t(256) * RS_MAX_CTAS + 8 * 256 + 64) * sizeof(unsigned long long);
+}
+
+template <class V>
+int radix_sort_pairs(uint64_t** k0, V** v0, uint64_t** k1, V** v1, size_t n, int lo_bit, int hi_bit, void* tmp,
+                     size_t tmp_bytes, cudaStream_t st) {
+    if (n <= 1) return 0;
+    if (tmp_bytes < radix_tmp_bytes(n)) return int(cudaErrorInvalidValue);
+    unsigned long long* cnt = reinterpret_cast<unsigned long long*>(tmp);
+    unsigned long long* gh = cnt + size_t(256) * RS_MAX_CTAS;
+    cudaMemsetAsync(gh, 0, 8 * 256 * sizeof(unsigned long long), st);
+    k_digit_hist<<<grid_for(n, 256, 4), 256, 0, st>>>(*k0, n, gh);
+    std::vector<unsigned long long> h(8 * 256);
+    cudaMemcpyAsync(h.data(), gh, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return int(e);
+    size_t tiles = (n + RS_TILE - 1) / RS_TILE;
+    size_t ctas = std::min<size_t>(tiles, RS_MAX_CTAS);
+    size_t part = ((tiles + ctas - 1) / ctas) * RS_TILE;
+    ctas = (n + part - 1) / part;
+    for (int d = lo_bit / 8; d * 8 < hi_bit; ++d) {
+        bool trivial = false;
+        for (int b = 0; b < 256; ++b)
+            if (h[size_t(d) * 256 + b] == n) trivial = true;
+        if (trivial) continue;
+        k_rs_upsweep<<<unsigned(ctas), RS_THREADS, 0, st>>>(*k0, n, 8 * d, part, cnt);
+        k_scan_small<<<1, 1024, 0, st>>>(cnt, 256 * ctas);
+        k_rs_downsweep<V><<<unsigned(ctas), RS_THREADS, 0, st>>>(*k0, *v0, *k1, *v1, n, 8 * d, part, cnt);
+        std::swap(*k0, *k1);
+        std::swap(*v0, *v1);
+    }
+    return int(cudaGetLastError());
+}
+
+template int radix_sort_pairs<uint32_t>(uint64_t**, uint32_t**, uint64_t**, uint32_t**, size_t, int, int, void*,
+                                        size_t, cudaStream_t);
+template int radix_sort_pairs<uint64_t>(uint64_t**, uint64_t**, uint64_t**, uint64_t**, size_t, int, int, void*,
+                                        size_t, cudaStream_t);
+
+// ------------------------------------------------------------------------------ group ranks
+
+constexpr int HT_THREADS = 256;
+constexpr int HT_IPT = 8;
+constexpr int HT_TILE = HT_THREADS * HT_IPT;
+
+// per tile: max over i of (key[i] != key[i-1] ? i : 0), and the number of group starts
+__global__ void k_head_tiles(const uint64_t* __restrict__ key, size_t n, unsigned long long* __restrict__ tmax,
+                             unsigned long long* __restrict__ tcnt) {
+    __shared__ unsigned long long smax[HT_THREADS / 32], scnt[HT_THREADS / 32];
+    const size_t t0 = size_t(blockIdx.x) * HT_TILE;
+    unsigned long long m = 0, c = 0;
+    for (int j = threadIdx.x; j < HT_TILE; j += HT_THREADS) {
+        size_t i = t0 + j;
+        if (i >= n) break;
+        bool f = (i == 0) || key[i] != key[i - 1];
+        if (f) { m = i; c++; }
+    }
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        m = max(m, __shfl_down_sync(0xffffffffu, m, o));
+        c += __shfl_down_sync(0xffffffffu, c, o);
+    }
+    if ((threadIdx.x & 31) == 0) { smax[threadIdx.x >> 5] = m; scnt[threadIdx.x >> 5] = c; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long M = 0, Cn = 0;
+        for (int w = 0; w < HT_THREADS / 32; ++w) { M = max(M, smax[w]); Cn += scnt[w]; }
+        tmax[blockIdx.x] = M;
+        tcnt[blockIdx.x] = Cn;
+    }
+}
+
+// single CTA: exclusive max-scan of tile maxima (in place), total of tile counts into *groups
+__global__ void k_head_carry(unsigned long long* __restrict__ tmax, const unsigned long long* __restrict__ tcnt,
+                             size_t m, unsigned long long* __restrict__ groups) {
+    __shared__ unsigned long long wv[32], carry, total;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (threadIdx.x == 0) { carry = 0; total = 0; }
+    __syncthreads();
+    for (size_t base = 0; base < m; base += 1024) {
+        size_t i = base + threadIdx.x;
+        unsigned long long v = i < m ? tmax[i] : 0, x = v;
+        unsigned long long c = i < m ? tcnt[i] : 0;
+        #pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x = max(x, y);
+        }
+        #pragma unroll
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+        if (lane == 31) wv[wid] = x;
+        if (lane == 0) atomicAdd(&total, c);
+        __syncthreads();
+        unsigned long long pre = carry;
+        for (int w = 0; w < wid; ++w) pre = max(pre, wv[w]);
+        unsigned long long up = __shfl_up_sync(0xffffffffu, x, 1);
+        unsigned long long excl = lane ? max(pre, up) : pre;
+        if (i < m) tmax[i] = excl;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry = max(pre, x);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *groups = total;
+}
+
+// head[i] = last group start <= i; rank[val[i]] = head[i]; kout[i] = head[i] << 32
+// (kout != key: neighbouring threads still read key[i0-1])
+template <class V>
+__global__ void k_head_apply(const uint64_t* __restrict__ key, uint64_t* __restrict__ kout, const V* __restrict__ val,
+                             size_t n, const unsigned long long* __restrict__ carry, uint32_t* __restrict__ rank) {
+    __shared__ unsigned long long wv[HT_THREADS / 32];
+    const size_t t0 = size_t(blockIdx.x) * HT_TILE;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    // thread owns HT_IPT consecutive items
+    const size_t i0 = t0 + size_t(threadIdx.x) * HT_IPT;
+    unsigned long long h[HT_IPT];
+    uint64_t prevk = (i0 > 0 && i0 < n) ? key[i0 - 1] : 0;
+    unsigned long long run = 0;
+    #pragma unroll
+    for (int j = 0; j < HT_IPT; ++j) {
+        size_t i = i0 + j;
+        uint64_t kk = i < n ? key[i] : 0;
+        bool f = i < n && (i == 0 || kk != prevk);
+        if (f) run = i;
+        h[j] = run;
+        prevk = kk;
+    }
+    unsigned long long x = run;
+    #pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x = max(x, y);
+    }
+    if (lane == 31) wv[wid] = x;
+    __syncthreads();
+    unsigned long long pre = carry[blockIdx.x];
+    for (int w = 0; w < wid; ++w) pre = max(pre, wv[w]);
+    unsigned long long up = __shfl_up_sync(0xffffffffu, x, 1);
+    unsigned long long excl = lane ? max(pre, up) : pre;
+    #pragma unroll
+    for (int j = 0; j < HT_IPT; ++j) {
+        size_t i = i0 + j;
+        if (i < n) {
+            unsigned long long hd = max(excl, h[j]);
+            rank[val[i]] = uint32_t(hd);
+            kout[i] = uint64_t(hd) << 32;
+        }
+    }
+}
+
+// key[i] |= rank of the suffix h bases further (+1), or 0 when that lies past the read end
+template <class V>
+__global__ void k_second_keys(uint64_t* __restrict__ key, const V* __restrict__ val, size_t n, idx_t L, size_t h,
+                              const uint32_t* __restrict__ rank) {
+    const size_t stride = size_t(gridDim.x) * blockDim.x;
+    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
+        size_t p = val[i];
+        size_t off = p % L;
+        uint64_t second = (off + h < size_t(L)) ? uint64_t(rank[p + h]) + 1 : 0;
+        key[i] |= second;
+    }
+}
+
+template <class V>
+__global__ void k_copy_vals(const V* __restrict__ v, size_t n, idx_t* __restrict__ sa) {
+    const size_t stride = size_t(gridDim.x) * blockDim.x;
+    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) sa[i] = idx_t(v[i]);
+}
+
+// ------------------------------------------------------------------------------ driver
+
+static size_t al(size_t b) { return (b + 255) & ~size_t(255); }
+
+size_t suffix_sort_tmp_bytes(size_t n) {
+    size_t tiles = (n + HT_TILE - 1) / HT_TILE + 1;
+    return 2 * al(n * sizeof(uint64_t)) + 2 * al(n * sizeof(idx_t)) +
+           al(n * sizeof(uint32_t)) + al((n / 32 + 4) * sizeof(uint64_t)) + al(radix_tmp_bytes(n)) +
+           al(3 * tiles * sizeof(unsigned long long)) + 1024;
+}
+
+int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa, void* tmp, size_t tmp_bytes,
+                cudaStream_t st) {
+    const size_t n = size_t(num_reads) * size_t(L);
+    if (n == 0) return 0;
+    if (n >= (size_t(1) << 31)) return int(cudaErrorNotSupported);   // 32-bit group ranks
+    if (tmp_bytes < suffix_sort_tmp_bytes(n)) return int(cudaErrorInvalidValue);
+    char* p = static_cast<char*>(tmp);
+    uint64_t* ka = reinterpret_cast<uint64_t*>(p); p += al(n * sizeof(uint64_t));
+    uint64_t* kb = reinterpret_cast<uint64_t*>(p); p += al(n * sizeof(uint64_t));
+    idx_t* va = reinterpret_cast<idx_t*>(p); p += al(n * sizeof(idx_t));
+    idx_t* vb = reinterpret_cast<idx_t*>(p); p += al(n * sizeof(idx_t));
+    uint32_t* rank = reinterpret_cast<uint32_t*>(p); p += al(n * sizeof(uint32_t));
+    const size_t nwords = n / 32 + 4;
+    uint64_t* pk = reinterpret_cast<uint64_t*>(p); p += al(nwords * sizeof(uint64_t));
+    void* rtmp = p; p += al(radix_tmp_bytes(n));
+    const size_t tiles = (n + HT_TILE - 1) / HT_TILE;
+    unsigned long long* tmax = reinterpret_cast<unsigned long long*>(p);
+    unsigned long long* tcnt = tmax + tiles + 1;
+    unsigned long long* groups = tcnt + tiles + 1;
+
+    k_pack_text<<<grid_for(nwords, 256), 256, 0, st>>>(reads, n, idx_t(L), dir, nwords, pk);
+    k_init_keys<<<grid_for(n, 256), 256, 0, st>>>(pk, n, idx_t(L), ka, va);
+    int rc = radix_sort_pairs<idx_t>(&ka, &va, &kb, &vb, n, 0, 64, rtmp, radix_tmp_bytes(n), st);
+    if (rc) return rc;
+    for (size_t h = kHead;; h *= 2) {
+        k_head_tiles<<<unsigned(tiles), HT_THREADS, 0, st>>>(ka, n, tmax, tcnt);
+        k_head_carry<<<1, 1024, 0, st>>>(tmax, tcnt, tiles, groups);
+        k_head_apply<idx_t><<<unsigned(tiles), HT_THREADS, 0, st>>>(ka, kb, va, n, tmax, rank);
+        std::swap(ka, kb);
+        unsigned long long g = 0;
+        cudaMemcpyAsync(&g, groups, sizeof g, cudaMemcpyDeviceToHost, st);
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return int(e);
+        if (g == n || h >= size_t(L)) break;
+        k_second_keys<idx_t><<<grid_for(n, 256), 256, 0, st>>>(ka, va, n, idx_t(L), h, rank);
+        int bits = 1;
+        while ((size_t(1) << bits) <= n + 1) ++bits;
+        rc = radix_sort_pairs<idx_t>(&ka, &va, &kb, &vb, n, 0, 32 + bits, rtmp, radix_tmp_bytes(n), st);
+        if (rc) return rc;
+    }
+    k_copy_vals<idx_t><<<grid_for(n, 256), 256, 0, st>>>(va, n, sa);
+    return int(cudaGetLastError());
+}
+
+}  // namespace pq

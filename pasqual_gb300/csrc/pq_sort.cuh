@@ -1,0 +1,25 @@
+// pq_sort.cuh — GPU suffix sort of read-bounded suffixes (internal).
+#pragma once
+#include "pq_common.cuh"
+
+namespace pq {
+
+size_t suffix_sort_tmp_bytes(size_t n);
+
+// Suffix array of direction dir in the canonical order (suffix string with end-of-read lowest,
+// then text position).  Returns 0 or a cudaError_t value.
+int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa, void* tmp,
+                size_t tmp_bytes, cudaStream_t st);
+
+// Per-read seeds from a k-mer table (pq_index.cu).
+cudaError_t read_seeds(const uint8_t* reads, idx_t num_reads, int L, int dir, int k, const idx_t* kstart,
+                       const idx_t* kend, idx_t* start, idx_t* size, cudaStream_t st);
+
+// Stable LSD radix sort of (key, value) pairs on the bits [lo_bit, hi_bit) of the key.
+// Buffers are ping-ponged; the sorted result ends in (*k0, *v0) (pointers may be swapped).
+template <class V>
+int radix_sort_pairs(uint64_t** k0, V** v0, uint64_t** k1, V** v1, size_t n, int lo_bit, int hi_bit,
+                     void* tmp, size_t tmp_bytes, cudaStream_t st);
+size_t radix_tmp_bytes(size_t n);
+
+}  // namespace pq

@@ -1,0 +1,83 @@
+"""Regenerate the golden fixtures in this folder from the UNMODIFIED reference.
+
+Needs the reference sources (read where they lie) and an x86 host: it builds oracle/_ref with
+oracle/Makefile, writes seeded synthetic reads as FASTA, runs oracle/_ref/ref_dump_uXX (which
+drives the reference's construct_index / sufsort / construct_string_graph) and stores, per case:
+
+* the reads the reference kept after its Bloom-filter de-duplication (codes 1..4),
+* C[], suffix_count, prefix_count,
+* SHA-256 digests of every array the hot path produces: both suffix arrays, both FM-indexes in
+  the reference layout (OCC_bitmap, OCC_sample, reads_index), the per-node edge counts and node
+  fields, and the ordered edge list (dest, overlap length, type, path trans),
+* the full edge arrays for the small cases.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from pasqual_gb300 import synth  # noqa: E402
+from oracle import port  # noqa: E402
+
+# name: genome length, gc, repeat fraction, divergence, low-complexity fraction, read length,
+#       coverage, error rate, t, index width, keep full edge arrays
+CASES = {
+    "iid8k_L50_t31_u32": (8000, 0.50, 0.00, (0.0, 0.0), 0.00, 50, 30, 0.0, 31, 32, True),
+    "rep15k_L100_t63_u32": (15000, 0.41, 0.10, (0.01, 0.01), 0.00, 100, 30, 0.005, 63, 32, True),
+    "lowc12k_L150_t63_u64": (12000, 0.40, 0.12, (0.005, 0.02), 0.02, 150, 20, 0.003, 63, 64, True),
+    "iid3k_L40_t10_u32": (3000, 0.50, 0.00, (0.0, 0.0), 0.00, 40, 40, 0.0, 10, 32, False),
+    "iid5k_L60_t59_u32": (5000, 0.50, 0.00, (0.0, 0.0), 0.00, 60, 50, 0.0, 59, 32, False),
+    "dinuc6k_L60_t20_u32": (6000, 0.45, 0.00, (0.0, 0.0), 0.50, 60, 30, 0.002, 20, 32, False),
+    "rep20k_L100_t63_u64": (20000, 0.41, 0.10, (0.01, 0.01), 0.00, 100, 20, 0.005, 63, 64, False),
+}
+
+DIGEST_KEYS = ["sa0", "sa1", "bitmap0", "bitmap1", "sample0", "sample1", "reads_index0",
+               "reads_index1", "num_B", "num_F", "node_types", "dest", "length", "etype", "trans"]
+
+
+def digest(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def case_reads(name: str) -> np.ndarray:
+    g_len, gc, rep, div, lowc, L, cov, err, t, width, full = CASES[name]
+    seed = sum(map(ord, name))
+    g = synth.genome(g_len, gc, rep, div, lowc, seed=seed)
+    return synth.reads_for_coverage(g, L, cov, err, seed=seed + 1)
+
+
+def make(name: str, tmp: str) -> None:
+    g_len, gc, rep, div, lowc, L, cov, err, t, width, full = CASES[name]
+    rd = case_reads(name)
+    fa = os.path.join(tmp, name + ".fa")
+    synth.write_fasta(fa, rd)
+    d = port.run_ref_dump(fa, L, t, os.path.join(tmp, name), width=width)
+    idt = np.uint64 if width == 64 else np.uint32
+    d["dest"] = d["dest"].astype(idt)
+    out = {"reads": d["reads"], "t": np.int64(t), "width": np.int64(width), "C": d["C"],
+           "suffix_count": d["suffix_count"], "prefix_count": d["prefix_count"],
+           "num_edges": np.int64(len(d["dest"]))}
+    for k in DIGEST_KEYS:
+        out["sha_" + k] = np.array(digest(d[k]))
+    if full:
+        for k in ("num_B", "num_F", "dest", "length", "etype", "trans"):
+            out["full_" + k] = d[k]
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print("%-24s reads=%-6d edges=%-7d" % (name, d["reads"].shape[0], len(d["dest"])))
+
+
+if __name__ == "__main__":
+    port.build(ref=True)
+    with tempfile.TemporaryDirectory() as tmp:
+        for name in (sys.argv[1:] or CASES):
+            make(name, tmp)

@@ -1,0 +1,143 @@
+"""CUDA path (through the C ABI) against the golden vectors of the unmodified reference and
+against the C restatement at larger sizes.  Integer work: every comparison is bit-exact."""
+import numpy as np
+import pytest
+
+from conftest import golden_cases, load_golden, sha, idx_dtype
+import pasqual_gb300 as pq
+from pasqual_gb300 import graph, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_ctx(width):
+    return pq.Pasqual(width)
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_sort_and_index_match_reference(name):
+    g = load_golden(name)
+    with gpu_ctx(int(g["width"])) as P:
+        P.set_reads(g["reads"], int(g["t"]))
+        C, sfx, pfx = P.counts()
+        assert np.array_equal(C, g["C"])
+        assert np.array_equal(sfx, g["suffix_count"]) and np.array_equal(pfx, g["prefix_count"])
+        for d in (0, 1):
+            P.sort(d)
+            assert sha(P.get_sa(d)) == str(g["sha_sa%d" % d]), "suffix array %d" % d
+            P.build_fm(d)
+            bm, smp, ri = P.index_ref(d)
+            assert sha(bm) == str(g["sha_bitmap%d" % d]), "OCC_bitmap %d" % d
+            assert sha(smp) == str(g["sha_sample%d" % d]), "OCC_sample %d" % d
+            assert sha(ri) == str(g["sha_reads_index%d" % d]), "reads_index %d" % d
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_overlaps_match_reference(name):
+    g = load_golden(name)
+    dt = idx_dtype(g["width"])
+    with gpu_ctx(int(g["width"])) as P:
+        P.construct_index(g["reads"], int(g["t"]))
+        out = P.construct_string_graph()
+    assert len(out.dest) == int(g["num_edges"])
+    assert sha(out.num_B) == str(g["sha_num_B"])
+    assert sha(out.num_F) == str(g["sha_num_F"])
+    assert sha(out.dest.astype(dt)) == str(g["sha_dest"])
+    assert sha(out.length) == str(g["sha_length"])
+    assert sha(out.etype) == str(g["sha_etype"])
+    assert sha(graph.trans_with_mask(out.num_B, out.num_F, out.edge_off, out.trans)) == \
+        str(g["sha_trans"])
+    assert sha(graph.node_fields(out.num_B, out.num_F, out.olp_B, out.olp_F)) == \
+        str(g["sha_node_types"])
+    if "full_dest" in g:
+        assert np.array_equal(out.dest.astype(np.uint64), g["full_dest"])
+
+
+@pytest.mark.parametrize("k", [1, 5, 10])
+def test_seed_depth_does_not_change_edges(k):
+    g = load_golden("rep15k_L100_t63_u32")
+    with gpu_ctx(32) as P:
+        P.set_reads(g["reads"], int(g["t"]))
+        P.set_seed_k(k)
+        P.build_index()
+        out = P.construct_string_graph()
+    assert sha(out.dest.astype(np.uint32)) == str(g["sha_dest"])
+    assert sha(out.num_F) == str(g["sha_num_F"])
+
+
+def test_wide_tier_used_and_exact():
+    """Dinucleotide runs give reads with many edges: some must go through the wide kernel."""
+    g = load_golden("dinuc6k_L60_t20_u32")
+    with gpu_ctx(32) as P:
+        P.construct_index(g["reads"], int(g["t"]))
+        out = P.construct_string_graph()
+    assert out.wide_reads > 0
+    assert sha(out.dest.astype(np.uint32)) == str(g["sha_dest"])
+
+
+def _oracle_run(reads, t, width):
+    from oracle import port
+    P = port.Port(width)
+    ix = P.build_index(reads, t)
+    return ix, P.overlaps(ix)
+
+
+@pytest.mark.parametrize("width", [32, 64])
+def test_against_oracle_config1_shape(width):
+    """1 Mbp-shaped workload at 1/5 scale (200 kbp, L=50, 40x, t=31): GPU == oracle."""
+    gen = synth.genome(200_000, 0.5, seed=21)
+    rd = synth.reads_for_coverage(gen, 50, 40, 0.0, seed=22)
+    rd = np.unique(rd, axis=0)          # distinct reads, as after de-duplication
+    ix, ref = _oracle_run(rd, 31, width)
+    with gpu_ctx(width) as P:
+        P.construct_index(rd, 31)
+        for d in (0, 1):
+            assert np.array_equal(P.get_sa(d), ix["sa%d" % d])
+            bm, smp, ri = P.index_ref(d)
+            assert np.array_equal(bm, ix["bitmap%d" % d])
+            assert np.array_equal(smp, ix["sample%d" % d])
+            assert np.array_equal(ri, ix["reads_index%d" % d])
+        out = P.construct_string_graph()
+    assert np.array_equal(out.edge_off, ref.edge_off)
+    assert np.array_equal(out.dest, ref.dest)
+    assert np.array_equal(out.length, ref.length)
+    assert np.array_equal(out.etype, ref.etype)
+    assert np.array_equal(out.trans, ref.trans)
+    assert np.array_equal(out.olp_B, ref.olp_B) and np.array_equal(out.olp_F, ref.olp_F)
+
+
+def test_repeats_errors_long_reads_against_oracle():
+    """L=150 reads with repeats, low-complexity runs and errors (U32): GPU == oracle."""
+    gen = synth.genome(300_000, 0.40, 0.12, (0.005, 0.02), 0.02, seed=31)
+    rd = np.unique(synth.reads_for_coverage(gen, 150, 20, 0.003, seed=32), axis=0)
+    ix, ref = _oracle_run(rd, 63, 32)
+    with gpu_ctx(32) as P:
+        P.construct_index(rd, 63)
+        assert np.array_equal(P.get_sa(0), ix["sa0"])
+        assert np.array_equal(P.get_sa(1), ix["sa1"])
+        out = P.construct_string_graph()
+    assert np.array_equal(out.dest, ref.dest)
+    assert np.array_equal(out.trans, ref.trans)
+    assert np.array_equal(out.num_B, ref.num_B) and np.array_equal(out.num_F, ref.num_F)
+
+
+def test_empty_and_tiny_inputs():
+    with gpu_ctx(32) as P:
+        P.construct_index(np.zeros((0, 50), np.uint8), 31)
+        out = P.construct_string_graph()
+        assert len(out.dest) == 0 and len(out.num_B) == 0
+    one = np.array([[1, 2, 3, 4] * 12 + [1, 2]], np.uint8)
+    with gpu_ctx(32) as P:
+        P.construct_index(one, 31)
+        out = P.construct_string_graph()
+        assert len(out.dest) == 0
+
+
+def test_invalid_arguments_raise():
+    with gpu_ctx(32) as P:
+        with pytest.raises(pq.PQError):
+            P.set_reads(np.ones((10, 50), np.uint8), 9)      # t must exceed SEQ_DEPTH (9)
+        with pytest.raises(pq.PQError):
+            P.set_reads(np.ones((10, 50), np.uint8), 50)     # t must be below L
+        with pytest.raises(pq.PQError):
+            P.overlaps()                                     # no index yet

@@ -1,0 +1,65 @@
+"""The C restatement (oracle) against the golden vectors made by the unmodified reference.
+
+Pins every array of the hot path: both suffix arrays (canonical single-thread order), both
+FM-indexes in the reference layout, and the per-read ordered edge lists with node fields.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_cases, load_golden, sha, idx_dtype
+from oracle import port
+from pasqual_gb300 import graph
+
+
+@pytest.fixture(scope="module")
+def ports():
+    port.build()
+    return {32: port.Port(32), 64: port.Port(64)}
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_oracle_matches_reference(name, ports):
+    g = load_golden(name)
+    P = ports[int(g["width"])]
+    ix = P.build_index(g["reads"], int(g["t"]), threads=4)
+    C, sfx, pfx = ix["C"], ix["suffix_count"], ix["prefix_count"]
+    assert np.array_equal(C, g["C"]) and np.array_equal(sfx, g["suffix_count"])
+    assert np.array_equal(pfx, g["prefix_count"])
+    for k in ("sa0", "sa1", "bitmap0", "bitmap1", "sample0", "sample1", "reads_index0",
+              "reads_index1"):
+        assert sha(ix[k]) == str(g["sha_" + k]), k
+    out = P.overlaps(ix, threads=4)
+    dt = idx_dtype(g["width"])
+    assert int(g["num_edges"]) == len(out.dest)
+    assert sha(out.num_B) == str(g["sha_num_B"])
+    assert sha(out.num_F) == str(g["sha_num_F"])
+    assert sha(out.dest.astype(np.uint64).astype(dt)) == str(g["sha_dest"])
+    assert sha(out.length) == str(g["sha_length"])
+    assert sha(out.etype) == str(g["sha_etype"])
+    assert sha(graph.trans_with_mask(out.num_B, out.num_F, out.edge_off, out.trans)) == \
+        str(g["sha_trans"])
+    nf = graph.node_fields(out.num_B, out.num_F, out.olp_B, out.olp_F)
+    assert sha(nf) == str(g["sha_node_types"])
+
+
+def test_oracle_seed_equivalence(ports):
+    """Any exact seed interval gives the same edges (k-mer seeds vs depth-1 starts)."""
+    g = load_golden("rep15k_L100_t63_u32")
+    P = ports[32]
+    ix = P.build_index(g["reads"], int(g["t"]), threads=4, seed_k=12)
+    a = P.overlaps(ix, threads=4)
+    b = P.overlaps(ix, threads=4, seeds=(ix["seed0"], ix["seed1"]))
+    assert np.array_equal(a.dest, b.dest) and np.array_equal(a.trans, b.trans)
+    assert b.probes < a.probes
+
+
+def test_oracle_bounded_sample_equals_full(ports):
+    """A read range gives the same per-read edges as the full run (used by the CPU baseline)."""
+    g = load_golden("iid8k_L50_t31_u32")
+    P = ports[32]
+    ix = P.build_index(g["reads"], int(g["t"]), threads=4)
+    full = P.overlaps(ix, threads=4)
+    part = P.overlaps(ix, first=1000, count=500, threads=2)
+    o = full.edge_off.astype(np.int64)
+    assert np.array_equal(part.dest, full.dest[o[1000]:o[1500]])
+    assert np.array_equal(part.num_F, full.num_F[1000:1500])
