@@ -1,0 +1,327 @@
+#!/usr/bin/env python
+"""Benchmark: overlap-search reads/s (and suffix-sort Msuffix/s) of PASQUAL's hot path.
+
+Workload (default): 50 Mbp synthetic genome, GC 41 %, 10 % repeat copies of 1-5 kbp segments at
+1 % divergence; 100 bp reads at 30x from both strands with 0.5 % substitution errors; t = 63;
+32-bit index.  Reads are de-duplicated (equal or reverse-complement reads dropped) before use.
+
+A step is one overlap search (find_intervals + transitive reduction + edge CSR) over every read,
+on indexes already resident in HBM.  ``value`` = reads searched / time, whole job.
+
+``e2e`` runs the public API end to end each step: host reads (pinned) -> GPU suffix sorts and
+FM-indexes -> overlap search -> edges back to host.
+
+``--impl reference`` times the reference's CPU algorithm for the same metric: the C restatement
+of the reference (oracle/), OpenMP over all host cores, on a bounded sample.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import signal
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "overlap-search reads/s + sort Msuffix/s, learned vs plain GPU, bit-exact"
+WORKLOAD = "50Mbp_L100_30x_t63"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=WORKLOAD)
+    ap.add_argument("--scale", type=float, default=1.0, help="genome-size scale (1.0 = full)")
+    ap.add_argument("--cpu-scale", type=float, default=0.1,
+                    help="genome-size scale of the CPU-baseline sample")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload_reads(name: str, scale: float):
+    from pasqual_gb300 import synth
+    _, rd, L, t = synth.make_workload(name, scale=scale)
+    return synth.dedup(rd), L, t
+
+
+def measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic_per_probe():
+    """DRAM bytes per rank probe of the search kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "k_search_fast.md")
+    try:
+        txt = open(p).read()
+    except OSError:
+        return None
+    m = re.search(r"dram_bytes_per_probe\s*=\s*([0-9.]+)", txt)
+    return float(m.group(1)) if m else None
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.send_signal(signal.SIGTERM)
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(workload: str, scale: float, seconds: float, threads: int | None = None):
+    """The C restatement of the reference's overlap search on the host cores (OpenMP), timed on a
+    bounded sample: index of a genome scaled by `scale`, search over as many reads as fit in
+    about `seconds` seconds."""
+    from oracle import port
+    port.build()
+    rd, L, t = workload_reads(workload, scale)
+    threads = threads or os.cpu_count() or 1
+    P = port.Port(32)
+    ix = P.build_index(rd, t, threads=threads, seed_k=min(12, t))
+    seeds = (ix["seed0"], ix["seed1"])
+    nr = rd.shape[0]
+    probe = min(nr, 20000)
+    t0 = time.perf_counter()
+    P.overlaps(ix, 0, probe, threads=threads, seeds=seeds)
+    dt = time.perf_counter() - t0
+    count = int(min(nr, max(probe, probe * seconds / max(dt, 1e-6))))
+    t0 = time.perf_counter()
+    g = P.overlaps(ix, 0, count, threads=threads, seeds=seeds)
+    dt = time.perf_counter() - t0
+    return {"value": count / dt, "unit": "reads/s", "cores": threads, "kind": "port",
+            "sample": "%d of %d reads of the %s workload at genome scale %g (%d bp reads, t=%d), "
+                      "forward/backward seeds at depth 12 as the reference's sort records them; "
+                      "%.1f s" % (count, nr, workload, scale, L, t, dt),
+            "probes_per_read": g.probes / max(count, 1)}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    cb = cpu_baseline(args.workload, args.cpu_scale, args.cpu_seconds)
+    vals = [cb["value"]]
+    for _ in range(max(0, args.steps - 1)):
+        vals.append(cpu_baseline(args.workload, args.cpu_scale, args.cpu_seconds / 2)["value"])
+    v = statistics.median(vals)
+    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": "reads/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "int32-index", "data": "synthetic",
+           "config": {"workload": args.workload, "index": "U32", "sample_scale": args.cpu_scale},
+           "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+           "e2e": {"value": v, "unit": "reads/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    out["cpu_baseline"]["value"] = v
+    print(json.dumps(out), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import pasqual_gb300 as pq
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    rd, L, t = workload_reads(args.workload, args.scale)
+    nr = rd.shape[0]
+    n = nr * L
+    stream = torch.cuda.Stream(device=dev)
+    P = pq.Pasqual(32, device=local, stream=stream.cuda_stream)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def max_over_ranks(x: float) -> float:
+        if world == 1:
+            return x
+        import torch.distributed as dist
+        tt = torch.tensor([x], device=dev, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        return float(tt.item())
+
+    # ---- index build (setup) and suffix-sort throughput
+    P.set_reads(rd, t)
+    P.build_index()                       # warm-up build
+    sort_ms = []
+    for _ in range(max(1, min(args.steps, 3))):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        e0.record(stream)
+        P.sort(0)
+        P.sort(1)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        sort_ms.append(e0.elapsed_time(e1))
+    P.build_fm(0)
+    P.build_fm(1)
+    sort_ms_med = statistics.median(sort_ms)
+
+    # ---- overlap search: warm-up, then K timed steps
+    for _ in range(args.warmup):
+        P.overlaps()
+    _, l0 = P.kernel_stats()
+    clocks = Clocks(local)
+    kern_ms = []
+    barrier()
+    torch.cuda.synchronize(dev)
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        P.overlaps()
+        kern_ms.append(P.kernel_stats()[0])
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    barrier()
+    ck = clocks.stop()
+    _, l1 = P.kernel_stats()
+    step_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
+    g = P.graph()
+    probes = g.probes
+    wide = g.wide_reads
+    ne = len(g.dest)
+
+    # ---- end to end through the public API with host buffers
+    pinned = torch.empty((nr, L), dtype=torch.uint8, pin_memory=True)
+    pinned.numpy()[:] = rd
+    e2e_ms = []
+    h2d = nr * L
+    d2h = 0
+    for s in range(args.e2e_steps + 1):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        P.set_reads(pinned.numpy(), t)
+        P.build_index()
+        gg = P.construct_string_graph()
+        d2h = sum(a.nbytes for a in (gg.num_B, gg.num_F, gg.olp_B, gg.olp_F, gg.edge_off, gg.dest,
+                                      gg.length, gg.etype, gg.trans))
+        torch.cuda.synchronize(dev)
+        if s > 0:                          # first pass is a warm-up
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_ms_med = max_over_ranks(statistics.median(e2e_ms))
+
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peak_hbm()
+    kms = statistics.median(kern_ms)
+    achieved = 32.0 * probes / (kms * 1e-3) / 1e9
+    tpp = profile_traffic_per_probe()
+    out = {
+        "metric": METRIC, "value": nr * world / (step_ms * 1e-3), "unit": "reads/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32-index",
+        "data": "synthetic",
+        "config": {"workload": args.workload, "genome_scale": args.scale, "reads": nr,
+                   "read_len": L, "t": t, "index": "U32", "suffixes_per_index": n,
+                   "edges": ne, "wide_tier_reads": wide, "seed_k": min(12, t),
+                   "l2": "inputs larger than L2 (two FM-indexes %.2f GB + reads %.2f GB)"
+                         % (2 * (n // 64 + 1) * 32 / 1e9, n / 1e9),
+                   "parallelism": "replica per GPU" if world > 1 else "single GPU"},
+        "sort": {"value": 2 * n / (sort_ms_med * 1e-3) / 1e6, "unit": "Msuffix/s",
+                 "ms_fw_plus_bw": sort_ms_med},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind,
+                     "kernel": "k_search_fast",
+                     "algorithmic_bytes_per_launch": 32 * probes,
+                     "probes_per_read": probes / max(nr, 1), "kernel_ms": kms,
+                     "traffic": (tpp * probes) if tpp else None},
+        "gpu_launches": int(l1 - l0),
+        "e2e": {"value": nr / (e2e_ms_med * 1e-3), "unit": "reads/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": e2e_ms_med},
+    }
+    if ck:
+        out["clocks"] = ck
+    if world == 1 and not args.no_cpu_baseline:
+        cb = cpu_baseline(args.workload, args.cpu_scale, args.cpu_seconds)
+        out["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    print(json.dumps(out), flush=True)
+    P.close()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

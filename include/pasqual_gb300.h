@@ -124,6 +124,11 @@ PQ_API int pq_get_graph (pq_ctx * ctx, uint16_t * num_B, uint16_t * num_F, int32
 /* Time (ms, CUDA events on the context stream) of the last pq_sort/pq_build_fm/pq_overlaps. */
 PQ_API int pq_get_stage_ms (pq_ctx * ctx, float *sort_ms, float *fm_ms, float *search_ms);
 
+/* Duration (ms, CUDA events on the context stream) of the fast search kernel in the last
+ * pq_overlaps, and the number of kernels this library has launched since it was loaded. */
+PQ_API int pq_get_kernel_stats (pq_ctx * ctx, float *search_kernel_ms,
+                                unsigned long long *launches);
+
 #ifdef __cplusplus
 }
 #endif

@@ -30,7 +30,7 @@ PQ_ERRORS = {1: "PQ_ERR_ARG", 2: "PQ_ERR_CUDA", 3: "PQ_ERR_NOMEM", 4: "PQ_ERR_TO
 EXPORTS = ["pq_idx_bytes", "pq_create", "pq_destroy", "pq_last_error", "pq_set_reads",
            "pq_get_counts", "pq_sort", "pq_set_sa", "pq_get_sa", "pq_build_fm", "pq_build_index",
            "pq_get_index_ref", "pq_get_seeds", "pq_set_seed_k", "pq_overlaps",
-           "pq_get_graph_sizes", "pq_get_graph", "pq_get_stage_ms"]
+           "pq_get_graph_sizes", "pq_get_graph", "pq_get_stage_ms", "pq_get_kernel_stats"]
 
 
 class PQError(RuntimeError):
@@ -76,6 +76,7 @@ def load_library(width: int = 32) -> ct.CDLL:
         "pq_get_graph_sizes": (c_int, [vp, vp, vp, vp]),
         "pq_get_graph": (c_int, [vp] + [vp] * 9),
         "pq_get_stage_ms": (c_int, [vp, vp, vp, vp]),
+        "pq_get_kernel_stats": (c_int, [vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -229,6 +230,13 @@ class Pasqual:
     def construct_string_graph(self) -> Graph:
         self.overlaps()
         return self.graph()
+
+    def kernel_stats(self):
+        """(fast search kernel ms of the last overlap search, kernels launched so far)."""
+        ms, n = ct.c_float(), ct.c_ulonglong()
+        self._ck(self.lib.pq_get_kernel_stats(self.h, ct.byref(ms), ct.byref(n)),
+                 "pq_get_kernel_stats")
+        return ms.value, n.value
 
     def stage_ms(self):
         a, b, c = ct.c_float(), ct.c_float(), ct.c_float()

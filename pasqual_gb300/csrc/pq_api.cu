@@ -12,6 +12,13 @@
 
 static_assert(sizeof(pq_idx) == sizeof(idx_t), "pq_idx and idx_t must agree");
 
+#include <atomic>
+namespace pq {
+static std::atomic<unsigned long long> g_launches{0};
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+unsigned long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
+}  // namespace pq
+
 namespace {
 
 struct DevBuf {
@@ -54,8 +61,8 @@ struct pq_ctx {
     cudaStream_t st = nullptr;
     bool own_stream = false;
     std::string err;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    float ms_sort = 0, ms_fm = 0, ms_search = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk0 = nullptr, evk1 = nullptr;
+    float ms_sort = 0, ms_fm = 0, ms_search = 0, ms_fast = 0;
 
     idx_t num_reads = 0;
     int L = 0, t = 0;
@@ -122,6 +129,8 @@ int pq_create(pq_ctx** out, int device, void* cuda_stream) {
     }
     cudaEventCreate(&ctx->ev0);
     cudaEventCreate(&ctx->ev1);
+    cudaEventCreate(&ctx->evk0);
+    cudaEventCreate(&ctx->evk1);
     *out = ctx;
     return PQ_OK;
 }
@@ -145,6 +154,8 @@ void pq_destroy(pq_ctx* ctx) {
     }
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->evk0) cudaEventDestroy(ctx->evk0);
+    if (ctx->evk1) cudaEventDestroy(ctx->evk1);
     if (ctx->own_stream) cudaStreamDestroy(ctx->st);
     delete ctx;
 }
@@ -408,10 +419,12 @@ int pq_overlaps(pq_ctx* ctx) {
     CK(cudaEventRecord(ctx->ev0, ctx->st));
     int dev_sms = 152;
     cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    CK(cudaEventRecord(ctx->evk0, ctx->st));
     if (nr) {
         int blocks = int(std::min<size_t>((nr + 127) / 128, size_t(dev_sms) * 16));
         CK(pq::search_fast(A, O, 128, blocks, ctx->st));
     }
+    CK(cudaEventRecord(ctx->evk1, ctx->st));
     unsigned long long hc[3];
     CK(cudaMemcpyAsync(hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
@@ -504,6 +517,7 @@ int pq_overlaps(pq_ctx* ctx) {
     CK(cudaEventSynchronize(ctx->ev1));
     CK(cudaStreamSynchronize(ctx->st));
     cudaEventElapsedTime(&ctx->ms_search, ctx->ev0, ctx->ev1);
+    cudaEventElapsedTime(&ctx->ms_fast, ctx->evk0, ctx->evk1);
     ctx->num_edges = total;
     ctx->probes = hc[1];
     ctx->graph_ok = true;
@@ -547,6 +561,13 @@ int pq_get_stage_ms(pq_ctx* ctx, float* sort_ms, float* fm_ms, float* search_ms)
     if (sort_ms) *sort_ms = ctx->ms_sort;
     if (fm_ms) *fm_ms = ctx->ms_fm;
     if (search_ms) *search_ms = ctx->ms_search;
+    return PQ_OK;
+}
+
+int pq_get_kernel_stats(pq_ctx* ctx, float* search_kernel_ms, unsigned long long* launches) {
+    if (!ctx) return PQ_ERR_ARG;
+    if (search_kernel_ms) *search_kernel_ms = ctx->ms_fast;
+    if (launches) *launches = pq::launch_count();
     return PQ_OK;
 }
 

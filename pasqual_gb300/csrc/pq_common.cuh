@@ -52,6 +52,12 @@ struct FmView {
     idx_t Cf[5];              // Cf[0] = C[0]; Cf[c] = C[c] + fix[c]  (LF-mapping base)
 };
 
+namespace pq {
+// Count of kernels this library has launched (reported through pq_get_kernel_stats).
+void note_launch();
+unsigned long long launch_count();
+}  // namespace pq
+
 // Status codes returned through the C ABI.
 enum : int {
     PQ_OK = 0,

@@ -295,17 +295,17 @@ cudaError_t build_occ(const idx_t* sa, const uint8_t* reads, idx_t num_reads, id
     const size_t n = size_t(num_reads) * L;
     const size_t nblk = n / 64 + 1;
     const size_t nsb = (nblk + kBlocksPerSuper - 1) / kBlocksPerSuper;
-    k_bwt_blocks<<<grid_for(nblk * 32, 256), 256, 0, st>>>(sa, reads, idx_t(n), L, dir, idx_t(nblk), blk);
-    k_super_prefix<<<unsigned(nsb), 256, 0, st>>>(blk, idx_t(nblk), sb);
-    k_super_scan<<<1, 1024, 0, st>>>(sb, nsb);
-    k_reads_index<<<grid_for(nblk * 32, 256), 256, 0, st>>>(sa, blk, sb, idx_t(n), L, idx_t(nblk), reads_index);
+    { k_bwt_blocks<<<grid_for(nblk * 32, 256), 256, 0, st>>>(sa, reads, idx_t(n), L, dir, idx_t(nblk), blk); note_launch(); }
+    { k_super_prefix<<<unsigned(nsb), 256, 0, st>>>(blk, idx_t(nblk), sb); note_launch(); }
+    { k_super_scan<<<1, 1024, 0, st>>>(sb, nsb); note_launch(); }
+    { k_reads_index<<<grid_for(nblk * 32, 256), 256, 0, st>>>(sa, blk, sb, idx_t(n), L, idx_t(nblk), reads_index); note_launch(); }
     return cudaGetLastError();
 }
 
 cudaError_t read_counts(const uint8_t* reads, idx_t num_reads, idx_t L, unsigned long long* out12,
                         cudaStream_t st) {
     cudaMemsetAsync(out12, 0, 12 * sizeof(unsigned long long), st);
-    if (num_reads) k_read_counts<<<grid_for(num_reads, 256), 256, 0, st>>>(reads, num_reads, L, out12);
+    if (num_reads) { k_read_counts<<<grid_for(num_reads, 256), 256, 0, st>>>(reads, num_reads, L, out12); note_launch(); }
     return cudaGetLastError();
 }
 
@@ -313,11 +313,11 @@ cudaError_t build_kmer_table(const idx_t* sa, const uint8_t* reads, idx_t num_re
                              int k, uint32_t* code_tmp, idx_t* kstart, idx_t* kend, cudaStream_t st) {
     const size_t n = size_t(num_reads) * L;
     const size_t nk = size_t(1) << (2 * k);
-    k_fill_idx<<<grid_for(nk, 256), 256, 0, st>>>(kstart, nk, idx_t(1));
-    k_fill_idx<<<grid_for(nk, 256), 256, 0, st>>>(kend, nk, idx_t(0));
+    { k_fill_idx<<<grid_for(nk, 256), 256, 0, st>>>(kstart, nk, idx_t(1)); note_launch(); }
+    { k_fill_idx<<<grid_for(nk, 256), 256, 0, st>>>(kend, nk, idx_t(0)); note_launch(); }
     if (n) {
-        k_kmer_codes<<<grid_for(n, 256), 256, 0, st>>>(sa, reads, idx_t(n), L, dir, k, code_tmp);
-        k_kmer_bounds<<<grid_for(n, 256), 256, 0, st>>>(code_tmp, idx_t(n), kstart, kend);
+        { k_kmer_codes<<<grid_for(n, 256), 256, 0, st>>>(sa, reads, idx_t(n), L, dir, k, code_tmp); note_launch(); }
+        { k_kmer_bounds<<<grid_for(n, 256), 256, 0, st>>>(code_tmp, idx_t(n), kstart, kend); note_launch(); }
     }
     return cudaGetLastError();
 }
@@ -325,7 +325,7 @@ cudaError_t build_kmer_table(const idx_t* sa, const uint8_t* reads, idx_t num_re
 cudaError_t read_seeds(const uint8_t* reads, idx_t num_reads, int L, int dir, int k, const idx_t* kstart,
                        const idx_t* kend, idx_t* start, idx_t* size, cudaStream_t st) {
     if (num_reads)
-        k_read_seeds<<<grid_for(num_reads, 256), 256, 0, st>>>(reads, num_reads, L, dir, k, kstart, kend, start, size);
+        { k_read_seeds<<<grid_for(num_reads, 256), 256, 0, st>>>(reads, num_reads, L, dir, k, kstart, kend, start, size); note_launch(); }
     return cudaGetLastError();
 }
 
@@ -333,8 +333,8 @@ cudaError_t export_ref_layout(const OccBlock* blk, const idx_t* sb, idx_t num_re
                               const idx_t fix[4], uint64_t* bitmap, idx_t* sample, cudaStream_t st) {
     const size_t n = size_t(num_reads) * L;
     const size_t nblk = n / 64 + 1;
-    k_export_ref<<<grid_for(nblk, 256), 256, 0, st>>>(blk, sb, idx_t(n), idx_t(nblk), fix[0], fix[1],
-                                                      fix[2], fix[3], bitmap, sample);
+    { k_export_ref<<<grid_for(nblk, 256), 256, 0, st>>>(blk, sb, idx_t(n), idx_t(nblk), fix[0], fix[1],
+                                                      fix[2], fix[3], bitmap, sample); note_launch(); }
     return cudaGetLastError();
 }
 

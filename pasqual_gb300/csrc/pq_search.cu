@@ -430,7 +430,7 @@ cudaError_t search_fast(const SearchArgs& a, const SearchOut& o, int threads_per
     if (threads_per_block != 128) return cudaErrorInvalidValue;
     const int words = (a.L + 15) / 16;
     size_t smem = size_t(words) * threads_per_block * sizeof(uint32_t);
-    k_search_fast<<<blocks, threads_per_block, smem, st>>>(a, o);
+    { k_search_fast<<<blocks, threads_per_block, smem, st>>>(a, o); note_launch(); }
     return cudaGetLastError();
 }
 
@@ -490,7 +490,7 @@ cudaError_t search_wide(const SearchArgs& a, const SearchOut& o, const idx_t* li
     const int words = (a.L + 15) / 16;
     size_t smem = size_t(words) * tpb * sizeof(uint32_t);
     int blocks = (ws.slots + tpb - 1) / tpb;
-    k_search_wide<<<blocks, tpb, smem, st>>>(a, o, list, count, ws);
+    { k_search_wide<<<blocks, tpb, smem, st>>>(a, o, list, count, ws); note_launch(); }
     return cudaGetLastError();
 }
 
@@ -541,14 +541,14 @@ static void scan_u64(const unsigned long long* in, size_t n, unsigned long long*
     if (n == 0) return;
     size_t tiles = (n + 1023) / 1024;
     if (tiles == 1) {
-        k_scan_tiles<<<1, 1024, 0, st>>>(in, n, out, nullptr);
+        { k_scan_tiles<<<1, 1024, 0, st>>>(in, n, out, nullptr); note_launch(); }
         return;
     }
     unsigned long long* sums = tmp;
     unsigned long long* sums_scan = tmp + tiles;
-    k_scan_tiles<<<unsigned(tiles), 1024, 0, st>>>(in, n, out, sums);
+    { k_scan_tiles<<<unsigned(tiles), 1024, 0, st>>>(in, n, out, sums); note_launch(); }
     scan_u64(sums, tiles, sums_scan, tmp + 2 * tiles, st);
-    k_scan_add<<<unsigned(tiles), 1024, 0, st>>>(out, n, sums_scan);
+    { k_scan_add<<<unsigned(tiles), 1024, 0, st>>>(out, n, sums_scan); note_launch(); }
 }
 
 size_t assemble_tmp_bytes(idx_t num_reads) {
@@ -580,7 +580,7 @@ cudaError_t assemble_counts_total(const SearchOut& o, idx_t num_reads, unsigned 
     unsigned long long* tmp = cnt + n + 1;
     cudaMemsetAsync(cnt, 0, (n + 1) * sizeof(unsigned long long), st);
     unsigned g = unsigned(std::min<size_t>((n + 255) / 256 + 1, 152 * 32));
-    if (n) k_edge_counts<<<g, 256, 0, st>>>(o.num_B, o.num_F, idx_t(n), cnt);
+    if (n) { k_edge_counts<<<g, 256, 0, st>>>(o.num_B, o.num_F, idx_t(n), cnt); note_launch(); }
     scan_u64(cnt, n + 1, out_off, tmp, st);
     return cudaGetLastError();
 }
@@ -589,7 +589,7 @@ cudaError_t assemble_gather(const SearchOut& o, idx_t num_reads, const unsigned 
                             uint16_t* len, uint8_t* type, int32_t* trans, cudaStream_t st) {
     const size_t n = size_t(num_reads);
     unsigned g = unsigned(std::min<size_t>((n + 255) / 256 + 1, 152 * 32));
-    if (n) k_gather_edges<<<g, 256, 0, st>>>(o, idx_t(n), off, dest, len, type, trans);
+    if (n) { k_gather_edges<<<g, 256, 0, st>>>(o, idx_t(n), off, dest, len, type, trans); note_launch(); }
     return cudaGetLastError();
 }
 

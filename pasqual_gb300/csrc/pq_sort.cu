@@ -261,7 +261,7 @@ int radix_sort_pairs(uint64_t** k0, V** v0, uint64_t** k1, V** v1, size_t n, int
     unsigned long long* cnt = reinterpret_cast<unsigned long long*>(tmp);
     unsigned long long* gh = cnt + size_t(256) * RS_MAX_CTAS;
     cudaMemsetAsync(gh, 0, 8 * 256 * sizeof(unsigned long long), st);
-    k_digit_hist<<<grid_for(n, 256, 4), 256, 0, st>>>(*k0, n, gh);
+    { k_digit_hist<<<grid_for(n, 256, 4), 256, 0, st>>>(*k0, n, gh); note_launch(); }
     std::vector<unsigned long long> h(8 * 256);
     cudaMemcpyAsync(h.data(), gh, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
     cudaError_t e = cudaStreamSynchronize(st);
@@ -275,9 +275,9 @@ int radix_sort_pairs(uint64_t** k0, V** v0, uint64_t** k1, V** v1, size_t n, int
         for (int b = 0; b < 256; ++b)
             if (h[size_t(d) * 256 + b] == n) trivial = true;
         if (trivial) continue;
-        k_rs_upsweep<<<unsigned(ctas), RS_THREADS, 0, st>>>(*k0, n, 8 * d, part, cnt);
-        k_scan_small<<<1, 1024, 0, st>>>(cnt, 256 * ctas);
-        k_rs_downsweep<V><<<unsigned(ctas), RS_THREADS, 0, st>>>(*k0, *v0, *k1, *v1, n, 8 * d, part, cnt);
+        { k_rs_upsweep<<<unsigned(ctas), RS_THREADS, 0, st>>>(*k0, n, 8 * d, part, cnt); note_launch(); }
+        { k_scan_small<<<1, 1024, 0, st>>>(cnt, 256 * ctas); note_launch(); }
+        { k_rs_downsweep<V><<<unsigned(ctas), RS_THREADS, 0, st>>>(*k0, *v0, *k1, *v1, n, 8 * d, part, cnt); note_launch(); }
         std::swap(*k0, *k1);
         std::swap(*v0, *v1);
     }
@@ -450,27 +450,27 @@ int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa
     unsigned long long* tcnt = tmax + tiles + 1;
     unsigned long long* groups = tcnt + tiles + 1;
 
-    k_pack_text<<<grid_for(nwords, 256), 256, 0, st>>>(reads, n, idx_t(L), dir, nwords, pk);
-    k_init_keys<<<grid_for(n, 256), 256, 0, st>>>(pk, n, idx_t(L), ka, va);
+    { k_pack_text<<<grid_for(nwords, 256), 256, 0, st>>>(reads, n, idx_t(L), dir, nwords, pk); note_launch(); }
+    { k_init_keys<<<grid_for(n, 256), 256, 0, st>>>(pk, n, idx_t(L), ka, va); note_launch(); }
     int rc = radix_sort_pairs<idx_t>(&ka, &va, &kb, &vb, n, 0, 64, rtmp, radix_tmp_bytes(n), st);
     if (rc) return rc;
     for (size_t h = kHead;; h *= 2) {
-        k_head_tiles<<<unsigned(tiles), HT_THREADS, 0, st>>>(ka, n, tmax, tcnt);
-        k_head_carry<<<1, 1024, 0, st>>>(tmax, tcnt, tiles, groups);
-        k_head_apply<idx_t><<<unsigned(tiles), HT_THREADS, 0, st>>>(ka, kb, va, n, tmax, rank);
+        { k_head_tiles<<<unsigned(tiles), HT_THREADS, 0, st>>>(ka, n, tmax, tcnt); note_launch(); }
+        { k_head_carry<<<1, 1024, 0, st>>>(tmax, tcnt, tiles, groups); note_launch(); }
+        { k_head_apply<idx_t><<<unsigned(tiles), HT_THREADS, 0, st>>>(ka, kb, va, n, tmax, rank); note_launch(); }
         std::swap(ka, kb);
         unsigned long long g = 0;
         cudaMemcpyAsync(&g, groups, sizeof g, cudaMemcpyDeviceToHost, st);
         cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return int(e);
         if (g == n || h >= size_t(L)) break;
-        k_second_keys<idx_t><<<grid_for(n, 256), 256, 0, st>>>(ka, va, n, idx_t(L), h, rank);
+        { k_second_keys<idx_t><<<grid_for(n, 256), 256, 0, st>>>(ka, va, n, idx_t(L), h, rank); note_launch(); }
         int bits = 1;
         while ((size_t(1) << bits) <= n + 1) ++bits;
         rc = radix_sort_pairs<idx_t>(&ka, &va, &kb, &vb, n, 0, 32 + bits, rtmp, radix_tmp_bytes(n), st);
         if (rc) return rc;
     }
-    k_copy_vals<idx_t><<<grid_for(n, 256), 256, 0, st>>>(va, n, sa);
+    { k_copy_vals<idx_t><<<grid_for(n, 256), 256, 0, st>>>(va, n, sa); note_launch(); }
     return int(cudaGetLastError());
 }
 

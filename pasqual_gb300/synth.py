@@ -118,3 +118,37 @@ def make_workload(name: str, scale: float = 1.0, seed: int = 11):
     gen = genome(glen, w["gc"], w["repeat"], w["div"], w["lowc"], seed=seed)
     rd = reads_for_coverage(gen, w["L"], w["cov"], w["err"], seed=seed + 1)
     return gen, rd, w["L"], w["t"]
+
+
+def _hash_rows(codes: np.ndarray) -> np.ndarray:
+    """64-bit hash per row of base codes (splitmix-style mixing over 2-bit packed words)."""
+    n, L = codes.shape
+    h = np.full(n, np.uint64(0x9E3779B97F4A7C15), dtype=np.uint64)
+    m1, m2 = np.uint64(0xBF58476D1CE4E5B9), np.uint64(0x94D049BB133111EB)
+    for s in range(0, L, 32):
+        blk = codes[:, s:s + 32].astype(np.uint64) - np.uint64(1)
+        w = np.zeros(n, dtype=np.uint64)
+        for j in range(blk.shape[1]):
+            w = (w << np.uint64(2)) | blk[:, j]
+        w ^= np.uint64(blk.shape[1])
+        h ^= w
+        h ^= h >> np.uint64(30)
+        h *= m1
+        h ^= h >> np.uint64(27)
+        h *= m2
+        h ^= h >> np.uint64(31)
+    return h
+
+
+def dedup(rd: np.ndarray) -> np.ndarray:
+    """Keep the first read of every group of reads that are equal or reverse complements of each
+    other (the duplicates the reference's Bloom filter is there to drop, src/index.c:325-333,
+    without its false positives).  Order of first occurrence is kept."""
+    if rd.shape[0] == 0:
+        return rd
+    hf = _hash_rows(rd)
+    hr = _hash_rows(revcomp(rd))
+    key = np.minimum(hf, hr)
+    _, first = np.unique(key, return_index=True)
+    first.sort()
+    return np.ascontiguousarray(rd[first])
