@@ -69,15 +69,24 @@ def reads(g: np.ndarray, read_len: int, num_reads: int, error: float = 0.0,
     rng = np.random.default_rng(seed)
     G = g.shape[0]
     starts = rng.integers(0, G - read_len + 1, size=num_reads)
-    idx = starts[:, None] + np.arange(read_len)[None, :]
-    r = g[idx]
     rc = rng.random(num_reads) < 0.5
-    r[rc] = revcomp(r[rc])
-    if error > 0:
-        hit = rng.random(r.shape) < error
-        shift = rng.integers(1, 4, size=int(hit.sum())).astype(np.uint8)
-        r[hit] = ((r[hit] - 1 + shift) % 4) + 1
-    return np.ascontiguousarray(r, dtype=np.uint8)
+    r = np.empty((num_reads, read_len), dtype=np.uint8)
+    ar = np.arange(read_len)
+    chunk = 1 << 18
+    for s in range(0, num_reads, chunk):
+        e = min(num_reads, s + chunk)
+        blk = g[starts[s:e, None] + ar]
+        m = rc[s:e]
+        blk[m] = revcomp(blk[m])
+        r[s:e] = blk
+    if error > 0 and r.size:
+        # error positions: Binomial(total, error) distinct positions, uniform
+        k = int(rng.binomial(r.size, error))
+        pos = np.unique(rng.integers(0, r.size, size=k))
+        flat = r.reshape(-1)
+        shift = rng.integers(1, 4, size=pos.size).astype(np.uint8)
+        flat[pos] = ((flat[pos] - 1 + shift) % 4) + 1
+    return r
 
 
 def reads_for_coverage(g: np.ndarray, read_len: int, coverage: float, error: float = 0.0,
@@ -126,11 +135,11 @@ def _hash_rows(codes: np.ndarray) -> np.ndarray:
     h = np.full(n, np.uint64(0x9E3779B97F4A7C15), dtype=np.uint64)
     m1, m2 = np.uint64(0xBF58476D1CE4E5B9), np.uint64(0x94D049BB133111EB)
     for s in range(0, L, 32):
-        blk = codes[:, s:s + 32].astype(np.uint64) - np.uint64(1)
-        w = np.zeros(n, dtype=np.uint64)
-        for j in range(blk.shape[1]):
-            w = (w << np.uint64(2)) | blk[:, j]
-        w ^= np.uint64(blk.shape[1])
+        blk = codes[:, s:s + 32]
+        k = blk.shape[1]
+        pow4 = (np.uint64(4) ** np.arange(k - 1, -1, -1, dtype=np.uint64)).astype(np.uint64)
+        w = (blk.astype(np.uint64) - np.uint64(1)) @ pow4
+        w ^= np.uint64(k)
         h ^= w
         h ^= h >> np.uint64(30)
         h *= m1
