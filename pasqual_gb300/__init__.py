@@ -33,6 +33,10 @@ EXPORTS = ["pq_idx_bytes", "pq_create", "pq_destroy", "pq_last_error", "pq_set_r
            "pq_get_graph_sizes", "pq_get_graph", "pq_get_stage_ms", "pq_get_kernel_stats"]
 
 
+# The reference's own entry points served by the same library (include/pasqual_gb300_dropin.h).
+DROPIN_EXPORTS = ["construct_index", "construct_string_graph", "destroy_graph", "pq_import_fasta"]
+
+
 class PQError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__("%s: %s" % (PQ_ERRORS.get(code, "PQ_ERR_%d" % code), msg))

@@ -15,8 +15,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 ROOT = os.path.dirname(HERE)
-SOURCES = ["pq_index.cu", "pq_search.cu", "pq_sort.cu", "pq_api.cu"]
+SOURCES = ["pq_index.cu", "pq_search.cu", "pq_sort.cu", "pq_api.cu", "pq_dropin.cu"]
 HEADERS = ["pq_common.cuh", "pq_index.cuh", "pq_sort.cuh"]
+PUBLIC = ["pasqual_gb300.h", "pasqual_gb300_dropin.h"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden"]
@@ -35,7 +36,7 @@ def _stale(target: str, deps) -> bool:
 
 def build(widths=(32, 64), verbose: bool = False) -> None:
     os.makedirs(OUT, exist_ok=True)
-    hdrs = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(ROOT, "include", "pasqual_gb300.h")]
+    hdrs = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(ROOT, "include", h) for h in PUBLIC]
     jobs = []
     for w in widths:
         defs = ["-DPQ_IDX64"] if w == 64 else []

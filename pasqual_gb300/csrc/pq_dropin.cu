@@ -1,0 +1,416 @@
+// pq_dropin.cu — the reference's own entry points (construct_index, construct_string_graph,
+// destroy_graph; src/index.h:63-68, src/string_graph.h:139-142) served by the GPU library, with
+// the reference's struct layouts (include/pasqual_gb300_dropin.h).
+//
+// Host work that stays on the CPU is restated here in plain C-style code: the FASTA import with
+// its Bloom-filter de-duplication (src/index.c:145-405, src/bloom.c:18-135) -- sequential by
+// definition, because which read of a duplicate pair survives depends on input order -- and
+// the node_t construction of src/string_graph.c:832-1017.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <sys/time.h>
+#include <unordered_map>
+#include <mutex>
+#include <vector>
+#include <string>
+#include <algorithm>
+
+#include "pq_common.cuh"
+#include "../../include/pasqual_gb300.h"
+#include "../../include/pasqual_gb300_dropin.h"
+
+static_assert(sizeof(pq_index_type) == sizeof(idx_t), "index widths must agree");
+
+// The reference's main() prints total time minus this (src/test.c:417-419).
+extern "C" __attribute__((visibility("default"))) double time_importreads = 0.0;
+
+namespace {
+
+double now_ms() {
+    struct timeval tv;
+    gettimeofday(&tv, nullptr);
+    return tv.tv_sec * 1000.0 + tv.tv_usec / 1000.0;
+}
+
+[[noreturn]] void error_exit(const char* msg) {
+    // ERROR_EXIT (src/common.h:87-94): message on stderr, exit status 0
+    fprintf(stderr, "Error: ");
+    fprintf(stderr, "%s", msg);
+    fflush(stderr);
+    exit(0);
+}
+
+// ---------------------------------------------------------------- Bloom filter (src/bloom.c)
+// Five string hashes over the 1..4 base codes, in index-width arithmetic; a read is a duplicate
+// when all of its own hash bits are already set, or all bits of its reverse complement's hashes
+// are; otherwise its own bits are set.
+typedef pq_index_type (*hash_fn)(const char*, pq_index_type);
+
+pq_index_type h_shift_xor(const char* k, pq_index_type m) {
+    pq_index_type h = 0;
+    while (*k) h ^= (h << 5) + (h >> 2) + (unsigned char)*k++;
+    return h % m;
+}
+pq_index_type h_sdbm(const char* k, pq_index_type m) {
+    pq_index_type h = 0;
+    while (*k) h = (unsigned char)*k++ + (h << 6) + (h << 16) - h;
+    return h % m;
+}
+pq_index_type h_sum(const char* k, pq_index_type m) {
+    pq_index_type h = 0;
+    while (*k) h += *k++;
+    return h % m;
+}
+pq_index_type h_xor(const char* k, pq_index_type m) {
+    pq_index_type h = 0;
+    while (*k) h ^= *k++;
+    return h % m;
+}
+pq_index_type h_times33(const char* k, pq_index_type m) {
+    pq_index_type h = 0;
+    while (*k) h = 33 * h + *k++;
+    return h % m;
+}
+const hash_fn kHashes[5] = {h_shift_xor, h_sdbm, h_sum, h_xor, h_times33};
+
+inline bool bit_get(const unsigned char* a, pq_index_type n) { return (a[n / 8] >> (n % 8)) & 1; }
+inline void bit_set(unsigned char* a, pq_index_type n) { a[n / 8] |= (unsigned char)(1u << (n % 8)); }
+
+// returns true when the read is a duplicate (src/bloom.c:91-135)
+bool bloom_seen(unsigned char* bits, pq_index_type m, int nfunc, const char* fw, const char* rc) {
+    pq_index_type hv[5];
+    bool all = true;
+    for (int i = 0; i < nfunc; ++i) {
+        hv[i] = kHashes[i](fw, m);
+        if (!bit_get(bits, hv[i])) all = false;
+    }
+    if (all) return true;
+    for (int i = 0; i < nfunc; ++i) {
+        if (!bit_get(bits, kHashes[i](rc, m))) {
+            for (int j = 0; j < nfunc; ++j) bit_set(bits, hv[j]);
+            return false;
+        }
+    }
+    return true;
+}
+
+std::string g_import_err;
+
+// ---------------------------------------------------------------- registry of GPU contexts
+std::mutex g_mu;
+std::unordered_map<const void*, pq_ctx*> g_ctx;
+
+// 1-3 base prefix rank with end-of-read lowest (the order of the reference's 85 "triplet"
+// codes): rank of the string s (|s| = 1..3) among all strings of length 1..3, 1-based.
+int prefix_rank(const int* s, int len) {
+    // enumerate strings in lexicographic order with shorter-prefix-first; rank = position
+    int r = 0;
+    // strings before s: for each position i, strings that share s[0..i) and then either end
+    // (counted once when i > 0 ... handled by ordering) or continue with a smaller base.
+    // Direct count: order is depth-first over the 4-ary tree of depth 3, a node before its
+    // children.
+    int sub[4] = {0, 21, 5, 1};   // size of the subtree below a node at depth d (incl. itself)
+    for (int i = 0; i < len; ++i) {
+        r += s[i] * sub[i + 1];    // whole subtrees of smaller siblings
+        r += 1;                    // the node itself (prefix s[0..i]) comes before its children
+    }
+    return r;                      // 1..84
+}
+
+}  // namespace
+
+extern "C" {
+
+int pq_import_fasta(const char* path, int read_len, int bloom_m, int n_hashfunc, uint8_t** reads_out,
+                    pq_index_type* num_reads_out, pq_index_type* removed_out, const char** err) {
+    char line[1000];
+    char msg[512];
+    auto bad = [&](pq_index_type kept) {
+        snprintf(msg, sizeof msg, "incorrect reads file at line %llu.\n", (unsigned long long)(kept * 2 + 2));
+        g_import_err = msg;
+        if (err) *err = g_import_err.c_str();
+        return PQ_ERR_ARG;
+    };
+    FILE* fp = fopen(path, "r");
+    if (!fp) {
+        snprintf(msg, sizeof msg, "open reads file %s failed.\n", path);
+        g_import_err = msg;
+        if (err) *err = g_import_err.c_str();
+        return PQ_ERR_ARG;
+    }
+    pq_index_type records = 0;
+    while (fgets(line, 1000, fp))
+        if (line[0] == '>') records++;
+    const pq_index_type m = records * (pq_index_type)bloom_m;
+    std::vector<unsigned char> bits((size_t(m) + 7) / 8 + 1, 0);
+    std::vector<uint8_t> out;
+    out.reserve(size_t(records) * read_len);
+    std::vector<char> fw(read_len + 1), rc(read_len + 1);
+    pq_index_type kept = 0, removed = 0;
+    fseek(fp, 0, SEEK_SET);
+    while (fgets(line, 1000, fp)) {
+        if (line[0] != '>') { fclose(fp); return bad(kept); }
+        if (!fgets(line, 1000, fp)) { fclose(fp); return bad(kept); }
+        line[strlen(line) - 1] = '\0';
+        if ((int)strlen(line) != read_len) { fclose(fp); return bad(kept); }
+        bool with_n = false;
+        for (int i = 0; i < read_len; ++i) {
+            int c, r;
+            switch (line[i]) {
+                case 'a': case 'A': c = 1; r = 4; break;
+                case 'c': case 'C': c = 2; r = 3; break;
+                case 'g': case 'G': c = 3; r = 2; break;
+                case 't': case 'T': c = 4; r = 1; break;
+                case 'n': case 'N': with_n = true; c = 'N'; r = 0; break;
+                default: fclose(fp); return bad(kept);
+            }
+            fw[i] = (char)c;
+            rc[read_len - 1 - i] = (char)r;
+        }
+        fw[read_len] = 0;
+        rc[read_len] = 0;
+        if (with_n || bloom_seen(bits.data(), m, n_hashfunc, fw.data(), rc.data())) {
+            removed++;
+            continue;
+        }
+        out.insert(out.end(), fw.begin(), fw.begin() + read_len);
+        kept++;
+    }
+    fclose(fp);
+    uint8_t* buf = (uint8_t*)malloc(out.size() ? out.size() : 1);
+    if (!buf) return PQ_ERR_NOMEM;
+    if (!out.empty()) memcpy(buf, out.data(), out.size());
+    *reads_out = buf;
+    *num_reads_out = kept;
+    if (removed_out) *removed_out = removed;
+    return PQ_OK;
+}
+
+pq_index_t* construct_index(char* single_file, char* pair_file1, char* pair_file2, char* mate_file1,
+                            char* mate_file2, int min_overlap, int read_len, int bloom_m, int n_hashfunc) {
+    pq_index_t* ix = (pq_index_t*)calloc(1, sizeof(pq_index_t));
+    if (!ix) error_exit("out of memory.\n");
+    ix->min_overlap = (uint16_t)min_overlap;
+    ix->read_len = (uint16_t)read_len;
+    ix->bloom_size = (pq_index_type)bloom_m;
+    ix->n_hashfunc = n_hashfunc;
+
+    if (single_file) {
+        double t0 = now_ms();
+        printf("Importing reads from %s ... ", single_file);
+        fflush(stdout);
+        uint8_t* reads = nullptr;
+        pq_index_type nr = 0, removed = 0;
+        const char* err = nullptr;
+        int rc = pq_import_fasta(single_file, read_len, bloom_m, n_hashfunc, &reads, &nr, &removed, &err);
+        if (rc) error_exit(err ? err : "import failed.\n");
+        ix->reads = (char*)reads;
+        ix->num_reads = nr;
+        ix->bloom_size = nr + removed == 0 ? 0 : (nr + removed) * (pq_index_type)bloom_m;
+        printf("done\n");
+        printf("  has imported %llu reads (removed %llu duplicate reads)\n", (unsigned long long)nr,
+               (unsigned long long)removed);
+        time_importreads = now_ms() - t0;
+        printf("  takes %.3lf ms\n", time_importreads);
+        fflush(stdout);
+    } else if (pair_file1 && pair_file2) {
+        error_exit("We do not support paired end reads.\nPlease input them as single reads.\n");
+    } else if (mate_file1 && mate_file2) {
+        error_exit("We do not support mate pair reads.\nPlease input them as single reads.\n");
+    }
+
+    pq_ctx* ctx = nullptr;
+    if (pq_create(&ctx, 0, nullptr) != PQ_OK) error_exit("no usable CUDA device.\n");
+    auto ck = [&](int rc) {
+        if (rc != PQ_OK) {
+            std::string m = std::string(pq_last_error(ctx)) + "\n";
+            error_exit(m.c_str());
+        }
+    };
+    ck(pq_set_reads(ctx, (const uint8_t*)ix->reads, ix->num_reads, read_len, min_overlap, 0));
+    ck(pq_get_counts(ctx, ix->C, ix->suffix_count, ix->prefix_count));
+    const size_t nr = ix->num_reads, n = nr * size_t(read_len), rowlen = n / 64 + 1;
+    for (int dir = 0; dir < 2; ++dir) {
+        double t0 = now_ms();
+        printf(dir ? "Sorting backward suffixes ... " : "Sorting forward suffixes ... ");
+        fflush(stdout);
+        ck(pq_sort(ctx, dir));
+        ck(pq_build_fm(ctx, dir));
+        std::vector<uint64_t> bm(rowlen * 5);
+        pq_index_type* sample = (pq_index_type*)malloc(rowlen * 5 * sizeof(pq_index_type));
+        pq_index_type* ri = (pq_index_type*)malloc((nr ? nr : 1) * sizeof(pq_index_type));
+        pq_index_type* ss = (pq_index_type*)malloc((nr ? nr : 1) * sizeof(pq_index_type));
+        pq_index_type* sz = (pq_index_type*)malloc((nr ? nr : 1) * sizeof(pq_index_type));
+        uint16_t* sd = (uint16_t*)malloc((nr ? nr : 1) * sizeof(uint16_t));
+        if (!sample || !ri || !ss || !sz || !sd) error_exit("out of memory.\n");
+        ck(pq_get_index_ref(ctx, dir, bm.data(), sample, ri));
+        ck(pq_get_seeds(ctx, dir, ss, sz, sd));
+        uint64_t** dst = dir ? ix->OCC_bitmap_bw : ix->OCC_bitmap;
+        for (int c = 0; c < 5; ++c) {
+            dst[c] = (uint64_t*)malloc(rowlen * sizeof(uint64_t));
+            if (!dst[c]) error_exit("out of memory.\n");
+            memcpy(dst[c], bm.data() + size_t(c) * rowlen, rowlen * sizeof(uint64_t));
+        }
+        // sort-slot sizes (src/sufsort.c:386-450): 5 slots of 17 first-prefix ranks
+        pq_index_type hist[85] = {0};
+        for (size_t r = 0; r < nr; ++r) {
+            const uint8_t* s = (const uint8_t*)ix->reads + r * read_len;
+            for (int j = 0; j < read_len; ++j) {
+                int q[3], len = std::min(3, read_len - j);
+                for (int a = 0; a < len; ++a) q[a] = (dir ? s[read_len - 1 - (j + a)] : s[j + a]) - 1;
+                hist[prefix_rank(q, len)]++;
+            }
+        }
+        pq_index_type* size = dir ? ix->size_bw : ix->size_fw;
+        pq_index_type* off = dir ? ix->offset_bw : ix->offset_fw;
+        pq_index_type mx = 0;
+        for (int k = 0; k < 5; ++k) {
+            size[k] = 0;
+            for (int j = 0; j < 17; ++j) size[k] += hist[k * 17 + j];
+            off[k] = k ? off[k - 1] + size[k - 1] : 0;
+            mx = std::max(mx, size[k]);
+        }
+        if (dir) {
+            ix->OCC_sample_bw = sample;
+            ix->reads_index_bw = ri;
+            ix->interval_start_bw = ss;
+            ix->interval_end_bw = sz;
+            ix->interval_depth_bw = sd;
+            ix->max_size_bw = mx;
+        } else {
+            ix->OCC_sample = sample;
+            ix->reads_index = ri;
+            ix->interval_start = ss;
+            ix->interval_end = sz;
+            ix->interval_depth = sd;
+            ix->max_size_fw = mx;
+        }
+        printf("done\n");
+        printf("  takes %.3lf ms\n", now_ms() - t0);
+        fflush(stdout);
+    }
+    {
+        std::lock_guard<std::mutex> g(g_mu);
+        auto it = g_ctx.find(ix);
+        if (it != g_ctx.end()) pq_destroy(it->second);
+        g_ctx[ix] = ctx;
+    }
+    return ix;
+}
+
+pq_string_graph_t* construct_string_graph(pq_index_t* ix) {
+    double t0 = now_ms();
+    printf("Building overlap graph ... ");
+    fflush(stdout);
+    pq_ctx* ctx = nullptr;
+    {
+        std::lock_guard<std::mutex> g(g_mu);
+        auto it = g_ctx.find(ix);
+        if (it != g_ctx.end()) {
+            ctx = it->second;
+            g_ctx.erase(it);
+        }
+    }
+    auto ck = [&](int rc) {
+        if (rc != PQ_OK) {
+            if (rc == PQ_ERR_TOO_MANY_EDGES) error_exit("assembly failed. Try a larger min overlap length.\n");
+            std::string m = std::string(pq_last_error(ctx)) + "\n";
+            error_exit(m.c_str());
+        }
+    };
+    if (!ctx) {   // index built elsewhere: rebuild the device index from its reads
+        if (pq_create(&ctx, 0, nullptr) != PQ_OK) error_exit("no usable CUDA device.\n");
+        ck(pq_set_reads(ctx, (const uint8_t*)ix->reads, ix->num_reads, ix->read_len, ix->min_overlap, 0));
+        ck(pq_build_index(ctx));
+    }
+    ck(pq_overlaps(ctx));
+    uint64_t ne = 0;
+    ck(pq_get_graph_sizes(ctx, &ne, nullptr, nullptr));
+    const size_t nr = ix->num_reads;
+    std::vector<uint16_t> nB(nr + 1), nF(nr + 1);
+    std::vector<int32_t> oB(nr + 1), oF(nr + 1), trans(ne + 1);
+    std::vector<uint64_t> off(nr + 1);
+    std::vector<pq_index_type> dest(ne + 1);
+    std::vector<uint16_t> len(ne + 1);
+    std::vector<uint8_t> type(ne + 1);
+    ck(pq_get_graph(ctx, nB.data(), nF.data(), oB.data(), oF.data(), off.data(), dest.data(), len.data(), type.data(),
+                    trans.data()));
+    pq_destroy(ctx);
+
+    pq_string_graph_t* g = (pq_string_graph_t*)malloc(sizeof(pq_string_graph_t));
+    if (!g) error_exit("out of memory.\n");
+    g->nodes = (pq_node_t*)calloc(nr ? nr : 1, sizeof(pq_node_t));
+    if (!g->nodes) error_exit("out of memory.\n");
+    g->num_reads = ix->num_reads;
+    g->read_len = ix->read_len;
+    g->min_overlap = ix->min_overlap;
+    const int L = ix->read_len;
+    const char ONE = 1, BRANCH = 2, ENDING = 4, REMOVED = 8, SUSPECT = 4, NONE = 0;
+    const char BB = 3, FB = 1;
+    pq_index_type run_max_F = 0, run_max_B = 0;   // I_F[1].uu / I_B[1].uu of one thread
+    double overlap_len = 0;
+    pq_index_type overlaps = 0;
+    for (size_t i = 0; i < nr; ++i) {
+        pq_node_t* nd = &g->nodes[i];
+        const int b = nB[i], f = nF[i];
+        const uint64_t e0 = off[i];
+        for (int j = 0; j < b; ++j) run_max_B = std::max(run_max_B, (pq_index_type)trans[e0 + j]);
+        for (int j = 0; j < f; ++j) run_max_F = std::max(run_max_F, (pq_index_type)trans[e0 + b + j]);
+        nd->max_B = nd->num_B = (uint16_t)b;
+        nd->max_F = nd->num_F = (uint16_t)f;
+        nd->status = 0;
+        nd->path_q = nullptr;
+        nd->edges = (pq_edge_t*)malloc((size_t(b) + f) * sizeof(pq_edge_t));
+        const int ob = oB[i], of = oF[i];
+        const int mx = std::max(ob, of);
+        double ratio = mx == 0 ? 0 : ((double)abs(ob - of)) / mx;
+        nd->marked = ratio > 0.6 ? SUSPECT : 0;
+        if (b || f) {
+            nd->B_type = b == 1 ? ONE : (b > 1 ? BRANCH : ENDING);
+            nd->F_type = f == 1 ? ONE : (f > 1 ? BRANCH : ENDING);
+        } else {
+            nd->B_type = nd->F_type = ENDING;
+            nd->status = REMOVED;
+        }
+        int olen = 0;
+        for (int j = 0; j < b + f; ++j) {
+            nd->edges[j].dest = dest[e0 + j];
+            nd->edges[j].overlap_len = len[e0 + j];
+            nd->edges[j].type = (char)type[e0 + j];
+            olen += len[e0 + j];
+        }
+        if ((nd->B_type == BRANCH && nd->F_type != ENDING) || (nd->F_type == BRANCH && nd->B_type != ENDING)) {
+            pq_path_q_t* q = (pq_path_q_t*)malloc(sizeof(pq_path_q_t));
+            q->max_B_endlen = q->max_F_endlen = q->max_B_len = q->max_F_len = 0;
+            q->path = (pq_path_t*)malloc(sizeof(pq_path_t) * (size_t(b) + f));
+            q->max_F_trans = (int)run_max_F;
+            q->max_B_trans = (int)run_max_B;
+            for (int j = 0; j < b + f; ++j) {
+                pq_path_t* p = &q->path[j];
+                const pq_edge_t* e = &nd->edges[j];
+                p->end = e->dest;
+                p->hop = e->dest;
+                p->len = 1;
+                p->end_len = (uint16_t)(L - e->overlap_len);
+                p->bubble_len = 0;
+                p->type = NONE;
+                p->updated = 0;
+                p->direction = j < b ? (e->type == BB ? 1 : 0) : (e->type == FB ? 1 : 0);
+                p->trans = trans[e0 + j];
+            }
+            nd->path_q = q;
+        }
+        overlaps += (pq_index_type)(b + f);
+        overlap_len += (double)olen;
+    }
+    printf("  takes %.3lf ms\n", now_ms() - t0);
+    g->average_overlap = overlap_len / overlaps;
+    printf("  average overlap length: %lf\n", g->average_overlap);
+    fflush(stdout);
+    return g;
+}
+
+void destroy_graph(pq_string_graph_t* graph) { (void)graph; }
+
+}  // extern "C"

@@ -76,8 +76,50 @@ def make(name: str, tmp: str) -> None:
     print("%-24s reads=%-6d edges=%-7d" % (name, d["reads"].shape[0], len(d["dest"])))
 
 
+IMPORT_FASTA = "import_L60.fa.gz"
+
+
+def make_import(tmp: str) -> None:
+    """FASTA import + Bloom de-duplication: exact duplicates, reverse-complement duplicates,
+    reads with N, lowercase bases; kept reads of both index widths (their Bloom hashes wrap in
+    the index width, so the kept sets can differ)."""
+    import gzip
+    rng = np.random.default_rng(7)
+    g = synth.genome(30000, 0.5, seed=77)
+    rd = synth.reads(g, 60, 6000, 0.01, seed=78)
+    seqs = [bytes(synth.ACGT[r]) for r in rd]
+    extra = []
+    for i in rng.choice(len(seqs), 400, replace=False):
+        extra.append(seqs[i])                                        # exact duplicate
+    for i in rng.choice(len(seqs), 400, replace=False):
+        extra.append(bytes(synth.ACGT[synth.revcomp(rd[i])]))       # reverse complement
+    for i in rng.choice(len(seqs), 100, replace=False):
+        s = bytearray(seqs[i]); s[int(rng.integers(0, 60))] = ord("N"); extra.append(bytes(s))
+    for i in rng.choice(len(seqs), 100, replace=False):
+        extra.append(seqs[i].lower())                                # lowercase duplicate
+    allseq = seqs + extra
+    order = rng.permutation(len(allseq))
+    text = b"".join(b">q%d\n%s\n" % (k, allseq[j]) for k, j in enumerate(order))
+    with gzip.open(os.path.join(HERE, IMPORT_FASTA), "wb") as f:
+        f.write(text)
+    fa = os.path.join(tmp, "import.fa")
+    with open(fa, "wb") as f:
+        f.write(text)
+    out = {"records": np.int64(len(allseq))}
+    for width in (32, 64):
+        d = port.run_ref_dump(fa, 60, 31, os.path.join(tmp, "imp%d" % width), width=width)
+        out["kept%d" % width] = np.int64(d["reads"].shape[0])
+        out["sha_reads%d" % width] = np.array(digest(d["reads"]))
+    np.savez_compressed(os.path.join(HERE, "import_L60.npz"), **out)
+    print("import: records=%d kept u32=%d u64=%d" % (len(allseq), out["kept32"], out["kept64"]))
+
+
 if __name__ == "__main__":
     port.build(ref=True)
     with tempfile.TemporaryDirectory() as tmp:
-        for name in (sys.argv[1:] or CASES):
-            make(name, tmp)
+        names = sys.argv[1:] or list(CASES) + ["import"]
+        for name in names:
+            if name == "import":
+                make_import(tmp)
+            else:
+                make(name, tmp)

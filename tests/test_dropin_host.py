@@ -1,0 +1,125 @@
+"""Host side of the drop-in layer (no GPU needed): the FASTA import with Bloom de-duplication
+against the reference's kept reads, and the struct layouts against the reference's headers."""
+import ctypes as ct
+import gzip
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, ROOT, sha
+import pasqual_gb300 as pq
+from pasqual_gb300 import build
+
+REF_SRC = "/root/reference/src"
+
+
+@pytest.fixture(scope="module")
+def fasta(tmp_path_factory):
+    build.build()
+    p = tmp_path_factory.mktemp("imp") / "import.fa"
+    with gzip.open(os.path.join(GOLDEN, "import_L60.fa.gz"), "rb") as f:
+        p.write_bytes(f.read())
+    return str(p)
+
+
+def import_fasta(width, path, L, bloom_m=36, nfunc=2):
+    lib = pq.load_library(width)
+    I = ct.c_uint64 if width == 64 else ct.c_uint32
+    f = lib.pq_import_fasta
+    f.restype = ct.c_int
+    f.argtypes = [ct.c_char_p, ct.c_int, ct.c_int, ct.c_int, ct.POINTER(ct.c_void_p),
+                  ct.POINTER(I), ct.POINTER(I), ct.POINTER(ct.c_char_p)]
+    buf, nr, rem, err = ct.c_void_p(), I(), I(), ct.c_char_p()
+    rc = f(path.encode(), L, bloom_m, nfunc, ct.byref(buf), ct.byref(nr), ct.byref(rem),
+           ct.byref(err))
+    if rc != 0:
+        return rc, err.value.decode(), None, None
+    n = nr.value * L
+    arr = np.ctypeslib.as_array(ct.cast(buf, ct.POINTER(ct.c_uint8)), shape=(max(n, 1),))[:n]
+    out = arr.copy().reshape(nr.value, L)
+    ct.CDLL(None).free(buf)
+    return 0, None, out, rem.value
+
+
+@pytest.mark.parametrize("width", [32, 64])
+def test_import_matches_reference(fasta, width):
+    z = np.load(os.path.join(GOLDEN, "import_L60.npz"))
+    rc, err, reads, removed = import_fasta(width, fasta, 60)
+    assert rc == 0, err
+    assert reads.shape[0] == int(z["kept%d" % width])
+    assert removed == int(z["records"]) - int(z["kept%d" % width])
+    assert sha(reads) == str(z["sha_reads%d" % width])
+
+
+def test_import_errors(tmp_path):
+    build.build()
+    bad = tmp_path / "bad.fa"
+    bad.write_bytes(b">a\nACGT\n>b\nACGX\n")
+    rc, err, _, _ = import_fasta(32, str(bad), 4)
+    assert rc == 1 and "incorrect reads file at line" in err
+    short = tmp_path / "short.fa"
+    short.write_bytes(b">a\nACGT\n>b\nACG\n")
+    rc, err, _, _ = import_fasta(32, str(short), 4)
+    assert rc == 1 and "incorrect reads file" in err
+    rc, err, _, _ = import_fasta(32, str(tmp_path / "missing.fa"), 4)
+    assert rc == 1 and "open reads file" in err
+
+
+LAYOUT_PROG = r"""
+#include <stdio.h>
+#include <stddef.h>
+#include HDR
+#define F(T, f) printf(#T "." #f " %zu %zu\n", offsetof(T, f), sizeof(((T*)0)->f))
+int main(void) {
+  printf("index_t %zu\n", sizeof(IX)); printf("node_t %zu\n", sizeof(ND));
+  printf("edge_t %zu\n", sizeof(ED)); printf("path_t %zu\n", sizeof(PT));
+  printf("path_q_t %zu\n", sizeof(PQ)); printf("string_graph_t %zu\n", sizeof(SG));
+  F(IX, bloom_array); F(IX, bloom_size); F(IX, n_hashfunc); F(IX, C); F(IX, suffix_count);
+  F(IX, prefix_count); F(IX, OCC_bitmap); F(IX, OCC_bitmap_bw); F(IX, OCC_sample);
+  F(IX, OCC_sample_bw); F(IX, reads_index); F(IX, reads_index_bw); F(IX, interval_start);
+  F(IX, interval_end); F(IX, interval_depth); F(IX, interval_start_bw); F(IX, interval_end_bw);
+  F(IX, interval_depth_bw); F(IX, read_lock); F(IX, reads); F(IX, read_len); F(IX, num_reads);
+  F(IX, min_overlap); F(IX, size_bw); F(IX, offset_bw); F(IX, size_fw); F(IX, offset_fw);
+  F(IX, max_size_fw); F(IX, max_size_bw);
+  F(ND, edges); F(ND, path_q); F(ND, num_F); F(ND, num_B); F(ND, max_F); F(ND, max_B);
+  F(ND, B_type); F(ND, F_type); F(ND, status); F(ND, marked);
+  F(ED, dest); F(ED, overlap_len); F(ED, type);
+  F(PT, end); F(PT, hop); F(PT, len); F(PT, end_len); F(PT, bubble_len); F(PT, trans);
+  F(PT, updated); F(PT, direction); F(PT, type);
+  F(PQ, path); F(PQ, max_F_endlen); F(PQ, max_B_endlen); F(PQ, max_B_len); F(PQ, max_F_len);
+  F(PQ, max_F_trans); F(PQ, max_B_trans);
+  F(SG, read_len); F(SG, min_overlap); F(SG, average_overlap); F(SG, num_reads); F(SG, nodes);
+  return 0; }
+"""
+
+
+def _layout(tmp_path, hdr, defs, names, incs, extra):
+    src = tmp_path / ("lay_%s.c" % names[0])
+    prog = LAYOUT_PROG.replace("IX", names[0]).replace("ND", names[1]).replace("ED", names[2]) \
+        .replace("PT", names[3]).replace("PQ", names[4]).replace("SG", names[5])
+    prog = prog.replace('#include HDR', "\n".join('#include "%s"' % h for h in hdr))
+    src.write_text(prog)
+    exe = tmp_path / ("lay_%s" % names[0])
+    subprocess.run(["gcc", "-std=gnu99", "-w"] + defs + ["-I" + i for i in incs] + extra +
+                   [str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout
+    # field names are the same in both; compare offsets and sizes line by line
+    return [" ".join([ln.split()[0].split(".")[-1]] + ln.split()[1:]) for ln in out.splitlines()]
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_SRC), reason="reference headers not present")
+@pytest.mark.parametrize("width", [32, 64])
+def test_struct_layout_matches_reference(tmp_path, width):
+    if shutil.which("gcc") is None:
+        pytest.skip("no gcc")
+    wdef = ["-D__INDEX_U64__"] if width == 64 else ["-D__INDEX_U32__"]
+    ref = _layout(tmp_path, ["index.h", "string_graph.h"], wdef + ["-D__OPENMP__"],
+                  ["index_t", "node_t", "edge_t", "path_t", "path_q_t", "string_graph_t"],
+                  [REF_SRC], ["-fopenmp"])
+    mine = _layout(tmp_path, ["pasqual_gb300_dropin.h"], ["-DPQ_IDX64"] if width == 64 else [],
+                   ["pq_index_t", "pq_node_t", "pq_edge_t", "pq_path_t", "pq_path_q_t",
+                    "pq_string_graph_t"], [os.path.join(ROOT, "include")], [])
+    assert ref == mine
