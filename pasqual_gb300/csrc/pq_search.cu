@@ -26,10 +26,13 @@ struct Cand {
     uint8_t type;
 };
 struct Frame {
-    uint32_t pos;
+    uint32_t pos;       // first candidate of this level
+    uint32_t cbase;     // first slot of the four extension sets
+    int32_t trans;      // sum of this level's interval sizes (path_t.trans of its edges)
     uint16_t size;
     uint16_t maxlen;
-    int32_t trans;
+    uint16_t P;         // slots per extension set
+    uint16_t csz[4];    // non-empty extensions by A, C, G, T
     uint8_t next_a;
 };
 struct EdgeRec {
@@ -187,55 +190,117 @@ struct ReadResult {
     int ne;
 };
 
-// One of the four candidate searches of find_intervals; appends to stk[*cnt...].
-__device__ __forceinline__ int candidate_search(const SearchArgs& A, const ReadView& rd, int kind, Cand* stk,
-                                                int cap, int& cnt, int32_t& olp, uint32_t& probes) {
-    const int L = A.L, t = A.t;
-    const int ia = (kind == PQ_FB || kind == PQ_BB) ? 0 : 1;   // index walked
-    const FmView& FA = A.fm[ia];
-    const FmView& FB_ = A.fm[1 - ia];
-    const bool strict = (kind == PQ_FB || kind == PQ_BF);
-    idx_t l, u, ll = 0, uu = 0;
-    int d;
-    // seed: exact SA interval of pat(k)..pat(1) from the k-mer table (k = 1 reproduces the
-    // reference's depth-1 start at C[c]; any exact interval of depth <= t is equivalent)
-    const int k = A.seed_k;
-    kmer_seed(FA, rd, L, kind, k, 1, -1, l, u, probes);
-    d = k;
-#define LIVE(l, u) (strict ? ((l) < (u)) : ((l) <= (u)))
-    while (LIVE(l, u) && d < t) {
-        lf_step(FA, pattern_at(rd, L, kind, d + 1), l, u, probes);
-        d++;
+__device__ __forceinline__ idx_t pick4(const idx_t r[4], int c) {   // r[c - 1] without local memory
+    return c == 1 ? r[0] : (c == 2 ? r[1] : (c == 3 ? r[2] : r[3]));
+}
+
+// search_2 from ranks already loaded at vl = l and vu = u + 1 (the same two blocks also give the
+// `$` count of search_3, so one pair of loads serves both).
+__device__ __forceinline__ void step_from_ranks(const FmView& f, int c, idx_t vl, idx_t vu, const idx_t rl[4],
+                                                const idx_t ru[4], idx_t& l, idx_t& u, idx_t& ll, idx_t& uu) {
+    idx_t gel = 0, geu = 0;
+    #pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (k + 1 >= c) { gel += rl[k]; geu += ru[k]; }
     }
-    if (LIVE(l, u)) {
-        // other index: pattern pat(1) pat(2) .. pat(d) (text order); seed with its last k bases
-        kmer_seed(FB_, rd, L, kind, d - k + 1, d, 1, ll, uu, probes);
-        for (int j = d - k; j >= 1; --j) lf_step(FB_, pattern_at(rd, L, kind, j), ll, uu, probes);
+    ll = ll + ((vu - geu) - (vl - gel));
+    const idx_t ol = pick4(rl, c), ou = pick4(ru, c);
+    const idx_t base = f.Cf[c];
+    l = base + ol;
+    u = base + ou - 1;
+    uu = ll + ou - ol - 1;
+}
+
+__device__ __forceinline__ bool live(int kind, idx_t l, idx_t u) {
+    return (kind == PQ_FB || kind == PQ_BF) ? (l < u) : (l <= u);   // src/string_graph.c:207 vs :251
+}
+__device__ __forceinline__ int walked_index(int kind) { return (kind == PQ_FB || kind == PQ_BB) ? 0 : 1; }
+
+// find_intervals for one side: kinds k0 then k1 (B-F and B-B, or F-B and F-F), searched in
+// lockstep so that each thread keeps two independent chains of loads in flight.
+//
+// The reference walks index A from its seed to depth t with search_1, then rebuilds the other
+// index's interval of the reversed pattern from depth 1 with another t-1 search_1 steps, and
+// only then continues with synchronised search_2 steps.  Here both intervals start from exact
+// k-mer seeds (one per index) and every step is a synchronised step, so the other interval is
+// known at every depth and the rebuild disappears; SA intervals are unique per string, so the
+// intervals at depth t -- and everything after -- are the reference's.  Candidates of kind k0
+// and k1 are collected in two regions of the stack and joined k0 first, the reference's order.
+__device__ __forceinline__ int side_candidates(const SearchArgs& A, const FmView* fm, const ReadView& rd, int k0,
+                                               int k1, Cand* stk, int cap, int& n_out, int32_t& olp,
+                                               uint32_t& probes) {
+    const int L = A.L, t = A.t, k = A.seed_k;
+    const int M = L - t;
+    if (2 * M > cap) return OVF_STACK;
+    idx_t l[2], u[2], ll[2], uu[2];
+    bool alive[2];
+    int n[2] = {0, 0};
+    #pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const int kind = q ? k1 : k0;
+        const int ia = walked_index(kind);
+        kmer_seed(fm[ia], rd, L, kind, k, 1, -1, l[q], u[q], probes);       // pat(k) .. pat(1)
+        kmer_seed(fm[1 - ia], rd, L, kind, 1, k, 1, ll[q], uu[q], probes);  // pat(1) .. pat(k)
+        alive[q] = live(kind, l[q], u[q]);
     }
-    while (LIVE(l, u) && d < L) {
-        if (kind != PQ_BB || d >= t) {
-            idx_t tmp = dollars_m1(FA, l, u, probes);
-            if (cnt >= cap) return OVF_STACK;
-            Cand& c = stk[cnt++];
-            c.ll = ll;
-            c.uu = ll + tmp;
+    int d = k;
+    while (d < t && (alive[0] || alive[1])) {
+        #pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            if (!alive[q]) continue;
+            const int kind = q ? k1 : k0;
+            const FmView& f = fm[walked_index(kind)];
+            const idx_t vl = l[q], vu = u[q] + 1;
+            idx_t rl[4], ru[4];
+            rank_all(f, vl, rl);
+            rank_all(f, vu, ru);
+            probes += 2;
+            step_from_ranks(f, pattern_at(rd, L, kind, d + 1), vl, vu, rl, ru, l[q], u[q], ll[q], uu[q]);
+            alive[q] = live(kind, l[q], u[q]);
+        }
+        ++d;
+    }
+    while (d < L && (alive[0] || alive[1])) {
+        #pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            if (!alive[q]) continue;
+            const int kind = q ? k1 : k0;
+            const FmView& f = fm[walked_index(kind)];
+            const idx_t vl = l[q], vu = u[q] + 1;
+            idx_t rl[4], ru[4];
+            rank_all(f, vl, rl);
+            rank_all(f, vu, ru);
+            probes += 2;
+            // (#$ in [l, u]) - 1, wrapping to all-ones when zero (the entry is kept, with
+            // remain 0 and uu = ll - 1, as `tmp >= 0` keeps it in src/string_graph.c:229)
+            const idx_t tmp = (vu - (ru[0] + ru[1] + ru[2] + ru[3])) - (vl - (rl[0] + rl[1] + rl[2] + rl[3])) - 1;
+            Cand& c = stk[q * M + n[q]++];
+            c.ll = ll[q];
+            c.uu = ll[q] + tmp;
             c.len = uint16_t(d);
             c.type = uint8_t(kind);
             c.remain = tmp + 1;
             olp = int32_t(uint32_t(olp) + uint32_t(tmp + 1));
+            step_from_ranks(f, pattern_at(rd, L, kind, d + 1), vl, vu, rl, ru, l[q], u[q], ll[q], uu[q]);
+            alive[q] = live(kind, l[q], u[q]);
         }
-        bi_step(FA, pattern_at(rd, L, kind, d + 1), l, u, ll, uu, probes);
-        d++;
+        ++d;
     }
-#undef LIVE
+    for (int i = 0; i < n[1]; ++i) stk[n[0] + i] = stk[M + i];
+    n_out = n[0] + n[1];
     return OVF_NONE;
 }
 
 __device__ __forceinline__ int cand_index(int type) { return (type == PQ_FB || type == PQ_BB) ? 1 : 0; }
 
-// extract_fw_edges / extract_bw_edges as an explicit DFS over stk[0, n0).
-__device__ __forceinline__ int reduce_side(const SearchArgs& A, idx_t self, Cand* stk, int cap, int n0,
-                                           Frame* fr, int frcap, EdgeRec* eb, int ebcap, int& ne,
+// extract_fw_edges / extract_bw_edges as an explicit DFS over stk[0, n0).  On entering a level the
+// emission check runs as in the reference; then all four extension sets are computed at once
+// from one pair of block loads per interval (the reference re-probes the same two blocks for
+// every base) and stored side by side; the DFS then descends into them in base order A, C, G, T.
+// Computing an extension the reference skips (its remaining-size counter reached zero) only
+// finds it empty, so the sets are the reference's.
+__device__ __forceinline__ int reduce_side(const SearchArgs& A, const FmView* fm, idx_t self, Cand* stk, int cap,
+                                           int n0, Frame* fr, int frcap, EdgeRec* eb, int ebcap, int& ne,
                                            int& side_count, uint32_t& probes) {
     const int L = A.L;
     int level = 0;
@@ -248,13 +313,12 @@ __device__ __forceinline__ int reduce_side(const SearchArgs& A, idx_t self, Cand
         Frame& F = fr[level];
         if (entering) {
             entering = false;
-            F.next_a = 1;
             if (int(F.maxlen) + level == L) {
                 bool flag = false;
                 for (int i = 0; i < F.size; ++i) {
                     const Cand& c = stk[F.pos + i];
                     if (int(c.len) + level != L) continue;
-                    const FmView& fo = A.fm[cand_index(c.type)];
+                    const FmView& fo = fm[cand_index(c.type)];
                     idx_t lll = fo.Cf[0] + rank_dollar(fo, c.ll);
                     idx_t uuu = fo.Cf[0] + rank_dollar(fo, c.uu + 1) - 1;
                     probes += 2;
@@ -282,69 +346,87 @@ __device__ __forceinline__ int reduce_side(const SearchArgs& A, idx_t self, Cand
                     continue;
                 }
             }
+            int P = 0;
+            for (int i = 0; i < F.size; ++i) P += stk[F.pos + i].remain != 0;
+            const uint32_t cbase = F.pos + F.size;
+            if (int(cbase) + 4 * P > cap) return OVF_STACK;
+            int cnt[4] = {0, 0, 0, 0};
+            for (int i = 0; i < F.size; ++i) {
+                const Cand c = stk[F.pos + i];
+                if (c.remain == 0) continue;
+                const int o = cand_index(c.type);
+                const FmView& f = fm[o];
+                idx_t rl[4], ru[4];
+                rank_all(f, c.ll, rl);
+                rank_all(f, c.uu + 1, ru);
+                probes += 2;
+                #pragma unroll
+                for (int a = 1; a <= 4; ++a) {
+                    const int ch = o == 0 ? complement(a) : a;
+                    const idx_t ol = pick4(rl, ch), ou = pick4(ru, ch);
+                    const idx_t l2 = f.Cf[ch] + ol, u2 = f.Cf[ch] + ou - 1;
+                    if (l2 <= u2) {
+                        Cand& x = stk[cbase + (a - 1) * P + cnt[a - 1]++];
+                        x.ll = l2;
+                        x.uu = u2;
+                        x.len = c.len;
+                        x.type = c.type;
+                        x.remain = u2 - l2 + 1;
+                    }
+                }
+            }
+            F.cbase = cbase;
+            F.P = uint16_t(P);
+            #pragma unroll
+            for (int a = 0; a < 4; ++a) F.csz[a] = uint16_t(cnt[a]);
+            F.next_a = 1;
         }
+        while (F.next_a <= 4 && F.csz[F.next_a - 1] == 0) F.next_a++;
         if (F.next_a > 4) {
             if (level == 0) return OVF_NONE;
             --level;
             continue;
         }
         const int a = F.next_a++;
-        const uint32_t cpos = F.pos + F.size;
-        int cnt = 0, maxl = 0;
-        uint32_t tr = 0;
-        for (int i = 0; i < F.size; ++i) {
-            Cand& c = stk[F.pos + i];
-            if (c.remain == 0) continue;
-            const int o = cand_index(c.type);
-            const int ch = o == 0 ? complement(a) : a;
-            idx_t l2 = c.ll, u2 = c.uu;
-            lf_step(A.fm[o], ch, l2, u2, probes);
-            c.remain = c.remain - (u2 - l2 + 1);
-            if (l2 <= u2) {
-                if (int(cpos) + cnt >= cap) return OVF_STACK;
-                Cand& ch_ = stk[cpos + cnt++];
-                ch_.ll = l2;
-                ch_.uu = u2;
-                ch_.len = c.len;
-                ch_.type = c.type;
-                ch_.remain = u2 - l2 + 1;
-                tr += uint32_t(u2 - l2 + 1);
-                if (maxl < c.len) maxl = c.len;
-            }
-        }
-        if (cnt == 0) continue;
         if (level + 1 >= frcap) return OVF_LEVELS;
-        ++level;
-        Frame& G = fr[level];
-        G.pos = cpos;
-        G.size = uint16_t(cnt);
+        Frame& G = fr[level + 1];
+        G.pos = F.cbase + uint32_t(a - 1) * F.P;
+        G.size = F.csz[a - 1];
+        int maxl = 0;
+        uint32_t tr = 0;
+        for (int i = 0; i < G.size; ++i) {
+            const Cand& c = stk[G.pos + i];
+            tr += uint32_t(c.remain);
+            maxl = max(maxl, int(c.len));
+        }
         G.maxlen = uint16_t(maxl);
         G.trans = int32_t(tr);
+        ++level;
         entering = true;
     }
 }
 
-__device__ __forceinline__ ReadResult search_read(const SearchArgs& A, idx_t self, const ReadView& rd, Cand* stk,
-                                                  int cap, Frame* fr, int frcap, EdgeRec* eb, int ebcap,
-                                                  uint32_t& probes) {
+__device__ __forceinline__ ReadResult search_read(const SearchArgs& A, const FmView* fm, idx_t self,
+                                                  const ReadView& rd, Cand* stk, int cap, Frame* fr, int frcap,
+                                                  EdgeRec* eb, int ebcap, uint32_t& probes) {
     ReadResult R;
     R.status = OVF_NONE;
     R.nB = R.nF = 0;
     R.olpB = R.olpF = 0;
     R.ne = 0;
     int n0 = 0, sc = 0;
-    // B side: B-F then B-B candidates, then extract_bw_edges
-    int s = candidate_search(A, rd, PQ_BF, stk, cap, n0, R.olpB, probes);
-    if (s == OVF_NONE) s = candidate_search(A, rd, PQ_BB, stk, cap, n0, R.olpB, probes);
-    if (s == OVF_NONE && R.olpB != 0) s = reduce_side(A, self, stk, cap, n0, fr, frcap, eb, ebcap, R.ne, sc, probes);
+    // B side: B-F then B-B candidates, then extract_bw_edges (src/string_graph.c:824-825)
+    int s = side_candidates(A, fm, rd, PQ_BF, PQ_BB, stk, cap, n0, R.olpB, probes);
+    if (s == OVF_NONE && R.olpB != 0)
+        s = reduce_side(A, fm, self, stk, cap, n0, fr, frcap, eb, ebcap, R.ne, sc, probes);
     if (s != OVF_NONE) { R.status = s; return R; }
     R.nB = sc;
-    // F side: F-B then F-F candidates, then extract_fw_edges
+    // F side: F-B then F-F candidates, then extract_fw_edges (src/string_graph.c:828-829)
     n0 = 0;
     sc = 0;
-    s = candidate_search(A, rd, PQ_FB, stk, cap, n0, R.olpF, probes);
-    if (s == OVF_NONE) s = candidate_search(A, rd, PQ_FF, stk, cap, n0, R.olpF, probes);
-    if (s == OVF_NONE && R.olpF != 0) s = reduce_side(A, self, stk, cap, n0, fr, frcap, eb, ebcap, R.ne, sc, probes);
+    s = side_candidates(A, fm, rd, PQ_FB, PQ_FF, stk, cap, n0, R.olpF, probes);
+    if (s == OVF_NONE && R.olpF != 0)
+        s = reduce_side(A, fm, self, stk, cap, n0, fr, frcap, eb, ebcap, R.ne, sc, probes);
     if (s != OVF_NONE) { R.status = s; return R; }
     R.nF = sc;
     return R;
@@ -408,6 +490,9 @@ constexpr int kFastEdges = 48;
 
 __global__ void __launch_bounds__(128) k_search_fast(SearchArgs A, SearchOut O) {
     extern __shared__ uint32_t s_reads[];
+    __shared__ FmView s_fm[2];
+    if (threadIdx.x < 2) s_fm[threadIdx.x] = A.fm[threadIdx.x];
+    __syncthreads();
     Cand stk[kFastCap];
     Frame fr[kFastFrames];
     EdgeRec eb[kFastEdges];
@@ -418,7 +503,8 @@ __global__ void __launch_bounds__(128) k_search_fast(SearchArgs A, SearchOut O) 
         if (r < A.num_reads) {
             load_read(A, idx_t(r), s_reads + threadIdx.x, blockDim.x);
             ReadView rd{s_reads + threadIdx.x, int(blockDim.x)};
-            ReadResult R = search_read(A, idx_t(r), rd, stk, kFastCap, fr, kFastFrames, eb, kFastEdges, probes);
+            ReadResult R = search_read(A, s_fm, idx_t(r), rd, stk, kFastCap, fr, kFastFrames, eb, kFastEdges,
+                                       probes);
             publish(O, idx_t(r), R, eb);
         }
     }
@@ -438,6 +524,9 @@ cudaError_t search_fast(const SearchArgs& a, const SearchOut& o, int threads_per
 __global__ void __launch_bounds__(64) k_search_wide(SearchArgs A, SearchOut O, const idx_t* list, unsigned count,
                                                     WideScratch W) {
     extern __shared__ uint32_t s_reads[];
+    __shared__ FmView s_fm[2];
+    if (threadIdx.x < 2) s_fm[threadIdx.x] = A.fm[threadIdx.x];
+    __syncthreads();
     const unsigned slot = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t probes = 0;
     if (slot < unsigned(W.slots)) {
@@ -448,8 +537,8 @@ __global__ void __launch_bounds__(64) k_search_wide(SearchArgs A, SearchOut O, c
             idx_t r = list[i];
             load_read(A, r, s_reads + threadIdx.x, blockDim.x);
             ReadView rd{s_reads + threadIdx.x, int(blockDim.x)};
-            ReadResult R = search_read(A, r, rd, stk, int(W.stack_cap), fr, int(W.frame_cap), eb, int(W.edge_cap),
-                                       probes);
+            ReadResult R = search_read(A, s_fm, r, rd, stk, int(W.stack_cap), fr, int(W.frame_cap), eb,
+                                       int(W.edge_cap), probes);
             if (R.status == OVF_STACK || R.status == OVF_LEVELS) R.status = ERR_CAP;
             if (R.status == ERR_CAP || R.status == ERR_TOO_MANY || R.status == OVF_EDGES) {
                 O.status[r] = uint8_t(R.status == OVF_EDGES ? ERR_CAP : R.status);
