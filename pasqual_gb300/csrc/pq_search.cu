@@ -27,6 +27,7 @@ struct Cand {
 };
 struct Frame {
     uint32_t pos;       // first candidate of this level
+    uint32_t free;      // first stack slot this level may use for its extension sets
     uint32_t cbase;     // first slot of the four extension sets
     int32_t trans;      // sum of this level's interval sizes (path_t.trans of its edges)
     uint16_t size;
@@ -305,6 +306,7 @@ __device__ __forceinline__ int reduce_side(const SearchArgs& A, const FmView* fm
     const int L = A.L;
     int level = 0;
     fr[0].pos = 0;
+    fr[0].free = uint32_t(n0);
     fr[0].size = uint16_t(n0);
     fr[0].maxlen = 0;
     fr[0].trans = 0;
@@ -348,7 +350,7 @@ __device__ __forceinline__ int reduce_side(const SearchArgs& A, const FmView* fm
             }
             int P = 0;
             for (int i = 0; i < F.size; ++i) P += stk[F.pos + i].remain != 0;
-            const uint32_t cbase = F.pos + F.size;
+            const uint32_t cbase = F.free;
             if (int(cbase) + 4 * P > cap) return OVF_STACK;
             int cnt[4] = {0, 0, 0, 0};
             for (int i = 0; i < F.size; ++i) {
@@ -391,6 +393,7 @@ __device__ __forceinline__ int reduce_side(const SearchArgs& A, const FmView* fm
         if (level + 1 >= frcap) return OVF_LEVELS;
         Frame& G = fr[level + 1];
         G.pos = F.cbase + uint32_t(a - 1) * F.P;
+        G.free = F.cbase + 4u * F.P;        // below it: the parent's four sets, still pending
         G.size = F.csz[a - 1];
         int maxl = 0;
         uint32_t tr = 0;
