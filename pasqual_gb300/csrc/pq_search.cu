@@ -20,19 +20,21 @@
 
 namespace pq {
 
+// One candidate interval (interval_t, src/string_graph.h:47-54).  Its remaining size is always
+// uu - ll + 1 here: zero-$ level-0 entries are not stored (see side_candidates) and no counter is
+// decremented, so the field is not kept.
 struct Cand {
-    idx_t ll, uu, remain;
+    idx_t ll, uu;
     uint16_t len;
     uint8_t type;
 };
 struct Frame {
     uint32_t pos;       // first candidate of this level
     uint32_t free;      // first stack slot this level may use for its extension sets
-    uint32_t cbase;     // first slot of the four extension sets
+    uint32_t cbase;     // first slot of the four extension sets (stored back to back, A..T)
     int32_t trans;      // sum of this level's interval sizes (path_t.trans of its edges)
     uint16_t size;
     uint16_t maxlen;
-    uint16_t P;         // slots per extension set
     uint16_t csz[4];    // non-empty extensions by A, C, G, T
     uint8_t next_a;
 };
@@ -272,15 +274,18 @@ __device__ __forceinline__ int side_candidates(const SearchArgs& A, const FmView
             rank_all(f, vl, rl);
             rank_all(f, vu, ru);
             probes += 2;
-            // (#$ in [l, u]) - 1, wrapping to all-ones when zero (the entry is kept, with
-            // remain 0 and uu = ll - 1, as `tmp >= 0` keeps it in src/string_graph.c:229)
+            // (#$ in [l, u]) - 1.  The reference also appends the zero-$ case (`tmp >= 0` is
+            // always true, src/string_graph.c:229) with remaining size 0; such an entry is never
+            // extended, and level 0 never runs the emission check (its max length plus level 0
+            // cannot reach L), so it can never contribute and is not stored.
             const idx_t tmp = (vu - (ru[0] + ru[1] + ru[2] + ru[3])) - (vl - (rl[0] + rl[1] + rl[2] + rl[3])) - 1;
-            Cand& c = stk[q * M + n[q]++];
-            c.ll = ll[q];
-            c.uu = ll[q] + tmp;
-            c.len = uint16_t(d);
-            c.type = uint8_t(kind);
-            c.remain = tmp + 1;
+            if (tmp + 1 != 0) {
+                Cand& c = stk[q * M + n[q]++];
+                c.ll = ll[q];
+                c.uu = ll[q] + tmp;
+                c.len = uint16_t(d);
+                c.type = uint8_t(kind);
+            }
             olp = int32_t(uint32_t(olp) + uint32_t(tmp + 1));
             step_from_ranks(f, pattern_at(rd, L, kind, d + 1), vl, vu, rl, ru, l[q], u[q], ll[q], uu[q]);
             alive[q] = live(kind, l[q], u[q]);
@@ -348,14 +353,14 @@ __device__ __forceinline__ int reduce_side(const SearchArgs& A, const FmView* fm
                     continue;
                 }
             }
-            int P = 0;
-            for (int i = 0; i < F.size; ++i) P += stk[F.pos + i].remain != 0;
+            // all four extension sets from one pair of loads per interval, first in four
+            // regions of P slots, then packed back to back in base order
+            const int P = F.size;
             const uint32_t cbase = F.free;
             if (int(cbase) + 4 * P > cap) return OVF_STACK;
             int cnt[4] = {0, 0, 0, 0};
-            for (int i = 0; i < F.size; ++i) {
+            for (int i = 0; i < P; ++i) {
                 const Cand c = stk[F.pos + i];
-                if (c.remain == 0) continue;
                 const int o = cand_index(c.type);
                 const FmView& f = fm[o];
                 idx_t rl[4], ru[4];
@@ -373,12 +378,15 @@ __device__ __forceinline__ int reduce_side(const SearchArgs& A, const FmView* fm
                         x.uu = u2;
                         x.len = c.len;
                         x.type = c.type;
-                        x.remain = u2 - l2 + 1;
                     }
                 }
             }
+            int run = cnt[0];
+            for (int a = 1; a < 4; ++a) {
+                for (int j = 0; j < cnt[a]; ++j) stk[cbase + run + j] = stk[cbase + a * P + j];
+                run += cnt[a];
+            }
             F.cbase = cbase;
-            F.P = uint16_t(P);
             #pragma unroll
             for (int a = 0; a < 4; ++a) F.csz[a] = uint16_t(cnt[a]);
             F.next_a = 1;
@@ -392,14 +400,20 @@ __device__ __forceinline__ int reduce_side(const SearchArgs& A, const FmView* fm
         const int a = F.next_a++;
         if (level + 1 >= frcap) return OVF_LEVELS;
         Frame& G = fr[level + 1];
-        G.pos = F.cbase + uint32_t(a - 1) * F.P;
-        G.free = F.cbase + 4u * F.P;        // below it: the parent's four sets, still pending
+        uint32_t before = 0, all = 0;
+        #pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            before += (b < a - 1) ? F.csz[b] : 0;
+            all += F.csz[b];
+        }
+        G.pos = F.cbase + before;
+        G.free = F.cbase + all;             // below it: the parent's four sets, still pending
         G.size = F.csz[a - 1];
         int maxl = 0;
         uint32_t tr = 0;
         for (int i = 0; i < G.size; ++i) {
             const Cand& c = stk[G.pos + i];
-            tr += uint32_t(c.remain);
+            tr += uint32_t(c.uu - c.ll + 1);
             maxl = max(maxl, int(c.len));
         }
         G.maxlen = uint16_t(maxl);
