@@ -361,6 +361,9 @@ __device__ __forceinline__ int reduce_side(const SearchArgs& A, const FmView* fm
             int cnt[4] = {0, 0, 0, 0};
             for (int i = 0; i < P; ++i) {
                 const Cand c = stk[F.pos + i];
+                // remaining size uu - ll + 1 is 0 only for a wrapped [0, all-ones] interval (an
+                // empty extension at a zero LF base); the reference keeps it but never extends it
+                if (idx_t(c.uu - c.ll + 1) == 0) continue;
                 const int o = cand_index(c.type);
                 const FmView& f = fm[o];
                 idx_t rl[4], ru[4];
