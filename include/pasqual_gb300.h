@@ -124,6 +124,27 @@ PQ_API int pq_get_graph (pq_ctx * ctx, uint16_t * num_B, uint16_t * num_F, int32
 /* Time (ms, CUDA events on the context stream) of the last pq_sort/pq_build_fm/pq_overlaps. */
 PQ_API int pq_get_stage_ms (pq_ctx * ctx, float *sort_ms, float *fm_ms, float *search_ms);
 
+/* Largest num_reads * read_len that pq_suffix_sort_static accepts. */
+#define PQ_STATIC_SORT_MAX_SUFFIXES (1u << 20)
+
+/* No counterpart in the reference.  The suffix sort of pq_sort (same canonical order, same
+ * kernels) for callers that cannot allocate device memory -- for example a host application that
+ * owns all device memory through its own pool and forbids cudaMalloc, or a latency-critical path
+ * that cannot take cudaMalloc's implicit device-wide synchronisation.  It calls no cudaMalloc,
+ * cudaFree or other allocating routine: the caller passes device pointers to the reads
+ * (num_reads * read_len codes 1..4) and to the output suffix array (num_reads * read_len
+ * entries), and the working memory is a fixed array inside this library (about 30 MB for the
+ * 32-bit build, 38 MB for the 64-bit one) that every GPU which loads the library keeps until the
+ * process exits.  Sizes above PQ_STATIC_SORT_MAX_SUFFIXES return PQ_ERR_CAPACITY without doing
+ * any work.  The first call on each device looks up the array's device address (once, with that
+ * device current); make that first call before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU (other streams, other host threads) race and must be ordered by
+ * the caller.  Work is queued on `cuda_stream` (a cudaStream_t, NULL = the default stream) and
+ * the call returns once the suffix array is written.  Returns PQ_OK, PQ_ERR_ARG, PQ_ERR_CAPACITY
+ * or PQ_ERR_CUDA. */
+PQ_API int pq_suffix_sort_static (const uint8_t * reads_dev, pq_idx num_reads, int read_len,
+                                  int dir, pq_idx * sa_dev, void *cuda_stream);
+
 /* Duration (ms, CUDA events on the context stream) of the fast search kernel in the last
  * pq_overlaps, and the number of kernels this library has launched since it was loaded. */
 PQ_API int pq_get_kernel_stats (pq_ctx * ctx, float *search_kernel_ms,

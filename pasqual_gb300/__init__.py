@@ -30,7 +30,8 @@ PQ_ERRORS = {1: "PQ_ERR_ARG", 2: "PQ_ERR_CUDA", 3: "PQ_ERR_NOMEM", 4: "PQ_ERR_TO
 EXPORTS = ["pq_idx_bytes", "pq_create", "pq_destroy", "pq_last_error", "pq_set_reads",
            "pq_get_counts", "pq_sort", "pq_set_sa", "pq_get_sa", "pq_build_fm", "pq_build_index",
            "pq_get_index_ref", "pq_get_seeds", "pq_set_seed_k", "pq_overlaps",
-           "pq_get_graph_sizes", "pq_get_graph", "pq_get_stage_ms", "pq_get_kernel_stats"]
+           "pq_get_graph_sizes", "pq_get_graph", "pq_get_stage_ms", "pq_get_kernel_stats",
+           "pq_suffix_sort_static"]
 
 
 # The reference's own entry points served by the same library (include/pasqual_gb300_dropin.h).

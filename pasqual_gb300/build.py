@@ -15,7 +15,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 ROOT = os.path.dirname(HERE)
-SOURCES = ["pq_index.cu", "pq_search.cu", "pq_sort.cu", "pq_api.cu", "pq_dropin.cu"]
+SOURCES = ["pq_index.cu", "pq_search.cu", "pq_sort.cu", "pq_api.cu", "pq_dropin.cu",
+           "pq_sort_static.cu"]
 HEADERS = ["pq_common.cuh", "pq_index.cuh", "pq_sort.cuh"]
 PUBLIC = ["pasqual_gb300.h", "pasqual_gb300_dropin.h"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
