@@ -219,47 +219,39 @@ __device__ __forceinline__ bool live(int kind, idx_t l, idx_t u) {
 }
 __device__ __forceinline__ int walked_index(int kind) { return (kind == PQ_FB || kind == PQ_BB) ? 0 : 1; }
 
-// find_intervals (src/string_graph.c:163-383) for all four search kinds of one read, run in
-// lockstep so that each thread keeps four independent chains of loads in flight.
+// find_intervals for one side: kinds k0 then k1 (B-F and B-B, or F-B and F-F), searched in
+// lockstep so that each thread keeps two independent chains of loads in flight.
 //
 // The reference walks index A from its seed to depth t with search_1, then rebuilds the other
 // index's interval of the reversed pattern from depth 1 with another t-1 search_1 steps, and
 // only then continues with synchronised search_2 steps.  Here both intervals start from exact
 // k-mer seeds (one per index) and every step is a synchronised step, so the other interval is
 // known at every depth and the rebuild disappears; SA intervals are unique per string, so the
-// intervals at depth t -- and everything after -- are the reference's.  Chain q's candidates go
-// to stk[q*M, q*M + n[q]) with M = L - t, the most any kind can produce; olp[q] is its $ total.
-template <int NQ>
-__device__ __forceinline__ int chain_candidates(const SearchArgs& A, const FmView* fm, const ReadView& rd,
-                                                const int (&kinds)[NQ], Cand* stk, int cap, int (&n)[NQ],
-                                                int32_t (&olp)[NQ], uint32_t& probes) {
+// intervals at depth t -- and everything after -- are the reference's.  Candidates of kind k0
+// and k1 are collected in two regions of the stack and joined k0 first, the reference's order.
+__device__ __forceinline__ int side_candidates(const SearchArgs& A, const FmView* fm, const ReadView& rd, int k0,
+                                               int k1, Cand* stk, int cap, int& n_out, int32_t& olp,
+                                               uint32_t& probes) {
     const int L = A.L, t = A.t, k = A.seed_k;
     const int M = L - t;
-    if (NQ * M > cap) return OVF_STACK;
-    idx_t l[NQ], u[NQ], ll[NQ], uu[NQ];
-    bool alive[NQ];
+    if (2 * M > cap) return OVF_STACK;
+    idx_t l[2], u[2], ll[2], uu[2];
+    bool alive[2];
+    int n[2] = {0, 0};
     #pragma unroll
-    for (int q = 0; q < NQ; ++q) {
-        const int kind = kinds[q];
+    for (int q = 0; q < 2; ++q) {
+        const int kind = q ? k1 : k0;
         const int ia = walked_index(kind);
         kmer_seed(fm[ia], rd, L, kind, k, 1, -1, l[q], u[q], probes);       // pat(k) .. pat(1)
         kmer_seed(fm[1 - ia], rd, L, kind, 1, k, 1, ll[q], uu[q], probes);  // pat(1) .. pat(k)
         alive[q] = live(kind, l[q], u[q]);
-        n[q] = 0;
-        olp[q] = 0;
     }
-    auto any_alive = [&]() {
-        bool a = false;
-        #pragma unroll
-        for (int q = 0; q < NQ; ++q) a |= alive[q];
-        return a;
-    };
     int d = k;
-    while (d < t && any_alive()) {
+    while (d < t && (alive[0] || alive[1])) {
         #pragma unroll
-        for (int q = 0; q < NQ; ++q) {
+        for (int q = 0; q < 2; ++q) {
             if (!alive[q]) continue;
-            const int kind = kinds[q];
+            const int kind = q ? k1 : k0;
             const FmView& f = fm[walked_index(kind)];
             const idx_t vl = l[q], vu = u[q] + 1;
             idx_t rl[4], ru[4];
@@ -271,11 +263,11 @@ __device__ __forceinline__ int chain_candidates(const SearchArgs& A, const FmVie
         }
         ++d;
     }
-    while (d < L && any_alive()) {
+    while (d < L && (alive[0] || alive[1])) {
         #pragma unroll
-        for (int q = 0; q < NQ; ++q) {
+        for (int q = 0; q < 2; ++q) {
             if (!alive[q]) continue;
-            const int kind = kinds[q];
+            const int kind = q ? k1 : k0;
             const FmView& f = fm[walked_index(kind)];
             const idx_t vl = l[q], vu = u[q] + 1;
             idx_t rl[4], ru[4];
@@ -294,12 +286,14 @@ __device__ __forceinline__ int chain_candidates(const SearchArgs& A, const FmVie
                 c.len = uint16_t(d);
                 c.type = uint8_t(kind);
             }
-            olp[q] = int32_t(uint32_t(olp[q]) + uint32_t(tmp + 1));
+            olp = int32_t(uint32_t(olp) + uint32_t(tmp + 1));
             step_from_ranks(f, pattern_at(rd, L, kind, d + 1), vl, vu, rl, ru, l[q], u[q], ll[q], uu[q]);
             alive[q] = live(kind, l[q], u[q]);
         }
         ++d;
     }
+    for (int i = 0; i < n[1]; ++i) stk[n[0] + i] = stk[M + i];
+    n_out = n[0] + n[1];
     return OVF_NONE;
 }
 
@@ -440,31 +434,19 @@ __device__ __forceinline__ ReadResult search_read(const SearchArgs& A, const FmV
     R.nB = R.nF = 0;
     R.olpB = R.olpF = 0;
     R.ne = 0;
-    const int M = A.L - A.t;
-    if (6 * M > cap) { R.status = OVF_STACK; return R; }
-    // all four searches at once: B-F, B-B (B side), F-B, F-F (F side)
-    const int kinds[4] = {PQ_BF, PQ_BB, PQ_FB, PQ_FF};
-    int n[4];
-    int32_t op[4];
-    int s = chain_candidates<4>(A, fm, rd, kinds, stk, cap, n, op, probes);
-    if (s != OVF_NONE) { R.status = s; return R; }
-    R.olpB = int32_t(uint32_t(op[0]) + uint32_t(op[1]));
-    R.olpF = int32_t(uint32_t(op[2]) + uint32_t(op[3]));
-    // B side level 0 = B-F then B-B candidates at the bottom; F side (F-B then F-F) parked at the
-    // top of the stack while the B side is reduced
-    const int nB0 = n[0] + n[1], nF0 = n[2] + n[3];
-    for (int i = 0; i < n[1]; ++i) stk[n[0] + i] = stk[M + i];
-    const int top = cap - nF0;                      // >= 5M: no overlap with the four regions
-    for (int i = 0; i < n[2]; ++i) stk[top + i] = stk[2 * M + i];
-    for (int i = 0; i < n[3]; ++i) stk[top + n[2] + i] = stk[3 * M + i];
-    int sc = 0;
-    // extract_bw_edges first, then extract_fw_edges (src/string_graph.c:824-829)
-    if (R.olpB != 0) s = reduce_side(A, fm, self, stk, top, nB0, fr, frcap, eb, ebcap, R.ne, sc, probes);
+    int n0 = 0, sc = 0;
+    // B side: B-F then B-B candidates, then extract_bw_edges (src/string_graph.c:824-825)
+    int s = side_candidates(A, fm, rd, PQ_BF, PQ_BB, stk, cap, n0, R.olpB, probes);
+    if (s == OVF_NONE && R.olpB != 0)
+        s = reduce_side(A, fm, self, stk, cap, n0, fr, frcap, eb, ebcap, R.ne, sc, probes);
     if (s != OVF_NONE) { R.status = s; return R; }
     R.nB = sc;
-    for (int i = 0; i < nF0; ++i) stk[i] = stk[top + i];
+    // F side: F-B then F-F candidates, then extract_fw_edges (src/string_graph.c:828-829)
+    n0 = 0;
     sc = 0;
-    if (R.olpF != 0) s = reduce_side(A, fm, self, stk, cap, nF0, fr, frcap, eb, ebcap, R.ne, sc, probes);
+    s = side_candidates(A, fm, rd, PQ_FB, PQ_FF, stk, cap, n0, R.olpF, probes);
+    if (s == OVF_NONE && R.olpF != 0)
+        s = reduce_side(A, fm, self, stk, cap, n0, fr, frcap, eb, ebcap, R.ne, sc, probes);
     if (s != OVF_NONE) { R.status = s; return R; }
     R.nF = sc;
     return R;
