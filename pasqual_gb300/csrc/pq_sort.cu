@@ -116,38 +116,38 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_upsweep(const uint64_t* __res
     }
 }
 
-// single-CTA exclusive scan of m 64-bit counts, in place
+// single-CTA exclusive scan of m 64-bit counts, in place: each of the 1024 threads sums one
+// contiguous segment, the segment totals are scanned once, and each thread rewrites its segment
 __global__ void k_scan_small(unsigned long long* __restrict__ a, size_t m) {
     __shared__ unsigned long long wsum[32];
-    __shared__ unsigned long long carry;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (threadIdx.x == 0) carry = 0;
+    const size_t seg = (m + 1023) / 1024;
+    const size_t b = zmin(m, size_t(threadIdx.x) * seg), e = zmin(m, b + seg);
+    unsigned long long mine = 0;
+    for (size_t i = b; i < e; ++i) mine += a[i];
+    unsigned long long x = mine;
+    #pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[wid] = x;
     __syncthreads();
-    for (size_t base = 0; base < m; base += 1024) {
-        size_t i = base + threadIdx.x;
-        unsigned long long v = i < m ? a[i] : 0, x = v;
+    if (wid == 0) {
+        unsigned long long w = wsum[lane], z = w;
         #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x += y;
+            unsigned long long y = __shfl_up_sync(0xffffffffu, z, o);
+            if (lane >= o) z += y;
         }
-        if (lane == 31) wsum[wid] = x;
-        __syncthreads();
-        if (wid == 0) {
-            unsigned long long w = wsum[lane], z = w;
-            #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                unsigned long long y = __shfl_up_sync(0xffffffffu, z, o);
-                if (lane >= o) z += y;
-            }
-            wsum[lane] = z - w;
-        }
-        __syncthreads();
-        unsigned long long c = carry;
-        if (i < m) a[i] = c + wsum[wid] + x - v;
-        __syncthreads();
-        if (threadIdx.x == 1023) carry = c + wsum[wid] + x;
-        __syncthreads();
+        wsum[lane] = z - w;
+    }
+    __syncthreads();
+    unsigned long long run = wsum[wid] + x - mine;
+    for (size_t i = b; i < e; ++i) {
+        unsigned long long v = a[i];
+        a[i] = run;
+        run += v;
     }
 }
 
