@@ -79,7 +79,7 @@ struct pq_ctx {
 
     // overlap-search output
     DevBuf nB, nF, oB, oF, status, esrc, e_dest, e_trans, e_len, e_type, ctrs, ovf_list;
-    DevBuf off, g_dest, g_len, g_type, g_trans, asm_tmp, wide;
+    DevBuf off, g_dest, g_len, g_type, g_trans, asm_tmp, wide, warp_scratch;
     bool graph_ok = false;
     uint64_t num_edges = 0, probes = 0, wide_reads = 0;
 };
@@ -142,7 +142,7 @@ void pq_destroy(pq_ctx* ctx) {
     DevBuf* bufs[] = {&ctx->reads, &ctx->ktmp, &ctx->sort_tmp, &ctx->counts, &ctx->nB, &ctx->nF, &ctx->oB,
                       &ctx->oF, &ctx->status, &ctx->esrc, &ctx->e_dest, &ctx->e_trans, &ctx->e_len,
                       &ctx->e_type, &ctx->ctrs, &ctx->ovf_list, &ctx->off, &ctx->g_dest, &ctx->g_len,
-                      &ctx->g_type, &ctx->g_trans, &ctx->asm_tmp, &ctx->wide};
+                      &ctx->g_type, &ctx->g_trans, &ctx->asm_tmp, &ctx->wide, &ctx->warp_scratch};
     for (DevBuf* b : bufs) b->release();
     for (int d = 0; d < 2; ++d) {
         ctx->sa[d].release();
@@ -421,8 +421,12 @@ int pq_overlaps(pq_ctx* ctx) {
     cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device);
     CK(cudaEventRecord(ctx->evk0, ctx->st));
     if (nr) {
-        int blocks = int(std::min<size_t>((nr + 127) / 128, size_t(dev_sms) * 16));
-        CK(pq::search_fast(A, O, 128, blocks, ctx->st));
+        // 4 warps per block, each warp 32 reads per batch; enough blocks to fill every SM
+        const int scap = 4096, ebcap = 64;
+        int blocks = int(std::min<size_t>((nr + 127) / 128, size_t(pq::search_fast_blocks(ctx->L, dev_sms))));
+        const size_t wsb = pq::warp_scratch_bytes(ctx->L, ctx->t, size_t(blocks) * 4, scap, ebcap);
+        CK(ctx->warp_scratch.ensure(wsb));
+        CK(pq::search_fast(A, O, blocks, ctx->warp_scratch.p, wsb, scap, ebcap, ctx->st));
     }
     CK(cudaEventRecord(ctx->evk1, ctx->st));
     unsigned long long hc[3];

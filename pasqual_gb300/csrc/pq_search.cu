@@ -227,17 +227,15 @@ __device__ __forceinline__ int walked_index(int kind) { return (kind == PQ_FB ||
 // only then continues with synchronised search_2 steps.  Here both intervals start from exact
 // k-mer seeds (one per index) and every step is a synchronised step, so the other interval is
 // known at every depth and the rebuild disappears; SA intervals are unique per string, so the
-// intervals at depth t -- and everything after -- are the reference's.  Candidates of kind k0
-// and k1 are collected in two regions of the stack and joined k0 first, the reference's order.
-__device__ __forceinline__ int side_candidates(const SearchArgs& A, const FmView* fm, const ReadView& rd, int k0,
-                                               int k1, Cand* stk, int cap, int& n_out, int32_t& olp,
-                                               uint32_t& probes) {
+// intervals at depth t -- and everything after -- are the reference's.  The i-th stored candidate
+// of kind k0 (q = 0) or k1 (q = 1) goes to sink(q, i, ll, uu, depth, kind); n[q] counts them.
+template <class Sink>
+__device__ __forceinline__ void chain_pair(const SearchArgs& A, const FmView* fm, const ReadView& rd, int k0, int k1,
+                                           int (&n)[2], int32_t& olp, uint32_t& probes, Sink sink) {
     const int L = A.L, t = A.t, k = A.seed_k;
-    const int M = L - t;
-    if (2 * M > cap) return OVF_STACK;
     idx_t l[2], u[2], ll[2], uu[2];
     bool alive[2];
-    int n[2] = {0, 0};
+    n[0] = n[1] = 0;
     #pragma unroll
     for (int q = 0; q < 2; ++q) {
         const int kind = q ? k1 : k0;
@@ -279,19 +277,29 @@ __device__ __forceinline__ int side_candidates(const SearchArgs& A, const FmView
             // extended, and level 0 never runs the emission check (its max length plus level 0
             // cannot reach L), so it can never contribute and is not stored.
             const idx_t tmp = (vu - (ru[0] + ru[1] + ru[2] + ru[3])) - (vl - (rl[0] + rl[1] + rl[2] + rl[3])) - 1;
-            if (tmp + 1 != 0) {
-                Cand& c = stk[q * M + n[q]++];
-                c.ll = ll[q];
-                c.uu = ll[q] + tmp;
-                c.len = uint16_t(d);
-                c.type = uint8_t(kind);
-            }
+            if (tmp + 1 != 0) sink(q, n[q]++, ll[q], ll[q] + tmp, d, kind);
             olp = int32_t(uint32_t(olp) + uint32_t(tmp + 1));
             step_from_ranks(f, pattern_at(rd, L, kind, d + 1), vl, vu, rl, ru, l[q], u[q], ll[q], uu[q]);
             alive[q] = live(kind, l[q], u[q]);
         }
         ++d;
     }
+}
+
+// One side's candidates into the thread's stack: kind k0 then k1, the reference's order.
+__device__ __forceinline__ int side_candidates(const SearchArgs& A, const FmView* fm, const ReadView& rd, int k0,
+                                               int k1, Cand* stk, int cap, int& n_out, int32_t& olp,
+                                               uint32_t& probes) {
+    const int M = A.L - A.t;
+    if (2 * M > cap) return OVF_STACK;
+    int n[2];
+    chain_pair(A, fm, rd, k0, k1, n, olp, probes, [&](int q, int i, idx_t l0, idx_t u0, int d, int kind) {
+        Cand& c = stk[q * M + i];
+        c.ll = l0;
+        c.uu = u0;
+        c.len = uint16_t(d);
+        c.type = uint8_t(kind);
+    });
     for (int i = 0; i < n[1]; ++i) stk[n[0] + i] = stk[M + i];
     n_out = n[0] + n[1];
     return OVF_NONE;
@@ -504,39 +512,433 @@ __device__ __forceinline__ void add_probes(const SearchOut& O, uint32_t probes) 
     if ((threadIdx.x & 31) == 0 && v) atomicAdd(O.probes, v);
 }
 
-constexpr int kFastCap = 768;
-constexpr int kFastFrames = 128;
-constexpr int kFastEdges = 48;
+// ------------------------------------------------------------------------------ fast tier
+//
+// A warp takes 32 reads.  Phase A: each lane runs the candidate searches of its read (two chains
+// at a time, B side then F side) and stores the level-0 candidates in the warp's scratch.
+// Phase B: the whole warp reduces one (read, side) at a time -- the extract_*_edges DFS with the
+// intervals of a level spread over the lanes: every lane loads the blocks of its interval, the
+// four extension sets are packed with ballots, the emission check finds the first completing
+// interval with a ballot, and the edge reads are fetched by all lanes at once.  Control flow of
+// phase B is uniform across the warp (all decisions come from ballots, shuffles and the frames
+// in shared memory), and the stack lives in global memory as three coalesced arrays.
+// Phase C: each lane publishes its read (edge-pool reservation, copy, per-read counts).
 
-__global__ void __launch_bounds__(128) k_search_fast(SearchArgs A, SearchOut O) {
+constexpr int kWarpsPerCta = 4;
+constexpr int kWarpFrames = 64;
+
+struct WFrame {
+    uint32_t pos, free, cbase;
+    int32_t trans;
+    uint16_t size, maxlen;
+    uint16_t csz[4];
+    uint32_t next_a;
+};
+
+__device__ __forceinline__ uint32_t pack_meta(int len, int type) { return uint32_t(len) | (uint32_t(type) << 16); }
+__device__ __forceinline__ int meta_len(uint32_t m) { return int(m & 0xffff); }
+__device__ __forceinline__ int meta_type(uint32_t m) { return int(m >> 16); }
+
+template <class T> __device__ __forceinline__ T warp_max(T v) {
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+template <class T> __device__ __forceinline__ T warp_sum(T v) {
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// extract_fw_edges / extract_bw_edges for one (read, side), cooperatively by one warp.  Level 0
+// is already in stack[0, n0).  Edges go to the read's scratch slots [ne, ...).  Returns OVF_* or
+// ERR_* (uniform across the warp).
+__device__ int warp_reduce_side(const SearchArgs& A, const FmView* fm, idx_t self, const WarpScratch& S,
+                                size_t sbase, int n0, WFrame* fr, size_t ebase, int& ne, int& side_count,
+                                uint32_t& probes) {
+    const int L = A.L;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1;
+    idx_t* s_ll = S.s_ll + sbase;
+    idx_t* s_uu = S.s_uu + sbase;
+    uint32_t* s_meta = S.s_meta + sbase;
+    const int scap = S.scap;
+    if (lane == 0) {
+        WFrame f0;
+        f0.pos = 0;
+        f0.free = uint32_t(n0);
+        f0.cbase = 0;
+        f0.trans = 0;
+        f0.size = uint16_t(n0);
+        f0.maxlen = 0;
+        f0.csz[0] = f0.csz[1] = f0.csz[2] = f0.csz[3] = 0;
+        f0.next_a = 1;
+        fr[0] = f0;
+    }
+    __syncwarp();
+    int level = 0;
+    bool entering = true;
+    while (true) {
+        WFrame F = fr[level];
+        if (entering) {
+            entering = false;
+            if (int(F.maxlen) + level == L) {
+                // first interval (in order) that completes a read at this level and holds $ rows
+                bool found = false;
+                idx_t lll = 0, uuu = 0;
+                int elen = 0, etype = 0;
+                for (int base = 0; base < F.size && !found; base += 32) {
+                    const int i = base + lane;
+                    bool hit = false;
+                    idx_t a = 0, b = 0;
+                    uint32_t m = 0;
+                    if (i < F.size) {
+                        m = s_meta[F.pos + i];
+                        if (meta_len(m) + level == L) {
+                            const FmView& fo = fm[cand_index(meta_type(m))];
+                            a = fo.Cf[0] + rank_dollar(fo, s_ll[F.pos + i]);
+                            b = fo.Cf[0] + rank_dollar(fo, s_uu[F.pos + i] + 1) - 1;
+                            probes += 2;
+                            hit = a <= b;
+                        }
+                    }
+                    const unsigned hm = __ballot_sync(0xffffffffu, hit);
+                    if (hm) {
+                        const int src = __ffs(hm) - 1;
+#ifdef PQ_IDX64
+                        lll = __shfl_sync(0xffffffffu, (unsigned long long)a, src);
+                        uuu = __shfl_sync(0xffffffffu, (unsigned long long)b, src);
+#else
+                        lll = __shfl_sync(0xffffffffu, a, src);
+                        uuu = __shfl_sync(0xffffffffu, b, src);
+#endif
+                        const uint32_t mm = __shfl_sync(0xffffffffu, m, src);
+                        elen = meta_len(mm);
+                        etype = meta_type(mm);
+                        found = true;
+                    }
+                }
+                if (found) {
+                    // the reference's loop k = lll .. uuu (k < uuu + 1): no iteration when uuu + 1 wraps
+                    const idx_t endk = uuu + 1;
+                    const idx_t cnt = endk > lll ? endk - lll : 0;
+                    const int other = cand_index(etype);
+                    for (idx_t kb = 0; kb < cnt; kb += 32) {
+                        const bool act = kb + lane < cnt;
+                        idx_t r = self;
+                        if (act) r = __ldg(fm[other].reads_index + (lll + kb + lane));
+                        const bool em = act && r != self;
+                        const unsigned emm = __ballot_sync(0xffffffffu, em);
+                        const int k = __popc(emm);
+                        if (side_count + k > 65535) return ERR_TOO_MANY;
+                        if (ne + k > S.ebcap) return OVF_EDGES;
+                        if (em) {
+                            const size_t p = ebase + ne + __popc(emm & lt);
+                            S.e_dest[p] = r;
+                            S.e_trans[p] = F.trans;
+                            S.e_meta[p] = pack_meta(elen, etype);
+                        }
+                        ne += k;
+                        side_count += k;
+                    }
+                    if (cnt > 0) {   // flag: this branch is finished
+                        if (level == 0) return OVF_NONE;
+                        --level;
+                        continue;
+                    }
+                }
+            }
+            // all four extension sets from one pair of loads per interval
+            const int P = F.size;
+            const uint32_t cbase = F.free;
+            if (int(cbase) + 4 * P > scap) return OVF_STACK;
+            int c0 = 0, c1 = 0, c2 = 0, c3 = 0;
+            for (int base = 0; base < P; base += 32) {
+                const int i = base + lane;
+                idx_t lo[4], hi[4];
+                bool has[4] = {false, false, false, false};
+                uint32_t m = 0;
+                if (i < P) {
+                    const idx_t cl = s_ll[F.pos + i], cu = s_uu[F.pos + i];
+                    m = s_meta[F.pos + i];
+                    if (idx_t(cu - cl + 1) != 0) {   // a wrapped [0, all-ones] interval is kept, never extended
+                        const int o = cand_index(meta_type(m));
+                        const FmView& f = fm[o];
+                        idx_t rl[4], ru[4];
+                        rank_all(f, cl, rl);
+                        rank_all(f, cu + 1, ru);
+                        probes += 2;
+                        #pragma unroll
+                        for (int a = 1; a <= 4; ++a) {
+                            const int ch = o == 0 ? complement(a) : a;
+                            lo[a - 1] = f.Cf[ch] + pick4(rl, ch);
+                            hi[a - 1] = f.Cf[ch] + pick4(ru, ch) - 1;
+                            has[a - 1] = lo[a - 1] <= hi[a - 1];
+                        }
+                    }
+                }
+                #pragma unroll
+                for (int a = 0; a < 4; ++a) {
+                    const unsigned hm = __ballot_sync(0xffffffffu, has[a]);
+                    int& c = a == 0 ? c0 : (a == 1 ? c1 : (a == 2 ? c2 : c3));
+                    if (has[a]) {
+                        const size_t p = size_t(cbase) + size_t(a) * P + c + __popc(hm & lt);
+                        s_ll[p] = lo[a];
+                        s_uu[p] = hi[a];
+                        s_meta[p] = m;
+                    }
+                    c += __popc(hm);
+                }
+            }
+            __syncwarp();
+            // pack the sets back to back (each chunk read before it is written: destination <= source)
+            int run = c0;
+            const int cs[3] = {c1, c2, c3};
+            #pragma unroll
+            for (int a = 1; a < 4; ++a) {
+                const int ca = cs[a - 1];
+                if (run != a * P) {
+                    for (int jb = 0; jb < ca; jb += 32) {
+                        const int j = jb + lane;
+                        idx_t x = 0, y = 0;
+                        uint32_t z = 0;
+                        if (j < ca) {
+                            const size_t src = size_t(cbase) + size_t(a) * P + j;
+                            x = s_ll[src];
+                            y = s_uu[src];
+                            z = s_meta[src];
+                        }
+                        __syncwarp();
+                        if (j < ca) {
+                            const size_t dst = size_t(cbase) + run + j;
+                            s_ll[dst] = x;
+                            s_uu[dst] = y;
+                            s_meta[dst] = z;
+                        }
+                        __syncwarp();
+                    }
+                }
+                run += ca;
+            }
+            F.cbase = cbase;
+            F.csz[0] = uint16_t(c0);
+            F.csz[1] = uint16_t(c1);
+            F.csz[2] = uint16_t(c2);
+            F.csz[3] = uint16_t(c3);
+            F.next_a = 1;
+            if (lane == 0) fr[level] = F;
+            __syncwarp();
+        }
+        int a = int(F.next_a);
+        while (a <= 4 && F.csz[a - 1] == 0) ++a;
+        if (a > 4) {
+            if (level == 0) return OVF_NONE;
+            --level;
+            continue;
+        }
+        if (level + 1 >= kWarpFrames) return OVF_LEVELS;
+        uint32_t before = 0, all = 0;
+        #pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            before += (b < a - 1) ? F.csz[b] : 0;
+            all += F.csz[b];
+        }
+        WFrame G;
+        G.pos = F.cbase + before;
+        G.free = F.cbase + all;        // below it: the parent's four sets, still pending
+        G.cbase = 0;
+        G.size = F.csz[a - 1];
+        int maxl = 0;
+        uint32_t tr = 0;
+        for (int i = lane; i < G.size; i += 32) {
+            maxl = max(maxl, meta_len(s_meta[G.pos + i]));
+            tr += uint32_t(s_uu[G.pos + i] - s_ll[G.pos + i] + 1);
+        }
+        G.maxlen = uint16_t(warp_max(maxl));
+        G.trans = int32_t(warp_sum(tr));
+        G.csz[0] = G.csz[1] = G.csz[2] = G.csz[3] = 0;
+        G.next_a = 1;
+        __syncwarp();
+        if (lane == 0) {
+            fr[level].next_a = uint32_t(a + 1);
+            fr[level + 1] = G;
+        }
+        __syncwarp();
+        ++level;
+        entering = true;
+    }
+}
+
+__global__ void __launch_bounds__(128) k_search_fast(SearchArgs A, SearchOut O, WarpScratch S) {
     extern __shared__ uint32_t s_reads[];
     __shared__ FmView s_fm[2];
+    __shared__ WFrame s_fr[kWarpsPerCta][kWarpFrames];
+    __shared__ int s_n[kWarpsPerCta][32][4];
+    __shared__ int32_t s_olp[kWarpsPerCta][32][2];
+    __shared__ int s_st[kWarpsPerCta][32];
+    __shared__ int s_ne[kWarpsPerCta][32][2];
     if (threadIdx.x < 2) s_fm[threadIdx.x] = A.fm[threadIdx.x];
     __syncthreads();
-    Cand stk[kFastCap];
-    Frame fr[kFastFrames];
-    EdgeRec eb[kFastEdges];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const size_t gw = size_t(blockIdx.x) * kWarpsPerCta + wid;
+    const size_t nw = size_t(gridDim.x) * kWarpsPerCta;
+    const int M = A.L - A.t;
+    const size_t cbase_w = gw * 32 * 4 * size_t(M);        // level-0 candidates of this warp
+    const size_t sbase_w = gw * size_t(S.scap);            // DFS stack of this warp
+    const size_t ebase_w = gw * 32 * size_t(S.ebcap);      // edge slots of this warp
     uint32_t probes = 0;
-    const size_t stride = size_t(gridDim.x) * blockDim.x;
-    const size_t nwork = ((size_t(A.num_reads) + 31) / 32) * 32;   // whole warps for the probe reduction
-    for (size_t r = size_t(blockIdx.x) * blockDim.x + threadIdx.x; r < nwork; r += stride) {
-        if (r < A.num_reads) {
+    for (size_t batch = gw; batch * 32 < size_t(A.num_reads); batch += nw) {
+        const size_t r = batch * 32 + lane;
+        const bool have = r < size_t(A.num_reads);
+        // phase A
+        if (have) {
             load_read(A, idx_t(r), s_reads + threadIdx.x, blockDim.x);
             ReadView rd{s_reads + threadIdx.x, int(blockDim.x)};
-            ReadResult R = search_read(A, s_fm, idx_t(r), rd, stk, kFastCap, fr, kFastFrames, eb, kFastEdges,
-                                       probes);
-            publish(O, idx_t(r), R, eb);
+            const size_t cb = cbase_w + size_t(lane) * 4 * M;
+            auto sink = [&](int qbase) {
+                return [=](int q, int i, idx_t l0, idx_t u0, int d, int kind) {
+                    const size_t p = cb + size_t(qbase + q) * M + i;
+                    S.c_ll[p] = l0;
+                    S.c_uu[p] = u0;
+                    S.c_meta[p] = pack_meta(d, kind);
+                };
+            };
+            int nb[2], nf[2];
+            int32_t ob = 0, of = 0;
+            chain_pair(A, s_fm, rd, PQ_BF, PQ_BB, nb, ob, probes, sink(0));
+            chain_pair(A, s_fm, rd, PQ_FB, PQ_FF, nf, of, probes, sink(2));
+            s_n[wid][lane][0] = nb[0];
+            s_n[wid][lane][1] = nb[1];
+            s_n[wid][lane][2] = nf[0];
+            s_n[wid][lane][3] = nf[1];
+            s_olp[wid][lane][0] = ob;
+            s_olp[wid][lane][1] = of;
+            s_st[wid][lane] = OVF_NONE;
+        } else {
+            s_st[wid][lane] = -1;
         }
+        __syncwarp();
+        // phase B: reduce (read j, B side) then (read j, F side), whole warp
+        for (int j = 0; j < 32; ++j) {
+            if (s_st[wid][j] != OVF_NONE) continue;
+            const idx_t self = idx_t(batch * 32 + j);
+            const size_t cb = cbase_w + size_t(j) * 4 * M;
+            const size_t eb = ebase_w + size_t(j) * S.ebcap;
+            int ne = 0, st = OVF_NONE;
+            int counts[2] = {0, 0};
+            for (int side = 0; side < 2 && st == OVF_NONE; ++side) {
+                if (s_olp[wid][j][side] == 0) continue;   // src/string_graph.c:824, 828
+                const int na = s_n[wid][j][2 * side], nb = s_n[wid][j][2 * side + 1];
+                const int n0 = na + nb;
+                if (n0 > S.scap) { st = OVF_STACK; break; }
+                for (int i = lane; i < n0; i += 32) {
+                    const size_t src = cb + (i < na ? size_t(2 * side) * M + i : size_t(2 * side + 1) * M + (i - na));
+                    S.s_ll[sbase_w + i] = S.c_ll[src];
+                    S.s_uu[sbase_w + i] = S.c_uu[src];
+                    S.s_meta[sbase_w + i] = S.c_meta[src];
+                }
+                __syncwarp();
+                int sc = 0;
+                st = warp_reduce_side(A, s_fm, self, S, sbase_w, n0, s_fr[wid], eb, ne, sc, probes);
+                counts[side] = sc;
+                __syncwarp();
+            }
+            if (lane == 0) {
+                s_st[wid][j] = st;
+                s_ne[wid][j][0] = counts[0];
+                s_ne[wid][j][1] = counts[1];
+            }
+            __syncwarp();
+        }
+        // phase C: publish
+        if (have) {
+            const int st = s_st[wid][lane];
+            if (st != OVF_NONE) {
+                O.status[r] = uint8_t(st);
+                if (st != ERR_TOO_MANY) {
+                    unsigned k = atomicAdd(O.ovf_count, 1u);
+                    O.ovf_list[k] = idx_t(r);
+                }
+            } else {
+                const int nB = s_ne[wid][lane][0], nF = s_ne[wid][lane][1], ne = nB + nF;
+                unsigned long long base = 0;
+                bool ok = true;
+                if (ne) {
+                    base = atomicAdd(O.e_count, (unsigned long long)ne);
+                    if (base + ne > O.e_cap) {
+                        ok = false;
+                        O.status[r] = OVF_POOL;
+                        unsigned k = atomicAdd(O.ovf_count, 1u);
+                        O.ovf_list[k] = idx_t(r);
+                    } else {
+                        const size_t eb = ebase_w + size_t(lane) * S.ebcap;
+                        for (int e = 0; e < ne; ++e) {
+                            const uint32_t mt = S.e_meta[eb + e];
+                            O.e_dest[base + e] = S.e_dest[eb + e];
+                            O.e_trans[base + e] = S.e_trans[eb + e];
+                            O.e_len[base + e] = uint16_t(meta_len(mt));
+                            O.e_type[base + e] = uint8_t(meta_type(mt));
+                        }
+                    }
+                }
+                if (ok) {
+                    O.status[r] = OVF_NONE;
+                    O.num_B[r] = uint16_t(nB);
+                    O.num_F[r] = uint16_t(nF);
+                    O.olp_B[r] = s_olp[wid][lane][0];
+                    O.olp_F[r] = s_olp[wid][lane][1];
+                    O.edge_src[r] = base;
+                }
+            }
+        }
+        __syncwarp();
     }
     add_probes(O, probes);
 }
 
-cudaError_t search_fast(const SearchArgs& a, const SearchOut& o, int threads_per_block, int blocks,
-                        cudaStream_t st) {
-    if (threads_per_block != 128) return cudaErrorInvalidValue;
+int search_fast_blocks(int L, int num_sms) {
+    const int words = (L + 15) / 16;
+    const size_t smem = size_t(words) * 32 * kWarpsPerCta * sizeof(uint32_t);
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search_fast, 32 * kWarpsPerCta, smem) !=
+            cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    return per_sm * num_sms;
+}
+
+size_t warp_scratch_bytes(int L, int t, size_t nwarps, int scap, int ebcap) {
+    const size_t M = size_t(L - t);
+    const size_t cand = nwarps * 32 * 4 * M, stk = nwarps * size_t(scap), edg = nwarps * 32 * size_t(ebcap);
+    return (cand + stk) * (2 * sizeof(idx_t) + 4) + edg * (sizeof(idx_t) + 8) + 16 * 256;
+}
+
+cudaError_t search_fast(const SearchArgs& a, const SearchOut& o, int blocks, void* scratch, size_t scratch_bytes,
+                        int scap, int ebcap, cudaStream_t st) {
+    const size_t nwarps = size_t(blocks) * kWarpsPerCta;
+    if (scratch_bytes < warp_scratch_bytes(a.L, a.t, nwarps, scap, ebcap)) return cudaErrorInvalidValue;
+    const size_t M = size_t(a.L - a.t);
+    const size_t cand = nwarps * 32 * 4 * M, stk = nwarps * size_t(scap), edg = nwarps * 32 * size_t(ebcap);
+    char* p = static_cast<char*>(scratch);
+    auto take = [&](size_t bytes) {
+        char* q = p;
+        p += (bytes + 255) & ~size_t(255);
+        return q;
+    };
+    WarpScratch S;
+    S.c_ll = reinterpret_cast<idx_t*>(take(cand * sizeof(idx_t)));
+    S.c_uu = reinterpret_cast<idx_t*>(take(cand * sizeof(idx_t)));
+    S.c_meta = reinterpret_cast<uint32_t*>(take(cand * 4));
+    S.s_ll = reinterpret_cast<idx_t*>(take(stk * sizeof(idx_t)));
+    S.s_uu = reinterpret_cast<idx_t*>(take(stk * sizeof(idx_t)));
+    S.s_meta = reinterpret_cast<uint32_t*>(take(stk * 4));
+    S.e_dest = reinterpret_cast<idx_t*>(take(edg * sizeof(idx_t)));
+    S.e_trans = reinterpret_cast<int32_t*>(take(edg * 4));
+    S.e_meta = reinterpret_cast<uint32_t*>(take(edg * 4));
+    S.scap = scap;
+    S.ebcap = ebcap;
     const int words = (a.L + 15) / 16;
-    size_t smem = size_t(words) * threads_per_block * sizeof(uint32_t);
-    { k_search_fast<<<blocks, threads_per_block, smem, st>>>(a, o); note_launch(); }
+    size_t smem = size_t(words) * 32 * kWarpsPerCta * sizeof(uint32_t);
+    { k_search_fast<<<blocks, 32 * kWarpsPerCta, smem, st>>>(a, o, S); note_launch(); }
     return cudaGetLastError();
 }
 
