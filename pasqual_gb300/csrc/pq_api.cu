@@ -422,11 +422,11 @@ int pq_overlaps(pq_ctx* ctx) {
     CK(cudaEventRecord(ctx->evk0, ctx->st));
     if (nr) {
         // 4 warps per block, each warp 32 reads per batch; enough blocks to fill every SM
-        const int scap = 4096, ebcap = 64;
+        const int ebcap = 64;
         int blocks = int(std::min<size_t>((nr + 127) / 128, size_t(pq::search_fast_blocks(ctx->L, dev_sms))));
-        const size_t wsb = pq::warp_scratch_bytes(ctx->L, ctx->t, size_t(blocks) * 4, scap, ebcap);
+        const size_t wsb = pq::warp_scratch_bytes(ctx->L, ctx->t, size_t(blocks) * 4, ebcap);
         CK(ctx->warp_scratch.ensure(wsb));
-        CK(pq::search_fast(A, O, blocks, ctx->warp_scratch.p, wsb, scap, ebcap, ctx->st));
+        CK(pq::search_fast(A, O, blocks, ctx->warp_scratch.p, wsb, ebcap, ctx->st));
     }
     CK(cudaEventRecord(ctx->evk1, ctx->st));
     unsigned long long hc[3];

@@ -43,24 +43,23 @@ struct SearchArgs {
     int seed_k;                 // k-mer seed depth (0 = start at depth 1 from C[])
 };
 
-// Scratch of the warp-cooperative fast kernel, per warp: level-0 candidates of 32 reads
-// (4 kinds x (L - t) slots each), a DFS stack of scap intervals, ebcap edge slots per read.
+// Global scratch of the warp-cooperative fast kernel, per warp: level-0 candidates of 32 reads
+// (4 kinds x (L - t) slots each) and ebcap edge slots per read.  (The DFS stack itself is in
+// shared memory.)
 struct WarpScratch {
     idx_t *c_ll, *c_uu;
     uint32_t* c_meta;
-    idx_t *s_ll, *s_uu;
-    uint32_t* s_meta;
     idx_t* e_dest;
     int32_t* e_trans;
     uint32_t* e_meta;
-    int scap, ebcap;
+    int ebcap;
 };
-size_t warp_scratch_bytes(int L, int t, size_t nwarps, int scap, int ebcap);
+size_t warp_scratch_bytes(int L, int t, size_t nwarps, int ebcap);
 int search_fast_blocks(int L, int num_sms);   // resident blocks of the fast kernel on the device
-// blocks of 128 threads (4 warps); reads that outgrow scap/ebcap or 64 DFS levels are listed
-// for the wide kernel.
+// blocks of 128 threads (4 warps); reads that outgrow the shared-memory stack, ebcap edges or
+// the frame count are listed for the wide kernel.
 cudaError_t search_fast(const SearchArgs& a, const SearchOut& o, int blocks, void* scratch, size_t scratch_bytes,
-                        int scap, int ebcap, cudaStream_t st);
+                        int ebcap, cudaStream_t st);
 
 struct WideScratch {
     void* stack;                // slots * stack_cap candidates

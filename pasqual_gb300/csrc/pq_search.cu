@@ -525,7 +525,8 @@ __device__ __forceinline__ void add_probes(const SearchOut& O, uint32_t probes) 
 // Phase C: each lane publishes its read (edge-pool reservation, copy, per-read counts).
 
 constexpr int kWarpsPerCta = 4;
-constexpr int kWarpFrames = 64;
+constexpr int kWarpFrames = 48;     // DFS levels per warp (deeper reads go to the wide kernel)
+constexpr int kSmemStack = 384;     // intervals per warp in shared memory
 
 struct WFrame {
     uint32_t pos, free, cbase;
@@ -533,6 +534,13 @@ struct WFrame {
     uint16_t size, maxlen;
     uint16_t csz[4];
     uint32_t next_a;
+};
+
+// A warp's DFS stack in shared memory, struct of arrays.
+struct WarpStack {
+    idx_t* ll;
+    idx_t* uu;
+    uint32_t* meta;
 };
 
 __device__ __forceinline__ uint32_t pack_meta(int len, int type) { return uint32_t(len) | (uint32_t(type) << 16); }
@@ -549,20 +557,27 @@ template <class T> __device__ __forceinline__ T warp_sum(T v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
+__device__ __forceinline__ idx_t shfl_idx(idx_t v, int src) {
+#ifdef PQ_IDX64
+    return __shfl_sync(0xffffffffu, (unsigned long long)v, src);
+#else
+    return __shfl_sync(0xffffffffu, v, src);
+#endif
+}
 
-// extract_fw_edges / extract_bw_edges for one (read, side), cooperatively by one warp.  Level 0
-// is already in stack[0, n0).  Edges go to the read's scratch slots [ne, ...).  Returns OVF_* or
-// ERR_* (uniform across the warp).
-__device__ int warp_reduce_side(const SearchArgs& A, const FmView* fm, idx_t self, const WarpScratch& S,
-                                size_t sbase, int n0, WFrame* fr, size_t ebase, int& ne, int& side_count,
+// extract_fw_edges / extract_bw_edges for one (read, side), cooperatively by one warp, with the
+// stack in shared memory.  Level 0 is already in W[0, n0).  On each level every interval's two
+// blocks are loaded once and serve both the emission check (the `$` counts at its ends) and the
+// four extensions; the first interval (in order) that completes a read and holds `$` rows is
+// found with a ballot.  If the level emits, the extensions computed with it are simply dropped,
+// as the reference never computes them.  Edges go to the read's scratch slots [ne, ...).
+// Returns OVF_* or ERR_* (uniform across the warp).
+__device__ int warp_reduce_side(const SearchArgs& A, const FmView* fm, idx_t self, const WarpStack& W, int n0,
+                                WFrame* fr, const WarpScratch& S, size_t ebase, int& ne, int& side_count,
                                 uint32_t& probes) {
     const int L = A.L;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1;
-    idx_t* s_ll = S.s_ll + sbase;
-    idx_t* s_uu = S.s_uu + sbase;
-    uint32_t* s_meta = S.s_meta + sbase;
-    const int scap = S.scap;
     if (lane == 0) {
         WFrame f0;
         f0.pos = 0;
@@ -582,138 +597,119 @@ __device__ int warp_reduce_side(const SearchArgs& A, const FmView* fm, idx_t sel
         WFrame F = fr[level];
         if (entering) {
             entering = false;
-            if (int(F.maxlen) + level == L) {
-                // first interval (in order) that completes a read at this level and holds $ rows
-                bool found = false;
-                idx_t lll = 0, uuu = 0;
-                int elen = 0, etype = 0;
-                for (int base = 0; base < F.size && !found; base += 32) {
-                    const int i = base + lane;
-                    bool hit = false;
-                    idx_t a = 0, b = 0;
-                    uint32_t m = 0;
-                    if (i < F.size) {
-                        m = s_meta[F.pos + i];
-                        if (meta_len(m) + level == L) {
-                            const FmView& fo = fm[cand_index(meta_type(m))];
-                            a = fo.Cf[0] + rank_dollar(fo, s_ll[F.pos + i]);
-                            b = fo.Cf[0] + rank_dollar(fo, s_uu[F.pos + i] + 1) - 1;
-                            probes += 2;
-                            hit = a <= b;
-                        }
-                    }
-                    const unsigned hm = __ballot_sync(0xffffffffu, hit);
-                    if (hm) {
-                        const int src = __ffs(hm) - 1;
-#ifdef PQ_IDX64
-                        lll = __shfl_sync(0xffffffffu, (unsigned long long)a, src);
-                        uuu = __shfl_sync(0xffffffffu, (unsigned long long)b, src);
-#else
-                        lll = __shfl_sync(0xffffffffu, a, src);
-                        uuu = __shfl_sync(0xffffffffu, b, src);
-#endif
-                        const uint32_t mm = __shfl_sync(0xffffffffu, m, src);
-                        elen = meta_len(mm);
-                        etype = meta_type(mm);
-                        found = true;
-                    }
-                }
-                if (found) {
-                    // the reference's loop k = lll .. uuu (k < uuu + 1): no iteration when uuu + 1 wraps
-                    const idx_t endk = uuu + 1;
-                    const idx_t cnt = endk > lll ? endk - lll : 0;
-                    const int other = cand_index(etype);
-                    for (idx_t kb = 0; kb < cnt; kb += 32) {
-                        const bool act = kb + lane < cnt;
-                        idx_t r = self;
-                        if (act) r = __ldg(fm[other].reads_index + (lll + kb + lane));
-                        const bool em = act && r != self;
-                        const unsigned emm = __ballot_sync(0xffffffffu, em);
-                        const int k = __popc(emm);
-                        if (side_count + k > 65535) return ERR_TOO_MANY;
-                        if (ne + k > S.ebcap) return OVF_EDGES;
-                        if (em) {
-                            const size_t p = ebase + ne + __popc(emm & lt);
-                            S.e_dest[p] = r;
-                            S.e_trans[p] = F.trans;
-                            S.e_meta[p] = pack_meta(elen, etype);
-                        }
-                        ne += k;
-                        side_count += k;
-                    }
-                    if (cnt > 0) {   // flag: this branch is finished
-                        if (level == 0) return OVF_NONE;
-                        --level;
-                        continue;
-                    }
-                }
-            }
-            // all four extension sets from one pair of loads per interval
+            const bool chk = int(F.maxlen) + level == L;
             const int P = F.size;
             const uint32_t cbase = F.free;
-            if (int(cbase) + 4 * P > scap) return OVF_STACK;
+            if (int(cbase) + 4 * P > kSmemStack) return OVF_STACK;
+            bool found = false;
+            idx_t lll = 0, uuu = 0;
+            uint32_t em_meta = 0;
             int c0 = 0, c1 = 0, c2 = 0, c3 = 0;
             for (int base = 0; base < P; base += 32) {
                 const int i = base + lane;
-                idx_t lo[4], hi[4];
-                bool has[4] = {false, false, false, false};
+                idx_t cl = 0, cu = 0;
                 uint32_t m = 0;
+                bool ext = false, ends = false;
                 if (i < P) {
-                    const idx_t cl = s_ll[F.pos + i], cu = s_uu[F.pos + i];
-                    m = s_meta[F.pos + i];
-                    if (idx_t(cu - cl + 1) != 0) {   // a wrapped [0, all-ones] interval is kept, never extended
-                        const int o = cand_index(meta_type(m));
-                        const FmView& f = fm[o];
-                        idx_t rl[4], ru[4];
-                        rank_all(f, cl, rl);
-                        rank_all(f, cu + 1, ru);
-                        probes += 2;
-                        #pragma unroll
-                        for (int a = 1; a <= 4; ++a) {
-                            const int ch = o == 0 ? complement(a) : a;
-                            lo[a - 1] = f.Cf[ch] + pick4(rl, ch);
-                            hi[a - 1] = f.Cf[ch] + pick4(ru, ch) - 1;
-                            has[a - 1] = lo[a - 1] <= hi[a - 1];
-                        }
-                    }
+                    cl = W.ll[F.pos + i];
+                    cu = W.uu[F.pos + i];
+                    m = W.meta[F.pos + i];
+                    ext = idx_t(cu - cl + 1) != 0;   // a wrapped [0, all-ones] interval is kept, never extended
+                    ends = chk && meta_len(m) + level == L;
+                }
+                const int o = cand_index(meta_type(m));
+                const FmView& f = fm[o];
+                idx_t rl[4] = {0, 0, 0, 0}, ru[4] = {0, 0, 0, 0};
+                if (ext || ends) {
+                    rank_all(f, cl, rl);
+                    rank_all(f, cu + 1, ru);
+                    probes += 2;
+                }
+                bool hit = false;
+                idx_t ea = 0, eb2 = 0;
+                if (ends) {
+                    ea = f.Cf[0] + (cl - (rl[0] + rl[1] + rl[2] + rl[3]));
+                    eb2 = f.Cf[0] + ((cu + 1) - (ru[0] + ru[1] + ru[2] + ru[3])) - 1;
+                    hit = ea <= eb2;
+                }
+                const unsigned hm = __ballot_sync(0xffffffffu, hit);
+                if (hm && !found) {
+                    const int src = __ffs(hm) - 1;
+                    lll = shfl_idx(ea, src);
+                    uuu = shfl_idx(eb2, src);
+                    em_meta = __shfl_sync(0xffffffffu, m, src);
+                    found = true;
                 }
                 #pragma unroll
-                for (int a = 0; a < 4; ++a) {
-                    const unsigned hm = __ballot_sync(0xffffffffu, has[a]);
-                    int& c = a == 0 ? c0 : (a == 1 ? c1 : (a == 2 ? c2 : c3));
-                    if (has[a]) {
-                        const size_t p = size_t(cbase) + size_t(a) * P + c + __popc(hm & lt);
-                        s_ll[p] = lo[a];
-                        s_uu[p] = hi[a];
-                        s_meta[p] = m;
+                for (int a = 1; a <= 4; ++a) {
+                    const int ch = o == 0 ? complement(a) : a;
+                    const idx_t lo = f.Cf[ch] + pick4(rl, ch);
+                    const idx_t hi = f.Cf[ch] + pick4(ru, ch) - 1;
+                    const bool has = ext && lo <= hi;
+                    const unsigned am = __ballot_sync(0xffffffffu, has);
+                    int& c = a == 1 ? c0 : (a == 2 ? c1 : (a == 3 ? c2 : c3));
+                    if (has) {
+                        const int p = int(cbase) + (a - 1) * P + c + __popc(am & lt);
+                        W.ll[p] = lo;
+                        W.uu[p] = hi;
+                        W.meta[p] = m;
                     }
-                    c += __popc(hm);
+                    c += __popc(am);
                 }
             }
             __syncwarp();
-            // pack the sets back to back (each chunk read before it is written: destination <= source)
+            if (found) {
+                // the reference's loop k = lll .. uuu (k < uuu + 1): no iteration when uuu + 1 wraps
+                const idx_t endk = uuu + 1;
+                const idx_t cnt = endk > lll ? endk - lll : 0;
+                const int etype = meta_type(em_meta), elen = meta_len(em_meta);
+                const idx_t* rix = fm[cand_index(etype)].reads_index;
+                for (idx_t kb = 0; kb < cnt; kb += 32) {
+                    const bool act = kb + lane < cnt;
+                    idx_t r = self;
+                    if (act) r = __ldg(rix + (lll + kb + lane));
+                    const bool em = act && r != self;
+                    const unsigned emm = __ballot_sync(0xffffffffu, em);
+                    const int k = __popc(emm);
+                    if (side_count + k > 65535) return ERR_TOO_MANY;
+                    if (ne + k > S.ebcap) return OVF_EDGES;
+                    if (em) {
+                        const size_t pe = ebase + ne + __popc(emm & lt);
+                        S.e_dest[pe] = r;
+                        S.e_trans[pe] = F.trans;
+                        S.e_meta[pe] = pack_meta(elen, etype);
+                    }
+                    ne += k;
+                    side_count += k;
+                }
+                if (cnt > 0) {   // flag: this branch is finished
+                    if (level == 0) return OVF_NONE;
+                    --level;
+                    continue;
+                }
+            }
+            // pack the four sets back to back (each chunk read before it is written: dst <= src)
             int run = c0;
-            const int cs[3] = {c1, c2, c3};
             #pragma unroll
             for (int a = 1; a < 4; ++a) {
-                const int ca = cs[a - 1];
+                const int ca = a == 1 ? c1 : (a == 2 ? c2 : c3);
                 if (run != a * P) {
                     for (int jb = 0; jb < ca; jb += 32) {
                         const int j = jb + lane;
                         idx_t x = 0, y = 0;
                         uint32_t z = 0;
                         if (j < ca) {
-                            const size_t src = size_t(cbase) + size_t(a) * P + j;
-                            x = s_ll[src];
-                            y = s_uu[src];
-                            z = s_meta[src];
+                            const int src = int(cbase) + a * P + j;
+                            x = W.ll[src];
+                            y = W.uu[src];
+                            z = W.meta[src];
                         }
                         __syncwarp();
                         if (j < ca) {
-                            const size_t dst = size_t(cbase) + run + j;
-                            s_ll[dst] = x;
-                            s_uu[dst] = y;
-                            s_meta[dst] = z;
+                            const int dst = int(cbase) + run + j;
+                            W.ll[dst] = x;
+                            W.uu[dst] = y;
+                            W.meta[dst] = z;
                         }
                         __syncwarp();
                     }
@@ -751,8 +747,8 @@ __device__ int warp_reduce_side(const SearchArgs& A, const FmView* fm, idx_t sel
         int maxl = 0;
         uint32_t tr = 0;
         for (int i = lane; i < G.size; i += 32) {
-            maxl = max(maxl, meta_len(s_meta[G.pos + i]));
-            tr += uint32_t(s_uu[G.pos + i] - s_ll[G.pos + i] + 1);
+            maxl = max(maxl, meta_len(W.meta[G.pos + i]));
+            tr += uint32_t(W.uu[G.pos + i] - W.ll[G.pos + i] + 1);
         }
         G.maxlen = uint16_t(warp_max(maxl));
         G.trans = int32_t(warp_sum(tr));
@@ -773,6 +769,8 @@ __global__ void __launch_bounds__(128) k_search_fast(SearchArgs A, SearchOut O, 
     extern __shared__ uint32_t s_reads[];
     __shared__ FmView s_fm[2];
     __shared__ WFrame s_fr[kWarpsPerCta][kWarpFrames];
+    __shared__ idx_t s_sll[kWarpsPerCta][kSmemStack], s_suu[kWarpsPerCta][kSmemStack];
+    __shared__ uint32_t s_smeta[kWarpsPerCta][kSmemStack];
     __shared__ int s_n[kWarpsPerCta][32][4];
     __shared__ int32_t s_olp[kWarpsPerCta][32][2];
     __shared__ int s_st[kWarpsPerCta][32];
@@ -784,8 +782,8 @@ __global__ void __launch_bounds__(128) k_search_fast(SearchArgs A, SearchOut O, 
     const size_t nw = size_t(gridDim.x) * kWarpsPerCta;
     const int M = A.L - A.t;
     const size_t cbase_w = gw * 32 * 4 * size_t(M);        // level-0 candidates of this warp
-    const size_t sbase_w = gw * size_t(S.scap);            // DFS stack of this warp
     const size_t ebase_w = gw * 32 * size_t(S.ebcap);      // edge slots of this warp
+    const WarpStack W{s_sll[wid], s_suu[wid], s_smeta[wid]};
     uint32_t probes = 0;
     for (size_t batch = gw; batch * 32 < size_t(A.num_reads); batch += nw) {
         const size_t r = batch * 32 + lane;
@@ -830,16 +828,16 @@ __global__ void __launch_bounds__(128) k_search_fast(SearchArgs A, SearchOut O, 
                 if (s_olp[wid][j][side] == 0) continue;   // src/string_graph.c:824, 828
                 const int na = s_n[wid][j][2 * side], nb = s_n[wid][j][2 * side + 1];
                 const int n0 = na + nb;
-                if (n0 > S.scap) { st = OVF_STACK; break; }
+                if (n0 > kSmemStack) { st = OVF_STACK; break; }
                 for (int i = lane; i < n0; i += 32) {
                     const size_t src = cb + (i < na ? size_t(2 * side) * M + i : size_t(2 * side + 1) * M + (i - na));
-                    S.s_ll[sbase_w + i] = S.c_ll[src];
-                    S.s_uu[sbase_w + i] = S.c_uu[src];
-                    S.s_meta[sbase_w + i] = S.c_meta[src];
+                    W.ll[i] = S.c_ll[src];
+                    W.uu[i] = S.c_uu[src];
+                    W.meta[i] = S.c_meta[src];
                 }
                 __syncwarp();
                 int sc = 0;
-                st = warp_reduce_side(A, s_fm, self, S, sbase_w, n0, s_fr[wid], eb, ne, sc, probes);
+                st = warp_reduce_side(A, s_fm, self, W, n0, s_fr[wid], S, eb, ne, sc, probes);
                 counts[side] = sc;
                 __syncwarp();
             }
@@ -906,18 +904,18 @@ int search_fast_blocks(int L, int num_sms) {
     return per_sm * num_sms;
 }
 
-size_t warp_scratch_bytes(int L, int t, size_t nwarps, int scap, int ebcap) {
+size_t warp_scratch_bytes(int L, int t, size_t nwarps, int ebcap) {
     const size_t M = size_t(L - t);
-    const size_t cand = nwarps * 32 * 4 * M, stk = nwarps * size_t(scap), edg = nwarps * 32 * size_t(ebcap);
-    return (cand + stk) * (2 * sizeof(idx_t) + 4) + edg * (sizeof(idx_t) + 8) + 16 * 256;
+    const size_t cand = nwarps * 32 * 4 * M, edg = nwarps * 32 * size_t(ebcap);
+    return cand * (2 * sizeof(idx_t) + 4) + edg * (sizeof(idx_t) + 8) + 16 * 256;
 }
 
 cudaError_t search_fast(const SearchArgs& a, const SearchOut& o, int blocks, void* scratch, size_t scratch_bytes,
-                        int scap, int ebcap, cudaStream_t st) {
+                        int ebcap, cudaStream_t st) {
     const size_t nwarps = size_t(blocks) * kWarpsPerCta;
-    if (scratch_bytes < warp_scratch_bytes(a.L, a.t, nwarps, scap, ebcap)) return cudaErrorInvalidValue;
+    if (scratch_bytes < warp_scratch_bytes(a.L, a.t, nwarps, ebcap)) return cudaErrorInvalidValue;
     const size_t M = size_t(a.L - a.t);
-    const size_t cand = nwarps * 32 * 4 * M, stk = nwarps * size_t(scap), edg = nwarps * 32 * size_t(ebcap);
+    const size_t cand = nwarps * 32 * 4 * M, edg = nwarps * 32 * size_t(ebcap);
     char* p = static_cast<char*>(scratch);
     auto take = [&](size_t bytes) {
         char* q = p;
@@ -928,13 +926,9 @@ cudaError_t search_fast(const SearchArgs& a, const SearchOut& o, int blocks, voi
     S.c_ll = reinterpret_cast<idx_t*>(take(cand * sizeof(idx_t)));
     S.c_uu = reinterpret_cast<idx_t*>(take(cand * sizeof(idx_t)));
     S.c_meta = reinterpret_cast<uint32_t*>(take(cand * 4));
-    S.s_ll = reinterpret_cast<idx_t*>(take(stk * sizeof(idx_t)));
-    S.s_uu = reinterpret_cast<idx_t*>(take(stk * sizeof(idx_t)));
-    S.s_meta = reinterpret_cast<uint32_t*>(take(stk * 4));
     S.e_dest = reinterpret_cast<idx_t*>(take(edg * sizeof(idx_t)));
     S.e_trans = reinterpret_cast<int32_t*>(take(edg * 4));
     S.e_meta = reinterpret_cast<uint32_t*>(take(edg * 4));
-    S.scap = scap;
     S.ebcap = ebcap;
     const int words = (a.L + 15) / 16;
     size_t smem = size_t(words) * 32 * kWarpsPerCta * sizeof(uint32_t);
