@@ -419,6 +419,299 @@ __global__ void k_copy_vals(const V* __restrict__ v, size_t n, idx_t* __restrict
     for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) sa[i] = idx_t(v[i]);
 }
 
+// ------------------------------------------------------------------------------ group refinement
+//
+// After the sort on 29-base keys, every group of equal keys whose suffixes all go on past base 29
+// still has to be ordered.  At read coverage c such groups hold about c suffixes, so instead of
+// more whole-array passes each group is finished where it lies: every suffix loads the rest of
+// its bases as W 64-bit words (bases past its end read as A) and the group is sorted by
+// (words, suffix length, position) -- the end-of-read-lowest order, ties by position.  Groups of
+// up to 32 suffixes are sorted by one warp in registers, up to 1024 by one CTA in shared memory,
+// larger ones by one CTA in global scratch; all with bitonic networks.
+
+constexpr int kRefineMaxWords = 8;          // suffixes up to 29 + 256 bases
+constexpr int kGroupCta = 1024;             // largest group sorted in shared memory
+
+struct GroupLists {
+    unsigned long long* small;              // (start << 24) | size, 2 <= size <= 32
+    unsigned long long* mid;                // (start << 24) | size, 33 <= size <= 1024
+    unsigned long long* big;                // start, size pairs
+    unsigned long long* counts;             // [3]
+    size_t cap_small, cap_mid, cap_big;
+};
+
+__global__ void k_group_lists(const uint64_t* __restrict__ key, size_t n, GroupLists G) {
+    const size_t stride = size_t(gridDim.x) * blockDim.x;
+    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const uint64_t k = key[i];
+        if ((k & 63) != uint64_t(kHead)) continue;            // suffix ends within the first 29 bases
+        if (i > 0 && key[i - 1] == k) continue;               // not the first of its group
+        size_t e = i + 1;
+        while (e < n && key[e] == k) ++e;
+        const size_t m = e - i;
+        if (m < 2) continue;
+        if (m <= 32) {
+            unsigned long long s = atomicAdd(&G.counts[0], 1ull);
+            if (s < G.cap_small) G.small[s] = (uint64_t(i) << 24) | m;
+        } else if (m <= size_t(kGroupCta)) {
+            unsigned long long s = atomicAdd(&G.counts[1], 1ull);
+            if (s < G.cap_mid) G.mid[s] = (uint64_t(i) << 24) | m;
+        } else {
+            unsigned long long s = atomicAdd(&G.counts[2], 1ull);
+            if (s < G.cap_big) {
+                G.big[2 * s] = i;
+                G.big[2 * s + 1] = m;
+            }
+        }
+    }
+}
+
+// the W words of bases 29, 29+32, ... of the suffix at p (length m_len), zero past its end
+template <int W>
+__device__ __forceinline__ void suffix_words(const uint64_t* __restrict__ pk, size_t p, int m_len, uint64_t w[W]) {
+    #pragma unroll
+    for (int j = 0; j < W; ++j) {
+        const int rem = m_len - kHead - 32 * j;
+        uint64_t x = 0;
+        if (rem > 0) {
+            x = window(pk, p + kHead + 32 * size_t(j));
+            if (rem < 32) x &= ~uint64_t(0) << (64 - 2 * rem);
+        }
+        w[j] = x;
+    }
+}
+
+template <int W>
+__device__ __forceinline__ bool tuple_less(const uint64_t a[W], uint64_t alen, uint64_t apos, const uint64_t b[W],
+                                           uint64_t blen, uint64_t bpos) {
+    #pragma unroll
+    for (int j = 0; j < W; ++j)
+        if (a[j] != b[j]) return a[j] < b[j];
+    if (alen != blen) return alen < blen;
+    return apos < bpos;
+}
+
+template <int W>
+__global__ void k_refine_warp(const unsigned long long* __restrict__ list, const unsigned long long* __restrict__ cnt,
+                              const uint64_t* __restrict__ pk, idx_t L, idx_t* __restrict__ val) {
+    const int lane = threadIdx.x & 31;
+    const size_t warp = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const size_t nwarps = (size_t(gridDim.x) * blockDim.x) >> 5;
+    const size_t groups = *cnt;
+    for (size_t g = warp; g < groups; g += nwarps) {
+        const unsigned long long e = list[g];
+        const size_t start = size_t(e >> 24);
+        const int m = int(e & 0xffffff);
+        uint64_t w[W], len, pos;
+        if (lane < m) {
+            pos = uint64_t(val[start + lane]);
+            len = uint64_t(L - idx_t(pos % L));
+            suffix_words<W>(pk, size_t(pos), int(len), w);
+        } else {
+            #pragma unroll
+            for (int j = 0; j < W; ++j) w[j] = ~uint64_t(0);
+            len = ~uint64_t(0);
+            pos = ~uint64_t(0);
+        }
+        #pragma unroll
+        for (int k = 2; k <= 32; k <<= 1) {
+            #pragma unroll
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                uint64_t ow[W];
+                #pragma unroll
+                for (int q = 0; q < W; ++q) ow[q] = __shfl_xor_sync(0xffffffffu, w[q], j);
+                const uint64_t olen = __shfl_xor_sync(0xffffffffu, len, j);
+                const uint64_t opos = __shfl_xor_sync(0xffffffffu, pos, j);
+                const bool keep_min = ((lane & j) == 0) == ((lane & k) == 0);
+                const bool other_less = tuple_less<W>(ow, olen, opos, w, len, pos);
+                if (keep_min == other_less) {
+                    #pragma unroll
+                    for (int q = 0; q < W; ++q) w[q] = ow[q];
+                    len = olen;
+                    pos = opos;
+                }
+            }
+        }
+        if (lane < m) val[start + lane] = idx_t(pos);
+    }
+}
+
+// bitonic sort of one group of m suffixes held as columns: words w[j][P2], len[P2], pos[P2]
+template <int W>
+__device__ void cta_bitonic(uint64_t* cols, int P2) {
+    uint64_t* lenc = cols + size_t(W) * P2;
+    uint64_t* posc = lenc + P2;
+    for (int k = 2; k <= P2; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < P2; i += blockDim.x) {
+                const int o = i ^ j;
+                if (o <= i) continue;
+                uint64_t a[W], b[W];
+                #pragma unroll
+                for (int q = 0; q < W; ++q) {
+                    a[q] = cols[size_t(q) * P2 + i];
+                    b[q] = cols[size_t(q) * P2 + o];
+                }
+                const bool asc = (i & k) == 0;
+                const bool b_less = tuple_less<W>(b, lenc[o], posc[o], a, lenc[i], posc[i]);
+                if (b_less == asc) {
+                    #pragma unroll
+                    for (int q = 0; q < W; ++q) {
+                        cols[size_t(q) * P2 + i] = b[q];
+                        cols[size_t(q) * P2 + o] = a[q];
+                    }
+                    const uint64_t tl = lenc[i], tp = posc[i];
+                    lenc[i] = lenc[o];
+                    posc[i] = posc[o];
+                    lenc[o] = tl;
+                    posc[o] = tp;
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+template <int W>
+__device__ void cta_load_group(uint64_t* cols, int P2, size_t start, int m, const uint64_t* __restrict__ pk, idx_t L,
+                               const idx_t* __restrict__ val) {
+    uint64_t* lenc = cols + size_t(W) * P2;
+    uint64_t* posc = lenc + P2;
+    for (int i = threadIdx.x; i < P2; i += blockDim.x) {
+        uint64_t w[W];
+        uint64_t len = ~uint64_t(0), pos = ~uint64_t(0);
+        if (i < m) {
+            pos = uint64_t(val[start + i]);
+            len = uint64_t(L - idx_t(pos % L));
+            suffix_words<W>(pk, size_t(pos), int(len), w);
+        } else {
+            #pragma unroll
+            for (int q = 0; q < W; ++q) w[q] = ~uint64_t(0);
+        }
+        #pragma unroll
+        for (int q = 0; q < W; ++q) cols[size_t(q) * P2 + i] = w[q];
+        lenc[i] = len;
+        posc[i] = pos;
+    }
+    __syncthreads();
+}
+
+template <int W>
+__global__ void k_refine_cta(const unsigned long long* __restrict__ list, const unsigned long long* __restrict__ cnt,
+                             const uint64_t* __restrict__ pk, idx_t L, idx_t* __restrict__ val) {
+    extern __shared__ uint64_t s_cols[];
+    const size_t groups = *cnt;
+    for (size_t g = blockIdx.x; g < groups; g += gridDim.x) {
+        const unsigned long long e = list[g];
+        const size_t start = size_t(e >> 24);
+        const int m = int(e & 0xffffff);
+        int P2 = 32;
+        while (P2 < m) P2 <<= 1;
+        cta_load_group<W>(s_cols, P2, start, m, pk, L, val);
+        cta_bitonic<W>(s_cols, P2);
+        const uint64_t* posc = s_cols + size_t(W + 1) * P2;
+        for (int i = threadIdx.x; i < m; i += blockDim.x) val[start + i] = idx_t(posc[i]);
+        __syncthreads();
+    }
+}
+
+// one CTA per big group, columns in global scratch at cols + offset[g]
+template <int W>
+__global__ void k_refine_big(const unsigned long long* __restrict__ big, const unsigned long long* __restrict__ offs,
+                             const uint64_t* __restrict__ pk, idx_t L, idx_t* __restrict__ val, uint64_t* cols) {
+    const size_t g = blockIdx.x;
+    const size_t start = size_t(big[2 * g]);
+    const int m = int(big[2 * g + 1]);
+    int P2 = 32;
+    while (P2 < m) P2 <<= 1;
+    uint64_t* c = cols + offs[g];
+    cta_load_group<W>(c, P2, start, m, pk, L, val);
+    cta_bitonic<W>(c, P2);
+    const uint64_t* posc = c + size_t(W + 1) * P2;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) val[start + i] = idx_t(posc[i]);
+}
+
+template <int W>
+static int refine_groups_w(const GroupLists& G, unsigned long long n_small, unsigned long long n_mid,
+                           const std::vector<unsigned long long>& big, const uint64_t* pk, idx_t L, idx_t* val,
+                           uint64_t* cols, size_t cols_cap, cudaStream_t st) {
+    if (n_small) {
+        unsigned g = unsigned(std::min<unsigned long long>((n_small + 7) / 8, 152ull * 64));
+        { k_refine_warp<W><<<g, 256, 0, st>>>(G.small, G.counts + 0, pk, L, val); note_launch(); }
+    }
+    if (n_mid) {
+        const size_t smem = size_t(W + 2) * kGroupCta * sizeof(uint64_t);
+        cudaFuncSetAttribute(k_refine_cta<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        unsigned g = unsigned(std::min<unsigned long long>(n_mid, 152ull * 8));
+        { k_refine_cta<W><<<g, 512, smem, st>>>(G.mid, G.counts + 1, pk, L, val); note_launch(); }
+    }
+    // big groups in rounds that fit the column scratch
+    size_t i = 0;
+    const size_t nb = big.size() / 2;
+    std::vector<unsigned long long> offs;
+    while (i < nb) {
+        offs.clear();
+        size_t used = 0, j = i;
+        for (; j < nb; ++j) {
+            size_t P2 = 32;
+            while (P2 < big[2 * j + 1]) P2 <<= 1;
+            const size_t need = size_t(W + 2) * P2;
+            if (used + need > cols_cap) break;
+            offs.push_back(used);
+            used += need;
+        }
+        if (j == i) return -1;   // one group alone does not fit: caller falls back
+        // offsets and the group entries of this round go behind the columns
+        unsigned long long* dev_meta = reinterpret_cast<unsigned long long*>(cols + used);
+        if ((used + offs.size() * 3 + 8) > cols_cap) return -1;
+        cudaMemcpyAsync(dev_meta, offs.data(), offs.size() * 8, cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(dev_meta + offs.size(), big.data() + 2 * i, (j - i) * 16, cudaMemcpyHostToDevice, st);
+        { k_refine_big<W><<<unsigned(j - i), 1024, 0, st>>>(dev_meta + offs.size(), dev_meta, pk, L, val, cols);
+          note_launch(); }
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return int(e);
+        i = j;
+    }
+    return int(cudaGetLastError());
+}
+
+// Returns 0 when every group was refined, -1 when the caller must fall back to prefix doubling.
+static int refine_groups(const uint64_t* key, idx_t* val, size_t n, idx_t L, const uint64_t* pk, uint64_t* lists_mem,
+                         uint64_t* cols, size_t cols_cap, unsigned long long* counters, cudaStream_t st) {
+    const int W = int((2 * (size_t(L) - kHead) + 63) / 64);
+    if (W < 1 || W > kRefineMaxWords) return -1;
+    GroupLists G;
+    G.cap_small = n / 2 + 1;
+    G.cap_mid = n / 33 + 1;
+    G.cap_big = n / 1025 + 1;
+    G.small = reinterpret_cast<unsigned long long*>(lists_mem);
+    G.mid = G.small + G.cap_small;
+    G.big = G.mid + G.cap_mid;
+    G.counts = counters;
+    cudaMemsetAsync(counters, 0, 3 * sizeof(unsigned long long), st);
+    { k_group_lists<<<grid_for(n, 256), 256, 0, st>>>(key, n, G); note_launch(); }
+    unsigned long long c[3];
+    cudaMemcpyAsync(c, counters, sizeof c, cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return int(e);
+    std::vector<unsigned long long> big(2 * c[2]);
+    if (c[2]) {
+        cudaMemcpyAsync(big.data(), G.big, big.size() * 8, cudaMemcpyDeviceToHost, st);
+        e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return int(e);
+    }
+    switch (W) {
+        case 1: return refine_groups_w<1>(G, c[0], c[1], big, pk, L, val, cols, cols_cap, st);
+        case 2: return refine_groups_w<2>(G, c[0], c[1], big, pk, L, val, cols, cols_cap, st);
+        case 3: return refine_groups_w<3>(G, c[0], c[1], big, pk, L, val, cols, cols_cap, st);
+        case 4: return refine_groups_w<4>(G, c[0], c[1], big, pk, L, val, cols, cols_cap, st);
+        case 5: return refine_groups_w<5>(G, c[0], c[1], big, pk, L, val, cols, cols_cap, st);
+        case 6: return refine_groups_w<6>(G, c[0], c[1], big, pk, L, val, cols, cols_cap, st);
+        case 7: return refine_groups_w<7>(G, c[0], c[1], big, pk, L, val, cols, cols_cap, st);
+        default: return refine_groups_w<8>(G, c[0], c[1], big, pk, L, val, cols, cols_cap, st);
+    }
+}
+
 // ------------------------------------------------------------------------------ driver
 
 static size_t al(size_t b) { return (b + 255) & ~size_t(255); }
@@ -454,6 +747,25 @@ int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa
     { k_init_keys<<<grid_for(n, 256), 256, 0, st>>>(pk, n, idx_t(L), ka, va); note_launch(); }
     int rc = radix_sort_pairs<idx_t>(&ka, &va, &kb, &vb, n, 0, 64, rtmp, radix_tmp_bytes(n), st);
     if (rc) return rc;
+    if (size_t(L) <= size_t(kHead)) {   // every suffix fits in its key: already in final order
+        { k_copy_vals<idx_t><<<grid_for(n, 256), 256, 0, st>>>(va, n, sa); note_launch(); }
+        return int(cudaGetLastError());
+    }
+    {
+        // finish the groups where they lie; lists go to kb, big-group columns to vb + rank
+        uint64_t* cols = reinterpret_cast<uint64_t*>(vb);
+        const size_t cols_cap = (al(n * sizeof(idx_t)) + al(n * sizeof(uint32_t))) / sizeof(uint64_t);
+        rc = refine_groups(ka, va, n, idx_t(L), pk, kb, cols, cols_cap, tcnt, st);
+        if (rc > 0) return rc;
+        if (rc == 0) {
+            { k_copy_vals<idx_t><<<grid_for(n, 256), 256, 0, st>>>(va, n, sa); note_launch(); }
+            return int(cudaGetLastError());
+        }
+        // a group too large for the scratch (or reads longer than 285 bases): prefix doubling
+        { k_init_keys<<<grid_for(n, 256), 256, 0, st>>>(pk, n, idx_t(L), ka, va); note_launch(); }
+        rc = radix_sort_pairs<idx_t>(&ka, &va, &kb, &vb, n, 0, 64, rtmp, radix_tmp_bytes(n), st);
+        if (rc) return rc;
+    }
     for (size_t h = kHead;; h *= 2) {
         { k_head_tiles<<<unsigned(tiles), HT_THREADS, 0, st>>>(ka, n, tmax, tcnt); note_launch(); }
         { k_head_carry<<<1, 1024, 0, st>>>(tmax, tcnt, tiles, groups); note_launch(); }
