@@ -532,9 +532,10 @@ struct WFrame {
     uint32_t pos, free, cbase;
     int32_t trans;
     uint16_t size, maxlen;
-    uint16_t csz[4];
     uint32_t next_a;
+    uint64_t csz4;      // sizes of the four extension sets, 16 bits each (A in the low bits)
 };
+__device__ __forceinline__ int csz_at(uint64_t c4, int i) { return int((c4 >> (16 * i)) & 0xffff); }
 
 // A warp's DFS stack in shared memory, struct of arrays.
 struct WarpStack {
@@ -586,7 +587,7 @@ __device__ int warp_reduce_side(const SearchArgs& A, const FmView* fm, idx_t sel
         f0.trans = 0;
         f0.size = uint16_t(n0);
         f0.maxlen = 0;
-        f0.csz[0] = f0.csz[1] = f0.csz[2] = f0.csz[3] = 0;
+        f0.csz4 = 0;
         f0.next_a = 1;
         fr[0] = f0;
     }
@@ -604,7 +605,7 @@ __device__ int warp_reduce_side(const SearchArgs& A, const FmView* fm, idx_t sel
             bool found = false;
             idx_t lll = 0, uuu = 0;
             uint32_t em_meta = 0;
-            int c0 = 0, c1 = 0, c2 = 0, c3 = 0;
+            int cs[4] = {0, 0, 0, 0};   // only indexed by unrolled constants: stays in registers
             for (int base = 0; base < P; base += 32) {
                 const int i = base + lane;
                 idx_t cl = 0, cu = 0;
@@ -647,16 +648,16 @@ __device__ int warp_reduce_side(const SearchArgs& A, const FmView* fm, idx_t sel
                     const idx_t hi = f.Cf[ch] + pick4(ru, ch) - 1;
                     const bool has = ext && lo <= hi;
                     const unsigned am = __ballot_sync(0xffffffffu, has);
-                    int& c = a == 1 ? c0 : (a == 2 ? c1 : (a == 3 ? c2 : c3));
                     if (has) {
-                        const int p = int(cbase) + (a - 1) * P + c + __popc(am & lt);
+                        const int p = int(cbase) + (a - 1) * P + cs[a - 1] + __popc(am & lt);
                         W.ll[p] = lo;
                         W.uu[p] = hi;
                         W.meta[p] = m;
                     }
-                    c += __popc(am);
+                    cs[a - 1] += __popc(am);
                 }
             }
+            const int c0 = cs[0], c1 = cs[1], c2 = cs[2], c3 = cs[3];
             __syncwarp();
             if (found) {
                 // the reference's loop k = lll .. uuu (k < uuu + 1): no iteration when uuu + 1 wraps
@@ -717,16 +718,13 @@ __device__ int warp_reduce_side(const SearchArgs& A, const FmView* fm, idx_t sel
                 run += ca;
             }
             F.cbase = cbase;
-            F.csz[0] = uint16_t(c0);
-            F.csz[1] = uint16_t(c1);
-            F.csz[2] = uint16_t(c2);
-            F.csz[3] = uint16_t(c3);
+            F.csz4 = uint64_t(c0) | (uint64_t(c1) << 16) | (uint64_t(c2) << 32) | (uint64_t(c3) << 48);
             F.next_a = 1;
             if (lane == 0) fr[level] = F;
             __syncwarp();
         }
         int a = int(F.next_a);
-        while (a <= 4 && F.csz[a - 1] == 0) ++a;
+        while (a <= 4 && csz_at(F.csz4, a - 1) == 0) ++a;
         if (a > 4) {
             if (level == 0) return OVF_NONE;
             --level;
@@ -736,14 +734,14 @@ __device__ int warp_reduce_side(const SearchArgs& A, const FmView* fm, idx_t sel
         uint32_t before = 0, all = 0;
         #pragma unroll
         for (int b = 0; b < 4; ++b) {
-            before += (b < a - 1) ? F.csz[b] : 0;
-            all += F.csz[b];
+            before += (b < a - 1) ? csz_at(F.csz4, b) : 0;
+            all += csz_at(F.csz4, b);
         }
         WFrame G;
         G.pos = F.cbase + before;
         G.free = F.cbase + all;        // below it: the parent's four sets, still pending
         G.cbase = 0;
-        G.size = F.csz[a - 1];
+        G.size = uint16_t(csz_at(F.csz4, a - 1));
         int maxl = 0;
         uint32_t tr = 0;
         for (int i = lane; i < G.size; i += 32) {
@@ -752,7 +750,7 @@ __device__ int warp_reduce_side(const SearchArgs& A, const FmView* fm, idx_t sel
         }
         G.maxlen = uint16_t(warp_max(maxl));
         G.trans = int32_t(warp_sum(tr));
-        G.csz[0] = G.csz[1] = G.csz[2] = G.csz[3] = 0;
+        G.csz4 = 0;
         G.next_a = 1;
         __syncwarp();
         if (lane == 0) {
@@ -823,8 +821,10 @@ __global__ void __launch_bounds__(128) k_search_fast(SearchArgs A, SearchOut O, 
             const size_t cb = cbase_w + size_t(j) * 4 * M;
             const size_t eb = ebase_w + size_t(j) * S.ebcap;
             int ne = 0, st = OVF_NONE;
-            int counts[2] = {0, 0};
-            for (int side = 0; side < 2 && st == OVF_NONE; ++side) {
+            int count_b = 0, count_f = 0;
+            #pragma unroll
+            for (int side = 0; side < 2; ++side) {
+                if (st != OVF_NONE) break;
                 if (s_olp[wid][j][side] == 0) continue;   // src/string_graph.c:824, 828
                 const int na = s_n[wid][j][2 * side], nb = s_n[wid][j][2 * side + 1];
                 const int n0 = na + nb;
@@ -838,13 +838,14 @@ __global__ void __launch_bounds__(128) k_search_fast(SearchArgs A, SearchOut O, 
                 __syncwarp();
                 int sc = 0;
                 st = warp_reduce_side(A, s_fm, self, W, n0, s_fr[wid], S, eb, ne, sc, probes);
-                counts[side] = sc;
+                if (side == 0) count_b = sc;
+                else count_f = sc;
                 __syncwarp();
             }
             if (lane == 0) {
                 s_st[wid][j] = st;
-                s_ne[wid][j][0] = counts[0];
-                s_ne[wid][j][1] = counts[1];
+                s_ne[wid][j][0] = count_b;
+                s_ne[wid][j][1] = count_f;
             }
             __syncwarp();
         }
