@@ -43,15 +43,22 @@ struct SearchArgs {
     int seed_k;                 // k-mer seed depth (0 = start at depth 1 from C[])
 };
 
-// Global scratch of the warp-cooperative fast kernel, per warp: level-0 candidates of 32 reads
-// (4 kinds x (L - t) slots each) and ebcap edge slots per read.  (The DFS stack itself is in
-// shared memory.)
+// Global scratch of the fast kernel, per warp of 32 reads: level-0 candidates (4 kinds x (L - t)
+// slots per read), ebcap edge slots per read, and per (read, side) task a DFS stack, sparse
+// extension slots, emission bounds and DFS frames.
+struct TFrame;
 struct WarpScratch {
     idx_t *c_ll, *c_uu;
     uint32_t* c_meta;
     idx_t* e_dest;
     int32_t* e_trans;
     uint32_t* e_meta;
+    idx_t *t_ll, *t_uu;
+    uint32_t* t_meta;
+    idx_t *x_ll, *x_uu;
+    uint32_t* x_meta;
+    idx_t *em_l, *em_u;
+    TFrame* frames;
     int ebcap;
 };
 size_t warp_scratch_bytes(int L, int t, size_t nwarps, int ebcap);

@@ -525,268 +525,111 @@ __device__ __forceinline__ void add_probes(const SearchOut& O, uint32_t probes) 
 // Phase C: each lane publishes its read (edge-pool reservation, copy, per-read counts).
 
 constexpr int kWarpsPerCta = 4;
-constexpr int kWarpFrames = 48;     // DFS levels per warp (deeper reads go to the wide kernel)
-constexpr int kSmemStack = 384;     // intervals per warp in shared memory
-
-struct WFrame {
-    uint32_t pos, free, cbase;
-    int32_t trans;
-    uint16_t size, maxlen;
-    uint32_t next_a;
-    uint64_t csz4;      // sizes of the four extension sets, 16 bits each (A in the low bits)
-};
-__device__ __forceinline__ int csz_at(uint64_t c4, int i) { return int((c4 >> (16 * i)) & 0xffff); }
-
-// A warp's DFS stack in shared memory, struct of arrays.
-struct WarpStack {
-    idx_t* ll;
-    idx_t* uu;
-    uint32_t* meta;
-};
+constexpr int kTaskCap = 512;       // stack intervals per (read, side) task
+constexpr int kTaskFrames = 48;     // DFS levels per task (deeper reads go to the wide kernel)
+constexpr int kPMax = 128;          // intervals of one level of one task
 
 __device__ __forceinline__ uint32_t pack_meta(int len, int type) { return uint32_t(len) | (uint32_t(type) << 16); }
 __device__ __forceinline__ int meta_len(uint32_t m) { return int(m & 0xffff); }
 __device__ __forceinline__ int meta_type(uint32_t m) { return int(m >> 16); }
+__device__ __forceinline__ int csz_at(uint64_t c4, int i) { return int((c4 >> (16 * i)) & 0xffff); }
 
-template <class T> __device__ __forceinline__ T warp_max(T v) {
-    #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
-    return v;
-}
-template <class T> __device__ __forceinline__ T warp_sum(T v) {
-    #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-__device__ __forceinline__ idx_t shfl_idx(idx_t v, int src) {
-#ifdef PQ_IDX64
-    return __shfl_sync(0xffffffffu, (unsigned long long)v, src);
-#else
-    return __shfl_sync(0xffffffffu, v, src);
-#endif
+// One DFS level of one task (the reference's recursion frame of extract_*_edges).
+struct TFrame {
+    uint32_t pos;       // first interval of this level in the task's stack
+    uint32_t free;      // first stack slot this level may use for its extension sets
+    uint32_t cbase;     // first slot of the four extension sets (back to back, A..T)
+    int32_t trans;      // sum of this level's interval sizes (path_t.trans of its edges)
+    uint16_t size, maxlen;
+    uint32_t next_a;
+    uint64_t csz4;      // sizes of the four sets, 16 bits each (A lowest)
+    uint64_t cml4;      // largest overlap length in each set, 16 bits each
+    int32_t ctr[4];     // interval-size sum of each set
+};
+
+// Shared memory of one warp for the level-synchronous DFS of its 32 tasks.
+struct MultiSmem {
+    unsigned long long mask[32][4][2];   // extension present, by entry index (kPMax bits)
+    int hit[32];                         // first entry that completes a read with $ rows
+    int cml[32][4];
+    unsigned ctr[32][4];
+    int setoff[32][4];
+    int pref[33];
+    uint32_t pos[32], cbase[32];
+    int lvl[32], chk[32], size[32], na[32];
+};
+
+__device__ __forceinline__ int popc128(const unsigned long long m[2]) { return __popcll(m[0]) + __popcll(m[1]); }
+__device__ __forceinline__ int popc128_below(const unsigned long long m[2], int i) {
+    if (i < 64) return __popcll(m[0] & ((1ull << i) - 1));
+    return __popcll(m[0]) + __popcll(m[1] & ((i == 64) ? 0ull : ((1ull << (i - 64)) - 1)));
 }
 
-// extract_fw_edges / extract_bw_edges for one (read, side), cooperatively by one warp, with the
-// stack in shared memory.  Level 0 is already in W[0, n0).  On each level every interval's two
-// blocks are loaded once and serve both the emission check (the `$` counts at its ends) and the
-// four extensions; the first interval (in order) that completes a read and holds `$` rows is
-// found with a ballot.  If the level emits, the extensions computed with it are simply dropped,
-// as the reference never computes them.  Edges go to the read's scratch slots [ne, ...).
-// Returns OVF_* or ERR_* (uniform across the warp).
-__device__ int warp_reduce_side(const SearchArgs& A, const FmView* fm, idx_t self, const WarpStack& W, int n0,
-                                WFrame* fr, const WarpScratch& S, size_t ebase, int& ne, int& side_count,
-                                uint32_t& probes) {
-    const int L = A.L;
+// exclusive prefix of v over the warp into pref[0..32] (pref[32] = total), returns the total
+__device__ __forceinline__ int warp_prefix(int v, int* pref) {
     const int lane = threadIdx.x & 31;
-    const unsigned lt = (1u << lane) - 1;
-    if (lane == 0) {
-        WFrame f0;
-        f0.pos = 0;
-        f0.free = uint32_t(n0);
-        f0.cbase = 0;
-        f0.trans = 0;
-        f0.size = uint16_t(n0);
-        f0.maxlen = 0;
-        f0.csz4 = 0;
-        f0.next_a = 1;
-        fr[0] = f0;
+    int x = v;
+    #pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
     }
+    pref[lane] = x - v;
+    if (lane == 31) pref[32] = x;
     __syncwarp();
-    int level = 0;
-    bool entering = true;
-    while (true) {
-        WFrame F = fr[level];
-        if (entering) {
-            entering = false;
-            const bool chk = int(F.maxlen) + level == L;
-            const int P = F.size;
-            const uint32_t cbase = F.free;
-            if (int(cbase) + 4 * P > kSmemStack) return OVF_STACK;
-            bool found = false;
-            idx_t lll = 0, uuu = 0;
-            uint32_t em_meta = 0;
-            int cs[4] = {0, 0, 0, 0};   // only indexed by unrolled constants: stays in registers
-            for (int base = 0; base < P; base += 32) {
-                const int i = base + lane;
-                idx_t cl = 0, cu = 0;
-                uint32_t m = 0;
-                bool ext = false, ends = false;
-                if (i < P) {
-                    cl = W.ll[F.pos + i];
-                    cu = W.uu[F.pos + i];
-                    m = W.meta[F.pos + i];
-                    ext = idx_t(cu - cl + 1) != 0;   // a wrapped [0, all-ones] interval is kept, never extended
-                    ends = chk && meta_len(m) + level == L;
-                }
-                const int o = cand_index(meta_type(m));
-                const FmView& f = fm[o];
-                idx_t rl[4] = {0, 0, 0, 0}, ru[4] = {0, 0, 0, 0};
-                if (ext || ends) {
-                    rank_all(f, cl, rl);
-                    rank_all(f, cu + 1, ru);
-                    probes += 2;
-                }
-                bool hit = false;
-                idx_t ea = 0, eb2 = 0;
-                if (ends) {
-                    ea = f.Cf[0] + (cl - (rl[0] + rl[1] + rl[2] + rl[3]));
-                    eb2 = f.Cf[0] + ((cu + 1) - (ru[0] + ru[1] + ru[2] + ru[3])) - 1;
-                    hit = ea <= eb2;
-                }
-                const unsigned hm = __ballot_sync(0xffffffffu, hit);
-                if (hm && !found) {
-                    const int src = __ffs(hm) - 1;
-                    lll = shfl_idx(ea, src);
-                    uuu = shfl_idx(eb2, src);
-                    em_meta = __shfl_sync(0xffffffffu, m, src);
-                    found = true;
-                }
-                #pragma unroll
-                for (int a = 1; a <= 4; ++a) {
-                    const int ch = o == 0 ? complement(a) : a;
-                    const idx_t lo = f.Cf[ch] + pick4(rl, ch);
-                    const idx_t hi = f.Cf[ch] + pick4(ru, ch) - 1;
-                    const bool has = ext && lo <= hi;
-                    const unsigned am = __ballot_sync(0xffffffffu, has);
-                    if (has) {
-                        const int p = int(cbase) + (a - 1) * P + cs[a - 1] + __popc(am & lt);
-                        W.ll[p] = lo;
-                        W.uu[p] = hi;
-                        W.meta[p] = m;
-                    }
-                    cs[a - 1] += __popc(am);
-                }
-            }
-            const int c0 = cs[0], c1 = cs[1], c2 = cs[2], c3 = cs[3];
-            __syncwarp();
-            if (found) {
-                // the reference's loop k = lll .. uuu (k < uuu + 1): no iteration when uuu + 1 wraps
-                const idx_t endk = uuu + 1;
-                const idx_t cnt = endk > lll ? endk - lll : 0;
-                const int etype = meta_type(em_meta), elen = meta_len(em_meta);
-                const idx_t* rix = fm[cand_index(etype)].reads_index;
-                for (idx_t kb = 0; kb < cnt; kb += 32) {
-                    const bool act = kb + lane < cnt;
-                    idx_t r = self;
-                    if (act) r = __ldg(rix + (lll + kb + lane));
-                    const bool em = act && r != self;
-                    const unsigned emm = __ballot_sync(0xffffffffu, em);
-                    const int k = __popc(emm);
-                    if (side_count + k > 65535) return ERR_TOO_MANY;
-                    if (ne + k > S.ebcap) return OVF_EDGES;
-                    if (em) {
-                        const size_t pe = ebase + ne + __popc(emm & lt);
-                        S.e_dest[pe] = r;
-                        S.e_trans[pe] = F.trans;
-                        S.e_meta[pe] = pack_meta(elen, etype);
-                    }
-                    ne += k;
-                    side_count += k;
-                }
-                if (cnt > 0) {   // flag: this branch is finished
-                    if (level == 0) return OVF_NONE;
-                    --level;
-                    continue;
-                }
-            }
-            // pack the four sets back to back (each chunk read before it is written: dst <= src)
-            int run = c0;
-            #pragma unroll
-            for (int a = 1; a < 4; ++a) {
-                const int ca = a == 1 ? c1 : (a == 2 ? c2 : c3);
-                if (run != a * P) {
-                    for (int jb = 0; jb < ca; jb += 32) {
-                        const int j = jb + lane;
-                        idx_t x = 0, y = 0;
-                        uint32_t z = 0;
-                        if (j < ca) {
-                            const int src = int(cbase) + a * P + j;
-                            x = W.ll[src];
-                            y = W.uu[src];
-                            z = W.meta[src];
-                        }
-                        __syncwarp();
-                        if (j < ca) {
-                            const int dst = int(cbase) + run + j;
-                            W.ll[dst] = x;
-                            W.uu[dst] = y;
-                            W.meta[dst] = z;
-                        }
-                        __syncwarp();
-                    }
-                }
-                run += ca;
-            }
-            F.cbase = cbase;
-            F.csz4 = uint64_t(c0) | (uint64_t(c1) << 16) | (uint64_t(c2) << 32) | (uint64_t(c3) << 48);
-            F.next_a = 1;
-            if (lane == 0) fr[level] = F;
-            __syncwarp();
-        }
-        int a = int(F.next_a);
-        while (a <= 4 && csz_at(F.csz4, a - 1) == 0) ++a;
-        if (a > 4) {
-            if (level == 0) return OVF_NONE;
-            --level;
-            continue;
-        }
-        if (level + 1 >= kWarpFrames) return OVF_LEVELS;
-        uint32_t before = 0, all = 0;
-        #pragma unroll
-        for (int b = 0; b < 4; ++b) {
-            before += (b < a - 1) ? csz_at(F.csz4, b) : 0;
-            all += csz_at(F.csz4, b);
-        }
-        WFrame G;
-        G.pos = F.cbase + before;
-        G.free = F.cbase + all;        // below it: the parent's four sets, still pending
-        G.cbase = 0;
-        G.size = uint16_t(csz_at(F.csz4, a - 1));
-        int maxl = 0;
-        uint32_t tr = 0;
-        for (int i = lane; i < G.size; i += 32) {
-            maxl = max(maxl, meta_len(W.meta[G.pos + i]));
-            tr += uint32_t(W.uu[G.pos + i] - W.ll[G.pos + i] + 1);
-        }
-        G.maxlen = uint16_t(warp_max(maxl));
-        G.trans = int32_t(warp_sum(tr));
-        G.csz4 = 0;
-        G.next_a = 1;
-        __syncwarp();
-        if (lane == 0) {
-            fr[level].next_a = uint32_t(a + 1);
-            fr[level + 1] = G;
-        }
-        __syncwarp();
-        ++level;
-        entering = true;
-    }
+    return pref[32];
 }
+
+// task owning flattened item e (pref ascending, pref[32] = total)
+__device__ __forceinline__ int owner_of(const int* pref, int e) {
+    int lo = 0, hi = 31;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (pref[mid] <= e) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// ------------------------------------------------------------------------------ fast tier
+//
+// A warp takes 32 reads.  Phase A: each lane runs the candidate searches of its read (two chains
+// at a time, B side then F side) and stores the level-0 candidates in the warp's scratch.
+// Phase B, once for the B side and once for the F side: the 32 (read, side) DFS of
+// extract_*_edges advance together, one level per step.  Each lane owns the control of its
+// read's DFS (frames, emission, backtracking); the intervals of all tasks expanding in a step
+// are spread over the lanes, so the block loads of up to 32 tasks are in flight together.  The
+// order of the extension sets, the first emitting interval and the DFS order of the edges are
+// fixed by entry index (bit masks with population counts, an atomic minimum), never by the order
+// in which lanes happen to run, so every edge list is the reference's.
+// Phase C: each lane publishes its read (edge-pool reservation, copy, per-read counts).
 
 __global__ void __launch_bounds__(128) k_search_fast(SearchArgs A, SearchOut O, WarpScratch S) {
     extern __shared__ uint32_t s_reads[];
     __shared__ FmView s_fm[2];
-    __shared__ WFrame s_fr[kWarpsPerCta][kWarpFrames];
-    __shared__ idx_t s_sll[kWarpsPerCta][kSmemStack], s_suu[kWarpsPerCta][kSmemStack];
-    __shared__ uint32_t s_smeta[kWarpsPerCta][kSmemStack];
+    __shared__ MultiSmem s_ms[kWarpsPerCta];
     __shared__ int s_n[kWarpsPerCta][32][4];
     __shared__ int32_t s_olp[kWarpsPerCta][32][2];
-    __shared__ int s_st[kWarpsPerCta][32];
-    __shared__ int s_ne[kWarpsPerCta][32][2];
     if (threadIdx.x < 2) s_fm[threadIdx.x] = A.fm[threadIdx.x];
     __syncthreads();
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const size_t gw = size_t(blockIdx.x) * kWarpsPerCta + wid;
     const size_t nw = size_t(gridDim.x) * kWarpsPerCta;
     const int M = A.L - A.t;
-    const size_t cbase_w = gw * 32 * 4 * size_t(M);        // level-0 candidates of this warp
-    const size_t ebase_w = gw * 32 * size_t(S.ebcap);      // edge slots of this warp
-    const WarpStack W{s_sll[wid], s_suu[wid], s_smeta[wid]};
+    const int L = A.L;
+    MultiSmem& sm = s_ms[wid];
+    const size_t cbase_w = gw * 32 * 4 * size_t(M);            // level-0 candidates of this warp
+    const size_t ebase_w = gw * 32 * size_t(S.ebcap);          // edge slots of this warp
+    const size_t tbase_w = gw * 32 * size_t(kTaskCap);         // task stacks
+    const size_t xbase_w = gw * 32 * 4 * size_t(kPMax);        // sparse extension slots
+    const size_t mbase_w = gw * 32 * size_t(kPMax);            // emission bounds
+    TFrame* const frw = S.frames + gw * 32 * kTaskFrames;
     uint32_t probes = 0;
     for (size_t batch = gw; batch * 32 < size_t(A.num_reads); batch += nw) {
         const size_t r = batch * 32 + lane;
         const bool have = r < size_t(A.num_reads);
-        // phase A
+        const idx_t self = idx_t(r);
+        // ---- phase A
         if (have) {
             load_read(A, idx_t(r), s_reads + threadIdx.x, blockDim.x);
             ReadView rd{s_reads + threadIdx.x, int(blockDim.x)};
@@ -809,57 +652,244 @@ __global__ void __launch_bounds__(128) k_search_fast(SearchArgs A, SearchOut O, 
             s_n[wid][lane][3] = nf[1];
             s_olp[wid][lane][0] = ob;
             s_olp[wid][lane][1] = of;
-            s_st[wid][lane] = OVF_NONE;
-        } else {
-            s_st[wid][lane] = -1;
         }
         __syncwarp();
-        // phase B: reduce (read j, B side) then (read j, F side), whole warp
-        for (int j = 0; j < 32; ++j) {
-            if (s_st[wid][j] != OVF_NONE) continue;
-            const idx_t self = idx_t(batch * 32 + j);
-            const size_t cb = cbase_w + size_t(j) * 4 * M;
-            const size_t eb = ebase_w + size_t(j) * S.ebcap;
-            int ne = 0, st = OVF_NONE;
-            int count_b = 0, count_f = 0;
-            #pragma unroll
-            for (int side = 0; side < 2; ++side) {
-                if (st != OVF_NONE) break;
-                if (s_olp[wid][j][side] == 0) continue;   // src/string_graph.c:824, 828
-                const int na = s_n[wid][j][2 * side], nb = s_n[wid][j][2 * side + 1];
-                const int n0 = na + nb;
-                if (n0 > kSmemStack) { st = OVF_STACK; break; }
-                for (int i = lane; i < n0; i += 32) {
-                    const size_t src = cb + (i < na ? size_t(2 * side) * M + i : size_t(2 * side + 1) * M + (i - na));
-                    W.ll[i] = S.c_ll[src];
-                    W.uu[i] = S.c_uu[src];
-                    W.meta[i] = S.c_meta[src];
-                }
-                __syncwarp();
-                int sc = 0;
-                st = warp_reduce_side(A, s_fm, self, W, n0, s_fr[wid], S, eb, ne, sc, probes);
-                if (side == 0) count_b = sc;
-                else count_f = sc;
-                __syncwarp();
-            }
-            if (lane == 0) {
-                s_st[wid][j] = st;
-                s_ne[wid][j][0] = count_b;
-                s_ne[wid][j][1] = count_f;
+        // ---- phase B
+        int status = have ? OVF_NONE : -1;
+        int ne = 0, count_b = 0, count_f = 0;
+        const size_t tb = tbase_w + size_t(lane) * kTaskCap;    // this lane's task stack
+        TFrame* const fr = frw + lane * kTaskFrames;
+        const size_t eb = ebase_w + size_t(lane) * S.ebcap;
+        #pragma unroll 1
+        for (int side = 0; side < 2; ++side) {
+            bool active = have && status == OVF_NONE && s_olp[wid][lane][side] != 0;   // src/string_graph.c:824, 828
+            const int na = active ? s_n[wid][lane][2 * side] : 0;
+            const int n0 = active ? na + s_n[wid][lane][2 * side + 1] : 0;
+            if (active && n0 > kTaskCap) { status = OVF_STACK; active = false; }
+            // level 0 = kind-0 candidates then kind-1 candidates, copied into the task stacks
+            sm.na[lane] = na;
+            const int tot0 = warp_prefix(active ? n0 : 0, sm.pref);
+            for (int e = lane; e < tot0; e += 32) {
+                const int j = owner_of(sm.pref, e);
+                const int i = e - sm.pref[j];
+                const int nj = sm.na[j];
+                const size_t src = cbase_w + size_t(j) * 4 * M +
+                                   (i < nj ? size_t(2 * side) * M + i : size_t(2 * side + 1) * M + (i - nj));
+                const size_t dst = tbase_w + size_t(j) * kTaskCap + i;
+                S.t_ll[dst] = S.c_ll[src];
+                S.t_uu[dst] = S.c_uu[src];
+                S.t_meta[dst] = S.c_meta[src];
             }
             __syncwarp();
+            TFrame F;
+            F.pos = 0;
+            F.free = uint32_t(n0);
+            F.cbase = 0;
+            F.trans = 0;
+            F.size = uint16_t(n0);
+            F.maxlen = 0;
+            F.next_a = 1;
+            F.csz4 = 0;
+            F.cml4 = 0;
+            F.ctr[0] = F.ctr[1] = F.ctr[2] = F.ctr[3] = 0;
+            bool entering = true;
+            int level = 0, sc = 0;
+            while (__any_sync(0xffffffffu, active)) {
+                // (1) own control: backtrack / descend until this task needs an expansion
+                if (active && !entering) {
+                    while (true) {
+                        int a = int(F.next_a);
+                        while (a <= 4 && csz_at(F.csz4, a - 1) == 0) ++a;
+                        if (a > 4) {
+                            if (level == 0) { active = false; break; }
+                            --level;
+                            F = fr[level];
+                            continue;
+                        }
+                        if (level + 1 >= kTaskFrames) { status = OVF_LEVELS; active = false; break; }
+                        F.next_a = uint32_t(a + 1);
+                        fr[level] = F;
+                        uint32_t before = 0, all = 0;
+                        #pragma unroll
+                        for (int b = 0; b < 4; ++b) {
+                            before += (b < a - 1) ? csz_at(F.csz4, b) : 0;
+                            all += csz_at(F.csz4, b);
+                        }
+                        TFrame G;
+                        G.pos = F.cbase + before;
+                        G.free = F.cbase + all;      // below it: the parent's four sets, still pending
+                        G.cbase = 0;
+                        G.size = uint16_t(csz_at(F.csz4, a - 1));
+                        G.maxlen = uint16_t(csz_at(F.cml4, a - 1));
+                        G.trans = a == 1 ? F.ctr[0] : (a == 2 ? F.ctr[1] : (a == 3 ? F.ctr[2] : F.ctr[3]));
+                        G.next_a = 1;
+                        G.csz4 = 0;
+                        G.cml4 = 0;
+                        G.ctr[0] = G.ctr[1] = G.ctr[2] = G.ctr[3] = 0;
+                        F = G;
+                        ++level;
+                        entering = true;
+                        break;
+                    }
+                }
+                const bool expand = active && entering;
+                if (expand && F.size > kPMax) { status = OVF_STACK; active = false; }
+                const bool go = active && entering;
+                sm.size[lane] = go ? int(F.size) : 0;
+                sm.pos[lane] = F.pos;
+                sm.lvl[lane] = level;
+                sm.chk[lane] = int(F.maxlen) + level == L;
+                sm.hit[lane] = 0x7fffffff;
+                #pragma unroll
+                for (int a = 0; a < 4; ++a) {
+                    sm.mask[lane][a][0] = sm.mask[lane][a][1] = 0;
+                    sm.cml[lane][a] = 0;
+                    sm.ctr[lane][a] = 0;
+                }
+                // (2) every interval of every expanding task: one pair of block loads serves the
+                // emission check and the four extensions
+                const int tot = warp_prefix(go ? int(F.size) : 0, sm.pref);
+                for (int e = lane; e < tot; e += 32) {
+                    const int j = owner_of(sm.pref, e);
+                    const int i = e - sm.pref[j];
+                    const size_t tj = tbase_w + size_t(j) * kTaskCap + sm.pos[j] + i;
+                    const idx_t cl = S.t_ll[tj], cu = S.t_uu[tj];
+                    const uint32_t m = S.t_meta[tj];
+                    const bool ext = idx_t(cu - cl + 1) != 0;   // wrapped [0, all-ones]: kept, never extended
+                    const bool ends = sm.chk[j] && meta_len(m) + sm.lvl[j] == L;
+                    const int o = cand_index(meta_type(m));
+                    const FmView& f = s_fm[o];
+                    idx_t rl[4] = {0, 0, 0, 0}, ru[4] = {0, 0, 0, 0};
+                    if (ext || ends) {
+                        rank_all(f, cl, rl);
+                        rank_all(f, cu + 1, ru);
+                        probes += 2;
+                    }
+                    if (ends) {
+                        const idx_t ea = f.Cf[0] + (cl - (rl[0] + rl[1] + rl[2] + rl[3]));
+                        const idx_t eb2 = f.Cf[0] + ((cu + 1) - (ru[0] + ru[1] + ru[2] + ru[3])) - 1;
+                        if (ea <= eb2) {
+                            const size_t me = mbase_w + size_t(j) * kPMax + i;
+                            S.em_l[me] = ea;
+                            S.em_u[me] = eb2;
+                            atomicMin(&sm.hit[j], i);
+                        }
+                    }
+                    if (ext) {
+                        #pragma unroll
+                        for (int a = 1; a <= 4; ++a) {
+                            const int ch = o == 0 ? complement(a) : a;
+                            const idx_t lo = f.Cf[ch] + pick4(rl, ch);
+                            const idx_t hi = f.Cf[ch] + pick4(ru, ch) - 1;
+                            if (lo <= hi) {
+                                const size_t x = xbase_w + (size_t(j) * 4 + (a - 1)) * kPMax + i;
+                                S.x_ll[x] = lo;
+                                S.x_uu[x] = hi;
+                                S.x_meta[x] = m;
+                                atomicOr(&sm.mask[j][a - 1][i >> 6], 1ull << (i & 63));
+                                atomicMax(&sm.cml[j][a - 1], meta_len(m));
+                                atomicAdd(&sm.ctr[j][a - 1], unsigned(hi - lo + 1));
+                            }
+                        }
+                    }
+                }
+                __syncwarp();
+                // (3) own control: emit, or record the four sets
+                bool place = false;
+                if (go) {
+                    const int h = sm.hit[lane];
+                    bool popped = false;
+                    if (h != 0x7fffffff) {
+                        const size_t me = mbase_w + size_t(lane) * kPMax + h;
+                        const idx_t lll = S.em_l[me], uuu = S.em_u[me];
+                        const uint32_t hm = S.t_meta[tb + F.pos + h];
+                        const idx_t endk = uuu + 1;      // k < uuu + 1: no iteration when uuu + 1 wraps
+                        const idx_t cnt = endk > lll ? endk - lll : 0;
+                        const idx_t* rix = s_fm[cand_index(meta_type(hm))].reads_index;
+                        for (idx_t k = 0; k < cnt; ++k) {
+                            const idx_t rr = __ldg(rix + (lll + k));
+                            if (rr == self) continue;
+                            if (sc + 1 > 65535) { status = ERR_TOO_MANY; break; }
+                            if (ne + 1 > S.ebcap) { status = OVF_EDGES; break; }
+                            S.e_dest[eb + ne] = rr;
+                            S.e_trans[eb + ne] = F.trans;
+                            S.e_meta[eb + ne] = hm;
+                            ++ne;
+                            ++sc;
+                        }
+                        if (status != OVF_NONE) {
+                            active = false;
+                        } else if (cnt > 0) {           // flag: this branch is finished
+                            popped = true;
+                            entering = false;
+                            if (level == 0) active = false;
+                            else {
+                                --level;
+                                F = fr[level];
+                            }
+                        }
+                    }
+                    if (!popped && active) {
+                        int c[4];
+                        int run = 0;
+                        #pragma unroll
+                        for (int a = 0; a < 4; ++a) {
+                            c[a] = popc128(sm.mask[lane][a]);
+                            sm.setoff[lane][a] = run;
+                            run += c[a];
+                        }
+                        if (int(F.free) + run > kTaskCap) {
+                            status = OVF_STACK;
+                            active = false;
+                        } else {
+                            F.cbase = F.free;
+                            F.csz4 = uint64_t(c[0]) | (uint64_t(c[1]) << 16) | (uint64_t(c[2]) << 32) |
+                                     (uint64_t(c[3]) << 48);
+                            F.cml4 = uint64_t(sm.cml[lane][0]) | (uint64_t(sm.cml[lane][1]) << 16) |
+                                     (uint64_t(sm.cml[lane][2]) << 32) | (uint64_t(sm.cml[lane][3]) << 48);
+                            F.ctr[0] = int32_t(sm.ctr[lane][0]);
+                            F.ctr[1] = int32_t(sm.ctr[lane][1]);
+                            F.ctr[2] = int32_t(sm.ctr[lane][2]);
+                            F.ctr[3] = int32_t(sm.ctr[lane][3]);
+                            F.next_a = 1;
+                            entering = false;
+                            place = true;
+                        }
+                    }
+                }
+                // (4) pack the sets of every expanded task into its stack, in entry order
+                sm.cbase[lane] = F.cbase;
+                const int totx = warp_prefix(place ? 4 * int(F.size) : 0, sm.pref);
+                __syncwarp();
+                for (int e = lane; e < totx; e += 32) {
+                    const int j = owner_of(sm.pref, e);
+                    const int rel = e - sm.pref[j];
+                    const int Pj = (sm.pref[j + 1] - sm.pref[j]) >> 2;
+                    const int a = rel / Pj, i = rel - a * Pj;
+                    const unsigned long long* mk = sm.mask[j][a];
+                    if ((mk[i >> 6] >> (i & 63)) & 1) {
+                        const int dst = int(sm.cbase[j]) + sm.setoff[j][a] + popc128_below(mk, i);
+                        const size_t x = xbase_w + (size_t(j) * 4 + a) * kPMax + i;
+                        const size_t t = tbase_w + size_t(j) * kTaskCap + dst;
+                        S.t_ll[t] = S.x_ll[x];
+                        S.t_uu[t] = S.x_uu[x];
+                        S.t_meta[t] = S.x_meta[x];
+                    }
+                }
+                __syncwarp();
+            }
+            if (side == 0) count_b = sc;
+            else count_f = sc;
         }
-        // phase C: publish
+        // ---- phase C: publish
         if (have) {
-            const int st = s_st[wid][lane];
-            if (st != OVF_NONE) {
-                O.status[r] = uint8_t(st);
-                if (st != ERR_TOO_MANY) {
+            if (status != OVF_NONE) {
+                O.status[r] = uint8_t(status);
+                if (status != ERR_TOO_MANY) {
                     unsigned k = atomicAdd(O.ovf_count, 1u);
                     O.ovf_list[k] = idx_t(r);
                 }
             } else {
-                const int nB = s_ne[wid][lane][0], nF = s_ne[wid][lane][1], ne = nB + nF;
                 unsigned long long base = 0;
                 bool ok = true;
                 if (ne) {
@@ -870,7 +900,6 @@ __global__ void __launch_bounds__(128) k_search_fast(SearchArgs A, SearchOut O, 
                         unsigned k = atomicAdd(O.ovf_count, 1u);
                         O.ovf_list[k] = idx_t(r);
                     } else {
-                        const size_t eb = ebase_w + size_t(lane) * S.ebcap;
                         for (int e = 0; e < ne; ++e) {
                             const uint32_t mt = S.e_meta[eb + e];
                             O.e_dest[base + e] = S.e_dest[eb + e];
@@ -882,8 +911,8 @@ __global__ void __launch_bounds__(128) k_search_fast(SearchArgs A, SearchOut O, 
                 }
                 if (ok) {
                     O.status[r] = OVF_NONE;
-                    O.num_B[r] = uint16_t(nB);
-                    O.num_F[r] = uint16_t(nF);
+                    O.num_B[r] = uint16_t(count_b);
+                    O.num_F[r] = uint16_t(count_f);
                     O.olp_B[r] = s_olp[wid][lane][0];
                     O.olp_F[r] = s_olp[wid][lane][1];
                     O.edge_src[r] = base;
@@ -905,32 +934,48 @@ int search_fast_blocks(int L, int num_sms) {
     return per_sm * num_sms;
 }
 
-size_t warp_scratch_bytes(int L, int t, size_t nwarps, int ebcap) {
+static size_t scratch_layout(int L, int t, size_t nwarps, int ebcap, void* base, WarpScratch* S) {
     const size_t M = size_t(L - t);
     const size_t cand = nwarps * 32 * 4 * M, edg = nwarps * 32 * size_t(ebcap);
-    return cand * (2 * sizeof(idx_t) + 4) + edg * (sizeof(idx_t) + 8) + 16 * 256;
+    const size_t tsk = nwarps * 32 * size_t(kTaskCap), spr = nwarps * 32 * 4 * size_t(kPMax);
+    const size_t emb = nwarps * 32 * size_t(kPMax), frm = nwarps * 32 * size_t(kTaskFrames);
+    char* p = static_cast<char*>(base);
+    size_t used = 0;
+    auto take = [&](size_t bytes) {
+        char* q = p ? p + used : nullptr;
+        used += (bytes + 255) & ~size_t(255);
+        return q;
+    };
+    WarpScratch T;
+    T.c_ll = reinterpret_cast<idx_t*>(take(cand * sizeof(idx_t)));
+    T.c_uu = reinterpret_cast<idx_t*>(take(cand * sizeof(idx_t)));
+    T.c_meta = reinterpret_cast<uint32_t*>(take(cand * 4));
+    T.e_dest = reinterpret_cast<idx_t*>(take(edg * sizeof(idx_t)));
+    T.e_trans = reinterpret_cast<int32_t*>(take(edg * 4));
+    T.e_meta = reinterpret_cast<uint32_t*>(take(edg * 4));
+    T.t_ll = reinterpret_cast<idx_t*>(take(tsk * sizeof(idx_t)));
+    T.t_uu = reinterpret_cast<idx_t*>(take(tsk * sizeof(idx_t)));
+    T.t_meta = reinterpret_cast<uint32_t*>(take(tsk * 4));
+    T.x_ll = reinterpret_cast<idx_t*>(take(spr * sizeof(idx_t)));
+    T.x_uu = reinterpret_cast<idx_t*>(take(spr * sizeof(idx_t)));
+    T.x_meta = reinterpret_cast<uint32_t*>(take(spr * 4));
+    T.em_l = reinterpret_cast<idx_t*>(take(emb * sizeof(idx_t)));
+    T.em_u = reinterpret_cast<idx_t*>(take(emb * sizeof(idx_t)));
+    T.frames = reinterpret_cast<TFrame*>(take(frm * sizeof(TFrame)));
+    T.ebcap = ebcap;
+    if (S) *S = T;
+    return used;
+}
+
+size_t warp_scratch_bytes(int L, int t, size_t nwarps, int ebcap) {
+    return scratch_layout(L, t, nwarps, ebcap, nullptr, nullptr);
 }
 
 cudaError_t search_fast(const SearchArgs& a, const SearchOut& o, int blocks, void* scratch, size_t scratch_bytes,
                         int ebcap, cudaStream_t st) {
     const size_t nwarps = size_t(blocks) * kWarpsPerCta;
-    if (scratch_bytes < warp_scratch_bytes(a.L, a.t, nwarps, ebcap)) return cudaErrorInvalidValue;
-    const size_t M = size_t(a.L - a.t);
-    const size_t cand = nwarps * 32 * 4 * M, edg = nwarps * 32 * size_t(ebcap);
-    char* p = static_cast<char*>(scratch);
-    auto take = [&](size_t bytes) {
-        char* q = p;
-        p += (bytes + 255) & ~size_t(255);
-        return q;
-    };
     WarpScratch S;
-    S.c_ll = reinterpret_cast<idx_t*>(take(cand * sizeof(idx_t)));
-    S.c_uu = reinterpret_cast<idx_t*>(take(cand * sizeof(idx_t)));
-    S.c_meta = reinterpret_cast<uint32_t*>(take(cand * 4));
-    S.e_dest = reinterpret_cast<idx_t*>(take(edg * sizeof(idx_t)));
-    S.e_trans = reinterpret_cast<int32_t*>(take(edg * 4));
-    S.e_meta = reinterpret_cast<uint32_t*>(take(edg * 4));
-    S.ebcap = ebcap;
+    if (scratch_bytes < scratch_layout(a.L, a.t, nwarps, ebcap, scratch, &S)) return cudaErrorInvalidValue;
     const int words = (a.L + 15) / 16;
     size_t smem = size_t(words) * 32 * kWarpsPerCta * sizeof(uint32_t);
     { k_search_fast<<<blocks, 32 * kWarpsPerCta, smem, st>>>(a, o, S); note_launch(); }
