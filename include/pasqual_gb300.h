@@ -103,6 +103,12 @@ PQ_API int pq_get_seeds (pq_ctx * ctx, int dir, pq_idx * start, pq_idx * size, u
 /* Seed depth k of the overlap search (1 <= k <= min(13, t)); default min(12, t). */
 PQ_API int pq_set_seed_k (pq_ctx * ctx, int k);
 
+/* How each search reaches depth t: 1 (default, t <= 128) binary-searches the suffix arrays for
+ * the depth-t intervals inside the k-mer table interval of the pattern's first k bases; 0 walks
+ * from the depth-k seed with one synchronised step per base, as the reference walks from its
+ * sort-recorded seed (src/string_graph.c:207-224).  Both give the same intervals. */
+PQ_API int pq_set_seed_mode (pq_ctx * ctx, int mode);
+
 /* Overlap search with transitive reduction for every read: find_intervals +
  * extract_bw_edges + extract_fw_edges (src/string_graph.c:163-731) as driven by
  * construct_string_graph (src/string_graph.c:800-830). */

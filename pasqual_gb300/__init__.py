@@ -29,7 +29,7 @@ PQ_ERRORS = {1: "PQ_ERR_ARG", 2: "PQ_ERR_CUDA", 3: "PQ_ERR_NOMEM", 4: "PQ_ERR_TO
 # Every entry point of include/pasqual_gb300.h (checked against the header by the tests).
 EXPORTS = ["pq_idx_bytes", "pq_create", "pq_destroy", "pq_last_error", "pq_set_reads",
            "pq_get_counts", "pq_sort", "pq_set_sa", "pq_get_sa", "pq_build_fm", "pq_build_index",
-           "pq_get_index_ref", "pq_get_seeds", "pq_set_seed_k", "pq_overlaps",
+           "pq_get_index_ref", "pq_get_seeds", "pq_set_seed_k", "pq_set_seed_mode", "pq_overlaps",
            "pq_get_graph_sizes", "pq_get_graph", "pq_get_stage_ms", "pq_get_kernel_stats",
            "pq_suffix_sort_static"]
 
@@ -77,6 +77,7 @@ def load_library(width: int = 32) -> ct.CDLL:
         "pq_get_index_ref": (c_int, [vp, c_int, vp, vp, vp]),
         "pq_get_seeds": (c_int, [vp, c_int, vp, vp, vp]),
         "pq_set_seed_k": (c_int, [vp, c_int]),
+        "pq_set_seed_mode": (c_int, [vp, c_int]),
         "pq_overlaps": (c_int, [vp]),
         "pq_get_graph_sizes": (c_int, [vp, vp, vp, vp]),
         "pq_get_graph": (c_int, [vp] + [vp] * 9),
@@ -161,6 +162,10 @@ class Pasqual:
 
     def set_seed_k(self, k: int) -> None:
         self._ck(self.lib.pq_set_seed_k(self.h, int(k)), "pq_set_seed_k")
+
+    def set_seed_mode(self, mode: int) -> None:
+        """1: depth-t seeds by suffix-array search (default); 0: walk from the k-mer seed."""
+        self._ck(self.lib.pq_set_seed_mode(self.h, int(mode)), "pq_set_seed_mode")
 
     def sort(self, direction: int) -> None:
         self._ck(self.lib.pq_sort(self.h, direction), "pq_sort")

@@ -67,12 +67,13 @@ struct pq_ctx {
     idx_t num_reads = 0;
     int L = 0, t = 0;
     int seed_k = 0;
+    int seed_mode = 1;        // 1: depth-t seeds by suffix-array search, 0: walk from the k-mer seed
     DevBuf reads;
     idx_t C[6] = {0}, sfx[4] = {0}, pfx[4] = {0};
     bool have_reads = false;
 
     // per direction
-    DevBuf sa[2], blk[2], sb[2], ri[2], kstart[2], kend[2];
+    DevBuf sa[2], blk[2], sb[2], ri[2], kstart[2], kend[2], pk[2];
     bool sa_ok[2] = {false, false}, fm_ok[2] = {false, false};
     int fm_k[2] = {0, 0};
     DevBuf ktmp, sort_tmp, counts;
@@ -151,6 +152,7 @@ void pq_destroy(pq_ctx* ctx) {
         ctx->ri[d].release();
         ctx->kstart[d].release();
         ctx->kend[d].release();
+        ctx->pk[d].release();
     }
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -270,6 +272,14 @@ int pq_set_seed_k(pq_ctx* ctx, int k) {
     return PQ_OK;
 }
 
+int pq_set_seed_mode(pq_ctx* ctx, int mode) {
+    if (!ctx) return PQ_ERR_ARG;
+    if (mode != 0 && mode != 1) return fail(ctx, PQ_ERR_ARG, "seed mode must be 0 (walk) or 1 (suffix-array search)");
+    ctx->seed_mode = mode;
+    ctx->graph_ok = false;
+    return PQ_OK;
+}
+
 int pq_build_fm(pq_ctx* ctx, int dir) {
     if (!ctx || (dir != 0 && dir != 1)) return PQ_ERR_ARG;
     if (!ctx->sa_ok[dir]) return fail(ctx, PQ_ERR_STATE, "no suffix array for this direction");
@@ -283,12 +293,14 @@ int pq_build_fm(pq_ctx* ctx, int dir) {
     CK(ctx->kstart[dir].ensure(nk * sizeof(idx_t)));
     CK(ctx->kend[dir].ensure(nk * sizeof(idx_t)));
     CK(ctx->ktmp.ensure(n * sizeof(uint32_t) + 64));
+    CK(ctx->pk[dir].ensure((n / 32 + 4) * sizeof(uint64_t)));
     CK(cudaEventRecord(ctx->ev0, ctx->st));
     CK(pq::build_occ(ctx->sa[dir].as<idx_t>(), ctx->reads.as<uint8_t>(), ctx->num_reads, idx_t(ctx->L), dir,
                      ctx->blk[dir].as<OccBlock>(), ctx->sb[dir].as<idx_t>(), ctx->ri[dir].as<idx_t>(), ctx->st));
     CK(pq::build_kmer_table(ctx->sa[dir].as<idx_t>(), ctx->reads.as<uint8_t>(), ctx->num_reads, idx_t(ctx->L), dir,
                             k, ctx->ktmp.as<uint32_t>(), ctx->kstart[dir].as<idx_t>(), ctx->kend[dir].as<idx_t>(),
                             ctx->st));
+    CK(pq::pack_text(ctx->reads.as<uint8_t>(), n, idx_t(ctx->L), dir, ctx->pk[dir].as<uint64_t>(), ctx->st));
     CK(cudaEventRecord(ctx->ev1, ctx->st));
     CK(cudaEventSynchronize(ctx->ev1));
     cudaEventElapsedTime(&ctx->ms_fm, ctx->ev0, ctx->ev1);
@@ -387,6 +399,8 @@ int pq_overlaps(pq_ctx* ctx) {
         f.reads_index = ctx->ri[d].as<idx_t>();
         f.kstart = ctx->kstart[d].as<idx_t>();
         f.kend = ctx->kend[d].as<idx_t>();
+        f.sa = ctx->sa[d].as<idx_t>();
+        f.pk = ctx->pk[d].as<uint64_t>();
         const idx_t* fix = d == 0 ? ctx->sfx : ctx->pfx;
         f.Cf[0] = ctx->C[0];
         for (int c = 1; c <= 4; ++c) f.Cf[c] = ctx->C[c] + fix[c - 1];
@@ -396,6 +410,7 @@ int pq_overlaps(pq_ctx* ctx) {
     A.L = ctx->L;
     A.t = ctx->t;
     A.seed_k = ctx->fm_k[0];
+    A.sa_seed = (ctx->seed_mode == 1 && ctx->t <= 128 && ctx->sa_ok[0] && ctx->sa_ok[1]) ? 1 : 0;
 
     unsigned long long* ctr = ctx->ctrs.as<unsigned long long>();   // [0] e_count [1] probes [2] ovf(u32)
     pq::SearchOut O;

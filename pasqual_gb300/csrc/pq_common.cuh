@@ -49,6 +49,8 @@ struct FmView {
     const idx_t* reads_index; // read id of the k-th `$` row
     const idx_t* kstart;      // k-mer seed table: first row of each k-mer (or nullptr)
     const idx_t* kend;        // last row (kend < kstart when the k-mer is absent)
+    const idx_t* sa;          // suffix array (for seeds found by binary search), or nullptr
+    const uint64_t* pk;       // the text, 32 bases per word, first base in the top bits
     idx_t Cf[5];              // Cf[0] = C[0]; Cf[c] = C[c] + fix[c]  (LF-mapping base)
 };
 

@@ -41,6 +41,7 @@ struct SearchArgs {
     int L;
     int t;
     int seed_k;                 // k-mer seed depth (0 = start at depth 1 from C[])
+    int sa_seed;                // 1: depth-t intervals by suffix-array search (needs fm[].sa/pk)
 };
 
 // Global scratch of the fast kernel, per warp of 32 reads: level-0 candidates (4 kinds x (L - t)

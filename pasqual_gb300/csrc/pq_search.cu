@@ -229,6 +229,114 @@ __device__ __forceinline__ int walked_index(int kind) { return (kind == PQ_FB ||
 // known at every depth and the rebuild disappears; SA intervals are unique per string, so the
 // intervals at depth t -- and everything after -- are the reference's.  The i-th stored candidate
 // of kind k0 (q = 0) or k1 (q = 1) goes to sink(q, i, ll, uu, depth, kind); n[q] counts them.
+// ---------------------------------------------------------------- depth-t seeds by SA search
+//
+// The walk from the k-mer seed to depth t only serves to find two SA intervals: the rows of the
+// walked index that start with P = pat(t) .. pat(1) and the rows of the other index that start
+// with its reverse.  Both are found directly here by binary search over the suffix arrays,
+// inside the table interval of the pattern's first k bases: about log2(interval) steps of two
+// dependent loads (SA entry, then 64 bases of text) per bound instead of t - k steps.  A row
+// compares as its suffix string with end-of-read lowest, so the bounds are exactly the rows the
+// backward search reaches.  A search that dies before depth t (the interval shrinks to one row,
+// or to none) is dead at depth t too -- interval sizes only shrink with depth -- so the chain
+// continues exactly when the reference's does.
+
+constexpr int kSeedWords = 4;       // patterns up to 128 bases (longer t walks instead)
+
+// base c (0-based) of the pattern in text order for index A (dir 0) or its reverse (dir 1)
+__device__ __forceinline__ int seed_base(const ReadView& rd, int L, int t, int kind, int dir, int c) {
+    return pattern_at(rd, L, kind, dir == 0 ? t - c : c + 1);
+}
+
+__device__ __forceinline__ void pack_pattern(const ReadView& rd, int L, int t, int kind, int dir,
+                                             uint64_t (&P)[kSeedWords]) {
+    #pragma unroll
+    for (int w = 0; w < kSeedWords; ++w) {
+        uint64_t x = 0;
+        for (int j = 0; j < 32; ++j) {
+            const int c = 32 * w + j;
+            x = (x << 2) | uint64_t(c < t ? seed_base(rd, L, t, kind, dir, c) - 1 : 0);
+        }
+        P[w] = x;
+    }
+}
+
+// -1 / 0 / +1: row suffix (m bases at text position p) is below / starts with / above P (t bases)
+__device__ __forceinline__ int cmp_row(const uint64_t* __restrict__ pk, idx_t p, int m, const uint64_t (&P)[kSeedWords],
+                                       int t) {
+    const int nb = m < t ? m : t;
+    const size_t w0 = size_t(p) >> 5;
+    const int s = int(p & 31) * 2;
+    uint64_t prev = __ldg(pk + w0);
+    #pragma unroll
+    for (int w = 0; w < kSeedWords; ++w) {
+        const int v = nb - 32 * w;
+        if (v <= 0) break;
+        const uint64_t next = __ldg(pk + w0 + w + 1);
+        uint64_t x = s ? ((prev << s) | (next >> (64 - s))) : prev;
+        prev = next;
+        const uint64_t mask = v >= 32 ? ~uint64_t(0) : (~uint64_t(0) << (64 - 2 * v));
+        x &= mask;
+        const uint64_t y = P[w] & mask;
+        if (x != y) return x < y ? -1 : 1;
+    }
+    return m < t ? -1 : 0;
+}
+
+// rows of index f whose suffix starts with P, searched within [lo, hi): returns [first, end)
+__device__ __forceinline__ void sa_bounds(const FmView& f, int L, const uint64_t (&P)[kSeedWords], int t, idx_t lo,
+                                          idx_t hi, idx_t& first, idx_t& end, uint32_t& probes) {
+    idx_t a0 = lo, a1 = hi, b0 = lo, b1 = hi;     // lower bound in [a0, a1), upper bound in [b0, b1)
+    while (a0 < a1 || b0 < b1) {
+        const bool ga = a0 < a1, gb = b0 < b1;
+        const idx_t ma = a0 + (a1 - a0) / 2, mb = b0 + (b1 - b0) / 2;
+        idx_t pa = 0, pb = 0;
+        if (ga) pa = __ldg(f.sa + ma);
+        if (gb) pb = __ldg(f.sa + mb);
+        if (ga) {
+            const int c = cmp_row(f.pk, pa, L - int(pa % idx_t(L)), P, t);
+            if (c < 0) a0 = ma + 1;
+            else a1 = ma;
+            probes += 2;
+        }
+        if (gb) {
+            const int c = cmp_row(f.pk, pb, L - int(pb % idx_t(L)), P, t);
+            if (c <= 0) b0 = mb + 1;
+            else b1 = mb;
+            probes += 2;
+        }
+    }
+    first = a0;
+    end = b0;
+}
+
+// the walked index's interval [l, u] of pat(t)..pat(1) and the other index's [ll, uu] of its
+// reverse; an empty interval comes back as l = 1 > u = 0
+__device__ __forceinline__ void sa_seed(const FmView& fa, const FmView& fb, const ReadView& rd, int L, int t, int k,
+                                        int kind, idx_t& l, idx_t& u, idx_t& ll, idx_t& uu, uint32_t& probes) {
+    uint64_t P[kSeedWords];
+    idx_t s0, s1;
+    // walked index: prefix of P is pat(t) .. pat(t-k+1)
+    pack_pattern(rd, L, t, kind, 0, P);
+    {
+        uint32_t code = uint32_t(P[0] >> (64 - 2 * k));
+        const idx_t lo = __ldg(fa.kstart + code), hi = __ldg(fa.kend + code) + 1;
+        probes += 1;
+        sa_bounds(fa, L, P, t, lo, lo < hi ? hi : lo, s0, s1, probes);
+    }
+    if (s0 < s1) { l = s0; u = s1 - 1; }
+    else { l = 1; u = 0; }
+    pack_pattern(rd, L, t, kind, 1, P);
+    {
+        uint32_t code = uint32_t(P[0] >> (64 - 2 * k));
+        const idx_t lo = __ldg(fb.kstart + code), hi = __ldg(fb.kend + code) + 1;
+        probes += 1;
+        sa_bounds(fb, L, P, t, lo, lo < hi ? hi : lo, s0, s1, probes);
+    }
+    if (s0 < s1) { ll = s0; uu = s1 - 1; }
+    else { ll = 1; uu = 0; }
+}
+
 template <class Sink>
 __device__ __forceinline__ void chain_pair(const SearchArgs& A, const FmView* fm, const ReadView& rd, int k0, int k1,
                                            int (&n)[2], int32_t& olp, uint32_t& probes, Sink sink) {
@@ -236,15 +344,27 @@ __device__ __forceinline__ void chain_pair(const SearchArgs& A, const FmView* fm
     idx_t l[2], u[2], ll[2], uu[2];
     bool alive[2];
     n[0] = n[1] = 0;
-    #pragma unroll
-    for (int q = 0; q < 2; ++q) {
-        const int kind = q ? k1 : k0;
-        const int ia = walked_index(kind);
-        kmer_seed(fm[ia], rd, L, kind, k, 1, -1, l[q], u[q], probes);       // pat(k) .. pat(1)
-        kmer_seed(fm[1 - ia], rd, L, kind, 1, k, 1, ll[q], uu[q], probes);  // pat(1) .. pat(k)
-        alive[q] = live(kind, l[q], u[q]);
+    int d;
+    if (A.sa_seed) {
+        #pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const int kind = q ? k1 : k0;
+            const int ia = walked_index(kind);
+            sa_seed(fm[ia], fm[1 - ia], rd, L, t, k, kind, l[q], u[q], ll[q], uu[q], probes);
+            alive[q] = live(kind, l[q], u[q]);
+        }
+        d = t;
+    } else {
+        #pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const int kind = q ? k1 : k0;
+            const int ia = walked_index(kind);
+            kmer_seed(fm[ia], rd, L, kind, k, 1, -1, l[q], u[q], probes);       // pat(k) .. pat(1)
+            kmer_seed(fm[1 - ia], rd, L, kind, 1, k, 1, ll[q], uu[q], probes);  // pat(1) .. pat(k)
+            alive[q] = live(kind, l[q], u[q]);
+        }
+        d = k;
     }
-    int d = k;
     while (d < t && (alive[0] || alive[1])) {
         #pragma unroll
         for (int q = 0; q < 2; ++q) {
@@ -604,7 +724,7 @@ __device__ __forceinline__ int owner_of(const int* pref, int e) {
 // in which lanes happen to run, so every edge list is the reference's.
 // Phase C: each lane publishes its read (edge-pool reservation, copy, per-read counts).
 
-__global__ void __launch_bounds__(128) k_search_fast(SearchArgs A, SearchOut O, WarpScratch S) {
+__global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A, SearchOut O, WarpScratch S) {
     extern __shared__ uint32_t s_reads[];
     __shared__ FmView s_fm[2];
     __shared__ MultiSmem s_ms[kWarpsPerCta];

@@ -248,6 +248,12 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(const uint64_t* __r
     }
 }
 
+cudaError_t pack_text(const uint8_t* reads, size_t n, idx_t L, int dir, uint64_t* pk, cudaStream_t st) {
+    const size_t nwords = n / 32 + 4;
+    { k_pack_text<<<grid_for(nwords, 256), 256, 0, st>>>(reads, n, L, dir, nwords, pk); note_launch(); }
+    return cudaGetLastError();
+}
+
 size_t radix_tmp_bytes(size_t n) {
     (void)n;
     return (size_t(256) * RS_MAX_CTAS + 8 * 256 + 64) * sizeof(unsigned long long);

@@ -22,4 +22,8 @@ int radix_sort_pairs(uint64_t** k0, V** v0, uint64_t** k1, V** v1, size_t n, int
                      void* tmp, size_t tmp_bytes, cudaStream_t st);
 size_t radix_tmp_bytes(size_t n);
 
+// The text of direction dir packed 32 bases per 64-bit word, first base in the top bits
+// (n/32 + 4 words; the last words are zero padding).
+cudaError_t pack_text(const uint8_t* reads, size_t n, idx_t L, int dir, uint64_t* pk, cudaStream_t st);
+
 }  // namespace pq

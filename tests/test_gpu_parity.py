@@ -65,6 +65,25 @@ def test_seed_depth_does_not_change_edges(k):
     assert sha(out.num_F) == str(g["sha_num_F"])
 
 
+@pytest.mark.parametrize("name", ["rep15k_L100_t63_u32", "lowc12k_L150_t63_u64", "iid3k_L40_t10_u32"])
+def test_seed_modes_agree(name):
+    """Depth-t seeds by suffix-array search and by walking from the k-mer seed give the
+    reference's edges, and the search mode issues fewer probes."""
+    g = load_golden(name)
+    dt = idx_dtype(g["width"])
+    probes = {}
+    for mode in (0, 1):
+        with gpu_ctx(int(g["width"])) as P:
+            P.set_reads(g["reads"], int(g["t"]))
+            P.set_seed_mode(mode)
+            P.build_index()
+            out = P.construct_string_graph()
+        assert sha(out.dest.astype(dt)) == str(g["sha_dest"]), mode
+        assert sha(out.num_B) == str(g["sha_num_B"]) and sha(out.num_F) == str(g["sha_num_F"])
+        probes[mode] = out.probes
+    assert probes[1] < probes[0]
+
+
 def test_wide_tier_used_and_exact():
     """Dinucleotide runs give reads with many edges: some must go through the wide kernel."""
     g = load_golden("dinuc6k_L60_t20_u32")
