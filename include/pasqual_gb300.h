@@ -103,8 +103,9 @@ PQ_API int pq_get_seeds (pq_ctx * ctx, int dir, pq_idx * start, pq_idx * size, u
 /* Seed depth k of the overlap search (1 <= k <= min(13, t)); default min(12, t). */
 PQ_API int pq_set_seed_k (pq_ctx * ctx, int k);
 
-/* How each search reaches depth t: 1 (default, t <= 128) binary-searches the suffix arrays for
- * the depth-t intervals inside the k-mer table interval of the pattern's first k bases; 0 walks
+/* How each search reaches depth t: 1 (default; used when k + 8 <= t <= 128) binary-searches the
+ * suffix arrays for the depth-t intervals inside the k-mer table interval of the pattern's first
+ * k bases; 0 walks
  * from the depth-k seed with one synchronised step per base, as the reference walks from its
  * sort-recorded seed (src/string_graph.c:207-224).  Both give the same intervals. */
 PQ_API int pq_set_seed_mode (pq_ctx * ctx, int mode);

@@ -410,7 +410,9 @@ int pq_overlaps(pq_ctx* ctx) {
     A.L = ctx->L;
     A.t = ctx->t;
     A.seed_k = ctx->fm_k[0];
-    A.sa_seed = (ctx->seed_mode == 1 && ctx->t <= 128 && ctx->sa_ok[0] && ctx->sa_ok[1]) ? 1 : 0;
+    // a walk of fewer than 8 bases (2 probes a base) costs less than the bound searches
+    A.sa_seed = (ctx->seed_mode == 1 && ctx->t <= 128 && ctx->t - A.seed_k >= 8 && ctx->sa_ok[0] &&
+                 ctx->sa_ok[1]) ? 1 : 0;
 
     unsigned long long* ctr = ctx->ctrs.as<unsigned long long>();   // [0] e_count [1] probes [2] ovf(u32)
     pq::SearchOut O;
