@@ -103,11 +103,15 @@ PQ_API int pq_get_seeds (pq_ctx * ctx, int dir, pq_idx * start, pq_idx * size, u
 /* Seed depth k of the overlap search (1 <= k <= min(13, t)); default min(12, t). */
 PQ_API int pq_set_seed_k (pq_ctx * ctx, int k);
 
-/* How each search reaches depth t: 1 (default; used when k + 8 <= t <= 128) binary-searches the
- * suffix arrays for the depth-t intervals inside the k-mer table interval of the pattern's first
- * k bases; 0 walks
- * from the depth-k seed with one synchronised step per base, as the reference walks from its
- * sort-recorded seed (src/string_graph.c:207-224).  Both give the same intervals. */
+/* How the candidates of each read are found.  0 walks from the depth-k seed to depth L with one
+ * synchronised backward-search step per base, as the reference does from its sort-recorded seed
+ * (src/string_graph.c:207-237).  1 (default) finds the depth-t interval of the walked index by
+ * binary search over its suffix array inside the k-mer table interval of the pattern's first k
+ * bases, reads that interval's rows once (a read r' whose suffix at offset o matches, and whose
+ * first o bases continue the pattern, is a candidate at depth t + o) and takes the other index's
+ * interval from the inverse suffix array.  Mode 1 applies when t <= 64, L - t <= 128 and
+ * 4^t > 64 * num_reads * read_len (depth-t intervals are small), and a read whose depth-t
+ * interval exceeds 256 rows walks.  Both give the reference's candidates. */
 PQ_API int pq_set_seed_mode (pq_ctx * ctx, int mode);
 
 /* Overlap search with transitive reduction for every read: find_intervals +

@@ -1,5 +1,6 @@
 // pq_api.cu — the C ABI (include/pasqual_gb300.h): a context owning the device buffers of both
 // FM-indexes and the overlap-search output, and the entry points that sequence the kernels.
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -67,13 +68,13 @@ struct pq_ctx {
     idx_t num_reads = 0;
     int L = 0, t = 0;
     int seed_k = 0;
-    int seed_mode = 1;        // 1: depth-t seeds by suffix-array search, 0: walk from the k-mer seed
+    int seed_mode = 1;        // 1: candidates by depth-t interval scan, 0: walk from the k-mer seed
     DevBuf reads;
     idx_t C[6] = {0}, sfx[4] = {0}, pfx[4] = {0};
     bool have_reads = false;
 
     // per direction
-    DevBuf sa[2], blk[2], sb[2], ri[2], kstart[2], kend[2], pk[2];
+    DevBuf sa[2], blk[2], sb[2], ri[2], kstart[2], kend[2], pk[2], isa[2];
     bool sa_ok[2] = {false, false}, fm_ok[2] = {false, false};
     int fm_k[2] = {0, 0};
     DevBuf ktmp, sort_tmp, counts;
@@ -153,6 +154,7 @@ void pq_destroy(pq_ctx* ctx) {
         ctx->kstart[d].release();
         ctx->kend[d].release();
         ctx->pk[d].release();
+        ctx->isa[d].release();
     }
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -294,6 +296,7 @@ int pq_build_fm(pq_ctx* ctx, int dir) {
     CK(ctx->kend[dir].ensure(nk * sizeof(idx_t)));
     CK(ctx->ktmp.ensure(n * sizeof(uint32_t) + 64));
     CK(ctx->pk[dir].ensure((n / 32 + 4) * sizeof(uint64_t)));
+    CK(ctx->isa[dir].ensure(n * sizeof(idx_t) + 64));
     CK(cudaEventRecord(ctx->ev0, ctx->st));
     CK(pq::build_occ(ctx->sa[dir].as<idx_t>(), ctx->reads.as<uint8_t>(), ctx->num_reads, idx_t(ctx->L), dir,
                      ctx->blk[dir].as<OccBlock>(), ctx->sb[dir].as<idx_t>(), ctx->ri[dir].as<idx_t>(), ctx->st));
@@ -301,6 +304,7 @@ int pq_build_fm(pq_ctx* ctx, int dir) {
                             k, ctx->ktmp.as<uint32_t>(), ctx->kstart[dir].as<idx_t>(), ctx->kend[dir].as<idx_t>(),
                             ctx->st));
     CK(pq::pack_text(ctx->reads.as<uint8_t>(), n, idx_t(ctx->L), dir, ctx->pk[dir].as<uint64_t>(), ctx->st));
+    CK(pq::build_isa(ctx->sa[dir].as<idx_t>(), n, ctx->isa[dir].as<idx_t>(), ctx->st));
     CK(cudaEventRecord(ctx->ev1, ctx->st));
     CK(cudaEventSynchronize(ctx->ev1));
     cudaEventElapsedTime(&ctx->ms_fm, ctx->ev0, ctx->ev1);
@@ -401,6 +405,7 @@ int pq_overlaps(pq_ctx* ctx) {
         f.kend = ctx->kend[d].as<idx_t>();
         f.sa = ctx->sa[d].as<idx_t>();
         f.pk = ctx->pk[d].as<uint64_t>();
+        f.isa = ctx->isa[d].as<idx_t>();
         const idx_t* fix = d == 0 ? ctx->sfx : ctx->pfx;
         f.Cf[0] = ctx->C[0];
         for (int c = 1; c <= 4; ++c) f.Cf[c] = ctx->C[c] + fix[c - 1];
@@ -410,9 +415,14 @@ int pq_overlaps(pq_ctx* ctx) {
     A.L = ctx->L;
     A.t = ctx->t;
     A.seed_k = ctx->fm_k[0];
-    // a walk of fewer than 8 bases (2 probes a base) costs less than the bound searches
-    A.sa_seed = (ctx->seed_mode == 1 && ctx->t <= 128 && ctx->t - A.seed_k >= 8 && ctx->sa_ok[0] &&
-                 ctx->sa_ok[1]) ? 1 : 0;
+    // Interval scan where depth-t intervals are small: 4^t well above 64 n (chance hits rare) and
+    // patterns of up to 64 bases; otherwise the walk.
+    {
+        const double n = double(n_rows(ctx)) + 1.0;
+        const bool small_intervals = 2.0 * ctx->t > std::log2(n) + 6.0;
+        A.sa_seed = (ctx->seed_mode == 1 && small_intervals && ctx->t <= 64 && ctx->L - ctx->t <= 128 &&
+                     ctx->t > A.seed_k) ? 1 : 0;
+    }
 
     unsigned long long* ctr = ctx->ctrs.as<unsigned long long>();   // [0] e_count [1] probes [2] ovf(u32)
     pq::SearchOut O;

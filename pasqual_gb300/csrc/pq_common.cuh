@@ -51,6 +51,7 @@ struct FmView {
     const idx_t* kend;        // last row (kend < kstart when the k-mer is absent)
     const idx_t* sa;          // suffix array (for seeds found by binary search), or nullptr
     const uint64_t* pk;       // the text, 32 bases per word, first base in the top bits
+    const idx_t* isa;         // inverse suffix array (row of each text position), or nullptr
     idx_t Cf[5];              // Cf[0] = C[0]; Cf[c] = C[c] + fix[c]  (LF-mapping base)
 };
 

@@ -229,6 +229,12 @@ __global__ void k_kmer_bounds(const uint32_t* __restrict__ code, idx_t n, idx_t*
     }
 }
 
+// inverse suffix array: isa[sa[r]] = r
+__global__ void k_isa(const idx_t* __restrict__ sa, size_t n, idx_t* __restrict__ isa) {
+    const size_t stride = size_t(gridDim.x) * blockDim.x;
+    for (size_t r = size_t(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride) isa[sa[r]] = idx_t(r);
+}
+
 __global__ void k_fill_idx(idx_t* __restrict__ a, size_t m, idx_t v) {
     const size_t stride = size_t(gridDim.x) * blockDim.x;
     for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < m; i += stride) a[i] = v;
@@ -326,6 +332,11 @@ cudaError_t read_seeds(const uint8_t* reads, idx_t num_reads, int L, int dir, in
                        const idx_t* kend, idx_t* start, idx_t* size, cudaStream_t st) {
     if (num_reads)
         { k_read_seeds<<<grid_for(num_reads, 256), 256, 0, st>>>(reads, num_reads, L, dir, k, kstart, kend, start, size); note_launch(); }
+    return cudaGetLastError();
+}
+
+cudaError_t build_isa(const idx_t* sa, size_t n, idx_t* isa, cudaStream_t st) {
+    if (n) { k_isa<<<grid_for(n, 256), 256, 0, st>>>(sa, n, isa); note_launch(); }
     return cudaGetLastError();
 }
 

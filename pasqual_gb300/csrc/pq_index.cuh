@@ -11,6 +11,7 @@ cudaError_t read_counts(const uint8_t* reads, idx_t num_reads, idx_t L, unsigned
                         cudaStream_t st);
 cudaError_t build_kmer_table(const idx_t* sa, const uint8_t* reads, idx_t num_reads, idx_t L, int dir,
                              int k, uint32_t* code_tmp, idx_t* kstart, idx_t* kend, cudaStream_t st);
+cudaError_t build_isa(const idx_t* sa, size_t n, idx_t* isa, cudaStream_t st);
 cudaError_t export_ref_layout(const OccBlock* blk, const idx_t* sb, idx_t num_reads, idx_t L,
                               const idx_t fix[4], uint64_t* bitmap, idx_t* sample, cudaStream_t st);
 
@@ -41,7 +42,7 @@ struct SearchArgs {
     int L;
     int t;
     int seed_k;                 // k-mer seed depth (0 = start at depth 1 from C[])
-    int sa_seed;                // 1: depth-t intervals by suffix-array search (needs fm[].sa/pk)
+    int sa_seed;                // 1: candidates by depth-t interval scan (needs fm[].sa/pk/isa)
 };
 
 // Global scratch of the fast kernel, per warp of 32 reads: level-0 candidates (4 kinds x (L - t)

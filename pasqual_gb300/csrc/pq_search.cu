@@ -219,6 +219,241 @@ __device__ __forceinline__ bool live(int kind, idx_t l, idx_t u) {
 }
 __device__ __forceinline__ int walked_index(int kind) { return (kind == PQ_FB || kind == PQ_BB) ? 0 : 1; }
 
+__device__ __forceinline__ uint32_t pack_meta(int len, int type) { return uint32_t(len) | (uint32_t(type) << 16); }
+__device__ __forceinline__ int meta_len(uint32_t m) { return int(m & 0xffff); }
+__device__ __forceinline__ int meta_type(uint32_t m) { return int(m >> 16); }
+
+// ---------------------------------------------------------------- candidates by interval scan
+//
+// A candidate of kind `kind` at depth d (t <= d < L) is a read r' whose first d bases, in the
+// walked index's text, equal P_d = pat(d) .. pat(1).  Its last t bases there are P_t, so r'
+// appears in the depth-t interval I_t of the walked index as the row of its suffix at offset
+// o = d - t; conversely a row (r', o) of I_t with o < L - t is a candidate at depth t + o exactly
+// when r'[0, o) = pat(t + o) .. pat(t + 1).  So instead of walking from depth t to L one base at a
+// time (the reference's search_2/search_3 loop, src/string_graph.c:226-237), the rows of I_t are
+// read once: one suffix-array entry and one text comparison each, all independent loads.
+//
+// The reference stores, for each depth with candidates, the other index's interval of the
+// reversed pattern restricted to its `$` rows: the rows whose suffix is exactly rev(P_d) followed
+// by end-of-read.  Those are precisely the candidates' suffixes of length d in the other index
+// (text position r' * L + L - d), consecutive and ordered by position, so the interval is
+// [ISA(r'min * L + L - d), + count - 1] with r'min the smallest candidate.
+//
+// Chains are alive at depth d whenever a candidate exists there (a strict kind also holds the
+// read's own suffix, a second row), so the depths reported are the reference's.  I_t itself is
+// found by binary search over the suffix array inside the k-mer table interval of P_t's first k
+// bases, the two chains of a side searched together.  A row compares as its suffix string with
+// end-of-read lowest, the order of the backward search.
+
+constexpr int kScanWords = 2;       // depth-t patterns up to 64 bases
+constexpr int kScanMax = 256;       // larger depth-t intervals walk instead
+
+// 64 bases of packed text starting at base p (first base in the top bits)
+__device__ __forceinline__ uint64_t text_window(const uint64_t* __restrict__ pk, size_t p) {
+    const size_t w = p >> 5;
+    const int s = int(p & 31) * 2;
+    const uint64_t a = __ldg(pk + w), b = __ldg(pk + w + 1);
+    return s ? ((a << s) | (b >> (64 - s))) : a;
+}
+
+__device__ __forceinline__ uint64_t top_mask(int nbases) {      // 1 <= nbases <= 32
+    return nbases >= 32 ? ~uint64_t(0) : ~(~uint64_t(0) >> (2 * nbases));
+}
+
+// P = pat(t) .. pat(1) of `kind`, packed in the walked index's text order
+__device__ __forceinline__ void pack_pattern(const ReadView& rd, int L, int t, int kind,
+                                             uint64_t (&P)[kScanWords]) {
+    #pragma unroll
+    for (int w = 0; w < kScanWords; ++w) {
+        uint64_t x = 0;
+        for (int j = 0; j < 32; ++j) {
+            const int c = 32 * w + j;
+            x = (x << 2) | uint64_t(c < t ? pattern_at(rd, L, kind, t - c) - 1 : 0);
+        }
+        P[w] = x;
+    }
+}
+
+// -1 / 0 / +1: the suffix at text position p (m bases to end-of-read) is below / starts with /
+// above P (t bases)
+__device__ __forceinline__ int cmp_row(const uint64_t* __restrict__ pk, idx_t p, int m,
+                                       const uint64_t (&P)[kScanWords], int t) {
+    const int nb = m < t ? m : t;
+    const size_t w0 = size_t(p) >> 5;
+    const int s = int(p & 31) * 2;
+    const uint64_t a = __ldg(pk + w0), b = __ldg(pk + w0 + 1), c = __ldg(pk + w0 + 2);
+    const uint64_t x0 = s ? ((a << s) | (b >> (64 - s))) : a;
+    const uint64_t x1 = s ? ((b << s) | (c >> (64 - s))) : b;
+    const uint64_t k0 = top_mask(nb);
+    if ((x0 & k0) != (P[0] & k0)) return (x0 & k0) < (P[0] & k0) ? -1 : 1;
+    if (nb > 32) {
+        const uint64_t k1 = top_mask(nb - 32);
+        if ((x1 & k1) != (P[1] & k1)) return (x1 & k1) < (P[1] & k1) ? -1 : 1;
+    }
+    return m < t ? -1 : 0;
+}
+
+// Rows [first, end) of each chain's index that start with its pattern, searched within
+// [lo, hi): lower and upper bounds of both chains advance together (four independent searches).
+__device__ __forceinline__ void sa_bounds2(const FmView* f0, const FmView* f1, int L, const uint64_t (&P0)[kScanWords],
+                                           const uint64_t (&P1)[kScanWords], int t, const idx_t (&lo)[2],
+                                           const idx_t (&hi)[2], idx_t (&first)[2], idx_t (&end)[2],
+                                           uint32_t& probes) {
+    idx_t a0[2] = {lo[0], lo[1]}, a1[2] = {hi[0], hi[1]}, b0[2] = {lo[0], lo[1]}, b1[2] = {hi[0], hi[1]};
+    const FmView* fq[2] = {f0, f1};
+    while (a0[0] < a1[0] || b0[0] < b1[0] || a0[1] < a1[1] || b0[1] < b1[1]) {
+        idx_t pa[2], pb[2];
+        #pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            pa[q] = a0[q] < a1[q] ? __ldg(fq[q]->sa + (a0[q] + (a1[q] - a0[q]) / 2)) : 0;
+            pb[q] = b0[q] < b1[q] ? __ldg(fq[q]->sa + (b0[q] + (b1[q] - b0[q]) / 2)) : 0;
+        }
+        #pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const uint64_t (&P)[kScanWords] = q ? P1 : P0;
+            if (a0[q] < a1[q]) {
+                const idx_t ma = a0[q] + (a1[q] - a0[q]) / 2;
+                const int c = cmp_row(fq[q]->pk, pa[q], L - int(pa[q] % idx_t(L)), P, t);
+                if (c < 0) a0[q] = ma + 1;
+                else a1[q] = ma;
+                probes += 2;
+            }
+            if (b0[q] < b1[q]) {
+                const idx_t mb = b0[q] + (b1[q] - b0[q]) / 2;
+                const int c = cmp_row(fq[q]->pk, pb[q], L - int(pb[q] % idx_t(L)), P, t);
+                if (c <= 0) b0[q] = mb + 1;
+                else b1[q] = mb;
+                probes += 2;
+            }
+        }
+    }
+    first[0] = a0[0]; first[1] = a0[1];
+    end[0] = b0[0]; end[1] = b0[1];
+}
+
+// r'[0, o) (walked index text at ra) == pat(t + o) .. pat(t + 1): the read's own bases at
+// self * L + L - t - o of the walked index's text (strict kinds) or, complemented, of the other
+// index's text (FF, BB)
+__device__ __forceinline__ bool prefix_matches(const uint64_t* __restrict__ pka, size_t ra,
+                                               const uint64_t* __restrict__ pks, size_t rs, int o, bool cmpl) {
+    for (int c = 0; c < o; c += 32) {
+        const int m = o - c < 32 ? o - c : 32;
+        const uint64_t x = text_window(pka, ra + c);
+        uint64_t y = text_window(pks, rs + c);
+        if (cmpl) y = ~y;
+        if ((x ^ y) & top_mask(m)) return false;
+    }
+    return true;
+}
+
+// Slots of the level-0 candidates of the two chains of one side: q * M + i.
+struct SlotsFast {     // fast tier: the warp's global scratch
+    idx_t* ll;
+    idx_t* uu;
+    uint32_t* meta;
+    size_t base;
+    int M;
+    __device__ __forceinline__ void set(int q, int i, idx_t a, idx_t b, uint32_t m) const {
+        const size_t p = base + size_t(q) * M + i;
+        ll[p] = a;
+        uu[p] = b;
+        meta[p] = m;
+    }
+    __device__ __forceinline__ void get(int q, int i, idx_t& a, idx_t& b) const {
+        const size_t p = base + size_t(q) * M + i;
+        a = ll[p];
+        b = uu[p];
+    }
+};
+struct SlotsStack {    // wide tier: the slot's candidate stack
+    Cand* stk;
+    int M;
+    __device__ __forceinline__ void set(int q, int i, idx_t a, idx_t b, uint32_t m) const {
+        Cand& c = stk[q * M + i];
+        c.ll = a;
+        c.uu = b;
+        c.len = uint16_t(meta_len(m));
+        c.type = uint8_t(meta_type(m));
+    }
+    __device__ __forceinline__ void get(int q, int i, idx_t& a, idx_t& b) const {
+        a = stk[q * M + i].ll;
+        b = stk[q * M + i].uu;
+    }
+};
+
+// Candidates of both chains by interval scan; false (nothing stored) when a depth-t interval
+// holds more than kScanMax rows, and the caller walks instead.
+template <class Slots>
+__device__ __forceinline__ bool scan_pair(const SearchArgs& A, const FmView* fm, const ReadView& rd, idx_t self,
+                                          int k0, int k1, int (&n)[2], int32_t& olp, uint32_t& probes,
+                                          const Slots& slots) {
+    const int L = A.L, t = A.t, k = A.seed_k, M = L - t;
+    uint64_t P0[kScanWords], P1[kScanWords];
+    pack_pattern(rd, L, t, k0, P0);
+    pack_pattern(rd, L, t, k1, P1);
+    const FmView* f0 = fm + walked_index(k0);
+    const FmView* f1 = fm + walked_index(k1);
+    idx_t lo[2], hi[2], first[2], end[2];
+    {
+        const uint32_t c0 = uint32_t(P0[0] >> (64 - 2 * k)), c1 = uint32_t(P1[0] >> (64 - 2 * k));
+        lo[0] = __ldg(f0->kstart + c0);
+        hi[0] = __ldg(f0->kend + c0) + 1;
+        lo[1] = __ldg(f1->kstart + c1);
+        hi[1] = __ldg(f1->kend + c1) + 1;
+        probes += 2;
+        if (hi[0] < lo[0]) hi[0] = lo[0];
+        if (hi[1] < lo[1]) hi[1] = lo[1];
+    }
+    sa_bounds2(f0, f1, L, P0, P1, t, lo, hi, first, end, probes);
+    if (end[0] - first[0] > idx_t(kScanMax) || end[1] - first[1] > idx_t(kScanMax)) return false;
+    #pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const int kind = q ? k1 : k0;
+        const FmView& fa = *(q ? f1 : f0);
+        const FmView& fb = fm[1 - walked_index(kind)];
+        const bool cmpl = !(kind == PQ_FB || kind == PQ_BF);
+        const uint64_t* pks = cmpl ? fb.pk : fa.pk;
+        const size_t src = size_t(self) * L + size_t(L - t);     // minus o
+        uint64_t m0 = 0, m1 = 0;                                   // depths with candidates
+        for (idx_t row = first[q]; row < end[q]; ++row) {
+            const idx_t p = __ldg(fa.sa + row);
+            const idx_t rp = p / idx_t(L);
+            const int o = int(p - rp * idx_t(L));
+            probes += 2;
+            if (o >= M || !prefix_matches(fa.pk, size_t(rp) * L, pks, src - o, o, cmpl)) continue;
+            const uint64_t bit = uint64_t(1) << (o & 63);
+            const bool seen = ((o < 64 ? m0 : m1) & bit) != 0;
+            if (!seen) {
+                slots.set(q, o, rp, 1, 0);
+                if (o < 64) m0 |= bit;
+                else m1 |= bit;
+            } else {
+                idx_t r0, cnt;
+                slots.get(q, o, r0, cnt);
+                slots.set(q, o, rp < r0 ? rp : r0, cnt + 1, 0);
+            }
+        }
+        int i = 0;
+        #pragma unroll 1
+        for (int h = 0; h < 2; ++h) {
+            uint64_t m = h ? m1 : m0;
+            while (m) {
+                const int o = 64 * h + __ffsll((long long)m) - 1;
+                m &= m - 1;
+                idx_t r0, cnt;
+                slots.get(q, o, r0, cnt);
+                const int d = t + o;
+                const idx_t l0 = __ldg(fb.isa + (size_t(r0) * L + size_t(L - d)));
+                probes += 1;
+                slots.set(q, i++, l0, l0 + cnt - 1, pack_meta(d, kind));
+                olp = int32_t(uint32_t(olp) + uint32_t(cnt));
+            }
+        }
+        n[q] = i;
+    }
+    return true;
+}
+
 // find_intervals for one side: kinds k0 then k1 (B-F and B-B, or F-B and F-F), searched in
 // lockstep so that each thread keeps two independent chains of loads in flight.
 //
@@ -227,144 +462,27 @@ __device__ __forceinline__ int walked_index(int kind) { return (kind == PQ_FB ||
 // only then continues with synchronised search_2 steps.  Here both intervals start from exact
 // k-mer seeds (one per index) and every step is a synchronised step, so the other interval is
 // known at every depth and the rebuild disappears; SA intervals are unique per string, so the
-// intervals at depth t -- and everything after -- are the reference's.  The i-th stored candidate
-// of kind k0 (q = 0) or k1 (q = 1) goes to sink(q, i, ll, uu, depth, kind); n[q] counts them.
-// ---------------------------------------------------------------- depth-t seeds by SA search
-//
-// The walk from the k-mer seed to depth t only serves to find two SA intervals: the rows of the
-// walked index that start with P = pat(t) .. pat(1) and the rows of the other index that start
-// with its reverse.  Both are found directly here by binary search over the suffix arrays,
-// inside the table interval of the pattern's first k bases: about log2(interval) steps of two
-// dependent loads (SA entry, then 64 bases of text) per bound instead of t - k steps.  A row
-// compares as its suffix string with end-of-read lowest, so the bounds are exactly the rows the
-// backward search reaches.  A search that dies before depth t (the interval shrinks to one row,
-// or to none) is dead at depth t too -- interval sizes only shrink with depth -- so the chain
-// continues exactly when the reference's does.
-
-constexpr int kSeedWords = 4;       // patterns up to 128 bases (longer t walks instead)
-
-// base c (0-based) of the pattern in text order for index A (dir 0) or its reverse (dir 1)
-__device__ __forceinline__ int seed_base(const ReadView& rd, int L, int t, int kind, int dir, int c) {
-    return pattern_at(rd, L, kind, dir == 0 ? t - c : c + 1);
-}
-
-__device__ __forceinline__ void pack_pattern(const ReadView& rd, int L, int t, int kind, int dir,
-                                             uint64_t (&P)[kSeedWords]) {
-    #pragma unroll
-    for (int w = 0; w < kSeedWords; ++w) {
-        uint64_t x = 0;
-        for (int j = 0; j < 32; ++j) {
-            const int c = 32 * w + j;
-            x = (x << 2) | uint64_t(c < t ? seed_base(rd, L, t, kind, dir, c) - 1 : 0);
-        }
-        P[w] = x;
-    }
-}
-
-// -1 / 0 / +1: row suffix (m bases at text position p) is below / starts with / above P (t bases)
-__device__ __forceinline__ int cmp_row(const uint64_t* __restrict__ pk, idx_t p, int m, const uint64_t (&P)[kSeedWords],
-                                       int t) {
-    const int nb = m < t ? m : t;
-    const size_t w0 = size_t(p) >> 5;
-    const int s = int(p & 31) * 2;
-    uint64_t prev = __ldg(pk + w0);
-    #pragma unroll
-    for (int w = 0; w < kSeedWords; ++w) {
-        const int v = nb - 32 * w;
-        if (v <= 0) break;
-        const uint64_t next = __ldg(pk + w0 + w + 1);
-        uint64_t x = s ? ((prev << s) | (next >> (64 - s))) : prev;
-        prev = next;
-        const uint64_t mask = v >= 32 ? ~uint64_t(0) : (~uint64_t(0) << (64 - 2 * v));
-        x &= mask;
-        const uint64_t y = P[w] & mask;
-        if (x != y) return x < y ? -1 : 1;
-    }
-    return m < t ? -1 : 0;
-}
-
-// rows of index f whose suffix starts with P, searched within [lo, hi): returns [first, end)
-__device__ __forceinline__ void sa_bounds(const FmView& f, int L, const uint64_t (&P)[kSeedWords], int t, idx_t lo,
-                                          idx_t hi, idx_t& first, idx_t& end, uint32_t& probes) {
-    idx_t a0 = lo, a1 = hi, b0 = lo, b1 = hi;     // lower bound in [a0, a1), upper bound in [b0, b1)
-    while (a0 < a1 || b0 < b1) {
-        const bool ga = a0 < a1, gb = b0 < b1;
-        const idx_t ma = a0 + (a1 - a0) / 2, mb = b0 + (b1 - b0) / 2;
-        idx_t pa = 0, pb = 0;
-        if (ga) pa = __ldg(f.sa + ma);
-        if (gb) pb = __ldg(f.sa + mb);
-        if (ga) {
-            const int c = cmp_row(f.pk, pa, L - int(pa % idx_t(L)), P, t);
-            if (c < 0) a0 = ma + 1;
-            else a1 = ma;
-            probes += 2;
-        }
-        if (gb) {
-            const int c = cmp_row(f.pk, pb, L - int(pb % idx_t(L)), P, t);
-            if (c <= 0) b0 = mb + 1;
-            else b1 = mb;
-            probes += 2;
-        }
-    }
-    first = a0;
-    end = b0;
-}
-
-// the walked index's interval [l, u] of pat(t)..pat(1) and the other index's [ll, uu] of its
-// reverse; an empty interval comes back as l = 1 > u = 0
-__device__ __forceinline__ void sa_seed(const FmView& fa, const FmView& fb, const ReadView& rd, int L, int t, int k,
-                                        int kind, idx_t& l, idx_t& u, idx_t& ll, idx_t& uu, uint32_t& probes) {
-    uint64_t P[kSeedWords];
-    idx_t s0, s1;
-    // walked index: prefix of P is pat(t) .. pat(t-k+1)
-    pack_pattern(rd, L, t, kind, 0, P);
-    {
-        uint32_t code = uint32_t(P[0] >> (64 - 2 * k));
-        const idx_t lo = __ldg(fa.kstart + code), hi = __ldg(fa.kend + code) + 1;
-        probes += 1;
-        sa_bounds(fa, L, P, t, lo, lo < hi ? hi : lo, s0, s1, probes);
-    }
-    if (s0 < s1) { l = s0; u = s1 - 1; }
-    else { l = 1; u = 0; }
-    pack_pattern(rd, L, t, kind, 1, P);
-    {
-        uint32_t code = uint32_t(P[0] >> (64 - 2 * k));
-        const idx_t lo = __ldg(fb.kstart + code), hi = __ldg(fb.kend + code) + 1;
-        probes += 1;
-        sa_bounds(fb, L, P, t, lo, lo < hi ? hi : lo, s0, s1, probes);
-    }
-    if (s0 < s1) { ll = s0; uu = s1 - 1; }
-    else { ll = 1; uu = 0; }
-}
-
-template <class Sink>
-__device__ __forceinline__ void chain_pair(const SearchArgs& A, const FmView* fm, const ReadView& rd, int k0, int k1,
-                                           int (&n)[2], int32_t& olp, uint32_t& probes, Sink sink) {
+// intervals at depth t -- and everything after -- are the reference's.  With A.sa_seed the
+// candidates come from the interval scan above instead, unless a depth-t interval is too large.
+// The i-th stored candidate of kind k0 (q = 0) or k1 (q = 1) goes to slot (q, i); n[q] counts them.
+template <class Slots>
+__device__ __forceinline__ void chain_pair(const SearchArgs& A, const FmView* fm, const ReadView& rd, idx_t self,
+                                           int k0, int k1, int (&n)[2], int32_t& olp, uint32_t& probes,
+                                           const Slots& slots) {
     const int L = A.L, t = A.t, k = A.seed_k;
+    n[0] = n[1] = 0;
+    if (A.sa_seed && scan_pair(A, fm, rd, self, k0, k1, n, olp, probes, slots)) return;
     idx_t l[2], u[2], ll[2], uu[2];
     bool alive[2];
-    n[0] = n[1] = 0;
-    int d;
-    if (A.sa_seed) {
-        #pragma unroll
-        for (int q = 0; q < 2; ++q) {
-            const int kind = q ? k1 : k0;
-            const int ia = walked_index(kind);
-            sa_seed(fm[ia], fm[1 - ia], rd, L, t, k, kind, l[q], u[q], ll[q], uu[q], probes);
-            alive[q] = live(kind, l[q], u[q]);
-        }
-        d = t;
-    } else {
-        #pragma unroll
-        for (int q = 0; q < 2; ++q) {
-            const int kind = q ? k1 : k0;
-            const int ia = walked_index(kind);
-            kmer_seed(fm[ia], rd, L, kind, k, 1, -1, l[q], u[q], probes);       // pat(k) .. pat(1)
-            kmer_seed(fm[1 - ia], rd, L, kind, 1, k, 1, ll[q], uu[q], probes);  // pat(1) .. pat(k)
-            alive[q] = live(kind, l[q], u[q]);
-        }
-        d = k;
+    #pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const int kind = q ? k1 : k0;
+        const int ia = walked_index(kind);
+        kmer_seed(fm[ia], rd, L, kind, k, 1, -1, l[q], u[q], probes);       // pat(k) .. pat(1)
+        kmer_seed(fm[1 - ia], rd, L, kind, 1, k, 1, ll[q], uu[q], probes);  // pat(1) .. pat(k)
+        alive[q] = live(kind, l[q], u[q]);
     }
+    int d = k;
     while (d < t && (alive[0] || alive[1])) {
         #pragma unroll
         for (int q = 0; q < 2; ++q) {
@@ -397,7 +515,7 @@ __device__ __forceinline__ void chain_pair(const SearchArgs& A, const FmView* fm
             // extended, and level 0 never runs the emission check (its max length plus level 0
             // cannot reach L), so it can never contribute and is not stored.
             const idx_t tmp = (vu - (ru[0] + ru[1] + ru[2] + ru[3])) - (vl - (rl[0] + rl[1] + rl[2] + rl[3])) - 1;
-            if (tmp + 1 != 0) sink(q, n[q]++, ll[q], ll[q] + tmp, d, kind);
+            if (tmp + 1 != 0) slots.set(q, n[q]++, ll[q], ll[q] + tmp, pack_meta(d, kind));
             olp = int32_t(uint32_t(olp) + uint32_t(tmp + 1));
             step_from_ranks(f, pattern_at(rd, L, kind, d + 1), vl, vu, rl, ru, l[q], u[q], ll[q], uu[q]);
             alive[q] = live(kind, l[q], u[q]);
@@ -407,19 +525,13 @@ __device__ __forceinline__ void chain_pair(const SearchArgs& A, const FmView* fm
 }
 
 // One side's candidates into the thread's stack: kind k0 then k1, the reference's order.
-__device__ __forceinline__ int side_candidates(const SearchArgs& A, const FmView* fm, const ReadView& rd, int k0,
-                                               int k1, Cand* stk, int cap, int& n_out, int32_t& olp,
+__device__ __forceinline__ int side_candidates(const SearchArgs& A, const FmView* fm, const ReadView& rd, idx_t self,
+                                               int k0, int k1, Cand* stk, int cap, int& n_out, int32_t& olp,
                                                uint32_t& probes) {
     const int M = A.L - A.t;
     if (2 * M > cap) return OVF_STACK;
     int n[2];
-    chain_pair(A, fm, rd, k0, k1, n, olp, probes, [&](int q, int i, idx_t l0, idx_t u0, int d, int kind) {
-        Cand& c = stk[q * M + i];
-        c.ll = l0;
-        c.uu = u0;
-        c.len = uint16_t(d);
-        c.type = uint8_t(kind);
-    });
+    chain_pair(A, fm, rd, self, k0, k1, n, olp, probes, SlotsStack{stk, M});
     for (int i = 0; i < n[1]; ++i) stk[n[0] + i] = stk[M + i];
     n_out = n[0] + n[1];
     return OVF_NONE;
@@ -564,7 +676,7 @@ __device__ __forceinline__ ReadResult search_read(const SearchArgs& A, const FmV
     R.ne = 0;
     int n0 = 0, sc = 0;
     // B side: B-F then B-B candidates, then extract_bw_edges (src/string_graph.c:824-825)
-    int s = side_candidates(A, fm, rd, PQ_BF, PQ_BB, stk, cap, n0, R.olpB, probes);
+    int s = side_candidates(A, fm, rd, self, PQ_BF, PQ_BB, stk, cap, n0, R.olpB, probes);
     if (s == OVF_NONE && R.olpB != 0)
         s = reduce_side(A, fm, self, stk, cap, n0, fr, frcap, eb, ebcap, R.ne, sc, probes);
     if (s != OVF_NONE) { R.status = s; return R; }
@@ -572,7 +684,7 @@ __device__ __forceinline__ ReadResult search_read(const SearchArgs& A, const FmV
     // F side: F-B then F-F candidates, then extract_fw_edges (src/string_graph.c:828-829)
     n0 = 0;
     sc = 0;
-    s = side_candidates(A, fm, rd, PQ_FB, PQ_FF, stk, cap, n0, R.olpF, probes);
+    s = side_candidates(A, fm, rd, self, PQ_FB, PQ_FF, stk, cap, n0, R.olpF, probes);
     if (s == OVF_NONE && R.olpF != 0)
         s = reduce_side(A, fm, self, stk, cap, n0, fr, frcap, eb, ebcap, R.ne, sc, probes);
     if (s != OVF_NONE) { R.status = s; return R; }
@@ -649,9 +761,6 @@ constexpr int kTaskCap = 512;       // stack intervals per (read, side) task
 constexpr int kTaskFrames = 48;     // DFS levels per task (deeper reads go to the wide kernel)
 constexpr int kPMax = 128;          // intervals of one level of one task
 
-__device__ __forceinline__ uint32_t pack_meta(int len, int type) { return uint32_t(len) | (uint32_t(type) << 16); }
-__device__ __forceinline__ int meta_len(uint32_t m) { return int(m & 0xffff); }
-__device__ __forceinline__ int meta_type(uint32_t m) { return int(m >> 16); }
 __device__ __forceinline__ int csz_at(uint64_t c4, int i) { return int((c4 >> (16 * i)) & 0xffff); }
 
 // One DFS level of one task (the reference's recursion frame of extract_*_edges).
@@ -754,18 +863,11 @@ __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A, SearchOut 
             load_read(A, idx_t(r), s_reads + threadIdx.x, blockDim.x);
             ReadView rd{s_reads + threadIdx.x, int(blockDim.x)};
             const size_t cb = cbase_w + size_t(lane) * 4 * M;
-            auto sink = [&](int qbase) {
-                return [=](int q, int i, idx_t l0, idx_t u0, int d, int kind) {
-                    const size_t p = cb + size_t(qbase + q) * M + i;
-                    S.c_ll[p] = l0;
-                    S.c_uu[p] = u0;
-                    S.c_meta[p] = pack_meta(d, kind);
-                };
-            };
             int nb[2], nf[2];
             int32_t ob = 0, of = 0;
-            chain_pair(A, s_fm, rd, PQ_BF, PQ_BB, nb, ob, probes, sink(0));
-            chain_pair(A, s_fm, rd, PQ_FB, PQ_FF, nf, of, probes, sink(2));
+            chain_pair(A, s_fm, rd, self, PQ_BF, PQ_BB, nb, ob, probes, SlotsFast{S.c_ll, S.c_uu, S.c_meta, cb, M});
+            chain_pair(A, s_fm, rd, self, PQ_FB, PQ_FF, nf, of, probes,
+                       SlotsFast{S.c_ll, S.c_uu, S.c_meta, cb + 2 * size_t(M), M});
             s_n[wid][lane][0] = nb[0];
             s_n[wid][lane][1] = nb[1];
             s_n[wid][lane][2] = nf[0];
