@@ -109,9 +109,10 @@ PQ_API int pq_set_seed_k (pq_ctx * ctx, int k);
  * binary search over its suffix array inside the k-mer table interval of the pattern's first k
  * bases, reads that interval's rows once (a read r' whose suffix at offset o matches, and whose
  * first o bases continue the pattern, is a candidate at depth t + o) and takes the other index's
- * interval from the inverse suffix array.  Mode 1 applies when t <= 64, L - t <= 128 and
- * 4^t > 64 * num_reads * read_len (depth-t intervals are small), and a read whose depth-t
- * interval exceeds 256 rows walks.  Both give the reference's candidates. */
+ * interval from the inverse suffix array.  2 is mode 1 with the learned index's window in place
+ * of the k-mer table's (t >= 16).  Modes 1 and 2 apply when t <= 64, L - t <= 128 and
+ * 4^t > 64 * num_reads * read_len (depth-t intervals are small); a read whose depth-t interval
+ * exceeds 256 rows walks.  All modes give the reference's candidates. */
 PQ_API int pq_set_seed_mode (pq_ctx * ctx, int mode);
 
 /* Overlap search with transitive reduction for every read: find_intervals +
@@ -155,6 +156,56 @@ PQ_API int pq_get_stage_ms (pq_ctx * ctx, float *sort_ms, float *fm_ms, float *s
  * or PQ_ERR_CUDA. */
 PQ_API int pq_suffix_sort_static (const uint8_t * reads_dev, pq_idx num_reads, int read_len,
                                   int dir, pq_idx * sa_dev, void *cuda_stream);
+
+/* ---- Learned index (no counterpart in the reference) ---------------------------------------
+ *
+ * A model of each suffix array, trained on the GPU right after the index is built: the first 16
+ * bases of a row's suffix, 2 bits a base (bases past the end of the read = A), form a 32-bit key
+ * that never decreases down the suffix array.  The distinct keys are cut into up to 1024 segments
+ * of equal key count; a piecewise-linear root maps a key onto its segment's rows and a per-segment
+ * 2-layer MLP (1 -> 64 ReLU -> 1, FP32) corrects it.  After training, every key present is
+ * predicted once and each segment stores the two int32 bounds e_lo, e_hi such that the key's
+ * whole row group lies in [pred - e_lo, pred + e_hi).  Seed mode 2 (pq_set_seed_mode) replaces
+ * the k-mer table window of mode 1 by that window: one inference per search, a bounded binary
+ * search inside it, a check of the two rows just outside it, and the plain backward search of
+ * mode 0 whenever the check fails. */
+typedef struct pq_learned_info {
+    uint64_t num_keys;          /* distinct keys in the suffix array */
+    int32_t segments;           /* root segments */
+    int32_t hidden;             /* hidden units of each segment's MLP (64) */
+    int32_t steps;              /* Adam steps of the training */
+    float keys_ms;              /* key extraction and distinct-key pass */
+    float train_ms;             /* training kernel */
+    float eval_ms;              /* error pass over every key */
+    double mean_window;         /* mean over keys of their segment's e_lo + e_hi, trained model */
+    double mean_window_root;    /* the same for the root alone (untrained network) */
+    int64_t max_window;         /* largest e_lo + e_hi over segments, trained model */
+    int64_t max_window_root;
+    uint64_t queries;           /* window inferences of the last pq_overlaps in seed mode 2 */
+    uint64_t misses;            /* of those, windows whose check failed (searches that walked) */
+} pq_learned_info;
+
+/* Build (or rebuild) direction dir's learned index with `steps` training steps (0 = the root
+ * alone: the MLP outputs 0).  Needs pq_build_fm(dir).  Seed mode 2 builds missing models itself
+ * with 400 steps. */
+PQ_API int pq_learned_build (pq_ctx * ctx, int dir, int steps);
+PQ_API int pq_learned_get_info (pq_ctx * ctx, int dir, pq_learned_info * info);
+/* Copy the model out: bnd[segments], base[segments + 1], params[segments * 196] (w1[64] b1[64]
+ * w2[64] b2, padded), err[2 * segments] and err_root[2 * segments] (e_lo, e_hi of each segment). */
+PQ_API int pq_learned_export (pq_ctx * ctx, int dir, uint32_t * bnd, pq_idx * base, float *params,
+                              int32_t * err, int32_t * err_root);
+/* Predicted row (and segment) of n keys, with the search's own function; host arrays. */
+PQ_API int pq_learned_predict (pq_ctx * ctx, int dir, const uint32_t * keys, uint64_t n, int64_t * pred,
+                               int32_t * seg);
+/* The distinct keys of direction dir's suffix array and the first row of each (up to cap of
+ * them); *num_keys = their number. */
+PQ_API int pq_learned_keys (pq_ctx * ctx, int dir, uint32_t * keys, pq_idx * first_row, uint64_t cap,
+                            uint64_t * num_keys);
+/* The network of one segment on its own, on the current CUDA device (host arrays; params is one
+ * 196-float record): y[i] = mlp(x[i]), and grad[193] = d/d(w1, b1, w2, b2) of sum_i dy[i] * mlp(x[i]).
+ * These are the kernels the training runs. */
+PQ_API int pq_mlp_forward (const float *params, const float *x, int n, float *y);
+PQ_API int pq_mlp_backward (const float *params, const float *x, const float *dy, int n, float *grad);
 
 /* Duration (ms, CUDA events on the context stream) of the fast search kernel in the last
  * pq_overlaps, and the number of kernels this library has launched since it was loaded. */

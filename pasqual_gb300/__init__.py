@@ -21,7 +21,8 @@ import numpy as np
 
 from . import build as _build
 
-__all__ = ["Pasqual", "Graph", "PQError", "load_library", "library_path", "EXPORTS"]
+__all__ = ["Pasqual", "Graph", "PQError", "load_library", "library_path", "EXPORTS", "mlp_forward",
+           "mlp_backward", "LearnedInfo"]
 
 PQ_ERRORS = {1: "PQ_ERR_ARG", 2: "PQ_ERR_CUDA", 3: "PQ_ERR_NOMEM", 4: "PQ_ERR_TOO_MANY_EDGES",
              5: "PQ_ERR_STATE", 6: "PQ_ERR_CAPACITY", 7: "PQ_ERR_INTERNAL"}
@@ -31,7 +32,8 @@ EXPORTS = ["pq_idx_bytes", "pq_create", "pq_destroy", "pq_last_error", "pq_set_r
            "pq_get_counts", "pq_sort", "pq_set_sa", "pq_get_sa", "pq_build_fm", "pq_build_index",
            "pq_get_index_ref", "pq_get_seeds", "pq_set_seed_k", "pq_set_seed_mode", "pq_overlaps",
            "pq_get_graph_sizes", "pq_get_graph", "pq_get_stage_ms", "pq_get_kernel_stats",
-           "pq_suffix_sort_static"]
+           "pq_suffix_sort_static", "pq_learned_build", "pq_learned_get_info", "pq_learned_export",
+           "pq_learned_predict", "pq_learned_keys", "pq_mlp_forward", "pq_mlp_backward"]
 
 
 # The reference's own entry points served by the same library (include/pasqual_gb300_dropin.h).
@@ -83,6 +85,13 @@ def load_library(width: int = 32) -> ct.CDLL:
         "pq_get_graph": (c_int, [vp] + [vp] * 9),
         "pq_get_stage_ms": (c_int, [vp, vp, vp, vp]),
         "pq_get_kernel_stats": (c_int, [vp, vp, vp]),
+        "pq_learned_build": (c_int, [vp, c_int, c_int]),
+        "pq_learned_get_info": (c_int, [vp, c_int, vp]),
+        "pq_learned_export": (c_int, [vp, c_int, vp, vp, vp, vp, vp]),
+        "pq_learned_predict": (c_int, [vp, c_int, vp, ct.c_uint64, vp, vp]),
+        "pq_learned_keys": (c_int, [vp, c_int, vp, vp, ct.c_uint64, vp]),
+        "pq_mlp_forward": (c_int, [vp, vp, c_int, vp]),
+        "pq_mlp_backward": (c_int, [vp, vp, vp, c_int, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -92,6 +101,47 @@ def load_library(width: int = 32) -> ct.CDLL:
         raise RuntimeError("library %s has the wrong index width" % path)
     _LIBS[width] = lib
     return lib
+
+
+class LearnedInfo(ct.Structure):
+    """pq_learned_info of include/pasqual_gb300.h."""
+    _fields_ = [("num_keys", ct.c_uint64), ("segments", ct.c_int32), ("hidden", ct.c_int32),
+                ("steps", ct.c_int32), ("keys_ms", ct.c_float), ("train_ms", ct.c_float),
+                ("eval_ms", ct.c_float), ("mean_window", ct.c_double), ("mean_window_root", ct.c_double),
+                ("max_window", ct.c_int64), ("max_window_root", ct.c_int64), ("queries", ct.c_uint64),
+                ("misses", ct.c_uint64)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+LX_STRIDE = 196      # floats per segment record: w1[64] b1[64] w2[64] b2, padded
+LX_HIDDEN = 64
+
+
+def mlp_forward(params: np.ndarray, x: np.ndarray, width: int = 32) -> np.ndarray:
+    """The learned index's per-segment network on the GPU: y = mlp(x) (params: one record)."""
+    lib = load_library(width)
+    params = np.ascontiguousarray(params, np.float32)
+    x = np.ascontiguousarray(x, np.float32)
+    y = np.empty_like(x)
+    rc = lib.pq_mlp_forward(_p(params), _p(x), len(x), _p(y))
+    if rc != 0:
+        raise PQError(rc, "pq_mlp_forward")
+    return y
+
+
+def mlp_backward(params: np.ndarray, x: np.ndarray, dy: np.ndarray, width: int = 32) -> np.ndarray:
+    """Gradient of sum(dy * mlp(x)) with respect to (w1, b1, w2, b2), 193 values, on the GPU."""
+    lib = load_library(width)
+    params = np.ascontiguousarray(params, np.float32)
+    x = np.ascontiguousarray(x, np.float32)
+    dy = np.ascontiguousarray(dy, np.float32)
+    g = np.empty(3 * LX_HIDDEN + 1, np.float32)
+    rc = lib.pq_mlp_backward(_p(params), _p(x), _p(dy), len(x), _p(g))
+    if rc != 0:
+        raise PQError(rc, "pq_mlp_backward")
+    return g
 
 
 @dataclass
@@ -164,7 +214,8 @@ class Pasqual:
         self._ck(self.lib.pq_set_seed_k(self.h, int(k)), "pq_set_seed_k")
 
     def set_seed_mode(self, mode: int) -> None:
-        """1: depth-t seeds by suffix-array search (default); 0: walk from the k-mer seed."""
+        """0: walk from the k-mer seed; 1: depth-t interval scan (default); 2: the scan with
+        learned-index windows."""
         self._ck(self.lib.pq_set_seed_mode(self.h, int(mode)), "pq_set_seed_mode")
 
     def sort(self, direction: int) -> None:
@@ -247,6 +298,43 @@ class Pasqual:
         self._ck(self.lib.pq_get_kernel_stats(self.h, ct.byref(ms), ct.byref(n)),
                  "pq_get_kernel_stats")
         return ms.value, n.value
+
+    # -- learned index -----------------------------------------------------------------------
+    def learned_build(self, direction: int, steps: int = 400) -> None:
+        self._ck(self.lib.pq_learned_build(self.h, direction, int(steps)), "pq_learned_build")
+
+    def learned_info(self, direction: int) -> dict:
+        info = LearnedInfo()
+        self._ck(self.lib.pq_learned_get_info(self.h, direction, ct.byref(info)), "pq_learned_get_info")
+        return info.as_dict()
+
+    def learned_export(self, direction: int) -> dict:
+        S = self.learned_info(direction)["segments"]
+        out = {"bnd": np.empty(S, np.uint32), "base": np.empty(S + 1, self.dt),
+               "params": np.empty((S, LX_STRIDE), np.float32), "err": np.empty((S, 2), np.int32),
+               "err_root": np.empty((S, 2), np.int32)}
+        self._ck(self.lib.pq_learned_export(self.h, direction, _p(out["bnd"]), _p(out["base"]),
+                                            _p(out["params"]), _p(out["err"]), _p(out["err_root"])),
+                 "pq_learned_export")
+        return out
+
+    def learned_predict(self, direction: int, keys: np.ndarray):
+        keys = np.ascontiguousarray(keys, np.uint32)
+        pred = np.empty(len(keys), np.int64)
+        seg = np.empty(len(keys), np.int32)
+        self._ck(self.lib.pq_learned_predict(self.h, direction, _p(keys), len(keys), _p(pred), _p(seg)),
+                 "pq_learned_predict")
+        return pred, seg
+
+    def learned_keys(self, direction: int):
+        """Distinct 16-base keys of the suffix array and the first row of each."""
+        n = self.num_reads * self.read_len
+        keys = np.empty(max(n, 1), np.uint32)
+        first = np.empty(max(n, 1), self.dt)
+        m = ct.c_uint64()
+        self._ck(self.lib.pq_learned_keys(self.h, direction, _p(keys), _p(first), n, ct.byref(m)),
+                 "pq_learned_keys")
+        return keys[:m.value], first[:m.value]
 
     def stage_ms(self):
         a, b, c = ct.c_float(), ct.c_float(), ct.c_float()

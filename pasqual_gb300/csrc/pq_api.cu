@@ -9,6 +9,7 @@
 
 #include "pq_index.cuh"
 #include "pq_sort.cuh"
+#include "pq_learned_build.cuh"
 #include "../../include/pasqual_gb300.h"
 
 static_assert(sizeof(pq_idx) == sizeof(idx_t), "pq_idx and idx_t must agree");
@@ -79,6 +80,13 @@ struct pq_ctx {
     int fm_k[2] = {0, 0};
     DevBuf ktmp, sort_tmp, counts;
 
+    // learned index per direction (pq_learned.cu)
+    DevBuf lx_bnd[2], lx_base[2], lx_par[2], lx_err[2], lx_err_root[2], lx_segof[2], lx_tmp;
+    int lx_segs[2] = {0, 0};
+    bool lx_ok[2] = {false, false};
+    pq_learned_info lx_info[2] = {};
+    uint64_t lx_queries = 0, lx_misses = 0;
+
     // overlap-search output
     DevBuf nB, nF, oB, oF, status, esrc, e_dest, e_trans, e_len, e_type, ctrs, ovf_list;
     DevBuf off, g_dest, g_len, g_type, g_trans, asm_tmp, wide, warp_scratch;
@@ -103,6 +111,19 @@ static inline size_t n_rows(const pq_ctx* c) { return size_t(c->num_reads) * siz
 static inline size_t n_blocks(const pq_ctx* c) { return n_rows(c) / 64 + 1; }
 static inline size_t n_supers(const pq_ctx* c) {
     return (n_blocks(c) + kBlocksPerSuper - 1) / kBlocksPerSuper;
+}
+
+static constexpr int kLxDefaultSteps = 400;
+
+static LearnedView lx_view(const pq_ctx* c, int d) {
+    LearnedView v;
+    v.bnd = c->lx_bnd[d].as<uint32_t>();
+    v.base = c->lx_base[d].as<idx_t>();
+    v.par = c->lx_par[d].as<float>();
+    v.err = c->lx_err[d].as<int32_t>();
+    v.segof = c->lx_segof[d].as<uint16_t>();
+    v.segs = c->lx_ok[d] ? c->lx_segs[d] : 0;
+    return v;
 }
 
 extern "C" {
@@ -155,6 +176,12 @@ void pq_destroy(pq_ctx* ctx) {
         ctx->kend[d].release();
         ctx->pk[d].release();
         ctx->isa[d].release();
+        ctx->lx_bnd[d].release();
+        ctx->lx_base[d].release();
+        ctx->lx_par[d].release();
+        ctx->lx_err[d].release();
+        ctx->lx_err_root[d].release();
+        ctx->lx_segof[d].release();
     }
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -276,7 +303,8 @@ int pq_set_seed_k(pq_ctx* ctx, int k) {
 
 int pq_set_seed_mode(pq_ctx* ctx, int mode) {
     if (!ctx) return PQ_ERR_ARG;
-    if (mode != 0 && mode != 1) return fail(ctx, PQ_ERR_ARG, "seed mode must be 0 (walk) or 1 (suffix-array search)");
+    if (mode < 0 || mode > 2)
+        return fail(ctx, PQ_ERR_ARG, "seed mode must be 0 (walk), 1 (interval scan) or 2 (learned windows)");
     ctx->seed_mode = mode;
     ctx->graph_ok = false;
     return PQ_OK;
@@ -310,6 +338,7 @@ int pq_build_fm(pq_ctx* ctx, int dir) {
     cudaEventElapsedTime(&ctx->ms_fm, ctx->ev0, ctx->ev1);
     ctx->fm_ok[dir] = true;
     ctx->fm_k[dir] = k;
+    ctx->lx_ok[dir] = false;
     ctx->graph_ok = false;
     return PQ_OK;
 }
@@ -416,13 +445,25 @@ int pq_overlaps(pq_ctx* ctx) {
     A.t = ctx->t;
     A.seed_k = ctx->fm_k[0];
     // Interval scan where depth-t intervals are small: 4^t well above 64 n (chance hits rare) and
-    // patterns of up to 64 bases; otherwise the walk.
+    // patterns of up to 64 bases; otherwise the walk.  Learned windows need 16-base keys.
     {
         const double n = double(n_rows(ctx)) + 1.0;
         const bool small_intervals = 2.0 * ctx->t > std::log2(n) + 6.0;
-        A.sa_seed = (ctx->seed_mode == 1 && small_intervals && ctx->t <= 64 && ctx->L - ctx->t <= 128 &&
-                     ctx->t > A.seed_k) ? 1 : 0;
+        const bool scan = small_intervals && ctx->t <= 64 && ctx->L - ctx->t <= 128 && ctx->t > A.seed_k;
+        A.sa_seed = 0;
+        if (scan && ctx->seed_mode == 1) A.sa_seed = 1;
+        if (scan && ctx->seed_mode == 2 && ctx->t >= pq::kLxKeyBases && nr) {
+            for (int d = 0; d < 2; ++d) {
+                if (!ctx->lx_ok[d]) {
+                    const int rc = pq_learned_build(ctx, d, kLxDefaultSteps);
+                    if (rc != PQ_OK) return rc;
+                }
+            }
+            if (ctx->lx_segs[0] && ctx->lx_segs[1]) A.sa_seed = 2;
+        }
+        for (int d = 0; d < 2; ++d) A.fm[d].lx = lx_view(ctx, d);
     }
+    ctx->lx_queries = A.sa_seed == 2 ? 4 * uint64_t(nr) : 0;
 
     unsigned long long* ctr = ctx->ctrs.as<unsigned long long>();   // [0] e_count [1] probes [2] ovf(u32)
     pq::SearchOut O;
@@ -441,6 +482,7 @@ int pq_overlaps(pq_ctx* ctx) {
     O.ovf_list = ctx->ovf_list.as<idx_t>();
     O.ovf_count = reinterpret_cast<unsigned int*>(ctr + 2);
     O.probes = ctr + 1;
+    A.lx_misses = ctr + 3;
 
     CK(cudaMemsetAsync(ctr, 0, 64, ctx->st));
     CK(cudaEventRecord(ctx->ev0, ctx->st));
@@ -456,9 +498,10 @@ int pq_overlaps(pq_ctx* ctx) {
         CK(pq::search_fast(A, O, blocks, ctx->warp_scratch.p, wsb, ebcap, ctx->st));
     }
     CK(cudaEventRecord(ctx->evk1, ctx->st));
-    unsigned long long hc[3];
+    unsigned long long hc[4];
     CK(cudaMemcpyAsync(hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
+    ctx->lx_misses = hc[3];
     unsigned ovf = unsigned(hc[2] & 0xffffffffu);
     ctx->wide_reads = ovf;
     if (ovf) {
@@ -600,6 +643,177 @@ int pq_get_kernel_stats(pq_ctx* ctx, float* search_kernel_ms, unsigned long long
     if (search_kernel_ms) *search_kernel_ms = ctx->ms_fast;
     if (launches) *launches = pq::launch_count();
     return PQ_OK;
+}
+
+// ---------------------------------------------------------------------------- learned index
+
+int pq_learned_build(pq_ctx* ctx, int dir, int steps) {
+    if (!ctx || (dir != 0 && dir != 1) || steps < 0) return PQ_ERR_ARG;
+    if (!ctx->fm_ok[dir]) return fail(ctx, PQ_ERR_STATE, "pq_learned_build needs pq_build_fm first");
+    cudaSetDevice(ctx->device);
+    const size_t n = n_rows(ctx);
+    ctx->lx_ok[dir] = false;
+    pq_learned_info info = {};
+    info.hidden = pq::kLxHidden;
+    info.steps = steps;
+    if (n == 0) {
+        ctx->lx_segs[dir] = 0;
+        ctx->lx_info[dir] = info;
+        ctx->lx_ok[dir] = true;
+        return PQ_OK;
+    }
+    CK(ctx->lx_tmp.ensure(pq::lx_tmp_bytes(n)));
+    const pq::LxTmp T = pq::lx_tmp_layout(ctx->lx_tmp.p, n);
+    unsigned long long m = 0;
+    CK(cudaEventRecord(ctx->ev0, ctx->st));
+    CK(pq::lx_distinct_keys(ctx->sa[dir].as<idx_t>(), ctx->pk[dir].as<uint64_t>(), n, idx_t(ctx->L), T, &m, ctx->st));
+    CK(cudaEventRecord(ctx->ev1, ctx->st));
+    CK(cudaEventSynchronize(ctx->ev1));
+    cudaEventElapsedTime(&info.keys_ms, ctx->ev0, ctx->ev1);
+    const int S = int(std::min<unsigned long long>(pq::kLxMaxSegs, m));
+    CK(ctx->lx_bnd[dir].ensure(size_t(S) * 4 + 64));
+    CK(ctx->lx_base[dir].ensure(size_t(S + 1) * sizeof(idx_t) + 64));
+    CK(ctx->lx_par[dir].ensure(size_t(S) * pq::kLxStride * sizeof(float) + 64));
+    CK(ctx->lx_err[dir].ensure(size_t(S) * 8 + 64));
+    CK(ctx->lx_err_root[dir].ensure(size_t(S) * 8 + 64));
+    CK(ctx->lx_segof[dir].ensure(65537 * 2 + 64));
+    CK(pq::lx_root(T, m, n, S, ctx->lx_bnd[dir].as<uint32_t>(), ctx->lx_base[dir].as<idx_t>(),
+                   ctx->lx_segof[dir].as<uint16_t>(), ctx->st));
+    CK(cudaEventRecord(ctx->ev0, ctx->st));
+    CK(pq::lx_train(T, ctx->lx_bnd[dir].as<uint32_t>(), ctx->lx_base[dir].as<idx_t>(), S, steps, 0.03f,
+                    0x51ed5eedu + uint32_t(dir), ctx->lx_par[dir].as<float>(), ctx->st));
+    CK(cudaEventRecord(ctx->ev1, ctx->st));
+    CK(cudaEventSynchronize(ctx->ev1));
+    cudaEventElapsedTime(&info.train_ms, ctx->ev0, ctx->ev1);
+    ctx->lx_segs[dir] = S;
+    ctx->lx_ok[dir] = true;
+    const LearnedView v = lx_view(ctx, dir);
+    CK(cudaEventRecord(ctx->ev0, ctx->st));
+    CK(pq::lx_errors(T, v, ctx->lx_err[dir].as<int32_t>(), ctx->lx_err_root[dir].as<int32_t>(), ctx->st));
+    CK(cudaEventRecord(ctx->ev1, ctx->st));
+    CK(cudaEventSynchronize(ctx->ev1));
+    cudaEventElapsedTime(&info.eval_ms, ctx->ev0, ctx->ev1);
+    // window statistics, weighted by the keys of each segment
+    std::vector<int32_t> e(2 * S), er(2 * S);
+    std::vector<unsigned long long> dsi(S + 1);
+    CK(cudaMemcpy(e.data(), ctx->lx_err[dir].p, 8 * size_t(S), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(er.data(), ctx->lx_err_root[dir].p, 8 * size_t(S), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(dsi.data(), T.dsi, 8 * size_t(S + 1), cudaMemcpyDeviceToHost));
+    double sw = 0, swr = 0;
+    for (int s = 0; s < S; ++s) {
+        const double keys = double(dsi[s + 1] - dsi[s]);
+        const int64_t w = int64_t(e[2 * s]) + e[2 * s + 1], wr = int64_t(er[2 * s]) + er[2 * s + 1];
+        sw += keys * double(w);
+        swr += keys * double(wr);
+        info.max_window = std::max(info.max_window, w);
+        info.max_window_root = std::max(info.max_window_root, wr);
+    }
+    info.num_keys = m;
+    info.segments = S;
+    info.mean_window = m ? sw / double(m) : 0.0;
+    info.mean_window_root = m ? swr / double(m) : 0.0;
+    ctx->lx_info[dir] = info;
+    ctx->lx_tmp.release();
+    ctx->graph_ok = false;
+    return PQ_OK;
+}
+
+int pq_learned_get_info(pq_ctx* ctx, int dir, pq_learned_info* info) {
+    if (!ctx || (dir != 0 && dir != 1) || !info) return PQ_ERR_ARG;
+    if (!ctx->lx_ok[dir]) return fail(ctx, PQ_ERR_STATE, "no learned index for this direction");
+    *info = ctx->lx_info[dir];
+    info->queries = ctx->lx_queries;
+    info->misses = ctx->lx_misses;
+    return PQ_OK;
+}
+
+int pq_learned_export(pq_ctx* ctx, int dir, uint32_t* bnd, pq_idx* base, float* params, int32_t* err,
+                      int32_t* err_root) {
+    if (!ctx || (dir != 0 && dir != 1)) return PQ_ERR_ARG;
+    if (!ctx->lx_ok[dir]) return fail(ctx, PQ_ERR_STATE, "no learned index for this direction");
+    const size_t S = size_t(ctx->lx_segs[dir]);
+    if (!S) return PQ_OK;
+    if (bnd) CK(cudaMemcpy(bnd, ctx->lx_bnd[dir].p, S * 4, cudaMemcpyDeviceToHost));
+    if (base) CK(cudaMemcpy(base, ctx->lx_base[dir].p, (S + 1) * sizeof(idx_t), cudaMemcpyDeviceToHost));
+    if (params) CK(cudaMemcpy(params, ctx->lx_par[dir].p, S * pq::kLxStride * 4, cudaMemcpyDeviceToHost));
+    if (err) CK(cudaMemcpy(err, ctx->lx_err[dir].p, S * 8, cudaMemcpyDeviceToHost));
+    if (err_root) CK(cudaMemcpy(err_root, ctx->lx_err_root[dir].p, S * 8, cudaMemcpyDeviceToHost));
+    return PQ_OK;
+}
+
+int pq_learned_predict(pq_ctx* ctx, int dir, const uint32_t* keys, uint64_t n, int64_t* pred, int32_t* seg) {
+    if (!ctx || (dir != 0 && dir != 1) || (n && (!keys || !pred || !seg))) return PQ_ERR_ARG;
+    if (!ctx->lx_ok[dir] || !ctx->lx_segs[dir]) return fail(ctx, PQ_ERR_STATE, "no learned index for this direction");
+    if (!n) return PQ_OK;
+    cudaSetDevice(ctx->device);
+    DevBuf dk, dp, ds;
+    CK(dk.ensure(n * 4));
+    CK(dp.ensure(n * 8));
+    CK(ds.ensure(n * 4));
+    CK(cudaMemcpyAsync(dk.p, keys, n * 4, cudaMemcpyHostToDevice, ctx->st));
+    CK(pq::lx_predict_keys(lx_view(ctx, dir), dk.as<uint32_t>(), n, dp.as<long long>(), ds.as<int32_t>(), ctx->st));
+    CK(cudaMemcpyAsync(pred, dp.p, n * 8, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(seg, ds.p, n * 4, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    dk.release();
+    dp.release();
+    ds.release();
+    return PQ_OK;
+}
+
+int pq_learned_keys(pq_ctx* ctx, int dir, uint32_t* keys, pq_idx* first_row, uint64_t cap, uint64_t* num_keys) {
+    if (!ctx || (dir != 0 && dir != 1) || !num_keys) return PQ_ERR_ARG;
+    if (!ctx->fm_ok[dir]) return fail(ctx, PQ_ERR_STATE, "pq_learned_keys needs pq_build_fm first");
+    cudaSetDevice(ctx->device);
+    const size_t n = n_rows(ctx);
+    *num_keys = 0;
+    if (!n) return PQ_OK;
+    CK(ctx->lx_tmp.ensure(pq::lx_tmp_bytes(n)));
+    const pq::LxTmp T = pq::lx_tmp_layout(ctx->lx_tmp.p, n);
+    unsigned long long m = 0;
+    CK(pq::lx_distinct_keys(ctx->sa[dir].as<idx_t>(), ctx->pk[dir].as<uint64_t>(), n, idx_t(ctx->L), T, &m, ctx->st));
+    const size_t c = size_t(std::min<unsigned long long>(m, cap));
+    if (keys && c) CK(cudaMemcpy(keys, T.kd, c * 4, cudaMemcpyDeviceToHost));
+    if (first_row && c) CK(cudaMemcpy(first_row, T.fd, c * sizeof(idx_t), cudaMemcpyDeviceToHost));
+    *num_keys = m;
+    ctx->lx_tmp.release();
+    return PQ_OK;
+}
+
+int pq_mlp_forward(const float* params, const float* x, int n, float* y) {
+    if (!params || n < 0 || (n && (!x || !y))) return PQ_ERR_ARG;
+    DevBuf dp, dx, dy;
+    if (dp.ensure(pq::kLxStride * 4) || dx.ensure(size_t(n) * 4 + 4) || dy.ensure(size_t(n) * 4 + 4)) return PQ_ERR_NOMEM;
+    int rc = PQ_OK;
+    if (cudaMemcpy(dp.p, params, pq::kLxStride * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+        (n && cudaMemcpy(dx.p, x, size_t(n) * 4, cudaMemcpyHostToDevice) != cudaSuccess) ||
+        pq::mlp_forward(dp.as<float>(), dx.as<float>(), n, dy.as<float>(), 0) != cudaSuccess ||
+        (n && cudaMemcpy(y, dy.p, size_t(n) * 4, cudaMemcpyDeviceToHost) != cudaSuccess))
+        rc = PQ_ERR_CUDA;
+    dp.release();
+    dx.release();
+    dy.release();
+    return rc;
+}
+
+int pq_mlp_backward(const float* params, const float* x, const float* dy, int n, float* grad) {
+    if (!params || !grad || n < 0 || (n && (!x || !dy))) return PQ_ERR_ARG;
+    DevBuf dp, dx, dg, dd;
+    if (dp.ensure(pq::kLxStride * 4) || dx.ensure(size_t(n) * 4 + 4) || dd.ensure(size_t(n) * 4 + 4) ||
+        dg.ensure(pq::kLxParams * 4))
+        return PQ_ERR_NOMEM;
+    int rc = PQ_OK;
+    if (cudaMemcpy(dp.p, params, pq::kLxStride * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+        (n && cudaMemcpy(dx.p, x, size_t(n) * 4, cudaMemcpyHostToDevice) != cudaSuccess) ||
+        (n && cudaMemcpy(dd.p, dy, size_t(n) * 4, cudaMemcpyHostToDevice) != cudaSuccess) ||
+        pq::mlp_backward(dp.as<float>(), dx.as<float>(), dd.as<float>(), n, dg.as<float>(), 0) != cudaSuccess ||
+        cudaMemcpy(grad, dg.p, pq::kLxParams * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+        rc = PQ_ERR_CUDA;
+    dp.release();
+    dx.release();
+    dd.release();
+    dg.release();
+    return rc;
 }
 
 }  // extern "C"

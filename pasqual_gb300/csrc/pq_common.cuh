@@ -42,6 +42,18 @@ constexpr int kBlockShift = 6;                    // 64 rows per block
 constexpr int kSuperShift = 16;                   // 65536 rows per superblock
 constexpr int kBlocksPerSuper = 1 << (kSuperShift - kBlockShift);
 
+// Device view of one direction's learned index (pq_learned.cuh): segment boundary keys, the
+// root's row at each boundary, per-segment MLP parameters, per-segment window bounds
+// (e_lo, e_hi) and the segment of each 16-bit key prefix.
+struct LearnedView {
+    const uint32_t* bnd;      // [S] first key of each segment (bnd[0] = 0); segment S-1 ends at 2^32
+    const idx_t* base;        // [S + 1] rows with a smaller key; base[S] = number of rows
+    const float* par;         // [S * 196] w1[64] b1[64] w2[64] b2, padded
+    const int32_t* err;       // [2 S] e_lo, e_hi
+    const uint16_t* segof;    // [65537] segment holding key h << 16 (segof[65536] = S - 1)
+    int segs;                 // S (0 = no model)
+};
+
 // Device view of one FM-index direction.
 struct FmView {
     const OccBlock* blk;      // n/64 + 1 blocks
@@ -52,6 +64,7 @@ struct FmView {
     const idx_t* sa;          // suffix array (for seeds found by binary search), or nullptr
     const uint64_t* pk;       // the text, 32 bases per word, first base in the top bits
     const idx_t* isa;         // inverse suffix array (row of each text position), or nullptr
+    LearnedView lx;           // learned index of 16-base keys (lx.segs = 0 when absent)
     idx_t Cf[5];              // Cf[0] = C[0]; Cf[c] = C[c] + fix[c]  (LF-mapping base)
 };
 

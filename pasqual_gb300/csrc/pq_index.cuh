@@ -42,7 +42,9 @@ struct SearchArgs {
     int L;
     int t;
     int seed_k;                 // k-mer seed depth (0 = start at depth 1 from C[])
-    int sa_seed;                // 1: candidates by depth-t interval scan (needs fm[].sa/pk/isa)
+    int sa_seed;                // 1: candidates by depth-t interval scan (needs fm[].sa/pk/isa),
+                                // 2: the same with learned windows (needs fm[].lx)
+    unsigned long long* lx_misses;  // learned windows that missed (those chains walk)
 };
 
 // Global scratch of the fast kernel, per warp of 32 reads: level-0 candidates (4 kinds x (L - t)

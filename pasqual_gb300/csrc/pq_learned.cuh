@@ -29,16 +29,6 @@ constexpr int kLxParams = 3 * kLxHidden + 1;     // w1[64] b1[64] w2[64] b2
 constexpr int kLxStride = 196;                    // floats per segment (49 float4)
 constexpr int kLxKeyBases = 16;
 
-// Device view of one direction's model (part of FmView).
-struct LearnedView {
-    const uint32_t* bnd;      // [S] first key of each segment (bnd[0] = 0); segment S-1 ends at 2^32
-    const idx_t* base;        // [S + 1] F(bnd[s]); base[S] = number of rows
-    const float* par;         // [S * kLxStride]
-    const int32_t* err;       // [2 S] e_lo, e_hi
-    const uint16_t* segof;    // [65537] segment holding key h << 16 (segof[65536] = S - 1)
-    int segs;                 // S (0 = no model)
-};
-
 __device__ __forceinline__ float lx_mlp(const float* __restrict__ p, float x) {
     const float4* q = reinterpret_cast<const float4*>(p);
     float y = __ldg(p + 3 * kLxHidden);
@@ -79,7 +69,8 @@ __device__ __forceinline__ long long lx_predict(const LearnedView& v, int s, uin
     const float R = float(b1 - b0);
     float o = r * R;
     o = fminf(fmaxf(o, 0.f), R);
-    return (long long)b0 + __float2ll_rd(o);
+    const long long p = (long long)b0 + __float2ll_rd(o);
+    return p < (long long)b1 ? p : (long long)b1;
 }
 
 }  // namespace pq

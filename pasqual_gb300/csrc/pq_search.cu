@@ -15,6 +15,7 @@
 // wide kernel, whose per-slot scratch has the reference's own bounds ((2L)^2 candidates,
 // 65535 edges per side), so every read completes with the reference's result.
 #include "pq_index.cuh"
+#include "pq_learned.cuh"
 
 #include <algorithm>
 
@@ -394,7 +395,21 @@ __device__ __forceinline__ bool scan_pair(const SearchArgs& A, const FmView* fm,
     const FmView* f0 = fm + walked_index(k0);
     const FmView* f1 = fm + walked_index(k1);
     idx_t lo[2], hi[2], first[2], end[2];
-    {
+    if (A.sa_seed == 2) {
+        // learned window of P_t's first 16 bases: one inference per chain
+        #pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const LearnedView& v = (q ? f1 : f0)->lx;
+            const uint32_t K = uint32_t((q ? P1 : P0)[0] >> 32);
+            const int sg = lx_segment(v, K);
+            const long long pr = lx_predict(v, sg, K);
+            const long long b0 = (long long)__ldg(v.base + sg), b1 = (long long)__ldg(v.base + sg + 1);
+            const long long a = pr - (long long)__ldg(v.err + 2 * sg), b = pr + (long long)__ldg(v.err + 2 * sg + 1);
+            lo[q] = idx_t(a > b0 ? a : b0);
+            hi[q] = idx_t(b < b1 ? b : b1);
+            if (hi[q] < lo[q]) hi[q] = lo[q];
+        }
+    } else {
         const uint32_t c0 = uint32_t(P0[0] >> (64 - 2 * k)), c1 = uint32_t(P1[0] >> (64 - 2 * k));
         lo[0] = __ldg(f0->kstart + c0);
         hi[0] = __ldg(f0->kend + c0) + 1;
@@ -405,6 +420,31 @@ __device__ __forceinline__ bool scan_pair(const SearchArgs& A, const FmView* fm,
         if (hi[1] < lo[1]) hi[1] = lo[1];
     }
     sa_bounds2(f0, f1, L, P0, P1, t, lo, hi, first, end, probes);
+    if (A.sa_seed == 2) {
+        // The window holds the answer for every key present in the index; for any other key it
+        // is checked: the rows just outside the window must not start with P_t.
+        const idx_t n_rows = A.num_reads * idx_t(L);
+        bool ok = true;
+        #pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const FmView& fa = *(q ? f1 : f0);
+            const uint64_t (&P)[kScanWords] = q ? P1 : P0;
+            if (first[q] == lo[q] && lo[q] > 0) {
+                const idx_t p = __ldg(fa.sa + lo[q] - 1);
+                ok = ok && cmp_row(fa.pk, p, L - int(p % idx_t(L)), P, t) < 0;
+                probes += 2;
+            }
+            if (end[q] == hi[q] && hi[q] < n_rows) {
+                const idx_t p = __ldg(fa.sa + hi[q]);
+                ok = ok && cmp_row(fa.pk, p, L - int(p % idx_t(L)), P, t) > 0;
+                probes += 2;
+            }
+        }
+        if (!ok) {
+            atomicAdd(A.lx_misses, 1ull);
+            return false;           // plain backward search
+        }
+    }
     if (end[0] - first[0] > idx_t(kScanMax) || end[1] - first[1] > idx_t(kScanMax)) return false;
     #pragma unroll
     for (int q = 0; q < 2; ++q) {
