@@ -207,6 +207,29 @@ PQ_API int pq_learned_keys (pq_ctx * ctx, int dir, uint32_t * keys, pq_idx * fir
 PQ_API int pq_mlp_forward (const float *params, const float *x, int n, float *y);
 PQ_API int pq_mlp_backward (const float *params, const float *x, const float *dy, int n, float *grad);
 
+/* ---- Queued search over several read sets (no counterpart in the reference) ----------------
+ *
+ * Each context holds one read set with its own read length L, min overlap t and index pair (the
+ * reference handles one fixed-length read set per run; here several such runs share one launch).
+ * pq_overlaps_batched searches all of them with ONE persistent kernel: warps take work items
+ * (a batch and a group of 32 reads) from a device queue until it is empty, loading each batch's
+ * index pair, L and t when they change; every context then holds the same result pq_overlaps
+ * would give it.  With PQ_BATCH_GRAPH the queue reset and the kernel are captured once into a
+ * CUDA graph (re-captured when a buffer moved or the launch shape changed) and replayed.  Work is
+ * ordered on ctxs[0]'s stream; all contexts must be on one device, each appearing once. */
+#define PQ_BATCH_GRAPH 1
+PQ_API int pq_overlaps_batched (pq_ctx ** ctxs, int count, int flags);
+/* Launch plan of queued searches led by `lead`: CTAs (4 warps each) per SM (0 = as many as fit),
+ * groups of 32 reads per work item, and edge slots per read in the fast kernel's scratch (reads
+ * with more edges go to the wide kernel). */
+PQ_API int pq_set_batch_plan (pq_ctx * lead, int ctas_per_sm, int groups_per_item, int edge_slots);
+PQ_API int pq_get_batch_stats (pq_ctx * lead, float *kernel_ms, int *ctas_per_sm, int *groups_per_item,
+                               int *edge_slots, int *graph_used);
+/* Time every plan (CTAs per SM from 2 to the occupancy limit, 1/2/4 groups per item, 32/64 edge
+ * slots) on this batch set with pq_overlaps_batched(flags), keep the fastest kernel time as the
+ * lead's plan; *best_ms = its time.  The contexts hold the last run's (identical) results. */
+PQ_API int pq_autotune_batched (pq_ctx ** ctxs, int count, int flags, float *best_ms);
+
 /* Duration (ms, CUDA events on the context stream) of the fast search kernel in the last
  * pq_overlaps, and the number of kernels this library has launched since it was loaded. */
 PQ_API int pq_get_kernel_stats (pq_ctx * ctx, float *search_kernel_ms,

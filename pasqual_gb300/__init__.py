@@ -22,7 +22,7 @@ import numpy as np
 from . import build as _build
 
 __all__ = ["Pasqual", "Graph", "PQError", "load_library", "library_path", "EXPORTS", "mlp_forward",
-           "mlp_backward", "LearnedInfo"]
+           "mlp_backward", "LearnedInfo", "overlaps_batched", "autotune_batched"]
 
 PQ_ERRORS = {1: "PQ_ERR_ARG", 2: "PQ_ERR_CUDA", 3: "PQ_ERR_NOMEM", 4: "PQ_ERR_TOO_MANY_EDGES",
              5: "PQ_ERR_STATE", 6: "PQ_ERR_CAPACITY", 7: "PQ_ERR_INTERNAL"}
@@ -33,7 +33,8 @@ EXPORTS = ["pq_idx_bytes", "pq_create", "pq_destroy", "pq_last_error", "pq_set_r
            "pq_get_index_ref", "pq_get_seeds", "pq_set_seed_k", "pq_set_seed_mode", "pq_overlaps",
            "pq_get_graph_sizes", "pq_get_graph", "pq_get_stage_ms", "pq_get_kernel_stats",
            "pq_suffix_sort_static", "pq_learned_build", "pq_learned_get_info", "pq_learned_export",
-           "pq_learned_predict", "pq_learned_keys", "pq_mlp_forward", "pq_mlp_backward"]
+           "pq_learned_predict", "pq_learned_keys", "pq_mlp_forward", "pq_mlp_backward",
+           "pq_overlaps_batched", "pq_set_batch_plan", "pq_get_batch_stats", "pq_autotune_batched"]
 
 
 # The reference's own entry points served by the same library (include/pasqual_gb300_dropin.h).
@@ -92,6 +93,10 @@ def load_library(width: int = 32) -> ct.CDLL:
         "pq_learned_keys": (c_int, [vp, c_int, vp, vp, ct.c_uint64, vp]),
         "pq_mlp_forward": (c_int, [vp, vp, c_int, vp]),
         "pq_mlp_backward": (c_int, [vp, vp, vp, c_int, vp]),
+        "pq_overlaps_batched": (c_int, [vp, c_int, c_int]),
+        "pq_set_batch_plan": (c_int, [vp, c_int, c_int, c_int]),
+        "pq_get_batch_stats": (c_int, [vp, vp, vp, vp, vp, vp]),
+        "pq_autotune_batched": (c_int, [vp, c_int, c_int, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -142,6 +147,34 @@ def mlp_backward(params: np.ndarray, x: np.ndarray, dy: np.ndarray, width: int =
     if rc != 0:
         raise PQError(rc, "pq_mlp_backward")
     return g
+
+
+BATCH_GRAPH = 1
+
+
+def _handles(ctxs):
+    if not ctxs:
+        raise ValueError("empty batch")
+    w = ctxs[0].width
+    if any(c.width != w for c in ctxs):
+        raise ValueError("all contexts of a batch must have the same index width")
+    arr = (ct.c_void_p * len(ctxs))(*[c.h for c in ctxs])
+    return ctxs[0], arr
+
+
+def overlaps_batched(ctxs, graph: bool = False) -> None:
+    """One persistent search over the read sets of several contexts (each with its own L and t)."""
+    lead, arr = _handles(ctxs)
+    lead._ck(lead.lib.pq_overlaps_batched(arr, len(ctxs), BATCH_GRAPH if graph else 0), "pq_overlaps_batched")
+
+
+def autotune_batched(ctxs, graph: bool = False) -> float:
+    """Time every launch plan on this batch set, keep the fastest; returns its kernel ms."""
+    lead, arr = _handles(ctxs)
+    ms = ct.c_float()
+    lead._ck(lead.lib.pq_autotune_batched(arr, len(ctxs), BATCH_GRAPH if graph else 0, ct.byref(ms)),
+             "pq_autotune_batched")
+    return ms.value
 
 
 @dataclass
@@ -335,6 +368,16 @@ class Pasqual:
         self._ck(self.lib.pq_learned_keys(self.h, direction, _p(keys), _p(first), n, ct.byref(m)),
                  "pq_learned_keys")
         return keys[:m.value], first[:m.value]
+
+    def set_batch_plan(self, ctas_per_sm: int = 0, groups_per_item: int = 1, edge_slots: int = 64) -> None:
+        self._ck(self.lib.pq_set_batch_plan(self.h, ctas_per_sm, groups_per_item, edge_slots), "pq_set_batch_plan")
+
+    def batch_stats(self) -> dict:
+        ms, c, g, e, gr = ct.c_float(), ct.c_int(), ct.c_int(), ct.c_int(), ct.c_int()
+        self._ck(self.lib.pq_get_batch_stats(self.h, ct.byref(ms), ct.byref(c), ct.byref(g), ct.byref(e),
+                                             ct.byref(gr)), "pq_get_batch_stats")
+        return {"kernel_ms": ms.value, "ctas_per_sm": c.value, "groups_per_item": g.value,
+                "edge_slots": e.value, "graph_used": gr.value}
 
     def stage_ms(self):
         a, b, c = ct.c_float(), ct.c_float(), ct.c_float()

@@ -87,6 +87,17 @@ struct pq_ctx {
     pq_learned_info lx_info[2] = {};
     uint64_t lx_queries = 0, lx_misses = 0;
 
+    // queued search over several contexts (this context leading): plan, queue buffers, graph
+    int q_ctas_per_sm = 0;          // 0: as many as fit
+    int q_groups_per_item = 1;
+    int q_ebcap = 64;
+    DevBuf q_batches, q_items, q_next;
+    cudaGraph_t q_graph = nullptr;
+    cudaGraphExec_t q_exec = nullptr;
+    std::vector<uintptr_t> q_key;
+    float q_kernel_ms = 0;
+    int q_graph_used = 0;
+
     // overlap-search output
     DevBuf nB, nF, oB, oF, status, esrc, e_dest, e_trans, e_len, e_type, ctrs, ovf_list;
     DevBuf off, g_dest, g_len, g_type, g_trans, asm_tmp, wide, warp_scratch;
@@ -188,6 +199,11 @@ void pq_destroy(pq_ctx* ctx) {
     if (ctx->evk0) cudaEventDestroy(ctx->evk0);
     if (ctx->evk1) cudaEventDestroy(ctx->evk1);
     if (ctx->own_stream) cudaStreamDestroy(ctx->st);
+    if (ctx->q_exec) cudaGraphExecDestroy(ctx->q_exec);
+    if (ctx->q_graph) cudaGraphDestroy(ctx->q_graph);
+    ctx->q_batches.release();
+    ctx->q_items.release();
+    ctx->q_next.release();
     delete ctx;
 }
 
@@ -403,8 +419,8 @@ int pq_get_seeds(pq_ctx* ctx, int dir, pq_idx* start, pq_idx* size, uint16_t* de
     return PQ_OK;
 }
 
-int pq_overlaps(pq_ctx* ctx) {
-    if (!ctx) return PQ_ERR_ARG;
+// Output buffers, search arguments and zeroed counters of one context's overlap search.
+static int search_prepare(pq_ctx* ctx, pq::SearchArgs& A, pq::SearchOut& O) {
     if (!ctx->fm_ok[0] || !ctx->fm_ok[1]) return fail(ctx, PQ_ERR_STATE, "build both FM-indexes first");
     if (ctx->fm_k[0] != ctx->fm_k[1]) return fail(ctx, PQ_ERR_STATE, "seed tables of different depth");
     cudaSetDevice(ctx->device);
@@ -424,7 +440,6 @@ int pq_overlaps(pq_ctx* ctx) {
     CK(ctx->e_len.ensure(ecap * 2));
     CK(ctx->e_type.ensure(ecap));
 
-    pq::SearchArgs A;
     for (int d = 0; d < 2; ++d) {
         FmView& f = A.fm[d];
         f.blk = ctx->blk[d].as<OccBlock>();
@@ -466,7 +481,6 @@ int pq_overlaps(pq_ctx* ctx) {
     ctx->lx_queries = A.sa_seed == 2 ? 4 * uint64_t(nr) : 0;
 
     unsigned long long* ctr = ctx->ctrs.as<unsigned long long>();   // [0] e_count [1] probes [2] ovf(u32)
-    pq::SearchOut O;
     O.num_B = ctx->nB.as<uint16_t>();
     O.num_F = ctx->nF.as<uint16_t>();
     O.olp_B = ctx->oB.as<int32_t>();
@@ -485,19 +499,14 @@ int pq_overlaps(pq_ctx* ctx) {
     A.lx_misses = ctr + 3;
 
     CK(cudaMemsetAsync(ctr, 0, 64, ctx->st));
-    CK(cudaEventRecord(ctx->ev0, ctx->st));
-    int dev_sms = 152;
-    cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device);
-    CK(cudaEventRecord(ctx->evk0, ctx->st));
-    if (nr) {
-        // 4 warps per block, each warp 32 reads per batch; enough blocks to fill every SM
-        const int ebcap = 64;
-        int blocks = int(std::min<size_t>((nr + 127) / 128, size_t(pq::search_fast_blocks(ctx->L, dev_sms))));
-        const size_t wsb = pq::warp_scratch_bytes(ctx->L, ctx->t, size_t(blocks) * 4, ebcap);
-        CK(ctx->warp_scratch.ensure(wsb));
-        CK(pq::search_fast(A, O, blocks, ctx->warp_scratch.p, wsb, ebcap, ctx->st));
-    }
-    CK(cudaEventRecord(ctx->evk1, ctx->st));
+    return PQ_OK;
+}
+
+// After the fast kernel: the wide tier for the reads it handed over, then the CSR in read order.
+static int search_finish(pq_ctx* ctx, pq::SearchArgs& A, pq::SearchOut& O) {
+    const size_t nr = ctx->num_reads;
+    const size_t nrp = nr + 1;
+    unsigned long long* ctr = ctx->ctrs.as<unsigned long long>();
     unsigned long long hc[4];
     CK(cudaMemcpyAsync(hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
@@ -596,6 +605,29 @@ int pq_overlaps(pq_ctx* ctx) {
     ctx->probes = hc[1];
     ctx->graph_ok = true;
     return PQ_OK;
+}
+
+int pq_overlaps(pq_ctx* ctx) {
+    if (!ctx) return PQ_ERR_ARG;
+    pq::SearchArgs A;
+    pq::SearchOut O;
+    int rc = search_prepare(ctx, A, O);
+    if (rc != PQ_OK) return rc;
+    const size_t nr = ctx->num_reads;
+    CK(cudaEventRecord(ctx->ev0, ctx->st));
+    int dev_sms = 152;
+    cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    CK(cudaEventRecord(ctx->evk0, ctx->st));
+    if (nr) {
+        // 4 warps per block, each warp 32 reads per batch; enough blocks to fill every SM
+        const int ebcap = 64;
+        int blocks = int(std::min<size_t>((nr + 127) / 128, size_t(pq::search_fast_blocks(ctx->L, dev_sms))));
+        const size_t wsb = pq::warp_scratch_bytes(ctx->L, ctx->t, size_t(blocks) * 4, ebcap);
+        CK(ctx->warp_scratch.ensure(wsb));
+        CK(pq::search_fast(A, O, blocks, ctx->warp_scratch.p, wsb, ebcap, ctx->st));
+    }
+    CK(cudaEventRecord(ctx->evk1, ctx->st));
+    return search_finish(ctx, A, O);
 }
 
 int pq_get_graph_sizes(pq_ctx* ctx, uint64_t* num_edges, uint64_t* probes, uint64_t* wide_reads) {
@@ -814,6 +846,193 @@ int pq_mlp_backward(const float* params, const float* x, const float* dy, int n,
     dd.release();
     dg.release();
     return rc;
+}
+
+// ---------------------------------------------------------------------------- queued search
+
+static int queue_launch(pq_ctx* lead, const std::vector<uint32_t>& ib, const std::vector<uint32_t>& ig, int L_max,
+                        int M_max, int use_graph) {
+    pq_ctx* ctx = lead;
+    int dev_sms = 152;
+    cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, lead->device);
+    int per_sm = pq::search_fast_blocks(L_max, 1);
+    if (lead->q_ctas_per_sm > 0) per_sm = lead->q_ctas_per_sm;
+    const size_t nitems = ib.size();
+    const unsigned gpi = unsigned(std::max(1, lead->q_groups_per_item));
+    const int blocks = int(std::max<size_t>(1, std::min<size_t>(size_t(per_sm) * dev_sms, (nitems + 3) / 4)));
+    const size_t wsb = pq::queue_scratch_bytes(L_max, M_max, size_t(blocks) * 4, lead->q_ebcap);
+    CK(lead->warp_scratch.ensure(wsb));
+    CK(lead->q_items.ensure(nitems * 8 + 64));
+    CK(lead->q_next.ensure(64));
+    uint32_t* d_items = lead->q_items.as<uint32_t>();
+    CK(cudaMemcpyAsync(d_items, ib.data(), nitems * 4, cudaMemcpyHostToDevice, lead->st));
+    CK(cudaMemcpyAsync(d_items + nitems, ig.data(), nitems * 4, cudaMemcpyHostToDevice, lead->st));
+    pq::SearchQueue Q;
+    Q.batches = lead->q_batches.as<pq::SearchBatch>();
+    Q.item_batch = d_items;
+    Q.item_group = d_items + nitems;
+    Q.count = unsigned(nitems);
+    Q.groups_per_item = gpi;
+    Q.next = lead->q_next.as<unsigned>();
+    lead->q_graph_used = 0;
+    if (!use_graph) {
+        CK(cudaMemsetAsync(Q.next, 0, 4, lead->st));
+        CK(cudaEventRecord(lead->evk0, lead->st));
+        CK(pq::search_fast_queue(Q, L_max, M_max, blocks, lead->warp_scratch.p, wsb, lead->q_ebcap, lead->st));
+        CK(cudaEventRecord(lead->evk1, lead->st));
+    } else {
+        // one captured graph per launch shape: queue reset + persistent search kernel
+        const std::vector<uintptr_t> key = {uintptr_t(Q.batches), uintptr_t(d_items), uintptr_t(Q.next),
+                                            uintptr_t(lead->warp_scratch.p), nitems, uintptr_t(L_max),
+                                            uintptr_t(M_max), uintptr_t(blocks), gpi, uintptr_t(lead->q_ebcap)};
+        if (!lead->q_exec || lead->q_key != key) {
+            if (lead->q_exec) cudaGraphExecDestroy(lead->q_exec);
+            if (lead->q_graph) cudaGraphDestroy(lead->q_graph);
+            lead->q_exec = nullptr;
+            lead->q_graph = nullptr;
+            CK(cudaStreamSynchronize(lead->st));
+            CK(cudaStreamBeginCapture(lead->st, cudaStreamCaptureModeThreadLocal));
+            cudaError_t e1 = cudaMemsetAsync(Q.next, 0, 4, lead->st);
+            cudaError_t e2 = pq::search_fast_queue(Q, L_max, M_max, blocks, lead->warp_scratch.p, wsb, lead->q_ebcap,
+                                                   lead->st);
+            cudaGraph_t g = nullptr;
+            cudaError_t e3 = cudaStreamEndCapture(lead->st, &g);
+            CK(e1);
+            CK(e2);
+            CK(e3);
+            lead->q_graph = g;
+            CK(cudaGraphInstantiate(&lead->q_exec, g, 0));
+            lead->q_key = key;
+        }
+        CK(cudaEventRecord(lead->evk0, lead->st));
+        CK(cudaGraphLaunch(lead->q_exec, lead->st));
+        pq::note_launch();
+        CK(cudaEventRecord(lead->evk1, lead->st));
+        lead->q_graph_used = 1;
+    }
+    CK(cudaEventSynchronize(lead->evk1));
+    cudaEventElapsedTime(&lead->q_kernel_ms, lead->evk0, lead->evk1);
+    return PQ_OK;
+}
+
+int pq_overlaps_batched(pq_ctx** ctxs, int count, int flags) {
+    if (!ctxs || count <= 0) return PQ_ERR_ARG;
+    pq_ctx* lead = ctxs[0];
+    if (!lead) return PQ_ERR_ARG;
+    for (int b = 0; b < count; ++b) {
+        if (!ctxs[b]) return fail(lead, PQ_ERR_ARG, "null context in batch");
+        if (ctxs[b]->device != lead->device) return fail(lead, PQ_ERR_ARG, "batched contexts must share a device");
+        for (int c = 0; c < b; ++c)
+            if (ctxs[c] == ctxs[b]) return fail(lead, PQ_ERR_ARG, "a context appears twice in the batch");
+    }
+    cudaSetDevice(lead->device);
+    std::vector<pq::SearchBatch> hb(count);
+    int L_max = 1, M_max = 1;
+    for (int b = 0; b < count; ++b) {
+        const int rc = search_prepare(ctxs[b], hb[b].a, hb[b].o);
+        if (rc != PQ_OK) {
+            if (b) fail(lead, rc, std::string("batch ") + std::to_string(b) + ": " + ctxs[b]->err);
+            return rc;
+        }
+        if (ctxs[b]->st != lead->st && cudaStreamSynchronize(ctxs[b]->st) != cudaSuccess)
+            return fail(lead, PQ_ERR_CUDA, "batch stream synchronisation failed");
+        L_max = std::max(L_max, ctxs[b]->L);
+        M_max = std::max(M_max, ctxs[b]->L - ctxs[b]->t);
+    }
+    // items: longest reads first (they take longest), groups of 32 reads in order within a batch
+    std::vector<int> order(count);
+    for (int b = 0; b < count; ++b) order[b] = b;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return ctxs[x]->L > ctxs[y]->L; });
+    const unsigned gpi = unsigned(std::max(1, lead->q_groups_per_item));
+    std::vector<uint32_t> ib, ig;
+    for (int b : order) {
+        const size_t groups = (size_t(ctxs[b]->num_reads) + 31) / 32;
+        for (size_t g = 0; g < groups; g += gpi) {
+            ib.push_back(uint32_t(b));
+            ig.push_back(uint32_t(g));
+        }
+    }
+    pq_ctx* ctx = lead;
+    CK(lead->q_batches.ensure(sizeof(pq::SearchBatch) * size_t(count)));
+    CK(cudaMemcpyAsync(lead->q_batches.p, hb.data(), sizeof(pq::SearchBatch) * size_t(count), cudaMemcpyHostToDevice,
+                       lead->st));
+    for (int b = 0; b < count; ++b) CK(cudaEventRecord(ctxs[b]->ev0, lead->st));
+    if (!ib.empty()) {
+        const int rc = queue_launch(lead, ib, ig, L_max, M_max, (flags & PQ_BATCH_GRAPH) ? 1 : 0);
+        if (rc != PQ_OK) return rc;
+    } else {
+        lead->q_kernel_ms = 0;
+    }
+    CK(cudaStreamSynchronize(lead->st));
+    for (int b = 0; b < count; ++b) {
+        const int rc = search_finish(ctxs[b], hb[b].a, hb[b].o);
+        if (rc != PQ_OK) {
+            if (b) fail(lead, rc, std::string("batch ") + std::to_string(b) + ": " + ctxs[b]->err);
+            return rc;
+        }
+        ctxs[b]->ms_fast = lead->q_kernel_ms;
+    }
+    return PQ_OK;
+}
+
+int pq_set_batch_plan(pq_ctx* lead, int ctas_per_sm, int groups_per_item, int edge_slots) {
+    if (!lead || ctas_per_sm < 0 || ctas_per_sm > 32 || groups_per_item < 1 || groups_per_item > 64 ||
+        edge_slots < 8 || edge_slots > 4096)
+        return PQ_ERR_ARG;
+    lead->q_ctas_per_sm = ctas_per_sm;
+    lead->q_groups_per_item = groups_per_item;
+    lead->q_ebcap = edge_slots;
+    return PQ_OK;
+}
+
+int pq_get_batch_stats(pq_ctx* lead, float* kernel_ms, int* ctas_per_sm, int* groups_per_item, int* edge_slots,
+                       int* graph_used) {
+    if (!lead) return PQ_ERR_ARG;
+    if (kernel_ms) *kernel_ms = lead->q_kernel_ms;
+    if (ctas_per_sm) *ctas_per_sm = lead->q_ctas_per_sm;
+    if (groups_per_item) *groups_per_item = lead->q_groups_per_item;
+    if (edge_slots) *edge_slots = lead->q_ebcap;
+    if (graph_used) *graph_used = lead->q_graph_used;
+    return PQ_OK;
+}
+
+int pq_autotune_batched(pq_ctx** ctxs, int count, int flags, float* best_ms) {
+    if (!ctxs || count <= 0 || !ctxs[0]) return PQ_ERR_ARG;
+    pq_ctx* lead = ctxs[0];
+    int max_per_sm = 0;
+    int L_max = 1;
+    for (int b = 0; b < count; ++b)
+        if (ctxs[b]) L_max = std::max(L_max, ctxs[b]->L);
+    max_per_sm = pq::search_fast_blocks(L_max, 1);
+    float best = -1.f;
+    int bc = 0, bg = 1, be = 64;
+    const int edge_opts[2] = {32, 64};
+    for (int c = 2; c <= max_per_sm; ++c) {
+        for (int g = 1; g <= 4; g *= 2) {
+            for (int e : edge_opts) {
+                lead->q_ctas_per_sm = c;
+                lead->q_groups_per_item = g;
+                lead->q_ebcap = e;
+                float t = 0.f;
+                for (int rep = 0; rep < 2; ++rep) {     // first run warms up, second is timed
+                    const int rc = pq_overlaps_batched(ctxs, count, flags);
+                    if (rc != PQ_OK) return rc;
+                    t = lead->q_kernel_ms;
+                }
+                if (best < 0.f || t < best) {
+                    best = t;
+                    bc = c;
+                    bg = g;
+                    be = e;
+                }
+            }
+        }
+    }
+    lead->q_ctas_per_sm = bc;
+    lead->q_groups_per_item = bg;
+    lead->q_ebcap = be;
+    if (best_ms) *best_ms = best;
+    return PQ_OK;
 }
 
 }  // extern "C"

@@ -64,6 +64,24 @@ struct WarpScratch {
     idx_t *em_l, *em_u;
     TFrame* frames;
     int ebcap;
+    int mstride;                // candidate slots per kind and read (largest L - t searched)
+};
+
+// One read set of a queued search: its index pair, L and t, and its outputs.
+struct SearchBatch {
+    SearchArgs a;
+    SearchOut o;
+};
+// Work items of a queued search: item i is group item_group[i] (reads 32 g .. 32 g + 31, and
+// the following groups_per_item - 1 groups) of batch item_batch[i].  Warps take items in order
+// from *next, which is zero at launch.
+struct SearchQueue {
+    const SearchBatch* batches;
+    const uint32_t* item_batch;
+    const uint32_t* item_group;
+    unsigned count;             // 0: no queue
+    unsigned groups_per_item;
+    unsigned* next;
 };
 size_t warp_scratch_bytes(int L, int t, size_t nwarps, int ebcap);
 int search_fast_blocks(int L, int num_sms);   // resident blocks of the fast kernel on the device
@@ -71,6 +89,10 @@ int search_fast_blocks(int L, int num_sms);   // resident blocks of the fast ker
 // the frame count are listed for the wide kernel.
 cudaError_t search_fast(const SearchArgs& a, const SearchOut& o, int blocks, void* scratch, size_t scratch_bytes,
                         int ebcap, cudaStream_t st);
+// One persistent launch over a queue of batches (L_max, M_max: the largest L and L - t).
+size_t queue_scratch_bytes(int L_max, int M_max, size_t nwarps, int ebcap);
+cudaError_t search_fast_queue(const SearchQueue& q, int L_max, int M_max, int blocks, void* scratch,
+                              size_t scratch_bytes, int ebcap, cudaStream_t st);
 
 struct WideScratch {
     void* stack;                // slots * stack_cap candidates

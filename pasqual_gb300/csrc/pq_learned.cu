@@ -410,26 +410,42 @@ __global__ void k_lx_predict(LearnedView v, const uint32_t* __restrict__ keys, s
 
 // ---------------------------------------------------------------------------------- host
 
+// sizes of the working arrays, in layout order; each starts on a 256-byte boundary
+static void lx_tmp_parts(size_t n, size_t (&bytes)[5], size_t& ntiles) {
+    ntiles = (n + kTileRows - 1) / kTileRows;
+    bytes[0] = 4 * n;                          // row keys
+    bytes[1] = 8 * (ntiles + 1);               // tile offsets
+    bytes[2] = 4 * n;                          // distinct keys
+    bytes[3] = sizeof(idx_t) * (n + 1);        // group starts
+    bytes[4] = 8 * (kLxMaxSegs + 1);           // segment starts in key order
+}
+
+static size_t round256(size_t b) { return (b + 255) & ~size_t(255); }
+
 size_t lx_tmp_bytes(size_t n) {
-    const size_t ntiles = (n + kTileRows - 1) / kTileRows;
-    return 4 * n + 64 +                          // row keys
-           8 * (ntiles + 1) + 64 +               // tile offsets
-           4 * n + 64 +                          // distinct keys
-           sizeof(idx_t) * (n + 1) + 64 +        // group starts
-           8 * (kLxMaxSegs + 1) + 64;            // segment starts in key order
+    size_t b[5], nt;
+    lx_tmp_parts(n, b, nt);
+    size_t total = 0;
+    for (size_t x : b) total += round256(x);
+    return total;
 }
 
 LxTmp lx_tmp_layout(void* tmp, size_t n) {
-    const size_t ntiles = (n + kTileRows - 1) / kTileRows;
+    size_t b[5], nt;
+    lx_tmp_parts(n, b, nt);
     char* p = static_cast<char*>(tmp);
-    auto take = [&](size_t bytes) { char* q = p; p += (bytes + 63) / 64 * 64 + 64; return q; };
+    char* q[5];
+    for (int i = 0; i < 5; ++i) {
+        q[i] = p;
+        p += round256(b[i]);
+    }
     LxTmp t;
-    t.keys = reinterpret_cast<uint32_t*>(take(4 * n));
-    t.toff = reinterpret_cast<unsigned long long*>(take(8 * (ntiles + 1)));
-    t.kd = reinterpret_cast<uint32_t*>(take(4 * n));
-    t.fd = reinterpret_cast<idx_t*>(take(sizeof(idx_t) * (n + 1)));
-    t.dsi = reinterpret_cast<unsigned long long*>(take(8 * (kLxMaxSegs + 1)));
-    t.ntiles = ntiles;
+    t.keys = reinterpret_cast<uint32_t*>(q[0]);
+    t.toff = reinterpret_cast<unsigned long long*>(q[1]);
+    t.kd = reinterpret_cast<uint32_t*>(q[2]);
+    t.fd = reinterpret_cast<idx_t*>(q[3]);
+    t.dsi = reinterpret_cast<unsigned long long*>(q[4]);
+    t.ntiles = nt;
     return t;
 }
 

@@ -873,40 +873,84 @@ __device__ __forceinline__ int owner_of(const int* pref, int e) {
 // in which lanes happen to run, so every edge list is the reference's.
 // Phase C: each lane publishes its read (edge-pool reservation, copy, per-read counts).
 
-__global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A, SearchOut O, WarpScratch S) {
+// warp-cooperative copy of one batch description into shared memory
+__device__ __forceinline__ void load_batch(SearchBatch& dst, const SearchBatch* src, int lane) {
+    static_assert(sizeof(SearchBatch) % 4 == 0, "batch description is copied in 32-bit words");
+    const uint32_t* s = reinterpret_cast<const uint32_t*>(src);
+    uint32_t* d = reinterpret_cast<uint32_t*>(&dst);
+    for (int i = lane; i < int(sizeof(SearchBatch) / 4); i += 32) d[i] = s[i];
+    __syncwarp();
+}
+
+// Without a queue (Q.count == 0) the kernel searches the one read set of (A0, O0), warp w taking
+// groups of 32 reads w, w + #warps, ...  With a queue, each warp takes the next item (a batch and
+// a group of its reads) from a shared counter until the queue is empty; the batch's description
+// (index pair, L, t, outputs) is loaded into the warp's shared memory when it changes.
+__global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A0, SearchOut O0, WarpScratch S, SearchQueue Q) {
     extern __shared__ uint32_t s_reads[];
-    __shared__ FmView s_fm[2];
+    __shared__ SearchBatch s_b[kWarpsPerCta];
     __shared__ MultiSmem s_ms[kWarpsPerCta];
     __shared__ int s_n[kWarpsPerCta][32][4];
     __shared__ int32_t s_olp[kWarpsPerCta][32][2];
-    if (threadIdx.x < 2) s_fm[threadIdx.x] = A.fm[threadIdx.x];
-    __syncthreads();
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const size_t gw = size_t(blockIdx.x) * kWarpsPerCta + wid;
     const size_t nw = size_t(gridDim.x) * kWarpsPerCta;
-    const int M = A.L - A.t;
-    const int L = A.L;
+    SearchBatch& B = s_b[wid];
+    const SearchArgs& A = B.a;
+    const SearchOut& O = B.o;
+    if (Q.count == 0) {
+        if (lane == 0) {
+            B.a = A0;
+            B.o = O0;
+        }
+        __syncwarp();
+    }
     MultiSmem& sm = s_ms[wid];
-    const size_t cbase_w = gw * 32 * 4 * size_t(M);            // level-0 candidates of this warp
+    const size_t cbase_w = gw * 32 * 4 * size_t(S.mstride);    // level-0 candidates of this warp
     const size_t ebase_w = gw * 32 * size_t(S.ebcap);          // edge slots of this warp
     const size_t tbase_w = gw * 32 * size_t(kTaskCap);         // task stacks
     const size_t xbase_w = gw * 32 * 4 * size_t(kPMax);        // sparse extension slots
     const size_t mbase_w = gw * 32 * size_t(kPMax);            // emission bounds
     TFrame* const frw = S.frames + gw * 32 * kTaskFrames;
     uint32_t probes = 0;
-    for (size_t batch = gw; batch * 32 < size_t(A.num_reads); batch += nw) {
-        const size_t r = batch * 32 + lane;
+    int cur = -1;
+    for (size_t iter = 0;; ++iter) {
+        size_t group, gend;
+        if (Q.count) {
+            unsigned it = 0;
+            if (lane == 0) it = atomicAdd(Q.next, 1u);
+            it = __shfl_sync(0xffffffffu, it, 0);
+            if (it >= Q.count) break;
+            const int b = int(Q.item_batch[it]);
+            group = Q.item_group[it];
+            gend = group + Q.groups_per_item;
+            if (b != cur) {
+                if (cur >= 0) add_probes(O, probes);
+                probes = 0;
+                __syncwarp();
+                load_batch(B, Q.batches + b, lane);
+                cur = b;
+            }
+        } else {
+            group = gw + iter * nw;
+            gend = group + 1;
+            if (group * 32 >= size_t(A.num_reads)) break;
+        }
+        for (; group < gend && group * 32 < size_t(A.num_reads); ++group) {
+        const int M = A.L - A.t;
+        const int L = A.L;
+        const size_t r = group * 32 + lane;
         const bool have = r < size_t(A.num_reads);
         const idx_t self = idx_t(r);
         // ---- phase A
         if (have) {
             load_read(A, idx_t(r), s_reads + threadIdx.x, blockDim.x);
             ReadView rd{s_reads + threadIdx.x, int(blockDim.x)};
-            const size_t cb = cbase_w + size_t(lane) * 4 * M;
+            const size_t cb = cbase_w + size_t(lane) * 4 * size_t(S.mstride);
             int nb[2], nf[2];
             int32_t ob = 0, of = 0;
-            chain_pair(A, s_fm, rd, self, PQ_BF, PQ_BB, nb, ob, probes, SlotsFast{S.c_ll, S.c_uu, S.c_meta, cb, M});
-            chain_pair(A, s_fm, rd, self, PQ_FB, PQ_FF, nf, of, probes,
+            chain_pair(A, A.fm, rd, self, PQ_BF, PQ_BB, nb, ob, probes, SlotsFast{S.c_ll, S.c_uu, S.c_meta, cb, M});
+            chain_pair(A, A.fm, rd, self, PQ_FB, PQ_FF, nf, of, probes,
                        SlotsFast{S.c_ll, S.c_uu, S.c_meta, cb + 2 * size_t(M), M});
             s_n[wid][lane][0] = nb[0];
             s_n[wid][lane][1] = nb[1];
@@ -935,7 +979,7 @@ __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A, SearchOut 
                 const int j = owner_of(sm.pref, e);
                 const int i = e - sm.pref[j];
                 const int nj = sm.na[j];
-                const size_t src = cbase_w + size_t(j) * 4 * M +
+                const size_t src = cbase_w + size_t(j) * 4 * size_t(S.mstride) +
                                    (i < nj ? size_t(2 * side) * M + i : size_t(2 * side + 1) * M + (i - nj));
                 const size_t dst = tbase_w + size_t(j) * kTaskCap + i;
                 S.t_ll[dst] = S.c_ll[src];
@@ -1020,7 +1064,7 @@ __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A, SearchOut 
                     const bool ext = idx_t(cu - cl + 1) != 0;   // wrapped [0, all-ones]: kept, never extended
                     const bool ends = sm.chk[j] && meta_len(m) + sm.lvl[j] == L;
                     const int o = cand_index(meta_type(m));
-                    const FmView& f = s_fm[o];
+                    const FmView& f = A.fm[o];
                     idx_t rl[4] = {0, 0, 0, 0}, ru[4] = {0, 0, 0, 0};
                     if (ext || ends) {
                         rank_all(f, cl, rl);
@@ -1067,7 +1111,7 @@ __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A, SearchOut 
                         const uint32_t hm = S.t_meta[tb + F.pos + h];
                         const idx_t endk = uuu + 1;      // k < uuu + 1: no iteration when uuu + 1 wraps
                         const idx_t cnt = endk > lll ? endk - lll : 0;
-                        const idx_t* rix = s_fm[cand_index(meta_type(hm))].reads_index;
+                        const idx_t* rix = A.fm[cand_index(meta_type(hm))].reads_index;
                         for (idx_t k = 0; k < cnt; ++k) {
                             const idx_t rr = __ldg(rix + (lll + k));
                             if (rr == self) continue;
@@ -1182,8 +1226,9 @@ __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A, SearchOut 
             }
         }
         __syncwarp();
+        }
     }
-    add_probes(O, probes);
+    if (Q.count == 0 || cur >= 0) add_probes(O, probes);
 }
 
 int search_fast_blocks(int L, int num_sms) {
@@ -1196,8 +1241,8 @@ int search_fast_blocks(int L, int num_sms) {
     return per_sm * num_sms;
 }
 
-static size_t scratch_layout(int L, int t, size_t nwarps, int ebcap, void* base, WarpScratch* S) {
-    const size_t M = size_t(L - t);
+static size_t scratch_layout(int M_max, size_t nwarps, int ebcap, void* base, WarpScratch* S) {
+    const size_t M = size_t(M_max);
     const size_t cand = nwarps * 32 * 4 * M, edg = nwarps * 32 * size_t(ebcap);
     const size_t tsk = nwarps * 32 * size_t(kTaskCap), spr = nwarps * 32 * 4 * size_t(kPMax);
     const size_t emb = nwarps * 32 * size_t(kPMax), frm = nwarps * 32 * size_t(kTaskFrames);
@@ -1225,22 +1270,42 @@ static size_t scratch_layout(int L, int t, size_t nwarps, int ebcap, void* base,
     T.em_u = reinterpret_cast<idx_t*>(take(emb * sizeof(idx_t)));
     T.frames = reinterpret_cast<TFrame*>(take(frm * sizeof(TFrame)));
     T.ebcap = ebcap;
+    T.mstride = int(M);
     if (S) *S = T;
     return used;
 }
 
 size_t warp_scratch_bytes(int L, int t, size_t nwarps, int ebcap) {
-    return scratch_layout(L, t, nwarps, ebcap, nullptr, nullptr);
+    return scratch_layout(L - t, nwarps, ebcap, nullptr, nullptr);
 }
 
 cudaError_t search_fast(const SearchArgs& a, const SearchOut& o, int blocks, void* scratch, size_t scratch_bytes,
                         int ebcap, cudaStream_t st) {
     const size_t nwarps = size_t(blocks) * kWarpsPerCta;
     WarpScratch S;
-    if (scratch_bytes < scratch_layout(a.L, a.t, nwarps, ebcap, scratch, &S)) return cudaErrorInvalidValue;
+    if (scratch_bytes < scratch_layout(a.L - a.t, nwarps, ebcap, scratch, &S)) return cudaErrorInvalidValue;
     const int words = (a.L + 15) / 16;
     size_t smem = size_t(words) * 32 * kWarpsPerCta * sizeof(uint32_t);
-    { k_search_fast<<<blocks, 32 * kWarpsPerCta, smem, st>>>(a, o, S); note_launch(); }
+    SearchQueue Q{};
+    { k_search_fast<<<blocks, 32 * kWarpsPerCta, smem, st>>>(a, o, S, Q); note_launch(); }
+    return cudaGetLastError();
+}
+
+size_t queue_scratch_bytes(int L_max, int M_max, size_t nwarps, int ebcap) {
+    (void)L_max;
+    return scratch_layout(M_max, nwarps, ebcap, nullptr, nullptr);
+}
+
+cudaError_t search_fast_queue(const SearchQueue& q, int L_max, int M_max, int blocks, void* scratch,
+                              size_t scratch_bytes, int ebcap, cudaStream_t st) {
+    const size_t nwarps = size_t(blocks) * kWarpsPerCta;
+    WarpScratch S;
+    if (scratch_bytes < scratch_layout(M_max, nwarps, ebcap, scratch, &S)) return cudaErrorInvalidValue;
+    const int words = (L_max + 15) / 16;
+    size_t smem = size_t(words) * 32 * kWarpsPerCta * sizeof(uint32_t);
+    SearchArgs a{};
+    SearchOut o{};
+    { k_search_fast<<<blocks, 32 * kWarpsPerCta, smem, st>>>(a, o, S, q); note_launch(); }
     return cudaGetLastError();
 }
 
