@@ -49,6 +49,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-modes", action="store_true", help="skip the plain/learned comparison")
+    ap.add_argument("--batched-scale", type=float, default=0.25,
+                    help="genome scale of the queued-search workload (0 = skip)")
     return ap.parse_args()
 
 
@@ -183,6 +186,90 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def seed_modes(P, nr: int, steps: int):
+    """Plain backward search (mode 0), interval scan with the k-mer table (1) and with the learned
+    index (2) on the same index: search reads/s (whole pq_overlaps, CSR included), kernel time and
+    probes per read of each, plus the learned model's build figures."""
+    out = {}
+    ref = None
+    P.learned_build(0, 400)
+    P.learned_build(1, 400)
+    for name, mode in (("plain", 0), ("scan", 1), ("learned", 2)):
+        P.set_seed_mode(mode)
+        P.overlaps()
+        search, kern = [], []
+        for _ in range(steps):
+            P.overlaps()
+            search.append(P.stage_ms()[2])
+            kern.append(P.kernel_stats()[0])
+        g = P.graph()
+        same = ref is None or (np.array_equal(g.dest, ref[0]) and np.array_equal(g.edge_off, ref[1]))
+        if ref is None:
+            ref = (g.dest.copy(), g.edge_off.copy())
+        out[name] = {"reads_per_s": nr / (statistics.median(search) * 1e-3),
+                     "search_ms": statistics.median(search), "kernel_ms": statistics.median(kern),
+                     "probes_per_read": g.probes / max(nr, 1), "edges_identical_to_plain": bool(same)}
+    lx = [P.learned_info(d) for d in (0, 1)]
+    out["learned_model"] = {
+        "segments": lx[0]["segments"], "hidden": lx[0]["hidden"], "train_steps": lx[0]["steps"],
+        "distinct_keys": [x["num_keys"] for x in lx],
+        "build_ms": sum(x["keys_ms"] + x["train_ms"] + x["eval_ms"] for x in lx),
+        "train_ms": sum(x["train_ms"] for x in lx),
+        "mean_window_rows": [x["mean_window"] for x in lx],
+        "mean_window_rows_root_only": [x["mean_window_root"] for x in lx],
+        "window_misses": lx[0]["misses"], "window_queries": lx[0]["queries"]}
+    out["learned_vs_plain"] = out["learned"]["reads_per_s"] / out["plain"]["reads_per_s"]
+    out["scan_vs_plain"] = out["scan"]["reads_per_s"] / out["plain"]["reads_per_s"]
+    P.set_seed_mode(1)
+    return out
+
+
+def batched(scale: float, steps: int, device: int, stream):
+    """Queued search: several read sets (own L and t each) in one persistent kernel from a device
+    work queue, replayed from a CUDA graph with the autotuned plan, against one search launch per
+    read set."""
+    import torch
+    import pasqual_gb300 as pq
+    from pasqual_gb300 import synth
+    name = "100Mbp_L75-250_25x_batched"
+    sets = synth.make_batches(name, scale=scale)
+    ctxs = []
+    for rd, L, t in sets:
+        P = pq.Pasqual(32, device=device, stream=stream.cuda_stream)
+        P.set_reads(rd, t)
+        P.build_index()
+        ctxs.append(P)
+    total = sum(rd.shape[0] for rd, _, _ in sets)
+
+    def timed(fn):
+        fn()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(device)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize(device)
+        return e0.elapsed_time(e1) / steps
+
+    seq_ms = timed(lambda: [P.overlaps() for P in ctxs])
+    ref = [(P.graph().dest.copy()) for P in ctxs]
+    tune_ms = pq.autotune_batched(ctxs, graph=True)
+    q_ms = timed(lambda: pq.overlaps_batched(ctxs, graph=True))
+    same = all(np.array_equal(P.graph().dest, r) for P, r in zip(ctxs, ref))
+    st = ctxs[0].batch_stats()
+    for P in ctxs:
+        P.close()
+    return {"workload": name, "genome_scale": scale,
+            "read_sets": [{"reads": int(rd.shape[0]), "read_len": L, "t": t} for rd, L, t in sets],
+            "reads": int(total), "sequential_reads_per_s": total / (seq_ms * 1e-3),
+            "queued_graph_reads_per_s": total / (q_ms * 1e-3), "queued_vs_sequential": seq_ms / q_ms,
+            "queued_kernel_ms": st["kernel_ms"], "autotuned_kernel_ms": tune_ms,
+            "plan": {k: st[k] for k in ("ctas_per_sm", "groups_per_item", "edge_slots")},
+            "graph": bool(st["graph_used"]), "edges_identical_to_sequential": bool(same)}
+
+
 def run_ours(args):
     import torch
     import pasqual_gb300 as pq
@@ -308,6 +395,10 @@ def run_ours(args):
     }
     if ck:
         out["clocks"] = ck
+    if not args.no_modes:
+        out["seed_modes"] = seed_modes(P, nr, max(1, min(args.steps, 3)))
+    if args.batched_scale > 0:
+        out["batched"] = batched(args.batched_scale, max(1, min(args.steps, 3)), local, stream)
     if world == 1 and not args.no_cpu_baseline:
         cb = cpu_baseline(args.workload, args.cpu_scale, args.cpu_seconds)
         out["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}

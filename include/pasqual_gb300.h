@@ -110,9 +110,10 @@ PQ_API int pq_set_seed_k (pq_ctx * ctx, int k);
  * bases, reads that interval's rows once (a read r' whose suffix at offset o matches, and whose
  * first o bases continue the pattern, is a candidate at depth t + o) and takes the other index's
  * interval from the inverse suffix array.  2 is mode 1 with the learned index's window in place
- * of the k-mer table's (t >= 16).  Modes 1 and 2 apply when t <= 64, L - t <= 128 and
- * 4^t > 64 * num_reads * read_len (depth-t intervals are small); a read whose depth-t interval
- * exceeds 256 rows walks.  All modes give the reference's candidates. */
+ * of the k-mer table's (t >= 16).  Modes 1 and 2 apply when L - t <= 256 and
+ * 4^min(t, 64) > 64 * num_reads * read_len (depth-t intervals are small; beyond 64 bases the
+ * pattern is checked row by row); a read whose depth-t interval exceeds 256 rows walks.  All
+ * modes give the reference's candidates. */
 PQ_API int pq_set_seed_mode (pq_ctx * ctx, int mode);
 
 /* Overlap search with transitive reduction for every read: find_intervals +

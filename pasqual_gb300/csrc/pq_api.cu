@@ -372,6 +372,9 @@ int pq_build_index(pq_ctx* ctx) {
     }
     ctx->ms_sort = s;
     ctx->ms_fm = f;
+    // the sort and k-mer working memory is not needed by the search: give it back
+    ctx->sort_tmp.release();
+    ctx->ktmp.release();
     return PQ_OK;
 }
 
@@ -459,12 +462,12 @@ static int search_prepare(pq_ctx* ctx, pq::SearchArgs& A, pq::SearchOut& O) {
     A.L = ctx->L;
     A.t = ctx->t;
     A.seed_k = ctx->fm_k[0];
-    // Interval scan where depth-t intervals are small: 4^t well above 64 n (chance hits rare) and
-    // patterns of up to 64 bases; otherwise the walk.  Learned windows need 16-base keys.
+    // Interval scan where depth-t intervals are small (4^min(t, 64) well above 64 n: chance hits
+    // rare) and L - t <= 256; otherwise the walk.  Learned windows need 16-base keys.
     {
         const double n = double(n_rows(ctx)) + 1.0;
-        const bool small_intervals = 2.0 * ctx->t > std::log2(n) + 6.0;
-        const bool scan = small_intervals && ctx->t <= 64 && ctx->L - ctx->t <= 128 && ctx->t > A.seed_k;
+        const bool small_intervals = 2.0 * std::min(ctx->t, 64) > std::log2(n) + 6.0;
+        const bool scan = small_intervals && ctx->L - ctx->t <= 256 && ctx->t > A.seed_k;
         A.sa_seed = 0;
         if (scan && ctx->seed_mode == 1) A.sa_seed = 1;
         if (scan && ctx->seed_mode == 2 && ctx->t >= pq::kLxKeyBases && nr) {

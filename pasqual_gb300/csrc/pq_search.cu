@@ -246,8 +246,9 @@ __device__ __forceinline__ int meta_type(uint32_t m) { return int(m >> 16); }
 // bases, the two chains of a side searched together.  A row compares as its suffix string with
 // end-of-read lowest, the order of the backward search.
 
-constexpr int kScanWords = 2;       // depth-t patterns up to 64 bases
+constexpr int kScanWords = 2;       // bases of P_t searched by bisection: the first 64 at most
 constexpr int kScanMax = 256;       // larger depth-t intervals walk instead
+constexpr int kScanMaskWords = 4;   // L - t up to 256
 
 // 64 bases of packed text starting at base p (first base in the top bits)
 __device__ __forceinline__ uint64_t text_window(const uint64_t* __restrict__ pk, size_t p) {
@@ -332,9 +333,9 @@ __device__ __forceinline__ void sa_bounds2(const FmView* f0, const FmView* f1, i
     end[0] = b0[0]; end[1] = b0[1];
 }
 
-// r'[0, o) (walked index text at ra) == pat(t + o) .. pat(t + 1): the read's own bases at
-// self * L + L - t - o of the walked index's text (strict kinds) or, complemented, of the other
-// index's text (FF, BB)
+// `o` bases of the walked index's text at ra equal those of the pattern source at rs.  The
+// pattern P_d (d = t + o) of a strict kind is the read's own text in the walked index at
+// self * L + L - d; of FF and BB it is the complement of the other index's text there.
 __device__ __forceinline__ bool prefix_matches(const uint64_t* __restrict__ pka, size_t ra,
                                                const uint64_t* __restrict__ pks, size_t rs, int o, bool cmpl) {
     for (int c = 0; c < o; c += 32) {
@@ -389,6 +390,7 @@ __device__ __forceinline__ bool scan_pair(const SearchArgs& A, const FmView* fm,
                                           int k0, int k1, int (&n)[2], int32_t& olp, uint32_t& probes,
                                           const Slots& slots) {
     const int L = A.L, t = A.t, k = A.seed_k, M = L - t;
+    const int tb = t < 32 * kScanWords ? t : 32 * kScanWords;    // bases bisected; the rest checked per row
     uint64_t P0[kScanWords], P1[kScanWords];
     pack_pattern(rd, L, t, k0, P0);
     pack_pattern(rd, L, t, k1, P1);
@@ -419,7 +421,7 @@ __device__ __forceinline__ bool scan_pair(const SearchArgs& A, const FmView* fm,
         if (hi[0] < lo[0]) hi[0] = lo[0];
         if (hi[1] < lo[1]) hi[1] = lo[1];
     }
-    sa_bounds2(f0, f1, L, P0, P1, t, lo, hi, first, end, probes);
+    sa_bounds2(f0, f1, L, P0, P1, tb, lo, hi, first, end, probes);
     if (A.sa_seed == 2) {
         // The window holds the answer for every key present in the index; for any other key it
         // is checked: the rows just outside the window must not start with P_t.
@@ -431,12 +433,12 @@ __device__ __forceinline__ bool scan_pair(const SearchArgs& A, const FmView* fm,
             const uint64_t (&P)[kScanWords] = q ? P1 : P0;
             if (first[q] == lo[q] && lo[q] > 0) {
                 const idx_t p = __ldg(fa.sa + lo[q] - 1);
-                ok = ok && cmp_row(fa.pk, p, L - int(p % idx_t(L)), P, t) < 0;
+                ok = ok && cmp_row(fa.pk, p, L - int(p % idx_t(L)), P, tb) < 0;
                 probes += 2;
             }
             if (end[q] == hi[q] && hi[q] < n_rows) {
                 const idx_t p = __ldg(fa.sa + hi[q]);
-                ok = ok && cmp_row(fa.pk, p, L - int(p % idx_t(L)), P, t) > 0;
+                ok = ok && cmp_row(fa.pk, p, L - int(p % idx_t(L)), P, tb) > 0;
                 probes += 2;
             }
         }
@@ -453,20 +455,25 @@ __device__ __forceinline__ bool scan_pair(const SearchArgs& A, const FmView* fm,
         const FmView& fb = fm[1 - walked_index(kind)];
         const bool cmpl = !(kind == PQ_FB || kind == PQ_BF);
         const uint64_t* pks = cmpl ? fb.pk : fa.pk;
-        const size_t src = size_t(self) * L + size_t(L - t);     // minus o
-        uint64_t m0 = 0, m1 = 0;                                   // depths with candidates
+        const size_t src = size_t(self) * L + size_t(L - t);     // P_t in the pattern source
+        uint64_t mk0 = 0, mk1 = 0, mk2 = 0, mk3 = 0;              // depths with candidates (o < 256)
         for (idx_t row = first[q]; row < end[q]; ++row) {
             const idx_t p = __ldg(fa.sa + row);
             const idx_t rp = p / idx_t(L);
             const int o = int(p - rp * idx_t(L));
             probes += 2;
             if (o >= M || !prefix_matches(fa.pk, size_t(rp) * L, pks, src - o, o, cmpl)) continue;
+            if (t > tb && !prefix_matches(fa.pk, size_t(p) + tb, pks, src + tb, t - tb, cmpl)) continue;
             const uint64_t bit = uint64_t(1) << (o & 63);
-            const bool seen = ((o < 64 ? m0 : m1) & bit) != 0;
+            const int hw = o >> 6;
+            const uint64_t cur = hw == 0 ? mk0 : hw == 1 ? mk1 : hw == 2 ? mk2 : mk3;
+            const bool seen = (cur & bit) != 0;
+            mk0 |= hw == 0 ? bit : 0;
+            mk1 |= hw == 1 ? bit : 0;
+            mk2 |= hw == 2 ? bit : 0;
+            mk3 |= hw == 3 ? bit : 0;
             if (!seen) {
                 slots.set(q, o, rp, 1, 0);
-                if (o < 64) m0 |= bit;
-                else m1 |= bit;
             } else {
                 idx_t r0, cnt;
                 slots.get(q, o, r0, cnt);
@@ -474,9 +481,9 @@ __device__ __forceinline__ bool scan_pair(const SearchArgs& A, const FmView* fm,
             }
         }
         int i = 0;
-        #pragma unroll 1
-        for (int h = 0; h < 2; ++h) {
-            uint64_t m = h ? m1 : m0;
+        #pragma unroll
+        for (int h = 0; h < kScanMaskWords; ++h) {
+            uint64_t m = h == 0 ? mk0 : h == 1 ? mk1 : h == 2 ? mk2 : mk3;
             while (m) {
                 const int o = 64 * h + __ffsll((long long)m) - 1;
                 m &= m - 1;

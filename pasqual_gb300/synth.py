@@ -117,6 +117,17 @@ WORKLOADS = {
                              L=50, cov=40, err=0.0, t=31),
     "50Mbp_L100_30x_t63": dict(genome=50_000_000, gc=0.41, repeat=0.10, div=(0.01, 0.01),
                                lowc=0.0, L=100, cov=30, err=0.005, t=63),
+    # learned-index workload: 12 % repeats, 2 % dinucleotide runs; 64-bit index
+    "200Mbp_L150_20x_t63": dict(genome=200_000_000, gc=0.40, repeat=0.12, div=(0.01, 0.01),
+                                lowc=0.02, L=150, cov=20, err=0.003, t=63),
+}
+
+# Queued-search workload: one genome, several read sets, each with its own read length (uniform
+# in [75, 250]) and min overlap (from {31, 47, 63, 95}, below L - 4); together 25x coverage.
+BATCHED = {
+    "100Mbp_L75-250_25x_batched": dict(genome=100_000_000, gc=0.45, repeat=0.08, div=(0.01, 0.01),
+                                       lowc=0.0, L=(75, 250), cov=25, err=0.005,
+                                       t=(31, 47, 63, 95), batches=8),
 }
 
 
@@ -161,3 +172,19 @@ def dedup(rd: np.ndarray) -> np.ndarray:
     _, first = np.unique(key, return_index=True)
     first.sort()
     return np.ascontiguousarray(rd[first])
+
+
+def make_batches(name: str = "100Mbp_L75-250_25x_batched", scale: float = 1.0, seed: int = 31):
+    """Read sets of a queued-search workload: [(reads, L, t)], de-duplicated."""
+    w = BATCHED[name]
+    glen = max(int(w["genome"] * scale), 4 * w["L"][1])
+    gen = genome(glen, w["gc"], w["repeat"], w["div"], w["lowc"], seed=seed)
+    rng = np.random.default_rng(seed + 1000)
+    out = []
+    for b in range(w["batches"]):
+        L = int(rng.integers(w["L"][0], w["L"][1] + 1))
+        ts = [x for x in w["t"] if x < L - 4]
+        t = int(ts[int(rng.integers(0, len(ts)))])
+        rd = reads_for_coverage(gen, L, w["cov"] / w["batches"], w["err"], seed=seed + 1 + b)
+        out.append((dedup(rd), L, t))
+    return out
