@@ -880,6 +880,127 @@ __device__ __forceinline__ int owner_of(const int* pref, int e) {
 // in which lanes happen to run, so every edge list is the reference's.
 // Phase C: each lane publishes its read (edge-pool reservation, copy, per-read counts).
 
+// ------------------------------------------------------------------------------ sorted reduction
+//
+// extract_*_edges as a function of the candidate set.  At DFS level j an interval of candidate
+// group (kind, d) holds exactly the candidates r' whose next j bases after the overlap -- their
+// continuation lambda(r') -- equal the DFS path s: extending the other index's interval by base a
+// selects the candidates whose next base is a (the complement on the forward index).  So the DFS
+// is a walk over the trie of continuations in base order, and:
+//   * it emits at node s exactly when some candidate's continuation is s (its len + level == L),
+//     taking the first interval in stack order with that length -- the group of the side's first
+//     kind if it has a candidate there, else the second kind's -- and its reads (in row order,
+//     i.e. ascending read id, the read itself left out), with path_t.trans = the number of
+//     candidates whose continuation starts with s (the frame's interval sizes summed);
+//   * an emission ends the branch, so a candidate whose continuation has another candidate's as a
+//     proper prefix is never reached.
+// Below, each candidate's continuation (L - d <= 64 bases) is read from the packed text -- the
+// forward text from r' * L + d for candidates on the backward index, the complemented backward
+// text there for candidates on the forward index -- and the emitted edges are ordered by
+// continuation, then read id: the DFS order.  No FM-index step is taken.
+
+constexpr int kRedMax = 64;          // candidates of one (read, side) reduced this way
+
+__device__ __forceinline__ void continuation(const SearchArgs& A, int type, idx_t rp, int d, uint64_t& w0,
+                                             uint64_t& w1) {
+    const int L = A.L, len = L - d;
+    const bool fwd = cand_index(type) == 1;
+    const uint64_t* pk = A.fm[fwd ? 0 : 1].pk;
+    const size_t pos = size_t(rp) * L + size_t(d);
+    w0 = text_window(pk, pos);
+    w1 = len > 32 ? text_window(pk, pos + 32) : 0;
+    if (!fwd) {
+        w0 = ~w0;
+        w1 = ~w1;
+    }
+    w0 &= top_mask(len < 32 ? len : 32);
+    w1 = len > 32 ? (w1 & top_mask(len - 32)) : 0;
+}
+
+// the first n bases (1 <= n <= 64) of two continuations agree
+__device__ __forceinline__ bool same_prefix(uint64_t a0, uint64_t a1, uint64_t b0, uint64_t b1, int n) {
+    if (n <= 32) return ((a0 ^ b0) & top_mask(n)) == 0;
+    return a0 == b0 && ((a1 ^ b1) & top_mask(n - 32)) == 0;
+}
+
+// Edges of one side of one read from its level-0 candidate groups (na of the first kind, then
+// n0 - na of the second) in the candidate scratch at `cand`; per-lane scratch at `red`.
+__device__ __forceinline__ int reduce_sorted(const SearchArgs& A, const WarpScratch& S, idx_t self, int side,
+                                             size_t cand, int na, int n0, size_t red, size_t eb, int& ne,
+                                             int& count, uint32_t& probes) {
+    const int L = A.L, M = L - A.t;
+    const int first_kind = side ? PQ_FB : PQ_BF;
+    int m = 0;
+    for (int g = 0; g < n0; ++g) {
+        const size_t src = cand + (g < na ? size_t(2 * side) * M + g : size_t(2 * side + 1) * M + (g - na));
+        const idx_t ll = S.c_ll[src], uu = S.c_uu[src];
+        const uint32_t mt = S.c_meta[src];
+        const int d = meta_len(mt), type = meta_type(mt);
+        const FmView& fb = A.fm[cand_index(type)];
+        for (idx_t row = ll; row <= uu; ++row) {
+            const idx_t p = __ldg(fb.sa + row);
+            const idx_t rp = p / idx_t(L);
+            uint64_t w0, w1;
+            continuation(A, type, rp, d, w0, w1);
+            S.r_k0[red + m] = w0;
+            S.r_k1[red + m] = w1;
+            S.r_id[red + m] = rp;
+            S.r_meta[red + m] = mt;
+            probes += 2;
+            ++m;
+        }
+    }
+    int nemit = 0;
+    for (int c = 0; c < m; ++c) {
+        const uint64_t c0 = S.r_k0[red + c], c1 = S.r_k1[red + c];
+        const uint32_t mc = S.r_meta[red + c];
+        const int lc = L - meta_len(mc);
+        bool covered = false, first_same = false;
+        int trans = 0;
+        for (int e = 0; e < m; ++e) {
+            const uint32_t me = S.r_meta[red + e];
+            const int le = L - meta_len(me);
+            if (!same_prefix(c0, c1, S.r_k0[red + e], S.r_k1[red + e], le < lc ? le : lc)) continue;
+            if (le < lc) {
+                covered = true;
+                break;
+            }
+            ++trans;
+            if (le == lc && meta_type(me) == first_kind) first_same = true;
+        }
+        if (covered || S.r_id[red + c] == self || (meta_type(mc) != first_kind && first_same)) continue;
+        S.r_emit[red + nemit++] = uint32_t(c) | (uint32_t(trans) << 16);
+    }
+    // DFS order: continuation, then read id (insertion sort; a handful of edges)
+    for (int i = 1; i < nemit; ++i) {
+        const uint32_t x = S.r_emit[red + i];
+        const int cx = int(x & 0xffff);
+        const uint64_t x0 = S.r_k0[red + cx], x1 = S.r_k1[red + cx];
+        const idx_t xi = S.r_id[red + cx];
+        int j = i - 1;
+        while (j >= 0) {
+            const int cy = int(S.r_emit[red + j] & 0xffff);
+            const uint64_t y0 = S.r_k0[red + cy], y1 = S.r_k1[red + cy];
+            const bool greater = y0 != x0 ? y0 > x0 : (y1 != x1 ? y1 > x1 : S.r_id[red + cy] > xi);
+            if (!greater) break;
+            S.r_emit[red + j + 1] = S.r_emit[red + j];
+            --j;
+        }
+        S.r_emit[red + j + 1] = x;
+    }
+    for (int i = 0; i < nemit; ++i) {
+        const uint32_t x = S.r_emit[red + i];
+        const int c = int(x & 0xffff);
+        if (ne >= S.ebcap) return OVF_EDGES;
+        S.e_dest[eb + ne] = S.r_id[red + c];
+        S.e_trans[eb + ne] = int32_t(x >> 16);
+        S.e_meta[eb + ne] = S.r_meta[red + c];
+        ++ne;
+    }
+    count = nemit;
+    return OVF_NONE;
+}
+
 // warp-cooperative copy of one batch description into shared memory
 __device__ __forceinline__ void load_batch(SearchBatch& dst, const SearchBatch* src, int lane) {
     static_assert(sizeof(SearchBatch) % 4 == 0, "batch description is copied in 32-bit words");
@@ -918,6 +1039,7 @@ __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A0, SearchOut
     const size_t tbase_w = gw * 32 * size_t(kTaskCap);         // task stacks
     const size_t xbase_w = gw * 32 * 4 * size_t(kPMax);        // sparse extension slots
     const size_t mbase_w = gw * 32 * size_t(kPMax);            // emission bounds
+    const size_t rbase_w = gw * 32 * size_t(kRedMax);          // sorted-reduction candidates
     TFrame* const frw = S.frames + gw * 32 * kTaskFrames;
     uint32_t probes = 0;
     int cur = -1;
@@ -978,6 +1100,13 @@ __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A0, SearchOut
             bool active = have && status == OVF_NONE && s_olp[wid][lane][side] != 0;   // src/string_graph.c:824, 828
             const int na = active ? s_n[wid][lane][2 * side] : 0;
             const int n0 = active ? na + s_n[wid][lane][2 * side + 1] : 0;
+            int sc_sorted = -1;
+            if (active && A.sorted_reduce && s_olp[wid][lane][side] <= kRedMax) {
+                const int st = reduce_sorted(A, S, self, side, cbase_w + size_t(lane) * 4 * size_t(S.mstride), na,
+                                             n0, rbase_w + size_t(lane) * kRedMax, eb, ne, sc_sorted, probes);
+                if (st != OVF_NONE) status = st;
+                active = false;
+            }
             if (active && n0 > kTaskCap) { status = OVF_STACK; active = false; }
             // level 0 = kind-0 candidates then kind-1 candidates, copied into the task stacks
             sm.na[lane] = na;
@@ -1191,6 +1320,7 @@ __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A0, SearchOut
                 }
                 __syncwarp();
             }
+            if (sc_sorted >= 0) sc = sc_sorted;
             if (side == 0) count_b = sc;
             else count_f = sc;
         }
@@ -1276,6 +1406,12 @@ static size_t scratch_layout(int M_max, size_t nwarps, int ebcap, void* base, Wa
     T.em_l = reinterpret_cast<idx_t*>(take(emb * sizeof(idx_t)));
     T.em_u = reinterpret_cast<idx_t*>(take(emb * sizeof(idx_t)));
     T.frames = reinterpret_cast<TFrame*>(take(frm * sizeof(TFrame)));
+    const size_t red = nwarps * 32 * size_t(kRedMax);
+    T.r_k0 = reinterpret_cast<uint64_t*>(take(red * 8));
+    T.r_k1 = reinterpret_cast<uint64_t*>(take(red * 8));
+    T.r_id = reinterpret_cast<idx_t*>(take(red * sizeof(idx_t)));
+    T.r_meta = reinterpret_cast<uint32_t*>(take(red * 4));
+    T.r_emit = reinterpret_cast<uint32_t*>(take(red * 4));
     T.ebcap = ebcap;
     T.mstride = int(M);
     if (S) *S = T;
