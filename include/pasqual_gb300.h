@@ -114,7 +114,7 @@ PQ_API int pq_set_seed_k (pq_ctx * ctx, int k);
  * 4^min(t, 64) > 64 * num_reads * read_len (depth-t intervals are small; beyond 64 bases the
  * pattern is checked row by row); a read whose depth-t interval exceeds 256 rows walks.  All
  * modes give the reference's candidates.  Modes 1 and 2 also reduce each (read, side) with at
- * most 64 candidates, when L - t <= 64, from the candidates' continuations (the bases after the
+ * most 64 candidates, when L - t <= 256, from the candidates' continuations (the bases after the
  * overlap, read from the packed text) instead of the FM-index DFS of extract_*_edges: an edge is
  * emitted exactly when no other candidate's continuation is a proper prefix of its own, ordered
  * as the DFS visits them.  Mode 0 runs the reference's method throughout. */

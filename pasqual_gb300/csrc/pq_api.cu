@@ -483,8 +483,8 @@ static int search_prepare(pq_ctx* ctx, pq::SearchArgs& A, pq::SearchOut& O) {
     }
     ctx->lx_queries = A.sa_seed == 2 ? 4 * uint64_t(nr) : 0;
     // seed mode 0 is the reference's method throughout (walk + FM-index DFS); 1 and 2 reduce by
-    // sorted continuations wherever those fit in 64 bases
-    A.sorted_reduce = (ctx->seed_mode != 0 && ctx->L - ctx->t <= 64) ? 1 : 0;
+    // sorted continuations wherever those fit in 256 bases
+    A.sorted_reduce = (ctx->seed_mode != 0 && ctx->L - ctx->t <= 256) ? 1 : 0;
 
     unsigned long long* ctr = ctx->ctrs.as<unsigned long long>();   // [0] e_count [1] probes [2] ovf(u32)
     O.num_B = ctx->nB.as<uint16_t>();

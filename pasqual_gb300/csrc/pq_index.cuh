@@ -45,7 +45,7 @@ struct SearchArgs {
     int sa_seed;                // 1: candidates by depth-t interval scan (needs fm[].sa/pk/isa),
                                 // 2: the same with learned windows (needs fm[].lx)
     unsigned long long* lx_misses;  // learned windows that missed (those chains walk)
-    int sorted_reduce;          // 1: edges from sorted continuations where L - t <= 64
+    int sorted_reduce;          // 1: edges from sorted continuations (L - t <= 256)
 };
 
 // Global scratch of the fast kernel, per warp of 32 reads: level-0 candidates (4 kinds x (L - t)
@@ -64,7 +64,7 @@ struct WarpScratch {
     uint32_t* x_meta;
     idx_t *em_l, *em_u;
     TFrame* frames;
-    uint64_t *r_k0, *r_k1;      // sorted reduction: continuation words,
+    uint64_t* r_k;              // sorted reduction: continuation words (8 per candidate),
     idx_t* r_id;                //   read ids,
     uint32_t *r_meta, *r_emit;  //   (overlap, type) and emitted (index, trans)
     int ebcap;

@@ -894,33 +894,43 @@ __device__ __forceinline__ int owner_of(const int* pref, int e) {
 //     candidates whose continuation starts with s (the frame's interval sizes summed);
 //   * an emission ends the branch, so a candidate whose continuation has another candidate's as a
 //     proper prefix is never reached.
-// Below, each candidate's continuation (L - d <= 64 bases) is read from the packed text -- the
+// Below, each candidate's continuation (L - d <= 256 bases) is read from the packed text -- the
 // forward text from r' * L + d for candidates on the backward index, the complemented backward
 // text there for candidates on the forward index -- and the emitted edges are ordered by
 // continuation, then read id: the DFS order.  No FM-index step is taken.
 
 constexpr int kRedMax = 64;          // candidates of one (read, side) reduced this way
+constexpr int kLamWords = 8;         // continuations up to 256 bases (L - t <= 256)
 
-__device__ __forceinline__ void continuation(const SearchArgs& A, int type, idx_t rp, int d, uint64_t& w0,
-                                             uint64_t& w1) {
+// continuation of candidate r' at overlap d: L - d bases, 32 a word, first base in the top bits,
+// zero past the end
+__device__ __forceinline__ void continuation(const SearchArgs& A, int type, idx_t rp, int d, uint64_t* out) {
     const int L = A.L, len = L - d;
     const bool fwd = cand_index(type) == 1;
     const uint64_t* pk = A.fm[fwd ? 0 : 1].pk;
     const size_t pos = size_t(rp) * L + size_t(d);
-    w0 = text_window(pk, pos);
-    w1 = len > 32 ? text_window(pk, pos + 32) : 0;
-    if (!fwd) {
-        w0 = ~w0;
-        w1 = ~w1;
+    const uint64_t flip = fwd ? 0 : ~uint64_t(0);
+    #pragma unroll
+    for (int w = 0; w < kLamWords; ++w) {
+        const int left = len - 32 * w;
+        out[w] = left > 0 ? ((text_window(pk, pos + 32 * w) ^ flip) & top_mask(left < 32 ? left : 32)) : 0;
     }
-    w0 &= top_mask(len < 32 ? len : 32);
-    w1 = len > 32 ? (w1 & top_mask(len - 32)) : 0;
 }
 
-// the first n bases (1 <= n <= 64) of two continuations agree
-__device__ __forceinline__ bool same_prefix(uint64_t a0, uint64_t a1, uint64_t b0, uint64_t b1, int n) {
-    if (n <= 32) return ((a0 ^ b0) & top_mask(n)) == 0;
-    return a0 == b0 && ((a1 ^ b1) & top_mask(n - 32)) == 0;
+// the first n bases (1 <= n <= 256) of continuations a and b agree
+__device__ __forceinline__ bool same_prefix(const uint64_t* a, const uint64_t* b, int n) {
+    int w = 0;
+    for (; 32 * (w + 1) <= n; ++w)
+        if (a[w] != b[w]) return false;
+    const int rest = n - 32 * w;
+    return rest == 0 || ((a[w] ^ b[w]) & top_mask(rest)) == 0;
+}
+
+// a < b as zero-padded base strings
+__device__ __forceinline__ int cmp_cont(const uint64_t* a, const uint64_t* b) {
+    for (int w = 0; w < kLamWords; ++w)
+        if (a[w] != b[w]) return a[w] < b[w] ? -1 : 1;
+    return 0;
 }
 
 // Edges of one side of one read from its level-0 candidate groups (na of the first kind, then
@@ -940,10 +950,7 @@ __device__ __forceinline__ int reduce_sorted(const SearchArgs& A, const WarpScra
         for (idx_t row = ll; row <= uu; ++row) {
             const idx_t p = __ldg(fb.sa + row);
             const idx_t rp = p / idx_t(L);
-            uint64_t w0, w1;
-            continuation(A, type, rp, d, w0, w1);
-            S.r_k0[red + m] = w0;
-            S.r_k1[red + m] = w1;
+            continuation(A, type, rp, d, S.r_k + (red + m) * kLamWords);
             S.r_id[red + m] = rp;
             S.r_meta[red + m] = mt;
             probes += 2;
@@ -952,7 +959,7 @@ __device__ __forceinline__ int reduce_sorted(const SearchArgs& A, const WarpScra
     }
     int nemit = 0;
     for (int c = 0; c < m; ++c) {
-        const uint64_t c0 = S.r_k0[red + c], c1 = S.r_k1[red + c];
+        const uint64_t* kc = S.r_k + (red + c) * kLamWords;
         const uint32_t mc = S.r_meta[red + c];
         const int lc = L - meta_len(mc);
         bool covered = false, first_same = false;
@@ -960,7 +967,7 @@ __device__ __forceinline__ int reduce_sorted(const SearchArgs& A, const WarpScra
         for (int e = 0; e < m; ++e) {
             const uint32_t me = S.r_meta[red + e];
             const int le = L - meta_len(me);
-            if (!same_prefix(c0, c1, S.r_k0[red + e], S.r_k1[red + e], le < lc ? le : lc)) continue;
+            if (!same_prefix(kc, S.r_k + (red + e) * kLamWords, le < lc ? le : lc)) continue;
             if (le < lc) {
                 covered = true;
                 break;
@@ -975,13 +982,13 @@ __device__ __forceinline__ int reduce_sorted(const SearchArgs& A, const WarpScra
     for (int i = 1; i < nemit; ++i) {
         const uint32_t x = S.r_emit[red + i];
         const int cx = int(x & 0xffff);
-        const uint64_t x0 = S.r_k0[red + cx], x1 = S.r_k1[red + cx];
+        const uint64_t* kx = S.r_k + (red + cx) * kLamWords;
         const idx_t xi = S.r_id[red + cx];
         int j = i - 1;
         while (j >= 0) {
             const int cy = int(S.r_emit[red + j] & 0xffff);
-            const uint64_t y0 = S.r_k0[red + cy], y1 = S.r_k1[red + cy];
-            const bool greater = y0 != x0 ? y0 > x0 : (y1 != x1 ? y1 > x1 : S.r_id[red + cy] > xi);
+            const int o = cmp_cont(S.r_k + (red + cy) * kLamWords, kx);
+            const bool greater = o != 0 ? o > 0 : S.r_id[red + cy] > xi;
             if (!greater) break;
             S.r_emit[red + j + 1] = S.r_emit[red + j];
             --j;
@@ -1407,8 +1414,7 @@ static size_t scratch_layout(int M_max, size_t nwarps, int ebcap, void* base, Wa
     T.em_u = reinterpret_cast<idx_t*>(take(emb * sizeof(idx_t)));
     T.frames = reinterpret_cast<TFrame*>(take(frm * sizeof(TFrame)));
     const size_t red = nwarps * 32 * size_t(kRedMax);
-    T.r_k0 = reinterpret_cast<uint64_t*>(take(red * 8));
-    T.r_k1 = reinterpret_cast<uint64_t*>(take(red * 8));
+    T.r_k = reinterpret_cast<uint64_t*>(take(red * 8 * kLamWords));
     T.r_id = reinterpret_cast<idx_t*>(take(red * sizeof(idx_t)));
     T.r_meta = reinterpret_cast<uint32_t*>(take(red * 4));
     T.r_emit = reinterpret_cast<uint32_t*>(take(red * 4));

@@ -140,6 +140,26 @@ def test_repeats_errors_long_reads_against_oracle():
     assert np.array_equal(out.num_B, ref.num_B) and np.array_equal(out.num_F, ref.num_F)
 
 
+@pytest.mark.parametrize("t", [31, 95])
+def test_long_reads_against_oracle(t):
+    """L = 180 (continuations up to 149 bases, DFS depth beyond the fast tier's frames) with
+    repeats and errors: every seed mode equals the oracle."""
+    gen = synth.genome(120_000, 0.45, 0.08, (0.01, 0.01), 0.0, seed=41 + t)
+    rd = np.unique(synth.reads_for_coverage(gen, 180, 12, 0.005, seed=42 + t), axis=0)
+    ix, ref = _oracle_run(rd, t, 32)
+    for mode in (0, 1, 2):
+        with gpu_ctx(32) as P:
+            P.set_reads(rd, t)
+            P.set_seed_mode(mode)
+            P.build_index()
+            out = P.construct_string_graph()
+        assert np.array_equal(out.edge_off, ref.edge_off), mode
+        assert np.array_equal(out.dest, ref.dest), mode
+        assert np.array_equal(out.length, ref.length) and np.array_equal(out.etype, ref.etype)
+        assert np.array_equal(out.trans, ref.trans), mode
+        assert np.array_equal(out.olp_B, ref.olp_B) and np.array_equal(out.olp_F, ref.olp_F)
+
+
 def test_empty_and_tiny_inputs():
     with gpu_ctx(32) as P:
         P.construct_index(np.zeros((0, 50), np.uint8), 31)
