@@ -64,7 +64,8 @@ struct WarpScratch {
     uint32_t* x_meta;
     idx_t *em_l, *em_u;
     TFrame* frames;
-    uint64_t* r_k;              // sorted reduction: continuation words (8 per candidate),
+    uint64_t* r_k;              // sorted reduction: continuation words (word w of slot i at
+    size_t r_plane;             //   r_k[w * r_plane + i]),
     idx_t* r_id;                //   read ids,
     uint32_t *r_meta, *r_emit;  //   (overlap, type) and emitted (index, trans)
     int ebcap;

@@ -902,35 +902,37 @@ __device__ __forceinline__ int owner_of(const int* pref, int e) {
 constexpr int kRedMax = 64;          // candidates of one (read, side) reduced this way
 constexpr int kLamWords = 8;         // continuations up to 256 bases (L - t <= 256)
 
-// continuation of candidate r' at overlap d: L - d bases, 32 a word, first base in the top bits,
-// zero past the end
-__device__ __forceinline__ void continuation(const SearchArgs& A, int type, idx_t rp, int d, uint64_t* out) {
+// continuation of candidate r' at overlap d: L - d bases in ceil((L - d) / 32) words, first base
+// in the top bits, zero past the end
+__device__ __forceinline__ void continuation(const SearchArgs& A, int type, idx_t rp, int d, uint64_t* out,
+                                             size_t plane) {
     const int L = A.L, len = L - d;
     const bool fwd = cand_index(type) == 1;
     const uint64_t* pk = A.fm[fwd ? 0 : 1].pk;
     const size_t pos = size_t(rp) * L + size_t(d);
     const uint64_t flip = fwd ? 0 : ~uint64_t(0);
-    #pragma unroll
-    for (int w = 0; w < kLamWords; ++w) {
+    for (int w = 0; 32 * w < len; ++w) {
         const int left = len - 32 * w;
-        out[w] = left > 0 ? ((text_window(pk, pos + 32 * w) ^ flip) & top_mask(left < 32 ? left : 32)) : 0;
+        out[w * plane] = (text_window(pk, pos + 32 * w) ^ flip) & top_mask(left < 32 ? left : 32);
     }
 }
 
-// the first n bases (1 <= n <= 256) of continuations a and b agree
-__device__ __forceinline__ bool same_prefix(const uint64_t* a, const uint64_t* b, int n) {
+// the first n bases (1 <= n <= 256) of continuations a and b agree (word w at a[w * plane])
+__device__ __forceinline__ bool same_prefix(const uint64_t* a, const uint64_t* b, int n, size_t plane) {
     int w = 0;
     for (; 32 * (w + 1) <= n; ++w)
-        if (a[w] != b[w]) return false;
+        if (a[w * plane] != b[w * plane]) return false;
     const int rest = n - 32 * w;
-    return rest == 0 || ((a[w] ^ b[w]) & top_mask(rest)) == 0;
+    return rest == 0 || ((a[w * plane] ^ b[w * plane]) & top_mask(rest)) == 0;
 }
 
-// a < b as zero-padded base strings
-__device__ __forceinline__ int cmp_cont(const uint64_t* a, const uint64_t* b) {
-    for (int w = 0; w < kLamWords; ++w)
-        if (a[w] != b[w]) return a[w] < b[w] ? -1 : 1;
-    return 0;
+// order of two continuations of la and lb bases that are equal or not prefixes of one another:
+// their first differing base, else equal
+__device__ __forceinline__ int cmp_cont(const uint64_t* a, int la, const uint64_t* b, int lb, size_t plane) {
+    const int nw = ((la < lb ? la : lb) + 31) / 32;
+    for (int w = 0; w < nw; ++w)
+        if (a[w * plane] != b[w * plane]) return a[w * plane] < b[w * plane] ? -1 : 1;
+    return la == lb ? 0 : (la < lb ? -1 : 1);
 }
 
 // Edges of one side of one read from its level-0 candidate groups (na of the first kind, then
@@ -950,7 +952,7 @@ __device__ __forceinline__ int reduce_sorted(const SearchArgs& A, const WarpScra
         for (idx_t row = ll; row <= uu; ++row) {
             const idx_t p = __ldg(fb.sa + row);
             const idx_t rp = p / idx_t(L);
-            continuation(A, type, rp, d, S.r_k + (red + m) * kLamWords);
+            continuation(A, type, rp, d, S.r_k + red + m, S.r_plane);
             S.r_id[red + m] = rp;
             S.r_meta[red + m] = mt;
             probes += 2;
@@ -959,7 +961,7 @@ __device__ __forceinline__ int reduce_sorted(const SearchArgs& A, const WarpScra
     }
     int nemit = 0;
     for (int c = 0; c < m; ++c) {
-        const uint64_t* kc = S.r_k + (red + c) * kLamWords;
+        const uint64_t* kc = S.r_k + red + c;
         const uint32_t mc = S.r_meta[red + c];
         const int lc = L - meta_len(mc);
         bool covered = false, first_same = false;
@@ -967,7 +969,7 @@ __device__ __forceinline__ int reduce_sorted(const SearchArgs& A, const WarpScra
         for (int e = 0; e < m; ++e) {
             const uint32_t me = S.r_meta[red + e];
             const int le = L - meta_len(me);
-            if (!same_prefix(kc, S.r_k + (red + e) * kLamWords, le < lc ? le : lc)) continue;
+            if (!same_prefix(kc, S.r_k + red + e, le < lc ? le : lc, S.r_plane)) continue;
             if (le < lc) {
                 covered = true;
                 break;
@@ -982,12 +984,13 @@ __device__ __forceinline__ int reduce_sorted(const SearchArgs& A, const WarpScra
     for (int i = 1; i < nemit; ++i) {
         const uint32_t x = S.r_emit[red + i];
         const int cx = int(x & 0xffff);
-        const uint64_t* kx = S.r_k + (red + cx) * kLamWords;
+        const uint64_t* kx = S.r_k + red + cx;
+        const int lx = L - meta_len(S.r_meta[red + cx]);
         const idx_t xi = S.r_id[red + cx];
         int j = i - 1;
         while (j >= 0) {
             const int cy = int(S.r_emit[red + j] & 0xffff);
-            const int o = cmp_cont(S.r_k + (red + cy) * kLamWords, kx);
+            const int o = cmp_cont(S.r_k + red + cy, L - meta_len(S.r_meta[red + cy]), kx, lx, S.r_plane);
             const bool greater = o != 0 ? o > 0 : S.r_id[red + cy] > xi;
             if (!greater) break;
             S.r_emit[red + j + 1] = S.r_emit[red + j];
@@ -1415,6 +1418,7 @@ static size_t scratch_layout(int M_max, size_t nwarps, int ebcap, void* base, Wa
     T.frames = reinterpret_cast<TFrame*>(take(frm * sizeof(TFrame)));
     const size_t red = nwarps * 32 * size_t(kRedMax);
     T.r_k = reinterpret_cast<uint64_t*>(take(red * 8 * kLamWords));
+    T.r_plane = red;
     T.r_id = reinterpret_cast<idx_t*>(take(red * sizeof(idx_t)));
     T.r_meta = reinterpret_cast<uint32_t*>(take(red * 4));
     T.r_emit = reinterpret_cast<uint32_t*>(take(red * 4));
