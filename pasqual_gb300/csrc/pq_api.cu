@@ -100,7 +100,7 @@ struct pq_ctx {
 
     // overlap-search output
     DevBuf nB, nF, oB, oF, status, esrc, e_dest, e_trans, e_len, e_type, ctrs, ovf_list;
-    DevBuf off, g_dest, g_len, g_type, g_trans, asm_tmp, wide, warp_scratch;
+    DevBuf off, g_dest, g_len, g_type, g_trans, asm_tmp, wide, warp_scratch, defer;
     bool graph_ok = false;
     uint64_t num_edges = 0, probes = 0, wide_reads = 0;
 };
@@ -176,7 +176,7 @@ void pq_destroy(pq_ctx* ctx) {
     DevBuf* bufs[] = {&ctx->reads, &ctx->ktmp, &ctx->sort_tmp, &ctx->counts, &ctx->nB, &ctx->nF, &ctx->oB,
                       &ctx->oF, &ctx->status, &ctx->esrc, &ctx->e_dest, &ctx->e_trans, &ctx->e_len,
                       &ctx->e_type, &ctx->ctrs, &ctx->ovf_list, &ctx->off, &ctx->g_dest, &ctx->g_len,
-                      &ctx->g_type, &ctx->g_trans, &ctx->asm_tmp, &ctx->wide, &ctx->warp_scratch};
+                      &ctx->g_type, &ctx->g_trans, &ctx->asm_tmp, &ctx->wide, &ctx->warp_scratch, &ctx->defer};
     for (DevBuf* b : bufs) b->release();
     for (int d = 0; d < 2; ++d) {
         ctx->sa[d].release();
@@ -624,10 +624,20 @@ int pq_overlaps(pq_ctx* ctx) {
     int dev_sms = 152;
     cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device);
     CK(cudaEventRecord(ctx->evk0, ctx->st));
-    if (nr) {
+    if (nr && A.sorted_reduce) {
+        // lean tier over every read (thread per read), then the fast tier over what it hands over
+        const int ebcap = 64;
+        const int lean = int(std::min<size_t>((nr + 127) / 128, size_t(pq::search_lean_blocks(ctx->L, ctx->L - ctx->t, dev_sms))));
+        const int fast = pq::search_fast_blocks(ctx->L, ctx->L - ctx->t, dev_sms);
+        const size_t wsb = pq::lean_scratch_bytes(ctx->L, ctx->t, lean, fast, ebcap);
+        CK(ctx->warp_scratch.ensure(wsb));
+        CK(ctx->defer.ensure((nr + 1) * sizeof(idx_t)));
+        CK(pq::search_lean(A, O, lean, fast, ctx->warp_scratch.p, wsb, ebcap, ctx->defer.as<idx_t>(),
+                           reinterpret_cast<unsigned*>(ctx->ctrs.as<unsigned long long>() + 4), ctx->st));
+    } else if (nr) {
         // 4 warps per block, each warp 32 reads per batch; enough blocks to fill every SM
         const int ebcap = 64;
-        int blocks = int(std::min<size_t>((nr + 127) / 128, size_t(pq::search_fast_blocks(ctx->L, dev_sms))));
+        int blocks = int(std::min<size_t>((nr + 127) / 128, size_t(pq::search_fast_blocks(ctx->L, ctx->L - ctx->t, dev_sms))));
         const size_t wsb = pq::warp_scratch_bytes(ctx->L, ctx->t, size_t(blocks) * 4, ebcap);
         CK(ctx->warp_scratch.ensure(wsb));
         CK(pq::search_fast(A, O, blocks, ctx->warp_scratch.p, wsb, ebcap, ctx->st));
@@ -861,7 +871,7 @@ static int queue_launch(pq_ctx* lead, const std::vector<uint32_t>& ib, const std
     pq_ctx* ctx = lead;
     int dev_sms = 152;
     cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, lead->device);
-    int per_sm = pq::search_fast_blocks(L_max, 1);
+    int per_sm = pq::search_fast_blocks(L_max, M_max, 1);
     if (lead->q_ctas_per_sm > 0) per_sm = lead->q_ctas_per_sm;
     const size_t nitems = ib.size();
     const unsigned gpi = unsigned(std::max(1, lead->q_groups_per_item));
@@ -1009,7 +1019,7 @@ int pq_autotune_batched(pq_ctx** ctxs, int count, int flags, float* best_ms) {
     int L_max = 1;
     for (int b = 0; b < count; ++b)
         if (ctxs[b]) L_max = std::max(L_max, ctxs[b]->L);
-    max_per_sm = pq::search_fast_blocks(L_max, 1);
+    max_per_sm = pq::search_fast_blocks(L_max, 256, 1);
     float best = -1.f;
     int bc = 0, bg = 1, be = 64;
     const int edge_opts[2] = {32, 64};

@@ -87,13 +87,22 @@ struct SearchQueue {
     unsigned count;             // 0: no queue
     unsigned groups_per_item;
     unsigned* next;
+    // without a queue: search only the reads read_list[0, *list_count) (nullptr: every read)
+    const idx_t* read_list;
+    const unsigned* list_count;
 };
 size_t warp_scratch_bytes(int L, int t, size_t nwarps, int ebcap);
-int search_fast_blocks(int L, int num_sms);   // resident blocks of the fast kernel on the device
+int search_fast_blocks(int L, int M, int num_sms);   // resident blocks of the fast kernel (M = L - t)
 // blocks of 128 threads (4 warps); reads that outgrow the shared-memory stack, ebcap edges or
 // the frame count are listed for the wide kernel.
 cudaError_t search_fast(const SearchArgs& a, const SearchOut& o, int blocks, void* scratch, size_t scratch_bytes,
                         int ebcap, cudaStream_t st);
+// Lean tier (thread per read, sorted reduction) over every read, then the fast tier over the reads
+// it hands over (more than 64 candidates on a side); needs a.sorted_reduce.
+int search_lean_blocks(int L, int M, int num_sms);
+size_t lean_scratch_bytes(int L, int t, int lean_blocks, int fast_blocks, int ebcap);
+cudaError_t search_lean(const SearchArgs& a, const SearchOut& o, int lean_blocks, int fast_blocks, void* scratch,
+                        size_t scratch_bytes, int ebcap, idx_t* defer, unsigned* defer_count, cudaStream_t st);
 // One persistent launch over a queue of batches (L_max, M_max: the largest L and L - t).
 size_t queue_scratch_bytes(int L_max, int M_max, size_t nwarps, int ebcap);
 cudaError_t search_fast_queue(const SearchQueue& q, int L_max, int M_max, int blocks, void* scratch,

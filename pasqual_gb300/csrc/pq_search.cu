@@ -902,8 +902,12 @@ __device__ __forceinline__ int owner_of(const int* pref, int e) {
 constexpr int kRedMax = 64;          // candidates of one (read, side) reduced this way
 constexpr int kLamWords = 8;         // continuations up to 256 bases (L - t <= 256)
 
-// continuation of candidate r' at overlap d: L - d bases in ceil((L - d) / 32) words, first base
-// in the top bits, zero past the end
+// continuation words the kernels are built for: 2 (L - t <= 64) or kLamWords
+__host__ __device__ constexpr int lam_words(int M) { return M <= 64 ? 2 : kLamWords; }
+
+// continuation of candidate r' at overlap d: L - d bases (at most 32 W) in ceil((L - d) / 32)
+// words, first base in the top bits, zero past the end; word w at out[w * plane]
+template <int W>
 __device__ __forceinline__ void continuation(const SearchArgs& A, int type, idx_t rp, int d, uint64_t* out,
                                              size_t plane) {
     const int L = A.L, len = L - d;
@@ -911,32 +915,45 @@ __device__ __forceinline__ void continuation(const SearchArgs& A, int type, idx_
     const uint64_t* pk = A.fm[fwd ? 0 : 1].pk;
     const size_t pos = size_t(rp) * L + size_t(d);
     const uint64_t flip = fwd ? 0 : ~uint64_t(0);
-    for (int w = 0; 32 * w < len; ++w) {
+    #pragma unroll
+    for (int w = 0; w < W; ++w) {
         const int left = len - 32 * w;
+        if (left <= 0) break;
         out[w * plane] = (text_window(pk, pos + 32 * w) ^ flip) & top_mask(left < 32 ? left : 32);
     }
 }
 
-// the first n bases (1 <= n <= 256) of continuations a and b agree (word w at a[w * plane])
+// the first n bases (1 <= n <= 32 W) of continuations a and b agree
+template <int W>
 __device__ __forceinline__ bool same_prefix(const uint64_t* a, const uint64_t* b, int n, size_t plane) {
-    int w = 0;
-    for (; 32 * (w + 1) <= n; ++w)
-        if (a[w * plane] != b[w * plane]) return false;
-    const int rest = n - 32 * w;
-    return rest == 0 || ((a[w * plane] ^ b[w * plane]) & top_mask(rest)) == 0;
+    #pragma unroll
+    for (int w = 0; w < W; ++w) {
+        const int rest = n - 32 * w;
+        if (rest <= 0) return true;
+        const uint64_t x = a[w * plane] ^ b[w * plane];
+        if (rest < 32) return (x & top_mask(rest)) == 0;
+        if (x) return false;
+    }
+    return true;
 }
 
 // order of two continuations of la and lb bases that are equal or not prefixes of one another:
 // their first differing base, else equal
+template <int W>
 __device__ __forceinline__ int cmp_cont(const uint64_t* a, int la, const uint64_t* b, int lb, size_t plane) {
-    const int nw = ((la < lb ? la : lb) + 31) / 32;
-    for (int w = 0; w < nw; ++w)
-        if (a[w * plane] != b[w * plane]) return a[w * plane] < b[w * plane] ? -1 : 1;
+    const int n = la < lb ? la : lb;
+    #pragma unroll
+    for (int w = 0; w < W; ++w) {
+        if (32 * w >= n) break;
+        const uint64_t x = a[w * plane], y = b[w * plane];
+        if (x != y) return x < y ? -1 : 1;
+    }
     return la == lb ? 0 : (la < lb ? -1 : 1);
 }
 
 // Edges of one side of one read from its level-0 candidate groups (na of the first kind, then
 // n0 - na of the second) in the candidate scratch at `cand`; per-lane scratch at `red`.
+template <int W>
 __device__ __forceinline__ int reduce_sorted(const SearchArgs& A, const WarpScratch& S, idx_t self, int side,
                                              size_t cand, int na, int n0, size_t red, size_t eb, int& ne,
                                              int& count, uint32_t& probes) {
@@ -952,7 +969,7 @@ __device__ __forceinline__ int reduce_sorted(const SearchArgs& A, const WarpScra
         for (idx_t row = ll; row <= uu; ++row) {
             const idx_t p = __ldg(fb.sa + row);
             const idx_t rp = p / idx_t(L);
-            continuation(A, type, rp, d, S.r_k + red + m, S.r_plane);
+            continuation<W>(A, type, rp, d, S.r_k + red + m, S.r_plane);
             S.r_id[red + m] = rp;
             S.r_meta[red + m] = mt;
             probes += 2;
@@ -969,7 +986,7 @@ __device__ __forceinline__ int reduce_sorted(const SearchArgs& A, const WarpScra
         for (int e = 0; e < m; ++e) {
             const uint32_t me = S.r_meta[red + e];
             const int le = L - meta_len(me);
-            if (!same_prefix(kc, S.r_k + red + e, le < lc ? le : lc, S.r_plane)) continue;
+            if (!same_prefix<W>(kc, S.r_k + red + e, le < lc ? le : lc, S.r_plane)) continue;
             if (le < lc) {
                 covered = true;
                 break;
@@ -990,7 +1007,7 @@ __device__ __forceinline__ int reduce_sorted(const SearchArgs& A, const WarpScra
         int j = i - 1;
         while (j >= 0) {
             const int cy = int(S.r_emit[red + j] & 0xffff);
-            const int o = cmp_cont(S.r_k + red + cy, L - meta_len(S.r_meta[red + cy]), kx, lx, S.r_plane);
+            const int o = cmp_cont<W>(S.r_k + red + cy, L - meta_len(S.r_meta[red + cy]), kx, lx, S.r_plane);
             const bool greater = o != 0 ? o > 0 : S.r_id[red + cy] > xi;
             if (!greater) break;
             S.r_emit[red + j + 1] = S.r_emit[red + j];
@@ -1024,6 +1041,7 @@ __device__ __forceinline__ void load_batch(SearchBatch& dst, const SearchBatch* 
 // groups of 32 reads w, w + #warps, ...  With a queue, each warp takes the next item (a batch and
 // a group of its reads) from a shared counter until the queue is empty; the batch's description
 // (index pair, L, t, outputs) is loaded into the warp's shared memory when it changes.
+template <int W>
 __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A0, SearchOut O0, WarpScratch S, SearchQueue Q) {
     extern __shared__ uint32_t s_reads[];
     __shared__ SearchBatch s_b[kWarpsPerCta];
@@ -1053,6 +1071,8 @@ __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A0, SearchOut
     TFrame* const frw = S.frames + gw * 32 * kTaskFrames;
     uint32_t probes = 0;
     int cur = -1;
+    // reads of the current batch (or of the list of reads handed over by the lean tier)
+    const size_t list_n = Q.read_list ? size_t(*Q.list_count) : 0;
     for (size_t iter = 0;; ++iter) {
         size_t group, gend;
         if (Q.count) {
@@ -1073,13 +1093,15 @@ __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A0, SearchOut
         } else {
             group = gw + iter * nw;
             gend = group + 1;
-            if (group * 32 >= size_t(A.num_reads)) break;
+            if (group * 32 >= (Q.read_list ? list_n : size_t(A.num_reads))) break;
         }
-        for (; group < gend && group * 32 < size_t(A.num_reads); ++group) {
+        const size_t n_items = Q.read_list ? list_n : size_t(A.num_reads);
+        for (; group < gend && group * 32 < n_items; ++group) {
         const int M = A.L - A.t;
         const int L = A.L;
-        const size_t r = group * 32 + lane;
-        const bool have = r < size_t(A.num_reads);
+        const size_t item = group * 32 + lane;
+        const bool have = item < n_items;
+        const size_t r = Q.read_list ? (have ? size_t(Q.read_list[item]) : 0) : item;
         const idx_t self = idx_t(r);
         // ---- phase A
         if (have) {
@@ -1112,7 +1134,7 @@ __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A0, SearchOut
             const int n0 = active ? na + s_n[wid][lane][2 * side + 1] : 0;
             int sc_sorted = -1;
             if (active && A.sorted_reduce && s_olp[wid][lane][side] <= kRedMax) {
-                const int st = reduce_sorted(A, S, self, side, cbase_w + size_t(lane) * 4 * size_t(S.mstride), na,
+                const int st = reduce_sorted<W>(A, S, self, side, cbase_w + size_t(lane) * 4 * size_t(S.mstride), na,
                                              n0, rbase_w + size_t(lane) * kRedMax, eb, ne, sc_sorted, probes);
                 if (st != OVF_NONE) status = st;
                 active = false;
@@ -1378,12 +1400,105 @@ __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A0, SearchOut
     if (Q.count == 0 || cur >= 0) add_probes(O, probes);
 }
 
-int search_fast_blocks(int L, int num_sms) {
+// ------------------------------------------------------------------------------ lean tier
+//
+// One thread per read, no warp-level phases: candidates by the interval scan (or the walk where
+// the scan does not apply) and each side's edges by sorted continuations.  A read with more than
+// kRedMax candidates on a side is listed in `defer` for the fast tier (which runs the DFS there);
+// a read whose edges outgrow its edge slots goes to the wide tier like any other overflow.  With
+// no shared-memory DFS state and fewer registers, more warps stay resident to hide the latency of
+// the independent suffix-array and text loads.
+constexpr int kLeanThreads = 128;
+
+template <int W>
+__global__ void __launch_bounds__(kLeanThreads, 8) k_search_lean(SearchArgs A0, SearchOut O, WarpScratch S, idx_t* defer,
+                                                             unsigned* defer_count) {
+    extern __shared__ uint32_t s_reads[];
+    __shared__ SearchArgs s_a;
+    if (threadIdx.x == 0) s_a = A0;
+    __syncthreads();
+    const SearchArgs& A = s_a;
+    const size_t tid = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const size_t nth = size_t(gridDim.x) * blockDim.x;
+    const int M = A.L - A.t;
+    const size_t cb = tid * 4 * size_t(S.mstride);
+    const size_t eb = tid * size_t(S.ebcap);
+    const size_t red = tid * size_t(kRedMax);
+    uint32_t probes = 0;
+    for (size_t r = tid; r < size_t(A.num_reads); r += nth) {
+        const idx_t self = idx_t(r);
+        load_read(A, self, s_reads + threadIdx.x, blockDim.x);
+        ReadView rd{s_reads + threadIdx.x, int(blockDim.x)};
+        int nb[2], nf[2];
+        int32_t ob = 0, of = 0;
+        chain_pair(A, A.fm, rd, self, PQ_BF, PQ_BB, nb, ob, probes, SlotsFast{S.c_ll, S.c_uu, S.c_meta, cb, M});
+        chain_pair(A, A.fm, rd, self, PQ_FB, PQ_FF, nf, of, probes,
+                   SlotsFast{S.c_ll, S.c_uu, S.c_meta, cb + 2 * size_t(M), M});
+        if (uint32_t(ob) > uint32_t(kRedMax) || uint32_t(of) > uint32_t(kRedMax)) {
+            const unsigned k = atomicAdd(defer_count, 1u);
+            defer[k] = self;
+            continue;
+        }
+        int ne = 0, count_b = 0, count_f = 0;
+        int status = OVF_NONE;
+        if (ob != 0)     // src/string_graph.c:824
+            status = reduce_sorted<W>(A, S, self, 0, cb, nb[0], nb[0] + nb[1], red, eb, ne, count_b, probes);
+        if (status == OVF_NONE && of != 0)     // src/string_graph.c:828
+            status = reduce_sorted<W>(A, S, self, 1, cb, nf[0], nf[0] + nf[1], red, eb, ne, count_f, probes);
+        if (status != OVF_NONE) {
+            O.status[r] = uint8_t(status);
+            const unsigned k = atomicAdd(O.ovf_count, 1u);
+            O.ovf_list[k] = self;
+            continue;
+        }
+        unsigned long long base = 0;
+        if (ne) {
+            base = atomicAdd(O.e_count, (unsigned long long)ne);
+            if (base + ne > O.e_cap) {
+                O.status[r] = OVF_POOL;
+                const unsigned k = atomicAdd(O.ovf_count, 1u);
+                O.ovf_list[k] = self;
+                continue;
+            }
+            for (int e = 0; e < ne; ++e) {
+                const uint32_t mt = S.e_meta[eb + e];
+                O.e_dest[base + e] = S.e_dest[eb + e];
+                O.e_trans[base + e] = S.e_trans[eb + e];
+                O.e_len[base + e] = uint16_t(meta_len(mt));
+                O.e_type[base + e] = uint8_t(meta_type(mt));
+            }
+        }
+        O.status[r] = OVF_NONE;
+        O.num_B[r] = uint16_t(count_b);
+        O.num_F[r] = uint16_t(count_f);
+        O.olp_B[r] = ob;
+        O.olp_F[r] = of;
+        O.edge_src[r] = base;
+    }
+    add_probes(O, probes);
+}
+
+int search_lean_blocks(int L, int M, int num_sms) {
+    const int words = (L + 15) / 16;
+    const size_t smem = size_t(words) * kLeanThreads * sizeof(uint32_t);
+    int per_sm = 0;
+    const cudaError_t e = lam_words(M) == 2
+        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search_lean<2>, kLeanThreads, smem)
+        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search_lean<kLamWords>, kLeanThreads, smem);
+    if (e != cudaSuccess ||
+        per_sm < 1)
+        per_sm = 1;
+    return per_sm * num_sms;
+}
+
+int search_fast_blocks(int L, int M, int num_sms) {
     const int words = (L + 15) / 16;
     const size_t smem = size_t(words) * 32 * kWarpsPerCta * sizeof(uint32_t);
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search_fast, 32 * kWarpsPerCta, smem) !=
-            cudaSuccess || per_sm < 1)
+    const cudaError_t e = lam_words(M) == 2
+        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search_fast<2>, 32 * kWarpsPerCta, smem)
+        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search_fast<kLamWords>, 32 * kWarpsPerCta, smem);
+    if (e != cudaSuccess || per_sm < 1)
         per_sm = 1;
     return per_sm * num_sms;
 }
@@ -1440,8 +1555,37 @@ cudaError_t search_fast(const SearchArgs& a, const SearchOut& o, int blocks, voi
     const int words = (a.L + 15) / 16;
     size_t smem = size_t(words) * 32 * kWarpsPerCta * sizeof(uint32_t);
     SearchQueue Q{};
-    { k_search_fast<<<blocks, 32 * kWarpsPerCta, smem, st>>>(a, o, S, Q); note_launch(); }
+    if (lam_words(a.L - a.t) == 2) k_search_fast<2><<<blocks, 32 * kWarpsPerCta, smem, st>>>(a, o, S, Q);
+    else k_search_fast<kLamWords><<<blocks, 32 * kWarpsPerCta, smem, st>>>(a, o, S, Q);
+    note_launch();
     return cudaGetLastError();
+}
+
+cudaError_t search_lean(const SearchArgs& a, const SearchOut& o, int lean_blocks, int fast_blocks, void* scratch,
+                        size_t scratch_bytes, int ebcap, idx_t* defer, unsigned* defer_count, cudaStream_t st) {
+    const size_t nwarps = size_t(std::max(lean_blocks * (kLeanThreads / 32), fast_blocks * kWarpsPerCta));
+    WarpScratch S;
+    if (scratch_bytes < scratch_layout(a.L - a.t, nwarps, ebcap, scratch, &S)) return cudaErrorInvalidValue;
+    const int words = (a.L + 15) / 16;
+    cudaError_t e = cudaMemsetAsync(defer_count, 0, sizeof(unsigned), st);
+    if (e != cudaSuccess) return e;
+    const size_t lsm = size_t(words) * kLeanThreads * 4, fsm = size_t(words) * 32 * kWarpsPerCta * 4;
+    if (lam_words(a.L - a.t) == 2) k_search_lean<2><<<lean_blocks, kLeanThreads, lsm, st>>>(a, o, S, defer, defer_count);
+    else k_search_lean<kLamWords><<<lean_blocks, kLeanThreads, lsm, st>>>(a, o, S, defer, defer_count);
+    note_launch();
+    // the handed-over reads, whatever their number (read on the device): the fast tier's DFS
+    SearchQueue Q{};
+    Q.read_list = defer;
+    Q.list_count = defer_count;
+    if (lam_words(a.L - a.t) == 2) k_search_fast<2><<<fast_blocks, 32 * kWarpsPerCta, fsm, st>>>(a, o, S, Q);
+    else k_search_fast<kLamWords><<<fast_blocks, 32 * kWarpsPerCta, fsm, st>>>(a, o, S, Q);
+    note_launch();
+    return cudaGetLastError();
+}
+
+size_t lean_scratch_bytes(int L, int t, int lean_blocks, int fast_blocks, int ebcap) {
+    const size_t nwarps = size_t(std::max(lean_blocks * (kLeanThreads / 32), fast_blocks * kWarpsPerCta));
+    return scratch_layout(L - t, nwarps, ebcap, nullptr, nullptr);
 }
 
 size_t queue_scratch_bytes(int L_max, int M_max, size_t nwarps, int ebcap) {
@@ -1458,7 +1602,9 @@ cudaError_t search_fast_queue(const SearchQueue& q, int L_max, int M_max, int bl
     size_t smem = size_t(words) * 32 * kWarpsPerCta * sizeof(uint32_t);
     SearchArgs a{};
     SearchOut o{};
-    { k_search_fast<<<blocks, 32 * kWarpsPerCta, smem, st>>>(a, o, S, q); note_launch(); }
+    if (lam_words(M_max) == 2) k_search_fast<2><<<blocks, 32 * kWarpsPerCta, smem, st>>>(a, o, S, q);
+    else k_search_fast<kLamWords><<<blocks, 32 * kWarpsPerCta, smem, st>>>(a, o, S, q);
+    note_launch();
     return cudaGetLastError();
 }
 
