@@ -503,6 +503,9 @@ static int search_prepare(pq_ctx* ctx, pq::SearchArgs& A, pq::SearchOut& O) {
     O.ovf_count = reinterpret_cast<unsigned int*>(ctr + 2);
     O.probes = ctr + 1;
     A.lx_misses = ctr + 3;
+    CK(ctx->defer.ensure((nr + 1) * sizeof(idx_t)));
+    A.defer = ctx->defer.as<idx_t>();
+    A.defer_count = reinterpret_cast<unsigned*>(ctr + 4);
 
     CK(cudaMemsetAsync(ctr, 0, 64, ctx->st));
     return PQ_OK;
@@ -527,7 +530,7 @@ static int search_finish(pq_ctx* ctx, pq::SearchArgs& A, pq::SearchOut& O) {
         const size_t slot_bytes = pq::wide_slot_bytes(ctx->L);
         int slots = int(std::max<size_t>(1, std::min<size_t>({size_t(ovf), size_t(1024),
                                                               (size_t(4) << 30) / slot_bytes})));
-        pq::WideScratch W;
+        pq::WideScratch W{};
         W.stack_cap = size_t(2 * ctx->L) * size_t(2 * ctx->L);
         W.frame_cap = size_t(ctx->L + 2);
         W.edge_cap = size_t(2 * 65535 + 2);
@@ -615,8 +618,8 @@ static int search_finish(pq_ctx* ctx, pq::SearchArgs& A, pq::SearchOut& O) {
 
 int pq_overlaps(pq_ctx* ctx) {
     if (!ctx) return PQ_ERR_ARG;
-    pq::SearchArgs A;
-    pq::SearchOut O;
+    pq::SearchArgs A{};
+    pq::SearchOut O{};
     int rc = search_prepare(ctx, A, O);
     if (rc != PQ_OK) return rc;
     const size_t nr = ctx->num_reads;
@@ -631,9 +634,7 @@ int pq_overlaps(pq_ctx* ctx) {
         const int fast = pq::search_fast_blocks(ctx->L, ctx->L - ctx->t, dev_sms);
         const size_t wsb = pq::lean_scratch_bytes(ctx->L, ctx->t, lean, fast, ebcap);
         CK(ctx->warp_scratch.ensure(wsb));
-        CK(ctx->defer.ensure((nr + 1) * sizeof(idx_t)));
-        CK(pq::search_lean(A, O, lean, fast, ctx->warp_scratch.p, wsb, ebcap, ctx->defer.as<idx_t>(),
-                           reinterpret_cast<unsigned*>(ctx->ctrs.as<unsigned long long>() + 4), ctx->st));
+        CK(pq::search_lean(A, O, lean, fast, ctx->warp_scratch.p, wsb, ebcap, ctx->st));
     } else if (nr) {
         // 4 warps per block, each warp 32 reads per batch; enough blocks to fill every SM
         const int ebcap = 64;
@@ -866,41 +867,66 @@ int pq_mlp_backward(const float* params, const float* x, const float* dy, int n,
 
 // ---------------------------------------------------------------------------- queued search
 
-static int queue_launch(pq_ctx* lead, const std::vector<uint32_t>& ib, const std::vector<uint32_t>& ig, int L_max,
-                        int M_max, int use_graph) {
+static uint64_t fnv1a(const void* p, size_t n) {
+    const unsigned char* c = static_cast<const unsigned char*>(p);
+    uint64_t h = 1469598103934665603ull;
+    for (size_t i = 0; i < n; ++i) h = (h ^ c[i]) * 1099511628211ull;
+    return h;
+}
+
+// One queued search over the batch descriptions already on the device (lead->q_batches, copies
+// of hb).  Lean path (every batch reduces by sorted continuations): the persistent lean kernel
+// over the queue, then the fast tier over each batch's handed-over reads.  Otherwise the fast
+// kernel over the queue.
+static int queue_launch(pq_ctx* lead, const std::vector<pq::SearchBatch>& hb, const std::vector<uint32_t>& ib,
+                        const std::vector<uint32_t>& ig, int L_max, int M_max, int use_graph) {
     pq_ctx* ctx = lead;
     int dev_sms = 152;
     cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, lead->device);
-    int per_sm = pq::search_fast_blocks(L_max, M_max, 1);
-    if (lead->q_ctas_per_sm > 0) per_sm = lead->q_ctas_per_sm;
+    bool lean = true;
+    for (const auto& b : hb) lean = lean && b.a.sorted_reduce;
     const size_t nitems = ib.size();
     const unsigned gpi = unsigned(std::max(1, lead->q_groups_per_item));
+    const int fast_max = pq::search_fast_blocks(L_max, M_max, 1);
+    const int lean_max = pq::search_lean_blocks(L_max, M_max, 1);
+    int per_sm = lean ? lean_max : fast_max;
+    if (lead->q_ctas_per_sm > 0) per_sm = std::min(lead->q_ctas_per_sm, per_sm);
     const int blocks = int(std::max<size_t>(1, std::min<size_t>(size_t(per_sm) * dev_sms, (nitems + 3) / 4)));
-    const size_t wsb = pq::queue_scratch_bytes(L_max, M_max, size_t(blocks) * 4, lead->q_ebcap);
+    const int fast_blocks = fast_max * dev_sms;
+    const size_t nwarps = size_t(lean ? std::max(blocks, fast_blocks) : blocks) * 4;
+    const size_t wsb = pq::queue_scratch_bytes(L_max, M_max, nwarps, lead->q_ebcap);
     CK(lead->warp_scratch.ensure(wsb));
     CK(lead->q_items.ensure(nitems * 8 + 64));
     CK(lead->q_next.ensure(64));
     uint32_t* d_items = lead->q_items.as<uint32_t>();
     CK(cudaMemcpyAsync(d_items, ib.data(), nitems * 4, cudaMemcpyHostToDevice, lead->st));
     CK(cudaMemcpyAsync(d_items + nitems, ig.data(), nitems * 4, cudaMemcpyHostToDevice, lead->st));
-    pq::SearchQueue Q;
+    pq::SearchQueue Q{};
     Q.batches = lead->q_batches.as<pq::SearchBatch>();
     Q.item_batch = d_items;
     Q.item_group = d_items + nitems;
     Q.count = unsigned(nitems);
     Q.groups_per_item = gpi;
     Q.next = lead->q_next.as<unsigned>();
+    auto enqueue = [&]() -> cudaError_t {
+        cudaError_t e = cudaMemsetAsync(Q.next, 0, 4, lead->st);
+        if (e != cudaSuccess) return e;
+        if (lean)
+            return pq::search_lean_queue(Q, hb.data(), int(hb.size()), L_max, M_max, blocks, fast_blocks,
+                                         lead->warp_scratch.p, wsb, lead->q_ebcap, lead->st);
+        return pq::search_fast_queue(Q, L_max, M_max, blocks, lead->warp_scratch.p, wsb, lead->q_ebcap, lead->st);
+    };
     lead->q_graph_used = 0;
     if (!use_graph) {
-        CK(cudaMemsetAsync(Q.next, 0, 4, lead->st));
         CK(cudaEventRecord(lead->evk0, lead->st));
-        CK(pq::search_fast_queue(Q, L_max, M_max, blocks, lead->warp_scratch.p, wsb, lead->q_ebcap, lead->st));
+        CK(enqueue());
         CK(cudaEventRecord(lead->evk1, lead->st));
     } else {
-        // one captured graph per launch shape: queue reset + persistent search kernel
+        // one captured graph per launch shape and batch set: queue reset + the search launches
         const std::vector<uintptr_t> key = {uintptr_t(Q.batches), uintptr_t(d_items), uintptr_t(Q.next),
                                             uintptr_t(lead->warp_scratch.p), nitems, uintptr_t(L_max),
-                                            uintptr_t(M_max), uintptr_t(blocks), gpi, uintptr_t(lead->q_ebcap)};
+                                            uintptr_t(M_max), uintptr_t(blocks), gpi, uintptr_t(lead->q_ebcap),
+                                            uintptr_t(lean), uintptr_t(fnv1a(hb.data(), hb.size() * sizeof(hb[0])))};
         if (!lead->q_exec || lead->q_key != key) {
             if (lead->q_exec) cudaGraphExecDestroy(lead->q_exec);
             if (lead->q_graph) cudaGraphDestroy(lead->q_graph);
@@ -908,14 +934,11 @@ static int queue_launch(pq_ctx* lead, const std::vector<uint32_t>& ib, const std
             lead->q_graph = nullptr;
             CK(cudaStreamSynchronize(lead->st));
             CK(cudaStreamBeginCapture(lead->st, cudaStreamCaptureModeThreadLocal));
-            cudaError_t e1 = cudaMemsetAsync(Q.next, 0, 4, lead->st);
-            cudaError_t e2 = pq::search_fast_queue(Q, L_max, M_max, blocks, lead->warp_scratch.p, wsb, lead->q_ebcap,
-                                                   lead->st);
+            const cudaError_t e1 = enqueue();
             cudaGraph_t g = nullptr;
-            cudaError_t e3 = cudaStreamEndCapture(lead->st, &g);
+            const cudaError_t e2 = cudaStreamEndCapture(lead->st, &g);
             CK(e1);
             CK(e2);
-            CK(e3);
             lead->q_graph = g;
             CK(cudaGraphInstantiate(&lead->q_exec, g, 0));
             lead->q_key = key;
@@ -974,7 +997,7 @@ int pq_overlaps_batched(pq_ctx** ctxs, int count, int flags) {
                        lead->st));
     for (int b = 0; b < count; ++b) CK(cudaEventRecord(ctxs[b]->ev0, lead->st));
     if (!ib.empty()) {
-        const int rc = queue_launch(lead, ib, ig, L_max, M_max, (flags & PQ_BATCH_GRAPH) ? 1 : 0);
+        const int rc = queue_launch(lead, hb, ib, ig, L_max, M_max, (flags & PQ_BATCH_GRAPH) ? 1 : 0);
         if (rc != PQ_OK) return rc;
     } else {
         lead->q_kernel_ms = 0;
@@ -1019,7 +1042,7 @@ int pq_autotune_batched(pq_ctx** ctxs, int count, int flags, float* best_ms) {
     int L_max = 1;
     for (int b = 0; b < count; ++b)
         if (ctxs[b]) L_max = std::max(L_max, ctxs[b]->L);
-    max_per_sm = pq::search_fast_blocks(L_max, 256, 1);
+    max_per_sm = std::max(pq::search_fast_blocks(L_max, 256, 1), pq::search_lean_blocks(L_max, 256, 1));
     float best = -1.f;
     int bc = 0, bg = 1, be = 64;
     const int edge_opts[2] = {32, 64};

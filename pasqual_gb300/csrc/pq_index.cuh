@@ -46,6 +46,8 @@ struct SearchArgs {
                                 // 2: the same with learned windows (needs fm[].lx)
     unsigned long long* lx_misses;  // learned windows that missed (those chains walk)
     int sorted_reduce;          // 1: edges from sorted continuations (L - t <= 256)
+    idx_t* defer;               // lean tier: reads handed to the fast tier ...
+    unsigned* defer_count;      //   ... and their number (zero before the search)
 };
 
 // Global scratch of the fast kernel, per warp of 32 reads: level-0 candidates (4 kinds x (L - t)
@@ -102,7 +104,12 @@ cudaError_t search_fast(const SearchArgs& a, const SearchOut& o, int blocks, voi
 int search_lean_blocks(int L, int M, int num_sms);
 size_t lean_scratch_bytes(int L, int t, int lean_blocks, int fast_blocks, int ebcap);
 cudaError_t search_lean(const SearchArgs& a, const SearchOut& o, int lean_blocks, int fast_blocks, void* scratch,
-                        size_t scratch_bytes, int ebcap, idx_t* defer, unsigned* defer_count, cudaStream_t st);
+                        size_t scratch_bytes, int ebcap, cudaStream_t st);
+// One persistent lean launch over a queue of batches, then the fast tier over each batch's
+// handed-over reads (host_batches: the same descriptions the queue holds).
+cudaError_t search_lean_queue(const SearchQueue& q, const SearchBatch* host_batches, int nbatch, int L_max, int M_max,
+                              int lean_blocks, int fast_blocks, void* scratch, size_t scratch_bytes, int ebcap,
+                              cudaStream_t st);
 // One persistent launch over a queue of batches (L_max, M_max: the largest L and L - t).
 size_t queue_scratch_bytes(int L_max, int M_max, size_t nwarps, int ebcap);
 cudaError_t search_fast_queue(const SearchQueue& q, int L_max, int M_max, int blocks, void* scratch,

@@ -1411,71 +1411,107 @@ __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A0, SearchOut
 constexpr int kLeanThreads = 128;
 
 template <int W>
-__global__ void __launch_bounds__(kLeanThreads, 8) k_search_lean(SearchArgs A0, SearchOut O, WarpScratch S, idx_t* defer,
-                                                             unsigned* defer_count) {
+__global__ void __launch_bounds__(kLeanThreads, 8) k_search_lean(SearchArgs A0, SearchOut O0, WarpScratch S,
+                                                                SearchQueue Q) {
     extern __shared__ uint32_t s_reads[];
-    __shared__ SearchArgs s_a;
-    if (threadIdx.x == 0) s_a = A0;
-    __syncthreads();
-    const SearchArgs& A = s_a;
-    const size_t tid = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    const size_t nth = size_t(gridDim.x) * blockDim.x;
-    const int M = A.L - A.t;
+    __shared__ SearchBatch s_b[kLeanThreads / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const size_t gw = size_t(blockIdx.x) * (kLeanThreads / 32) + wid;
+    const size_t nw = size_t(gridDim.x) * (kLeanThreads / 32);
+    SearchBatch& B = s_b[wid];
+    const SearchArgs& A = B.a;
+    const SearchOut& O = B.o;
+    if (Q.count == 0) {
+        if (lane == 0) {
+            B.a = A0;
+            B.o = O0;
+        }
+        __syncwarp();
+    }
+    const size_t tid = gw * 32 + lane;
     const size_t cb = tid * 4 * size_t(S.mstride);
     const size_t eb = tid * size_t(S.ebcap);
     const size_t red = tid * size_t(kRedMax);
     uint32_t probes = 0;
-    for (size_t r = tid; r < size_t(A.num_reads); r += nth) {
-        const idx_t self = idx_t(r);
-        load_read(A, self, s_reads + threadIdx.x, blockDim.x);
-        ReadView rd{s_reads + threadIdx.x, int(blockDim.x)};
-        int nb[2], nf[2];
-        int32_t ob = 0, of = 0;
-        chain_pair(A, A.fm, rd, self, PQ_BF, PQ_BB, nb, ob, probes, SlotsFast{S.c_ll, S.c_uu, S.c_meta, cb, M});
-        chain_pair(A, A.fm, rd, self, PQ_FB, PQ_FF, nf, of, probes,
-                   SlotsFast{S.c_ll, S.c_uu, S.c_meta, cb + 2 * size_t(M), M});
-        if (uint32_t(ob) > uint32_t(kRedMax) || uint32_t(of) > uint32_t(kRedMax)) {
-            const unsigned k = atomicAdd(defer_count, 1u);
-            defer[k] = self;
-            continue;
+    int cur = -1;
+    for (size_t iter = 0;; ++iter) {
+        size_t group, gend;
+        if (Q.count) {
+            unsigned it = 0;
+            if (lane == 0) it = atomicAdd(Q.next, 1u);
+            it = __shfl_sync(0xffffffffu, it, 0);
+            if (it >= Q.count) break;
+            const int b = int(Q.item_batch[it]);
+            group = Q.item_group[it];
+            gend = group + Q.groups_per_item;
+            if (b != cur) {
+                if (cur >= 0) add_probes(O, probes);
+                probes = 0;
+                __syncwarp();
+                load_batch(B, Q.batches + b, lane);
+                cur = b;
+            }
+        } else {
+            group = gw + iter * nw;
+            gend = group + 1;
+            if (group * 32 >= size_t(A.num_reads)) break;
         }
-        int ne = 0, count_b = 0, count_f = 0;
-        int status = OVF_NONE;
-        if (ob != 0)     // src/string_graph.c:824
-            status = reduce_sorted<W>(A, S, self, 0, cb, nb[0], nb[0] + nb[1], red, eb, ne, count_b, probes);
-        if (status == OVF_NONE && of != 0)     // src/string_graph.c:828
-            status = reduce_sorted<W>(A, S, self, 1, cb, nf[0], nf[0] + nf[1], red, eb, ne, count_f, probes);
-        if (status != OVF_NONE) {
-            O.status[r] = uint8_t(status);
-            const unsigned k = atomicAdd(O.ovf_count, 1u);
-            O.ovf_list[k] = self;
-            continue;
-        }
-        unsigned long long base = 0;
-        if (ne) {
-            base = atomicAdd(O.e_count, (unsigned long long)ne);
-            if (base + ne > O.e_cap) {
-                O.status[r] = OVF_POOL;
+        const int M = A.L - A.t;
+        for (; group < gend && group * 32 < size_t(A.num_reads); ++group) {
+            const size_t r = group * 32 + lane;
+            if (r >= size_t(A.num_reads)) continue;
+            const idx_t self = idx_t(r);
+            load_read(A, self, s_reads + threadIdx.x, blockDim.x);
+            ReadView rd{s_reads + threadIdx.x, int(blockDim.x)};
+            int nb[2], nf[2];
+            int32_t ob = 0, of = 0;
+            chain_pair(A, A.fm, rd, self, PQ_BF, PQ_BB, nb, ob, probes, SlotsFast{S.c_ll, S.c_uu, S.c_meta, cb, M});
+            chain_pair(A, A.fm, rd, self, PQ_FB, PQ_FF, nf, of, probes,
+                       SlotsFast{S.c_ll, S.c_uu, S.c_meta, cb + 2 * size_t(M), M});
+            if (uint32_t(ob) > uint32_t(kRedMax) || uint32_t(of) > uint32_t(kRedMax)) {
+                const unsigned k = atomicAdd(A.defer_count, 1u);
+                A.defer[k] = self;
+                continue;
+            }
+            int ne = 0, count_b = 0, count_f = 0;
+            int status = OVF_NONE;
+            if (ob != 0)     // src/string_graph.c:824
+                status = reduce_sorted<W>(A, S, self, 0, cb, nb[0], nb[0] + nb[1], red, eb, ne, count_b, probes);
+            if (status == OVF_NONE && of != 0)     // src/string_graph.c:828
+                status = reduce_sorted<W>(A, S, self, 1, cb, nf[0], nf[0] + nf[1], red, eb, ne, count_f, probes);
+            if (status != OVF_NONE) {
+                O.status[r] = uint8_t(status);
                 const unsigned k = atomicAdd(O.ovf_count, 1u);
                 O.ovf_list[k] = self;
                 continue;
             }
-            for (int e = 0; e < ne; ++e) {
-                const uint32_t mt = S.e_meta[eb + e];
-                O.e_dest[base + e] = S.e_dest[eb + e];
-                O.e_trans[base + e] = S.e_trans[eb + e];
-                O.e_len[base + e] = uint16_t(meta_len(mt));
-                O.e_type[base + e] = uint8_t(meta_type(mt));
+            unsigned long long base = 0;
+            if (ne) {
+                base = atomicAdd(O.e_count, (unsigned long long)ne);
+                if (base + ne > O.e_cap) {
+                    O.status[r] = OVF_POOL;
+                    const unsigned k = atomicAdd(O.ovf_count, 1u);
+                    O.ovf_list[k] = self;
+                    continue;
+                }
+                for (int e = 0; e < ne; ++e) {
+                    const uint32_t mt = S.e_meta[eb + e];
+                    O.e_dest[base + e] = S.e_dest[eb + e];
+                    O.e_trans[base + e] = S.e_trans[eb + e];
+                    O.e_len[base + e] = uint16_t(meta_len(mt));
+                    O.e_type[base + e] = uint8_t(meta_type(mt));
+                }
             }
+            O.status[r] = OVF_NONE;
+            O.num_B[r] = uint16_t(count_b);
+            O.num_F[r] = uint16_t(count_f);
+            O.olp_B[r] = ob;
+            O.olp_F[r] = of;
+            O.edge_src[r] = base;
         }
-        O.status[r] = OVF_NONE;
-        O.num_B[r] = uint16_t(count_b);
-        O.num_F[r] = uint16_t(count_f);
-        O.olp_B[r] = ob;
-        O.olp_F[r] = of;
-        O.edge_src[r] = base;
+        __syncwarp();
     }
-    add_probes(O, probes);
+    if (Q.count == 0 || cur >= 0) add_probes(O, probes);
 }
 
 int search_lean_blocks(int L, int M, int num_sms) {
@@ -1515,7 +1551,7 @@ static size_t scratch_layout(int M_max, size_t nwarps, int ebcap, void* base, Wa
         used += (bytes + 255) & ~size_t(255);
         return q;
     };
-    WarpScratch T;
+    WarpScratch T{};
     T.c_ll = reinterpret_cast<idx_t*>(take(cand * sizeof(idx_t)));
     T.c_uu = reinterpret_cast<idx_t*>(take(cand * sizeof(idx_t)));
     T.c_meta = reinterpret_cast<uint32_t*>(take(cand * 4));
@@ -1562,24 +1598,53 @@ cudaError_t search_fast(const SearchArgs& a, const SearchOut& o, int blocks, voi
 }
 
 cudaError_t search_lean(const SearchArgs& a, const SearchOut& o, int lean_blocks, int fast_blocks, void* scratch,
-                        size_t scratch_bytes, int ebcap, idx_t* defer, unsigned* defer_count, cudaStream_t st) {
+                        size_t scratch_bytes, int ebcap, cudaStream_t st) {
     const size_t nwarps = size_t(std::max(lean_blocks * (kLeanThreads / 32), fast_blocks * kWarpsPerCta));
     WarpScratch S;
     if (scratch_bytes < scratch_layout(a.L - a.t, nwarps, ebcap, scratch, &S)) return cudaErrorInvalidValue;
     const int words = (a.L + 15) / 16;
-    cudaError_t e = cudaMemsetAsync(defer_count, 0, sizeof(unsigned), st);
+    cudaError_t e = cudaMemsetAsync(a.defer_count, 0, sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
     const size_t lsm = size_t(words) * kLeanThreads * 4, fsm = size_t(words) * 32 * kWarpsPerCta * 4;
-    if (lam_words(a.L - a.t) == 2) k_search_lean<2><<<lean_blocks, kLeanThreads, lsm, st>>>(a, o, S, defer, defer_count);
-    else k_search_lean<kLamWords><<<lean_blocks, kLeanThreads, lsm, st>>>(a, o, S, defer, defer_count);
+    SearchQueue none{};
+    if (lam_words(a.L - a.t) == 2) k_search_lean<2><<<lean_blocks, kLeanThreads, lsm, st>>>(a, o, S, none);
+    else k_search_lean<kLamWords><<<lean_blocks, kLeanThreads, lsm, st>>>(a, o, S, none);
     note_launch();
     // the handed-over reads, whatever their number (read on the device): the fast tier's DFS
     SearchQueue Q{};
-    Q.read_list = defer;
-    Q.list_count = defer_count;
+    Q.read_list = a.defer;
+    Q.list_count = a.defer_count;
     if (lam_words(a.L - a.t) == 2) k_search_fast<2><<<fast_blocks, 32 * kWarpsPerCta, fsm, st>>>(a, o, S, Q);
     else k_search_fast<kLamWords><<<fast_blocks, 32 * kWarpsPerCta, fsm, st>>>(a, o, S, Q);
     note_launch();
+    return cudaGetLastError();
+}
+
+// Queued lean search: one persistent lean launch over the queue, then the fast tier over each
+// batch's handed-over reads (one launch per batch, counts read on the device; no host sync).
+cudaError_t search_lean_queue(const SearchQueue& q, const SearchBatch* host_batches, int nbatch, int L_max, int M_max,
+                              int lean_blocks, int fast_blocks, void* scratch, size_t scratch_bytes, int ebcap,
+                              cudaStream_t st) {
+    const size_t nwarps = size_t(std::max(lean_blocks * (kLeanThreads / 32), fast_blocks * kWarpsPerCta));
+    WarpScratch S;
+    if (scratch_bytes < scratch_layout(M_max, nwarps, ebcap, scratch, &S)) return cudaErrorInvalidValue;
+    const int words = (L_max + 15) / 16;
+    const size_t lsm = size_t(words) * kLeanThreads * 4, fsm = size_t(words) * 32 * kWarpsPerCta * 4;
+    const bool two = lam_words(M_max) == 2;
+    SearchArgs a0{};
+    SearchOut o0{};
+    if (two) k_search_lean<2><<<lean_blocks, kLeanThreads, lsm, st>>>(a0, o0, S, q);
+    else k_search_lean<kLamWords><<<lean_blocks, kLeanThreads, lsm, st>>>(a0, o0, S, q);
+    note_launch();
+    for (int b = 0; b < nbatch; ++b) {
+        const SearchArgs& a = host_batches[b].a;
+        SearchQueue Q{};
+        Q.read_list = a.defer;
+        Q.list_count = a.defer_count;
+        if (two) k_search_fast<2><<<fast_blocks, 32 * kWarpsPerCta, fsm, st>>>(a, host_batches[b].o, S, Q);
+        else k_search_fast<kLamWords><<<fast_blocks, 32 * kWarpsPerCta, fsm, st>>>(a, host_batches[b].o, S, Q);
+        note_launch();
+    }
     return cudaGetLastError();
 }
 
