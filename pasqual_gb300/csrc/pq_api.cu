@@ -875,46 +875,90 @@ static uint64_t fnv1a(const void* p, size_t n) {
 }
 
 // One queued search over the batch descriptions already on the device (lead->q_batches, copies
-// of hb).  Lean path (every batch reduces by sorted continuations): the persistent lean kernel
-// over the queue, then the fast tier over each batch's handed-over reads.  Otherwise the fast
-// kernel over the queue.
-static int queue_launch(pq_ctx* lead, const std::vector<pq::SearchBatch>& hb, const std::vector<uint32_t>& ib,
-                        const std::vector<uint32_t>& ig, int L_max, int M_max, int use_graph) {
+// of hb).  Lean path (every batch reduces by sorted continuations): the batches are split by the
+// continuation words their kernels are built for (L - t <= 64 or not); each class is one
+// persistent lean launch over its own queue, followed by the fast tier over its batches'
+// handed-over reads.  Otherwise one fast-kernel launch over the whole queue.
+static int queue_launch(pq_ctx* lead, const std::vector<pq::SearchBatch>& hb, const std::vector<int>& order,
+                        int use_graph) {
     pq_ctx* ctx = lead;
     int dev_sms = 152;
     cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, lead->device);
     bool lean = true;
     for (const auto& b : hb) lean = lean && b.a.sorted_reduce;
-    const size_t nitems = ib.size();
     const unsigned gpi = unsigned(std::max(1, lead->q_groups_per_item));
-    const int fast_max = pq::search_fast_blocks(L_max, M_max, 1);
-    const int lean_max = pq::search_lean_blocks(L_max, M_max, 1);
-    int per_sm = lean ? lean_max : fast_max;
-    if (lead->q_ctas_per_sm > 0) per_sm = std::min(lead->q_ctas_per_sm, per_sm);
-    const int blocks = int(std::max<size_t>(1, std::min<size_t>(size_t(per_sm) * dev_sms, (nitems + 3) / 4)));
-    const int fast_blocks = fast_max * dev_sms;
-    const size_t nwarps = size_t(lean ? std::max(blocks, fast_blocks) : blocks) * 4;
-    const size_t wsb = pq::queue_scratch_bytes(L_max, M_max, nwarps, lead->q_ebcap);
-    CK(lead->warp_scratch.ensure(wsb));
+    // classes of batches, each with its items (batch, first group), longest reads first
+    struct Class {
+        std::vector<int> batches;
+        std::vector<uint32_t> ib, ig;
+        int L_max = 1, M_max = 1;
+    };
+    std::vector<Class> cls(lean ? 2 : 1);
+    for (int b : order) {
+        const int M = hb[b].a.L - hb[b].a.t;
+        Class& c = cls[lean && pq::lam_words_host(M) != 2 ? 1 : 0];
+        c.batches.push_back(b);
+        c.L_max = std::max(c.L_max, hb[b].a.L);
+        c.M_max = std::max(c.M_max, M);
+        const size_t groups = (size_t(hb[b].a.num_reads) + 31) / 32;
+        for (size_t g = 0; g < groups; g += gpi) {
+            c.ib.push_back(uint32_t(b));
+            c.ig.push_back(uint32_t(g));
+        }
+    }
+    size_t nitems = 0, scratch = 0;
+    struct Plan {
+        int blocks, fast_blocks;
+        size_t wsb, first;
+    };
+    std::vector<Plan> plan(cls.size());
+    for (size_t k = 0; k < cls.size(); ++k) {
+        const Class& c = cls[k];
+        const int fast_max = pq::search_fast_blocks(c.L_max, c.M_max, 1);
+        const int lean_max = pq::search_lean_blocks(c.L_max, c.M_max, 1);
+        int per_sm = lean ? lean_max : fast_max;
+        if (lead->q_ctas_per_sm > 0) per_sm = std::min(lead->q_ctas_per_sm, per_sm);
+        Plan& p = plan[k];
+        p.blocks = int(std::max<size_t>(1, std::min<size_t>(size_t(per_sm) * dev_sms, (c.ib.size() + 3) / 4)));
+        p.fast_blocks = fast_max * dev_sms;
+        const size_t nwarps = size_t(lean ? std::max(p.blocks, p.fast_blocks) : p.blocks) * 4;
+        p.wsb = pq::queue_scratch_bytes(c.L_max, c.M_max, nwarps, lead->q_ebcap);
+        p.first = nitems;
+        nitems += c.ib.size();
+        scratch = std::max(scratch, p.wsb);
+    }
+    CK(lead->warp_scratch.ensure(scratch));
     CK(lead->q_items.ensure(nitems * 8 + 64));
     CK(lead->q_next.ensure(64));
     uint32_t* d_items = lead->q_items.as<uint32_t>();
-    CK(cudaMemcpyAsync(d_items, ib.data(), nitems * 4, cudaMemcpyHostToDevice, lead->st));
-    CK(cudaMemcpyAsync(d_items + nitems, ig.data(), nitems * 4, cudaMemcpyHostToDevice, lead->st));
-    pq::SearchQueue Q{};
-    Q.batches = lead->q_batches.as<pq::SearchBatch>();
-    Q.item_batch = d_items;
-    Q.item_group = d_items + nitems;
-    Q.count = unsigned(nitems);
-    Q.groups_per_item = gpi;
-    Q.next = lead->q_next.as<unsigned>();
+    for (size_t k = 0; k < cls.size(); ++k) {
+        if (cls[k].ib.empty()) continue;
+        CK(cudaMemcpyAsync(d_items + plan[k].first, cls[k].ib.data(), cls[k].ib.size() * 4, cudaMemcpyHostToDevice,
+                           lead->st));
+        CK(cudaMemcpyAsync(d_items + nitems + plan[k].first, cls[k].ig.data(), cls[k].ig.size() * 4,
+                           cudaMemcpyHostToDevice, lead->st));
+    }
     auto enqueue = [&]() -> cudaError_t {
-        cudaError_t e = cudaMemsetAsync(Q.next, 0, 4, lead->st);
-        if (e != cudaSuccess) return e;
-        if (lean)
-            return pq::search_lean_queue(Q, hb.data(), int(hb.size()), L_max, M_max, blocks, fast_blocks,
-                                         lead->warp_scratch.p, wsb, lead->q_ebcap, lead->st);
-        return pq::search_fast_queue(Q, L_max, M_max, blocks, lead->warp_scratch.p, wsb, lead->q_ebcap, lead->st);
+        cudaError_t e = cudaMemsetAsync(lead->q_next.p, 0, 64, lead->st);
+        for (size_t k = 0; k < cls.size() && e == cudaSuccess; ++k) {
+            const Class& c = cls[k];
+            if (c.ib.empty()) continue;
+            pq::SearchQueue Q{};
+            Q.batches = lead->q_batches.as<pq::SearchBatch>();
+            Q.item_batch = d_items + plan[k].first;
+            Q.item_group = d_items + nitems + plan[k].first;
+            Q.count = unsigned(c.ib.size());
+            Q.groups_per_item = gpi;
+            Q.next = lead->q_next.as<unsigned>() + k;
+            if (lean)
+                e = pq::search_lean_queue(Q, hb.data(), c.batches.data(), int(c.batches.size()), c.L_max, c.M_max,
+                                          plan[k].blocks, plan[k].fast_blocks, lead->warp_scratch.p, plan[k].wsb,
+                                          lead->q_ebcap, lead->st);
+            else
+                e = pq::search_fast_queue(Q, c.L_max, c.M_max, plan[k].blocks, lead->warp_scratch.p, plan[k].wsb,
+                                          lead->q_ebcap, lead->st);
+        }
+        return e;
     };
     lead->q_graph_used = 0;
     if (!use_graph) {
@@ -923,10 +967,13 @@ static int queue_launch(pq_ctx* lead, const std::vector<pq::SearchBatch>& hb, co
         CK(cudaEventRecord(lead->evk1, lead->st));
     } else {
         // one captured graph per launch shape and batch set: queue reset + the search launches
-        const std::vector<uintptr_t> key = {uintptr_t(Q.batches), uintptr_t(d_items), uintptr_t(Q.next),
-                                            uintptr_t(lead->warp_scratch.p), nitems, uintptr_t(L_max),
-                                            uintptr_t(M_max), uintptr_t(blocks), gpi, uintptr_t(lead->q_ebcap),
-                                            uintptr_t(lean), uintptr_t(fnv1a(hb.data(), hb.size() * sizeof(hb[0])))};
+        std::vector<uintptr_t> key = {uintptr_t(lead->q_batches.p), uintptr_t(d_items), uintptr_t(lead->q_next.p),
+                                      uintptr_t(lead->warp_scratch.p), nitems, gpi, uintptr_t(lead->q_ebcap),
+                                      uintptr_t(lean), uintptr_t(fnv1a(hb.data(), hb.size() * sizeof(hb[0])))};
+        for (const Plan& p : plan) {
+            key.push_back(uintptr_t(p.blocks));
+            key.push_back(p.first);
+        }
         if (!lead->q_exec || lead->q_key != key) {
             if (lead->q_exec) cudaGraphExecDestroy(lead->q_exec);
             if (lead->q_graph) cudaGraphDestroy(lead->q_graph);
@@ -978,26 +1025,19 @@ int pq_overlaps_batched(pq_ctx** ctxs, int count, int flags) {
         L_max = std::max(L_max, ctxs[b]->L);
         M_max = std::max(M_max, ctxs[b]->L - ctxs[b]->t);
     }
-    // items: longest reads first (they take longest), groups of 32 reads in order within a batch
+    // batches longest reads first (they take longest); items are built per class in queue_launch
     std::vector<int> order(count);
     for (int b = 0; b < count; ++b) order[b] = b;
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return ctxs[x]->L > ctxs[y]->L; });
-    const unsigned gpi = unsigned(std::max(1, lead->q_groups_per_item));
-    std::vector<uint32_t> ib, ig;
-    for (int b : order) {
-        const size_t groups = (size_t(ctxs[b]->num_reads) + 31) / 32;
-        for (size_t g = 0; g < groups; g += gpi) {
-            ib.push_back(uint32_t(b));
-            ig.push_back(uint32_t(g));
-        }
-    }
+    size_t total_reads = 0;
+    for (int b = 0; b < count; ++b) total_reads += ctxs[b]->num_reads;
     pq_ctx* ctx = lead;
     CK(lead->q_batches.ensure(sizeof(pq::SearchBatch) * size_t(count)));
     CK(cudaMemcpyAsync(lead->q_batches.p, hb.data(), sizeof(pq::SearchBatch) * size_t(count), cudaMemcpyHostToDevice,
                        lead->st));
     for (int b = 0; b < count; ++b) CK(cudaEventRecord(ctxs[b]->ev0, lead->st));
-    if (!ib.empty()) {
-        const int rc = queue_launch(lead, hb, ib, ig, L_max, M_max, (flags & PQ_BATCH_GRAPH) ? 1 : 0);
+    if (total_reads) {
+        const int rc = queue_launch(lead, hb, order, (flags & PQ_BATCH_GRAPH) ? 1 : 0);
         if (rc != PQ_OK) return rc;
     } else {
         lead->q_kernel_ms = 0;

@@ -105,11 +105,12 @@ int search_lean_blocks(int L, int M, int num_sms);
 size_t lean_scratch_bytes(int L, int t, int lean_blocks, int fast_blocks, int ebcap);
 cudaError_t search_lean(const SearchArgs& a, const SearchOut& o, int lean_blocks, int fast_blocks, void* scratch,
                         size_t scratch_bytes, int ebcap, cudaStream_t st);
-// One persistent lean launch over a queue of batches, then the fast tier over each batch's
-// handed-over reads (host_batches: the same descriptions the queue holds).
-cudaError_t search_lean_queue(const SearchQueue& q, const SearchBatch* host_batches, int nbatch, int L_max, int M_max,
-                              int lean_blocks, int fast_blocks, void* scratch, size_t scratch_bytes, int ebcap,
-                              cudaStream_t st);
+// One persistent lean launch over a queue of batches, then the fast tier over the handed-over
+// reads of the batches listed in `batches` (host_batches: the descriptions the queue holds).
+cudaError_t search_lean_queue(const SearchQueue& q, const SearchBatch* host_batches, const int* batches, int nbatch,
+                              int L_max, int M_max, int lean_blocks, int fast_blocks, void* scratch,
+                              size_t scratch_bytes, int ebcap, cudaStream_t st);
+constexpr int lam_words_host(int M) { return M <= 64 ? 2 : 8; }
 // One persistent launch over a queue of batches (L_max, M_max: the largest L and L - t).
 size_t queue_scratch_bytes(int L_max, int M_max, size_t nwarps, int ebcap);
 cudaError_t search_fast_queue(const SearchQueue& q, int L_max, int M_max, int blocks, void* scratch,

@@ -1620,11 +1620,12 @@ cudaError_t search_lean(const SearchArgs& a, const SearchOut& o, int lean_blocks
     return cudaGetLastError();
 }
 
-// Queued lean search: one persistent lean launch over the queue, then the fast tier over each
-// batch's handed-over reads (one launch per batch, counts read on the device; no host sync).
-cudaError_t search_lean_queue(const SearchQueue& q, const SearchBatch* host_batches, int nbatch, int L_max, int M_max,
-                              int lean_blocks, int fast_blocks, void* scratch, size_t scratch_bytes, int ebcap,
-                              cudaStream_t st) {
+// Queued lean search: one persistent lean launch over the queue (kernel built for the words of
+// M_max), then the fast tier over the handed-over reads of each batch in `batches` (one launch per
+// batch, counts read on the device; no host sync).
+cudaError_t search_lean_queue(const SearchQueue& q, const SearchBatch* host_batches, const int* batches, int nbatch,
+                              int L_max, int M_max, int lean_blocks, int fast_blocks, void* scratch,
+                              size_t scratch_bytes, int ebcap, cudaStream_t st) {
     const size_t nwarps = size_t(std::max(lean_blocks * (kLeanThreads / 32), fast_blocks * kWarpsPerCta));
     WarpScratch S;
     if (scratch_bytes < scratch_layout(M_max, nwarps, ebcap, scratch, &S)) return cudaErrorInvalidValue;
@@ -1636,13 +1637,13 @@ cudaError_t search_lean_queue(const SearchQueue& q, const SearchBatch* host_batc
     if (two) k_search_lean<2><<<lean_blocks, kLeanThreads, lsm, st>>>(a0, o0, S, q);
     else k_search_lean<kLamWords><<<lean_blocks, kLeanThreads, lsm, st>>>(a0, o0, S, q);
     note_launch();
-    for (int b = 0; b < nbatch; ++b) {
-        const SearchArgs& a = host_batches[b].a;
+    for (int i = 0; i < nbatch; ++i) {
+        const SearchBatch& hbt = host_batches[batches[i]];
         SearchQueue Q{};
-        Q.read_list = a.defer;
-        Q.list_count = a.defer_count;
-        if (two) k_search_fast<2><<<fast_blocks, 32 * kWarpsPerCta, fsm, st>>>(a, host_batches[b].o, S, Q);
-        else k_search_fast<kLamWords><<<fast_blocks, 32 * kWarpsPerCta, fsm, st>>>(a, host_batches[b].o, S, Q);
+        Q.read_list = hbt.a.defer;
+        Q.list_count = hbt.a.defer_count;
+        if (two) k_search_fast<2><<<fast_blocks, 32 * kWarpsPerCta, fsm, st>>>(hbt.a, hbt.o, S, Q);
+        else k_search_fast<kLamWords><<<fast_blocks, 32 * kWarpsPerCta, fsm, st>>>(hbt.a, hbt.o, S, Q);
         note_launch();
     }
     return cudaGetLastError();
