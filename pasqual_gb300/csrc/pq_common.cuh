@@ -63,7 +63,8 @@ struct FmView {
     const idx_t* kend;        // last row (kend < kstart when the k-mer is absent)
     const idx_t* sa;          // suffix array (for seeds found by binary search), or nullptr
     const uint64_t* pk;       // the text, 32 bases per word, first base in the top bits
-    const idx_t* isa;         // inverse suffix array (row of each text position), or nullptr
+    const idx_t* isa;         // row of the suffix at read offset o (1 <= o <= L - t) of read r at
+                              // isa[r * (L - t) + o - 1], or nullptr
     LearnedView lx;           // learned index of 16-base keys (lx.segs = 0 when absent)
     idx_t Cf[5];              // Cf[0] = C[0]; Cf[c] = C[c] + fix[c]  (LF-mapping base)
 };

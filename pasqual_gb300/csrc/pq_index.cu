@@ -229,10 +229,15 @@ __global__ void k_kmer_bounds(const uint32_t* __restrict__ code, idx_t n, idx_t*
     }
 }
 
-// inverse suffix array: isa[sa[r]] = r
-__global__ void k_isa(const idx_t* __restrict__ sa, size_t n, idx_t* __restrict__ isa) {
+// inverse suffix array restricted to read offsets 1..M: isa[read * M + offset - 1] = row of the
+// suffix at that offset (the rows the interval scan looks up: suffixes of length L - M .. L - 1)
+__global__ void k_isa(const idx_t* __restrict__ sa, size_t n, idx_t L, idx_t M, idx_t* __restrict__ isa) {
     const size_t stride = size_t(gridDim.x) * blockDim.x;
-    for (size_t r = size_t(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride) isa[sa[r]] = idx_t(r);
+    for (size_t r = size_t(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride) {
+        const idx_t p = sa[r];
+        const idx_t rd = p / L, off = p - rd * L;
+        if (off >= 1 && off <= M) isa[size_t(rd) * M + (off - 1)] = idx_t(r);
+    }
 }
 
 __global__ void k_fill_idx(idx_t* __restrict__ a, size_t m, idx_t v) {
@@ -335,8 +340,8 @@ cudaError_t read_seeds(const uint8_t* reads, idx_t num_reads, int L, int dir, in
     return cudaGetLastError();
 }
 
-cudaError_t build_isa(const idx_t* sa, size_t n, idx_t* isa, cudaStream_t st) {
-    if (n) { k_isa<<<grid_for(n, 256), 256, 0, st>>>(sa, n, isa); note_launch(); }
+cudaError_t build_isa(const idx_t* sa, size_t n, idx_t L, idx_t M, idx_t* isa, cudaStream_t st) {
+    if (n && M) { k_isa<<<grid_for(n, 256), 256, 0, st>>>(sa, n, L, M, isa); note_launch(); }
     return cudaGetLastError();
 }
 

@@ -490,7 +490,7 @@ __device__ __forceinline__ bool scan_pair(const SearchArgs& A, const FmView* fm,
                 idx_t r0, cnt;
                 slots.get(q, o, r0, cnt);
                 const int d = t + o;
-                const idx_t l0 = __ldg(fb.isa + (size_t(r0) * L + size_t(L - d)));
+                const idx_t l0 = __ldg(fb.isa + (size_t(r0) * M + size_t(L - d - 1)));
                 probes += 1;
                 slots.set(q, i++, l0, l0 + cnt - 1, pack_meta(d, kind));
                 olp = int32_t(uint32_t(olp) + uint32_t(cnt));

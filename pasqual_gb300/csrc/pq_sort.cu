@@ -446,28 +446,42 @@ struct GroupLists {
     size_t cap_small, cap_mid, cap_big;
 };
 
+// one slot of list `which` per lane with `want` set, one atomic per warp
+__device__ __forceinline__ unsigned long long warp_slot(unsigned long long* counter, bool want) {
+    const unsigned mask = __ballot_sync(0xffffffffu, want);
+    if (!mask) return 0;
+    const int lane = threadIdx.x & 31, leader = __ffs(mask) - 1;
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    return base + __popc(mask & ((1u << lane) - 1));
+}
+
 __global__ void k_group_lists(const uint64_t* __restrict__ key, size_t n, GroupLists G) {
     const size_t stride = size_t(gridDim.x) * blockDim.x;
-    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const uint64_t k = key[i];
-        if ((k & 63) != uint64_t(kHead)) continue;            // suffix ends within the first 29 bases
-        if (i > 0 && key[i - 1] == k) continue;               // not the first of its group
-        size_t e = i + 1;
-        while (e < n && key[e] == k) ++e;
-        const size_t m = e - i;
-        if (m < 2) continue;
-        if (m <= 32) {
-            unsigned long long s = atomicAdd(&G.counts[0], 1ull);
-            if (s < G.cap_small) G.small[s] = (uint64_t(i) << 24) | m;
-        } else if (m <= size_t(kGroupCta)) {
-            unsigned long long s = atomicAdd(&G.counts[1], 1ull);
-            if (s < G.cap_mid) G.mid[s] = (uint64_t(i) << 24) | m;
-        } else {
-            unsigned long long s = atomicAdd(&G.counts[2], 1ull);
-            if (s < G.cap_big) {
-                G.big[2 * s] = i;
-                G.big[2 * s + 1] = m;
+    const size_t first = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const size_t rounds = (n + stride - 1) / stride;          // same trip count for the whole warp
+    for (size_t it = 0; it < rounds; ++it) {
+        const size_t i = first + it * stride;
+        size_t m = 0;
+        if (i < n) {
+            const uint64_t k = key[i];
+            // first of its group, suffix longer than the key's 29 bases
+            if ((k & 63) == uint64_t(kHead) && (i == 0 || key[i - 1] != k)) {
+                size_t e = i + 1;
+                while (e < n && key[e] == k) ++e;
+                m = e - i;
             }
+        }
+        const bool small = m >= 2 && m <= 32, mid = m > 32 && m <= size_t(kGroupCta), big = m > size_t(kGroupCta);
+        const unsigned long long ss = warp_slot(&G.counts[0], small);
+        const unsigned long long sm = warp_slot(&G.counts[1], mid);
+        const unsigned long long sb = warp_slot(&G.counts[2], big);
+        if (small && ss < G.cap_small) G.small[ss] = (uint64_t(i) << 24) | m;
+        if (mid && sm < G.cap_mid) G.mid[sm] = (uint64_t(i) << 24) | m;
+        if (big && sb < G.cap_big) {
+            G.big[2 * sb] = i;
+            G.big[2 * sb + 1] = m;
         }
     }
 }
@@ -497,48 +511,74 @@ __device__ __forceinline__ bool tuple_less(const uint64_t a[W], uint64_t alen, u
     return apos < bpos;
 }
 
+// Groups of 2..32 suffixes, several per warp: a warp takes 8 list entries at a time and packs
+// consecutive ones into its 32 lanes while they fit; one 32-lane bitonic network on
+// (segment, remaining bases, length, position) then sorts every packed group in place (each
+// segment keeps its lanes, since segments are numbered in lane order).
 template <int W>
 __global__ void k_refine_warp(const unsigned long long* __restrict__ list, const unsigned long long* __restrict__ cnt,
                               const uint64_t* __restrict__ pk, idx_t L, idx_t* __restrict__ val) {
+    constexpr int kChunk = 8;
     const int lane = threadIdx.x & 31;
     const size_t warp = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const size_t nwarps = (size_t(gridDim.x) * blockDim.x) >> 5;
     const size_t groups = *cnt;
-    for (size_t g = warp; g < groups; g += nwarps) {
-        const unsigned long long e = list[g];
-        const size_t start = size_t(e >> 24);
-        const int m = int(e & 0xffffff);
-        uint64_t w[W], len, pos;
-        if (lane < m) {
-            pos = uint64_t(val[start + lane]);
-            len = uint64_t(L - idx_t(pos % L));
-            suffix_words<W>(pk, size_t(pos), int(len), w);
-        } else {
-            #pragma unroll
-            for (int j = 0; j < W; ++j) w[j] = ~uint64_t(0);
-            len = ~uint64_t(0);
-            pos = ~uint64_t(0);
-        }
-        #pragma unroll
-        for (int k = 2; k <= 32; k <<= 1) {
-            #pragma unroll
-            for (int j = k >> 1; j > 0; j >>= 1) {
-                uint64_t ow[W];
+    for (size_t c0 = warp * kChunk; c0 < groups; c0 += nwarps * kChunk) {
+        const unsigned long long mine = (lane < kChunk && c0 + lane < groups) ? list[c0 + lane] : 0ull;
+        int next = 0;
+        while (next < kChunk) {
+            // consecutive entries next .. next + taken - 1 fit in 32 lanes
+            int taken = 0, total = 0, seg = 255, off = 0;
+            size_t start = 0;
+            for (int e = next; e < kChunk; ++e) {
+                const unsigned long long x = __shfl_sync(0xffffffffu, mine, e);
+                const int m = int(x & 0xffffff);
+                if (m == 0 || total + m > 32) break;
+                if (lane >= total && lane < total + m) {
+                    seg = e - next;
+                    off = lane - total;
+                    start = size_t(x >> 24);
+                }
+                total += m;
+                ++taken;
+            }
+            if (taken == 0) break;
+            uint64_t w[W], len, pos;
+            if (lane < total) {
+                pos = uint64_t(val[start + off]);
+                len = uint64_t(L - idx_t(pos % L));
+                suffix_words<W>(pk, size_t(pos), int(len), w);
+            } else {
                 #pragma unroll
-                for (int q = 0; q < W; ++q) ow[q] = __shfl_xor_sync(0xffffffffu, w[q], j);
-                const uint64_t olen = __shfl_xor_sync(0xffffffffu, len, j);
-                const uint64_t opos = __shfl_xor_sync(0xffffffffu, pos, j);
-                const bool keep_min = ((lane & j) == 0) == ((lane & k) == 0);
-                const bool other_less = tuple_less<W>(ow, olen, opos, w, len, pos);
-                if (keep_min == other_less) {
+                for (int j = 0; j < W; ++j) w[j] = ~uint64_t(0);
+                len = ~uint64_t(0);
+                pos = ~uint64_t(0);
+            }
+            int sg = seg;
+            #pragma unroll
+            for (int k = 2; k <= 32; k <<= 1) {
+                #pragma unroll
+                for (int j = k >> 1; j > 0; j >>= 1) {
+                    uint64_t ow[W];
                     #pragma unroll
-                    for (int q = 0; q < W; ++q) w[q] = ow[q];
-                    len = olen;
-                    pos = opos;
+                    for (int q = 0; q < W; ++q) ow[q] = __shfl_xor_sync(0xffffffffu, w[q], j);
+                    const uint64_t olen = __shfl_xor_sync(0xffffffffu, len, j);
+                    const uint64_t opos = __shfl_xor_sync(0xffffffffu, pos, j);
+                    const int osg = __shfl_xor_sync(0xffffffffu, sg, j);
+                    const bool keep_min = ((lane & j) == 0) == ((lane & k) == 0);
+                    const bool other_less = osg != sg ? osg < sg : tuple_less<W>(ow, olen, opos, w, len, pos);
+                    if (keep_min == other_less) {
+                        #pragma unroll
+                        for (int q = 0; q < W; ++q) w[q] = ow[q];
+                        len = olen;
+                        pos = opos;
+                        sg = osg;
+                    }
                 }
             }
+            if (lane < total) val[start + off] = idx_t(pos);
+            next += taken;
         }
-        if (lane < m) val[start + lane] = idx_t(pos);
     }
 }
 
@@ -642,7 +682,7 @@ static int refine_groups_w(const GroupLists& G, unsigned long long n_small, unsi
                            const std::vector<unsigned long long>& big, const uint64_t* pk, idx_t L, idx_t* val,
                            uint64_t* cols, size_t cols_cap, cudaStream_t st) {
     if (n_small) {
-        unsigned g = unsigned(std::min<unsigned long long>((n_small + 7) / 8, 152ull * 64));
+        unsigned g = unsigned(std::min<unsigned long long>((n_small + 63) / 64, 152ull * 64));
         { k_refine_warp<W><<<g, 256, 0, st>>>(G.small, G.counts + 0, pk, L, val); note_launch(); }
     }
     if (n_mid) {
