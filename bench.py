@@ -79,7 +79,7 @@ def measured_peak_hbm():
 
 def profile_figure(key: str):
     """A figure recorded in the committed ncu summary of the search kernel ("key = value")."""
-    p = os.path.join(ROOT, "profiles", "k_search_fast.md")
+    p = os.path.join(ROOT, "profiles", "k_search_lean.md")
     try:
         txt = open(p).read()
     except OSError:
@@ -409,7 +409,7 @@ def run_ours(args):
                  "ms_fw_plus_bw": sort_ms_med},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
-                     "kernel": "k_search_fast",
+                     "kernel": "k_search_lean (+ k_search_fast over handed-over reads)",
                      "algorithmic_bytes_per_launch": alg_bytes,
                      "reference_probes_per_read": oracle_ppr,
                      "probes_per_read": probes / max(nr, 1), "kernel_ms": kms,

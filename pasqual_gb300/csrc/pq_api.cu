@@ -79,6 +79,7 @@ struct pq_ctx {
     bool sa_ok[2] = {false, false}, fm_ok[2] = {false, false};
     int fm_k[2] = {0, 0};
     DevBuf ktmp, sort_tmp, counts;
+    const uint64_t* sorted_keys[2] = {nullptr, nullptr};   // the last sort's keys, inside sort_tmp
 
     // learned index per direction (pq_learned.cu)
     DevBuf lx_bnd[2], lx_base[2], lx_par[2], lx_err[2], lx_err_root[2], lx_segof[2], lx_tmp;
@@ -272,8 +273,9 @@ int pq_sort(pq_ctx* ctx, int dir) {
     size_t tmp_bytes = pq::suffix_sort_tmp_bytes(n);
     CK(ctx->sort_tmp.ensure(tmp_bytes));
     CK(cudaEventRecord(ctx->ev0, ctx->st));
+    ctx->sorted_keys[0] = ctx->sorted_keys[1] = nullptr;     // the scratch is about to be reused
     int rc = pq::suffix_sort(ctx->reads.as<uint8_t>(), ctx->num_reads, ctx->L, dir, ctx->sa[dir].as<idx_t>(),
-                             ctx->sort_tmp.p, tmp_bytes, ctx->st);
+                             ctx->sort_tmp.p, tmp_bytes, ctx->st, &ctx->sorted_keys[dir]);
     if (rc != 0) return fail(ctx, PQ_ERR_CUDA, std::string("suffix sort failed: ") + cudaGetErrorString(cudaGetLastError()));
     CK(cudaEventRecord(ctx->ev1, ctx->st));
     CK(cudaEventSynchronize(ctx->ev1));
@@ -294,6 +296,7 @@ int pq_set_sa(pq_ctx* ctx, int dir, const pq_idx* sa, int from_device) {
         CK(cudaMemcpyAsync(ctx->sa[dir].p, sa, n * sizeof(idx_t),
                            from_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
+    ctx->sorted_keys[dir] = nullptr;
     ctx->sa_ok[dir] = true;
     ctx->fm_ok[dir] = false;
     ctx->graph_ok = false;
@@ -338,7 +341,7 @@ int pq_build_fm(pq_ctx* ctx, int dir) {
     const size_t nk = size_t(1) << (2 * k);
     CK(ctx->kstart[dir].ensure(nk * sizeof(idx_t)));
     CK(ctx->kend[dir].ensure(nk * sizeof(idx_t)));
-    CK(ctx->ktmp.ensure(n * sizeof(uint32_t) + 64));
+    if (!ctx->sorted_keys[dir]) CK(ctx->ktmp.ensure(n * sizeof(uint32_t) + 64));
     CK(ctx->pk[dir].ensure((n / 32 + 4) * sizeof(uint64_t)));
     const size_t isa_n = size_t(ctx->num_reads) * size_t(ctx->L - ctx->t);
     CK(ctx->isa[dir].ensure(isa_n * sizeof(idx_t) + 64));
@@ -347,7 +350,7 @@ int pq_build_fm(pq_ctx* ctx, int dir) {
                      ctx->blk[dir].as<OccBlock>(), ctx->sb[dir].as<idx_t>(), ctx->ri[dir].as<idx_t>(), ctx->st));
     CK(pq::build_kmer_table(ctx->sa[dir].as<idx_t>(), ctx->reads.as<uint8_t>(), ctx->num_reads, idx_t(ctx->L), dir,
                             k, ctx->ktmp.as<uint32_t>(), ctx->kstart[dir].as<idx_t>(), ctx->kend[dir].as<idx_t>(),
-                            ctx->st));
+                            ctx->st, ctx->sorted_keys[dir]));
     CK(pq::pack_text(ctx->reads.as<uint8_t>(), n, idx_t(ctx->L), dir, ctx->pk[dir].as<uint64_t>(), ctx->st));
     CK(pq::build_isa(ctx->sa[dir].as<idx_t>(), n, idx_t(ctx->L), idx_t(ctx->L - ctx->t), ctx->isa[dir].as<idx_t>(),
                      ctx->st));
@@ -375,6 +378,7 @@ int pq_build_index(pq_ctx* ctx) {
     ctx->ms_sort = s;
     ctx->ms_fm = f;
     // the sort and k-mer working memory is not needed by the search: give it back
+    ctx->sorted_keys[0] = ctx->sorted_keys[1] = nullptr;
     ctx->sort_tmp.release();
     ctx->ktmp.release();
     return PQ_OK;

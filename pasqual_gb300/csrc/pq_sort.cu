@@ -457,33 +457,63 @@ __device__ __forceinline__ unsigned long long warp_slot(unsigned long long* coun
     return base + __popc(mask & ((1u << lane) - 1));
 }
 
-__global__ void k_group_lists(const uint64_t* __restrict__ key, size_t n, GroupLists G) {
-    const size_t stride = size_t(gridDim.x) * blockDim.x;
-    const size_t first = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    const size_t rounds = (n + stride - 1) / stride;          // same trip count for the whole warp
-    for (size_t it = 0; it < rounds; ++it) {
-        const size_t i = first + it * stride;
-        size_t m = 0;
-        if (i < n) {
-            const uint64_t k = key[i];
-            // first of its group, suffix longer than the key's 29 bases
-            if ((k & 63) == uint64_t(kHead) && (i == 0 || key[i - 1] != k)) {
-                size_t e = i + 1;
-                while (e < n && key[e] == k) ++e;
-                m = e - i;
+// One CTA per tile of 4096 sorted keys: group heads are marked in a shared bit mask, each head's
+// group ends at the next marked bit (read from the mask; only a group running past the tile end is
+// followed in global memory), and the groups longer than their 29-base key are listed by size.
+constexpr int kGlTile = 4096;
+
+__global__ void __launch_bounds__(256) k_group_lists(const uint64_t* __restrict__ key, size_t n, GroupLists G) {
+    __shared__ uint32_t hm[kGlTile / 32 + 1];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (size_t t0 = size_t(blockIdx.x) * kGlTile; t0 < n; t0 += size_t(gridDim.x) * kGlTile) {
+        for (int j = threadIdx.x; j < kGlTile; j += 256) {
+            const size_t i = t0 + j;
+            const bool head = i < n && (i == 0 || key[i] != key[i - 1]);
+            const uint32_t b = __ballot_sync(0xffffffffu, head);
+            if (lane == 0) hm[j >> 5] = b;
+        }
+        if (threadIdx.x == 0) hm[kGlTile / 32] = 1u;       // sentinel: the tile end
+        __syncthreads();
+        for (int j = threadIdx.x; j < kGlTile; j += 256) {
+            const size_t i = t0 + j;
+            size_t m = 0;
+            if ((hm[j >> 5] >> (j & 31)) & 1u) {
+                const uint64_t k = key[i];
+                if ((k & 63) == uint64_t(kHead)) {     // suffix longer than its 29-base key
+                    // next head after j inside the tile
+                    int w;
+                    uint32_t bits;
+                    if (j + 1 < kGlTile) {
+                        w = (j + 1) >> 5;
+                        bits = hm[w] & (~0u << ((j + 1) & 31));
+                    } else {
+                        w = kGlTile / 32;
+                        bits = hm[w];
+                    }
+                    while (!bits) bits = hm[++w];           // ends at the sentinel word at the latest
+                    size_t e = t0 + size_t(32 * w + __ffs(bits) - 1);
+                    if (32 * w + __ffs(bits) - 1 >= kGlTile) {   // runs past the tile
+                        e = t0 + kGlTile;
+                        while (e < n && key[e] == k) ++e;
+                    }
+                    if (e > n) e = n;
+                    m = e - i;
+                }
+            }
+            const bool small = m >= 2 && m <= 32, mid = m > 32 && m <= size_t(kGroupCta), big = m > size_t(kGroupCta);
+            const unsigned long long ss = warp_slot(&G.counts[0], small);
+            const unsigned long long sm = warp_slot(&G.counts[1], mid);
+            const unsigned long long sb = warp_slot(&G.counts[2], big);
+            if (small && ss < G.cap_small) G.small[ss] = (uint64_t(i) << 24) | m;
+            if (mid && sm < G.cap_mid) G.mid[sm] = (uint64_t(i) << 24) | m;
+            if (big && sb < G.cap_big) {
+                G.big[2 * sb] = i;
+                G.big[2 * sb + 1] = m;
             }
         }
-        const bool small = m >= 2 && m <= 32, mid = m > 32 && m <= size_t(kGroupCta), big = m > size_t(kGroupCta);
-        const unsigned long long ss = warp_slot(&G.counts[0], small);
-        const unsigned long long sm = warp_slot(&G.counts[1], mid);
-        const unsigned long long sb = warp_slot(&G.counts[2], big);
-        if (small && ss < G.cap_small) G.small[ss] = (uint64_t(i) << 24) | m;
-        if (mid && sm < G.cap_mid) G.mid[sm] = (uint64_t(i) << 24) | m;
-        if (big && sb < G.cap_big) {
-            G.big[2 * sb] = i;
-            G.big[2 * sb + 1] = m;
-        }
+        __syncthreads();
     }
+    (void)warp;
 }
 
 // the W words of bases 29, 29+32, ... of the suffix at p (length m_len), zero past its end
@@ -735,7 +765,7 @@ static int refine_groups(const uint64_t* key, idx_t* val, size_t n, idx_t L, con
     G.big = G.mid + G.cap_mid;
     G.counts = counters;
     cudaMemsetAsync(counters, 0, 3 * sizeof(unsigned long long), st);
-    { k_group_lists<<<grid_for(n, 256), 256, 0, st>>>(key, n, G); note_launch(); }
+    { k_group_lists<<<unsigned(std::min<size_t>((n + kGlTile - 1) / kGlTile, size_t(152) * 64)), 256, 0, st>>>(key, n, G); note_launch(); }
     unsigned long long c[3];
     cudaMemcpyAsync(c, counters, sizeof c, cudaMemcpyDeviceToHost, st);
     cudaError_t e = cudaStreamSynchronize(st);
@@ -770,7 +800,8 @@ size_t suffix_sort_tmp_bytes(size_t n) {
 }
 
 int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa, void* tmp, size_t tmp_bytes,
-                cudaStream_t st) {
+                cudaStream_t st, const uint64_t** keys_out) {
+    if (keys_out) *keys_out = nullptr;
     const size_t n = size_t(num_reads) * size_t(L);
     if (n == 0) return 0;
     if (n >= (size_t(1) << 31)) return int(cudaErrorNotSupported);   // 32-bit group ranks
@@ -795,6 +826,7 @@ int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa
     if (rc) return rc;
     if (size_t(L) <= size_t(kHead)) {   // every suffix fits in its key: already in final order
         { k_copy_vals<idx_t><<<grid_for(n, 256), 256, 0, st>>>(va, n, sa); note_launch(); }
+        if (keys_out) *keys_out = ka;
         return int(cudaGetLastError());
     }
     {
@@ -803,8 +835,9 @@ int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa
         const size_t cols_cap = (al(n * sizeof(idx_t)) + al(n * sizeof(uint32_t))) / sizeof(uint64_t);
         rc = refine_groups(ka, va, n, idx_t(L), pk, kb, cols, cols_cap, tcnt, st);
         if (rc > 0) return rc;
-        if (rc == 0) {
+        if (rc == 0) {   // the refinement permutes suffixes within groups of equal keys only
             { k_copy_vals<idx_t><<<grid_for(n, 256), 256, 0, st>>>(va, n, sa); note_launch(); }
+            if (keys_out) *keys_out = ka;
             return int(cudaGetLastError());
         }
         // a group too large for the scratch (or reads longer than 285 bases): prefix doubling

@@ -7,9 +7,12 @@ namespace pq {
 size_t suffix_sort_tmp_bytes(size_t n);
 
 // Suffix array of direction dir in the canonical order (suffix string with end-of-read lowest,
-// then text position).  Returns 0 or a cudaError_t value.
+// then text position).  Returns 0 or a cudaError_t value.  When keys_out is given it receives
+// the sorted 64-bit keys (first 29 bases, then min(length, 29) in the low 6 bits) aligned with the
+// suffix array, inside tmp (valid until tmp is reused), or nullptr when the sort ended by prefix
+// doubling (the key array then holds ranks).
 int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa, void* tmp,
-                size_t tmp_bytes, cudaStream_t st);
+                size_t tmp_bytes, cudaStream_t st, const uint64_t** keys_out = nullptr);
 
 // Per-read seeds from a k-mer table (pq_index.cu).
 cudaError_t read_seeds(const uint8_t* reads, idx_t num_reads, int L, int dir, int k, const idx_t* kstart,
