@@ -23,38 +23,53 @@ __device__ __forceinline__ int text_at(const uint8_t* __restrict__ reads, idx_t 
 // cnt[] for the superblock pass.
 __global__ void k_bwt_blocks(const idx_t* __restrict__ sa, const uint8_t* __restrict__ reads,
                              idx_t n, idx_t L, int dir, idx_t nblk, OccBlock* __restrict__ blk) {
+    constexpr int G = 4;                    // blocks per warp and round: 8 independent rows per lane
     const int lane = threadIdx.x & 31;
     const size_t warp = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const size_t nwarps = (size_t(gridDim.x) * blockDim.x) >> 5;
-    for (size_t b = warp; b < nblk; b += nwarps) {
-        uint32_t lo2[2], hi2[2], dl2[2], va2[2];
+    for (size_t b0 = warp * G; b0 < nblk; b0 += nwarps * G) {
+        idx_t p[2 * G];
         #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            size_t r = b * 64 + size_t(h) * 32 + lane;
-            int sym = -1;
-            if (r < n) {
-                idx_t p = sa[r];
-                idx_t off = p % L;
-                sym = off ? text_at(reads, L, dir, p - 1) : 0;
-            }
-            int code = sym > 0 ? sym - 1 : 0;
-            lo2[h] = __ballot_sync(0xffffffffu, code & 1);
-            hi2[h] = __ballot_sync(0xffffffffu, code >> 1);
-            dl2[h] = __ballot_sync(0xffffffffu, sym == 0);
-            va2[h] = __ballot_sync(0xffffffffu, sym >= 0);
+        for (int x = 0; x < 2 * G; ++x) {
+            const size_t r = b0 * 64 + size_t(x) * 32 + lane;
+            p[x] = r < n ? sa[r] : idx_t(0);
         }
-        if (lane == 0) {
-            OccBlock ob;
-            ob.lo = uint64_t(lo2[0]) | (uint64_t(lo2[1]) << 32);
-            ob.hi = uint64_t(hi2[0]) | (uint64_t(hi2[1]) << 32);
-            ob.dol = uint64_t(dl2[0]) | (uint64_t(dl2[1]) << 32);
-            uint64_t valid = uint64_t(va2[0]) | (uint64_t(va2[1]) << 32);
-            uint64_t base = valid & ~ob.dol;
-            ob.cnt[0] = (uint16_t)__popcll(base & ~ob.hi & ~ob.lo);
-            ob.cnt[1] = (uint16_t)__popcll(base & ~ob.hi & ob.lo);
-            ob.cnt[2] = (uint16_t)__popcll(base & ob.hi & ~ob.lo);
-            ob.cnt[3] = (uint16_t)__popcll(base & ob.hi & ob.lo);
-            blk[b] = ob;
+        int sym[2 * G];
+        #pragma unroll
+        for (int x = 0; x < 2 * G; ++x) {
+            const size_t r = b0 * 64 + size_t(x) * 32 + lane;
+            sym[x] = -1;
+            if (r < n) {
+                const idx_t off = p[x] % L;
+                sym[x] = off ? text_at(reads, L, dir, p[x] - 1) : 0;
+            }
+        }
+        #pragma unroll
+        for (int g = 0; g < G; ++g) {
+            if (b0 + g >= nblk) break;
+            uint32_t lo2[2], hi2[2], dl2[2], va2[2];
+            #pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int sy = sym[2 * g + h];
+                const int code = sy > 0 ? sy - 1 : 0;
+                lo2[h] = __ballot_sync(0xffffffffu, code & 1);
+                hi2[h] = __ballot_sync(0xffffffffu, code >> 1);
+                dl2[h] = __ballot_sync(0xffffffffu, sy == 0);
+                va2[h] = __ballot_sync(0xffffffffu, sy >= 0);
+            }
+            if (lane == 0) {
+                OccBlock ob;
+                ob.lo = uint64_t(lo2[0]) | (uint64_t(lo2[1]) << 32);
+                ob.hi = uint64_t(hi2[0]) | (uint64_t(hi2[1]) << 32);
+                ob.dol = uint64_t(dl2[0]) | (uint64_t(dl2[1]) << 32);
+                const uint64_t valid = uint64_t(va2[0]) | (uint64_t(va2[1]) << 32);
+                const uint64_t base = valid & ~ob.dol;
+                ob.cnt[0] = (uint16_t)__popcll(base & ~ob.hi & ~ob.lo);
+                ob.cnt[1] = (uint16_t)__popcll(base & ~ob.hi & ob.lo);
+                ob.cnt[2] = (uint16_t)__popcll(base & ob.hi & ~ob.lo);
+                ob.cnt[3] = (uint16_t)__popcll(base & ob.hi & ob.lo);
+                blk[b0 + g] = ob;
+            }
         }
     }
 }

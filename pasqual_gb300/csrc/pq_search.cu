@@ -262,18 +262,18 @@ __device__ __forceinline__ uint64_t top_mask(int nbases) {      // 1 <= nbases <
     return nbases >= 32 ? ~uint64_t(0) : ~(~uint64_t(0) >> (2 * nbases));
 }
 
-// P = pat(t) .. pat(1) of `kind`, packed in the walked index's text order
-__device__ __forceinline__ void pack_pattern(const ReadView& rd, int L, int t, int kind,
-                                             uint64_t (&P)[kScanWords]) {
+// P = pat(t) .. pat(1) of `kind` in the walked index's text order, its first 64 bases packed (the
+// bases past t are whatever follows; every comparison masks them).  P is the read's own text in
+// the walked index at self * L + L - t for a strict kind, and the complement of the other index's
+// text there for FF and BB.
+__device__ __forceinline__ void pattern_words(const FmView* fm, int L, int t, int kind, idx_t self,
+                                              uint64_t (&P)[kScanWords]) {
+    const bool strict = kind == PQ_FB || kind == PQ_BF;
+    const uint64_t* pk = fm[strict ? walked_index(kind) : 1 - walked_index(kind)].pk;
+    const size_t pos = size_t(self) * L + size_t(L - t);
+    const uint64_t flip = strict ? 0 : ~uint64_t(0);
     #pragma unroll
-    for (int w = 0; w < kScanWords; ++w) {
-        uint64_t x = 0;
-        for (int j = 0; j < 32; ++j) {
-            const int c = 32 * w + j;
-            x = (x << 2) | uint64_t(c < t ? pattern_at(rd, L, kind, t - c) - 1 : 0);
-        }
-        P[w] = x;
-    }
+    for (int w = 0; w < kScanWords; ++w) P[w] = text_window(pk, pos + 32 * w) ^ flip;
 }
 
 // -1 / 0 / +1: the suffix at text position p (m bases to end-of-read) is below / starts with /
@@ -386,14 +386,13 @@ struct SlotsStack {    // wide tier: the slot's candidate stack
 // Candidates of both chains by interval scan; false (nothing stored) when a depth-t interval
 // holds more than kScanMax rows, and the caller walks instead.
 template <class Slots>
-__device__ __forceinline__ bool scan_pair(const SearchArgs& A, const FmView* fm, const ReadView& rd, idx_t self,
-                                          int k0, int k1, int (&n)[2], int32_t& olp, uint32_t& probes,
-                                          const Slots& slots) {
+__device__ __forceinline__ bool scan_pair(const SearchArgs& A, const FmView* fm, idx_t self, int k0, int k1,
+                                          int (&n)[2], int32_t& olp, uint32_t& probes, const Slots& slots) {
     const int L = A.L, t = A.t, k = A.seed_k, M = L - t;
     const int tb = t < 32 * kScanWords ? t : 32 * kScanWords;    // bases bisected; the rest checked per row
     uint64_t P0[kScanWords], P1[kScanWords];
-    pack_pattern(rd, L, t, k0, P0);
-    pack_pattern(rd, L, t, k1, P1);
+    pattern_words(fm, L, t, k0, self, P0);
+    pattern_words(fm, L, t, k1, self, P1);
     const FmView* f0 = fm + walked_index(k0);
     const FmView* f1 = fm + walked_index(k1);
     idx_t lo[2], hi[2], first[2], end[2];
@@ -512,13 +511,15 @@ __device__ __forceinline__ bool scan_pair(const SearchArgs& A, const FmView* fm,
 // intervals at depth t -- and everything after -- are the reference's.  With A.sa_seed the
 // candidates come from the interval scan above instead, unless a depth-t interval is too large.
 // The i-th stored candidate of kind k0 (q = 0) or k1 (q = 1) goes to slot (q, i); n[q] counts them.
-template <class Slots>
+// `need_read()` makes rd valid (the walk reads the read's bases; the scan reads the packed text).
+template <class Slots, class NeedRead>
 __device__ __forceinline__ void chain_pair(const SearchArgs& A, const FmView* fm, const ReadView& rd, idx_t self,
                                            int k0, int k1, int (&n)[2], int32_t& olp, uint32_t& probes,
-                                           const Slots& slots) {
+                                           const Slots& slots, NeedRead need_read) {
     const int L = A.L, t = A.t, k = A.seed_k;
     n[0] = n[1] = 0;
-    if (A.sa_seed && scan_pair(A, fm, rd, self, k0, k1, n, olp, probes, slots)) return;
+    if (A.sa_seed && scan_pair(A, fm, self, k0, k1, n, olp, probes, slots)) return;
+    need_read();
     idx_t l[2], u[2], ll[2], uu[2];
     bool alive[2];
     #pragma unroll
@@ -578,7 +579,7 @@ __device__ __forceinline__ int side_candidates(const SearchArgs& A, const FmView
     const int M = A.L - A.t;
     if (2 * M > cap) return OVF_STACK;
     int n[2];
-    chain_pair(A, fm, rd, self, k0, k1, n, olp, probes, SlotsStack{stk, M});
+    chain_pair(A, fm, rd, self, k0, k1, n, olp, probes, SlotsStack{stk, M}, [] {});
     for (int i = 0; i < n[1]; ++i) stk[n[0] + i] = stk[M + i];
     n_out = n[0] + n[1];
     return OVF_NONE;
@@ -1110,9 +1111,10 @@ __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A0, SearchOut
             const size_t cb = cbase_w + size_t(lane) * 4 * size_t(S.mstride);
             int nb[2], nf[2];
             int32_t ob = 0, of = 0;
-            chain_pair(A, A.fm, rd, self, PQ_BF, PQ_BB, nb, ob, probes, SlotsFast{S.c_ll, S.c_uu, S.c_meta, cb, M});
+            chain_pair(A, A.fm, rd, self, PQ_BF, PQ_BB, nb, ob, probes, SlotsFast{S.c_ll, S.c_uu, S.c_meta, cb, M},
+                       [] {});
             chain_pair(A, A.fm, rd, self, PQ_FB, PQ_FF, nf, of, probes,
-                       SlotsFast{S.c_ll, S.c_uu, S.c_meta, cb + 2 * size_t(M), M});
+                       SlotsFast{S.c_ll, S.c_uu, S.c_meta, cb + 2 * size_t(M), M}, [] {});
             s_n[wid][lane][0] = nb[0];
             s_n[wid][lane][1] = nb[1];
             s_n[wid][lane][2] = nf[0];
@@ -1461,13 +1463,18 @@ __global__ void __launch_bounds__(kLeanThreads, 8) k_search_lean(SearchArgs A0, 
             const size_t r = group * 32 + lane;
             if (r >= size_t(A.num_reads)) continue;
             const idx_t self = idx_t(r);
-            load_read(A, self, s_reads + threadIdx.x, blockDim.x);
             ReadView rd{s_reads + threadIdx.x, int(blockDim.x)};
+            bool loaded = false;      // the read's bases are loaded only if a chain walks
+            auto need_read = [&] {
+                if (!loaded) load_read(A, self, s_reads + threadIdx.x, blockDim.x);
+                loaded = true;
+            };
             int nb[2], nf[2];
             int32_t ob = 0, of = 0;
-            chain_pair(A, A.fm, rd, self, PQ_BF, PQ_BB, nb, ob, probes, SlotsFast{S.c_ll, S.c_uu, S.c_meta, cb, M});
+            chain_pair(A, A.fm, rd, self, PQ_BF, PQ_BB, nb, ob, probes, SlotsFast{S.c_ll, S.c_uu, S.c_meta, cb, M},
+                       need_read);
             chain_pair(A, A.fm, rd, self, PQ_FB, PQ_FF, nf, of, probes,
-                       SlotsFast{S.c_ll, S.c_uu, S.c_meta, cb + 2 * size_t(M), M});
+                       SlotsFast{S.c_ll, S.c_uu, S.c_meta, cb + 2 * size_t(M), M}, need_read);
             if (uint32_t(ob) > uint32_t(kRedMax) || uint32_t(of) > uint32_t(kRedMax)) {
                 const unsigned k = atomicAdd(A.defer_count, 1u);
                 A.defer[k] = self;

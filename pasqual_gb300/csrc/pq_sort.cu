@@ -446,27 +446,50 @@ struct GroupLists {
     size_t cap_small, cap_mid, cap_big;
 };
 
-// one slot of list `which` per lane with `want` set, one atomic per warp
-__device__ __forceinline__ unsigned long long warp_slot(unsigned long long* counter, bool want) {
-    const unsigned mask = __ballot_sync(0xffffffffu, want);
-    if (!mask) return 0;
-    const int lane = threadIdx.x & 31, leader = __ffs(mask) - 1;
-    unsigned long long base = 0;
-    if (lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(mask));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    return base + __popc(mask & ((1u << lane) - 1));
-}
-
 // One CTA per tile of 4096 sorted keys: group heads are marked in a shared bit mask, each head's
 // group ends at the next marked bit (read from the mask; only a group running past the tile end is
 // followed in global memory), and the groups longer than their 29-base key are listed by size.
+// List slots are taken with one atomic per list per tile, after a block-wide prefix of the counts.
 constexpr int kGlTile = 4096;
+constexpr int kGlThreads = 256;
+constexpr int kGlPer = kGlTile / kGlThreads;      // positions per thread (j = tid + 256 i)
 
-__global__ void __launch_bounds__(256) k_group_lists(const uint64_t* __restrict__ key, size_t n, GroupLists G) {
-    __shared__ uint32_t hm[kGlTile / 32 + 1];
+__device__ __forceinline__ void block_scan3(unsigned (&c)[3], unsigned (&excl)[3], unsigned (*wsum)[3],
+                                            unsigned* tot) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned x[3] = {c[0], c[1], c[2]};
+    #pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        #pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, x[q], o);
+            if (lane >= o) x[q] += y;
+        }
+    }
+    if (lane == 31) {
+        #pragma unroll
+        for (int q = 0; q < 3; ++q) wsum[warp][q] = x[q];
+    }
+    __syncthreads();
+    #pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        unsigned before = 0, all = 0;
+        for (int w = 0; w < kGlThreads / 32; ++w) {
+            before += w < warp ? wsum[w][q] : 0u;
+            all += wsum[w][q];
+        }
+        excl[q] = before + x[q] - c[q];
+        tot[q] = all;
+    }
+}
+
+__global__ void __launch_bounds__(kGlThreads) k_group_lists(const uint64_t* __restrict__ key, size_t n, GroupLists G) {
+    __shared__ uint32_t hm[kGlTile / 32 + 1];
+    __shared__ unsigned wsum[kGlThreads / 32][3];
+    __shared__ unsigned long long sbase[3];
+    const int lane = threadIdx.x & 31;
     for (size_t t0 = size_t(blockIdx.x) * kGlTile; t0 < n; t0 += size_t(gridDim.x) * kGlTile) {
-        for (int j = threadIdx.x; j < kGlTile; j += 256) {
+        for (int j = threadIdx.x; j < kGlTile; j += kGlThreads) {
             const size_t i = t0 + j;
             const bool head = i < n && (i == 0 || key[i] != key[i - 1]);
             const uint32_t b = __ballot_sync(0xffffffffu, head);
@@ -474,13 +497,16 @@ __global__ void __launch_bounds__(256) k_group_lists(const uint64_t* __restrict_
         }
         if (threadIdx.x == 0) hm[kGlTile / 32] = 1u;       // sentinel: the tile end
         __syncthreads();
-        for (int j = threadIdx.x; j < kGlTile; j += 256) {
+        uint32_t mm[kGlPer];
+        unsigned c[3] = {0, 0, 0};
+        #pragma unroll
+        for (int q = 0; q < kGlPer; ++q) {
+            const int j = threadIdx.x + kGlThreads * q;
             const size_t i = t0 + j;
             size_t m = 0;
             if ((hm[j >> 5] >> (j & 31)) & 1u) {
                 const uint64_t k = key[i];
                 if ((k & 63) == uint64_t(kHead)) {     // suffix longer than its 29-base key
-                    // next head after j inside the tile
                     int w;
                     uint32_t bits;
                     if (j + 1 < kGlTile) {
@@ -491,8 +517,9 @@ __global__ void __launch_bounds__(256) k_group_lists(const uint64_t* __restrict_
                         bits = hm[w];
                     }
                     while (!bits) bits = hm[++w];           // ends at the sentinel word at the latest
-                    size_t e = t0 + size_t(32 * w + __ffs(bits) - 1);
-                    if (32 * w + __ffs(bits) - 1 >= kGlTile) {   // runs past the tile
+                    const int nxt = 32 * w + __ffs(bits) - 1;
+                    size_t e = t0 + size_t(nxt);
+                    if (nxt >= kGlTile) {                   // runs past the tile
                         e = t0 + kGlTile;
                         while (e < n && key[e] == k) ++e;
                     }
@@ -500,20 +527,39 @@ __global__ void __launch_bounds__(256) k_group_lists(const uint64_t* __restrict_
                     m = e - i;
                 }
             }
-            const bool small = m >= 2 && m <= 32, mid = m > 32 && m <= size_t(kGroupCta), big = m > size_t(kGroupCta);
-            const unsigned long long ss = warp_slot(&G.counts[0], small);
-            const unsigned long long sm = warp_slot(&G.counts[1], mid);
-            const unsigned long long sb = warp_slot(&G.counts[2], big);
-            if (small && ss < G.cap_small) G.small[ss] = (uint64_t(i) << 24) | m;
-            if (mid && sm < G.cap_mid) G.mid[sm] = (uint64_t(i) << 24) | m;
-            if (big && sb < G.cap_big) {
-                G.big[2 * sb] = i;
-                G.big[2 * sb + 1] = m;
+            mm[q] = uint32_t(m);
+            c[0] += (m >= 2 && m <= 32) ? 1u : 0u;
+            c[1] += (m > 32 && m <= size_t(kGroupCta)) ? 1u : 0u;
+            c[2] += (m > size_t(kGroupCta)) ? 1u : 0u;
+        }
+        unsigned excl[3], tot[3];
+        block_scan3(c, excl, wsum, tot);
+        if (threadIdx.x == 0) {
+            #pragma unroll
+            for (int q = 0; q < 3; ++q) sbase[q] = tot[q] ? atomicAdd(&G.counts[q], (unsigned long long)tot[q]) : 0ull;
+        }
+        __syncthreads();
+        unsigned long long at[3] = {sbase[0] + excl[0], sbase[1] + excl[1], sbase[2] + excl[2]};
+        #pragma unroll
+        for (int q = 0; q < kGlPer; ++q) {
+            const size_t i = t0 + threadIdx.x + kGlThreads * q;
+            const size_t m = mm[q];
+            if (m >= 2 && m <= 32) {
+                if (at[0] < G.cap_small) G.small[at[0]] = (uint64_t(i) << 24) | m;
+                ++at[0];
+            } else if (m > 32 && m <= size_t(kGroupCta)) {
+                if (at[1] < G.cap_mid) G.mid[at[1]] = (uint64_t(i) << 24) | m;
+                ++at[1];
+            } else if (m > size_t(kGroupCta)) {
+                if (at[2] < G.cap_big) {
+                    G.big[2 * at[2]] = i;
+                    G.big[2 * at[2] + 1] = m;
+                }
+                ++at[2];
             }
         }
         __syncthreads();
     }
-    (void)warp;
 }
 
 // the W words of bases 29, 29+32, ... of the suffix at p (length m_len), zero past its end
