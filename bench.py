@@ -292,8 +292,11 @@ def run_ours(args):
     rd, L, t = workload_reads(args.workload, args.scale)
     nr = rd.shape[0]
     n = nr * L
+    width = 32 if n < (1 << 32) else 64          # the reference's U32/U64 split by index size
+    from pasqual_gb300 import synth
+    width = max(width, synth.WORKLOADS[args.workload].get("index", 32))
     stream = torch.cuda.Stream(device=dev)
-    P = pq.Pasqual(32, device=local, stream=stream.cuda_stream)
+    P = pq.Pasqual(width, device=local, stream=stream.cuda_stream)
 
     def barrier():
         if world > 1:
@@ -397,10 +400,10 @@ def run_ours(args):
     out = {
         "metric": METRIC, "value": nr * world / (step_ms * 1e-3), "unit": "reads/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32-index",
-        "data": "synthetic",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "int%d-index" % width, "data": "synthetic",
         "config": {"workload": args.workload, "genome_scale": args.scale, "reads": nr,
-                   "read_len": L, "t": t, "index": "U32", "suffixes_per_index": n,
+                   "read_len": L, "t": t, "index": "U%d" % width, "suffixes_per_index": n,
                    "edges": ne, "wide_tier_reads": wide, "seed_k": min(12, t),
                    "l2": "inputs larger than L2 (two FM-indexes %.2f GB + reads %.2f GB)"
                          % (2 * (n // 64 + 1) * 32 / 1e9, n / 1e9),

@@ -80,6 +80,14 @@ PQ_API int pq_get_counts (pq_ctx * ctx, pq_idx C[6], pq_idx suffix_count[4], pq_
  * by text position.  Replaces transform_to_triplet[_reverse] + initial_sort + suf_sort over the
  * five slots (src/sufsort.h:29-46, driven by src/index.c:558-585). */
 PQ_API int pq_sort (pq_ctx * ctx, int dir);
+/* Largest number of suffixes pq_sort sorts in one pass (0, the default: 2^31 - 1, the limit of its
+ * 32-bit group ranks).  Larger indexes are sorted in chunks: every suffix falls in a bucket by its
+ * first 6 bases and min(length, 6), numbered in suffix order, and runs of consecutive buckets of
+ * at most this many suffixes are sorted one after the other into their place -- the sort the
+ * reference does over its 5 first-character slots (src/index.c:558-585), at a finer grain.  A
+ * bucket larger than a chunk makes pq_sort return PQ_ERR_CAPACITY.  Same suffix array either way. */
+PQ_API int pq_set_sort_chunk (pq_ctx * ctx, uint64_t max_suffixes);
+
 /* Use a given suffix array instead of sorting (testing and external sorters). */
 PQ_API int pq_set_sa (pq_ctx * ctx, int dir, const pq_idx * sa, int from_device);
 PQ_API int pq_get_sa (pq_ctx * ctx, int dir, pq_idx * sa_host);

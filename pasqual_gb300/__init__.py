@@ -34,7 +34,8 @@ EXPORTS = ["pq_idx_bytes", "pq_create", "pq_destroy", "pq_last_error", "pq_set_r
            "pq_get_graph_sizes", "pq_get_graph", "pq_get_stage_ms", "pq_get_kernel_stats",
            "pq_suffix_sort_static", "pq_learned_build", "pq_learned_get_info", "pq_learned_export",
            "pq_learned_predict", "pq_learned_keys", "pq_mlp_forward", "pq_mlp_backward",
-           "pq_overlaps_batched", "pq_set_batch_plan", "pq_get_batch_stats", "pq_autotune_batched"]
+           "pq_overlaps_batched", "pq_set_batch_plan", "pq_get_batch_stats", "pq_autotune_batched",
+           "pq_set_sort_chunk"]
 
 
 # The reference's own entry points served by the same library (include/pasqual_gb300_dropin.h).
@@ -97,6 +98,7 @@ def load_library(width: int = 32) -> ct.CDLL:
         "pq_set_batch_plan": (c_int, [vp, c_int, c_int, c_int]),
         "pq_get_batch_stats": (c_int, [vp, vp, vp, vp, vp, vp]),
         "pq_autotune_batched": (c_int, [vp, c_int, c_int, vp]),
+        "pq_set_sort_chunk": (c_int, [vp, ct.c_uint64]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -250,6 +252,10 @@ class Pasqual:
         """0: walk from the k-mer seed; 1: depth-t interval scan (default); 2: the scan with
         learned-index windows."""
         self._ck(self.lib.pq_set_seed_mode(self.h, int(mode)), "pq_set_seed_mode")
+
+    def set_sort_chunk(self, max_suffixes: int) -> None:
+        """Sort in chunks of at most this many suffixes (0: one pass up to 2^31 - 1)."""
+        self._ck(self.lib.pq_set_sort_chunk(self.h, int(max_suffixes)), "pq_set_sort_chunk")
 
     def sort(self, direction: int) -> None:
         self._ck(self.lib.pq_sort(self.h, direction), "pq_sort")

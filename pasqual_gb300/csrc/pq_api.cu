@@ -80,6 +80,7 @@ struct pq_ctx {
     int fm_k[2] = {0, 0};
     DevBuf ktmp, sort_tmp, counts;
     const uint64_t* sorted_keys[2] = {nullptr, nullptr};   // the last sort's keys, inside sort_tmp
+    uint64_t sort_chunk = 0;                                // suffixes per sort chunk (0: automatic)
 
     // learned index per direction (pq_learned.cu)
     DevBuf lx_bnd[2], lx_base[2], lx_par[2], lx_err[2], lx_err_root[2], lx_segof[2], lx_tmp;
@@ -270,12 +271,21 @@ int pq_sort(pq_ctx* ctx, int dir) {
     cudaSetDevice(ctx->device);
     const size_t n = n_rows(ctx);
     CK(ctx->sa[dir].ensure(n * sizeof(idx_t) + 64));
-    size_t tmp_bytes = pq::suffix_sort_tmp_bytes(n);
+    // one pass below 2^31 suffixes (32-bit group ranks), else chunks of 6-base buckets
+    const size_t one_pass_max = (size_t(1) << 31) - 1;
+    const bool chunked = n > one_pass_max || (ctx->sort_chunk && n > ctx->sort_chunk);
+    const size_t cap = std::min(ctx->sort_chunk ? size_t(ctx->sort_chunk) : (size_t(1) << 30), one_pass_max);
+    size_t tmp_bytes = chunked ? pq::suffix_sort_chunked_tmp_bytes(n, cap) : pq::suffix_sort_tmp_bytes(n);
     CK(ctx->sort_tmp.ensure(tmp_bytes));
     CK(cudaEventRecord(ctx->ev0, ctx->st));
     ctx->sorted_keys[0] = ctx->sorted_keys[1] = nullptr;     // the scratch is about to be reused
-    int rc = pq::suffix_sort(ctx->reads.as<uint8_t>(), ctx->num_reads, ctx->L, dir, ctx->sa[dir].as<idx_t>(),
-                             ctx->sort_tmp.p, tmp_bytes, ctx->st, &ctx->sorted_keys[dir]);
+    int rc = chunked ? pq::suffix_sort_chunked(ctx->reads.as<uint8_t>(), ctx->num_reads, ctx->L, dir,
+                                               ctx->sa[dir].as<idx_t>(), cap, ctx->sort_tmp.p, tmp_bytes, ctx->st)
+                     : pq::suffix_sort(ctx->reads.as<uint8_t>(), ctx->num_reads, ctx->L, dir,
+                                       ctx->sa[dir].as<idx_t>(), ctx->sort_tmp.p, tmp_bytes, ctx->st,
+                                       &ctx->sorted_keys[dir]);
+    if (rc == int(cudaErrorNotSupported))
+        return fail(ctx, PQ_ERR_CAPACITY, "suffix sort: a 6-base bucket holds more suffixes than a sort chunk");
     if (rc != 0) return fail(ctx, PQ_ERR_CUDA, std::string("suffix sort failed: ") + cudaGetErrorString(cudaGetLastError()));
     CK(cudaEventRecord(ctx->ev1, ctx->st));
     CK(cudaEventSynchronize(ctx->ev1));
@@ -317,6 +327,14 @@ int pq_set_seed_k(pq_ctx* ctx, int k) {
     if (k < 1 || k > 13) return fail(ctx, PQ_ERR_ARG, "seed depth must be in [1, 13]");
     if (ctx->have_reads && k > ctx->t) return fail(ctx, PQ_ERR_ARG, "seed depth must not exceed t");
     ctx->seed_k = k;
+    return PQ_OK;
+}
+
+int pq_set_sort_chunk(pq_ctx* ctx, uint64_t max_suffixes) {
+    if (!ctx) return PQ_ERR_ARG;
+    if (max_suffixes == 1 || max_suffixes >= (uint64_t(1) << 31))
+        return fail(ctx, PQ_ERR_ARG, "sort chunk must be 0 (automatic) or 2 .. 2^31 - 1 suffixes");
+    ctx->sort_chunk = max_suffixes;
     return PQ_OK;
 }
 

@@ -911,4 +911,185 @@ int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa
     return int(cudaGetLastError());
 }
 
+// ------------------------------------------------------------------------------ chunked sort
+//
+// For indexes too large for one pass (group ranks are 32-bit, and the working memory grows with
+// n): every suffix falls in a bucket by its first 6 bases (padded with A) and min(length, 6),
+// numbered in suffix order, so the suffix array is the concatenation of the buckets' own sorted
+// suffixes.  Consecutive buckets are gathered into chunks of at most `cap` suffixes; each chunk is
+// listed in text order (stable compaction), keyed, radix sorted and refined exactly as a whole
+// sort, and written at its offset.
+
+constexpr int kBucketBases = 6;
+constexpr int kBuckets = (1 << (2 * kBucketBases)) * 8;
+constexpr int kCkTile = 4096;
+
+__device__ __forceinline__ uint32_t bucket_of(const uint64_t* __restrict__ pk, size_t p, idx_t L) {
+    const int m = int(L - idx_t(p % L));
+    const int w = m < kBucketBases ? m : kBucketBases;
+    const uint32_t pre = uint32_t(window(pk, p) >> (64 - 2 * kBucketBases)) & (~0u << (2 * (kBucketBases - w)));
+    return (pre << 3) | uint32_t(w);
+}
+
+__global__ void k_bucket_hist(const uint64_t* __restrict__ pk, size_t n, idx_t L, unsigned long long* __restrict__ hist) {
+    const size_t stride = size_t(gridDim.x) * blockDim.x;
+    for (size_t p = size_t(blockIdx.x) * blockDim.x + threadIdx.x; p < n; p += stride)
+        atomicAdd(&hist[bucket_of(pk, p, L)], 1ull);
+}
+
+// per tile of 4096 positions: how many fall in buckets [lo, hi)
+__global__ void __launch_bounds__(256) k_chunk_count(const uint64_t* __restrict__ pk, size_t n, idx_t L, uint32_t lo,
+                                                    uint32_t hi, unsigned long long* __restrict__ tcnt) {
+    __shared__ unsigned red[8];
+    const size_t t0 = size_t(blockIdx.x) * kCkTile;
+    unsigned c = 0;
+    for (int j = threadIdx.x; j < kCkTile; j += 256) {
+        const size_t p = t0 + j;
+        if (p < n) {
+            const uint32_t b = bucket_of(pk, p, L);
+            c += (b >= lo && b < hi) ? 1u : 0u;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned t = 0;
+        for (int w = 0; w < 8; ++w) t += red[w];
+        tcnt[blockIdx.x] = t;
+    }
+}
+
+// the positions of a chunk in text order (tile offsets from the exclusive scan of the counts)
+template <class V>
+__global__ void __launch_bounds__(256) k_chunk_write(const uint64_t* __restrict__ pk, size_t n, idx_t L, uint32_t lo,
+                                                    uint32_t hi, const unsigned long long* __restrict__ toff,
+                                                    V* __restrict__ list) {
+    __shared__ unsigned wsum[8];
+    __shared__ unsigned long long run;
+    const size_t t0 = size_t(blockIdx.x) * kCkTile;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) run = toff[blockIdx.x];
+    __syncthreads();
+    for (int j0 = 0; j0 < kCkTile; j0 += 256) {
+        const size_t p = t0 + j0 + threadIdx.x;
+        bool in = false;
+        if (p < n) {
+            const uint32_t b = bucket_of(pk, p, L);
+            in = b >= lo && b < hi;
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, in);
+        if (lane == 0) wsum[warp] = __popc(bal);
+        __syncthreads();
+        unsigned before = 0, all = 0;
+        for (int w = 0; w < 8; ++w) {
+            before += w < warp ? wsum[w] : 0u;
+            all += wsum[w];
+        }
+        if (in) list[run + before + __popc(bal & ((1u << lane) - 1))] = V(p);
+        __syncthreads();
+        if (threadIdx.x == 0) run += all;
+        __syncthreads();
+    }
+}
+
+template <class V>
+__global__ void k_init_keys_list(const uint64_t* __restrict__ pk, const V* __restrict__ list, size_t m, idx_t L,
+                                 uint64_t* __restrict__ key) {
+    const size_t stride = size_t(gridDim.x) * blockDim.x;
+    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < m; i += stride) {
+        const size_t p = size_t(list[i]);
+        const int len = int(L - idx_t(p % L));
+        const int w = len < kHead ? len : kHead;
+        const uint64_t keep = ~uint64_t(0) << (64 - 2 * w);
+        key[i] = (window(pk, p) & keep) | uint64_t(w);
+    }
+}
+
+static size_t chunk_parts(size_t n, size_t cap, size_t (&b)[9]) {
+    const size_t ntiles = (n + kCkTile - 1) / kCkTile;
+    b[0] = cap * sizeof(uint64_t);                    // ka
+    b[1] = cap * sizeof(uint64_t);                    // kb (also the group lists)
+    b[2] = cap * sizeof(idx_t);                       // va
+    b[3] = cap * sizeof(idx_t);                       // vb (with rank: big-group columns)
+    b[4] = cap * sizeof(uint32_t);                    // rank
+    b[5] = (n / 32 + 4) * sizeof(uint64_t);           // packed text
+    b[6] = radix_tmp_bytes(cap);
+    b[7] = (ntiles + 1) * sizeof(unsigned long long); // tile counts / offsets
+    b[8] = (size_t(kBuckets) + 8) * sizeof(unsigned long long);
+    size_t t = 0;
+    for (size_t x : b) t += al(x);
+    return t + 1024;
+}
+
+size_t suffix_sort_chunked_tmp_bytes(size_t n, size_t cap) {
+    size_t b[9];
+    return chunk_parts(n, cap, b);
+}
+
+int suffix_sort_chunked(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa, size_t cap, void* tmp,
+                        size_t tmp_bytes, cudaStream_t st) {
+    const size_t n = size_t(num_reads) * size_t(L);
+    if (n == 0) return 0;
+    if (cap < 2 || cap >= (size_t(1) << 31)) return int(cudaErrorInvalidValue);
+    size_t b[9];
+    if (tmp_bytes < chunk_parts(n, cap, b)) return int(cudaErrorInvalidValue);
+    char* q = static_cast<char*>(tmp);
+    char* part[9];
+    for (int i = 0; i < 9; ++i) {
+        part[i] = q;
+        q += al(b[i]);
+    }
+    uint64_t* ka0 = reinterpret_cast<uint64_t*>(part[0]);
+    uint64_t* kb0 = reinterpret_cast<uint64_t*>(part[1]);
+    idx_t* va0 = reinterpret_cast<idx_t*>(part[2]);
+    idx_t* vb0 = reinterpret_cast<idx_t*>(part[3]);
+    uint64_t* pk = reinterpret_cast<uint64_t*>(part[5]);
+    void* rtmp = part[6];
+    unsigned long long* tcnt = reinterpret_cast<unsigned long long*>(part[7]);
+    unsigned long long* hist = reinterpret_cast<unsigned long long*>(part[8]);
+    unsigned long long* counters = hist + kBuckets;
+    const size_t nwords = n / 32 + 4;
+    const size_t ntiles = (n + kCkTile - 1) / kCkTile;
+    { k_pack_text<<<grid_for(nwords, 256), 256, 0, st>>>(reads, n, idx_t(L), dir, nwords, pk); note_launch(); }
+    cudaMemsetAsync(hist, 0, size_t(kBuckets) * sizeof(unsigned long long), st);
+    { k_bucket_hist<<<grid_for(n, 256), 256, 0, st>>>(pk, n, idx_t(L), hist); note_launch(); }
+    std::vector<unsigned long long> h(kBuckets);
+    cudaMemcpyAsync(h.data(), hist, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return int(e);
+    size_t offset = 0;
+    uint32_t lo = 0;
+    while (lo < uint32_t(kBuckets)) {
+        // the next run of buckets that fits the chunk capacity
+        uint32_t hi = lo;
+        size_t m = 0;
+        while (hi < uint32_t(kBuckets) && m + h[hi] <= cap) m += h[hi++];
+        if (hi == lo) return int(cudaErrorNotSupported);          // one bucket larger than a chunk
+        if (m) {
+            { k_chunk_count<<<unsigned(ntiles), 256, 0, st>>>(pk, n, idx_t(L), lo, hi, tcnt); note_launch(); }
+            { k_scan_small<<<1, 1024, 0, st>>>(tcnt, ntiles); note_launch(); }
+            { k_chunk_write<idx_t><<<unsigned(ntiles), 256, 0, st>>>(pk, n, idx_t(L), lo, hi, tcnt, va0); note_launch(); }
+            { k_init_keys_list<idx_t><<<grid_for(m, 256), 256, 0, st>>>(pk, va0, m, idx_t(L), ka0); note_launch(); }
+            uint64_t* ka = ka0;
+            uint64_t* kb = kb0;
+            idx_t* va = va0;
+            idx_t* vb = vb0;
+            int rc = radix_sort_pairs<idx_t>(&ka, &va, &kb, &vb, m, 0, 64, rtmp, radix_tmp_bytes(m), st);
+            if (rc) return rc;
+            if (size_t(L) > size_t(kHead)) {
+                uint64_t* cols = reinterpret_cast<uint64_t*>(vb);
+                const size_t cols_cap = (al(m * sizeof(idx_t)) + al(m * sizeof(uint32_t))) / sizeof(uint64_t);
+                rc = refine_groups(ka, va, m, idx_t(L), pk, kb, cols, cols_cap, counters, st);
+                if (rc > 0) return rc;
+                if (rc < 0) return int(cudaErrorNotSupported);      // would need prefix doubling
+            }
+            { k_copy_vals<idx_t><<<grid_for(m, 256), 256, 0, st>>>(va, m, sa + offset); note_launch(); }
+        }
+        offset += m;
+        lo = hi;
+    }
+    return int(cudaGetLastError());
+}
+
 }  // namespace pq

@@ -14,6 +14,13 @@ size_t suffix_sort_tmp_bytes(size_t n);
 int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa, void* tmp,
                 size_t tmp_bytes, cudaStream_t st, const uint64_t** keys_out = nullptr);
 
+// The same order for inputs too large for one pass: suffixes bucketed by their first 6 bases,
+// consecutive buckets sorted in chunks of at most cap (< 2^31) suffixes.  Returns
+// cudaErrorNotSupported if one bucket exceeds cap.
+size_t suffix_sort_chunked_tmp_bytes(size_t n, size_t cap);
+int suffix_sort_chunked(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa, size_t cap, void* tmp,
+                        size_t tmp_bytes, cudaStream_t st);
+
 // Per-read seeds from a k-mer table (pq_index.cu).
 cudaError_t read_seeds(const uint8_t* reads, idx_t num_reads, int L, int dir, int k, const idx_t* kstart,
                        const idx_t* kend, idx_t* start, idx_t* size, cudaStream_t st);

@@ -119,7 +119,7 @@ WORKLOADS = {
                                lowc=0.0, L=100, cov=30, err=0.005, t=63),
     # learned-index workload: 12 % repeats, 2 % dinucleotide runs; 64-bit index
     "200Mbp_L150_20x_t63": dict(genome=200_000_000, gc=0.40, repeat=0.12, div=(0.01, 0.01),
-                                lowc=0.02, L=150, cov=20, err=0.003, t=63),
+                                lowc=0.02, L=150, cov=20, err=0.003, t=63, index=64),
 }
 
 # Queued-search workload: one genome, several read sets, each with its own read length (uniform
