@@ -552,8 +552,11 @@ static int search_finish(pq_ctx* ctx, pq::SearchArgs& A, pq::SearchOut& O) {
         CK(cudaMemcpyAsync(list.data(), ctx->ovf_list.p, ovf * sizeof(idx_t), cudaMemcpyDeviceToHost, ctx->st));
         CK(cudaStreamSynchronize(ctx->st));
         const size_t slot_bytes = pq::wide_slot_bytes(ctx->L);
-        int slots = int(std::max<size_t>(1, std::min<size_t>({size_t(ovf), size_t(1024),
-                                                              (size_t(4) << 30) / slot_bytes})));
+        // one thread per read: as many slots as a quarter of the free memory holds (at most 32 GB)
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) free_b = size_t(16) << 30;
+        const size_t budget = std::min(free_b / 4, size_t(32) << 30);
+        int slots = int(std::max<size_t>(1, std::min<size_t>({size_t(ovf), size_t(16384), budget / slot_bytes})));
         pq::WideScratch W{};
         W.stack_cap = size_t(2 * ctx->L) * size_t(2 * ctx->L);
         W.frame_cap = size_t(ctx->L + 2);

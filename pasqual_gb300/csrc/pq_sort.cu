@@ -489,7 +489,8 @@ __device__ __forceinline__ void block_scan3(unsigned (&c)[3], unsigned (&excl)[3
     }
 }
 
-__global__ void __launch_bounds__(kGlThreads) k_group_lists(const uint64_t* __restrict__ key, size_t n, GroupLists G) {
+__global__ void __launch_bounds__(kGlThreads) k_group_lists(const uint64_t* __restrict__ key, size_t n, GroupLists G,
+                                                           size_t base) {
     __shared__ uint32_t hm[kGlTile / 32 + 1];
     __shared__ unsigned wsum[kGlThreads / 32][3];
     __shared__ unsigned long long sbase[3];
@@ -548,7 +549,7 @@ __global__ void __launch_bounds__(kGlThreads) k_group_lists(const uint64_t* __re
         unsigned long long at[3] = {sbase[0] + excl[0], sbase[1] + excl[1], sbase[2] + excl[2]};
         #pragma unroll
         for (int q = 0; q < kGlPer; ++q) {
-            const size_t i = t0 + threadIdx.x + kGlThreads * q;
+            const size_t i = base + t0 + threadIdx.x + kGlThreads * q;
             const size_t m = mm[q];
             if (m >= 2 && m <= 32) {
                 if (at[0] < G.cap_small) G.small[at[0]] = (uint64_t(i) << 24) | m;
@@ -568,15 +569,16 @@ __global__ void __launch_bounds__(kGlThreads) k_group_lists(const uint64_t* __re
     }
 }
 
-// the W words of bases 29, 29+32, ... of the suffix at p (length m_len), zero past its end
+// the W words of bases off, off+32, ... of the suffix at p (length m_len), zero past its end
 template <int W>
-__device__ __forceinline__ void suffix_words(const uint64_t* __restrict__ pk, size_t p, int m_len, uint64_t w[W]) {
+__device__ __forceinline__ void suffix_words(const uint64_t* __restrict__ pk, size_t p, int m_len, int off,
+                                             uint64_t w[W]) {
     #pragma unroll
     for (int j = 0; j < W; ++j) {
-        const int rem = m_len - kHead - 32 * j;
+        const int rem = m_len - off - 32 * j;
         uint64_t x = 0;
         if (rem > 0) {
-            x = window(pk, p + kHead + 32 * size_t(j));
+            x = window(pk, p + off + 32 * size_t(j));
             if (rem < 32) x &= ~uint64_t(0) << (64 - 2 * rem);
         }
         w[j] = x;
@@ -599,7 +601,7 @@ __device__ __forceinline__ bool tuple_less(const uint64_t a[W], uint64_t alen, u
 // segment keeps its lanes, since segments are numbered in lane order).
 template <int W>
 __global__ void k_refine_warp(const unsigned long long* __restrict__ list, const unsigned long long* __restrict__ cnt,
-                              const uint64_t* __restrict__ pk, idx_t L, idx_t* __restrict__ val) {
+                              const uint64_t* __restrict__ pk, idx_t L, idx_t* __restrict__ val, int off) {
     constexpr int kChunk = 8;
     const int lane = threadIdx.x & 31;
     const size_t warp = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
@@ -629,7 +631,7 @@ __global__ void k_refine_warp(const unsigned long long* __restrict__ list, const
             if (lane < total) {
                 pos = uint64_t(val[start + off]);
                 len = uint64_t(L - idx_t(pos % L));
-                suffix_words<W>(pk, size_t(pos), int(len), w);
+                suffix_words<W>(pk, size_t(pos), int(len), off, w);
             } else {
                 #pragma unroll
                 for (int j = 0; j < W; ++j) w[j] = ~uint64_t(0);
@@ -702,7 +704,7 @@ __device__ void cta_bitonic(uint64_t* cols, int P2) {
 
 template <int W>
 __device__ void cta_load_group(uint64_t* cols, int P2, size_t start, int m, const uint64_t* __restrict__ pk, idx_t L,
-                               const idx_t* __restrict__ val) {
+                               const idx_t* __restrict__ val, int off) {
     uint64_t* lenc = cols + size_t(W) * P2;
     uint64_t* posc = lenc + P2;
     for (int i = threadIdx.x; i < P2; i += blockDim.x) {
@@ -711,7 +713,7 @@ __device__ void cta_load_group(uint64_t* cols, int P2, size_t start, int m, cons
         if (i < m) {
             pos = uint64_t(val[start + i]);
             len = uint64_t(L - idx_t(pos % L));
-            suffix_words<W>(pk, size_t(pos), int(len), w);
+            suffix_words<W>(pk, size_t(pos), int(len), off, w);
         } else {
             #pragma unroll
             for (int q = 0; q < W; ++q) w[q] = ~uint64_t(0);
@@ -726,7 +728,7 @@ __device__ void cta_load_group(uint64_t* cols, int P2, size_t start, int m, cons
 
 template <int W>
 __global__ void k_refine_cta(const unsigned long long* __restrict__ list, const unsigned long long* __restrict__ cnt,
-                             const uint64_t* __restrict__ pk, idx_t L, idx_t* __restrict__ val) {
+                             const uint64_t* __restrict__ pk, idx_t L, idx_t* __restrict__ val, int off) {
     extern __shared__ uint64_t s_cols[];
     const size_t groups = *cnt;
     for (size_t g = blockIdx.x; g < groups; g += gridDim.x) {
@@ -735,7 +737,7 @@ __global__ void k_refine_cta(const unsigned long long* __restrict__ list, const 
         const int m = int(e & 0xffffff);
         int P2 = 32;
         while (P2 < m) P2 <<= 1;
-        cta_load_group<W>(s_cols, P2, start, m, pk, L, val);
+        cta_load_group<W>(s_cols, P2, start, m, pk, L, val, off);
         cta_bitonic<W>(s_cols, P2);
         const uint64_t* posc = s_cols + size_t(W + 1) * P2;
         for (int i = threadIdx.x; i < m; i += blockDim.x) val[start + i] = idx_t(posc[i]);
@@ -743,69 +745,90 @@ __global__ void k_refine_cta(const unsigned long long* __restrict__ list, const 
     }
 }
 
-// one CTA per big group, columns in global scratch at cols + offset[g]
-template <int W>
-__global__ void k_refine_big(const unsigned long long* __restrict__ big, const unsigned long long* __restrict__ offs,
-                             const uint64_t* __restrict__ pk, idx_t L, idx_t* __restrict__ val, uint64_t* cols) {
-    const size_t g = blockIdx.x;
-    const size_t start = size_t(big[2 * g]);
-    const int m = int(big[2 * g + 1]);
-    int P2 = 32;
-    while (P2 < m) P2 <<= 1;
-    uint64_t* c = cols + offs[g];
-    cta_load_group<W>(c, P2, start, m, pk, L, val);
-    cta_bitonic<W>(c, P2);
-    const uint64_t* posc = c + size_t(W + 1) * P2;
-    for (int i = threadIdx.x; i < m; i += blockDim.x) val[start + i] = idx_t(posc[i]);
+// keys of a range of suffixes on their bases [off, off + 29): those bases (padded) and how many of
+// them exist (0..29), as the initial keys
+__global__ void k_range_keys(const uint64_t* __restrict__ pk, const idx_t* __restrict__ val, size_t m, idx_t L,
+                             int off, uint64_t* __restrict__ key, idx_t* __restrict__ out) {
+    const size_t stride = size_t(gridDim.x) * blockDim.x;
+    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < m; i += stride) {
+        const idx_t p = val[i];
+        const int rem = int(L - p % L) - off;
+        const int w = rem < kHead ? (rem > 0 ? rem : 0) : kHead;
+        key[i] = w ? ((window(pk, size_t(p) + off) & (~uint64_t(0) << (64 - 2 * w))) | uint64_t(w)) : 0;
+        out[i] = p;
+    }
 }
 
 template <int W>
-static int refine_groups_w(const GroupLists& G, unsigned long long n_small, unsigned long long n_mid,
-                           const std::vector<unsigned long long>& big, const uint64_t* pk, idx_t L, idx_t* val,
-                           uint64_t* cols, size_t cols_cap, cudaStream_t st) {
+static void refine_small_mid(const GroupLists& G, unsigned long long n_small, unsigned long long n_mid,
+                             const uint64_t* pk, idx_t L, idx_t* val, int off, cudaStream_t st) {
     if (n_small) {
         unsigned g = unsigned(std::min<unsigned long long>((n_small + 63) / 64, 152ull * 64));
-        { k_refine_warp<W><<<g, 256, 0, st>>>(G.small, G.counts + 0, pk, L, val); note_launch(); }
+        { k_refine_warp<W><<<g, 256, 0, st>>>(G.small, G.counts + 0, pk, L, val, off); note_launch(); }
     }
     if (n_mid) {
         const size_t smem = size_t(W + 2) * kGroupCta * sizeof(uint64_t);
         cudaFuncSetAttribute(k_refine_cta<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         unsigned g = unsigned(std::min<unsigned long long>(n_mid, 152ull * 8));
-        { k_refine_cta<W><<<g, 512, smem, st>>>(G.mid, G.counts + 1, pk, L, val); note_launch(); }
+        { k_refine_cta<W><<<g, 512, smem, st>>>(G.mid, G.counts + 1, pk, L, val, off); note_launch(); }
     }
-    // big groups in rounds that fit the column scratch
-    size_t i = 0;
-    const size_t nb = big.size() / 2;
-    std::vector<unsigned long long> offs;
-    while (i < nb) {
-        offs.clear();
-        size_t used = 0, j = i;
-        for (; j < nb; ++j) {
-            size_t P2 = 32;
-            while (P2 < big[2 * j + 1]) P2 <<= 1;
-            const size_t need = size_t(W + 2) * P2;
-            if (used + need > cols_cap) break;
-            offs.push_back(used);
-            used += need;
-        }
-        if (j == i) return -1;   // one group alone does not fit: caller falls back
-        // offsets and the group entries of this round go behind the columns
-        unsigned long long* dev_meta = reinterpret_cast<unsigned long long*>(cols + used);
-        if ((used + offs.size() * 3 + 8) > cols_cap) return -1;
-        cudaMemcpyAsync(dev_meta, offs.data(), offs.size() * 8, cudaMemcpyHostToDevice, st);
-        cudaMemcpyAsync(dev_meta + offs.size(), big.data() + 2 * i, (j - i) * 16, cudaMemcpyHostToDevice, st);
-        { k_refine_big<W><<<unsigned(j - i), 1024, 0, st>>>(dev_meta + offs.size(), dev_meta, pk, L, val, cols);
-          note_launch(); }
+}
+
+// Groups of up to 1024 suffixes are finished in place by the warp and CTA kernels.  A larger group
+// (low-complexity or highly repeated sequence) gets a device-wide radix sort of its range on the
+// next 29 bases, and its subgroups are finished the same way, 29 bases further on each time.
+template <int W>
+static int refine_groups_w(const GroupLists& G, unsigned long long n_small, unsigned long long n_mid,
+                           const std::vector<unsigned long long>& big, const uint64_t* pk, idx_t L, idx_t* val,
+                           uint64_t* cols, size_t cols_cap, void* rtmp, size_t rtmp_bytes, cudaStream_t st) {
+    refine_small_mid<W>(G, n_small, n_mid, pk, L, val, kHead, st);
+    struct Item {
+        size_t start, m;
+        int off;
+    };
+    std::vector<Item> work;
+    for (size_t i = 0; i + 1 < big.size(); i += 2) work.push_back({size_t(big[i]), size_t(big[i + 1]), kHead});
+    std::vector<unsigned long long> sub;
+    while (!work.empty()) {
+        const Item it = work.back();
+        work.pop_back();
+        const size_t m = it.m;
+        // range scratch in the column area: two key arrays, two value arrays
+        const size_t kw = m, vw = (m * sizeof(idx_t) + 7) / 8;
+        if (2 * kw + 2 * vw + 64 > cols_cap) return -1;
+        uint64_t* ka = cols;
+        uint64_t* kb = cols + kw;
+        idx_t* va = reinterpret_cast<idx_t*>(cols + 2 * kw);
+        idx_t* vb = reinterpret_cast<idx_t*>(cols + 2 * kw + vw);
+        { k_range_keys<<<grid_for(m, 256), 256, 0, st>>>(pk, val + it.start, m, L, it.off, ka, va); note_launch(); }
+        int rc = radix_sort_pairs<idx_t>(&ka, &va, &kb, &vb, m, 0, 64, rtmp, rtmp_bytes, st);
+        if (rc) return rc;
+        { k_copy_vals<idx_t><<<grid_for(m, 256), 256, 0, st>>>(va, m, val + it.start); note_launch(); }
+        if (it.off + kHead >= int(L)) continue;          // every suffix is now fully compared
+        cudaMemsetAsync(G.counts, 0, 3 * sizeof(unsigned long long), st);
+        { k_group_lists<<<unsigned(std::min<size_t>((m + kGlTile - 1) / kGlTile, size_t(152) * 64)), 256, 0, st>>>(
+              ka, m, G, it.start); note_launch(); }
+        unsigned long long c[3];
+        cudaMemcpyAsync(c, G.counts, sizeof c, cudaMemcpyDeviceToHost, st);
         cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return int(e);
-        i = j;
+        if (c[0] > G.cap_small || c[1] > G.cap_mid || c[2] > G.cap_big) return -1;
+        refine_small_mid<W>(G, c[0], c[1], pk, L, val, it.off + kHead, st);
+        if (c[2]) {
+            sub.resize(2 * c[2]);
+            cudaMemcpyAsync(sub.data(), G.big, sub.size() * 8, cudaMemcpyDeviceToHost, st);
+            e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) return int(e);
+            for (size_t i = 0; i + 1 < sub.size(); i += 2)
+                work.push_back({size_t(sub[i]), size_t(sub[i + 1]), it.off + kHead});
+        }
     }
     return int(cudaGetLastError());
 }
 
-// Returns 0 when every group was refined, -1 when the caller must fall back to prefix doubling.
 static int refine_groups(const uint64_t* key, idx_t* val, size_t n, idx_t L, const uint64_t* pk, uint64_t* lists_mem,
-                         uint64_t* cols, size_t cols_cap, unsigned long long* counters, cudaStream_t st) {
+                         uint64_t* cols, size_t cols_cap, unsigned long long* counters, void* rtmp, size_t rtmp_bytes,
+                         cudaStream_t st) {
     const int W = int((2 * (size_t(L) - kHead) + 63) / 64);
     if (W < 1 || W > kRefineMaxWords) return -1;
     GroupLists G;
@@ -817,7 +840,8 @@ static int refine_groups(const uint64_t* key, idx_t* val, size_t n, idx_t L, con
     G.big = G.mid + G.cap_mid;
     G.counts = counters;
     cudaMemsetAsync(counters, 0, 3 * sizeof(unsigned long long), st);
-    { k_group_lists<<<unsigned(std::min<size_t>((n + kGlTile - 1) / kGlTile, size_t(152) * 64)), 256, 0, st>>>(key, n, G); note_launch(); }
+    { k_group_lists<<<unsigned(std::min<size_t>((n + kGlTile - 1) / kGlTile, size_t(152) * 64)), 256, 0, st>>>(
+          key, n, G, 0); note_launch(); }
     unsigned long long c[3];
     cudaMemcpyAsync(c, counters, sizeof c, cudaMemcpyDeviceToHost, st);
     cudaError_t e = cudaStreamSynchronize(st);
@@ -829,14 +853,14 @@ static int refine_groups(const uint64_t* key, idx_t* val, size_t n, idx_t L, con
         if (e != cudaSuccess) return int(e);
     }
     switch (W) {
-        case 1: return refine_groups_w<1>(G, c[0], c[1], big, pk, L, val, cols, cols_cap, st);
-        case 2: return refine_groups_w<2>(G, c[0], c[1], big, pk, L, val, cols, cols_cap, st);
-        case 3: return refine_groups_w<3>(G, c[0], c[1], big, pk, L, val, cols, cols_cap, st);
-        case 4: return refine_groups_w<4>(G, c[0], c[1], big, pk, L, val, cols, cols_cap, st);
-        case 5: return refine_groups_w<5>(G, c[0], c[1], big, pk, L, val, cols, cols_cap, st);
-        case 6: return refine_groups_w<6>(G, c[0], c[1], big, pk, L, val, cols, cols_cap, st);
-        case 7: return refine_groups_w<7>(G, c[0], c[1], big, pk, L, val, cols, cols_cap, st);
-        default: return refine_groups_w<8>(G, c[0], c[1], big, pk, L, val, cols, cols_cap, st);
+        case 1: return refine_groups_w<1>(G, c[0], c[1], big, pk, L, val, cols, cols_cap, rtmp, rtmp_bytes, st);
+        case 2: return refine_groups_w<2>(G, c[0], c[1], big, pk, L, val, cols, cols_cap, rtmp, rtmp_bytes, st);
+        case 3: return refine_groups_w<3>(G, c[0], c[1], big, pk, L, val, cols, cols_cap, rtmp, rtmp_bytes, st);
+        case 4: return refine_groups_w<4>(G, c[0], c[1], big, pk, L, val, cols, cols_cap, rtmp, rtmp_bytes, st);
+        case 5: return refine_groups_w<5>(G, c[0], c[1], big, pk, L, val, cols, cols_cap, rtmp, rtmp_bytes, st);
+        case 6: return refine_groups_w<6>(G, c[0], c[1], big, pk, L, val, cols, cols_cap, rtmp, rtmp_bytes, st);
+        case 7: return refine_groups_w<7>(G, c[0], c[1], big, pk, L, val, cols, cols_cap, rtmp, rtmp_bytes, st);
+        default: return refine_groups_w<8>(G, c[0], c[1], big, pk, L, val, cols, cols_cap, rtmp, rtmp_bytes, st);
     }
 }
 
@@ -885,7 +909,7 @@ int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa
         // finish the groups where they lie; lists go to kb, big-group columns to vb + rank
         uint64_t* cols = reinterpret_cast<uint64_t*>(vb);
         const size_t cols_cap = (al(n * sizeof(idx_t)) + al(n * sizeof(uint32_t))) / sizeof(uint64_t);
-        rc = refine_groups(ka, va, n, idx_t(L), pk, kb, cols, cols_cap, tcnt, st);
+        rc = refine_groups(ka, va, n, idx_t(L), pk, kb, cols, cols_cap, tcnt, rtmp, radix_tmp_bytes(n), st);
         if (rc > 0) return rc;
         if (rc == 0) {   // the refinement permutes suffixes within groups of equal keys only
             { k_copy_vals<idx_t><<<grid_for(n, 256), 256, 0, st>>>(va, n, sa); note_launch(); }
@@ -1086,7 +1110,7 @@ int suffix_sort_chunked(const uint8_t* reads, idx_t num_reads, int L, int dir, i
             if (size_t(L) > size_t(kHead)) {
                 uint64_t* cols = reinterpret_cast<uint64_t*>(vb);
                 const size_t cols_cap = (al(m * sizeof(idx_t)) + al(m * sizeof(uint32_t))) / sizeof(uint64_t);
-                rc = refine_groups(ka, va, m, idx_t(L), pk, kb, cols, cols_cap, counters, st);
+                rc = refine_groups(ka, va, m, idx_t(L), pk, kb, cols, cols_cap, counters, rtmp, radix_tmp_bytes(m), st);
                 if (rc > 0) return rc;
                 if (rc < 0) return int(cudaErrorNotSupported);      // would need prefix doubling
             }
