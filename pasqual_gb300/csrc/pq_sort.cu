@@ -896,6 +896,7 @@ int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa
     unsigned long long* tcnt = tmax + tiles + 1;
     unsigned long long* groups = tcnt + tiles + 1;
 
+    idx_t* const vb0 = vb;                 // followed by rank in memory
     { k_pack_text<<<grid_for(nwords, 256), 256, 0, st>>>(reads, n, idx_t(L), dir, nwords, pk); note_launch(); }
     { k_init_keys<<<grid_for(n, 256), 256, 0, st>>>(pk, n, idx_t(L), ka, va); note_launch(); }
     int rc = radix_sort_pairs<idx_t>(&ka, &va, &kb, &vb, n, 0, 64, rtmp, radix_tmp_bytes(n), st);
@@ -906,9 +907,11 @@ int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa
         return int(cudaGetLastError());
     }
     {
-        // finish the groups where they lie; lists go to kb, big-group columns to vb + rank
+        // finish the groups where they lie; lists go to kb, big-group scratch to the free value
+        // buffer (and rank behind it when that buffer is the second one: the sorted values may have
+        // ended in either, depending on how many radix passes ran)
         uint64_t* cols = reinterpret_cast<uint64_t*>(vb);
-        const size_t cols_cap = (al(n * sizeof(idx_t)) + al(n * sizeof(uint32_t))) / sizeof(uint64_t);
+        const size_t cols_cap = (al(n * sizeof(idx_t)) + (vb == vb0 ? al(n * sizeof(uint32_t)) : 0)) / sizeof(uint64_t);
         rc = refine_groups(ka, va, n, idx_t(L), pk, kb, cols, cols_cap, tcnt, rtmp, radix_tmp_bytes(n), st);
         if (rc > 0) return rc;
         if (rc == 0) {   // the refinement permutes suffixes within groups of equal keys only
@@ -1108,8 +1111,9 @@ int suffix_sort_chunked(const uint8_t* reads, idx_t num_reads, int L, int dir, i
             int rc = radix_sort_pairs<idx_t>(&ka, &va, &kb, &vb, m, 0, 64, rtmp, radix_tmp_bytes(m), st);
             if (rc) return rc;
             if (size_t(L) > size_t(kHead)) {
+                // scratch: the free value buffer, and rank behind it when that is the second buffer
                 uint64_t* cols = reinterpret_cast<uint64_t*>(vb);
-                const size_t cols_cap = (al(m * sizeof(idx_t)) + al(m * sizeof(uint32_t))) / sizeof(uint64_t);
+                const size_t cols_cap = (vb == vb0 ? al(b[3]) + b[4] : al(b[2])) / sizeof(uint64_t);
                 rc = refine_groups(ka, va, m, idx_t(L), pk, kb, cols, cols_cap, counters, rtmp, radix_tmp_bytes(m), st);
                 if (rc > 0) return rc;
                 if (rc < 0) return int(cudaErrorNotSupported);      // would need prefix doubling
