@@ -597,11 +597,11 @@ __device__ __forceinline__ bool tuple_less(const uint64_t a[W], uint64_t alen, u
 
 // Groups of 2..32 suffixes, several per warp: a warp takes 8 list entries at a time and packs
 // consecutive ones into its 32 lanes while they fit; one 32-lane bitonic network on
-// (segment, remaining bases, length, position) then sorts every packed group in place (each
+// (segment, bases from `from` on, length, position) then sorts every packed group in place (each
 // segment keeps its lanes, since segments are numbered in lane order).
 template <int W>
 __global__ void k_refine_warp(const unsigned long long* __restrict__ list, const unsigned long long* __restrict__ cnt,
-                              const uint64_t* __restrict__ pk, idx_t L, idx_t* __restrict__ val, int off) {
+                              const uint64_t* __restrict__ pk, idx_t L, idx_t* __restrict__ val, int from) {
     constexpr int kChunk = 8;
     const int lane = threadIdx.x & 31;
     const size_t warp = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
@@ -631,7 +631,7 @@ __global__ void k_refine_warp(const unsigned long long* __restrict__ list, const
             if (lane < total) {
                 pos = uint64_t(val[start + off]);
                 len = uint64_t(L - idx_t(pos % L));
-                suffix_words<W>(pk, size_t(pos), int(len), off, w);
+                suffix_words<W>(pk, size_t(pos), int(len), from, w);
             } else {
                 #pragma unroll
                 for (int j = 0; j < W; ++j) w[j] = ~uint64_t(0);
