@@ -102,7 +102,8 @@ struct pq_ctx {
 
     // overlap-search output
     DevBuf nB, nF, oB, oF, status, esrc, e_dest, e_trans, e_len, e_type, ctrs, ovf_list;
-    DevBuf off, g_dest, g_len, g_type, g_trans, asm_tmp, wide, warp_scratch, defer;
+    DevBuf off, g_dest, g_len, g_type, g_trans, asm_tmp, wide, warp_scratch, defer, heavy_scratch, ovf2;
+    uint64_t heavy_reads = 0;
     bool graph_ok = false;
     uint64_t num_edges = 0, probes = 0, wide_reads = 0;
 };
@@ -178,7 +179,8 @@ void pq_destroy(pq_ctx* ctx) {
     DevBuf* bufs[] = {&ctx->reads, &ctx->ktmp, &ctx->sort_tmp, &ctx->counts, &ctx->nB, &ctx->nF, &ctx->oB,
                       &ctx->oF, &ctx->status, &ctx->esrc, &ctx->e_dest, &ctx->e_trans, &ctx->e_len,
                       &ctx->e_type, &ctx->ctrs, &ctx->ovf_list, &ctx->off, &ctx->g_dest, &ctx->g_len,
-                      &ctx->g_type, &ctx->g_trans, &ctx->asm_tmp, &ctx->wide, &ctx->warp_scratch, &ctx->defer};
+                      &ctx->g_type, &ctx->g_trans, &ctx->asm_tmp, &ctx->wide, &ctx->warp_scratch, &ctx->defer,
+                      &ctx->heavy_scratch, &ctx->ovf2};
     for (DevBuf* b : bufs) b->release();
     for (int d = 0; d < 2; ++d) {
         ctx->sa[d].release();
@@ -545,11 +547,34 @@ static int search_finish(pq_ctx* ctx, pq::SearchArgs& A, pq::SearchOut& O) {
     CK(cudaStreamSynchronize(ctx->st));
     ctx->lx_misses = hc[3];
     unsigned ovf = unsigned(hc[2] & 0xffffffffu);
+    const idx_t* ovf_src = ctx->ovf_list.as<idx_t>();
+    ctx->heavy_reads = 0;
+    if (ovf) {
+        // heavy tier (the fast kernel's DFS with larger capacities) over the reads the fast tier
+        // could not hold; what it cannot hold either goes on to the wide tier
+        const int hebcap = 4096;
+        const int hblocks = int(std::min<size_t>((size_t(ovf) + 127) / 128, size_t(152) * 2));
+        const size_t hbytes = pq::heavy_scratch_bytes(ctx->L, ctx->t, hblocks, hebcap);
+        CK(ctx->heavy_scratch.ensure(hbytes));
+        CK(ctx->ovf2.ensure(nrp * sizeof(idx_t)));
+        pq::SearchOut O2 = O;
+        O2.ovf_list = ctx->ovf2.as<idx_t>();
+        O2.ovf_count = reinterpret_cast<unsigned int*>(ctr + 5);
+        CK(cudaMemsetAsync(ctr + 5, 0, sizeof(unsigned long long), ctx->st));
+        CK(pq::search_heavy(A, O2, ctx->ovf_list.as<idx_t>(), reinterpret_cast<const unsigned*>(ctr + 2), hblocks,
+                            ctx->heavy_scratch.p, hbytes, hebcap, ctx->st));
+        unsigned long long h5 = 0;
+        CK(cudaMemcpyAsync(&h5, ctr + 5, sizeof h5, cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+        ctx->heavy_reads = ovf;
+        ovf = unsigned(h5 & 0xffffffffu);
+        ovf_src = ctx->ovf2.as<idx_t>();
+    }
     ctx->wide_reads = ovf;
     if (ovf) {
         // wide tier over the overflow list; retried after growing the edge pool if needed
         std::vector<idx_t> list(ovf);
-        CK(cudaMemcpyAsync(list.data(), ctx->ovf_list.p, ovf * sizeof(idx_t), cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaMemcpyAsync(list.data(), ovf_src, ovf * sizeof(idx_t), cudaMemcpyDeviceToHost, ctx->st));
         CK(cudaStreamSynchronize(ctx->st));
         const size_t slot_bytes = pq::wide_slot_bytes(ctx->L);
         // one thread per read: as many slots as a quarter of the free memory holds (at most 32 GB)

@@ -109,6 +109,10 @@ int search_lean_blocks(int L, int M, int num_sms);
 size_t lean_scratch_bytes(int L, int t, int lean_blocks, int fast_blocks, int ebcap);
 cudaError_t search_lean(const SearchArgs& a, const SearchOut& o, int lean_blocks, int fast_blocks, void* scratch,
                         size_t scratch_bytes, int ebcap, cudaStream_t st);
+// Heavy tier over reads[0, *count) with a wider DFS (reads the fast tier could not hold).
+size_t heavy_scratch_bytes(int L, int t, int blocks, int ebcap);
+cudaError_t search_heavy(const SearchArgs& a, const SearchOut& o, const idx_t* list, const unsigned* count, int blocks,
+                         void* scratch, size_t scratch_bytes, int ebcap, cudaStream_t st);
 // One persistent lean launch over a queue of batches, then the fast tier over the handed-over
 // reads of the batches listed in `batches` (host_batches: the descriptions the queue holds).
 cudaError_t search_lean_queue(const SearchQueue& q, const SearchBatch* host_batches, const int* batches, int nbatch,

@@ -824,9 +824,11 @@ struct TFrame {
     int32_t ctr[4];     // interval-size sum of each set
 };
 
-// Shared memory of one warp for the level-synchronous DFS of its 32 tasks.
+// Shared memory of one warp for the level-synchronous DFS of its 32 tasks (MW 64-bit mask words
+// per task and base: one bit per interval of a level, up to 64 MW intervals).
+template <int MW>
 struct MultiSmem {
-    unsigned long long mask[32][4][2];   // extension present, by entry index (kPMax bits)
+    unsigned long long mask[32][4][MW];  // extension present, by entry index
     int hit[32];                         // first entry that completes a read with $ rows
     int cml[32][4];
     unsigned ctr[32][4];
@@ -836,10 +838,24 @@ struct MultiSmem {
     int lvl[32], chk[32], size[32], na[32];
 };
 
-__device__ __forceinline__ int popc128(const unsigned long long m[2]) { return __popcll(m[0]) + __popcll(m[1]); }
-__device__ __forceinline__ int popc128_below(const unsigned long long m[2], int i) {
-    if (i < 64) return __popcll(m[0] & ((1ull << i) - 1));
-    return __popcll(m[0]) + __popcll(m[1] & ((i == 64) ? 0ull : ((1ull << (i - 64)) - 1)));
+template <int MW>
+__device__ __forceinline__ int popc_words(const unsigned long long* m) {
+    int c = 0;
+    #pragma unroll
+    for (int w = 0; w < MW; ++w) c += __popcll(m[w]);
+    return c;
+}
+// set bits of m below bit i
+template <int MW>
+__device__ __forceinline__ int popc_below(const unsigned long long* m, int i) {
+    int c = 0;
+    #pragma unroll
+    for (int w = 0; w < MW; ++w) {
+        const int lo = 64 * w;
+        if (i >= lo + 64) c += __popcll(m[w]);
+        else if (i > lo) c += __popcll(m[w] & ((1ull << (i - lo)) - 1));
+    }
+    return c;
 }
 
 // exclusive prefix of v over the warp into pref[0..32] (pref[32] = total), returns the total
@@ -1042,11 +1058,12 @@ __device__ __forceinline__ void load_batch(SearchBatch& dst, const SearchBatch* 
 // groups of 32 reads w, w + #warps, ...  With a queue, each warp takes the next item (a batch and
 // a group of its reads) from a shared counter until the queue is empty; the batch's description
 // (index pair, L, t, outputs) is loaded into the warp's shared memory when it changes.
-template <int W>
+template <int W, int CAP, int FRAMES, int PMAX>
 __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A0, SearchOut O0, WarpScratch S, SearchQueue Q) {
+    constexpr int MW = PMAX / 64;
     extern __shared__ uint32_t s_reads[];
     __shared__ SearchBatch s_b[kWarpsPerCta];
-    __shared__ MultiSmem s_ms[kWarpsPerCta];
+    __shared__ MultiSmem<MW> s_ms[kWarpsPerCta];
     __shared__ int s_n[kWarpsPerCta][32][4];
     __shared__ int32_t s_olp[kWarpsPerCta][32][2];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -1062,14 +1079,14 @@ __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A0, SearchOut
         }
         __syncwarp();
     }
-    MultiSmem& sm = s_ms[wid];
+    MultiSmem<MW>& sm = s_ms[wid];
     const size_t cbase_w = gw * 32 * 4 * size_t(S.mstride);    // level-0 candidates of this warp
     const size_t ebase_w = gw * 32 * size_t(S.ebcap);          // edge slots of this warp
-    const size_t tbase_w = gw * 32 * size_t(kTaskCap);         // task stacks
-    const size_t xbase_w = gw * 32 * 4 * size_t(kPMax);        // sparse extension slots
-    const size_t mbase_w = gw * 32 * size_t(kPMax);            // emission bounds
+    const size_t tbase_w = gw * 32 * size_t(CAP);         // task stacks
+    const size_t xbase_w = gw * 32 * 4 * size_t(PMAX);        // sparse extension slots
+    const size_t mbase_w = gw * 32 * size_t(PMAX);            // emission bounds
     const size_t rbase_w = gw * 32 * size_t(kRedMax);          // sorted-reduction candidates
-    TFrame* const frw = S.frames + gw * 32 * kTaskFrames;
+    TFrame* const frw = S.frames + gw * 32 * FRAMES;
     uint32_t probes = 0;
     int cur = -1;
     // reads of the current batch (or of the list of reads handed over by the lean tier)
@@ -1126,8 +1143,8 @@ __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A0, SearchOut
         // ---- phase B
         int status = have ? OVF_NONE : -1;
         int ne = 0, count_b = 0, count_f = 0;
-        const size_t tb = tbase_w + size_t(lane) * kTaskCap;    // this lane's task stack
-        TFrame* const fr = frw + lane * kTaskFrames;
+        const size_t tb = tbase_w + size_t(lane) * CAP;    // this lane's task stack
+        TFrame* const fr = frw + lane * FRAMES;
         const size_t eb = ebase_w + size_t(lane) * S.ebcap;
         #pragma unroll 1
         for (int side = 0; side < 2; ++side) {
@@ -1141,7 +1158,7 @@ __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A0, SearchOut
                 if (st != OVF_NONE) status = st;
                 active = false;
             }
-            if (active && n0 > kTaskCap) { status = OVF_STACK; active = false; }
+            if (active && n0 > CAP) { status = OVF_STACK; active = false; }
             // level 0 = kind-0 candidates then kind-1 candidates, copied into the task stacks
             sm.na[lane] = na;
             const int tot0 = warp_prefix(active ? n0 : 0, sm.pref);
@@ -1151,7 +1168,7 @@ __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A0, SearchOut
                 const int nj = sm.na[j];
                 const size_t src = cbase_w + size_t(j) * 4 * size_t(S.mstride) +
                                    (i < nj ? size_t(2 * side) * M + i : size_t(2 * side + 1) * M + (i - nj));
-                const size_t dst = tbase_w + size_t(j) * kTaskCap + i;
+                const size_t dst = tbase_w + size_t(j) * CAP + i;
                 S.t_ll[dst] = S.c_ll[src];
                 S.t_uu[dst] = S.c_uu[src];
                 S.t_meta[dst] = S.c_meta[src];
@@ -1182,7 +1199,7 @@ __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A0, SearchOut
                             F = fr[level];
                             continue;
                         }
-                        if (level + 1 >= kTaskFrames) { status = OVF_LEVELS; active = false; break; }
+                        if (level + 1 >= FRAMES) { status = OVF_LEVELS; active = false; break; }
                         F.next_a = uint32_t(a + 1);
                         fr[level] = F;
                         uint32_t before = 0, all = 0;
@@ -1209,7 +1226,7 @@ __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A0, SearchOut
                     }
                 }
                 const bool expand = active && entering;
-                if (expand && F.size > kPMax) { status = OVF_STACK; active = false; }
+                if (expand && F.size > PMAX) { status = OVF_STACK; active = false; }
                 const bool go = active && entering;
                 sm.size[lane] = go ? int(F.size) : 0;
                 sm.pos[lane] = F.pos;
@@ -1218,7 +1235,8 @@ __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A0, SearchOut
                 sm.hit[lane] = 0x7fffffff;
                 #pragma unroll
                 for (int a = 0; a < 4; ++a) {
-                    sm.mask[lane][a][0] = sm.mask[lane][a][1] = 0;
+                    #pragma unroll
+                    for (int w = 0; w < MW; ++w) sm.mask[lane][a][w] = 0;
                     sm.cml[lane][a] = 0;
                     sm.ctr[lane][a] = 0;
                 }
@@ -1228,7 +1246,7 @@ __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A0, SearchOut
                 for (int e = lane; e < tot; e += 32) {
                     const int j = owner_of(sm.pref, e);
                     const int i = e - sm.pref[j];
-                    const size_t tj = tbase_w + size_t(j) * kTaskCap + sm.pos[j] + i;
+                    const size_t tj = tbase_w + size_t(j) * CAP + sm.pos[j] + i;
                     const idx_t cl = S.t_ll[tj], cu = S.t_uu[tj];
                     const uint32_t m = S.t_meta[tj];
                     const bool ext = idx_t(cu - cl + 1) != 0;   // wrapped [0, all-ones]: kept, never extended
@@ -1245,7 +1263,7 @@ __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A0, SearchOut
                         const idx_t ea = f.Cf[0] + (cl - (rl[0] + rl[1] + rl[2] + rl[3]));
                         const idx_t eb2 = f.Cf[0] + ((cu + 1) - (ru[0] + ru[1] + ru[2] + ru[3])) - 1;
                         if (ea <= eb2) {
-                            const size_t me = mbase_w + size_t(j) * kPMax + i;
+                            const size_t me = mbase_w + size_t(j) * PMAX + i;
                             S.em_l[me] = ea;
                             S.em_u[me] = eb2;
                             atomicMin(&sm.hit[j], i);
@@ -1258,7 +1276,7 @@ __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A0, SearchOut
                             const idx_t lo = f.Cf[ch] + pick4(rl, ch);
                             const idx_t hi = f.Cf[ch] + pick4(ru, ch) - 1;
                             if (lo <= hi) {
-                                const size_t x = xbase_w + (size_t(j) * 4 + (a - 1)) * kPMax + i;
+                                const size_t x = xbase_w + (size_t(j) * 4 + (a - 1)) * PMAX + i;
                                 S.x_ll[x] = lo;
                                 S.x_uu[x] = hi;
                                 S.x_meta[x] = m;
@@ -1276,7 +1294,7 @@ __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A0, SearchOut
                     const int h = sm.hit[lane];
                     bool popped = false;
                     if (h != 0x7fffffff) {
-                        const size_t me = mbase_w + size_t(lane) * kPMax + h;
+                        const size_t me = mbase_w + size_t(lane) * PMAX + h;
                         const idx_t lll = S.em_l[me], uuu = S.em_u[me];
                         const uint32_t hm = S.t_meta[tb + F.pos + h];
                         const idx_t endk = uuu + 1;      // k < uuu + 1: no iteration when uuu + 1 wraps
@@ -1310,11 +1328,11 @@ __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A0, SearchOut
                         int run = 0;
                         #pragma unroll
                         for (int a = 0; a < 4; ++a) {
-                            c[a] = popc128(sm.mask[lane][a]);
+                            c[a] = popc_words<MW>(sm.mask[lane][a]);
                             sm.setoff[lane][a] = run;
                             run += c[a];
                         }
-                        if (int(F.free) + run > kTaskCap) {
+                        if (int(F.free) + run > CAP) {
                             status = OVF_STACK;
                             active = false;
                         } else {
@@ -1344,9 +1362,9 @@ __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A0, SearchOut
                     const int a = rel / Pj, i = rel - a * Pj;
                     const unsigned long long* mk = sm.mask[j][a];
                     if ((mk[i >> 6] >> (i & 63)) & 1) {
-                        const int dst = int(sm.cbase[j]) + sm.setoff[j][a] + popc128_below(mk, i);
-                        const size_t x = xbase_w + (size_t(j) * 4 + a) * kPMax + i;
-                        const size_t t = tbase_w + size_t(j) * kTaskCap + dst;
+                        const int dst = int(sm.cbase[j]) + sm.setoff[j][a] + popc_below<MW>(mk, i);
+                        const size_t x = xbase_w + (size_t(j) * 4 + a) * PMAX + i;
+                        const size_t t = tbase_w + size_t(j) * CAP + dst;
                         S.t_ll[t] = S.x_ll[x];
                         S.t_uu[t] = S.x_uu[x];
                         S.t_meta[t] = S.x_meta[x];
@@ -1539,18 +1557,19 @@ int search_fast_blocks(int L, int M, int num_sms) {
     const size_t smem = size_t(words) * 32 * kWarpsPerCta * sizeof(uint32_t);
     int per_sm = 0;
     const cudaError_t e = lam_words(M) == 2
-        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search_fast<2>, 32 * kWarpsPerCta, smem)
-        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search_fast<kLamWords>, 32 * kWarpsPerCta, smem);
+        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search_fast<2, kTaskCap, kTaskFrames, kPMax>, 32 * kWarpsPerCta, smem)
+        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search_fast<kLamWords, kTaskCap, kTaskFrames, kPMax>, 32 * kWarpsPerCta, smem);
     if (e != cudaSuccess || per_sm < 1)
         per_sm = 1;
     return per_sm * num_sms;
 }
 
-static size_t scratch_layout(int M_max, size_t nwarps, int ebcap, void* base, WarpScratch* S) {
+static size_t scratch_layout(int M_max, size_t nwarps, int ebcap, void* base, WarpScratch* S, int cap = kTaskCap,
+                             int frames = kTaskFrames, int pmax = kPMax) {
     const size_t M = size_t(M_max);
     const size_t cand = nwarps * 32 * 4 * M, edg = nwarps * 32 * size_t(ebcap);
-    const size_t tsk = nwarps * 32 * size_t(kTaskCap), spr = nwarps * 32 * 4 * size_t(kPMax);
-    const size_t emb = nwarps * 32 * size_t(kPMax), frm = nwarps * 32 * size_t(kTaskFrames);
+    const size_t tsk = nwarps * 32 * size_t(cap), spr = nwarps * 32 * 4 * size_t(pmax);
+    const size_t emb = nwarps * 32 * size_t(pmax), frm = nwarps * 32 * size_t(frames);
     char* p = static_cast<char*>(base);
     size_t used = 0;
     auto take = [&](size_t bytes) {
@@ -1598,8 +1617,8 @@ cudaError_t search_fast(const SearchArgs& a, const SearchOut& o, int blocks, voi
     const int words = (a.L + 15) / 16;
     size_t smem = size_t(words) * 32 * kWarpsPerCta * sizeof(uint32_t);
     SearchQueue Q{};
-    if (lam_words(a.L - a.t) == 2) k_search_fast<2><<<blocks, 32 * kWarpsPerCta, smem, st>>>(a, o, S, Q);
-    else k_search_fast<kLamWords><<<blocks, 32 * kWarpsPerCta, smem, st>>>(a, o, S, Q);
+    if (lam_words(a.L - a.t) == 2) k_search_fast<2, kTaskCap, kTaskFrames, kPMax><<<blocks, 32 * kWarpsPerCta, smem, st>>>(a, o, S, Q);
+    else k_search_fast<kLamWords, kTaskCap, kTaskFrames, kPMax><<<blocks, 32 * kWarpsPerCta, smem, st>>>(a, o, S, Q);
     note_launch();
     return cudaGetLastError();
 }
@@ -1621,8 +1640,8 @@ cudaError_t search_lean(const SearchArgs& a, const SearchOut& o, int lean_blocks
     SearchQueue Q{};
     Q.read_list = a.defer;
     Q.list_count = a.defer_count;
-    if (lam_words(a.L - a.t) == 2) k_search_fast<2><<<fast_blocks, 32 * kWarpsPerCta, fsm, st>>>(a, o, S, Q);
-    else k_search_fast<kLamWords><<<fast_blocks, 32 * kWarpsPerCta, fsm, st>>>(a, o, S, Q);
+    if (lam_words(a.L - a.t) == 2) k_search_fast<2, kTaskCap, kTaskFrames, kPMax><<<fast_blocks, 32 * kWarpsPerCta, fsm, st>>>(a, o, S, Q);
+    else k_search_fast<kLamWords, kTaskCap, kTaskFrames, kPMax><<<fast_blocks, 32 * kWarpsPerCta, fsm, st>>>(a, o, S, Q);
     note_launch();
     return cudaGetLastError();
 }
@@ -1649,8 +1668,8 @@ cudaError_t search_lean_queue(const SearchQueue& q, const SearchBatch* host_batc
         SearchQueue Q{};
         Q.read_list = hbt.a.defer;
         Q.list_count = hbt.a.defer_count;
-        if (two) k_search_fast<2><<<fast_blocks, 32 * kWarpsPerCta, fsm, st>>>(hbt.a, hbt.o, S, Q);
-        else k_search_fast<kLamWords><<<fast_blocks, 32 * kWarpsPerCta, fsm, st>>>(hbt.a, hbt.o, S, Q);
+        if (two) k_search_fast<2, kTaskCap, kTaskFrames, kPMax><<<fast_blocks, 32 * kWarpsPerCta, fsm, st>>>(hbt.a, hbt.o, S, Q);
+        else k_search_fast<kLamWords, kTaskCap, kTaskFrames, kPMax><<<fast_blocks, 32 * kWarpsPerCta, fsm, st>>>(hbt.a, hbt.o, S, Q);
         note_launch();
     }
     return cudaGetLastError();
@@ -1659,6 +1678,36 @@ cudaError_t search_lean_queue(const SearchQueue& q, const SearchBatch* host_batc
 size_t lean_scratch_bytes(int L, int t, int lean_blocks, int fast_blocks, int ebcap) {
     const size_t nwarps = size_t(std::max(lean_blocks * (kLeanThreads / 32), fast_blocks * kWarpsPerCta));
     return scratch_layout(L - t, nwarps, ebcap, nullptr, nullptr);
+}
+
+// Heavy tier: the fast kernel's DFS with 32 times the stack, 4 times the level width and 256
+// levels, over a list of reads (the ones the fast tier could not hold: low-complexity sequence
+// gives thousands of candidates a side).  Its own overflow goes to the wide tier.
+constexpr int kHeavyCap = 16384, kHeavyFrames = 256, kHeavyPMax = 512;
+
+size_t heavy_scratch_bytes(int L, int t, int blocks, int ebcap) {
+    return scratch_layout(L - t, size_t(blocks) * kWarpsPerCta, ebcap, nullptr, nullptr, kHeavyCap, kHeavyFrames,
+                          kHeavyPMax);
+}
+
+cudaError_t search_heavy(const SearchArgs& a, const SearchOut& o, const idx_t* list, const unsigned* count, int blocks,
+                         void* scratch, size_t scratch_bytes, int ebcap, cudaStream_t st) {
+    WarpScratch S;
+    if (scratch_bytes < scratch_layout(a.L - a.t, size_t(blocks) * kWarpsPerCta, ebcap, scratch, &S, kHeavyCap,
+                                       kHeavyFrames, kHeavyPMax))
+        return cudaErrorInvalidValue;
+    const int words = (a.L + 15) / 16;
+    const size_t smem = size_t(words) * 32 * kWarpsPerCta * sizeof(uint32_t);
+    SearchQueue Q{};
+    Q.read_list = list;
+    Q.list_count = count;
+    if (lam_words(a.L - a.t) == 2)
+        k_search_fast<2, kHeavyCap, kHeavyFrames, kHeavyPMax><<<blocks, 32 * kWarpsPerCta, smem, st>>>(a, o, S, Q);
+    else
+        k_search_fast<kLamWords, kHeavyCap, kHeavyFrames, kHeavyPMax><<<blocks, 32 * kWarpsPerCta, smem, st>>>(a, o, S,
+                                                                                                            Q);
+    note_launch();
+    return cudaGetLastError();
 }
 
 size_t queue_scratch_bytes(int L_max, int M_max, size_t nwarps, int ebcap) {
@@ -1675,8 +1724,8 @@ cudaError_t search_fast_queue(const SearchQueue& q, int L_max, int M_max, int bl
     size_t smem = size_t(words) * 32 * kWarpsPerCta * sizeof(uint32_t);
     SearchArgs a{};
     SearchOut o{};
-    if (lam_words(M_max) == 2) k_search_fast<2><<<blocks, 32 * kWarpsPerCta, smem, st>>>(a, o, S, q);
-    else k_search_fast<kLamWords><<<blocks, 32 * kWarpsPerCta, smem, st>>>(a, o, S, q);
+    if (lam_words(M_max) == 2) k_search_fast<2, kTaskCap, kTaskFrames, kPMax><<<blocks, 32 * kWarpsPerCta, smem, st>>>(a, o, S, q);
+    else k_search_fast<kLamWords, kTaskCap, kTaskFrames, kPMax><<<blocks, 32 * kWarpsPerCta, smem, st>>>(a, o, S, q);
     note_launch();
     return cudaGetLastError();
 }

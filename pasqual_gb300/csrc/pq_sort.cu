@@ -176,18 +176,12 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(const uint64_t* __r
         V v[RS_IPT];
         unsigned int lr[RS_IPT];
         int dg[RS_IPT];
-        // all loads of the tile first (independent, in flight together), then the ranking
-        #pragma unroll
-        for (int r = 0; r < RS_IPT; ++r) {
-            const size_t idx = t0 + size_t(warp) * 32 * RS_IPT + r * 32 + lane;
-            const bool valid = idx < end;
-            k[r] = valid ? kin[idx] : 0;
-            v[r] = valid ? vin[idx] : V(0);
-        }
         #pragma unroll
         for (int r = 0; r < RS_IPT; ++r) {
             size_t idx = t0 + size_t(warp) * 32 * RS_IPT + r * 32 + lane;
             bool valid = idx < end;
+            k[r] = valid ? kin[idx] : 0;
+            v[r] = valid ? vin[idx] : V(0);
             int d = valid ? int((k[r] >> shift) & 255) : -1;
             dg[r] = d;
             unsigned peers = __ballot_sync(0xffffffffu, valid);
