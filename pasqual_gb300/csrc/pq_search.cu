@@ -1701,6 +1701,13 @@ cudaError_t search_heavy(const SearchArgs& a, const SearchOut& o, const idx_t* l
     SearchQueue Q{};
     Q.read_list = list;
     Q.list_count = count;
+    // static shared memory (~47 KB) plus the reads: past the 48 KB a launch may take unasked
+    cudaError_t e = lam_words(a.L - a.t) == 2
+        ? cudaFuncSetAttribute(k_search_fast<2, kHeavyCap, kHeavyFrames, kHeavyPMax>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem))
+        : cudaFuncSetAttribute(k_search_fast<kLamWords, kHeavyCap, kHeavyFrames, kHeavyPMax>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
     if (lam_words(a.L - a.t) == 2)
         k_search_fast<2, kHeavyCap, kHeavyFrames, kHeavyPMax><<<blocks, 32 * kWarpsPerCta, smem, st>>>(a, o, S, Q);
     else
