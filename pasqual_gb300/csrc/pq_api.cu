@@ -79,7 +79,7 @@ struct pq_ctx {
     bool sa_ok[2] = {false, false}, fm_ok[2] = {false, false};
     int fm_k[2] = {0, 0};
     DevBuf ktmp, sort_tmp, counts;
-    const uint64_t* sorted_keys[2] = {nullptr, nullptr};   // the last sort's keys, inside sort_tmp
+    const uint32_t* sorted_keys[2] = {nullptr, nullptr};   // the last sort's keys, inside sort_tmp
     uint64_t sort_chunk = 0;                                // suffixes per sort chunk (0: automatic)
 
     // learned index per direction (pq_learned.cu)

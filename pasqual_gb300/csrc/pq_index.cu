@@ -233,13 +233,13 @@ __global__ void k_kmer_codes(const idx_t* __restrict__ sa, const uint8_t* __rest
     }
 }
 
-// k-mer table straight from the sorted suffix keys (first 29 bases + min(length, 29) in the low
-// 6 bits), read in order: a row's k-mer is the key's top 2k bits when the suffix has k bases
-__device__ __forceinline__ uint32_t key_code(uint64_t key, int k) {
-    return int(key & 63) >= k ? uint32_t(key >> (64 - 2 * k)) : 0xffffffffu;
+// k-mer table straight from the sorted suffix keys (first 14 bases in bits 31..4, min(length, 14)
+// in bits 3..0), read in order: a row's k-mer is the key's top 2k bits when the suffix has k bases
+__device__ __forceinline__ uint32_t key_code(uint32_t key, int k) {
+    return int(key & 15) >= k ? (key >> (32 - 2 * k)) : 0xffffffffu;
 }
 
-__global__ void k_kmer_bounds_keys(const uint64_t* __restrict__ key, idx_t n, int k, idx_t* __restrict__ kstart,
+__global__ void k_kmer_bounds_keys(const uint32_t* __restrict__ key, idx_t n, int k, idx_t* __restrict__ kstart,
                                    idx_t* __restrict__ kend) {
     const size_t stride = size_t(gridDim.x) * blockDim.x;
     for (size_t r = size_t(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride) {
@@ -354,12 +354,12 @@ cudaError_t read_counts(const uint8_t* reads, idx_t num_reads, idx_t L, unsigned
 
 cudaError_t build_kmer_table(const idx_t* sa, const uint8_t* reads, idx_t num_reads, idx_t L, int dir,
                              int k, uint32_t* code_tmp, idx_t* kstart, idx_t* kend, cudaStream_t st,
-                             const uint64_t* sorted_keys) {
+                             const uint32_t* sorted_keys) {
     const size_t n = size_t(num_reads) * L;
     const size_t nk = size_t(1) << (2 * k);
     { k_fill_idx<<<grid_for(nk, 256), 256, 0, st>>>(kstart, nk, idx_t(1)); note_launch(); }
     { k_fill_idx<<<grid_for(nk, 256), 256, 0, st>>>(kend, nk, idx_t(0)); note_launch(); }
-    if (n && sorted_keys && k <= 29) {
+    if (n && sorted_keys && k <= kSortKeyBases) {
         { k_kmer_bounds_keys<<<grid_for(n, 256), 256, 0, st>>>(sorted_keys, idx_t(n), k, kstart, kend); note_launch(); }
     } else if (n) {
         { k_kmer_codes<<<grid_for(n, 256), 256, 0, st>>>(sa, reads, idx_t(n), L, dir, k, code_tmp); note_launch(); }

@@ -5,13 +5,17 @@
 // sort on 3-character "triplet" ranks with insertion sort for small buckets; its single-threaded
 // output order is: read-bounded suffix strings, end-of-read lowest, ties by text position.
 //
-// GB300 design: the text is packed 2 bits per base; every suffix gets a 64-bit key made of its
-// first 29 bases (padded with A) and the number of those bases that exist (0..29) -- comparing
-// (padded bases, length) is exactly the end-of-read-lowest order on the first 29 bases.  Keys
-// are radix sorted, each suffix's rank becomes the index of the first row of its group, and
-// prefix doubling sorts by (rank(p), rank(p+h) or "empty" past the read end) for
-// h = 29, 58, 116, ... until h covers the read length.  Every radix pass is stable and the
-// input starts in text order, so equal suffixes stay in text order: the canonical tie-break.
+// GB300 design: the text is packed 2 bits per base; every suffix gets a 32-bit key made of its
+// first 14 bases (padded with A) and the number of those bases that exist (0..14) -- comparing
+// (padded bases, length) is exactly the end-of-read-lowest order on the first 14 bases.  Four
+// stable radix passes sort the keys; every group of equal keys whose suffixes go on past base 14
+// is then finished where it lies (group refinement, below).  At read coverage c such a group
+// holds about c suffixes of one genome locus whatever the key length, so a short key costs the
+// refinement little and halves the radix passes of a 29-base key.  Every radix pass is stable and
+// the input starts in text order, so equal suffixes stay in text order: the canonical tie-break.
+// Inputs the refinement cannot finish (groups larger than its scratch, reads longer than
+// 14 + 256 bases) are sorted by prefix doubling on 29-base 64-bit keys instead: ranks by
+// (rank(p), rank(p+h) or "empty" past the read end) for h = 29, 58, 116, ...
 #include "pq_sort.cuh"
 
 #include <algorithm>
@@ -19,7 +23,21 @@
 
 namespace pq {
 
-constexpr int kHead = 29;                 // bases per initial key
+constexpr int kHead = kSortKeyBases;     // bases per 32-bit head key (4 radix passes)
+constexpr int kWide = 29;                 // bases per 64-bit key (big groups, prefix doubling)
+
+// Key layouts: the bases (padded with A, first base highest) above the number of them that exist.
+//   uint32_t: 14 bases in bits 31..4, length 0..14 in bits 3..0
+//   uint64_t: 29 bases in bits 63..6, length 0..29 in bits 5..0
+template <class K> struct KeyFmt;
+template <> struct KeyFmt<uint32_t> {
+    static constexpr int bases = kHead, len_bits = 4;
+};
+template <> struct KeyFmt<uint64_t> {
+    static constexpr int bases = kWide, len_bits = 6;
+};
+template <class K>
+__device__ __forceinline__ int key_len(K k) { return int(k & K((1u << KeyFmt<K>::len_bits) - 1)); }
 constexpr int RS_THREADS = 256;
 constexpr int RS_IPT = 8;
 constexpr int RS_TILE = RS_THREADS * RS_IPT;
@@ -65,39 +83,49 @@ __device__ __forceinline__ uint64_t window(const uint64_t* __restrict__ pk, size
     return s ? ((a << s) | (b >> (64 - s))) : a;
 }
 
-__global__ void k_init_keys(const uint64_t* __restrict__ pk, size_t n, idx_t L, uint64_t* __restrict__ key,
+// the key of a suffix whose bases start the 64-bit window x and of which m exist (m >= 0)
+template <class K>
+__device__ __forceinline__ K make_key(uint64_t x, int m) {
+    constexpr int B = KeyFmt<K>::bases;
+    const int w = m < B ? m : B;
+    if (w <= 0) return K(0);
+    const uint64_t top = x & (~uint64_t(0) << (64 - 2 * w));
+    return K(K(top >> (64 - 8 * int(sizeof(K)))) | K(w));
+}
+
+template <class K>
+__global__ void k_init_keys(const uint64_t* __restrict__ pk, size_t n, idx_t L, K* __restrict__ key,
                             idx_t* __restrict__ val) {
     const size_t stride = size_t(gridDim.x) * blockDim.x;
     for (size_t p = size_t(blockIdx.x) * blockDim.x + threadIdx.x; p < n; p += stride) {
-        int m = int(L - idx_t(p % L));
-        int w = m < kHead ? m : kHead;
-        uint64_t x = window(pk, p);
-        uint64_t keep = ~uint64_t(0) << (64 - 2 * w);     // w >= 1
-        key[p] = (x & keep) | uint64_t(w);
+        key[p] = make_key<K>(window(pk, p), int(L - idx_t(p % L)));
         val[p] = idx_t(p);
     }
 }
 
 // ------------------------------------------------------------------------------ radix sort
 
-// Digit histograms of all 8 byte positions over the whole key array (order independent): a pass
+// Digit histograms of all byte positions over the whole key array (order independent): a pass
 // whose digit is constant over all keys is the identity and is skipped.
-__global__ void k_digit_hist(const uint64_t* __restrict__ key, size_t n, unsigned long long* __restrict__ hist) {
-    __shared__ unsigned int h[8][256];
-    for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x) (&h[0][0])[i] = 0;
+template <class K>
+__global__ void k_digit_hist(const K* __restrict__ key, size_t n, unsigned long long* __restrict__ hist) {
+    constexpr int D = int(sizeof(K));
+    __shared__ unsigned int h[D][256];
+    for (int i = threadIdx.x; i < D * 256; i += blockDim.x) (&h[0][0])[i] = 0;
     __syncthreads();
     const size_t stride = size_t(gridDim.x) * blockDim.x;
     for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
-        uint64_t k = key[i];
+        const K k = key[i];
         #pragma unroll
-        for (int d = 0; d < 8; ++d) atomicAdd(&h[d][(k >> (8 * d)) & 255], 1u);
+        for (int d = 0; d < D; ++d) atomicAdd(&h[d][(k >> (8 * d)) & 255], 1u);
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x)
+    for (int i = threadIdx.x; i < D * 256; i += blockDim.x)
         if ((&h[0][0])[i]) atomicAdd(&hist[i], (unsigned long long)(&h[0][0])[i]);
 }
 
-__global__ void __launch_bounds__(RS_THREADS) k_rs_upsweep(const uint64_t* __restrict__ key, size_t n, int shift,
+template <class K>
+__global__ void __launch_bounds__(RS_THREADS) k_rs_upsweep(const K* __restrict__ key, size_t n, int shift,
                                                            size_t part, unsigned long long* __restrict__ cnt) {
     __shared__ unsigned int h[RS_WARPS][256];
     const int warp = threadIdx.x >> 5;
@@ -151,12 +179,12 @@ __global__ void k_scan_small(unsigned long long* __restrict__ a, size_t m) {
     }
 }
 
-template <class V>
-__global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(const uint64_t* __restrict__ kin, const V* __restrict__ vin,
-                                                             uint64_t* __restrict__ kout, V* __restrict__ vout, size_t n,
+template <class K, class V>
+__global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(const K* __restrict__ kin, const V* __restrict__ vin,
+                                                             K* __restrict__ kout, V* __restrict__ vout, size_t n,
                                                              int shift, size_t part,
                                                              const unsigned long long* __restrict__ offs) {
-    __shared__ uint64_t sk[RS_TILE];
+    __shared__ K sk[RS_TILE];
     __shared__ V sv[RS_TILE];
     __shared__ unsigned int wcnt[RS_WARPS][256];
     __shared__ unsigned int tcount[256];
@@ -172,7 +200,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(const uint64_t* __r
     for (size_t t0 = beg; t0 < end; t0 += RS_TILE) {
         for (int i = lane; i < 256; i += 32) wcnt[warp][i] = 0;
         __syncwarp();
-        uint64_t k[RS_IPT];
+        K k[RS_IPT];
         V v[RS_IPT];
         unsigned int lr[RS_IPT];
         int dg[RS_IPT];
@@ -180,7 +208,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(const uint64_t* __r
         for (int r = 0; r < RS_IPT; ++r) {
             size_t idx = t0 + size_t(warp) * 32 * RS_IPT + r * 32 + lane;
             bool valid = idx < end;
-            k[r] = valid ? kin[idx] : 0;
+            k[r] = valid ? kin[idx] : K(0);
             v[r] = valid ? vin[idx] : V(0);
             int d = valid ? int((k[r] >> shift) & 255) : -1;
             dg[r] = d;
@@ -236,7 +264,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(const uint64_t* __r
         __syncthreads();
         const int cnt = int(zmin(size_t(RS_TILE), end - t0));
         for (int j = tid; j < cnt; j += RS_THREADS) {
-            uint64_t key = sk[j];
+            const K key = sk[j];
             int d = int((key >> shift) & 255);
             unsigned long long g = base[d] + (unsigned)(j - dstart[d]);
             kout[g] = key;
@@ -259,16 +287,18 @@ size_t radix_tmp_bytes(size_t n) {
     return (size_t(256) * RS_MAX_CTAS + 8 * 256 + 64) * sizeof(unsigned long long);
 }
 
-template <class V>
-int radix_sort_pairs(uint64_t** k0, V** v0, uint64_t** k1, V** v1, size_t n, int lo_bit, int hi_bit, void* tmp,
+template <class K, class V>
+int radix_sort_pairs(K** k0, V** v0, K** k1, V** v1, size_t n, int lo_bit, int hi_bit, void* tmp,
                      size_t tmp_bytes, cudaStream_t st) {
+    constexpr int D = int(sizeof(K));
+    if (hi_bit > 8 * D) hi_bit = 8 * D;
     if (n <= 1) return 0;
     if (tmp_bytes < radix_tmp_bytes(n)) return int(cudaErrorInvalidValue);
     unsigned long long* cnt = reinterpret_cast<unsigned long long*>(tmp);
     unsigned long long* gh = cnt + size_t(256) * RS_MAX_CTAS;
     cudaMemsetAsync(gh, 0, 8 * 256 * sizeof(unsigned long long), st);
-    { k_digit_hist<<<grid_for(n, 256, 4), 256, 0, st>>>(*k0, n, gh); note_launch(); }
-    std::vector<unsigned long long> h(8 * 256);
+    { k_digit_hist<K><<<grid_for(n, 256, 4), 256, 0, st>>>(*k0, n, gh); note_launch(); }
+    std::vector<unsigned long long> h(size_t(D) * 256);
     cudaMemcpyAsync(h.data(), gh, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
     cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return int(e);
@@ -281,19 +311,23 @@ int radix_sort_pairs(uint64_t** k0, V** v0, uint64_t** k1, V** v1, size_t n, int
         for (int b = 0; b < 256; ++b)
             if (h[size_t(d) * 256 + b] == n) trivial = true;
         if (trivial) continue;
-        { k_rs_upsweep<<<unsigned(ctas), RS_THREADS, 0, st>>>(*k0, n, 8 * d, part, cnt); note_launch(); }
+        { k_rs_upsweep<K><<<unsigned(ctas), RS_THREADS, 0, st>>>(*k0, n, 8 * d, part, cnt); note_launch(); }
         { k_scan_small<<<1, 1024, 0, st>>>(cnt, 256 * ctas); note_launch(); }
-        { k_rs_downsweep<V><<<unsigned(ctas), RS_THREADS, 0, st>>>(*k0, *v0, *k1, *v1, n, 8 * d, part, cnt); note_launch(); }
+        { k_rs_downsweep<K, V><<<unsigned(ctas), RS_THREADS, 0, st>>>(*k0, *v0, *k1, *v1, n, 8 * d, part, cnt); note_launch(); }
         std::swap(*k0, *k1);
         std::swap(*v0, *v1);
     }
     return int(cudaGetLastError());
 }
 
-template int radix_sort_pairs<uint32_t>(uint64_t**, uint32_t**, uint64_t**, uint32_t**, size_t, int, int, void*,
-                                        size_t, cudaStream_t);
-template int radix_sort_pairs<uint64_t>(uint64_t**, uint64_t**, uint64_t**, uint64_t**, size_t, int, int, void*,
-                                        size_t, cudaStream_t);
+template int radix_sort_pairs<uint64_t, uint32_t>(uint64_t**, uint32_t**, uint64_t**, uint32_t**, size_t, int, int,
+                                                  void*, size_t, cudaStream_t);
+template int radix_sort_pairs<uint64_t, uint64_t>(uint64_t**, uint64_t**, uint64_t**, uint64_t**, size_t, int, int,
+                                                  void*, size_t, cudaStream_t);
+template int radix_sort_pairs<uint32_t, uint32_t>(uint32_t**, uint32_t**, uint32_t**, uint32_t**, size_t, int, int,
+                                                  void*, size_t, cudaStream_t);
+template int radix_sort_pairs<uint32_t, uint64_t>(uint32_t**, uint64_t**, uint32_t**, uint64_t**, size_t, int, int,
+                                                  void*, size_t, cudaStream_t);
 
 // ------------------------------------------------------------------------------ group ranks
 
@@ -427,52 +461,61 @@ __global__ void k_copy_vals(const V* __restrict__ v, size_t n, idx_t* __restrict
 
 // ------------------------------------------------------------------------------ group refinement
 //
-// After the sort on 29-base keys, every group of equal keys whose suffixes all go on past base 29
+// After the sort on 14-base keys, every group of equal keys whose suffixes all go on past base 14
 // still has to be ordered.  At read coverage c such groups hold about c suffixes, so instead of
 // more whole-array passes each group is finished where it lies: every suffix loads the rest of
 // its bases as W 64-bit words (bases past its end read as A) and the group is sorted by
 // (words, suffix length, position) -- the end-of-read-lowest order, ties by position.  Groups of
-// up to 32 suffixes are sorted by one warp in registers, up to 1024 by one CTA in shared memory,
-// larger ones by one CTA in global scratch; all with bitonic networks.
+// up to 32 and up to 128 suffixes are sorted by one warp in registers (1 or 4 per lane, several
+// groups packed per warp), up to 1024 by one CTA in shared memory, all with bitonic networks;
+// larger ones by a radix sort of their range on the next 29 bases.
 
-constexpr int kRefineMaxWords = 8;          // suffixes up to 29 + 256 bases
+constexpr int kRefineMaxWords = 8;          // suffixes up to 14 + 256 bases
+constexpr int kGroupWarp4 = 128;            // largest group sorted by one warp, 4 per lane
 constexpr int kGroupCta = 1024;             // largest group sorted in shared memory
 
+// Group classes: 0 = 2..32 suffixes, 1 = 33..128, 2 = 129..1024 (entries (start << 24) | size),
+// 3 = larger (start, size pairs).
 struct GroupLists {
-    unsigned long long* small;              // (start << 24) | size, 2 <= size <= 32
-    unsigned long long* mid;                // (start << 24) | size, 33 <= size <= 1024
-    unsigned long long* big;                // start, size pairs
-    unsigned long long* counts;             // [3]
-    size_t cap_small, cap_mid, cap_big;
+    unsigned long long* list[4];
+    unsigned long long* counts;             // [4]
+    size_t cap[4];                          // entries (pairs for class 3)
 };
+
+__device__ __forceinline__ int group_class(size_t m) {
+    if (m < 2) return -1;
+    if (m <= 32) return 0;
+    if (m <= size_t(kGroupWarp4)) return 1;
+    return m <= size_t(kGroupCta) ? 2 : 3;
+}
 
 // One CTA per tile of 4096 sorted keys: group heads are marked in a shared bit mask, each head's
 // group ends at the next marked bit (read from the mask; only a group running past the tile end is
-// followed in global memory), and the groups longer than their 29-base key are listed by size.
+// followed in global memory), and the groups longer than their key's bases are listed by size.
 // List slots are taken with one atomic per list per tile, after a block-wide prefix of the counts.
 constexpr int kGlTile = 4096;
 constexpr int kGlThreads = 256;
 constexpr int kGlPer = kGlTile / kGlThreads;      // positions per thread (j = tid + 256 i)
 
-__device__ __forceinline__ void block_scan3(unsigned (&c)[3], unsigned (&excl)[3], unsigned (*wsum)[3],
+__device__ __forceinline__ void block_scan4(unsigned (&c)[4], unsigned (&excl)[4], unsigned (*wsum)[4],
                                             unsigned* tot) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    unsigned x[3] = {c[0], c[1], c[2]};
+    unsigned x[4] = {c[0], c[1], c[2], c[3]};
     #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         #pragma unroll
-        for (int q = 0; q < 3; ++q) {
+        for (int q = 0; q < 4; ++q) {
             const unsigned y = __shfl_up_sync(0xffffffffu, x[q], o);
             if (lane >= o) x[q] += y;
         }
     }
     if (lane == 31) {
         #pragma unroll
-        for (int q = 0; q < 3; ++q) wsum[warp][q] = x[q];
+        for (int q = 0; q < 4; ++q) wsum[warp][q] = x[q];
     }
     __syncthreads();
     #pragma unroll
-    for (int q = 0; q < 3; ++q) {
+    for (int q = 0; q < 4; ++q) {
         unsigned before = 0, all = 0;
         for (int w = 0; w < kGlThreads / 32; ++w) {
             before += w < warp ? wsum[w][q] : 0u;
@@ -483,11 +526,12 @@ __device__ __forceinline__ void block_scan3(unsigned (&c)[3], unsigned (&excl)[3
     }
 }
 
-__global__ void __launch_bounds__(kGlThreads) k_group_lists(const uint64_t* __restrict__ key, size_t n, GroupLists G,
+template <class K>
+__global__ void __launch_bounds__(kGlThreads) k_group_lists(const K* __restrict__ key, size_t n, GroupLists G,
                                                            size_t base) {
     __shared__ uint32_t hm[kGlTile / 32 + 1];
-    __shared__ unsigned wsum[kGlThreads / 32][3];
-    __shared__ unsigned long long sbase[3];
+    __shared__ unsigned wsum[kGlThreads / 32][4];
+    __shared__ unsigned long long sbase[4];
     const int lane = threadIdx.x & 31;
     for (size_t t0 = size_t(blockIdx.x) * kGlTile; t0 < n; t0 += size_t(gridDim.x) * kGlTile) {
         for (int j = threadIdx.x; j < kGlTile; j += kGlThreads) {
@@ -499,15 +543,15 @@ __global__ void __launch_bounds__(kGlThreads) k_group_lists(const uint64_t* __re
         if (threadIdx.x == 0) hm[kGlTile / 32] = 1u;       // sentinel: the tile end
         __syncthreads();
         uint32_t mm[kGlPer];
-        unsigned c[3] = {0, 0, 0};
+        unsigned c[4] = {0, 0, 0, 0};
         #pragma unroll
         for (int q = 0; q < kGlPer; ++q) {
             const int j = threadIdx.x + kGlThreads * q;
             const size_t i = t0 + j;
             size_t m = 0;
             if ((hm[j >> 5] >> (j & 31)) & 1u) {
-                const uint64_t k = key[i];
-                if ((k & 63) == uint64_t(kHead)) {     // suffix longer than its 29-base key
+                const K k = key[i];
+                if (key_len<K>(k) == KeyFmt<K>::bases) {     // suffix longer than its key
                     int w;
                     uint32_t bits;
                     if (j + 1 < kGlTile) {
@@ -529,34 +573,37 @@ __global__ void __launch_bounds__(kGlThreads) k_group_lists(const uint64_t* __re
                 }
             }
             mm[q] = uint32_t(m);
-            c[0] += (m >= 2 && m <= 32) ? 1u : 0u;
-            c[1] += (m > 32 && m <= size_t(kGroupCta)) ? 1u : 0u;
-            c[2] += (m > size_t(kGroupCta)) ? 1u : 0u;
+            const int cl = group_class(m);
+            #pragma unroll
+            for (int z = 0; z < 4; ++z) c[z] += cl == z ? 1u : 0u;
         }
-        unsigned excl[3], tot[3];
-        block_scan3(c, excl, wsum, tot);
+        unsigned excl[4], tot[4];
+        block_scan4(c, excl, wsum, tot);
         if (threadIdx.x == 0) {
             #pragma unroll
-            for (int q = 0; q < 3; ++q) sbase[q] = tot[q] ? atomicAdd(&G.counts[q], (unsigned long long)tot[q]) : 0ull;
+            for (int q = 0; q < 4; ++q) sbase[q] = tot[q] ? atomicAdd(&G.counts[q], (unsigned long long)tot[q]) : 0ull;
         }
         __syncthreads();
-        unsigned long long at[3] = {sbase[0] + excl[0], sbase[1] + excl[1], sbase[2] + excl[2]};
+        unsigned long long at[4] = {sbase[0] + excl[0], sbase[1] + excl[1], sbase[2] + excl[2], sbase[3] + excl[3]};
         #pragma unroll
         for (int q = 0; q < kGlPer; ++q) {
             const size_t i = base + t0 + threadIdx.x + kGlThreads * q;
             const size_t m = mm[q];
-            if (m >= 2 && m <= 32) {
-                if (at[0] < G.cap_small) G.small[at[0]] = (uint64_t(i) << 24) | m;
-                ++at[0];
-            } else if (m > 32 && m <= size_t(kGroupCta)) {
-                if (at[1] < G.cap_mid) G.mid[at[1]] = (uint64_t(i) << 24) | m;
-                ++at[1];
-            } else if (m > size_t(kGroupCta)) {
-                if (at[2] < G.cap_big) {
-                    G.big[2 * at[2]] = i;
-                    G.big[2 * at[2] + 1] = m;
+            const int cl = group_class(m);
+            if (cl == 3) {
+                if (at[3] < G.cap[3]) {
+                    G.list[3][2 * at[3]] = i;
+                    G.list[3][2 * at[3] + 1] = m;
                 }
-                ++at[2];
+                ++at[3];
+            } else if (cl >= 0) {
+                #pragma unroll
+                for (int z = 0; z < 3; ++z) {
+                    if (cl == z) {
+                        if (at[z] < G.cap[z]) G.list[z][at[z]] = (uint64_t(i) << 24) | m;
+                        ++at[z];
+                    }
+                }
             }
         }
         __syncthreads();
@@ -589,14 +636,34 @@ __device__ __forceinline__ bool tuple_less(const uint64_t a[W], uint64_t alen, u
     return apos < bpos;
 }
 
-// Groups of 2..32 suffixes, several per warp: a warp takes 8 list entries at a time and packs
-// consecutive ones into its 32 lanes while they fit; one 32-lane bitonic network on
-// (segment, bases from `from` on, length, position) then sorts every packed group in place (each
-// segment keeps its lanes, since segments are numbered in lane order).
+// Groups of 2..32E suffixes, several per warp: a warp takes 8 list entries at a time and packs
+// consecutive ones into its 32E slots (slot e * 32 + lane is register set e of that lane) while
+// they fit; one bitonic network over the 32E slots on (segment, bases from `from` on, length,
+// position) then sorts every packed group in place (each segment keeps its slots, since segments
+// are numbered in slot order and empty slots sort last).  Distances below 32 exchange by shuffle,
+// larger ones swap registers within a lane.  Length and position travel as one word, length in
+// the top 16 bits (read length <= 65535, positions < 2^48).
 template <int W>
+struct RefineItem {
+    uint64_t w[W];
+    uint64_t tail;                              // (length << 48) | position
+    int seg;
+};
+
+template <int W>
+__device__ __forceinline__ bool item_less(const RefineItem<W>& a, const RefineItem<W>& b) {
+    if (a.seg != b.seg) return a.seg < b.seg;
+    #pragma unroll
+    for (int j = 0; j < W; ++j)
+        if (a.w[j] != b.w[j]) return a.w[j] < b.w[j];
+    return a.tail < b.tail;
+}
+
+template <int W, int E>
 __global__ void k_refine_warp(const unsigned long long* __restrict__ list, const unsigned long long* __restrict__ cnt,
                               const uint64_t* __restrict__ pk, idx_t L, idx_t* __restrict__ val, int from) {
     constexpr int kChunk = 8;
+    constexpr int N = 32 * E;
     const int lane = threadIdx.x & 31;
     const size_t warp = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const size_t nwarps = (size_t(gridDim.x) * blockDim.x) >> 5;
@@ -605,56 +672,80 @@ __global__ void k_refine_warp(const unsigned long long* __restrict__ list, const
         const unsigned long long mine = (lane < kChunk && c0 + lane < groups) ? list[c0 + lane] : 0ull;
         int next = 0;
         while (next < kChunk) {
-            // consecutive entries next .. next + taken - 1 fit in 32 lanes
-            int taken = 0, total = 0, seg = 255, off = 0;
-            size_t start = 0;
-            for (int e = next; e < kChunk; ++e) {
-                const unsigned long long x = __shfl_sync(0xffffffffu, mine, e);
+            // consecutive entries next .. next + taken - 1 fit in N slots
+            int taken = 0, total = 0;
+            int seg[E];
+            size_t at[E];
+            #pragma unroll
+            for (int e = 0; e < E; ++e) {
+                seg[e] = 255;
+                at[e] = 0;
+            }
+            for (int q = next; q < kChunk; ++q) {
+                const unsigned long long x = __shfl_sync(0xffffffffu, mine, q);
                 const int m = int(x & 0xffffff);
-                if (m == 0 || total + m > 32) break;
-                if (lane >= total && lane < total + m) {
-                    seg = e - next;
-                    off = lane - total;
-                    start = size_t(x >> 24);
+                if (m == 0 || total + m > N) break;
+                #pragma unroll
+                for (int e = 0; e < E; ++e) {
+                    const int slot = e * 32 + lane;
+                    if (slot >= total && slot < total + m) {
+                        seg[e] = q - next;
+                        at[e] = size_t(x >> 24) + size_t(slot - total);
+                    }
                 }
                 total += m;
                 ++taken;
             }
             if (taken == 0) break;
-            uint64_t w[W], len, pos;
-            if (lane < total) {
-                pos = uint64_t(val[start + off]);
-                len = uint64_t(L - idx_t(pos % L));
-                suffix_words<W>(pk, size_t(pos), int(len), from, w);
-            } else {
-                #pragma unroll
-                for (int j = 0; j < W; ++j) w[j] = ~uint64_t(0);
-                len = ~uint64_t(0);
-                pos = ~uint64_t(0);
-            }
-            int sg = seg;
+            RefineItem<W> it[E];
             #pragma unroll
-            for (int k = 2; k <= 32; k <<= 1) {
+            for (int e = 0; e < E; ++e) {
+                it[e].seg = seg[e];
+                if (seg[e] != 255) {
+                    const uint64_t pos = uint64_t(val[at[e]]);
+                    const uint64_t len = uint64_t(L - idx_t(pos % L));
+                    suffix_words<W>(pk, size_t(pos), int(len), from, it[e].w);
+                    it[e].tail = (len << 48) | pos;
+                } else {
+                    #pragma unroll
+                    for (int j = 0; j < W; ++j) it[e].w[j] = ~uint64_t(0);
+                    it[e].tail = ~uint64_t(0);
+                }
+            }
+            #pragma unroll
+            for (int k = 2; k <= N; k <<= 1) {
                 #pragma unroll
                 for (int j = k >> 1; j > 0; j >>= 1) {
-                    uint64_t ow[W];
-                    #pragma unroll
-                    for (int q = 0; q < W; ++q) ow[q] = __shfl_xor_sync(0xffffffffu, w[q], j);
-                    const uint64_t olen = __shfl_xor_sync(0xffffffffu, len, j);
-                    const uint64_t opos = __shfl_xor_sync(0xffffffffu, pos, j);
-                    const int osg = __shfl_xor_sync(0xffffffffu, sg, j);
-                    const bool keep_min = ((lane & j) == 0) == ((lane & k) == 0);
-                    const bool other_less = osg != sg ? osg < sg : tuple_less<W>(ow, olen, opos, w, len, pos);
-                    if (keep_min == other_less) {
+                    if (j >= 32) {
                         #pragma unroll
-                        for (int q = 0; q < W; ++q) w[q] = ow[q];
-                        len = olen;
-                        pos = opos;
-                        sg = osg;
+                        for (int e = 0; e < E; ++e) {
+                            const int f = e ^ (j >> 5);
+                            if (f > e) {
+                                const bool asc = ((e * 32 + lane) & k) == 0;
+                                if (item_less<W>(it[f], it[e]) == asc) {
+                                    const RefineItem<W> t = it[e];
+                                    it[e] = it[f];
+                                    it[f] = t;
+                                }
+                            }
+                        }
+                    } else {
+                        #pragma unroll
+                        for (int e = 0; e < E; ++e) {
+                            RefineItem<W> o;
+                            #pragma unroll
+                            for (int q = 0; q < W; ++q) o.w[q] = __shfl_xor_sync(0xffffffffu, it[e].w[q], j);
+                            o.tail = __shfl_xor_sync(0xffffffffu, it[e].tail, j);
+                            o.seg = __shfl_xor_sync(0xffffffffu, it[e].seg, j);
+                            const bool keep_min = ((lane & j) == 0) == (((e * 32 + lane) & k) == 0);
+                            if (keep_min == item_less<W>(o, it[e])) it[e] = o;
+                        }
                     }
                 }
             }
-            if (lane < total) val[start + off] = idx_t(pos);
+            #pragma unroll
+            for (int e = 0; e < E; ++e)
+                if (seg[e] != 255) val[at[e]] = idx_t(it[e].tail & ((uint64_t(1) << 48) - 1));
             next += taken;
         }
     }
@@ -739,43 +830,48 @@ __global__ void k_refine_cta(const unsigned long long* __restrict__ list, const 
     }
 }
 
-// keys of a range of suffixes on their bases [off, off + 29): those bases (padded) and how many of
-// them exist (0..29), as the initial keys
+// 64-bit keys of a range of suffixes on their bases [off, off + 29): those bases (padded) and how
+// many of them exist (0..29)
 __global__ void k_range_keys(const uint64_t* __restrict__ pk, const idx_t* __restrict__ val, size_t m, idx_t L,
                              int off, uint64_t* __restrict__ key, idx_t* __restrict__ out) {
     const size_t stride = size_t(gridDim.x) * blockDim.x;
     for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < m; i += stride) {
         const idx_t p = val[i];
         const int rem = int(L - p % L) - off;
-        const int w = rem < kHead ? (rem > 0 ? rem : 0) : kHead;
-        key[i] = w ? ((window(pk, size_t(p) + off) & (~uint64_t(0) << (64 - 2 * w))) | uint64_t(w)) : 0;
+        key[i] = rem > 0 ? make_key<uint64_t>(window(pk, size_t(p) + off), rem) : 0;
         out[i] = p;
     }
 }
 
+// the groups of classes 0..2 (c: their counts)
 template <int W>
-static void refine_small_mid(const GroupLists& G, unsigned long long n_small, unsigned long long n_mid,
-                             const uint64_t* pk, idx_t L, idx_t* val, int off, cudaStream_t st) {
-    if (n_small) {
-        unsigned g = unsigned(std::min<unsigned long long>((n_small + 63) / 64, 152ull * 64));
-        { k_refine_warp<W><<<g, 256, 0, st>>>(G.small, G.counts + 0, pk, L, val, off); note_launch(); }
+static void refine_small_mid(const GroupLists& G, const unsigned long long* c, const uint64_t* pk, idx_t L,
+                             idx_t* val, int off, cudaStream_t st) {
+    if (c[0]) {
+        unsigned g = unsigned(std::min<unsigned long long>((c[0] + 63) / 64, 152ull * 64));
+        { k_refine_warp<W, 1><<<g, 256, 0, st>>>(G.list[0], G.counts + 0, pk, L, val, off); note_launch(); }
     }
-    if (n_mid) {
+    if (c[1]) {
+        unsigned g = unsigned(std::min<unsigned long long>((c[1] + 15) / 16, 152ull * 64));
+        { k_refine_warp<W, 4><<<g, 256, 0, st>>>(G.list[1], G.counts + 1, pk, L, val, off); note_launch(); }
+    }
+    if (c[2]) {
         const size_t smem = size_t(W + 2) * kGroupCta * sizeof(uint64_t);
         cudaFuncSetAttribute(k_refine_cta<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-        unsigned g = unsigned(std::min<unsigned long long>(n_mid, 152ull * 8));
-        { k_refine_cta<W><<<g, 512, smem, st>>>(G.mid, G.counts + 1, pk, L, val, off); note_launch(); }
+        unsigned g = unsigned(std::min<unsigned long long>(c[2], 152ull * 8));
+        { k_refine_cta<W><<<g, 512, smem, st>>>(G.list[2], G.counts + 2, pk, L, val, off); note_launch(); }
     }
 }
 
 // Groups of up to 1024 suffixes are finished in place by the warp and CTA kernels.  A larger group
 // (low-complexity or highly repeated sequence) gets a device-wide radix sort of its range on the
-// next 29 bases, and its subgroups are finished the same way, 29 bases further on each time.
+// next 29 bases (64-bit keys), and its subgroups are finished the same way, 29 bases further on
+// each time.
 template <int W>
-static int refine_groups_w(const GroupLists& G, unsigned long long n_small, unsigned long long n_mid,
+static int refine_groups_w(const GroupLists& G, const unsigned long long* c0,
                            const std::vector<unsigned long long>& big, const uint64_t* pk, idx_t L, idx_t* val,
                            uint64_t* cols, size_t cols_cap, void* rtmp, size_t rtmp_bytes, cudaStream_t st) {
-    refine_small_mid<W>(G, n_small, n_mid, pk, L, val, kHead, st);
+    refine_small_mid<W>(G, c0, pk, L, val, kHead, st);
     struct Item {
         size_t start, m;
         int off;
@@ -795,66 +891,71 @@ static int refine_groups_w(const GroupLists& G, unsigned long long n_small, unsi
         idx_t* va = reinterpret_cast<idx_t*>(cols + 2 * kw);
         idx_t* vb = reinterpret_cast<idx_t*>(cols + 2 * kw + vw);
         { k_range_keys<<<grid_for(m, 256), 256, 0, st>>>(pk, val + it.start, m, L, it.off, ka, va); note_launch(); }
-        int rc = radix_sort_pairs<idx_t>(&ka, &va, &kb, &vb, m, 0, 64, rtmp, rtmp_bytes, st);
+        int rc = radix_sort_pairs<uint64_t, idx_t>(&ka, &va, &kb, &vb, m, 0, 64, rtmp, rtmp_bytes, st);
         if (rc) return rc;
         { k_copy_vals<idx_t><<<grid_for(m, 256), 256, 0, st>>>(va, m, val + it.start); note_launch(); }
-        if (it.off + kHead >= int(L)) continue;          // every suffix is now fully compared
-        cudaMemsetAsync(G.counts, 0, 3 * sizeof(unsigned long long), st);
-        { k_group_lists<<<unsigned(std::min<size_t>((m + kGlTile - 1) / kGlTile, size_t(152) * 64)), 256, 0, st>>>(
+        if (it.off + kWide >= int(L)) continue;          // every suffix is now fully compared
+        cudaMemsetAsync(G.counts, 0, 4 * sizeof(unsigned long long), st);
+        { k_group_lists<uint64_t><<<unsigned(std::min<size_t>((m + kGlTile - 1) / kGlTile, size_t(152) * 64)), 256, 0, st>>>(
               ka, m, G, it.start); note_launch(); }
-        unsigned long long c[3];
+        unsigned long long c[4];
         cudaMemcpyAsync(c, G.counts, sizeof c, cudaMemcpyDeviceToHost, st);
         cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return int(e);
-        if (c[0] > G.cap_small || c[1] > G.cap_mid || c[2] > G.cap_big) return -1;
-        refine_small_mid<W>(G, c[0], c[1], pk, L, val, it.off + kHead, st);
-        if (c[2]) {
-            sub.resize(2 * c[2]);
-            cudaMemcpyAsync(sub.data(), G.big, sub.size() * 8, cudaMemcpyDeviceToHost, st);
+        for (int z = 0; z < 4; ++z)
+            if (c[z] > G.cap[z]) return -1;
+        refine_small_mid<W>(G, c, pk, L, val, it.off + kWide, st);
+        if (c[3]) {
+            sub.resize(2 * c[3]);
+            cudaMemcpyAsync(sub.data(), G.list[3], sub.size() * 8, cudaMemcpyDeviceToHost, st);
             e = cudaStreamSynchronize(st);
             if (e != cudaSuccess) return int(e);
             for (size_t i = 0; i + 1 < sub.size(); i += 2)
-                work.push_back({size_t(sub[i]), size_t(sub[i + 1]), it.off + kHead});
+                work.push_back({size_t(sub[i]), size_t(sub[i + 1]), it.off + kWide});
         }
     }
     return int(cudaGetLastError());
 }
 
-static int refine_groups(const uint64_t* key, idx_t* val, size_t n, idx_t L, const uint64_t* pk, uint64_t* lists_mem,
+// lists_mem holds the four group lists: (n/2 + n/33 + n/129 + 2 n/1025 + 5) 64-bit entries,
+// under 0.55 n
+static int refine_groups(const uint32_t* key, idx_t* val, size_t n, idx_t L, const uint64_t* pk, uint64_t* lists_mem,
                          uint64_t* cols, size_t cols_cap, unsigned long long* counters, void* rtmp, size_t rtmp_bytes,
                          cudaStream_t st) {
     const int W = int((2 * (size_t(L) - kHead) + 63) / 64);
     if (W < 1 || W > kRefineMaxWords) return -1;
     GroupLists G;
-    G.cap_small = n / 2 + 1;
-    G.cap_mid = n / 33 + 1;
-    G.cap_big = n / 1025 + 1;
-    G.small = reinterpret_cast<unsigned long long*>(lists_mem);
-    G.mid = G.small + G.cap_small;
-    G.big = G.mid + G.cap_mid;
+    G.cap[0] = n / 2 + 1;
+    G.cap[1] = n / 33 + 1;
+    G.cap[2] = n / (kGroupWarp4 + 1) + 1;
+    G.cap[3] = n / (kGroupCta + 1) + 1;
+    G.list[0] = reinterpret_cast<unsigned long long*>(lists_mem);
+    G.list[1] = G.list[0] + G.cap[0];
+    G.list[2] = G.list[1] + G.cap[1];
+    G.list[3] = G.list[2] + G.cap[2];
     G.counts = counters;
-    cudaMemsetAsync(counters, 0, 3 * sizeof(unsigned long long), st);
-    { k_group_lists<<<unsigned(std::min<size_t>((n + kGlTile - 1) / kGlTile, size_t(152) * 64)), 256, 0, st>>>(
+    cudaMemsetAsync(counters, 0, 4 * sizeof(unsigned long long), st);
+    { k_group_lists<uint32_t><<<unsigned(std::min<size_t>((n + kGlTile - 1) / kGlTile, size_t(152) * 64)), 256, 0, st>>>(
           key, n, G, 0); note_launch(); }
-    unsigned long long c[3];
+    unsigned long long c[4];
     cudaMemcpyAsync(c, counters, sizeof c, cudaMemcpyDeviceToHost, st);
     cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return int(e);
-    std::vector<unsigned long long> big(2 * c[2]);
-    if (c[2]) {
-        cudaMemcpyAsync(big.data(), G.big, big.size() * 8, cudaMemcpyDeviceToHost, st);
+    std::vector<unsigned long long> big(2 * c[3]);
+    if (c[3]) {
+        cudaMemcpyAsync(big.data(), G.list[3], big.size() * 8, cudaMemcpyDeviceToHost, st);
         e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) return int(e);
     }
     switch (W) {
-        case 1: return refine_groups_w<1>(G, c[0], c[1], big, pk, L, val, cols, cols_cap, rtmp, rtmp_bytes, st);
-        case 2: return refine_groups_w<2>(G, c[0], c[1], big, pk, L, val, cols, cols_cap, rtmp, rtmp_bytes, st);
-        case 3: return refine_groups_w<3>(G, c[0], c[1], big, pk, L, val, cols, cols_cap, rtmp, rtmp_bytes, st);
-        case 4: return refine_groups_w<4>(G, c[0], c[1], big, pk, L, val, cols, cols_cap, rtmp, rtmp_bytes, st);
-        case 5: return refine_groups_w<5>(G, c[0], c[1], big, pk, L, val, cols, cols_cap, rtmp, rtmp_bytes, st);
-        case 6: return refine_groups_w<6>(G, c[0], c[1], big, pk, L, val, cols, cols_cap, rtmp, rtmp_bytes, st);
-        case 7: return refine_groups_w<7>(G, c[0], c[1], big, pk, L, val, cols, cols_cap, rtmp, rtmp_bytes, st);
-        default: return refine_groups_w<8>(G, c[0], c[1], big, pk, L, val, cols, cols_cap, rtmp, rtmp_bytes, st);
+        case 1: return refine_groups_w<1>(G, c, big, pk, L, val, cols, cols_cap, rtmp, rtmp_bytes, st);
+        case 2: return refine_groups_w<2>(G, c, big, pk, L, val, cols, cols_cap, rtmp, rtmp_bytes, st);
+        case 3: return refine_groups_w<3>(G, c, big, pk, L, val, cols, cols_cap, rtmp, rtmp_bytes, st);
+        case 4: return refine_groups_w<4>(G, c, big, pk, L, val, cols, cols_cap, rtmp, rtmp_bytes, st);
+        case 5: return refine_groups_w<5>(G, c, big, pk, L, val, cols, cols_cap, rtmp, rtmp_bytes, st);
+        case 6: return refine_groups_w<6>(G, c, big, pk, L, val, cols, cols_cap, rtmp, rtmp_bytes, st);
+        case 7: return refine_groups_w<7>(G, c, big, pk, L, val, cols, cols_cap, rtmp, rtmp_bytes, st);
+        default: return refine_groups_w<8>(G, c, big, pk, L, val, cols, cols_cap, rtmp, rtmp_bytes, st);
     }
 }
 
@@ -870,7 +971,7 @@ size_t suffix_sort_tmp_bytes(size_t n) {
 }
 
 int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa, void* tmp, size_t tmp_bytes,
-                cudaStream_t st, const uint64_t** keys_out) {
+                cudaStream_t st, const uint32_t** keys_out) {
     if (keys_out) *keys_out = nullptr;
     const size_t n = size_t(num_reads) * size_t(L);
     if (n == 0) return 0;
@@ -892,33 +993,40 @@ int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa
 
     idx_t* const vb0 = vb;                 // followed by rank in memory
     { k_pack_text<<<grid_for(nwords, 256), 256, 0, st>>>(reads, n, idx_t(L), dir, nwords, pk); note_launch(); }
-    { k_init_keys<<<grid_for(n, 256), 256, 0, st>>>(pk, n, idx_t(L), ka, va); note_launch(); }
-    int rc = radix_sort_pairs<idx_t>(&ka, &va, &kb, &vb, n, 0, 64, rtmp, radix_tmp_bytes(n), st);
+    // 32-bit head keys in the two 64-bit key buffers
+    uint32_t* ha = reinterpret_cast<uint32_t*>(ka);
+    uint32_t* hb = reinterpret_cast<uint32_t*>(kb);
+    { k_init_keys<uint32_t><<<grid_for(n, 256), 256, 0, st>>>(pk, n, idx_t(L), ha, va); note_launch(); }
+    int rc = radix_sort_pairs<uint32_t, idx_t>(&ha, &va, &hb, &vb, n, 0, 32, rtmp, radix_tmp_bytes(n), st);
     if (rc) return rc;
     if (size_t(L) <= size_t(kHead)) {   // every suffix fits in its key: already in final order
         { k_copy_vals<idx_t><<<grid_for(n, 256), 256, 0, st>>>(va, n, sa); note_launch(); }
-        if (keys_out) *keys_out = ka;
+        if (keys_out) *keys_out = ha;
         return int(cudaGetLastError());
     }
     {
-        // finish the groups where they lie; lists go to kb, big-group scratch to the free value
-        // buffer (and rank behind it when that buffer is the second one: the sorted values may have
-        // ended in either, depending on how many radix passes ran)
+        // finish the groups where they lie; lists go to the free key buffer, big-group scratch to
+        // the free value buffer (and rank behind it when that buffer is the second one: the sorted
+        // values may have ended in either, depending on how many radix passes ran)
         uint64_t* cols = reinterpret_cast<uint64_t*>(vb);
         const size_t cols_cap = (al(n * sizeof(idx_t)) + (vb == vb0 ? al(n * sizeof(uint32_t)) : 0)) / sizeof(uint64_t);
-        rc = refine_groups(ka, va, n, idx_t(L), pk, kb, cols, cols_cap, tcnt, rtmp, radix_tmp_bytes(n), st);
+        rc = refine_groups(ha, va, n, idx_t(L), pk, reinterpret_cast<uint64_t*>(hb), cols, cols_cap, tcnt, rtmp,
+                           radix_tmp_bytes(n), st);
         if (rc > 0) return rc;
         if (rc == 0) {   // the refinement permutes suffixes within groups of equal keys only
             { k_copy_vals<idx_t><<<grid_for(n, 256), 256, 0, st>>>(va, n, sa); note_launch(); }
-            if (keys_out) *keys_out = ka;
+            if (keys_out) *keys_out = ha;
             return int(cudaGetLastError());
         }
-        // a group too large for the scratch (or reads longer than 285 bases): prefix doubling
-        { k_init_keys<<<grid_for(n, 256), 256, 0, st>>>(pk, n, idx_t(L), ka, va); note_launch(); }
-        rc = radix_sort_pairs<idx_t>(&ka, &va, &kb, &vb, n, 0, 64, rtmp, radix_tmp_bytes(n), st);
+        // a group too large for the scratch (or reads longer than 270 bases): prefix doubling on
+        // 29-base keys
+        ka = reinterpret_cast<uint64_t*>(ha);
+        kb = reinterpret_cast<uint64_t*>(hb);
+        { k_init_keys<uint64_t><<<grid_for(n, 256), 256, 0, st>>>(pk, n, idx_t(L), ka, va); note_launch(); }
+        rc = radix_sort_pairs<uint64_t, idx_t>(&ka, &va, &kb, &vb, n, 0, 64, rtmp, radix_tmp_bytes(n), st);
         if (rc) return rc;
     }
-    for (size_t h = kHead;; h *= 2) {
+    for (size_t h = kWide;; h *= 2) {
         { k_head_tiles<<<unsigned(tiles), HT_THREADS, 0, st>>>(ka, n, tmax, tcnt); note_launch(); }
         { k_head_carry<<<1, 1024, 0, st>>>(tmax, tcnt, tiles, groups); note_launch(); }
         { k_head_apply<idx_t><<<unsigned(tiles), HT_THREADS, 0, st>>>(ka, kb, va, n, tmax, rank); note_launch(); }
@@ -931,7 +1039,7 @@ int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa
         { k_second_keys<idx_t><<<grid_for(n, 256), 256, 0, st>>>(ka, va, n, idx_t(L), h, rank); note_launch(); }
         int bits = 1;
         while ((size_t(1) << bits) <= n + 1) ++bits;
-        rc = radix_sort_pairs<idx_t>(&ka, &va, &kb, &vb, n, 0, 32 + bits, rtmp, radix_tmp_bytes(n), st);
+        rc = radix_sort_pairs<uint64_t, idx_t>(&ka, &va, &kb, &vb, n, 0, 32 + bits, rtmp, radix_tmp_bytes(n), st);
         if (rc) return rc;
     }
     { k_copy_vals<idx_t><<<grid_for(n, 256), 256, 0, st>>>(va, n, sa); note_launch(); }
@@ -1022,20 +1130,17 @@ __global__ void __launch_bounds__(256) k_chunk_write(const uint64_t* __restrict_
 
 template <class V>
 __global__ void k_init_keys_list(const uint64_t* __restrict__ pk, const V* __restrict__ list, size_t m, idx_t L,
-                                 uint64_t* __restrict__ key) {
+                                 uint32_t* __restrict__ key) {
     const size_t stride = size_t(gridDim.x) * blockDim.x;
     for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < m; i += stride) {
         const size_t p = size_t(list[i]);
-        const int len = int(L - idx_t(p % L));
-        const int w = len < kHead ? len : kHead;
-        const uint64_t keep = ~uint64_t(0) << (64 - 2 * w);
-        key[i] = (window(pk, p) & keep) | uint64_t(w);
+        key[i] = make_key<uint32_t>(window(pk, p), int(L - idx_t(p % L)));
     }
 }
 
 static size_t chunk_parts(size_t n, size_t cap, size_t (&b)[9]) {
     const size_t ntiles = (n + kCkTile - 1) / kCkTile;
-    b[0] = cap * sizeof(uint64_t);                    // ka
+    b[0] = cap * sizeof(uint64_t);                    // ka (32-bit head keys; 64-bit for big groups)
     b[1] = cap * sizeof(uint64_t);                    // kb (also the group lists)
     b[2] = cap * sizeof(idx_t);                       // va
     b[3] = cap * sizeof(idx_t);                       // vb (with rank: big-group columns)
@@ -1097,18 +1202,19 @@ int suffix_sort_chunked(const uint8_t* reads, idx_t num_reads, int L, int dir, i
             { k_chunk_count<<<unsigned(ntiles), 256, 0, st>>>(pk, n, idx_t(L), lo, hi, tcnt); note_launch(); }
             { k_scan_small<<<1, 1024, 0, st>>>(tcnt, ntiles); note_launch(); }
             { k_chunk_write<idx_t><<<unsigned(ntiles), 256, 0, st>>>(pk, n, idx_t(L), lo, hi, tcnt, va0); note_launch(); }
-            { k_init_keys_list<idx_t><<<grid_for(m, 256), 256, 0, st>>>(pk, va0, m, idx_t(L), ka0); note_launch(); }
-            uint64_t* ka = ka0;
-            uint64_t* kb = kb0;
+            uint32_t* ka = reinterpret_cast<uint32_t*>(ka0);
+            uint32_t* kb = reinterpret_cast<uint32_t*>(kb0);
+            { k_init_keys_list<idx_t><<<grid_for(m, 256), 256, 0, st>>>(pk, va0, m, idx_t(L), ka); note_launch(); }
             idx_t* va = va0;
             idx_t* vb = vb0;
-            int rc = radix_sort_pairs<idx_t>(&ka, &va, &kb, &vb, m, 0, 64, rtmp, radix_tmp_bytes(m), st);
+            int rc = radix_sort_pairs<uint32_t, idx_t>(&ka, &va, &kb, &vb, m, 0, 32, rtmp, radix_tmp_bytes(m), st);
             if (rc) return rc;
             if (size_t(L) > size_t(kHead)) {
                 // scratch: the free value buffer, and rank behind it when that is the second buffer
                 uint64_t* cols = reinterpret_cast<uint64_t*>(vb);
                 const size_t cols_cap = (vb == vb0 ? al(b[3]) + b[4] : al(b[2])) / sizeof(uint64_t);
-                rc = refine_groups(ka, va, m, idx_t(L), pk, kb, cols, cols_cap, counters, rtmp, radix_tmp_bytes(m), st);
+                rc = refine_groups(ka, va, m, idx_t(L), pk, reinterpret_cast<uint64_t*>(kb), cols, cols_cap, counters,
+                                   rtmp, radix_tmp_bytes(m), st);
                 if (rc > 0) return rc;
                 if (rc < 0) return int(cudaErrorNotSupported);      // would need prefix doubling
             }

@@ -8,11 +8,12 @@ size_t suffix_sort_tmp_bytes(size_t n);
 
 // Suffix array of direction dir in the canonical order (suffix string with end-of-read lowest,
 // then text position).  Returns 0 or a cudaError_t value.  When keys_out is given it receives
-// the sorted 64-bit keys (first 29 bases, then min(length, 29) in the low 6 bits) aligned with the
-// suffix array, inside tmp (valid until tmp is reused), or nullptr when the sort ended by prefix
-// doubling (the key array then holds ranks).
+// the sorted 32-bit keys (first 14 bases in bits 31..4, then min(length, 14) in bits 3..0)
+// aligned with the suffix array, inside tmp (valid until tmp is reused), or nullptr when the sort
+// ended by prefix doubling (the key array then holds ranks).
+constexpr int kSortKeyBases = 14;
 int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa, void* tmp,
-                size_t tmp_bytes, cudaStream_t st, const uint64_t** keys_out = nullptr);
+                size_t tmp_bytes, cudaStream_t st, const uint32_t** keys_out = nullptr);
 
 // The same order for inputs too large for one pass: suffixes bucketed by their first 6 bases,
 // consecutive buckets sorted in chunks of at most cap (< 2^31) suffixes.  Returns
@@ -25,10 +26,11 @@ int suffix_sort_chunked(const uint8_t* reads, idx_t num_reads, int L, int dir, i
 cudaError_t read_seeds(const uint8_t* reads, idx_t num_reads, int L, int dir, int k, const idx_t* kstart,
                        const idx_t* kend, idx_t* start, idx_t* size, cudaStream_t st);
 
-// Stable LSD radix sort of (key, value) pairs on the bits [lo_bit, hi_bit) of the key.
-// Buffers are ping-ponged; the sorted result ends in (*k0, *v0) (pointers may be swapped).
-template <class V>
-int radix_sort_pairs(uint64_t** k0, V** v0, uint64_t** k1, V** v1, size_t n, int lo_bit, int hi_bit,
+// Stable LSD radix sort of (key, value) pairs on the bits [lo_bit, hi_bit) of the key (K is
+// uint32_t or uint64_t).  Buffers are ping-ponged; the sorted result ends in (*k0, *v0) (pointers
+// may be swapped).
+template <class K, class V>
+int radix_sort_pairs(K** k0, V** v0, K** k1, V** v1, size_t n, int lo_bit, int hi_bit,
                      void* tmp, size_t tmp_bytes, cudaStream_t st);
 size_t radix_tmp_bytes(size_t n);
 
