@@ -179,8 +179,14 @@ __global__ void k_scan_small(unsigned long long* __restrict__ a, size_t m) {
     }
 }
 
+// One CTA per contiguous part of the input, tiles of RS_TILE keys in order.  Per tile: every
+// thread loads its RS_IPT (key, value) pairs first (all loads in flight together), then each warp
+// ranks its rows by digit (8 ballots per row give the lanes with the same digit; a per-warp count
+// per digit in shared memory carries the rank from row to row), the tile is reordered by digit in
+// shared memory, and written out in runs per digit at the part's running digit offsets.
 template <class K, class V>
-__global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(const K* __restrict__ kin, const V* __restrict__ vin,
+__global__ void __launch_bounds__(RS_THREADS, sizeof(K) == 4 ? 4 : 3)
+k_rs_downsweep(const K* __restrict__ kin, const V* __restrict__ vin,
                                                              K* __restrict__ kout, V* __restrict__ vout, size_t n,
                                                              int shift, size_t part,
                                                              const unsigned long long* __restrict__ offs) {
@@ -203,15 +209,17 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(const K* __restrict
         K k[RS_IPT];
         V v[RS_IPT];
         unsigned int lr[RS_IPT];
-        int dg[RS_IPT];
+        const size_t row0 = t0 + size_t(warp) * 32 * RS_IPT + lane;
         #pragma unroll
         for (int r = 0; r < RS_IPT; ++r) {
-            size_t idx = t0 + size_t(warp) * 32 * RS_IPT + r * 32 + lane;
-            bool valid = idx < end;
-            k[r] = valid ? kin[idx] : K(0);
-            v[r] = valid ? vin[idx] : V(0);
-            int d = valid ? int((k[r] >> shift) & 255) : -1;
-            dg[r] = d;
+            const size_t idx = row0 + r * 32;
+            k[r] = idx < end ? kin[idx] : K(0);
+            v[r] = idx < end ? vin[idx] : V(0);
+        }
+        #pragma unroll
+        for (int r = 0; r < RS_IPT; ++r) {
+            const bool valid = row0 + r * 32 < end;
+            const int d = valid ? int((k[r] >> shift) & 255) : -1;
             unsigned peers = __ballot_sync(0xffffffffu, valid);
             #pragma unroll
             for (int b = 0; b < 8; ++b) {
@@ -255,8 +263,9 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(const K* __restrict
         __syncthreads();
         #pragma unroll
         for (int r = 0; r < RS_IPT; ++r) {
-            if (dg[r] >= 0) {
-                unsigned pos = dstart[dg[r]] + wcnt[warp][dg[r]] + lr[r];
+            if (row0 + r * 32 < end) {
+                const int d = int((k[r] >> shift) & 255);
+                const unsigned pos = dstart[d] + wcnt[warp][d] + lr[r];
                 sk[pos] = k[r];
                 sv[pos] = v[r];
             }
@@ -650,14 +659,93 @@ struct RefineItem {
     int seg;
 };
 
+// a < b on (seg, w[0..W-1], tail) as one unsigned multi-word number: the borrow out of the
+// subtraction a - b, least significant word first, in one chain of subtract-with-borrow
+// instructions (no branches; the chain must sit in one asm statement to keep the carry flag).
+#define PQ_SUBC(x, y) "subc.cc.u64 t, %" #x ", %" #y ";\n\t"
+#define PQ_LT_HEAD "{\n\t.reg .u64 t;\n\t.reg .u32 s, z;\n\tmov.u32 z, 0;\n\tsub.cc.u64 t, %1, %2;\n\t"
+#define PQ_LT_TAIL(x, y) "subc.cc.u32 s, %" #x ", %" #y ";\n\tsubc.u32 %0, z, z;\n\t}"
+#define PQ_WORD(j) "l"(a.w[j]), "l"(b.w[j])
+
 template <int W>
-__device__ __forceinline__ bool item_less(const RefineItem<W>& a, const RefineItem<W>& b) {
-    if (a.seg != b.seg) return a.seg < b.seg;
-    #pragma unroll
-    for (int j = 0; j < W; ++j)
-        if (a.w[j] != b.w[j]) return a.w[j] < b.w[j];
-    return a.tail < b.tail;
+__device__ __forceinline__ bool item_less(const RefineItem<W>& a, const RefineItem<W>& b);
+
+template <>
+__device__ __forceinline__ bool item_less<1>(const RefineItem<1>& a, const RefineItem<1>& b) {
+    unsigned r;
+    asm(PQ_LT_HEAD PQ_SUBC(3, 4) PQ_LT_TAIL(5, 6)
+        : "=r"(r)
+        : "l"(a.tail), "l"(b.tail), PQ_WORD(0), "r"(a.seg), "r"(b.seg));
+    return r != 0;
 }
+
+template <>
+__device__ __forceinline__ bool item_less<2>(const RefineItem<2>& a, const RefineItem<2>& b) {
+    unsigned r;
+    asm(PQ_LT_HEAD PQ_SUBC(3, 4) PQ_SUBC(5, 6) PQ_LT_TAIL(7, 8)
+        : "=r"(r)
+        : "l"(a.tail), "l"(b.tail), PQ_WORD(1), PQ_WORD(0), "r"(a.seg), "r"(b.seg));
+    return r != 0;
+}
+
+template <>
+__device__ __forceinline__ bool item_less<3>(const RefineItem<3>& a, const RefineItem<3>& b) {
+    unsigned r;
+    asm(PQ_LT_HEAD PQ_SUBC(3, 4) PQ_SUBC(5, 6) PQ_SUBC(7, 8) PQ_LT_TAIL(9, 10)
+        : "=r"(r)
+        : "l"(a.tail), "l"(b.tail), PQ_WORD(2), PQ_WORD(1), PQ_WORD(0), "r"(a.seg), "r"(b.seg));
+    return r != 0;
+}
+
+template <>
+__device__ __forceinline__ bool item_less<4>(const RefineItem<4>& a, const RefineItem<4>& b) {
+    unsigned r;
+    asm(PQ_LT_HEAD PQ_SUBC(3, 4) PQ_SUBC(5, 6) PQ_SUBC(7, 8) PQ_SUBC(9, 10) PQ_LT_TAIL(11, 12)
+        : "=r"(r)
+        : "l"(a.tail), "l"(b.tail), PQ_WORD(3), PQ_WORD(2), PQ_WORD(1), PQ_WORD(0), "r"(a.seg), "r"(b.seg));
+    return r != 0;
+}
+
+template <>
+__device__ __forceinline__ bool item_less<5>(const RefineItem<5>& a, const RefineItem<5>& b) {
+    unsigned r;
+    asm(PQ_LT_HEAD PQ_SUBC(3, 4) PQ_SUBC(5, 6) PQ_SUBC(7, 8) PQ_SUBC(9, 10) PQ_SUBC(11, 12) PQ_LT_TAIL(13, 14)
+        : "=r"(r)
+        : "l"(a.tail), "l"(b.tail), PQ_WORD(4), PQ_WORD(3), PQ_WORD(2), PQ_WORD(1), PQ_WORD(0), "r"(a.seg), "r"(b.seg));
+    return r != 0;
+}
+
+template <>
+__device__ __forceinline__ bool item_less<6>(const RefineItem<6>& a, const RefineItem<6>& b) {
+    unsigned r;
+    asm(PQ_LT_HEAD PQ_SUBC(3, 4) PQ_SUBC(5, 6) PQ_SUBC(7, 8) PQ_SUBC(9, 10) PQ_SUBC(11, 12) PQ_SUBC(13, 14) PQ_LT_TAIL(15, 16)
+        : "=r"(r)
+        : "l"(a.tail), "l"(b.tail), PQ_WORD(5), PQ_WORD(4), PQ_WORD(3), PQ_WORD(2), PQ_WORD(1), PQ_WORD(0), "r"(a.seg), "r"(b.seg));
+    return r != 0;
+}
+
+template <>
+__device__ __forceinline__ bool item_less<7>(const RefineItem<7>& a, const RefineItem<7>& b) {
+    unsigned r;
+    asm(PQ_LT_HEAD PQ_SUBC(3, 4) PQ_SUBC(5, 6) PQ_SUBC(7, 8) PQ_SUBC(9, 10) PQ_SUBC(11, 12) PQ_SUBC(13, 14) PQ_SUBC(15, 16) PQ_LT_TAIL(17, 18)
+        : "=r"(r)
+        : "l"(a.tail), "l"(b.tail), PQ_WORD(6), PQ_WORD(5), PQ_WORD(4), PQ_WORD(3), PQ_WORD(2), PQ_WORD(1), PQ_WORD(0), "r"(a.seg), "r"(b.seg));
+    return r != 0;
+}
+
+template <>
+__device__ __forceinline__ bool item_less<8>(const RefineItem<8>& a, const RefineItem<8>& b) {
+    unsigned r;
+    asm(PQ_LT_HEAD PQ_SUBC(3, 4) PQ_SUBC(5, 6) PQ_SUBC(7, 8) PQ_SUBC(9, 10) PQ_SUBC(11, 12) PQ_SUBC(13, 14) PQ_SUBC(15, 16) PQ_SUBC(17, 18) PQ_LT_TAIL(19, 20)
+        : "=r"(r)
+        : "l"(a.tail), "l"(b.tail), PQ_WORD(7), PQ_WORD(6), PQ_WORD(5), PQ_WORD(4), PQ_WORD(3), PQ_WORD(2), PQ_WORD(1), PQ_WORD(0), "r"(a.seg), "r"(b.seg));
+    return r != 0;
+}
+
+#undef PQ_SUBC
+#undef PQ_LT_HEAD
+#undef PQ_LT_TAIL
+#undef PQ_WORD
 
 template <int W, int E>
 __global__ void k_refine_warp(const unsigned long long* __restrict__ list, const unsigned long long* __restrict__ cnt,
