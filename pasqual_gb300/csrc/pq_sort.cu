@@ -40,7 +40,6 @@ template <class K>
 __device__ __forceinline__ int key_len(K k) { return int(k & K((1u << KeyFmt<K>::len_bits) - 1)); }
 constexpr int RS_THREADS = 256;
 constexpr int RS_IPT = 8;
-constexpr int RS_TILE = RS_THREADS * RS_IPT;
 constexpr int RS_WARPS = RS_THREADS / 32;
 constexpr int RS_MAX_CTAS = 152 * 4;
 
@@ -179,42 +178,88 @@ __global__ void k_scan_small(unsigned long long* __restrict__ a, size_t m) {
     }
 }
 
-// One CTA per contiguous part of the input, tiles of RS_TILE keys in order.  Per tile: every
-// thread loads its RS_IPT (key, value) pairs first (all loads in flight together), then each warp
-// ranks its rows by digit (8 ballots per row give the lanes with the same digit; a per-warp count
-// per digit in shared memory carries the rank from row to row), the tile is reordered by digit in
-// shared memory, and written out in runs per digit at the part's running digit offsets.
+// 16-byte asynchronous global -> shared copies (bypassing registers and L1)
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const unsigned s = unsigned(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// Downsweep configuration: 512 threads (tiles of 4096) for 32-bit keys and values, whose tile,
+// staging buffer and reorder buffer fit two CTAs per SM; 256 threads otherwise.
 template <class K, class V>
-__global__ void __launch_bounds__(RS_THREADS, sizeof(K) == 4 ? 4 : 3)
-k_rs_downsweep(const K* __restrict__ kin, const V* __restrict__ vin,
-                                                             K* __restrict__ kout, V* __restrict__ vout, size_t n,
-                                                             int shift, size_t part,
-                                                             const unsigned long long* __restrict__ offs) {
-    __shared__ K sk[RS_TILE];
-    __shared__ V sv[RS_TILE];
-    __shared__ unsigned int wcnt[RS_WARPS][256];
-    __shared__ unsigned int tcount[256];
-    __shared__ unsigned int dstart[256];
-    __shared__ unsigned long long base[256];
-    __shared__ unsigned int wtot[RS_WARPS];
+struct RsCfg {
+    static constexpr int threads = (sizeof(K) == 4 && sizeof(V) == 4) ? 512 : 256;
+    static constexpr int tile = threads * RS_IPT;
+    static constexpr int min_blocks = threads == 512 ? 2 : (sizeof(K) == 4 ? 4 : 3);   // CTAs per SM
+};
+constexpr int RS_TILE_MAX = 4096;           // parts are whole multiples of every tile size
+
+// One CTA per contiguous part of the input, tiles in order.  Per tile: every thread takes its
+// RS_IPT (key, value) pairs, from the staging buffer when the tile was prefetched there (whole,
+// 16-byte aligned tiles: the next tile's copy runs while this one is ranked and written), else
+// straight from global memory; each warp ranks its rows by digit (8 ballots per row give the lanes
+// with the same digit; a per-warp count per digit in shared memory carries the rank from row to
+// row), the tile is reordered by digit in shared memory and written out in runs per digit at the
+// part's running digit offsets.
+template <class K, class V>
+__global__ void __launch_bounds__(RsCfg<K, V>::threads, RsCfg<K, V>::min_blocks)
+k_rs_downsweep(const K* __restrict__ kin, const V* __restrict__ vin, K* __restrict__ kout, V* __restrict__ vout,
+               size_t n, int shift, size_t part, const unsigned long long* __restrict__ offs, int staged) {
+    constexpr int T = RsCfg<K, V>::threads;
+    constexpr int TILE = RsCfg<K, V>::tile;
+    constexpr int NW = T / 32;
+    extern __shared__ __align__(16) unsigned char rs_smem[];
+    K* stk = reinterpret_cast<K*>(rs_smem);                          // staging: keys, values
+    V* stv = reinterpret_cast<V*>(stk + TILE);
+    K* sk = reinterpret_cast<K*>(stv + TILE);                         // reorder buffer
+    V* sv = reinterpret_cast<V*>(sk + TILE);
+    unsigned (*wcnt)[256] = reinterpret_cast<unsigned (*)[256]>(sv + TILE);
+    unsigned* tcount = &wcnt[NW][0];
+    unsigned* dstart = tcount + 256;
+    unsigned* wtot = dstart + 256;
+    unsigned long long* base = reinterpret_cast<unsigned long long*>(wtot + 32);
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const unsigned lt_mask = (1u << lane) - 1;
-    for (int d = tid; d < 256; d += RS_THREADS) base[d] = offs[size_t(d) * gridDim.x + blockIdx.x];
+    for (int d = tid; d < 256; d += T) base[d] = offs[size_t(d) * gridDim.x + blockIdx.x];
     const size_t beg = size_t(blockIdx.x) * part;
     const size_t end = zmin(n, beg + part);
-    for (size_t t0 = beg; t0 < end; t0 += RS_TILE) {
+    auto prefetch = [&](size_t t) {
+        constexpr int KC = TILE * int(sizeof(K)) / 16, VC = TILE * int(sizeof(V)) / 16;
+        for (int i = tid; i < KC; i += T)
+            cp_async16(reinterpret_cast<char*>(stk) + 16 * i, reinterpret_cast<const char*>(kin + t) + 16 * size_t(i));
+        for (int i = tid; i < VC; i += T)
+            cp_async16(reinterpret_cast<char*>(stv) + 16 * i, reinterpret_cast<const char*>(vin + t) + 16 * size_t(i));
+        cp_async_commit();
+    };
+    if (staged && beg + TILE <= end) prefetch(beg);
+    for (size_t t0 = beg; t0 < end; t0 += TILE) {
         for (int i = lane; i < 256; i += 32) wcnt[warp][i] = 0;
-        __syncwarp();
         K k[RS_IPT];
         V v[RS_IPT];
         unsigned int lr[RS_IPT];
-        const size_t row0 = t0 + size_t(warp) * 32 * RS_IPT + lane;
-        #pragma unroll
-        for (int r = 0; r < RS_IPT; ++r) {
-            const size_t idx = row0 + r * 32;
-            k[r] = idx < end ? kin[idx] : K(0);
-            v[r] = idx < end ? vin[idx] : V(0);
+        const int j0 = warp * 32 * RS_IPT + lane;
+        const size_t row0 = t0 + j0;
+        if (staged && t0 + TILE <= end) {
+            cp_async_wait_all();
+            __syncthreads();
+            #pragma unroll
+            for (int r = 0; r < RS_IPT; ++r) {
+                k[r] = stk[j0 + r * 32];
+                v[r] = stv[j0 + r * 32];
+            }
+            __syncthreads();                                    // the staging buffer is free again
+            if (t0 + 2 * size_t(TILE) <= end) prefetch(t0 + TILE);
+        } else {
+            #pragma unroll
+            for (int r = 0; r < RS_IPT; ++r) {
+                const size_t idx = row0 + r * 32;
+                k[r] = idx < end ? kin[idx] : K(0);
+                v[r] = idx < end ? vin[idx] : V(0);
+            }
+            __syncwarp();
         }
         #pragma unroll
         for (int r = 0; r < RS_IPT; ++r) {
@@ -235,10 +280,10 @@ k_rs_downsweep(const K* __restrict__ kin, const V* __restrict__ vin,
         }
         __syncthreads();
         // per digit: warp prefixes and tile count
-        for (int d = tid; d < 256; d += RS_THREADS) {
+        for (int d = tid; d < 256; d += T) {
             unsigned run = 0;
             #pragma unroll
-            for (int w = 0; w < RS_WARPS; ++w) {
+            for (int w = 0; w < NW; ++w) {
                 unsigned c = wcnt[w][d];
                 wcnt[w][d] = run;
                 run += c;
@@ -246,19 +291,25 @@ k_rs_downsweep(const K* __restrict__ kin, const V* __restrict__ vin,
             tcount[d] = run;
         }
         __syncthreads();
-        // exclusive scan of tcount over the 256 digits (one per thread)
+        // exclusive scan of tcount over the 256 digits (one per thread of the first 8 warps)
         {
-            unsigned v0 = tcount[tid], x = v0;
-            #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                unsigned y = __shfl_up_sync(0xffffffffu, x, o);
-                if (lane >= o) x += y;
+            unsigned v0 = 0, x = 0;
+            if (tid < 256) {
+                v0 = tcount[tid];
+                x = v0;
+                #pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+                    if (lane >= o) x += y;
+                }
+                if (lane == 31) wtot[warp] = x;
             }
-            if (lane == 31) wtot[warp] = x;
             __syncthreads();
-            unsigned pre = 0;
-            for (int w = 0; w < warp; ++w) pre += wtot[w];
-            dstart[tid] = pre + x - v0;
+            if (tid < 256) {
+                unsigned pre = 0;
+                for (int w = 0; w < warp; ++w) pre += wtot[w];
+                dstart[tid] = pre + x - v0;
+            }
         }
         __syncthreads();
         #pragma unroll
@@ -271,8 +322,8 @@ k_rs_downsweep(const K* __restrict__ kin, const V* __restrict__ vin,
             }
         }
         __syncthreads();
-        const int cnt = int(zmin(size_t(RS_TILE), end - t0));
-        for (int j = tid; j < cnt; j += RS_THREADS) {
+        const int cnt = int(zmin(size_t(TILE), end - t0));
+        for (int j = tid; j < cnt; j += T) {
             const K key = sk[j];
             int d = int((key >> shift) & 255);
             unsigned long long g = base[d] + (unsigned)(j - dstart[d]);
@@ -280,9 +331,15 @@ k_rs_downsweep(const K* __restrict__ kin, const V* __restrict__ vin,
             vout[g] = sv[j];
         }
         __syncthreads();
-        for (int d = tid; d < 256; d += RS_THREADS) base[d] += tcount[d];
+        for (int d = tid; d < 256; d += T) base[d] += tcount[d];
         __syncthreads();
     }
+}
+
+template <class K, class V>
+static size_t rs_down_smem() {
+    constexpr int T = RsCfg<K, V>::threads, TILE = RsCfg<K, V>::tile;
+    return 2 * size_t(TILE) * (sizeof(K) + sizeof(V)) + size_t(T / 32 + 2) * 256 * 4 + 32 * 4 + 256 * 8;
 }
 
 cudaError_t pack_text(const uint8_t* reads, size_t n, idx_t L, int dir, uint64_t* pk, cudaStream_t st) {
@@ -311,10 +368,13 @@ int radix_sort_pairs(K** k0, V** v0, K** k1, V** v1, size_t n, int lo_bit, int h
     cudaMemcpyAsync(h.data(), gh, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
     cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return int(e);
-    size_t tiles = (n + RS_TILE - 1) / RS_TILE;
-    size_t ctas = std::min<size_t>(tiles, RS_MAX_CTAS);
-    size_t part = ((tiles + ctas - 1) / ctas) * RS_TILE;
+    size_t tiles = (n + RS_TILE_MAX - 1) / RS_TILE_MAX;
+    // one wave of resident CTAs
+    size_t ctas = std::min<size_t>(tiles, std::min<size_t>(RS_MAX_CTAS, size_t(152) * RsCfg<K, V>::min_blocks));
+    size_t part = ((tiles + ctas - 1) / ctas) * RS_TILE_MAX;
     ctas = (n + part - 1) / part;
+    const size_t smem = rs_down_smem<K, V>();
+    cudaFuncSetAttribute(k_rs_downsweep<K, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     for (int d = lo_bit / 8; d * 8 < hi_bit; ++d) {
         bool trivial = false;
         for (int b = 0; b < 256; ++b)
@@ -322,7 +382,10 @@ int radix_sort_pairs(K** k0, V** v0, K** k1, V** v1, size_t n, int lo_bit, int h
         if (trivial) continue;
         { k_rs_upsweep<K><<<unsigned(ctas), RS_THREADS, 0, st>>>(*k0, n, 8 * d, part, cnt); note_launch(); }
         { k_scan_small<<<1, 1024, 0, st>>>(cnt, 256 * ctas); note_launch(); }
-        { k_rs_downsweep<K, V><<<unsigned(ctas), RS_THREADS, 0, st>>>(*k0, *v0, *k1, *v1, n, 8 * d, part, cnt); note_launch(); }
+        // whole tiles are prefetched by 16-byte copies when both inputs are 16-byte aligned
+        const int staged = (reinterpret_cast<uintptr_t>(*k0) % 16 == 0 && reinterpret_cast<uintptr_t>(*v0) % 16 == 0);
+        { k_rs_downsweep<K, V><<<unsigned(ctas), RsCfg<K, V>::threads, smem, st>>>(*k0, *v0, *k1, *v1, n, 8 * d, part,
+                                                                                   cnt, staged); note_launch(); }
         std::swap(*k0, *k1);
         std::swap(*v0, *v1);
     }
