@@ -366,12 +366,13 @@ int pq_build_fm(pq_ctx* ctx, int dir) {
     const size_t isa_n = size_t(ctx->num_reads) * size_t(ctx->L - ctx->t);
     CK(ctx->isa[dir].ensure(isa_n * sizeof(idx_t) + 64));
     CK(cudaEventRecord(ctx->ev0, ctx->st));
+    CK(pq::pack_text(ctx->reads.as<uint8_t>(), n, idx_t(ctx->L), dir, ctx->pk[dir].as<uint64_t>(), ctx->st));
     CK(pq::build_occ(ctx->sa[dir].as<idx_t>(), ctx->reads.as<uint8_t>(), ctx->num_reads, idx_t(ctx->L), dir,
-                     ctx->blk[dir].as<OccBlock>(), ctx->sb[dir].as<idx_t>(), ctx->ri[dir].as<idx_t>(), ctx->st));
+                     ctx->blk[dir].as<OccBlock>(), ctx->sb[dir].as<idx_t>(), ctx->ri[dir].as<idx_t>(), ctx->st,
+                     ctx->pk[dir].as<uint64_t>()));
     CK(pq::build_kmer_table(ctx->sa[dir].as<idx_t>(), ctx->reads.as<uint8_t>(), ctx->num_reads, idx_t(ctx->L), dir,
                             k, ctx->ktmp.as<uint32_t>(), ctx->kstart[dir].as<idx_t>(), ctx->kend[dir].as<idx_t>(),
                             ctx->st, ctx->sorted_keys[dir]));
-    CK(pq::pack_text(ctx->reads.as<uint8_t>(), n, idx_t(ctx->L), dir, ctx->pk[dir].as<uint64_t>(), ctx->st));
     CK(pq::build_isa(ctx->sa[dir].as<idx_t>(), n, idx_t(ctx->L), idx_t(ctx->L - ctx->t), ctx->isa[dir].as<idx_t>(),
                      ctx->st));
     CK(cudaEventRecord(ctx->ev1, ctx->st));

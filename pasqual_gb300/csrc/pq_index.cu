@@ -8,6 +8,8 @@
 #include "pq_index.cuh"
 #include "pq_sort.cuh"
 
+#include <algorithm>
+
 namespace pq {
 
 // Text character at position p (codes 1..4).  dir 1 = every read reversed in place, the text
@@ -18,11 +20,19 @@ __device__ __forceinline__ int text_at(const uint8_t* __restrict__ reads, idx_t 
     return reads[r * L + (L - 1 - off)];
 }
 
+// Base code (1..4) at position p of the packed text of a direction (32 bases per word, first base
+// in the top two bits).
+__device__ __forceinline__ int packed_at(const uint64_t* __restrict__ pk, size_t p) {
+    return int((pk[p >> 5] >> (62 - 2 * int(p & 31))) & 3) + 1;
+}
+
 // One warp per 64-row block: BWT symbol of each row (`$` for a read-start suffix, else the
-// preceding base), packed into lo/hi/dol masks with ballots; per-block symbol counts go into
+// preceding base, from the packed text when given: a quarter of the bytes of the text, so more of
+// it stays in L2), packed into lo/hi/dol masks with ballots; per-block symbol counts go into
 // cnt[] for the superblock pass.
 __global__ void k_bwt_blocks(const idx_t* __restrict__ sa, const uint8_t* __restrict__ reads,
-                             idx_t n, idx_t L, int dir, idx_t nblk, OccBlock* __restrict__ blk) {
+                             const uint64_t* __restrict__ pk, idx_t n, idx_t L, int dir, idx_t nblk,
+                             OccBlock* __restrict__ blk) {
     constexpr int G = 4;                    // blocks per warp and round: 8 independent rows per lane
     const int lane = threadIdx.x & 31;
     const size_t warp = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
@@ -41,7 +51,7 @@ __global__ void k_bwt_blocks(const idx_t* __restrict__ sa, const uint8_t* __rest
             sym[x] = -1;
             if (r < n) {
                 const idx_t off = p[x] % L;
-                sym[x] = off ? text_at(reads, L, dir, p[x] - 1) : 0;
+                sym[x] = off ? (pk ? packed_at(pk, size_t(p[x]) - 1) : text_at(reads, L, dir, p[x] - 1)) : 0;
             }
         }
         #pragma unroll
@@ -334,11 +344,11 @@ static inline unsigned grid_for(size_t work, int threads, int per_sm = 8) {
 }
 
 cudaError_t build_occ(const idx_t* sa, const uint8_t* reads, idx_t num_reads, idx_t L, int dir,
-                      OccBlock* blk, idx_t* sb, idx_t* reads_index, cudaStream_t st) {
+                      OccBlock* blk, idx_t* sb, idx_t* reads_index, cudaStream_t st, const uint64_t* pk) {
     const size_t n = size_t(num_reads) * L;
     const size_t nblk = n / 64 + 1;
     const size_t nsb = (nblk + kBlocksPerSuper - 1) / kBlocksPerSuper;
-    { k_bwt_blocks<<<grid_for(nblk * 32, 256), 256, 0, st>>>(sa, reads, idx_t(n), L, dir, idx_t(nblk), blk); note_launch(); }
+    { k_bwt_blocks<<<grid_for(nblk * 32, 256), 256, 0, st>>>(sa, reads, pk, idx_t(n), L, dir, idx_t(nblk), blk); note_launch(); }
     { k_super_prefix<<<unsigned(nsb), 256, 0, st>>>(blk, idx_t(nblk), sb); note_launch(); }
     { k_super_scan<<<1, 1024, 0, st>>>(sb, nsb); note_launch(); }
     { k_reads_index<<<grid_for(nblk * 32, 256), 256, 0, st>>>(sa, blk, sb, idx_t(n), L, idx_t(nblk), reads_index); note_launch(); }
