@@ -561,13 +561,16 @@ __device__ __forceinline__ int group_class(size_t m) {
     return m <= size_t(kGroupCta) ? 2 : 3;
 }
 
-// One CTA per tile of 4096 sorted keys: group heads are marked in a shared bit mask, each head's
-// group ends at the next marked bit (read from the mask; only a group running past the tile end is
-// followed in global memory), and the groups longer than their key's bases are listed by size.
-// List slots are taken with one atomic per list per tile, after a block-wide prefix of the counts.
+// One CTA per tile of 4096 sorted keys.  Two bit masks per tile, by ballots: group heads, and
+// keys whose suffix is longer than the key's bases.  Then one thread per mask word walks the set
+// bits of (head & long) only: a group ends at the next head bit (in the mask; a group running past
+// the tile end is followed in global memory by a galloping search), and the groups are listed by
+// size class.  List slots are taken with one atomic per list per tile, after a block-wide prefix
+// of the per-thread counts; the walk runs twice (count, then write).
 constexpr int kGlTile = 4096;
 constexpr int kGlThreads = 256;
 constexpr int kGlPer = kGlTile / kGlThreads;      // positions per thread (j = tid + 256 i)
+constexpr int kGlWords = kGlTile / 32;
 
 __device__ __forceinline__ void block_scan4(unsigned (&c)[4], unsigned (&excl)[4], unsigned (*wsum)[4],
                                             unsigned* tot) {
@@ -598,54 +601,83 @@ __device__ __forceinline__ void block_scan4(unsigned (&c)[4], unsigned (&excl)[4
     }
 }
 
+// first index >= e0 whose key differs from k (keys sorted; key[e0 - 1] == k), or n
+template <class K>
+__device__ size_t run_end(const K* __restrict__ key, size_t n, size_t e0, K k) {
+    size_t lo = e0, step = 32;                      // key[lo - 1] == k
+    size_t hi = lo;
+    while (true) {                                  // gallop: hi = first probe that differs (or n)
+        hi = lo + step < n ? lo + step : n;
+        if (hi == n || key[hi] != k) break;
+        lo = hi + 1;
+        step *= 2;
+    }
+    // the answer lies in [lo, hi]: the first index there with key != k (hi qualifies)
+    while (lo < hi) {
+        const size_t mid = lo + (hi - lo) / 2;
+        if (key[mid] != k) hi = mid;
+        else lo = mid + 1;
+    }
+    return lo;
+}
+
 template <class K>
 __global__ void __launch_bounds__(kGlThreads) k_group_lists(const K* __restrict__ key, size_t n, GroupLists G,
                                                            size_t base) {
-    __shared__ uint32_t hm[kGlTile / 32 + 1];
+    __shared__ uint32_t hm[kGlWords + 1];               // heads; sentinel word at the end
+    __shared__ uint32_t lm[kGlWords];                   // long suffixes
     __shared__ unsigned wsum[kGlThreads / 32][4];
     __shared__ unsigned long long sbase[4];
-    const int lane = threadIdx.x & 31;
+    __shared__ K last[kGlPer][kGlThreads / 32];         // each warp's lane-31 key, per round
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (size_t t0 = size_t(blockIdx.x) * kGlTile; t0 < n; t0 += size_t(gridDim.x) * kGlTile) {
-        for (int j = threadIdx.x; j < kGlTile; j += kGlThreads) {
-            const size_t i = t0 + j;
-            const bool head = i < n && (i == 0 || key[i] != key[i - 1]);
-            const uint32_t b = __ballot_sync(0xffffffffu, head);
-            if (lane == 0) hm[j >> 5] = b;
+        // all of the thread's keys in flight at once; a key's predecessor comes from the lane
+        // before, or for lane 0 from the warp before (or the round before) through shared memory
+        K kk[kGlPer];
+        #pragma unroll
+        for (int q = 0; q < kGlPer; ++q) {
+            const size_t i = t0 + threadIdx.x + size_t(kGlThreads) * q;
+            kk[q] = i < n ? key[i] : K(0);
         }
-        if (threadIdx.x == 0) hm[kGlTile / 32] = 1u;       // sentinel: the tile end
+        const K before_tile = (t0 > 0 && threadIdx.x == 0) ? key[t0 - 1] : K(0);
+        if (lane == 31) {
+            #pragma unroll
+            for (int q = 0; q < kGlPer; ++q) last[q][warp] = kk[q];
+        }
         __syncthreads();
-        uint32_t mm[kGlPer];
-        unsigned c[4] = {0, 0, 0, 0};
         #pragma unroll
         for (int q = 0; q < kGlPer; ++q) {
             const int j = threadIdx.x + kGlThreads * q;
             const size_t i = t0 + j;
-            size_t m = 0;
-            if ((hm[j >> 5] >> (j & 31)) & 1u) {
-                const K k = key[i];
-                if (key_len<K>(k) == KeyFmt<K>::bases) {     // suffix longer than its key
-                    int w;
-                    uint32_t bits;
-                    if (j + 1 < kGlTile) {
-                        w = (j + 1) >> 5;
-                        bits = hm[w] & (~0u << ((j + 1) & 31));
-                    } else {
-                        w = kGlTile / 32;
-                        bits = hm[w];
-                    }
-                    while (!bits) bits = hm[++w];           // ends at the sentinel word at the latest
-                    const int nxt = 32 * w + __ffs(bits) - 1;
-                    size_t e = t0 + size_t(nxt);
-                    if (nxt >= kGlTile) {                   // runs past the tile
-                        e = t0 + kGlTile;
-                        while (e < n && key[e] == k) ++e;
-                    }
-                    if (e > n) e = n;
-                    m = e - i;
-                }
+            K prev = __shfl_up_sync(0xffffffffu, kk[q], 1);
+            if (lane == 0) prev = warp ? last[q][warp - 1] : (q ? last[q - 1][kGlThreads / 32 - 1] : before_tile);
+            const bool head = i < n && (i == 0 || kk[q] != prev);
+            const uint32_t hb = __ballot_sync(0xffffffffu, head);
+            const uint32_t lb = __ballot_sync(0xffffffffu, i < n && key_len<K>(kk[q]) == KeyFmt<K>::bases);
+            if (lane == 0) {
+                hm[j >> 5] = hb;
+                lm[j >> 5] = lb;
             }
-            mm[q] = uint32_t(m);
-            const int cl = group_class(m);
+        }
+        if (threadIdx.x == 0) hm[kGlWords] = 1u;        // sentinel: the tile end
+        __syncthreads();
+        // walk: thread t < kGlWords owns mask word t
+        auto group_size = [&](int j) -> size_t {
+            int w = (j + 1) >> 5;
+            uint32_t bits = (j + 1 < kGlTile) ? hm[w] & (~0u << ((j + 1) & 31)) : hm[w];
+            while (!bits) bits = hm[++w];               // ends at the sentinel word at the latest
+            const int nxt = 32 * w + __ffs(bits) - 1;
+            const size_t i = t0 + size_t(j);
+            size_t e = t0 + size_t(nxt);
+            if (nxt >= kGlTile) e = t0 + kGlTile < n ? run_end<K>(key, n, t0 + kGlTile, key[i]) : n;
+            if (e > n) e = n;
+            return e - i;
+        };
+        const int tw = threadIdx.x;
+        const uint32_t mine = tw < kGlWords ? (hm[tw] & lm[tw]) : 0u;
+        unsigned c[4] = {0, 0, 0, 0};
+        for (uint32_t bits = mine; bits; bits &= bits - 1) {
+            const int cl = group_class(group_size(32 * tw + __ffs(bits) - 1));
             #pragma unroll
             for (int z = 0; z < 4; ++z) c[z] += cl == z ? 1u : 0u;
         }
@@ -657,11 +689,11 @@ __global__ void __launch_bounds__(kGlThreads) k_group_lists(const K* __restrict_
         }
         __syncthreads();
         unsigned long long at[4] = {sbase[0] + excl[0], sbase[1] + excl[1], sbase[2] + excl[2], sbase[3] + excl[3]};
-        #pragma unroll
-        for (int q = 0; q < kGlPer; ++q) {
-            const size_t i = base + t0 + threadIdx.x + kGlThreads * q;
-            const size_t m = mm[q];
+        for (uint32_t bits = mine; bits; bits &= bits - 1) {
+            const int j = 32 * tw + __ffs(bits) - 1;
+            const size_t m = group_size(j);
             const int cl = group_class(m);
+            const size_t i = base + t0 + size_t(j);
             if (cl == 3) {
                 if (at[3] < G.cap[3]) {
                     G.list[3][2 * at[3]] = i;
@@ -669,13 +701,8 @@ __global__ void __launch_bounds__(kGlThreads) k_group_lists(const K* __restrict_
                 }
                 ++at[3];
             } else if (cl >= 0) {
-                #pragma unroll
-                for (int z = 0; z < 3; ++z) {
-                    if (cl == z) {
-                        if (at[z] < G.cap[z]) G.list[z][at[z]] = (uint64_t(i) << 24) | m;
-                        ++at[z];
-                    }
-                }
+                if (at[cl] < G.cap[cl]) G.list[cl][at[cl]] = (uint64_t(i) << 24) | m;
+                ++at[cl];
             }
         }
         __syncthreads();
@@ -711,22 +738,23 @@ __device__ __forceinline__ bool tuple_less(const uint64_t a[W], uint64_t alen, u
 // Groups of 2..32E suffixes, several per warp: a warp takes 8 list entries at a time and packs
 // consecutive ones into its 32E slots (slot e * 32 + lane is register set e of that lane) while
 // they fit; one bitonic network over the 32E slots on (segment, bases from `from` on, length,
-// position) then sorts every packed group in place (each segment keeps its slots, since segments
-// are numbered in slot order and empty slots sort last).  Distances below 32 exchange by shuffle,
-// larger ones swap registers within a lane.  Length and position travel as one word, length in
-// the top 16 bits (read length <= 65535, positions < 2^48).
+// slot) then sorts every packed group in place (each segment keeps its slots, since segments are
+// numbered in slot order and empty slots sort last).  A group's members arrive in ascending
+// position (every radix pass is stable from text order), so the original slot breaks ties exactly
+// as the position does; the positions wait in shared memory and are gathered by slot at the end.
+// Distances below 32 exchange by shuffle, larger ones swap registers within a lane.
 template <int W>
 struct RefineItem {
     uint64_t w[W];
-    uint64_t tail;                              // (length << 48) | position
-    int seg;
+    uint32_t tail;                              // (length << 8) | original slot
+    uint32_t seg;
 };
 
 // a < b on (seg, w[0..W-1], tail) as one unsigned multi-word number: the borrow out of the
 // subtraction a - b, least significant word first, in one chain of subtract-with-borrow
 // instructions (no branches; the chain must sit in one asm statement to keep the carry flag).
 #define PQ_SUBC(x, y) "subc.cc.u64 t, %" #x ", %" #y ";\n\t"
-#define PQ_LT_HEAD "{\n\t.reg .u64 t;\n\t.reg .u32 s, z;\n\tmov.u32 z, 0;\n\tsub.cc.u64 t, %1, %2;\n\t"
+#define PQ_LT_HEAD "{\n\t.reg .u64 t;\n\t.reg .u32 s, z;\n\tmov.u32 z, 0;\n\tsub.cc.u32 s, %1, %2;\n\t"
 #define PQ_LT_TAIL(x, y) "subc.cc.u32 s, %" #x ", %" #y ";\n\tsubc.u32 %0, z, z;\n\t}"
 #define PQ_WORD(j) "l"(a.w[j]), "l"(b.w[j])
 
@@ -738,7 +766,7 @@ __device__ __forceinline__ bool item_less<1>(const RefineItem<1>& a, const Refin
     unsigned r;
     asm(PQ_LT_HEAD PQ_SUBC(3, 4) PQ_LT_TAIL(5, 6)
         : "=r"(r)
-        : "l"(a.tail), "l"(b.tail), PQ_WORD(0), "r"(a.seg), "r"(b.seg));
+        : "r"(a.tail), "r"(b.tail), PQ_WORD(0), "r"(a.seg), "r"(b.seg));
     return r != 0;
 }
 
@@ -747,7 +775,7 @@ __device__ __forceinline__ bool item_less<2>(const RefineItem<2>& a, const Refin
     unsigned r;
     asm(PQ_LT_HEAD PQ_SUBC(3, 4) PQ_SUBC(5, 6) PQ_LT_TAIL(7, 8)
         : "=r"(r)
-        : "l"(a.tail), "l"(b.tail), PQ_WORD(1), PQ_WORD(0), "r"(a.seg), "r"(b.seg));
+        : "r"(a.tail), "r"(b.tail), PQ_WORD(1), PQ_WORD(0), "r"(a.seg), "r"(b.seg));
     return r != 0;
 }
 
@@ -756,7 +784,7 @@ __device__ __forceinline__ bool item_less<3>(const RefineItem<3>& a, const Refin
     unsigned r;
     asm(PQ_LT_HEAD PQ_SUBC(3, 4) PQ_SUBC(5, 6) PQ_SUBC(7, 8) PQ_LT_TAIL(9, 10)
         : "=r"(r)
-        : "l"(a.tail), "l"(b.tail), PQ_WORD(2), PQ_WORD(1), PQ_WORD(0), "r"(a.seg), "r"(b.seg));
+        : "r"(a.tail), "r"(b.tail), PQ_WORD(2), PQ_WORD(1), PQ_WORD(0), "r"(a.seg), "r"(b.seg));
     return r != 0;
 }
 
@@ -765,7 +793,7 @@ __device__ __forceinline__ bool item_less<4>(const RefineItem<4>& a, const Refin
     unsigned r;
     asm(PQ_LT_HEAD PQ_SUBC(3, 4) PQ_SUBC(5, 6) PQ_SUBC(7, 8) PQ_SUBC(9, 10) PQ_LT_TAIL(11, 12)
         : "=r"(r)
-        : "l"(a.tail), "l"(b.tail), PQ_WORD(3), PQ_WORD(2), PQ_WORD(1), PQ_WORD(0), "r"(a.seg), "r"(b.seg));
+        : "r"(a.tail), "r"(b.tail), PQ_WORD(3), PQ_WORD(2), PQ_WORD(1), PQ_WORD(0), "r"(a.seg), "r"(b.seg));
     return r != 0;
 }
 
@@ -774,7 +802,7 @@ __device__ __forceinline__ bool item_less<5>(const RefineItem<5>& a, const Refin
     unsigned r;
     asm(PQ_LT_HEAD PQ_SUBC(3, 4) PQ_SUBC(5, 6) PQ_SUBC(7, 8) PQ_SUBC(9, 10) PQ_SUBC(11, 12) PQ_LT_TAIL(13, 14)
         : "=r"(r)
-        : "l"(a.tail), "l"(b.tail), PQ_WORD(4), PQ_WORD(3), PQ_WORD(2), PQ_WORD(1), PQ_WORD(0), "r"(a.seg), "r"(b.seg));
+        : "r"(a.tail), "r"(b.tail), PQ_WORD(4), PQ_WORD(3), PQ_WORD(2), PQ_WORD(1), PQ_WORD(0), "r"(a.seg), "r"(b.seg));
     return r != 0;
 }
 
@@ -783,7 +811,7 @@ __device__ __forceinline__ bool item_less<6>(const RefineItem<6>& a, const Refin
     unsigned r;
     asm(PQ_LT_HEAD PQ_SUBC(3, 4) PQ_SUBC(5, 6) PQ_SUBC(7, 8) PQ_SUBC(9, 10) PQ_SUBC(11, 12) PQ_SUBC(13, 14) PQ_LT_TAIL(15, 16)
         : "=r"(r)
-        : "l"(a.tail), "l"(b.tail), PQ_WORD(5), PQ_WORD(4), PQ_WORD(3), PQ_WORD(2), PQ_WORD(1), PQ_WORD(0), "r"(a.seg), "r"(b.seg));
+        : "r"(a.tail), "r"(b.tail), PQ_WORD(5), PQ_WORD(4), PQ_WORD(3), PQ_WORD(2), PQ_WORD(1), PQ_WORD(0), "r"(a.seg), "r"(b.seg));
     return r != 0;
 }
 
@@ -792,7 +820,7 @@ __device__ __forceinline__ bool item_less<7>(const RefineItem<7>& a, const Refin
     unsigned r;
     asm(PQ_LT_HEAD PQ_SUBC(3, 4) PQ_SUBC(5, 6) PQ_SUBC(7, 8) PQ_SUBC(9, 10) PQ_SUBC(11, 12) PQ_SUBC(13, 14) PQ_SUBC(15, 16) PQ_LT_TAIL(17, 18)
         : "=r"(r)
-        : "l"(a.tail), "l"(b.tail), PQ_WORD(6), PQ_WORD(5), PQ_WORD(4), PQ_WORD(3), PQ_WORD(2), PQ_WORD(1), PQ_WORD(0), "r"(a.seg), "r"(b.seg));
+        : "r"(a.tail), "r"(b.tail), PQ_WORD(6), PQ_WORD(5), PQ_WORD(4), PQ_WORD(3), PQ_WORD(2), PQ_WORD(1), PQ_WORD(0), "r"(a.seg), "r"(b.seg));
     return r != 0;
 }
 
@@ -801,7 +829,7 @@ __device__ __forceinline__ bool item_less<8>(const RefineItem<8>& a, const Refin
     unsigned r;
     asm(PQ_LT_HEAD PQ_SUBC(3, 4) PQ_SUBC(5, 6) PQ_SUBC(7, 8) PQ_SUBC(9, 10) PQ_SUBC(11, 12) PQ_SUBC(13, 14) PQ_SUBC(15, 16) PQ_SUBC(17, 18) PQ_LT_TAIL(19, 20)
         : "=r"(r)
-        : "l"(a.tail), "l"(b.tail), PQ_WORD(7), PQ_WORD(6), PQ_WORD(5), PQ_WORD(4), PQ_WORD(3), PQ_WORD(2), PQ_WORD(1), PQ_WORD(0), "r"(a.seg), "r"(b.seg));
+        : "r"(a.tail), "r"(b.tail), PQ_WORD(7), PQ_WORD(6), PQ_WORD(5), PQ_WORD(4), PQ_WORD(3), PQ_WORD(2), PQ_WORD(1), PQ_WORD(0), "r"(a.seg), "r"(b.seg));
     return r != 0;
 }
 
@@ -810,12 +838,18 @@ __device__ __forceinline__ bool item_less<8>(const RefineItem<8>& a, const Refin
 #undef PQ_LT_TAIL
 #undef PQ_WORD
 
+constexpr int kRefineThreads = 256;
+
 template <int W, int E>
-__global__ void k_refine_warp(const unsigned long long* __restrict__ list, const unsigned long long* __restrict__ cnt,
-                              const uint64_t* __restrict__ pk, idx_t L, idx_t* __restrict__ val, int from) {
+__global__ void __launch_bounds__(kRefineThreads) k_refine_warp(const unsigned long long* __restrict__ list,
+                                                                const unsigned long long* __restrict__ cnt,
+                                                                const uint64_t* __restrict__ pk, idx_t L,
+                                                                idx_t* __restrict__ val, int from) {
     constexpr int kChunk = 8;
     constexpr int N = 32 * E;
+    __shared__ idx_t spos[kRefineThreads / 32][N];
     const int lane = threadIdx.x & 31;
+    idx_t* const mypos = spos[threadIdx.x >> 5];
     const size_t warp = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const size_t nwarps = (size_t(gridDim.x) * blockDim.x) >> 5;
     const size_t groups = *cnt;
@@ -825,7 +859,7 @@ __global__ void k_refine_warp(const unsigned long long* __restrict__ list, const
         while (next < kChunk) {
             // consecutive entries next .. next + taken - 1 fit in N slots
             int taken = 0, total = 0;
-            int seg[E];
+            uint32_t seg[E];
             size_t at[E];
             #pragma unroll
             for (int e = 0; e < E; ++e) {
@@ -840,7 +874,7 @@ __global__ void k_refine_warp(const unsigned long long* __restrict__ list, const
                 for (int e = 0; e < E; ++e) {
                     const int slot = e * 32 + lane;
                     if (slot >= total && slot < total + m) {
-                        seg[e] = q - next;
+                        seg[e] = uint32_t(q - next);
                         at[e] = size_t(x >> 24) + size_t(slot - total);
                     }
                 }
@@ -853,14 +887,15 @@ __global__ void k_refine_warp(const unsigned long long* __restrict__ list, const
             for (int e = 0; e < E; ++e) {
                 it[e].seg = seg[e];
                 if (seg[e] != 255) {
-                    const uint64_t pos = uint64_t(val[at[e]]);
-                    const uint64_t len = uint64_t(L - idx_t(pos % L));
+                    const idx_t pos = val[at[e]];
+                    const uint32_t len = uint32_t(L - pos % L);
                     suffix_words<W>(pk, size_t(pos), int(len), from, it[e].w);
-                    it[e].tail = (len << 48) | pos;
+                    it[e].tail = (len << 8) | uint32_t(e * 32 + lane);
+                    mypos[e * 32 + lane] = pos;
                 } else {
                     #pragma unroll
                     for (int j = 0; j < W; ++j) it[e].w[j] = ~uint64_t(0);
-                    it[e].tail = ~uint64_t(0);
+                    it[e].tail = ~0u;
                 }
             }
             #pragma unroll
@@ -894,9 +929,11 @@ __global__ void k_refine_warp(const unsigned long long* __restrict__ list, const
                     }
                 }
             }
+            __syncwarp();
             #pragma unroll
             for (int e = 0; e < E; ++e)
-                if (seg[e] != 255) val[at[e]] = idx_t(it[e].tail & ((uint64_t(1) << 48) - 1));
+                if (seg[e] != 255) val[at[e]] = mypos[it[e].tail & 255u];
+            __syncwarp();
             next += taken;
         }
     }
@@ -1000,11 +1037,11 @@ static void refine_small_mid(const GroupLists& G, const unsigned long long* c, c
                              idx_t* val, int off, cudaStream_t st) {
     if (c[0]) {
         unsigned g = unsigned(std::min<unsigned long long>((c[0] + 63) / 64, 152ull * 64));
-        { k_refine_warp<W, 1><<<g, 256, 0, st>>>(G.list[0], G.counts + 0, pk, L, val, off); note_launch(); }
+        { k_refine_warp<W, 1><<<g, kRefineThreads, 0, st>>>(G.list[0], G.counts + 0, pk, L, val, off); note_launch(); }
     }
     if (c[1]) {
         unsigned g = unsigned(std::min<unsigned long long>((c[1] + 15) / 16, 152ull * 64));
-        { k_refine_warp<W, 4><<<g, 256, 0, st>>>(G.list[1], G.counts + 1, pk, L, val, off); note_launch(); }
+        { k_refine_warp<W, 4><<<g, kRefineThreads, 0, st>>>(G.list[1], G.counts + 1, pk, L, val, off); note_launch(); }
     }
     if (c[2]) {
         const size_t smem = size_t(W + 2) * kGroupCta * sizeof(uint64_t);
