@@ -80,6 +80,7 @@ struct pq_ctx {
     int fm_k[2] = {0, 0};
     DevBuf ktmp, sort_tmp, counts;
     const uint32_t* sorted_keys[2] = {nullptr, nullptr};   // the last sort's keys, inside sort_tmp
+    const uint8_t* bwt_hint[2] = {nullptr, nullptr};       // the last sort's BWT symbols, inside sort_tmp
     uint64_t sort_chunk = 0;                                // suffixes per sort chunk (0: automatic)
 
     // learned index per direction (pq_learned.cu)
@@ -281,11 +282,12 @@ int pq_sort(pq_ctx* ctx, int dir) {
     CK(ctx->sort_tmp.ensure(tmp_bytes));
     CK(cudaEventRecord(ctx->ev0, ctx->st));
     ctx->sorted_keys[0] = ctx->sorted_keys[1] = nullptr;     // the scratch is about to be reused
+    ctx->bwt_hint[0] = ctx->bwt_hint[1] = nullptr;
     int rc = chunked ? pq::suffix_sort_chunked(ctx->reads.as<uint8_t>(), ctx->num_reads, ctx->L, dir,
                                                ctx->sa[dir].as<idx_t>(), cap, ctx->sort_tmp.p, tmp_bytes, ctx->st)
                      : pq::suffix_sort(ctx->reads.as<uint8_t>(), ctx->num_reads, ctx->L, dir,
                                        ctx->sa[dir].as<idx_t>(), ctx->sort_tmp.p, tmp_bytes, ctx->st,
-                                       &ctx->sorted_keys[dir]);
+                                       &ctx->sorted_keys[dir], &ctx->bwt_hint[dir]);
     if (rc == int(cudaErrorNotSupported))
         return fail(ctx, PQ_ERR_CAPACITY, "suffix sort: a 6-base bucket holds more suffixes than a sort chunk");
     if (rc != 0) return fail(ctx, PQ_ERR_CUDA, std::string("suffix sort failed: ") + cudaGetErrorString(cudaGetLastError()));
@@ -309,6 +311,7 @@ int pq_set_sa(pq_ctx* ctx, int dir, const pq_idx* sa, int from_device) {
                            from_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
     ctx->sorted_keys[dir] = nullptr;
+    ctx->bwt_hint[dir] = nullptr;
     ctx->sa_ok[dir] = true;
     ctx->fm_ok[dir] = false;
     ctx->graph_ok = false;
@@ -369,7 +372,7 @@ int pq_build_fm(pq_ctx* ctx, int dir) {
     CK(pq::pack_text(ctx->reads.as<uint8_t>(), n, idx_t(ctx->L), dir, ctx->pk[dir].as<uint64_t>(), ctx->st));
     CK(pq::build_occ(ctx->sa[dir].as<idx_t>(), ctx->reads.as<uint8_t>(), ctx->num_reads, idx_t(ctx->L), dir,
                      ctx->blk[dir].as<OccBlock>(), ctx->sb[dir].as<idx_t>(), ctx->ri[dir].as<idx_t>(), ctx->st,
-                     ctx->pk[dir].as<uint64_t>()));
+                     ctx->pk[dir].as<uint64_t>(), ctx->bwt_hint[dir]));
     CK(pq::build_kmer_table(ctx->sa[dir].as<idx_t>(), ctx->reads.as<uint8_t>(), ctx->num_reads, idx_t(ctx->L), dir,
                             k, ctx->ktmp.as<uint32_t>(), ctx->kstart[dir].as<idx_t>(), ctx->kend[dir].as<idx_t>(),
                             ctx->st, ctx->sorted_keys[dir]));
@@ -400,6 +403,7 @@ int pq_build_index(pq_ctx* ctx) {
     ctx->ms_fm = f;
     // the sort and k-mer working memory is not needed by the search: give it back
     ctx->sorted_keys[0] = ctx->sorted_keys[1] = nullptr;
+    ctx->bwt_hint[0] = ctx->bwt_hint[1] = nullptr;
     ctx->sort_tmp.release();
     ctx->ktmp.release();
     return PQ_OK;

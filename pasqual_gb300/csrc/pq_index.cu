@@ -27,29 +27,33 @@ __device__ __forceinline__ int packed_at(const uint64_t* __restrict__ pk, size_t
 }
 
 // One warp per 64-row block: BWT symbol of each row (`$` for a read-start suffix, else the
-// preceding base, from the packed text when given: a quarter of the bytes of the text, so more of
-// it stays in L2), packed into lo/hi/dol masks with ballots; per-block symbol counts go into
-// cnt[] for the superblock pass.
+// preceding base), packed into lo/hi/dol masks with ballots; per-block symbol counts go into
+// cnt[] for the superblock pass.  A row's symbol comes from the sort's hints when it left one
+// (hint != 0xff: the rows its group refinement placed), else from the packed text when given (a
+// quarter of the bytes of the text, so more of it stays in L2), else from the text.
 __global__ void k_bwt_blocks(const idx_t* __restrict__ sa, const uint8_t* __restrict__ reads,
-                             const uint64_t* __restrict__ pk, idx_t n, idx_t L, int dir, idx_t nblk,
-                             OccBlock* __restrict__ blk) {
+                             const uint64_t* __restrict__ pk, const uint8_t* __restrict__ hint, idx_t n, idx_t L,
+                             int dir, idx_t nblk, OccBlock* __restrict__ blk) {
     constexpr int G = 4;                    // blocks per warp and round: 8 independent rows per lane
     const int lane = threadIdx.x & 31;
     const size_t warp = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const size_t nwarps = (size_t(gridDim.x) * blockDim.x) >> 5;
     for (size_t b0 = warp * G; b0 < nblk; b0 += nwarps * G) {
-        idx_t p[2 * G];
-        #pragma unroll
-        for (int x = 0; x < 2 * G; ++x) {
-            const size_t r = b0 * 64 + size_t(x) * 32 + lane;
-            p[x] = r < n ? sa[r] : idx_t(0);
-        }
         int sym[2 * G];
         #pragma unroll
         for (int x = 0; x < 2 * G; ++x) {
             const size_t r = b0 * 64 + size_t(x) * 32 + lane;
-            sym[x] = -1;
-            if (r < n) {
+            sym[x] = r < n ? (hint ? int(hint[r]) : 0xff) : -1;
+        }
+        idx_t p[2 * G];
+        #pragma unroll
+        for (int x = 0; x < 2 * G; ++x) {
+            const size_t r = b0 * 64 + size_t(x) * 32 + lane;
+            p[x] = sym[x] == 0xff ? sa[r] : idx_t(0);
+        }
+        #pragma unroll
+        for (int x = 0; x < 2 * G; ++x) {
+            if (sym[x] == 0xff) {
                 const idx_t off = p[x] % L;
                 sym[x] = off ? (pk ? packed_at(pk, size_t(p[x]) - 1) : text_at(reads, L, dir, p[x] - 1)) : 0;
             }
@@ -344,11 +348,12 @@ static inline unsigned grid_for(size_t work, int threads, int per_sm = 8) {
 }
 
 cudaError_t build_occ(const idx_t* sa, const uint8_t* reads, idx_t num_reads, idx_t L, int dir,
-                      OccBlock* blk, idx_t* sb, idx_t* reads_index, cudaStream_t st, const uint64_t* pk) {
+                      OccBlock* blk, idx_t* sb, idx_t* reads_index, cudaStream_t st, const uint64_t* pk,
+                      const uint8_t* hint) {
     const size_t n = size_t(num_reads) * L;
     const size_t nblk = n / 64 + 1;
     const size_t nsb = (nblk + kBlocksPerSuper - 1) / kBlocksPerSuper;
-    { k_bwt_blocks<<<grid_for(nblk * 32, 256), 256, 0, st>>>(sa, reads, pk, idx_t(n), L, dir, idx_t(nblk), blk); note_launch(); }
+    { k_bwt_blocks<<<grid_for(nblk * 32, 256), 256, 0, st>>>(sa, reads, pk, hint, idx_t(n), L, dir, idx_t(nblk), blk); note_launch(); }
     { k_super_prefix<<<unsigned(nsb), 256, 0, st>>>(blk, idx_t(nblk), sb); note_launch(); }
     { k_super_scan<<<1, 1024, 0, st>>>(sb, nsb); note_launch(); }
     { k_reads_index<<<grid_for(nblk * 32, 256), 256, 0, st>>>(sa, blk, sb, idx_t(n), L, idx_t(nblk), reads_index); note_launch(); }

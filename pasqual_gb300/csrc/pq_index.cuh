@@ -5,9 +5,11 @@
 namespace pq {
 
 // FM-index build from a suffix array (pq_index.cu)
-// pk: the packed text of direction dir (preferred for the BWT gathers), or nullptr
+// pk: the packed text of direction dir (preferred for the BWT gathers), or nullptr; hint: the
+// sort's per-row BWT symbols (0xff = none), or nullptr
 cudaError_t build_occ(const idx_t* sa, const uint8_t* reads, idx_t num_reads, idx_t L, int dir,
-                      OccBlock* blk, idx_t* sb, idx_t* reads_index, cudaStream_t st, const uint64_t* pk = nullptr);
+                      OccBlock* blk, idx_t* sb, idx_t* reads_index, cudaStream_t st, const uint64_t* pk = nullptr,
+                      const uint8_t* hint = nullptr);
 cudaError_t read_counts(const uint8_t* reads, idx_t num_reads, idx_t L, unsigned long long* out12,
                         cudaStream_t st);
 // k-mer table of direction dir; from the sort's keys when sorted_keys is given (one streaming

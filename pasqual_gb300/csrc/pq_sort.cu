@@ -355,19 +355,21 @@ size_t radix_tmp_bytes(size_t n) {
 
 template <class K, class V>
 int radix_sort_pairs(K** k0, V** v0, K** k1, V** v1, size_t n, int lo_bit, int hi_bit, void* tmp,
-                     size_t tmp_bytes, cudaStream_t st) {
+                     size_t tmp_bytes, cudaStream_t st, bool skip_trivial) {
     constexpr int D = int(sizeof(K));
     if (hi_bit > 8 * D) hi_bit = 8 * D;
     if (n <= 1) return 0;
     if (tmp_bytes < radix_tmp_bytes(n)) return int(cudaErrorInvalidValue);
     unsigned long long* cnt = reinterpret_cast<unsigned long long*>(tmp);
     unsigned long long* gh = cnt + size_t(256) * RS_MAX_CTAS;
-    cudaMemsetAsync(gh, 0, 8 * 256 * sizeof(unsigned long long), st);
-    { k_digit_hist<K><<<grid_for(n, 256, 4), 256, 0, st>>>(*k0, n, gh); note_launch(); }
-    std::vector<unsigned long long> h(size_t(D) * 256);
-    cudaMemcpyAsync(h.data(), gh, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
-    cudaError_t e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) return int(e);
+    std::vector<unsigned long long> h(size_t(D) * 256, 0);
+    if (skip_trivial) {
+        cudaMemsetAsync(gh, 0, 8 * 256 * sizeof(unsigned long long), st);
+        { k_digit_hist<K><<<grid_for(n, 256, 4), 256, 0, st>>>(*k0, n, gh); note_launch(); }
+        cudaMemcpyAsync(h.data(), gh, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return int(e);
+    }
     size_t tiles = (n + RS_TILE_MAX - 1) / RS_TILE_MAX;
     // one wave of resident CTAs
     size_t ctas = std::min<size_t>(tiles, std::min<size_t>(RS_MAX_CTAS, size_t(152) * RsCfg<K, V>::min_blocks));
@@ -393,13 +395,13 @@ int radix_sort_pairs(K** k0, V** v0, K** k1, V** v1, size_t n, int lo_bit, int h
 }
 
 template int radix_sort_pairs<uint64_t, uint32_t>(uint64_t**, uint32_t**, uint64_t**, uint32_t**, size_t, int, int,
-                                                  void*, size_t, cudaStream_t);
+                                                  void*, size_t, cudaStream_t, bool);
 template int radix_sort_pairs<uint64_t, uint64_t>(uint64_t**, uint64_t**, uint64_t**, uint64_t**, size_t, int, int,
-                                                  void*, size_t, cudaStream_t);
+                                                  void*, size_t, cudaStream_t, bool);
 template int radix_sort_pairs<uint32_t, uint32_t>(uint32_t**, uint32_t**, uint32_t**, uint32_t**, size_t, int, int,
-                                                  void*, size_t, cudaStream_t);
+                                                  void*, size_t, cudaStream_t, bool);
 template int radix_sort_pairs<uint32_t, uint64_t>(uint32_t**, uint64_t**, uint32_t**, uint64_t**, size_t, int, int,
-                                                  void*, size_t, cudaStream_t);
+                                                  void*, size_t, cudaStream_t, bool);
 
 // ------------------------------------------------------------------------------ group ranks
 
@@ -552,7 +554,15 @@ struct GroupLists {
     unsigned long long* list[4];
     unsigned long long* counts;             // [4]
     size_t cap[4];                          // entries (pairs for class 3)
+    uint8_t* bwt;                           // BWT symbols of the rows the refinement places, or null
 };
+
+// BWT symbol of the suffix at p: 0 (`$`) at a read start, else the preceding base (1..4)
+__device__ __forceinline__ uint8_t bwt_symbol(const uint64_t* __restrict__ pk, size_t p, idx_t L) {
+    if (p % size_t(L) == 0) return 0;
+    const size_t q = p - 1;
+    return uint8_t(((pk[q >> 5] >> (62 - 2 * int(q & 31))) & 3) + 1);
+}
 
 __device__ __forceinline__ int group_class(size_t m) {
     if (m < 2) return -1;
@@ -841,15 +851,18 @@ __device__ __forceinline__ bool item_less<8>(const RefineItem<8>& a, const Refin
 constexpr int kRefineThreads = 256;
 
 template <int W, int E>
-__global__ void __launch_bounds__(kRefineThreads) k_refine_warp(const unsigned long long* __restrict__ list,
+__global__ void __launch_bounds__(kRefineThreads, (E == 4 && W <= 4) ? 3 : 1) k_refine_warp(const unsigned long long* __restrict__ list,
                                                                 const unsigned long long* __restrict__ cnt,
                                                                 const uint64_t* __restrict__ pk, idx_t L,
-                                                                idx_t* __restrict__ val, int from) {
+                                                                idx_t* __restrict__ val, int from,
+                                                                uint8_t* __restrict__ bwt) {
     constexpr int kChunk = 8;
     constexpr int N = 32 * E;
     __shared__ idx_t spos[kRefineThreads / 32][N];
+    __shared__ uint8_t ssym[kRefineThreads / 32][N];
     const int lane = threadIdx.x & 31;
     idx_t* const mypos = spos[threadIdx.x >> 5];
+    uint8_t* const mysym = ssym[threadIdx.x >> 5];
     const size_t warp = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const size_t nwarps = (size_t(gridDim.x) * blockDim.x) >> 5;
     const size_t groups = *cnt;
@@ -892,6 +905,7 @@ __global__ void __launch_bounds__(kRefineThreads) k_refine_warp(const unsigned l
                     suffix_words<W>(pk, size_t(pos), int(len), from, it[e].w);
                     it[e].tail = (len << 8) | uint32_t(e * 32 + lane);
                     mypos[e * 32 + lane] = pos;
+                    if (bwt) mysym[e * 32 + lane] = bwt_symbol(pk, size_t(pos), L);
                 } else {
                     #pragma unroll
                     for (int j = 0; j < W; ++j) it[e].w[j] = ~uint64_t(0);
@@ -931,8 +945,12 @@ __global__ void __launch_bounds__(kRefineThreads) k_refine_warp(const unsigned l
             }
             __syncwarp();
             #pragma unroll
-            for (int e = 0; e < E; ++e)
-                if (seg[e] != 255) val[at[e]] = mypos[it[e].tail & 255u];
+            for (int e = 0; e < E; ++e) {
+                if (seg[e] != 255) {
+                    val[at[e]] = mypos[it[e].tail & 255u];
+                    if (bwt) bwt[at[e]] = mysym[it[e].tail & 255u];
+                }
+            }
             __syncwarp();
             next += taken;
         }
@@ -1001,7 +1019,8 @@ __device__ void cta_load_group(uint64_t* cols, int P2, size_t start, int m, cons
 
 template <int W>
 __global__ void k_refine_cta(const unsigned long long* __restrict__ list, const unsigned long long* __restrict__ cnt,
-                             const uint64_t* __restrict__ pk, idx_t L, idx_t* __restrict__ val, int off) {
+                             const uint64_t* __restrict__ pk, idx_t L, idx_t* __restrict__ val, int off,
+                             uint8_t* __restrict__ bwt) {
     extern __shared__ uint64_t s_cols[];
     const size_t groups = *cnt;
     for (size_t g = blockIdx.x; g < groups; g += gridDim.x) {
@@ -1013,7 +1032,10 @@ __global__ void k_refine_cta(const unsigned long long* __restrict__ list, const 
         cta_load_group<W>(s_cols, P2, start, m, pk, L, val, off);
         cta_bitonic<W>(s_cols, P2);
         const uint64_t* posc = s_cols + size_t(W + 1) * P2;
-        for (int i = threadIdx.x; i < m; i += blockDim.x) val[start + i] = idx_t(posc[i]);
+        for (int i = threadIdx.x; i < m; i += blockDim.x) {
+            val[start + i] = idx_t(posc[i]);
+            if (bwt) bwt[start + i] = bwt_symbol(pk, size_t(posc[i]), L);
+        }
         __syncthreads();
     }
 }
@@ -1037,17 +1059,17 @@ static void refine_small_mid(const GroupLists& G, const unsigned long long* c, c
                              idx_t* val, int off, cudaStream_t st) {
     if (c[0]) {
         unsigned g = unsigned(std::min<unsigned long long>((c[0] + 63) / 64, 152ull * 64));
-        { k_refine_warp<W, 1><<<g, kRefineThreads, 0, st>>>(G.list[0], G.counts + 0, pk, L, val, off); note_launch(); }
+        { k_refine_warp<W, 1><<<g, kRefineThreads, 0, st>>>(G.list[0], G.counts + 0, pk, L, val, off, G.bwt); note_launch(); }
     }
     if (c[1]) {
         unsigned g = unsigned(std::min<unsigned long long>((c[1] + 15) / 16, 152ull * 64));
-        { k_refine_warp<W, 4><<<g, kRefineThreads, 0, st>>>(G.list[1], G.counts + 1, pk, L, val, off); note_launch(); }
+        { k_refine_warp<W, 4><<<g, kRefineThreads, 0, st>>>(G.list[1], G.counts + 1, pk, L, val, off, G.bwt); note_launch(); }
     }
     if (c[2]) {
         const size_t smem = size_t(W + 2) * kGroupCta * sizeof(uint64_t);
         cudaFuncSetAttribute(k_refine_cta<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         unsigned g = unsigned(std::min<unsigned long long>(c[2], 152ull * 8));
-        { k_refine_cta<W><<<g, 512, smem, st>>>(G.list[2], G.counts + 2, pk, L, val, off); note_launch(); }
+        { k_refine_cta<W><<<g, 512, smem, st>>>(G.list[2], G.counts + 2, pk, L, val, off, G.bwt); note_launch(); }
     }
 }
 
@@ -1079,7 +1101,7 @@ static int refine_groups_w(const GroupLists& G, const unsigned long long* c0,
         idx_t* va = reinterpret_cast<idx_t*>(cols + 2 * kw);
         idx_t* vb = reinterpret_cast<idx_t*>(cols + 2 * kw + vw);
         { k_range_keys<<<grid_for(m, 256), 256, 0, st>>>(pk, val + it.start, m, L, it.off, ka, va); note_launch(); }
-        int rc = radix_sort_pairs<uint64_t, idx_t>(&ka, &va, &kb, &vb, m, 0, 64, rtmp, rtmp_bytes, st);
+        int rc = radix_sort_pairs<uint64_t, idx_t>(&ka, &va, &kb, &vb, m, 0, 64, rtmp, rtmp_bytes, st, true);
         if (rc) return rc;
         { k_copy_vals<idx_t><<<grid_for(m, 256), 256, 0, st>>>(va, m, val + it.start); note_launch(); }
         if (it.off + kWide >= int(L)) continue;          // every suffix is now fully compared
@@ -1109,7 +1131,7 @@ static int refine_groups_w(const GroupLists& G, const unsigned long long* c0,
 // under 0.55 n
 static int refine_groups(const uint32_t* key, idx_t* val, size_t n, idx_t L, const uint64_t* pk, uint64_t* lists_mem,
                          uint64_t* cols, size_t cols_cap, unsigned long long* counters, void* rtmp, size_t rtmp_bytes,
-                         cudaStream_t st) {
+                         cudaStream_t st, uint8_t* bwt = nullptr) {
     const int W = int((2 * (size_t(L) - kHead) + 63) / 64);
     if (W < 1 || W > kRefineMaxWords) return -1;
     GroupLists G;
@@ -1122,6 +1144,7 @@ static int refine_groups(const uint32_t* key, idx_t* val, size_t n, idx_t L, con
     G.list[2] = G.list[1] + G.cap[1];
     G.list[3] = G.list[2] + G.cap[2];
     G.counts = counters;
+    G.bwt = bwt;
     cudaMemsetAsync(counters, 0, 4 * sizeof(unsigned long long), st);
     { k_group_lists<uint32_t><<<unsigned(std::min<size_t>((n + kGlTile - 1) / kGlTile, size_t(152) * 64)), 256, 0, st>>>(
           key, n, G, 0); note_launch(); }
@@ -1153,14 +1176,15 @@ static size_t al(size_t b) { return (b + 255) & ~size_t(255); }
 
 size_t suffix_sort_tmp_bytes(size_t n) {
     size_t tiles = (n + HT_TILE - 1) / HT_TILE + 1;
-    return 2 * al(n * sizeof(uint64_t)) + 2 * al(n * sizeof(idx_t)) +
-           al(n * sizeof(uint32_t)) + al((n / 32 + 4) * sizeof(uint64_t)) + al(radix_tmp_bytes(n)) +
-           al(3 * tiles * sizeof(unsigned long long)) + 1024;
+    return 2 * al(n * sizeof(uint64_t)) + al(n * sizeof(idx_t)) + al(n * sizeof(uint32_t)) +
+           al((n / 32 + 4) * sizeof(uint64_t)) + al(radix_tmp_bytes(n)) + al(3 * tiles * sizeof(unsigned long long)) +
+           al(n) + 1024;
 }
 
 int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa, void* tmp, size_t tmp_bytes,
-                cudaStream_t st, const uint32_t** keys_out) {
+                cudaStream_t st, const uint32_t** keys_out, const uint8_t** bwt_out) {
     if (keys_out) *keys_out = nullptr;
+    if (bwt_out) *bwt_out = nullptr;
     const size_t n = size_t(num_reads) * size_t(L);
     if (n == 0) return 0;
     if (n >= (size_t(1) << 31)) return int(cudaErrorNotSupported);   // 32-bit group ranks
@@ -1168,7 +1192,8 @@ int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa
     char* p = static_cast<char*>(tmp);
     uint64_t* ka = reinterpret_cast<uint64_t*>(p); p += al(n * sizeof(uint64_t));
     uint64_t* kb = reinterpret_cast<uint64_t*>(p); p += al(n * sizeof(uint64_t));
-    idx_t* va = reinterpret_cast<idx_t*>(p); p += al(n * sizeof(idx_t));
+    // the values start in the suffix array itself (four radix passes bring them back there)
+    idx_t* va = sa;
     idx_t* vb = reinterpret_cast<idx_t*>(p); p += al(n * sizeof(idx_t));
     uint32_t* rank = reinterpret_cast<uint32_t*>(p); p += al(n * sizeof(uint32_t));
     const size_t nwords = n / 32 + 4;
@@ -1178,40 +1203,45 @@ int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa
     unsigned long long* tmax = reinterpret_cast<unsigned long long*>(p);
     unsigned long long* tcnt = tmax + tiles + 1;
     unsigned long long* groups = tcnt + tiles + 1;
+    p += al(3 * (tiles + 1) * sizeof(unsigned long long));
+    uint8_t* bwt = reinterpret_cast<uint8_t*>(p);    // BWT symbols of the refined rows, 0xff elsewhere
 
     idx_t* const vb0 = vb;                 // followed by rank in memory
+    auto finish = [&](const uint32_t* keys) {
+        if (va != sa) { k_copy_vals<idx_t><<<grid_for(n, 256), 256, 0, st>>>(va, n, sa); note_launch(); }
+        if (keys_out) *keys_out = keys;
+        return int(cudaGetLastError());
+    };
     { k_pack_text<<<grid_for(nwords, 256), 256, 0, st>>>(reads, n, idx_t(L), dir, nwords, pk); note_launch(); }
     // 32-bit head keys in the two 64-bit key buffers
     uint32_t* ha = reinterpret_cast<uint32_t*>(ka);
     uint32_t* hb = reinterpret_cast<uint32_t*>(kb);
     { k_init_keys<uint32_t><<<grid_for(n, 256), 256, 0, st>>>(pk, n, idx_t(L), ha, va); note_launch(); }
-    int rc = radix_sort_pairs<uint32_t, idx_t>(&ha, &va, &hb, &vb, n, 0, 32, rtmp, radix_tmp_bytes(n), st);
+    // all four digits vary on any real read set: no histogram pass, no host round trip
+    int rc = radix_sort_pairs<uint32_t, idx_t>(&ha, &va, &hb, &vb, n, 0, 32, rtmp, radix_tmp_bytes(n), st, false);
     if (rc) return rc;
-    if (size_t(L) <= size_t(kHead)) {   // every suffix fits in its key: already in final order
-        { k_copy_vals<idx_t><<<grid_for(n, 256), 256, 0, st>>>(va, n, sa); note_launch(); }
-        if (keys_out) *keys_out = ha;
-        return int(cudaGetLastError());
-    }
+    if (size_t(L) <= size_t(kHead)) return finish(ha);   // every suffix fits in its key: final order
     {
         // finish the groups where they lie; lists go to the free key buffer, big-group scratch to
-        // the free value buffer (and rank behind it when that buffer is the second one: the sorted
-        // values may have ended in either, depending on how many radix passes ran)
+        // the free value buffer (and rank behind it when that buffer is the scratch one; when the
+        // values ended in the scratch, the free one is the suffix array, exactly n entries)
         uint64_t* cols = reinterpret_cast<uint64_t*>(vb);
-        const size_t cols_cap = (al(n * sizeof(idx_t)) + (vb == vb0 ? al(n * sizeof(uint32_t)) : 0)) / sizeof(uint64_t);
+        const size_t cols_cap = vb == vb0 ? (al(n * sizeof(idx_t)) + al(n * sizeof(uint32_t))) / sizeof(uint64_t)
+                                          : n * sizeof(idx_t) / sizeof(uint64_t);
+        cudaMemsetAsync(bwt, 0xff, n, st);
         rc = refine_groups(ha, va, n, idx_t(L), pk, reinterpret_cast<uint64_t*>(hb), cols, cols_cap, tcnt, rtmp,
-                           radix_tmp_bytes(n), st);
+                           radix_tmp_bytes(n), st, bwt);
         if (rc > 0) return rc;
         if (rc == 0) {   // the refinement permutes suffixes within groups of equal keys only
-            { k_copy_vals<idx_t><<<grid_for(n, 256), 256, 0, st>>>(va, n, sa); note_launch(); }
-            if (keys_out) *keys_out = ha;
-            return int(cudaGetLastError());
+            if (bwt_out) *bwt_out = bwt;
+            return finish(ha);
         }
         // a group too large for the scratch (or reads longer than 270 bases): prefix doubling on
         // 29-base keys
         ka = reinterpret_cast<uint64_t*>(ha);
         kb = reinterpret_cast<uint64_t*>(hb);
         { k_init_keys<uint64_t><<<grid_for(n, 256), 256, 0, st>>>(pk, n, idx_t(L), ka, va); note_launch(); }
-        rc = radix_sort_pairs<uint64_t, idx_t>(&ka, &va, &kb, &vb, n, 0, 64, rtmp, radix_tmp_bytes(n), st);
+        rc = radix_sort_pairs<uint64_t, idx_t>(&ka, &va, &kb, &vb, n, 0, 64, rtmp, radix_tmp_bytes(n), st, true);
         if (rc) return rc;
     }
     for (size_t h = kWide;; h *= 2) {
@@ -1227,11 +1257,10 @@ int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa
         { k_second_keys<idx_t><<<grid_for(n, 256), 256, 0, st>>>(ka, va, n, idx_t(L), h, rank); note_launch(); }
         int bits = 1;
         while ((size_t(1) << bits) <= n + 1) ++bits;
-        rc = radix_sort_pairs<uint64_t, idx_t>(&ka, &va, &kb, &vb, n, 0, 32 + bits, rtmp, radix_tmp_bytes(n), st);
+        rc = radix_sort_pairs<uint64_t, idx_t>(&ka, &va, &kb, &vb, n, 0, 32 + bits, rtmp, radix_tmp_bytes(n), st, true);
         if (rc) return rc;
     }
-    { k_copy_vals<idx_t><<<grid_for(n, 256), 256, 0, st>>>(va, n, sa); note_launch(); }
-    return int(cudaGetLastError());
+    return finish(nullptr);
 }
 
 // ------------------------------------------------------------------------------ chunked sort
@@ -1395,7 +1424,7 @@ int suffix_sort_chunked(const uint8_t* reads, idx_t num_reads, int L, int dir, i
             { k_init_keys_list<idx_t><<<grid_for(m, 256), 256, 0, st>>>(pk, va0, m, idx_t(L), ka); note_launch(); }
             idx_t* va = va0;
             idx_t* vb = vb0;
-            int rc = radix_sort_pairs<uint32_t, idx_t>(&ka, &va, &kb, &vb, m, 0, 32, rtmp, radix_tmp_bytes(m), st);
+            int rc = radix_sort_pairs<uint32_t, idx_t>(&ka, &va, &kb, &vb, m, 0, 32, rtmp, radix_tmp_bytes(m), st, false);
             if (rc) return rc;
             if (size_t(L) > size_t(kHead)) {
                 // scratch: the free value buffer, and rank behind it when that is the second buffer

@@ -10,10 +10,13 @@ size_t suffix_sort_tmp_bytes(size_t n);
 // then text position).  Returns 0 or a cudaError_t value.  When keys_out is given it receives
 // the sorted 32-bit keys (first 14 bases in bits 31..4, then min(length, 14) in bits 3..0)
 // aligned with the suffix array, inside tmp (valid until tmp is reused), or nullptr when the sort
-// ended by prefix doubling (the key array then holds ranks).
+// ended by prefix doubling (the key array then holds ranks).  When bwt_out is given it receives
+// the BWT symbols (0 = `$`, 1..4) of the rows the group refinement placed, 0xff for the others,
+// inside tmp, or nullptr.
 constexpr int kSortKeyBases = 14;
 int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa, void* tmp,
-                size_t tmp_bytes, cudaStream_t st, const uint32_t** keys_out = nullptr);
+                size_t tmp_bytes, cudaStream_t st, const uint32_t** keys_out = nullptr,
+                const uint8_t** bwt_out = nullptr);
 
 // The same order for inputs too large for one pass: suffixes bucketed by their first 6 bases,
 // consecutive buckets sorted in chunks of at most cap (< 2^31) suffixes.  Returns
@@ -28,10 +31,11 @@ cudaError_t read_seeds(const uint8_t* reads, idx_t num_reads, int L, int dir, in
 
 // Stable LSD radix sort of (key, value) pairs on the bits [lo_bit, hi_bit) of the key (K is
 // uint32_t or uint64_t).  Buffers are ping-ponged; the sorted result ends in (*k0, *v0) (pointers
-// may be swapped).
+// may be swapped).  skip_trivial: first histogram every digit (one pass and a host round trip)
+// and skip the digits that are constant over all keys; else run every digit pass.
 template <class K, class V>
 int radix_sort_pairs(K** k0, V** v0, K** k1, V** v1, size_t n, int lo_bit, int hi_bit,
-                     void* tmp, size_t tmp_bytes, cudaStream_t st);
+                     void* tmp, size_t tmp_bytes, cudaStream_t st, bool skip_trivial = true);
 size_t radix_tmp_bytes(size_t n);
 
 // The text of direction dir packed 32 bases per 64-bit word, first base in the top bits
