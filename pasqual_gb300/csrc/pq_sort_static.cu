@@ -1,7 +1,7 @@
 // pq_sort_static.cu — a suffix sort that allocates no device memory.
 //
-// pq_sort() allocates its working memory (keys, values, ranks, packed text, radix histograms:
-// about 28 bytes per suffix) with cudaMalloc on first use.  Some callers cannot do that: code
+// pq_sort() allocates its working memory (keys, values, ranks, packed text, BWT symbols, radix
+// histograms: about 25 bytes per suffix) with cudaMalloc on first use.  Some callers cannot do that: code
 // that runs inside a host application which owns every byte of device memory through its own
 // pool and forbids direct cudaMalloc (an assembler or read-correction tool that embeds this sort
 // for many small per-bucket sorts), and code on latency-critical paths where cudaMalloc's
@@ -24,12 +24,13 @@ namespace {
 constexpr size_t al256(size_t b) { return (b + 255) & ~size_t(255); }
 constexpr size_t kMax = PQ_STATIC_SORT_MAX_SUFFIXES;
 
-// Upper bound of pq::suffix_sort_tmp_bytes(kMax): key and value double buffers, 32-bit ranks,
-// packed text, radix histograms of up to 608 CTAs plus 8 digit histograms, per-tile head data.
+// Upper bound of pq::suffix_sort_tmp_bytes(kMax): key double buffer, one value buffer (the other
+// is the caller's suffix array), 32-bit ranks, packed text, radix histograms of up to 608 CTAs
+// plus 8 digit histograms, per-tile head data, one BWT-symbol byte per suffix.
 constexpr size_t kScratchBytes =
-    2 * al256(kMax * sizeof(uint64_t)) + 2 * al256(kMax * sizeof(idx_t)) + al256(kMax * sizeof(uint32_t)) +
+    2 * al256(kMax * sizeof(uint64_t)) + al256(kMax * sizeof(idx_t)) + al256(kMax * sizeof(uint32_t)) +
     al256((kMax / 32 + 4) * sizeof(uint64_t)) + al256((256 * 608 + 8 * 256 + 64) * sizeof(unsigned long long)) +
-    al256(3 * (kMax / 2048 + 2) * sizeof(unsigned long long)) + 1024;
+    al256(3 * (kMax / 2048 + 2) * sizeof(unsigned long long)) + al256(kMax) + 1024;
 
 __device__ __align__(256) unsigned char g_sort_scratch[kScratchBytes];
 
