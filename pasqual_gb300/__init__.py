@@ -310,18 +310,27 @@ class Pasqual:
     def overlaps(self) -> None:
         self._ck(self.lib.pq_overlaps(self.h), "pq_overlaps")
 
-    def graph(self) -> Graph:
+    def graph(self, out: Graph | None = None) -> Graph:
+        """The last overlap search's graph.  With `out` (an earlier result, or any Graph whose
+        arrays are at least as long), the arrays are filled in place and views of the right
+        lengths are returned: host buffers that are reused skip the page faults of fresh ones."""
         ne = ct.c_uint64()
         pr = ct.c_uint64()
         wr = ct.c_uint64()
         self._ck(self.lib.pq_get_graph_sizes(self.h, ct.byref(ne), ct.byref(pr), ct.byref(wr)),
                  "pq_get_graph_sizes")
         nr, m = self.num_reads, ne.value
-        g = Graph(num_B=np.empty(nr, np.uint16), num_F=np.empty(nr, np.uint16),
-                  olp_B=np.empty(nr, np.int32), olp_F=np.empty(nr, np.int32),
-                  edge_off=np.empty(nr + 1, np.uint64), dest=np.empty(m, self.dt),
-                  length=np.empty(m, np.uint16), etype=np.empty(m, np.uint8),
-                  trans=np.empty(m, np.int32), probes=pr.value, wide_reads=wr.value)
+        want = {"num_B": (nr, np.uint16), "num_F": (nr, np.uint16), "olp_B": (nr, np.int32),
+                "olp_F": (nr, np.int32), "edge_off": (nr + 1, np.uint64), "dest": (m, self.dt),
+                "length": (m, np.uint16), "etype": (m, np.uint8), "trans": (m, np.int32)}
+        arrays = {}
+        for name, (size, dt) in want.items():
+            a = getattr(out, name, None) if out is not None else None
+            if (a is None or a.dtype != np.dtype(dt) or a.ndim != 1 or len(a) < size
+                    or not a.flags.c_contiguous or not a.flags.writeable):
+                a = np.empty(size, dt)
+            arrays[name] = a[:size]
+        g = Graph(**arrays, probes=pr.value, wide_reads=wr.value)
         self._ck(self.lib.pq_get_graph(self.h, _p(g.num_B), _p(g.num_F), _p(g.olp_B), _p(g.olp_F),
                                        _p(g.edge_off), _p(g.dest), _p(g.length), _p(g.etype),
                                        _p(g.trans)), "pq_get_graph")

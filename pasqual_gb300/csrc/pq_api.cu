@@ -401,11 +401,16 @@ int pq_build_index(pq_ctx* ctx) {
     }
     ctx->ms_sort = s;
     ctx->ms_fm = f;
-    // the sort and k-mer working memory is not needed by the search: give it back
+    // the sort and k-mer working memory is not needed by the search: give it back when device
+    // memory is short (under a quarter free), else keep it for the next build of the same size
+    // (a cudaMalloc and cudaFree of tens of GB per build)
     ctx->sorted_keys[0] = ctx->sorted_keys[1] = nullptr;
     ctx->bwt_hint[0] = ctx->bwt_hint[1] = nullptr;
-    ctx->sort_tmp.release();
-    ctx->ktmp.release();
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess || free_b < total_b / 4) {
+        ctx->sort_tmp.release();
+        ctx->ktmp.release();
+    }
     return PQ_OK;
 }
 
