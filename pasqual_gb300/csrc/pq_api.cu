@@ -236,12 +236,20 @@ int pq_set_reads(pq_ctx* ctx, const uint8_t* reads, pq_idx num_reads, int read_l
     if (bytes)
         CK(cudaMemcpyAsync(ctx->reads.p, reads, bytes, from_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                            ctx->st));
-    CK(ctx->counts.ensure(12 * sizeof(unsigned long long)));
+    CK(ctx->counts.ensure(13 * sizeof(unsigned long long)));
     CK(pq::read_counts(ctx->reads.as<uint8_t>(), num_reads, idx_t(read_len),
                        ctx->counts.as<unsigned long long>(), ctx->st));
-    unsigned long long h[12];
+    unsigned long long h[13];
     CK(cudaMemcpyAsync(h, ctx->counts.p, sizeof h, cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
+    if (h[12]) {   // the reference's import drops reads with N and rejects any other symbol
+        ctx->have_reads = false;
+        ctx->num_reads = 0;
+        ctx->sa_ok[0] = ctx->sa_ok[1] = false;
+        ctx->fm_ok[0] = ctx->fm_ok[1] = false;
+        ctx->graph_ok = false;
+        return fail(ctx, PQ_ERR_ARG, "reads must hold base codes 1..4 (A, C, G, T) only");
+    }
     ctx->C[0] = 0;
     ctx->C[1] = 0;
     ctx->C[2] = idx_t(h[0]);

@@ -209,24 +209,54 @@ __global__ void k_reads_index(const idx_t* __restrict__ sa, const OccBlock* __re
     }
 }
 
-// Read statistics: C[] (src/index.c:367-372), suffix_count / prefix_count (src/index.c:336-346).
+// Read statistics: C[] (src/index.c:367-372), suffix_count / prefix_count (src/index.c:336-346),
+// and the number of bytes that are not base codes 1..4.  The base counts stream the read set
+// 16 bytes a thread at a time (coalesced); the first and last base of every read are a strided
+// pass over the reads.
+__device__ __forceinline__ void count_word(uint32_t w, unsigned long long (&loc)[5]) {
+    #pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        const uint32_t c = (w >> (8 * b)) & 0xffu;
+        if (c >= 1 && c <= 4) loc[c - 1]++;
+        else loc[4]++;
+    }
+}
+
 __global__ void k_read_counts(const uint8_t* __restrict__ reads, idx_t nr, idx_t L,
-                              unsigned long long* __restrict__ out /* base[4], sfx[4], pfx[4] */) {
-    __shared__ unsigned long long acc[12];
-    if (threadIdx.x < 12) acc[threadIdx.x] = 0;
+                              unsigned long long* __restrict__ out /* base[4], sfx[4], pfx[4], bad */) {
+    __shared__ unsigned long long acc[13];
+    if (threadIdx.x < 13) acc[threadIdx.x] = 0;
     __syncthreads();
-    unsigned long long loc[12] = {0};
+    unsigned long long loc[5] = {0, 0, 0, 0, 0}, ends[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const size_t n = size_t(nr) * size_t(L);
+    const size_t tid = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     const size_t stride = size_t(gridDim.x) * blockDim.x;
-    for (size_t r = size_t(blockIdx.x) * blockDim.x + threadIdx.x; r < nr; r += stride) {
-        const uint8_t* s = reads + r * L;
-        loc[4 + s[L - 1] - 1]++;
-        loc[8 + s[0] - 1]++;
-        for (idx_t j = 0; j < L; ++j) loc[s[j] - 1]++;
+    const size_t n16 = reinterpret_cast<uintptr_t>(reads) % 16 == 0 ? n / 16 : 0;
+    const uint4* v = reinterpret_cast<const uint4*>(reads);
+    for (size_t i = tid; i < n16; i += stride) {
+        const uint4 q = v[i];
+        count_word(q.x, loc);
+        count_word(q.y, loc);
+        count_word(q.z, loc);
+        count_word(q.w, loc);
+    }
+    for (size_t i = n16 * 16 + tid; i < n; i += stride) {
+        const uint32_t c = reads[i];
+        if (c >= 1 && c <= 4) loc[c - 1]++;
+        else loc[4]++;
+    }
+    for (size_t r = tid; r < size_t(nr); r += stride) {
+        const uint32_t last = reads[r * L + L - 1], first = reads[r * L];
+        if (last >= 1 && last <= 4) ends[last - 1]++;
+        if (first >= 1 && first <= 4) ends[4 + first - 1]++;
     }
     #pragma unroll
-    for (int k = 0; k < 12; ++k) if (loc[k]) atomicAdd(&acc[k], loc[k]);
+    for (int k = 0; k < 4; ++k) if (loc[k]) atomicAdd(&acc[k], loc[k]);
+    #pragma unroll
+    for (int k = 0; k < 8; ++k) if (ends[k]) atomicAdd(&acc[4 + k], ends[k]);
+    if (loc[4]) atomicAdd(&acc[12], loc[4]);
     __syncthreads();
-    if (threadIdx.x < 12 && acc[threadIdx.x]) atomicAdd(&out[threadIdx.x], acc[threadIdx.x]);
+    if (threadIdx.x < 13 && acc[threadIdx.x]) atomicAdd(&out[threadIdx.x], acc[threadIdx.x]);
 }
 
 // k-mer seed table: rows whose suffix starts with a given k-mer are contiguous in a sorted SA;
@@ -360,10 +390,10 @@ cudaError_t build_occ(const idx_t* sa, const uint8_t* reads, idx_t num_reads, id
     return cudaGetLastError();
 }
 
-cudaError_t read_counts(const uint8_t* reads, idx_t num_reads, idx_t L, unsigned long long* out12,
+cudaError_t read_counts(const uint8_t* reads, idx_t num_reads, idx_t L, unsigned long long* out13,
                         cudaStream_t st) {
-    cudaMemsetAsync(out12, 0, 12 * sizeof(unsigned long long), st);
-    if (num_reads) { k_read_counts<<<grid_for(num_reads, 256), 256, 0, st>>>(reads, num_reads, L, out12); note_launch(); }
+    cudaMemsetAsync(out13, 0, 13 * sizeof(unsigned long long), st);
+    if (num_reads) { k_read_counts<<<grid_for(size_t(num_reads) * L / 16 + 1, 256), 256, 0, st>>>(reads, num_reads, L, out13); note_launch(); }
     return cudaGetLastError();
 }
 

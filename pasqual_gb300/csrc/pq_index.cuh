@@ -10,7 +10,8 @@ namespace pq {
 cudaError_t build_occ(const idx_t* sa, const uint8_t* reads, idx_t num_reads, idx_t L, int dir,
                       OccBlock* blk, idx_t* sb, idx_t* reads_index, cudaStream_t st, const uint64_t* pk = nullptr,
                       const uint8_t* hint = nullptr);
-cudaError_t read_counts(const uint8_t* reads, idx_t num_reads, idx_t L, unsigned long long* out12,
+// out13: base counts [4], last-base counts [4], first-base counts [4], bytes outside 1..4
+cudaError_t read_counts(const uint8_t* reads, idx_t num_reads, idx_t L, unsigned long long* out13,
                         cudaStream_t st);
 // k-mer table of direction dir; from the sort's keys when sorted_keys is given (one streaming
 // pass), else from the suffix array and the text

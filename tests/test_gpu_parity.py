@@ -204,3 +204,37 @@ def test_invalid_arguments_raise():
             P.set_reads(np.ones((10, 50), np.uint8), 50)     # t must be below L
         with pytest.raises(pq.PQError):
             P.overlaps()                                     # no index yet
+        for bad in (0, 5, 78):                               # only base codes 1..4 (the import drops N)
+            r = np.ones((40, 50), np.uint8)
+            r[17, 33] = bad
+            with pytest.raises(pq.PQError):
+                P.set_reads(r, 20)
+        r = np.random.default_rng(3).integers(1, 5, (40, 50), dtype=np.uint8)
+        P.set_reads(r, 20)                                   # a valid set after a rejected one
+        C, sfx, pfx = P.counts()
+        assert int(C[5]) == r.size and int(sfx.sum()) == 40 and int(pfx.sum()) == 40
+
+
+def test_graph_into_reused_arrays():
+    """graph(out=...) fills an earlier result's arrays in place (views of the new lengths) and
+    gives the same graph as fresh arrays; too-small or mistyped arrays are replaced."""
+    big, small = load_golden("rep15k_L100_t63_u32"), load_golden("iid8k_L50_t31_u32")
+    with gpu_ctx(32) as P:
+        P.construct_index(big["reads"], int(big["t"]))
+        g_big = P.construct_string_graph()
+        P.construct_index(small["reads"], int(small["t"]))
+        P.overlaps()
+        fresh = P.graph()
+        reused = P.graph(out=g_big)
+        for name in ("num_B", "num_F", "olp_B", "olp_F", "edge_off", "dest", "length", "etype", "trans"):
+            a, b = getattr(fresh, name), getattr(reused, name)
+            assert np.array_equal(a, b), name
+        if len(g_big.dest) >= len(fresh.dest):
+            assert np.shares_memory(reused.dest, g_big.dest)
+        assert len(reused.dest) == int(small["num_edges"])
+        # arrays too short for the bigger graph are replaced, not overrun
+        P.construct_index(big["reads"], int(big["t"]))
+        P.overlaps()
+        again = P.graph(out=reused)
+        assert len(again.dest) == int(big["num_edges"])
+        assert sha(again.dest) == str(big["sha_dest"])
