@@ -81,6 +81,7 @@ struct pq_ctx {
     DevBuf ktmp, sort_tmp, counts;
     const uint32_t* sorted_keys[2] = {nullptr, nullptr};   // the last sort's keys, inside sort_tmp
     const uint8_t* bwt_hint[2] = {nullptr, nullptr};       // the last sort's BWT symbols, inside sort_tmp
+    bool pk_ok[2] = {false, false};                        // pk[dir] holds this read set's packed text
     uint64_t sort_chunk = 0;                                // suffixes per sort chunk (0: automatic)
 
     // learned index per direction (pq_learned.cu)
@@ -245,6 +246,7 @@ int pq_set_reads(pq_ctx* ctx, const uint8_t* reads, pq_idx num_reads, int read_l
     if (h[12]) {   // the reference's import drops reads with N and rejects any other symbol
         ctx->have_reads = false;
         ctx->num_reads = 0;
+        ctx->pk_ok[0] = ctx->pk_ok[1] = false;
         ctx->sa_ok[0] = ctx->sa_ok[1] = false;
         ctx->fm_ok[0] = ctx->fm_ok[1] = false;
         ctx->graph_ok = false;
@@ -261,6 +263,7 @@ int pq_set_reads(pq_ctx* ctx, const uint8_t* reads, pq_idx num_reads, int read_l
         ctx->pfx[c] = idx_t(h[8 + c]);
     }
     ctx->have_reads = true;
+    ctx->pk_ok[0] = ctx->pk_ok[1] = false;
     ctx->sa_ok[0] = ctx->sa_ok[1] = false;
     ctx->fm_ok[0] = ctx->fm_ok[1] = false;
     ctx->graph_ok = false;
@@ -282,6 +285,7 @@ int pq_sort(pq_ctx* ctx, int dir) {
     cudaSetDevice(ctx->device);
     const size_t n = n_rows(ctx);
     CK(ctx->sa[dir].ensure(n * sizeof(idx_t) + 64));
+    CK(ctx->pk[dir].ensure((n / 32 + 4) * sizeof(uint64_t)));
     // one pass below 2^31 suffixes (32-bit group ranks), else chunks of 6-base buckets
     const size_t one_pass_max = (size_t(1) << 31) - 1;
     const bool chunked = n > one_pass_max || (ctx->sort_chunk && n > ctx->sort_chunk);
@@ -295,7 +299,8 @@ int pq_sort(pq_ctx* ctx, int dir) {
                                                ctx->sa[dir].as<idx_t>(), cap, ctx->sort_tmp.p, tmp_bytes, ctx->st)
                      : pq::suffix_sort(ctx->reads.as<uint8_t>(), ctx->num_reads, ctx->L, dir,
                                        ctx->sa[dir].as<idx_t>(), ctx->sort_tmp.p, tmp_bytes, ctx->st,
-                                       &ctx->sorted_keys[dir], &ctx->bwt_hint[dir]);
+                                       &ctx->sorted_keys[dir], &ctx->bwt_hint[dir], ctx->pk[dir].as<uint64_t>());
+    ctx->pk_ok[dir] = !chunked && rc == 0;
     if (rc == int(cudaErrorNotSupported))
         return fail(ctx, PQ_ERR_CAPACITY, "suffix sort: a 6-base bucket holds more suffixes than a sort chunk");
     if (rc != 0) return fail(ctx, PQ_ERR_CUDA, std::string("suffix sort failed: ") + cudaGetErrorString(cudaGetLastError()));
@@ -377,7 +382,9 @@ int pq_build_fm(pq_ctx* ctx, int dir) {
     const size_t isa_n = size_t(ctx->num_reads) * size_t(ctx->L - ctx->t);
     CK(ctx->isa[dir].ensure(isa_n * sizeof(idx_t) + 64));
     CK(cudaEventRecord(ctx->ev0, ctx->st));
-    CK(pq::pack_text(ctx->reads.as<uint8_t>(), n, idx_t(ctx->L), dir, ctx->pk[dir].as<uint64_t>(), ctx->st));
+    if (!ctx->pk_ok[dir])
+        CK(pq::pack_text(ctx->reads.as<uint8_t>(), n, idx_t(ctx->L), dir, ctx->pk[dir].as<uint64_t>(), ctx->st));
+    ctx->pk_ok[dir] = true;
     CK(pq::build_occ(ctx->sa[dir].as<idx_t>(), ctx->reads.as<uint8_t>(), ctx->num_reads, idx_t(ctx->L), dir,
                      ctx->blk[dir].as<OccBlock>(), ctx->sb[dir].as<idx_t>(), ctx->ri[dir].as<idx_t>(), ctx->st,
                      ctx->pk[dir].as<uint64_t>(), ctx->bwt_hint[dir]));

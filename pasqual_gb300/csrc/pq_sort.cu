@@ -851,7 +851,7 @@ __device__ __forceinline__ bool item_less<8>(const RefineItem<8>& a, const Refin
 constexpr int kRefineThreads = 256;
 
 template <int W, int E>
-__global__ void __launch_bounds__(kRefineThreads, (E == 4 && W <= 4) ? 3 : 1) k_refine_warp(const unsigned long long* __restrict__ list,
+__global__ void __launch_bounds__(kRefineThreads, E == 1 ? (W <= 3 ? 5 : 1) : (W <= 4 ? 3 : 1)) k_refine_warp(const unsigned long long* __restrict__ list,
                                                                 const unsigned long long* __restrict__ cnt,
                                                                 const uint64_t* __restrict__ pk, idx_t L,
                                                                 idx_t* __restrict__ val, int from,
@@ -1182,7 +1182,7 @@ size_t suffix_sort_tmp_bytes(size_t n) {
 }
 
 int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa, void* tmp, size_t tmp_bytes,
-                cudaStream_t st, const uint32_t** keys_out, const uint8_t** bwt_out) {
+                cudaStream_t st, const uint32_t** keys_out, const uint8_t** bwt_out, uint64_t* pk_out) {
     if (keys_out) *keys_out = nullptr;
     if (bwt_out) *bwt_out = nullptr;
     const size_t n = size_t(num_reads) * size_t(L);
@@ -1197,7 +1197,8 @@ int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa
     idx_t* vb = reinterpret_cast<idx_t*>(p); p += al(n * sizeof(idx_t));
     uint32_t* rank = reinterpret_cast<uint32_t*>(p); p += al(n * sizeof(uint32_t));
     const size_t nwords = n / 32 + 4;
-    uint64_t* pk = reinterpret_cast<uint64_t*>(p); p += al(nwords * sizeof(uint64_t));
+    uint64_t* pk = pk_out ? pk_out : reinterpret_cast<uint64_t*>(p);
+    p += al(nwords * sizeof(uint64_t));
     void* rtmp = p; p += al(radix_tmp_bytes(n));
     const size_t tiles = (n + HT_TILE - 1) / HT_TILE;
     unsigned long long* tmax = reinterpret_cast<unsigned long long*>(p);

@@ -12,11 +12,12 @@ size_t suffix_sort_tmp_bytes(size_t n);
 // aligned with the suffix array, inside tmp (valid until tmp is reused), or nullptr when the sort
 // ended by prefix doubling (the key array then holds ranks).  When bwt_out is given it receives
 // the BWT symbols (0 = `$`, 1..4) of the rows the group refinement placed, 0xff for the others,
-// inside tmp, or nullptr.
+// inside tmp, or nullptr.  pk_out (n/32 + 4 words), when given, receives the packed text of the
+// direction (see pack_text) instead of tmp.
 constexpr int kSortKeyBases = 14;
 int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa, void* tmp,
                 size_t tmp_bytes, cudaStream_t st, const uint32_t** keys_out = nullptr,
-                const uint8_t** bwt_out = nullptr);
+                const uint8_t** bwt_out = nullptr, uint64_t* pk_out = nullptr);
 
 // The same order for inputs too large for one pass: suffixes bucketed by their first 6 bases,
 // consecutive buckets sorted in chunks of at most cap (< 2^31) suffixes.  Returns
