@@ -120,6 +120,10 @@ WORKLOADS = {
     # learned-index workload: 12 % repeats, 2 % dinucleotide runs; 64-bit index
     "200Mbp_L150_20x_t63": dict(genome=200_000_000, gc=0.40, repeat=0.12, div=(0.01, 0.01),
                                 lowc=0.02, L=150, cov=20, err=0.003, t=63, index=64),
+    # large single-GPU workload: 15 % repeats at 0.5-2 % divergence, 50 M reads, 64-bit index,
+    # 5 G suffixes per index (sorted in chunks)
+    "250Mbp_L100_20x_t55": dict(genome=250_000_000, gc=0.42, repeat=0.15, div=(0.005, 0.02),
+                                lowc=0.0, L=100, cov=20, err=0.005, t=55, index=64),
 }
 
 # Queued-search workload: one genome, several read sets, each with its own read length (uniform
