@@ -296,11 +296,12 @@ int pq_sort(pq_ctx* ctx, int dir) {
     ctx->sorted_keys[0] = ctx->sorted_keys[1] = nullptr;     // the scratch is about to be reused
     ctx->bwt_hint[0] = ctx->bwt_hint[1] = nullptr;
     int rc = chunked ? pq::suffix_sort_chunked(ctx->reads.as<uint8_t>(), ctx->num_reads, ctx->L, dir,
-                                               ctx->sa[dir].as<idx_t>(), cap, ctx->sort_tmp.p, tmp_bytes, ctx->st)
+                                               ctx->sa[dir].as<idx_t>(), cap, ctx->sort_tmp.p, tmp_bytes, ctx->st,
+                                               &ctx->bwt_hint[dir], ctx->pk[dir].as<uint64_t>())
                      : pq::suffix_sort(ctx->reads.as<uint8_t>(), ctx->num_reads, ctx->L, dir,
                                        ctx->sa[dir].as<idx_t>(), ctx->sort_tmp.p, tmp_bytes, ctx->st,
                                        &ctx->sorted_keys[dir], &ctx->bwt_hint[dir], ctx->pk[dir].as<uint64_t>());
-    ctx->pk_ok[dir] = !chunked && rc == 0;
+    ctx->pk_ok[dir] = rc == 0;
     if (rc == int(cudaErrorNotSupported))
         return fail(ctx, PQ_ERR_CAPACITY, "suffix sort: a 6-base bucket holds more suffixes than a sort chunk");
     if (rc != 0) return fail(ctx, PQ_ERR_CUDA, std::string("suffix sort failed: ") + cudaGetErrorString(cudaGetLastError()));
@@ -377,7 +378,6 @@ int pq_build_fm(pq_ctx* ctx, int dir) {
     const size_t nk = size_t(1) << (2 * k);
     CK(ctx->kstart[dir].ensure(nk * sizeof(idx_t)));
     CK(ctx->kend[dir].ensure(nk * sizeof(idx_t)));
-    if (!ctx->sorted_keys[dir]) CK(ctx->ktmp.ensure(n * sizeof(uint32_t) + 64));
     CK(ctx->pk[dir].ensure((n / 32 + 4) * sizeof(uint64_t)));
     const size_t isa_n = size_t(ctx->num_reads) * size_t(ctx->L - ctx->t);
     CK(ctx->isa[dir].ensure(isa_n * sizeof(idx_t) + 64));
@@ -390,7 +390,7 @@ int pq_build_fm(pq_ctx* ctx, int dir) {
                      ctx->pk[dir].as<uint64_t>(), ctx->bwt_hint[dir]));
     CK(pq::build_kmer_table(ctx->sa[dir].as<idx_t>(), ctx->reads.as<uint8_t>(), ctx->num_reads, idx_t(ctx->L), dir,
                             k, ctx->ktmp.as<uint32_t>(), ctx->kstart[dir].as<idx_t>(), ctx->kend[dir].as<idx_t>(),
-                            ctx->st, ctx->sorted_keys[dir]));
+                            ctx->st, ctx->sorted_keys[dir], ctx->pk[dir].as<uint64_t>()));
     CK(pq::build_isa(ctx->sa[dir].as<idx_t>(), n, idx_t(ctx->L), idx_t(ctx->L - ctx->t), ctx->isa[dir].as<idx_t>(),
                      ctx->st));
     CK(cudaEventRecord(ctx->ev1, ctx->st));

@@ -277,6 +277,39 @@ __global__ void k_kmer_codes(const idx_t* __restrict__ sa, const uint8_t* __rest
     }
 }
 
+// k-mer table from the packed text, one pass: a warp takes 32 consecutive rows, each lane the
+// k-mer of its row's suffix (all-ones when shorter than k) from one 64-bit window of the packed
+// text; neighbours' k-mers come by shuffle (the warp's edge lanes fetch theirs).
+__device__ __forceinline__ uint32_t kmer_at(const idx_t* __restrict__ sa, const uint64_t* __restrict__ pk,
+                                            size_t r, idx_t L, int k) {
+    const size_t p = size_t(sa[r]);
+    const idx_t off = idx_t(p % size_t(L));
+    if (L - off < idx_t(k)) return 0xffffffffu;
+    const size_t w = p >> 5;
+    const int sh = int(p & 31) * 2;
+    const uint64_t x = sh ? ((pk[w] << sh) | (pk[w + 1] >> (64 - sh))) : pk[w];
+    return uint32_t(x >> (64 - 2 * k));
+}
+
+__global__ void k_kmer_bounds_pk(const idx_t* __restrict__ sa, const uint64_t* __restrict__ pk, size_t n, idx_t L,
+                                 int k, idx_t* __restrict__ kstart, idx_t* __restrict__ kend) {
+    const int lane = threadIdx.x & 31;
+    const size_t warp = (size_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const size_t nwarps = (size_t(gridDim.x) * blockDim.x) >> 5;
+    for (size_t base = warp * 32; base < n; base += nwarps * 32) {
+        const size_t r = base + lane;
+        const uint32_t c = r < n ? kmer_at(sa, pk, r, L, k) : 0xffffffffu;
+        uint32_t prev = __shfl_up_sync(0xffffffffu, c, 1);
+        uint32_t next = __shfl_down_sync(0xffffffffu, c, 1);
+        if (lane == 0) prev = r > 0 && r < n ? kmer_at(sa, pk, r - 1, L, k) : 0xfffffffeu;
+        if (lane == 31) next = r + 1 < n ? kmer_at(sa, pk, r + 1, L, k) : 0xfffffffeu;
+        if (r < n && c != 0xffffffffu) {
+            if (r == 0 || prev != c) kstart[c] = idx_t(r);
+            if (r + 1 == n || next != c) kend[c] = idx_t(r);
+        }
+    }
+}
+
 // k-mer table straight from the sorted suffix keys (first 14 bases in bits 31..4, min(length, 14)
 // in bits 3..0), read in order: a row's k-mer is the key's top 2k bits when the suffix has k bases
 __device__ __forceinline__ uint32_t key_code(uint32_t key, int k) {
@@ -399,13 +432,15 @@ cudaError_t read_counts(const uint8_t* reads, idx_t num_reads, idx_t L, unsigned
 
 cudaError_t build_kmer_table(const idx_t* sa, const uint8_t* reads, idx_t num_reads, idx_t L, int dir,
                              int k, uint32_t* code_tmp, idx_t* kstart, idx_t* kend, cudaStream_t st,
-                             const uint32_t* sorted_keys) {
+                             const uint32_t* sorted_keys, const uint64_t* pk) {
     const size_t n = size_t(num_reads) * L;
     const size_t nk = size_t(1) << (2 * k);
     { k_fill_idx<<<grid_for(nk, 256), 256, 0, st>>>(kstart, nk, idx_t(1)); note_launch(); }
     { k_fill_idx<<<grid_for(nk, 256), 256, 0, st>>>(kend, nk, idx_t(0)); note_launch(); }
     if (n && sorted_keys && k <= kSortKeyBases) {
         { k_kmer_bounds_keys<<<grid_for(n, 256), 256, 0, st>>>(sorted_keys, idx_t(n), k, kstart, kend); note_launch(); }
+    } else if (n && pk) {
+        { k_kmer_bounds_pk<<<grid_for(n, 256), 256, 0, st>>>(sa, pk, n, L, k, kstart, kend); note_launch(); }
     } else if (n) {
         { k_kmer_codes<<<grid_for(n, 256), 256, 0, st>>>(sa, reads, idx_t(n), L, dir, k, code_tmp); note_launch(); }
         { k_kmer_bounds<<<grid_for(n, 256), 256, 0, st>>>(code_tmp, idx_t(n), kstart, kend); note_launch(); }

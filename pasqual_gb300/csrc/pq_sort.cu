@@ -1356,7 +1356,7 @@ __global__ void k_init_keys_list(const uint64_t* __restrict__ pk, const V* __res
     }
 }
 
-static size_t chunk_parts(size_t n, size_t cap, size_t (&b)[9]) {
+static size_t chunk_parts(size_t n, size_t cap, size_t (&b)[10]) {
     const size_t ntiles = (n + kCkTile - 1) / kCkTile;
     b[0] = cap * sizeof(uint64_t);                    // ka (32-bit head keys; 64-bit for big groups)
     b[1] = cap * sizeof(uint64_t);                    // kb (also the group lists)
@@ -1367,26 +1367,28 @@ static size_t chunk_parts(size_t n, size_t cap, size_t (&b)[9]) {
     b[6] = radix_tmp_bytes(cap);
     b[7] = (ntiles + 1) * sizeof(unsigned long long); // tile counts / offsets
     b[8] = (size_t(kBuckets) + 8) * sizeof(unsigned long long);
+    b[9] = n;                                         // BWT symbols of the refined rows
     size_t t = 0;
     for (size_t x : b) t += al(x);
     return t + 1024;
 }
 
 size_t suffix_sort_chunked_tmp_bytes(size_t n, size_t cap) {
-    size_t b[9];
+    size_t b[10];
     return chunk_parts(n, cap, b);
 }
 
 int suffix_sort_chunked(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa, size_t cap, void* tmp,
-                        size_t tmp_bytes, cudaStream_t st) {
+                        size_t tmp_bytes, cudaStream_t st, const uint8_t** bwt_out, uint64_t* pk_out) {
+    if (bwt_out) *bwt_out = nullptr;
     const size_t n = size_t(num_reads) * size_t(L);
     if (n == 0) return 0;
     if (cap < 2 || cap >= (size_t(1) << 31)) return int(cudaErrorInvalidValue);
-    size_t b[9];
+    size_t b[10];
     if (tmp_bytes < chunk_parts(n, cap, b)) return int(cudaErrorInvalidValue);
     char* q = static_cast<char*>(tmp);
-    char* part[9];
-    for (int i = 0; i < 9; ++i) {
+    char* part[10];
+    for (int i = 0; i < 10; ++i) {
         part[i] = q;
         q += al(b[i]);
     }
@@ -1394,8 +1396,10 @@ int suffix_sort_chunked(const uint8_t* reads, idx_t num_reads, int L, int dir, i
     uint64_t* kb0 = reinterpret_cast<uint64_t*>(part[1]);
     idx_t* va0 = reinterpret_cast<idx_t*>(part[2]);
     idx_t* vb0 = reinterpret_cast<idx_t*>(part[3]);
-    uint64_t* pk = reinterpret_cast<uint64_t*>(part[5]);
+    uint64_t* pk = pk_out ? pk_out : reinterpret_cast<uint64_t*>(part[5]);
     void* rtmp = part[6];
+    uint8_t* bwt = reinterpret_cast<uint8_t*>(part[9]);
+    cudaMemsetAsync(bwt, 0xff, n, st);
     unsigned long long* tcnt = reinterpret_cast<unsigned long long*>(part[7]);
     unsigned long long* hist = reinterpret_cast<unsigned long long*>(part[8]);
     unsigned long long* counters = hist + kBuckets;
@@ -1432,7 +1436,7 @@ int suffix_sort_chunked(const uint8_t* reads, idx_t num_reads, int L, int dir, i
                 uint64_t* cols = reinterpret_cast<uint64_t*>(vb);
                 const size_t cols_cap = (vb == vb0 ? al(b[3]) + b[4] : al(b[2])) / sizeof(uint64_t);
                 rc = refine_groups(ka, va, m, idx_t(L), pk, reinterpret_cast<uint64_t*>(kb), cols, cols_cap, counters,
-                                   rtmp, radix_tmp_bytes(m), st);
+                                   rtmp, radix_tmp_bytes(m), st, bwt + offset);
                 if (rc > 0) return rc;
                 if (rc < 0) return int(cudaErrorNotSupported);      // would need prefix doubling
             }
@@ -1441,6 +1445,7 @@ int suffix_sort_chunked(const uint8_t* reads, idx_t num_reads, int L, int dir, i
         offset += m;
         lo = hi;
     }
+    if (bwt_out) *bwt_out = bwt;
     return int(cudaGetLastError());
 }
 

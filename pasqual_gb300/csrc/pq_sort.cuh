@@ -21,10 +21,11 @@ int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa
 
 // The same order for inputs too large for one pass: suffixes bucketed by their first 6 bases,
 // consecutive buckets sorted in chunks of at most cap (< 2^31) suffixes.  Returns
-// cudaErrorNotSupported if one bucket exceeds cap.
+// cudaErrorNotSupported if one bucket exceeds cap.  bwt_out and pk_out as for suffix_sort.
 size_t suffix_sort_chunked_tmp_bytes(size_t n, size_t cap);
 int suffix_sort_chunked(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa, size_t cap, void* tmp,
-                        size_t tmp_bytes, cudaStream_t st);
+                        size_t tmp_bytes, cudaStream_t st, const uint8_t** bwt_out = nullptr,
+                        uint64_t* pk_out = nullptr);
 
 // Per-read seeds from a k-mer table (pq_index.cu).
 cudaError_t read_seeds(const uint8_t* reads, idx_t num_reads, int L, int dir, int k, const idx_t* kstart,
