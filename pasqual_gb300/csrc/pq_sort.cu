@@ -14,7 +14,7 @@
 // refinement little and halves the radix passes of a 29-base key.  Every radix pass is stable and
 // the input starts in text order, so equal suffixes stay in text order: the canonical tie-break.
 // Inputs the refinement cannot finish (groups larger than its scratch, reads longer than
-// 14 + 256 bases) are sorted by prefix doubling on 29-base 64-bit keys instead: ranks by
+// 268 bases) are sorted by prefix doubling on 29-base 64-bit keys instead: ranks by
 // (rank(p), rank(p+h) or "empty" past the read end) for h = 29, 58, 116, ...
 #include "pq_sort.cuh"
 
@@ -544,7 +544,7 @@ __global__ void k_copy_vals(const V* __restrict__ v, size_t n, idx_t* __restrict
 // groups packed per warp), up to 1024 by one CTA in shared memory, all with bitonic networks;
 // larger ones by a radix sort of their range on the next 29 bases.
 
-constexpr int kRefineMaxWords = 8;          // suffixes up to 14 + 256 bases
+constexpr int kRefineMaxWords = 8;          // suffixes up to 14 + 30 + 224 bases
 constexpr int kGroupWarp4 = 128;            // largest group sorted by one warp, 4 per lane
 constexpr int kGroupCta = 1024;             // largest group sorted in shared memory
 
@@ -749,23 +749,47 @@ __device__ __forceinline__ bool tuple_less(const uint64_t a[W], uint64_t alen, u
 // consecutive ones into its 32E slots (slot e * 32 + lane is register set e of that lane) while
 // they fit; one bitonic network over the 32E slots on (segment, bases from `from` on, length,
 // slot) then sorts every packed group in place (each segment keeps its slots, since segments are
-// numbered in slot order and empty slots sort last).  A group's members arrive in ascending
-// position (every radix pass is stable from text order), so the original slot breaks ties exactly
-// as the position does; the positions wait in shared memory and are gathered by slot at the end.
-// Distances below 32 exchange by shuffle, larger ones swap registers within a lane.
+// numbered in slot order and empty slots sort last).  The segment number (3 bits) rides in the top
+// of the first word, which holds the next 30 bases; the other words hold 32 each.  A group's
+// members arrive in ascending position (every radix pass is stable from text order), so the
+// original slot breaks ties exactly as the position does; the positions wait in shared memory
+// and are gathered by slot at the end.  Distances below 32 exchange by shuffle, larger ones swap
+// registers within a lane.
 template <int W>
 struct RefineItem {
-    uint64_t w[W];
+    uint64_t w[W];                              // w[0] = segment (3 bits) | 30 bases | 0
     uint32_t tail;                              // (length << 8) | original slot
-    uint32_t seg;
 };
 
-// a < b on (seg, w[0..W-1], tail) as one unsigned multi-word number: the borrow out of the
+// the words of RefineItem for the suffix at p (length m_len): bases from `off` on, zero past its end
+template <int W>
+__device__ __forceinline__ void refine_words(const uint64_t* __restrict__ pk, size_t p, int m_len, int off, uint32_t seg,
+                                             uint64_t w[W]) {
+    const int rem0 = m_len - off;
+    uint64_t x = 0;
+    if (rem0 > 0) {
+        x = window(pk, p + off) & (~uint64_t(0) << 4);            // 30 bases
+        if (rem0 < 30) x &= ~uint64_t(0) << (64 - 2 * rem0);
+    }
+    w[0] = (uint64_t(seg) << 61) | (x >> 3);
+    #pragma unroll
+    for (int j = 1; j < W; ++j) {
+        const int rem = rem0 - 30 - 32 * (j - 1);
+        uint64_t y = 0;
+        if (rem > 0) {
+            y = window(pk, p + off + 30 + 32 * size_t(j - 1));
+            if (rem < 32) y &= ~uint64_t(0) << (64 - 2 * rem);
+        }
+        w[j] = y;
+    }
+}
+
+// a < b on (w[0..W-1], tail) as one unsigned multi-word number: the borrow out of the
 // subtraction a - b, least significant word first, in one chain of subtract-with-borrow
 // instructions (no branches; the chain must sit in one asm statement to keep the carry flag).
 #define PQ_SUBC(x, y) "subc.cc.u64 t, %" #x ", %" #y ";\n\t"
 #define PQ_LT_HEAD "{\n\t.reg .u64 t;\n\t.reg .u32 s, z;\n\tmov.u32 z, 0;\n\tsub.cc.u32 s, %1, %2;\n\t"
-#define PQ_LT_TAIL(x, y) "subc.cc.u32 s, %" #x ", %" #y ";\n\tsubc.u32 %0, z, z;\n\t}"
+#define PQ_LT_TAIL "subc.u32 %0, z, z;\n\t}"
 #define PQ_WORD(j) "l"(a.w[j]), "l"(b.w[j])
 
 template <int W>
@@ -774,72 +798,72 @@ __device__ __forceinline__ bool item_less(const RefineItem<W>& a, const RefineIt
 template <>
 __device__ __forceinline__ bool item_less<1>(const RefineItem<1>& a, const RefineItem<1>& b) {
     unsigned r;
-    asm(PQ_LT_HEAD PQ_SUBC(3, 4) PQ_LT_TAIL(5, 6)
+    asm(PQ_LT_HEAD PQ_SUBC(3, 4) PQ_LT_TAIL
         : "=r"(r)
-        : "r"(a.tail), "r"(b.tail), PQ_WORD(0), "r"(a.seg), "r"(b.seg));
+        : "r"(a.tail), "r"(b.tail), PQ_WORD(0));
     return r != 0;
 }
 
 template <>
 __device__ __forceinline__ bool item_less<2>(const RefineItem<2>& a, const RefineItem<2>& b) {
     unsigned r;
-    asm(PQ_LT_HEAD PQ_SUBC(3, 4) PQ_SUBC(5, 6) PQ_LT_TAIL(7, 8)
+    asm(PQ_LT_HEAD PQ_SUBC(3, 4) PQ_SUBC(5, 6) PQ_LT_TAIL
         : "=r"(r)
-        : "r"(a.tail), "r"(b.tail), PQ_WORD(1), PQ_WORD(0), "r"(a.seg), "r"(b.seg));
+        : "r"(a.tail), "r"(b.tail), PQ_WORD(1), PQ_WORD(0));
     return r != 0;
 }
 
 template <>
 __device__ __forceinline__ bool item_less<3>(const RefineItem<3>& a, const RefineItem<3>& b) {
     unsigned r;
-    asm(PQ_LT_HEAD PQ_SUBC(3, 4) PQ_SUBC(5, 6) PQ_SUBC(7, 8) PQ_LT_TAIL(9, 10)
+    asm(PQ_LT_HEAD PQ_SUBC(3, 4) PQ_SUBC(5, 6) PQ_SUBC(7, 8) PQ_LT_TAIL
         : "=r"(r)
-        : "r"(a.tail), "r"(b.tail), PQ_WORD(2), PQ_WORD(1), PQ_WORD(0), "r"(a.seg), "r"(b.seg));
+        : "r"(a.tail), "r"(b.tail), PQ_WORD(2), PQ_WORD(1), PQ_WORD(0));
     return r != 0;
 }
 
 template <>
 __device__ __forceinline__ bool item_less<4>(const RefineItem<4>& a, const RefineItem<4>& b) {
     unsigned r;
-    asm(PQ_LT_HEAD PQ_SUBC(3, 4) PQ_SUBC(5, 6) PQ_SUBC(7, 8) PQ_SUBC(9, 10) PQ_LT_TAIL(11, 12)
+    asm(PQ_LT_HEAD PQ_SUBC(3, 4) PQ_SUBC(5, 6) PQ_SUBC(7, 8) PQ_SUBC(9, 10) PQ_LT_TAIL
         : "=r"(r)
-        : "r"(a.tail), "r"(b.tail), PQ_WORD(3), PQ_WORD(2), PQ_WORD(1), PQ_WORD(0), "r"(a.seg), "r"(b.seg));
+        : "r"(a.tail), "r"(b.tail), PQ_WORD(3), PQ_WORD(2), PQ_WORD(1), PQ_WORD(0));
     return r != 0;
 }
 
 template <>
 __device__ __forceinline__ bool item_less<5>(const RefineItem<5>& a, const RefineItem<5>& b) {
     unsigned r;
-    asm(PQ_LT_HEAD PQ_SUBC(3, 4) PQ_SUBC(5, 6) PQ_SUBC(7, 8) PQ_SUBC(9, 10) PQ_SUBC(11, 12) PQ_LT_TAIL(13, 14)
+    asm(PQ_LT_HEAD PQ_SUBC(3, 4) PQ_SUBC(5, 6) PQ_SUBC(7, 8) PQ_SUBC(9, 10) PQ_SUBC(11, 12) PQ_LT_TAIL
         : "=r"(r)
-        : "r"(a.tail), "r"(b.tail), PQ_WORD(4), PQ_WORD(3), PQ_WORD(2), PQ_WORD(1), PQ_WORD(0), "r"(a.seg), "r"(b.seg));
+        : "r"(a.tail), "r"(b.tail), PQ_WORD(4), PQ_WORD(3), PQ_WORD(2), PQ_WORD(1), PQ_WORD(0));
     return r != 0;
 }
 
 template <>
 __device__ __forceinline__ bool item_less<6>(const RefineItem<6>& a, const RefineItem<6>& b) {
     unsigned r;
-    asm(PQ_LT_HEAD PQ_SUBC(3, 4) PQ_SUBC(5, 6) PQ_SUBC(7, 8) PQ_SUBC(9, 10) PQ_SUBC(11, 12) PQ_SUBC(13, 14) PQ_LT_TAIL(15, 16)
+    asm(PQ_LT_HEAD PQ_SUBC(3, 4) PQ_SUBC(5, 6) PQ_SUBC(7, 8) PQ_SUBC(9, 10) PQ_SUBC(11, 12) PQ_SUBC(13, 14) PQ_LT_TAIL
         : "=r"(r)
-        : "r"(a.tail), "r"(b.tail), PQ_WORD(5), PQ_WORD(4), PQ_WORD(3), PQ_WORD(2), PQ_WORD(1), PQ_WORD(0), "r"(a.seg), "r"(b.seg));
+        : "r"(a.tail), "r"(b.tail), PQ_WORD(5), PQ_WORD(4), PQ_WORD(3), PQ_WORD(2), PQ_WORD(1), PQ_WORD(0));
     return r != 0;
 }
 
 template <>
 __device__ __forceinline__ bool item_less<7>(const RefineItem<7>& a, const RefineItem<7>& b) {
     unsigned r;
-    asm(PQ_LT_HEAD PQ_SUBC(3, 4) PQ_SUBC(5, 6) PQ_SUBC(7, 8) PQ_SUBC(9, 10) PQ_SUBC(11, 12) PQ_SUBC(13, 14) PQ_SUBC(15, 16) PQ_LT_TAIL(17, 18)
+    asm(PQ_LT_HEAD PQ_SUBC(3, 4) PQ_SUBC(5, 6) PQ_SUBC(7, 8) PQ_SUBC(9, 10) PQ_SUBC(11, 12) PQ_SUBC(13, 14) PQ_SUBC(15, 16) PQ_LT_TAIL
         : "=r"(r)
-        : "r"(a.tail), "r"(b.tail), PQ_WORD(6), PQ_WORD(5), PQ_WORD(4), PQ_WORD(3), PQ_WORD(2), PQ_WORD(1), PQ_WORD(0), "r"(a.seg), "r"(b.seg));
+        : "r"(a.tail), "r"(b.tail), PQ_WORD(6), PQ_WORD(5), PQ_WORD(4), PQ_WORD(3), PQ_WORD(2), PQ_WORD(1), PQ_WORD(0));
     return r != 0;
 }
 
 template <>
 __device__ __forceinline__ bool item_less<8>(const RefineItem<8>& a, const RefineItem<8>& b) {
     unsigned r;
-    asm(PQ_LT_HEAD PQ_SUBC(3, 4) PQ_SUBC(5, 6) PQ_SUBC(7, 8) PQ_SUBC(9, 10) PQ_SUBC(11, 12) PQ_SUBC(13, 14) PQ_SUBC(15, 16) PQ_SUBC(17, 18) PQ_LT_TAIL(19, 20)
+    asm(PQ_LT_HEAD PQ_SUBC(3, 4) PQ_SUBC(5, 6) PQ_SUBC(7, 8) PQ_SUBC(9, 10) PQ_SUBC(11, 12) PQ_SUBC(13, 14) PQ_SUBC(15, 16) PQ_SUBC(17, 18) PQ_LT_TAIL
         : "=r"(r)
-        : "r"(a.tail), "r"(b.tail), PQ_WORD(7), PQ_WORD(6), PQ_WORD(5), PQ_WORD(4), PQ_WORD(3), PQ_WORD(2), PQ_WORD(1), PQ_WORD(0), "r"(a.seg), "r"(b.seg));
+        : "r"(a.tail), "r"(b.tail), PQ_WORD(7), PQ_WORD(6), PQ_WORD(5), PQ_WORD(4), PQ_WORD(3), PQ_WORD(2), PQ_WORD(1), PQ_WORD(0));
     return r != 0;
 }
 
@@ -898,11 +922,10 @@ __global__ void __launch_bounds__(kRefineThreads, E == 1 ? (W <= 3 ? 5 : 1) : (W
             RefineItem<W> it[E];
             #pragma unroll
             for (int e = 0; e < E; ++e) {
-                it[e].seg = seg[e];
                 if (seg[e] != 255) {
                     const idx_t pos = val[at[e]];
                     const uint32_t len = uint32_t(L - pos % L);
-                    suffix_words<W>(pk, size_t(pos), int(len), from, it[e].w);
+                    refine_words<W>(pk, size_t(pos), int(len), from, seg[e], it[e].w);
                     it[e].tail = (len << 8) | uint32_t(e * 32 + lane);
                     mypos[e * 32 + lane] = pos;
                     if (bwt) mysym[e * 32 + lane] = bwt_symbol(pk, size_t(pos), L);
@@ -936,7 +959,6 @@ __global__ void __launch_bounds__(kRefineThreads, E == 1 ? (W <= 3 ? 5 : 1) : (W
                             #pragma unroll
                             for (int q = 0; q < W; ++q) o.w[q] = __shfl_xor_sync(0xffffffffu, it[e].w[q], j);
                             o.tail = __shfl_xor_sync(0xffffffffu, it[e].tail, j);
-                            o.seg = __shfl_xor_sync(0xffffffffu, it[e].seg, j);
                             const bool keep_min = ((lane & j) == 0) == (((e * 32 + lane) & k) == 0);
                             if (keep_min == item_less<W>(o, it[e])) it[e] = o;
                         }
@@ -1132,7 +1154,8 @@ static int refine_groups_w(const GroupLists& G, const unsigned long long* c0,
 static int refine_groups(const uint32_t* key, idx_t* val, size_t n, idx_t L, const uint64_t* pk, uint64_t* lists_mem,
                          uint64_t* cols, size_t cols_cap, unsigned long long* counters, void* rtmp, size_t rtmp_bytes,
                          cudaStream_t st, uint8_t* bwt = nullptr) {
-    const int W = int((2 * (size_t(L) - kHead) + 63) / 64);
+    // words from base 14 on: 30 bases in the first (beside the segment number), 32 in each other
+    const int W = 1 + int((size_t(L) > size_t(kHead) + 30 ? size_t(L) - kHead - 30 + 31 : 0) / 32);
     if (W < 1 || W > kRefineMaxWords) return -1;
     GroupLists G;
     G.cap[0] = n / 2 + 1;
@@ -1237,7 +1260,7 @@ int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa
             if (bwt_out) *bwt_out = bwt;
             return finish(ha);
         }
-        // a group too large for the scratch (or reads longer than 270 bases): prefix doubling on
+        // a group too large for the scratch (or reads longer than 268 bases): prefix doubling on
         // 29-base keys
         ka = reinterpret_cast<uint64_t*>(ha);
         kb = reinterpret_cast<uint64_t*>(hb);
