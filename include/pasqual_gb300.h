@@ -68,7 +68,9 @@ PQ_API const char *pq_last_error (const pq_ctx * ctx);
 /* Reads after import and de-duplication: num_reads * read_len base codes 1..4 (A,C,G,T), the
  * layout of index_t.reads after import_singlereads (src/index.c:145-405).  min_overlap is the
  * -t of the CLI, with SEQ_DEPTH(9) < min_overlap < read_len (src/test.c:306-311).
- * from_device != 0: `reads` is a device pointer. */
+ * from_device != 0: `reads` is a device pointer.  PQ_ERR_ARG if any byte is not a base code
+ * (the reference's import drops reads with N and rejects other symbols, src/index.c:304-318);
+ * the context then holds no reads. */
 PQ_API int pq_set_reads (pq_ctx * ctx, const uint8_t * reads, pq_idx num_reads, int read_len,
                   int min_overlap, int from_device);
 
@@ -96,7 +98,9 @@ PQ_API int pq_get_sa (pq_ctx * ctx, int dir, pq_idx * sa_host);
  * k-mer seed table.  Replaces build_OCC + the occ prefix sum (src/index.c:26-142, 587-615). */
 PQ_API int pq_build_fm (pq_ctx * ctx, int dir);
 
-/* Both directions, sort + FM-index: the body of build_index (src/index.c:626-706). */
+/* Both directions, sort + FM-index: the body of build_index (src/index.c:626-706).  The sort's
+ * working memory (about 25 bytes per suffix) is kept for the next build of the same size unless
+ * less than a quarter of the device memory is free afterwards. */
 PQ_API int pq_build_index (pq_ctx * ctx);
 
 /* Reference-layout copies of an FM-index (index_t.OCC_bitmap[5] back to back, each
@@ -141,7 +145,9 @@ PQ_API int pq_get_graph_sizes (pq_ctx * ctx, uint64_t * num_edges, uint64_t * pr
 /* Copy the last pq_overlaps result to host arrays.  Per read: num_B, num_F (node_t.num_B/F),
  * olp_B, olp_F (overlaps_B/F of src/string_graph.c:807-808), edge_off[num_reads+1].  Per edge,
  * B edges then F edges of each read in the reference's DFS order: dest, overlap length, type
- * (BF=0 FB=1 FF=2 BB=3) and the path_t.trans value (src/string_graph.c:940, 970). */
+ * (BF=0 FB=1 FF=2 BB=3) and the path_t.trans value (src/string_graph.c:940, 970).  Any pointer
+ * may be NULL (that array is skipped).  Page-locked or already-touched host arrays copy at link
+ * speed; freshly allocated pageable ones pay their first-touch page faults inside this call. */
 PQ_API int pq_get_graph (pq_ctx * ctx, uint16_t * num_B, uint16_t * num_F, int32_t * olp_B,
                   int32_t * olp_F, uint64_t * edge_off, pq_idx * dest, uint16_t * len,
                   uint8_t * type, int32_t * trans);
