@@ -213,13 +213,16 @@ __global__ void k_reads_index(const idx_t* __restrict__ sa, const OccBlock* __re
 // and the number of bytes that are not base codes 1..4.  The base counts stream the read set
 // 16 bytes a thread at a time (coalesced); the first and last base of every read are a strided
 // pass over the reads.
-__device__ __forceinline__ void count_word(uint32_t w, unsigned long long (&loc)[5]) {
+__device__ __forceinline__ void count_word(uint32_t w, unsigned (&loc)[5]) {
+    // per code c: the bytes of w equal to c (per-byte compare masks, 8 bits a match)
+    unsigned hit = 0;
     #pragma unroll
-    for (int b = 0; b < 4; ++b) {
-        const uint32_t c = (w >> (8 * b)) & 0xffu;
-        if (c >= 1 && c <= 4) loc[c - 1]++;
-        else loc[4]++;
+    for (int c = 1; c <= 4; ++c) {
+        const unsigned h = uint32_t(__popc(__vcmpeq4(w, 0x01010101u * unsigned(c)))) >> 3;
+        loc[c - 1] += h;
+        hit += h;
     }
+    loc[4] += 4 - hit;
 }
 
 __global__ void k_read_counts(const uint8_t* __restrict__ reads, idx_t nr, idx_t L,
@@ -227,7 +230,8 @@ __global__ void k_read_counts(const uint8_t* __restrict__ reads, idx_t nr, idx_t
     __shared__ unsigned long long acc[13];
     if (threadIdx.x < 13) acc[threadIdx.x] = 0;
     __syncthreads();
-    unsigned long long loc[5] = {0, 0, 0, 0, 0}, ends[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    unsigned loc[5] = {0, 0, 0, 0, 0};                  // per thread: < 2^32 bytes each
+    unsigned long long ends[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     const size_t n = size_t(nr) * size_t(L);
     const size_t tid = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     const size_t stride = size_t(gridDim.x) * blockDim.x;
@@ -242,19 +246,23 @@ __global__ void k_read_counts(const uint8_t* __restrict__ reads, idx_t nr, idx_t
     }
     for (size_t i = n16 * 16 + tid; i < n; i += stride) {
         const uint32_t c = reads[i];
-        if (c >= 1 && c <= 4) loc[c - 1]++;
-        else loc[4]++;
+        #pragma unroll
+        for (int k = 1; k <= 4; ++k) loc[k - 1] += c == uint32_t(k);
+        loc[4] += c < 1u || c > 4u;
     }
     for (size_t r = tid; r < size_t(nr); r += stride) {
         const uint32_t last = reads[r * L + L - 1], first = reads[r * L];
-        if (last >= 1 && last <= 4) ends[last - 1]++;
-        if (first >= 1 && first <= 4) ends[4 + first - 1]++;
+        #pragma unroll
+        for (int c = 1; c <= 4; ++c) {
+            ends[c - 1] += last == uint32_t(c);
+            ends[4 + c - 1] += first == uint32_t(c);
+        }
     }
     #pragma unroll
-    for (int k = 0; k < 4; ++k) if (loc[k]) atomicAdd(&acc[k], loc[k]);
+    for (int k = 0; k < 4; ++k) if (loc[k]) atomicAdd(&acc[k], (unsigned long long)loc[k]);
     #pragma unroll
     for (int k = 0; k < 8; ++k) if (ends[k]) atomicAdd(&acc[4 + k], ends[k]);
-    if (loc[4]) atomicAdd(&acc[12], loc[4]);
+    if (loc[4]) atomicAdd(&acc[12], (unsigned long long)loc[4]);
     __syncthreads();
     if (threadIdx.x < 13 && acc[threadIdx.x]) atomicAdd(&out[threadIdx.x], acc[threadIdx.x]);
 }
