@@ -279,13 +279,19 @@ int pq_get_counts(pq_ctx* ctx, pq_idx C[6], pq_idx suffix_count[4], pq_idx prefi
     return PQ_OK;
 }
 
-int pq_sort(pq_ctx* ctx, int dir) {
+// side_outputs: also the BWT symbols and inverse-SA entries of the rows the group refinement
+// places (FM-index work done where the refinement leaves DRAM idle; pq_build_index asks for
+// them).  pq_sort itself computes the suffix array only.
+static int sort_dir(pq_ctx* ctx, int dir, bool side_outputs) {
     if (!ctx || (dir != 0 && dir != 1)) return PQ_ERR_ARG;
     if (!ctx->have_reads) return fail(ctx, PQ_ERR_STATE, "pq_set_reads first");
     cudaSetDevice(ctx->device);
     const size_t n = n_rows(ctx);
     CK(ctx->sa[dir].ensure(n * sizeof(idx_t) + 64));
     CK(ctx->pk[dir].ensure((n / 32 + 4) * sizeof(uint64_t)));
+    // the inverse SA (read offsets 1..L-t): the sort enters the rows its refinement places
+    const size_t isa_n = size_t(ctx->num_reads) * size_t(ctx->L - ctx->t);
+    CK(ctx->isa[dir].ensure(isa_n * sizeof(idx_t) + 64));
     // one pass below 2^31 suffixes (32-bit group ranks), else chunks of 6-base buckets
     const size_t one_pass_max = (size_t(1) << 31) - 1;
     const bool chunked = n > one_pass_max || (ctx->sort_chunk && n > ctx->sort_chunk);
@@ -295,12 +301,16 @@ int pq_sort(pq_ctx* ctx, int dir) {
     CK(cudaEventRecord(ctx->ev0, ctx->st));
     ctx->sorted_keys[0] = ctx->sorted_keys[1] = nullptr;     // the scratch is about to be reused
     ctx->bwt_hint[0] = ctx->bwt_hint[1] = nullptr;
+    const uint8_t** hint_out = side_outputs ? &ctx->bwt_hint[dir] : nullptr;
+    idx_t* isa_out = side_outputs ? ctx->isa[dir].as<idx_t>() : nullptr;
     int rc = chunked ? pq::suffix_sort_chunked(ctx->reads.as<uint8_t>(), ctx->num_reads, ctx->L, dir,
                                                ctx->sa[dir].as<idx_t>(), cap, ctx->sort_tmp.p, tmp_bytes, ctx->st,
-                                               &ctx->bwt_hint[dir], ctx->pk[dir].as<uint64_t>())
+                                               hint_out, ctx->pk[dir].as<uint64_t>(), isa_out,
+                                               idx_t(ctx->L - ctx->t))
                      : pq::suffix_sort(ctx->reads.as<uint8_t>(), ctx->num_reads, ctx->L, dir,
                                        ctx->sa[dir].as<idx_t>(), ctx->sort_tmp.p, tmp_bytes, ctx->st,
-                                       &ctx->sorted_keys[dir], &ctx->bwt_hint[dir], ctx->pk[dir].as<uint64_t>());
+                                       &ctx->sorted_keys[dir], hint_out, ctx->pk[dir].as<uint64_t>(), isa_out,
+                                       idx_t(ctx->L - ctx->t));
     ctx->pk_ok[dir] = rc == 0;
     if (rc == int(cudaErrorNotSupported))
         return fail(ctx, PQ_ERR_CAPACITY, "suffix sort: a 6-base bucket holds more suffixes than a sort chunk");
@@ -313,6 +323,8 @@ int pq_sort(pq_ctx* ctx, int dir) {
     ctx->graph_ok = false;
     return PQ_OK;
 }
+
+int pq_sort(pq_ctx* ctx, int dir) { return sort_dir(ctx, dir, false); }
 
 int pq_set_sa(pq_ctx* ctx, int dir, const pq_idx* sa, int from_device) {
     if (!ctx || (dir != 0 && dir != 1)) return PQ_ERR_ARG;
@@ -392,7 +404,7 @@ int pq_build_fm(pq_ctx* ctx, int dir) {
                             k, ctx->ktmp.as<uint32_t>(), ctx->kstart[dir].as<idx_t>(), ctx->kend[dir].as<idx_t>(),
                             ctx->st, ctx->sorted_keys[dir], ctx->pk[dir].as<uint64_t>()));
     CK(pq::build_isa(ctx->sa[dir].as<idx_t>(), n, idx_t(ctx->L), idx_t(ctx->L - ctx->t), ctx->isa[dir].as<idx_t>(),
-                     ctx->st));
+                     ctx->st, ctx->bwt_hint[dir]));
     CK(cudaEventRecord(ctx->ev1, ctx->st));
     CK(cudaEventSynchronize(ctx->ev1));
     cudaEventElapsedTime(&ctx->ms_fm, ctx->ev0, ctx->ev1);
@@ -407,7 +419,7 @@ int pq_build_index(pq_ctx* ctx) {
     if (!ctx) return PQ_ERR_ARG;
     float s = 0, f = 0;
     for (int d = 0; d < 2; ++d) {
-        int rc = pq_sort(ctx, d);
+        int rc = sort_dir(ctx, d, true);
         if (rc) return rc;
         s += ctx->ms_sort;
         rc = pq_build_fm(ctx, d);

@@ -348,9 +348,12 @@ __global__ void k_kmer_bounds(const uint32_t* __restrict__ code, idx_t n, idx_t*
 
 // inverse suffix array restricted to read offsets 1..M: isa[read * M + offset - 1] = row of the
 // suffix at that offset (the rows the interval scan looks up: suffixes of length L - M .. L - 1)
-__global__ void k_isa(const idx_t* __restrict__ sa, size_t n, idx_t L, idx_t M, idx_t* __restrict__ isa) {
+// hint (or null): the sort's BWT symbols; rows with one (!= 0xff) already have their entry
+__global__ void k_isa(const idx_t* __restrict__ sa, size_t n, idx_t L, idx_t M, idx_t* __restrict__ isa,
+                      const uint8_t* __restrict__ hint) {
     const size_t stride = size_t(gridDim.x) * blockDim.x;
     for (size_t r = size_t(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride) {
+        if (hint && hint[r] != 0xff) continue;
         const idx_t p = sa[r];
         const idx_t rd = p / L, off = p - rd * L;
         if (off >= 1 && off <= M) isa[size_t(rd) * M + (off - 1)] = idx_t(r);
@@ -463,8 +466,9 @@ cudaError_t read_seeds(const uint8_t* reads, idx_t num_reads, int L, int dir, in
     return cudaGetLastError();
 }
 
-cudaError_t build_isa(const idx_t* sa, size_t n, idx_t L, idx_t M, idx_t* isa, cudaStream_t st) {
-    if (n && M) { k_isa<<<grid_for(n, 256), 256, 0, st>>>(sa, n, L, M, isa); note_launch(); }
+cudaError_t build_isa(const idx_t* sa, size_t n, idx_t L, idx_t M, idx_t* isa, cudaStream_t st,
+                      const uint8_t* hint) {
+    if (n && M) { k_isa<<<grid_for(n, 256), 256, 0, st>>>(sa, n, L, M, isa, hint); note_launch(); }
     return cudaGetLastError();
 }
 

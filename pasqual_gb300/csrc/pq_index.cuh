@@ -19,8 +19,10 @@ cudaError_t read_counts(const uint8_t* reads, idx_t num_reads, idx_t L, unsigned
 cudaError_t build_kmer_table(const idx_t* sa, const uint8_t* reads, idx_t num_reads, idx_t L, int dir,
                              int k, uint32_t* code_tmp, idx_t* kstart, idx_t* kend, cudaStream_t st,
                              const uint32_t* sorted_keys = nullptr, const uint64_t* pk = nullptr);
-// rows of the suffixes at read offsets 1..M (isa[read * M + offset - 1]); M = L - t
-cudaError_t build_isa(const idx_t* sa, size_t n, idx_t L, idx_t M, idx_t* isa, cudaStream_t st);
+// rows of the suffixes at read offsets 1..M (isa[read * M + offset - 1]); M = L - t.  hint: the
+// sort's BWT symbols, whose rows (symbol != 0xff) the sort has already entered, or null (all rows)
+cudaError_t build_isa(const idx_t* sa, size_t n, idx_t L, idx_t M, idx_t* isa, cudaStream_t st,
+                      const uint8_t* hint = nullptr);
 cudaError_t export_ref_layout(const OccBlock* blk, const idx_t* sb, idx_t num_reads, idx_t L,
                               const idx_t fix[4], uint64_t* bitmap, idx_t* sample, cudaStream_t st);
 

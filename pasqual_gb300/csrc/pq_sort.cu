@@ -555,7 +555,22 @@ struct GroupLists {
     unsigned long long* counts;             // [4]
     size_t cap[4];                          // entries (pairs for class 3)
     uint8_t* bwt;                           // BWT symbols of the rows the refinement places, or null
+    idx_t* isa;                             // their inverse-SA entries (offsets 1..M), or null
+    idx_t isa_m;                            // M
+    size_t row_base;                        // suffix-array row of val[0]
 };
+
+// side outputs of a row the refinement has placed: its BWT symbol and, for read offsets 1..M,
+// its inverse-SA entry isa[read * M + offset - 1] = row (written here, where the refinement's
+// ALU-bound networks leave DRAM idle, instead of by a separate scatter over every row)
+__device__ __forceinline__ void row_outputs(uint8_t* __restrict__ bwt, idx_t* __restrict__ isa, idx_t M,
+                                            size_t row, idx_t pos, idx_t L, uint8_t sym) {
+    if (bwt) bwt[row] = sym;
+    if (isa) {
+        const idx_t rd = pos / L, off = pos - rd * L;
+        if (off >= 1 && off <= M) isa[size_t(rd) * M + (off - 1)] = idx_t(row);
+    }
+}
 
 // BWT symbol of the suffix at p: 0 (`$`) at a read start, else the preceding base (1..4)
 __device__ __forceinline__ uint8_t bwt_symbol(const uint64_t* __restrict__ pk, size_t p, idx_t L) {
@@ -879,7 +894,8 @@ __global__ void __launch_bounds__(kRefineThreads, E == 1 ? (W <= 3 ? 5 : 1) : (W
                                                                 const unsigned long long* __restrict__ cnt,
                                                                 const uint64_t* __restrict__ pk, idx_t L,
                                                                 idx_t* __restrict__ val, int from,
-                                                                uint8_t* __restrict__ bwt) {
+                                                                uint8_t* __restrict__ bwt, idx_t* __restrict__ isa,
+                                                                idx_t isa_m, size_t row_base) {
     constexpr int kChunk = 8;
     constexpr int N = 32 * E;
     __shared__ idx_t spos[kRefineThreads / 32][N];
@@ -969,8 +985,9 @@ __global__ void __launch_bounds__(kRefineThreads, E == 1 ? (W <= 3 ? 5 : 1) : (W
             #pragma unroll
             for (int e = 0; e < E; ++e) {
                 if (seg[e] != 255) {
-                    val[at[e]] = mypos[it[e].tail & 255u];
-                    if (bwt) bwt[at[e]] = mysym[it[e].tail & 255u];
+                    const idx_t pos = mypos[it[e].tail & 255u];
+                    val[at[e]] = pos;
+                    row_outputs(bwt, isa, isa_m, row_base + at[e], pos, L, bwt ? mysym[it[e].tail & 255u] : 0);
                 }
             }
             __syncwarp();
@@ -1042,7 +1059,7 @@ __device__ void cta_load_group(uint64_t* cols, int P2, size_t start, int m, cons
 template <int W>
 __global__ void k_refine_cta(const unsigned long long* __restrict__ list, const unsigned long long* __restrict__ cnt,
                              const uint64_t* __restrict__ pk, idx_t L, idx_t* __restrict__ val, int off,
-                             uint8_t* __restrict__ bwt) {
+                             uint8_t* __restrict__ bwt, idx_t* __restrict__ isa, idx_t isa_m, size_t row_base) {
     extern __shared__ uint64_t s_cols[];
     const size_t groups = *cnt;
     for (size_t g = blockIdx.x; g < groups; g += gridDim.x) {
@@ -1055,8 +1072,9 @@ __global__ void k_refine_cta(const unsigned long long* __restrict__ list, const 
         cta_bitonic<W>(s_cols, P2);
         const uint64_t* posc = s_cols + size_t(W + 1) * P2;
         for (int i = threadIdx.x; i < m; i += blockDim.x) {
-            val[start + i] = idx_t(posc[i]);
-            if (bwt) bwt[start + i] = bwt_symbol(pk, size_t(posc[i]), L);
+            const idx_t pos = idx_t(posc[i]);
+            val[start + i] = pos;
+            row_outputs(bwt, isa, isa_m, row_base + start + i, pos, L, bwt ? bwt_symbol(pk, size_t(pos), L) : 0);
         }
         __syncthreads();
     }
@@ -1081,17 +1099,17 @@ static void refine_small_mid(const GroupLists& G, const unsigned long long* c, c
                              idx_t* val, int off, cudaStream_t st) {
     if (c[0]) {
         unsigned g = unsigned(std::min<unsigned long long>((c[0] + 63) / 64, 152ull * 64));
-        { k_refine_warp<W, 1><<<g, kRefineThreads, 0, st>>>(G.list[0], G.counts + 0, pk, L, val, off, G.bwt); note_launch(); }
+        { k_refine_warp<W, 1><<<g, kRefineThreads, 0, st>>>(G.list[0], G.counts + 0, pk, L, val, off, G.bwt, G.isa, G.isa_m, G.row_base); note_launch(); }
     }
     if (c[1]) {
         unsigned g = unsigned(std::min<unsigned long long>((c[1] + 15) / 16, 152ull * 64));
-        { k_refine_warp<W, 4><<<g, kRefineThreads, 0, st>>>(G.list[1], G.counts + 1, pk, L, val, off, G.bwt); note_launch(); }
+        { k_refine_warp<W, 4><<<g, kRefineThreads, 0, st>>>(G.list[1], G.counts + 1, pk, L, val, off, G.bwt, G.isa, G.isa_m, G.row_base); note_launch(); }
     }
     if (c[2]) {
         const size_t smem = size_t(W + 2) * kGroupCta * sizeof(uint64_t);
         cudaFuncSetAttribute(k_refine_cta<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
         unsigned g = unsigned(std::min<unsigned long long>(c[2], 152ull * 8));
-        { k_refine_cta<W><<<g, 512, smem, st>>>(G.list[2], G.counts + 2, pk, L, val, off, G.bwt); note_launch(); }
+        { k_refine_cta<W><<<g, 512, smem, st>>>(G.list[2], G.counts + 2, pk, L, val, off, G.bwt, G.isa, G.isa_m, G.row_base); note_launch(); }
     }
 }
 
@@ -1153,7 +1171,8 @@ static int refine_groups_w(const GroupLists& G, const unsigned long long* c0,
 // under 0.55 n
 static int refine_groups(const uint32_t* key, idx_t* val, size_t n, idx_t L, const uint64_t* pk, uint64_t* lists_mem,
                          uint64_t* cols, size_t cols_cap, unsigned long long* counters, void* rtmp, size_t rtmp_bytes,
-                         cudaStream_t st, uint8_t* bwt = nullptr) {
+                         cudaStream_t st, uint8_t* bwt = nullptr, idx_t* isa = nullptr, idx_t isa_m = 0,
+                         size_t row_base = 0) {
     // words from base 14 on: 30 bases in the first (beside the segment number), 32 in each other
     const int W = 1 + int((size_t(L) > size_t(kHead) + 30 ? size_t(L) - kHead - 30 + 31 : 0) / 32);
     if (W < 1 || W > kRefineMaxWords) return -1;
@@ -1168,6 +1187,9 @@ static int refine_groups(const uint32_t* key, idx_t* val, size_t n, idx_t L, con
     G.list[3] = G.list[2] + G.cap[2];
     G.counts = counters;
     G.bwt = bwt;
+    G.isa = isa;
+    G.isa_m = isa_m;
+    G.row_base = row_base;
     cudaMemsetAsync(counters, 0, 4 * sizeof(unsigned long long), st);
     { k_group_lists<uint32_t><<<unsigned(std::min<size_t>((n + kGlTile - 1) / kGlTile, size_t(152) * 64)), 256, 0, st>>>(
           key, n, G, 0); note_launch(); }
@@ -1205,7 +1227,8 @@ size_t suffix_sort_tmp_bytes(size_t n) {
 }
 
 int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa, void* tmp, size_t tmp_bytes,
-                cudaStream_t st, const uint32_t** keys_out, const uint8_t** bwt_out, uint64_t* pk_out) {
+                cudaStream_t st, const uint32_t** keys_out, const uint8_t** bwt_out, uint64_t* pk_out,
+                idx_t* isa_out, idx_t isa_m) {
     if (keys_out) *keys_out = nullptr;
     if (bwt_out) *bwt_out = nullptr;
     const size_t n = size_t(num_reads) * size_t(L);
@@ -1228,7 +1251,8 @@ int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa
     unsigned long long* tcnt = tmax + tiles + 1;
     unsigned long long* groups = tcnt + tiles + 1;
     p += al(3 * (tiles + 1) * sizeof(unsigned long long));
-    uint8_t* bwt = reinterpret_cast<uint8_t*>(p);    // BWT symbols of the refined rows, 0xff elsewhere
+    // BWT symbols of the refined rows (0xff elsewhere), kept only when asked for
+    uint8_t* bwt = bwt_out ? reinterpret_cast<uint8_t*>(p) : nullptr;
 
     idx_t* const vb0 = vb;                 // followed by rank in memory
     auto finish = [&](const uint32_t* keys) {
@@ -1252,9 +1276,9 @@ int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa
         uint64_t* cols = reinterpret_cast<uint64_t*>(vb);
         const size_t cols_cap = vb == vb0 ? (al(n * sizeof(idx_t)) + al(n * sizeof(uint32_t))) / sizeof(uint64_t)
                                           : n * sizeof(idx_t) / sizeof(uint64_t);
-        cudaMemsetAsync(bwt, 0xff, n, st);
+        if (bwt) cudaMemsetAsync(bwt, 0xff, n, st);
         rc = refine_groups(ha, va, n, idx_t(L), pk, reinterpret_cast<uint64_t*>(hb), cols, cols_cap, tcnt, rtmp,
-                           radix_tmp_bytes(n), st, bwt);
+                           radix_tmp_bytes(n), st, bwt, isa_out, isa_m);
         if (rc > 0) return rc;
         if (rc == 0) {   // the refinement permutes suffixes within groups of equal keys only
             if (bwt_out) *bwt_out = bwt;
@@ -1402,7 +1426,8 @@ size_t suffix_sort_chunked_tmp_bytes(size_t n, size_t cap) {
 }
 
 int suffix_sort_chunked(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa, size_t cap, void* tmp,
-                        size_t tmp_bytes, cudaStream_t st, const uint8_t** bwt_out, uint64_t* pk_out) {
+                        size_t tmp_bytes, cudaStream_t st, const uint8_t** bwt_out, uint64_t* pk_out,
+                        idx_t* isa_out, idx_t isa_m) {
     if (bwt_out) *bwt_out = nullptr;
     const size_t n = size_t(num_reads) * size_t(L);
     if (n == 0) return 0;
@@ -1421,8 +1446,8 @@ int suffix_sort_chunked(const uint8_t* reads, idx_t num_reads, int L, int dir, i
     idx_t* vb0 = reinterpret_cast<idx_t*>(part[3]);
     uint64_t* pk = pk_out ? pk_out : reinterpret_cast<uint64_t*>(part[5]);
     void* rtmp = part[6];
-    uint8_t* bwt = reinterpret_cast<uint8_t*>(part[9]);
-    cudaMemsetAsync(bwt, 0xff, n, st);
+    uint8_t* bwt = bwt_out ? reinterpret_cast<uint8_t*>(part[9]) : nullptr;
+    if (bwt) cudaMemsetAsync(bwt, 0xff, n, st);
     unsigned long long* tcnt = reinterpret_cast<unsigned long long*>(part[7]);
     unsigned long long* hist = reinterpret_cast<unsigned long long*>(part[8]);
     unsigned long long* counters = hist + kBuckets;
@@ -1459,7 +1484,7 @@ int suffix_sort_chunked(const uint8_t* reads, idx_t num_reads, int L, int dir, i
                 uint64_t* cols = reinterpret_cast<uint64_t*>(vb);
                 const size_t cols_cap = (vb == vb0 ? al(b[3]) + b[4] : al(b[2])) / sizeof(uint64_t);
                 rc = refine_groups(ka, va, m, idx_t(L), pk, reinterpret_cast<uint64_t*>(kb), cols, cols_cap, counters,
-                                   rtmp, radix_tmp_bytes(m), st, bwt + offset);
+                                   rtmp, radix_tmp_bytes(m), st, bwt, isa_out, isa_m, offset);
                 if (rc > 0) return rc;
                 if (rc < 0) return int(cudaErrorNotSupported);      // would need prefix doubling
             }

@@ -13,11 +13,15 @@ size_t suffix_sort_tmp_bytes(size_t n);
 // ended by prefix doubling (the key array then holds ranks).  When bwt_out is given it receives
 // the BWT symbols (0 = `$`, 1..4) of the rows the group refinement placed, 0xff for the others,
 // inside tmp, or nullptr.  pk_out (n/32 + 4 words), when given, receives the packed text of the
-// direction (see pack_text) instead of tmp.
+// direction (see pack_text) instead of tmp.  isa_out (num_reads * isa_m entries), when given
+// together with bwt_out, receives the inverse-SA entries isa[read * isa_m + offset - 1] of the
+// rows the refinement placed (those with a BWT symbol); the other rows' entries are left for the
+// caller.  Without bwt_out the sort computes neither (suffix array only).
 constexpr int kSortKeyBases = 14;
 int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa, void* tmp,
                 size_t tmp_bytes, cudaStream_t st, const uint32_t** keys_out = nullptr,
-                const uint8_t** bwt_out = nullptr, uint64_t* pk_out = nullptr);
+                const uint8_t** bwt_out = nullptr, uint64_t* pk_out = nullptr, idx_t* isa_out = nullptr,
+                idx_t isa_m = 0);
 
 // The same order for inputs too large for one pass: suffixes bucketed by their first 6 bases,
 // consecutive buckets sorted in chunks of at most cap (< 2^31) suffixes.  Returns
@@ -25,7 +29,7 @@ int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa
 size_t suffix_sort_chunked_tmp_bytes(size_t n, size_t cap);
 int suffix_sort_chunked(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa, size_t cap, void* tmp,
                         size_t tmp_bytes, cudaStream_t st, const uint8_t** bwt_out = nullptr,
-                        uint64_t* pk_out = nullptr);
+                        uint64_t* pk_out = nullptr, idx_t* isa_out = nullptr, idx_t isa_m = 0);
 
 // Per-read seeds from a k-mer table (pq_index.cu).
 cudaError_t read_seeds(const uint8_t* reads, idx_t num_reads, int L, int dir, int k, const idx_t* kstart,

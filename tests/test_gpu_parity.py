@@ -75,6 +75,24 @@ def test_chunked_sort_matches_reference(name):
         P.build_fm(1)
         out = P.construct_string_graph()
     assert sha(out.dest.astype(idx_dtype(g["width"]))) == str(g["sha_dest"])
+    # the same through pq_build_index, whose chunked sorts also leave BWT symbols and inverse-SA
+    # entries for the FM build
+    with gpu_ctx(int(g["width"])) as P:
+        P.set_reads(g["reads"], int(g["t"]))
+        for chunk in (max(n // 6, 2), n // 2 + 1):
+            P.set_sort_chunk(chunk)
+            try:
+                P.build_index()
+                break
+            except pq.PQError as e:
+                assert e.code == 6
+        for d in (0, 1):
+            bm, smp, ri = P.index_ref(d)
+            assert sha(bm) == str(g["sha_bitmap%d" % d]) and sha(smp) == str(g["sha_sample%d" % d])
+            assert sha(ri) == str(g["sha_reads_index%d" % d])
+        out = P.construct_string_graph()
+    assert sha(out.dest.astype(idx_dtype(g["width"]))) == str(g["sha_dest"])
+    assert sha(out.length) == str(g["sha_length"])
 
 
 @pytest.mark.parametrize("k", [1, 5, 10])
