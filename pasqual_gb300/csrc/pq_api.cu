@@ -326,6 +326,10 @@ static int sort_dir(pq_ctx* ctx, int dir, bool side_outputs) {
 
 int pq_sort(pq_ctx* ctx, int dir) { return sort_dir(ctx, dir, false); }
 
+// The sort of an index build (with the FM side outputs), for the reference's own entry points
+// (pq_dropin.cu), which build one direction at a time; not part of the C ABI.
+int pq_sort_for_index(pq_ctx* ctx, int dir) { return sort_dir(ctx, dir, true); }
+
 int pq_set_sa(pq_ctx* ctx, int dir, const pq_idx* sa, int from_device) {
     if (!ctx || (dir != 0 && dir != 1)) return PQ_ERR_ARG;
     if (!ctx->have_reads) return fail(ctx, PQ_ERR_STATE, "pq_set_reads first");

@@ -22,6 +22,9 @@
 
 static_assert(sizeof(pq_index_type) == sizeof(idx_t), "index widths must agree");
 
+// pq_api.cu: the sort of an index build, which also leaves the FM side outputs
+extern "C" int pq_sort_for_index(pq_ctx* ctx, int dir);
+
 // The reference's main() prints total time minus this (src/test.c:417-419).
 extern "C" __attribute__((visibility("default"))) double time_importreads = 0.0;
 
@@ -235,7 +238,7 @@ pq_index_t* construct_index(char* single_file, char* pair_file1, char* pair_file
         double t0 = now_ms();
         printf(dir ? "Sorting backward suffixes ... " : "Sorting forward suffixes ... ");
         fflush(stdout);
-        ck(pq_sort(ctx, dir));
+        ck(pq_sort_for_index(ctx, dir));
         ck(pq_build_fm(ctx, dir));
         std::vector<uint64_t> bm(rowlen * 5);
         pq_index_type* sample = (pq_index_type*)malloc(rowlen * 5 * sizeof(pq_index_type));
