@@ -78,7 +78,7 @@ struct pq_ctx {
     DevBuf sa[2], blk[2], sb[2], ri[2], kstart[2], kend[2], pk[2], isa[2];
     bool sa_ok[2] = {false, false}, fm_ok[2] = {false, false};
     int fm_k[2] = {0, 0};
-    DevBuf ktmp, sort_tmp, counts;
+    DevBuf sort_tmp, counts;
     const uint32_t* sorted_keys[2] = {nullptr, nullptr};   // the last sort's keys, inside sort_tmp
     const uint8_t* bwt_hint[2] = {nullptr, nullptr};       // the last sort's BWT symbols, inside sort_tmp
     bool pk_ok[2] = {false, false};                        // pk[dir] holds this read set's packed text
@@ -178,7 +178,7 @@ void pq_destroy(pq_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->st);
-    DevBuf* bufs[] = {&ctx->reads, &ctx->ktmp, &ctx->sort_tmp, &ctx->counts, &ctx->nB, &ctx->nF, &ctx->oB,
+    DevBuf* bufs[] = {&ctx->reads, &ctx->sort_tmp, &ctx->counts, &ctx->nB, &ctx->nF, &ctx->oB,
                       &ctx->oF, &ctx->status, &ctx->esrc, &ctx->e_dest, &ctx->e_trans, &ctx->e_len,
                       &ctx->e_type, &ctx->ctrs, &ctx->ovf_list, &ctx->off, &ctx->g_dest, &ctx->g_len,
                       &ctx->g_type, &ctx->g_trans, &ctx->asm_tmp, &ctx->wide, &ctx->warp_scratch, &ctx->defer,
@@ -404,9 +404,8 @@ int pq_build_fm(pq_ctx* ctx, int dir) {
     CK(pq::build_occ(ctx->sa[dir].as<idx_t>(), ctx->reads.as<uint8_t>(), ctx->num_reads, idx_t(ctx->L), dir,
                      ctx->blk[dir].as<OccBlock>(), ctx->sb[dir].as<idx_t>(), ctx->ri[dir].as<idx_t>(), ctx->st,
                      ctx->pk[dir].as<uint64_t>(), ctx->bwt_hint[dir]));
-    CK(pq::build_kmer_table(ctx->sa[dir].as<idx_t>(), ctx->reads.as<uint8_t>(), ctx->num_reads, idx_t(ctx->L), dir,
-                            k, ctx->ktmp.as<uint32_t>(), ctx->kstart[dir].as<idx_t>(), ctx->kend[dir].as<idx_t>(),
-                            ctx->st, ctx->sorted_keys[dir], ctx->pk[dir].as<uint64_t>()));
+    CK(pq::build_kmer_table(ctx->sa[dir].as<idx_t>(), ctx->num_reads, idx_t(ctx->L), k, ctx->kstart[dir].as<idx_t>(),
+                            ctx->kend[dir].as<idx_t>(), ctx->st, ctx->sorted_keys[dir], ctx->pk[dir].as<uint64_t>()));
     CK(pq::build_isa(ctx->sa[dir].as<idx_t>(), n, idx_t(ctx->L), idx_t(ctx->L - ctx->t), ctx->isa[dir].as<idx_t>(),
                      ctx->st, ctx->bwt_hint[dir]));
     CK(cudaEventRecord(ctx->ev1, ctx->st));
@@ -432,7 +431,7 @@ int pq_build_index(pq_ctx* ctx) {
     }
     ctx->ms_sort = s;
     ctx->ms_fm = f;
-    // the sort and k-mer working memory is not needed by the search: give it back when device
+    // the sort's working memory is not needed by the search: give it back when device
     // memory is short (under a quarter free), else keep it for the next build of the same size
     // (a cudaMalloc and cudaFree of tens of GB per build)
     ctx->sorted_keys[0] = ctx->sorted_keys[1] = nullptr;
@@ -440,7 +439,6 @@ int pq_build_index(pq_ctx* ctx) {
     size_t free_b = 0, total_b = 0;
     if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess || free_b < total_b / 4) {
         ctx->sort_tmp.release();
-        ctx->ktmp.release();
     }
     return PQ_OK;
 }

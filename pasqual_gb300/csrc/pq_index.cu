@@ -267,24 +267,6 @@ __global__ void k_read_counts(const uint8_t* __restrict__ reads, idx_t nr, idx_t
     if (threadIdx.x < 13 && acc[threadIdx.x]) atomicAdd(&out[threadIdx.x], acc[threadIdx.x]);
 }
 
-// k-mer seed table: rows whose suffix starts with a given k-mer are contiguous in a sorted SA;
-// record the first and last row of each.  code[r] = k-mer of row r or all-ones if the suffix is
-// shorter than k.
-__global__ void k_kmer_codes(const idx_t* __restrict__ sa, const uint8_t* __restrict__ reads,
-                             idx_t n, idx_t L, int dir, int k, uint32_t* __restrict__ code) {
-    const size_t stride = size_t(gridDim.x) * blockDim.x;
-    for (size_t r = size_t(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride) {
-        idx_t p = sa[r];
-        idx_t off = p % L;
-        uint32_t c = 0xffffffffu;
-        if (L - off >= idx_t(k)) {
-            c = 0;
-            for (int j = 0; j < k; ++j) c = (c << 2) | uint32_t(text_at(reads, L, dir, p + j) - 1);
-        }
-        code[r] = c;
-    }
-}
-
 // k-mer table from the packed text, one pass: a warp takes 32 consecutive rows, each lane the
 // k-mer of its row's suffix (all-ones when shorter than k) from one 64-bit window of the packed
 // text; neighbours' k-mers come by shuffle (the warp's edge lanes fetch theirs).
@@ -335,16 +317,6 @@ __global__ void k_kmer_bounds_keys(const uint32_t* __restrict__ key, idx_t n, in
     }
 }
 
-__global__ void k_kmer_bounds(const uint32_t* __restrict__ code, idx_t n, idx_t* __restrict__ kstart,
-                              idx_t* __restrict__ kend) {
-    const size_t stride = size_t(gridDim.x) * blockDim.x;
-    for (size_t r = size_t(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride) {
-        uint32_t c = code[r];
-        if (c == 0xffffffffu) continue;
-        if (r == 0 || code[r - 1] != c) kstart[c] = idx_t(r);
-        if (r + 1 == n || code[r + 1] != c) kend[c] = idx_t(r);
-    }
-}
 
 // inverse suffix array restricted to read offsets 1..M: isa[read * M + offset - 1] = row of the
 // suffix at that offset (the rows the interval scan looks up: suffixes of length L - M .. L - 1)
@@ -441,20 +413,16 @@ cudaError_t read_counts(const uint8_t* reads, idx_t num_reads, idx_t L, unsigned
     return cudaGetLastError();
 }
 
-cudaError_t build_kmer_table(const idx_t* sa, const uint8_t* reads, idx_t num_reads, idx_t L, int dir,
-                             int k, uint32_t* code_tmp, idx_t* kstart, idx_t* kend, cudaStream_t st,
-                             const uint32_t* sorted_keys, const uint64_t* pk) {
+cudaError_t build_kmer_table(const idx_t* sa, idx_t num_reads, idx_t L, int k, idx_t* kstart, idx_t* kend,
+                             cudaStream_t st, const uint32_t* sorted_keys, const uint64_t* pk) {
     const size_t n = size_t(num_reads) * L;
     const size_t nk = size_t(1) << (2 * k);
     { k_fill_idx<<<grid_for(nk, 256), 256, 0, st>>>(kstart, nk, idx_t(1)); note_launch(); }
     { k_fill_idx<<<grid_for(nk, 256), 256, 0, st>>>(kend, nk, idx_t(0)); note_launch(); }
     if (n && sorted_keys && k <= kSortKeyBases) {
         { k_kmer_bounds_keys<<<grid_for(n, 256), 256, 0, st>>>(sorted_keys, idx_t(n), k, kstart, kend); note_launch(); }
-    } else if (n && pk) {
-        { k_kmer_bounds_pk<<<grid_for(n, 256), 256, 0, st>>>(sa, pk, n, L, k, kstart, kend); note_launch(); }
     } else if (n) {
-        { k_kmer_codes<<<grid_for(n, 256), 256, 0, st>>>(sa, reads, idx_t(n), L, dir, k, code_tmp); note_launch(); }
-        { k_kmer_bounds<<<grid_for(n, 256), 256, 0, st>>>(code_tmp, idx_t(n), kstart, kend); note_launch(); }
+        { k_kmer_bounds_pk<<<grid_for(n, 256), 256, 0, st>>>(sa, pk, n, L, k, kstart, kend); note_launch(); }
     }
     return cudaGetLastError();
 }

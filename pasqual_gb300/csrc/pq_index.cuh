@@ -13,12 +13,10 @@ cudaError_t build_occ(const idx_t* sa, const uint8_t* reads, idx_t num_reads, id
 // out13: base counts [4], last-base counts [4], first-base counts [4], bytes outside 1..4
 cudaError_t read_counts(const uint8_t* reads, idx_t num_reads, idx_t L, unsigned long long* out13,
                         cudaStream_t st);
-// k-mer table of direction dir; from the sort's keys when sorted_keys is given (one streaming
-// pass), else from the suffix array and the packed text pk when given (one pass), else from the
-// suffix array and the text (code_tmp: n 32-bit words)
-cudaError_t build_kmer_table(const idx_t* sa, const uint8_t* reads, idx_t num_reads, idx_t L, int dir,
-                             int k, uint32_t* code_tmp, idx_t* kstart, idx_t* kend, cudaStream_t st,
-                             const uint32_t* sorted_keys = nullptr, const uint64_t* pk = nullptr);
+// k-mer table of direction dir: from the sort's keys when sorted_keys is given, else from the
+// suffix array and the packed text pk (each one streaming pass)
+cudaError_t build_kmer_table(const idx_t* sa, idx_t num_reads, idx_t L, int k, idx_t* kstart, idx_t* kend,
+                             cudaStream_t st, const uint32_t* sorted_keys, const uint64_t* pk);
 // rows of the suffixes at read offsets 1..M (isa[read * M + offset - 1]); M = L - t.  hint: the
 // sort's BWT symbols, whose rows (symbol != 0xff) the sort has already entered, or null (all rows)
 cudaError_t build_isa(const idx_t* sa, size_t n, idx_t L, idx_t M, idx_t* isa, cudaStream_t st,
