@@ -102,6 +102,45 @@ __global__ void k_init_keys(const uint64_t* __restrict__ pk, size_t n, idx_t L, 
     }
 }
 
+// The 32-bit head keys four positions a thread: one division for the first position's read
+// offset, the windows of all four from the same two packed-text words, and 16-byte stores of the
+// keys (and of the values when they are 32-bit); the key and value arrays start 16-byte aligned.
+__global__ void k_init_keys4(const uint64_t* __restrict__ pk, size_t n, idx_t L, uint32_t* __restrict__ key,
+                             idx_t* __restrict__ val) {
+    const size_t stride = size_t(gridDim.x) * blockDim.x;
+    for (size_t q = size_t(blockIdx.x) * blockDim.x + threadIdx.x; 4 * q < n; q += stride) {
+        const size_t p0 = 4 * q;
+        int off = int(p0 % size_t(L));
+        const size_t w = p0 >> 5;
+        const uint64_t a = pk[w], b = pk[w + 1];
+        uint32_t kk[4];
+        idx_t vv[4];
+        #pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int s = int((p0 + u) & 31) * 2;
+            const uint64_t x = s ? ((a << s) | (b >> (64 - s))) : a;
+            kk[u] = make_key<uint32_t>(x, int(L) - off);
+            vv[u] = idx_t(p0 + u);
+            if (++off == int(L)) off = 0;
+        }
+        if (p0 + 4 <= n) {
+            *reinterpret_cast<uint4*>(key + p0) = make_uint4(kk[0], kk[1], kk[2], kk[3]);
+            if (sizeof(idx_t) == 4) {
+                *reinterpret_cast<uint4*>(val + p0) = make_uint4(uint32_t(vv[0]), uint32_t(vv[1]), uint32_t(vv[2]),
+                                                                 uint32_t(vv[3]));
+            } else {
+                #pragma unroll
+                for (int u = 0; u < 4; ++u) val[p0 + u] = vv[u];
+            }
+        } else {
+            for (int u = 0; p0 + u < n; ++u) {
+                key[p0 + u] = kk[u];
+                val[p0 + u] = vv[u];
+            }
+        }
+    }
+}
+
 // ------------------------------------------------------------------------------ radix sort
 
 // Digit histograms of all byte positions over the whole key array (order independent): a pass
@@ -1264,7 +1303,10 @@ int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa
     // 32-bit head keys in the two 64-bit key buffers
     uint32_t* ha = reinterpret_cast<uint32_t*>(ka);
     uint32_t* hb = reinterpret_cast<uint32_t*>(kb);
-    { k_init_keys<uint32_t><<<grid_for(n, 256), 256, 0, st>>>(pk, n, idx_t(L), ha, va); note_launch(); }
+    if (reinterpret_cast<uintptr_t>(va) % 16 == 0 && reinterpret_cast<uintptr_t>(ha) % 16 == 0)
+        { k_init_keys4<<<grid_for((n + 3) / 4, 256), 256, 0, st>>>(pk, n, idx_t(L), ha, va); note_launch(); }
+    else    // a caller's suffix array that is not 16-byte aligned
+        { k_init_keys<uint32_t><<<grid_for(n, 256), 256, 0, st>>>(pk, n, idx_t(L), ha, va); note_launch(); }
     // all four digits vary on any real read set: no histogram pass, no host round trip
     int rc = radix_sort_pairs<uint32_t, idx_t>(&ha, &va, &hb, &vb, n, 0, 32, rtmp, radix_tmp_bytes(n), st, false);
     if (rc) return rc;
