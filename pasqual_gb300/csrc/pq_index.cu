@@ -306,14 +306,34 @@ __device__ __forceinline__ uint32_t key_code(uint32_t key, int k) {
     return int(key & 15) >= k ? (key >> (32 - 2 * k)) : 0xffffffffu;
 }
 
+// four rows a thread from one 16-byte load (the key array starts 16-byte aligned), plus the
+// neighbours on either side
 __global__ void k_kmer_bounds_keys(const uint32_t* __restrict__ key, idx_t n, int k, idx_t* __restrict__ kstart,
                                    idx_t* __restrict__ kend) {
     const size_t stride = size_t(gridDim.x) * blockDim.x;
-    for (size_t r = size_t(blockIdx.x) * blockDim.x + threadIdx.x; r < n; r += stride) {
-        const uint32_t c = key_code(key[r], k);
-        if (c == 0xffffffffu) continue;
-        if (r == 0 || key_code(key[r - 1], k) != c) kstart[c] = idx_t(r);
-        if (r + 1 == n || key_code(key[r + 1], k) != c) kend[c] = idx_t(r);
+    const size_t nn = size_t(n);
+    for (size_t q = size_t(blockIdx.x) * blockDim.x + threadIdx.x; 4 * q < nn; q += stride) {
+        const size_t r0 = 4 * q;
+        uint32_t c[6];                               // rows r0 - 1 .. r0 + 4
+        if (r0 + 4 <= nn) {
+            const uint4 v = *reinterpret_cast<const uint4*>(key + r0);
+            c[1] = key_code(v.x, k);
+            c[2] = key_code(v.y, k);
+            c[3] = key_code(v.z, k);
+            c[4] = key_code(v.w, k);
+        } else {
+            #pragma unroll
+            for (int u = 0; u < 4; ++u) c[1 + u] = r0 + u < nn ? key_code(key[r0 + u], k) : 0xfffffffeu;
+        }
+        c[0] = r0 > 0 ? key_code(key[r0 - 1], k) : 0xfffffffeu;
+        c[5] = r0 + 4 < nn ? key_code(key[r0 + 4], k) : 0xfffffffeu;
+        #pragma unroll
+        for (int u = 1; u <= 4; ++u) {
+            const size_t r = r0 + u - 1;
+            if (r >= nn || c[u] == 0xffffffffu) continue;
+            if (c[u - 1] != c[u]) kstart[c[u]] = idx_t(r);
+            if (c[u + 1] != c[u]) kend[c[u]] = idx_t(r);
+        }
     }
 }
 
@@ -419,8 +439,8 @@ cudaError_t build_kmer_table(const idx_t* sa, idx_t num_reads, idx_t L, int k, i
     const size_t nk = size_t(1) << (2 * k);
     { k_fill_idx<<<grid_for(nk, 256), 256, 0, st>>>(kstart, nk, idx_t(1)); note_launch(); }
     { k_fill_idx<<<grid_for(nk, 256), 256, 0, st>>>(kend, nk, idx_t(0)); note_launch(); }
-    if (n && sorted_keys && k <= kSortKeyBases) {
-        { k_kmer_bounds_keys<<<grid_for(n, 256), 256, 0, st>>>(sorted_keys, idx_t(n), k, kstart, kend); note_launch(); }
+    if (n && sorted_keys && k <= kSortKeyBases && reinterpret_cast<uintptr_t>(sorted_keys) % 16 == 0) {
+        { k_kmer_bounds_keys<<<grid_for((n + 3) / 4, 256), 256, 0, st>>>(sorted_keys, idx_t(n), k, kstart, kend); note_launch(); }
     } else if (n) {
         { k_kmer_bounds_pk<<<grid_for(n, 256), 256, 0, st>>>(sa, pk, n, L, k, kstart, kend); note_launch(); }
     }
