@@ -686,7 +686,7 @@ __device__ size_t run_end(const K* __restrict__ key, size_t n, size_t e0, K k) {
 }
 
 template <class K>
-__global__ void __launch_bounds__(kGlThreads) k_group_lists(const K* __restrict__ key, size_t n, GroupLists G,
+__global__ void __launch_bounds__(kGlThreads, 5) k_group_lists(const K* __restrict__ key, size_t n, GroupLists G,
                                                            size_t base) {
     __shared__ uint32_t hm[kGlWords + 1];               // heads; sentinel word at the end
     __shared__ uint32_t lm[kGlWords];                   // long suffixes
