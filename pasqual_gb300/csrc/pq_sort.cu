@@ -53,22 +53,38 @@ static inline unsigned grid_for(size_t work, int threads, int per_sm = 8) {
 
 // ------------------------------------------------------------------------------ packed text
 
-__device__ __forceinline__ int text_code(const uint8_t* __restrict__ reads, idx_t L, int dir, size_t p) {
-    if (dir == 0) return reads[p];
-    size_t r = p / L, off = p - r * L;
-    return reads[r * L + (L - 1 - off)];
-}
-
-// 32 bases per word, first base in the top two bits (A=0 .. T=3)
+// 32 bases per word, first base in the top two bits (A=0 .. T=3).  The forward text of a whole
+// word comes in two 16-byte loads; the backward text walks the word's positions with one
+// division for the first (the read offset then steps and wraps).
 __global__ void k_pack_text(const uint8_t* __restrict__ reads, size_t n, idx_t L, int dir, size_t nwords,
                             uint64_t* __restrict__ pk) {
     const size_t stride = size_t(gridDim.x) * blockDim.x;
+    const bool vec = dir == 0 && reinterpret_cast<uintptr_t>(reads) % 16 == 0;
     for (size_t w = size_t(blockIdx.x) * blockDim.x + threadIdx.x; w < nwords; w += stride) {
+        const size_t p0 = w * 32;
         uint64_t v = 0;
-        for (int j = 0; j < 32; ++j) {
-            size_t p = w * 32 + j;
-            uint64_t c = p < n ? uint64_t(text_code(reads, L, dir, p) - 1) : 0;
-            v = (v << 2) | c;
+        if (vec && p0 + 32 <= n) {
+            const uint4 a = *reinterpret_cast<const uint4*>(reads + p0);
+            const uint4 b = *reinterpret_cast<const uint4*>(reads + p0 + 16);
+            const uint32_t q[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+            #pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                #pragma unroll
+                for (int by = 0; by < 4; ++by) v = (v << 2) | uint64_t(((q[i] >> (8 * by)) & 0xffu) - 1);
+            }
+        } else if (p0 < n) {
+            size_t r = p0 / size_t(L);
+            idx_t off = idx_t(p0 - r * size_t(L));
+            for (int j = 0; j < 32; ++j) {
+                const size_t p = p0 + size_t(j);
+                uint64_t c = 0;
+                if (p < n) c = uint64_t((dir == 0 ? reads[p] : reads[r * size_t(L) + size_t(L - 1 - off)]) - 1);
+                v = (v << 2) | c;
+                if (++off == L) {
+                    off = 0;
+                    ++r;
+                }
+            }
         }
         pk[w] = v;
     }
