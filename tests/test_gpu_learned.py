@@ -77,7 +77,7 @@ def test_every_key_inside_its_window(name):
 @pytest.mark.parametrize("name", ["iid8k_L50_t31_u32", "rep15k_L100_t63_u32", "lowc12k_L150_t63_u64",
                                   "iid5k_L60_t59_u32", "rep20k_L100_t63_u64"])
 def test_learned_search_matches_plain_and_reference(name):
-    """Plain backward search (mode 0) is the judge: the learned search's edges are identical, and
+    """Plain backward search (mode 0) is the yardstick: the learned search's edges are identical, and
     both are the reference's."""
     g = load_golden(name)
     dt = idx_dtype(g["width"])
