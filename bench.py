@@ -400,7 +400,7 @@ def run_ours(args):
         cb = cpu_baseline(args.workload, args.cpu_scale, args.cpu_seconds)
     # Algorithmic bytes: 32 B for every rank probe the reference's method takes on this workload
     # shape (counted by the C restatement on the CPU sample, or the figure recorded beside the ncu
-    # summary), whatever this build's own kernels skip.
+    # summary), whatever the GPU kernels skip.
     oracle_ppr = cb["probes_per_read"] if cb else profile_figure("oracle_probes_per_read")
     alg_bytes = 32.0 * oracle_ppr * nr if oracle_ppr else 32.0 * probes
     achieved = alg_bytes / (kms * 1e-3) / 1e9

@@ -1,5 +1,5 @@
-"""CPU oracle of the learned index (test infrastructure only: the tests import it as the checker,
-nothing in the product calls it).
+"""CPU oracle of the learned index (test infrastructure only: the tests compare the GPU kernels
+with it; nothing in the product calls it).
 
 The learned index has no counterpart in the reference; what is restated here is its
 mathematics, in float64, so that the GPU kernels can be checked against it:

@@ -1,8 +1,8 @@
 """ctypes wrapper of the C restatement (oracle/pq_oracle.c) and of the reference dump tool.
 
 TEST INFRASTRUCTURE: imported only by tests/, by ``__graft_entry__.smoke()`` and by the CPU
-baseline leg of ``bench.py``, always as the checker or the timed CPU baseline, never as the
-product path.
+baseline leg of ``bench.py``, always as the oracle the GPU results are compared with or as the
+timed CPU baseline, never as the product path.
 """
 from __future__ import annotations
 
