@@ -39,6 +39,8 @@ CASES = {
     "iid5k_L60_t59_u32": (5000, 0.50, 0.00, (0.0, 0.0), 0.00, 60, 50, 0.0, 59, 32, False),
     "dinuc6k_L60_t20_u32": (6000, 0.45, 0.00, (0.0, 0.0), 0.50, 60, 30, 0.002, 20, 32, False),
     "rep20k_L100_t63_u64": (20000, 0.41, 0.10, (0.01, 0.01), 0.00, 100, 20, 0.005, 63, 64, False),
+    # long reads: the sort's widest refinement words and the search's 8-word continuations
+    "rep12k_L250_t95_u32": (12000, 0.45, 0.08, (0.01, 0.01), 0.00, 250, 25, 0.005, 95, 32, False),
 }
 
 DIGEST_KEYS = ["sa0", "sa1", "bitmap0", "bitmap1", "sample0", "sample1", "reads_index0",
