@@ -26,7 +26,9 @@ static_assert(sizeof(pq_index_type) == sizeof(idx_t), "index widths must agree")
 extern "C" int pq_sort_for_index(pq_ctx* ctx, int dir);
 
 // The reference's main() prints total time minus this (src/test.c:417-419).
-extern "C" __attribute__((visibility("default"))) double time_importreads = 0.0;
+extern "C" {
+__attribute__((visibility("default"))) double time_importreads = 0.0;
+}
 
 namespace {
 
