@@ -10,11 +10,17 @@
 #include <cstdlib>
 #include <cstring>
 #include <sys/time.h>
+#include <sys/stat.h>
+#include <sys/mman.h>
+#include <fcntl.h>
+#include <unistd.h>
 #include <unordered_map>
+#include <memory>
 #include <mutex>
 #include <vector>
 #include <string>
 #include <algorithm>
+#include <thread>
 
 #include "pq_common.cuh"
 #include "../../include/pasqual_gb300.h"
@@ -125,10 +131,13 @@ int prefix_rank(const int* s, int len) {
 
 }  // namespace
 
-extern "C" {
+namespace {
 
-int pq_import_fasta(const char* path, int read_len, int bloom_m, int n_hashfunc, uint8_t** reads_out,
-                    pq_index_type* num_reads_out, pq_index_type* removed_out, const char** err) {
+// The import one line at a time, exactly as the reference reads the file (fgets into 1000
+// bytes); import_fasta_parallel falls back to it for inputs where a whole-file parse could
+// differ from that (lines of 999 or more characters, NUL bytes).
+int import_fasta_serial(const char* path, int read_len, int bloom_m, int n_hashfunc, uint8_t** reads_out,
+                        pq_index_type* num_reads_out, pq_index_type* removed_out, const char** err) {
     char line[1000];
     char msg[512];
     auto bad = [&](pq_index_type kept) {
@@ -190,6 +199,283 @@ int pq_import_fasta(const char* path, int read_len, int bloom_m, int n_hashfunc,
     *num_reads_out = kept;
     if (removed_out) *removed_out = removed;
     return PQ_OK;
+}
+
+// The five hashes of src/bloom.c over a read's codes (len bytes, no terminator needed), in
+// index-width arithmetic, all in one pass (five independent chains); out[f] = hash f mod m.
+void hash_codes5(const char* k, int len, pq_index_type m, pq_index_type (&out)[5]) {
+    pq_index_type h0 = 0, h1 = 0, h2 = 0, h3 = 0, h4 = 0;
+    for (int i = 0; i < len; ++i) {
+        const pq_index_type c = (unsigned char)k[i];
+        h0 ^= (h0 << 5) + (h0 >> 2) + c;
+        h1 = c + (h1 << 6) + (h1 << 16) - h1;
+        h2 += c;
+        h3 ^= c;
+        h4 = 33 * h4 + c;
+    }
+    out[0] = h0 % m;
+    out[1] = h1 % m;
+    out[2] = h2 % m;
+    out[3] = h3 % m;
+    out[4] = h4 % m;
+}
+
+// Base symbol -> code (A=1 C=2 G=3 T=4, either case), the code of its complement, and a class:
+// 0 = base, 1 = N (either case), 2 = any other byte.  Tables make the decode branch-free.
+struct BaseTables {
+    uint8_t fw[256], rc[256], cls[256];
+    BaseTables() {
+        for (int i = 0; i < 256; ++i) { fw[i] = 0; rc[i] = 0; cls[i] = 2; }
+        const char* up = "ACGT";
+        const char* lo = "acgt";
+        for (int b = 0; b < 4; ++b) {
+            for (const char* s : {up, lo}) {
+                const unsigned char ch = (unsigned char)s[b];
+                fw[ch] = uint8_t(b + 1);
+                rc[ch] = uint8_t(4 - b);
+                cls[ch] = 0;
+            }
+        }
+        cls['N'] = cls['n'] = 1;
+        fw['N'] = fw['n'] = 'N';
+    }
+};
+const BaseTables kBases;
+
+// malloc-compatible (free()-able) memory in 2 MB-aligned whole huge pages where the kernel
+// grants them on request: random accesses then miss the TLB far less often
+void* alloc_huge(size_t bytes) {
+    constexpr size_t kHuge = size_t(2) << 20;
+    const size_t sz = (bytes + kHuge - 1) / kHuge * kHuge;
+    void* p = aligned_alloc(kHuge, sz ? sz : kHuge);
+    if (p && sz) madvise(p, sz, MADV_HUGEPAGE);        // advice only: ignored where unsupported
+    return p;
+}
+
+template <class F>
+void parallel_ranges(size_t n, int threads, F f) {
+    if (n == 0) return;
+    threads = std::max(1, std::min<int>(threads, int((n + 4095) / 4096)));
+    if (threads == 1) { f(size_t(0), n, 0); return; }
+    std::vector<std::thread> th;
+    const size_t chunk = (n + threads - 1) / threads;
+    for (int t = 0; t < threads; ++t) {
+        const size_t b = size_t(t) * chunk, e = std::min(n, b + chunk);
+        if (b >= e) break;
+        th.emplace_back([=, &f] { f(b, e, t); });
+    }
+    for (auto& x : th) x.join();
+}
+
+// Whole-file import with the reference's outcome: the file is read once; line boundaries,
+// record count, validation, base codes and the Bloom hashes of every record are computed in
+// parallel; only the Bloom filter pass runs in input order (it decides which of two duplicates
+// survives), touching a few bits per record with the bits of the next records prefetched.
+int import_fasta_parallel(const char* path, int read_len, int bloom_m, int n_hashfunc, uint8_t** reads_out,
+                          pq_index_type* num_reads_out, pq_index_type* removed_out, const char** err) {
+    char msg[512];
+    const int fd = open(path, O_RDONLY);
+    if (fd < 0) {
+        snprintf(msg, sizeof msg, "open reads file %s failed.\n", path);
+        g_import_err = msg;
+        if (err) *err = g_import_err.c_str();
+        return PQ_ERR_ARG;
+    }
+    struct stat stt;
+    if (fstat(fd, &stt) != 0 || !S_ISREG(stt.st_mode)) {   // not a regular file: read line by line
+        close(fd);
+        return -1;
+    }
+    const int threads = std::max(1, int(std::thread::hardware_concurrency()));
+    const size_t nbytes = size_t(stt.st_size);
+    std::unique_ptr<char, decltype(&free)> text((char*)malloc(nbytes ? nbytes : 1), &free);
+    if (!text) { close(fd); return -1; }
+    bool read_ok = true;
+    std::mutex read_mu;
+    parallel_ranges(nbytes, threads, [&](size_t b, size_t e, int) {
+        size_t at = b;
+        while (at < e) {
+            const ssize_t got = pread(fd, text.get() + at, e - at, off_t(at));
+            if (got <= 0) {
+                std::lock_guard<std::mutex> g(read_mu);
+                read_ok = false;
+                return;
+            }
+            at += size_t(got);
+        }
+    });
+    close(fd);
+    if (!read_ok) return -1;
+    const char* T = text.get();
+    // lines: per chunk count of newlines and NUL bytes, then the line starts
+    std::vector<size_t> nl_count(threads + 1, 0), nul_count(threads + 1, 0);
+    parallel_ranges(nbytes, threads, [&](size_t b, size_t e, int t) {
+        size_t c = 0;
+        for (const char* q = T + b; (q = (const char*)memchr(q, '\n', size_t(T + e - q))) != nullptr; ++q) ++c;
+        nl_count[t] = c;
+        nul_count[t] = memchr(T + b, 0, e - b) != nullptr;
+    });
+    size_t nuls = 0, nls = 0;
+    for (int t = 0; t <= threads; ++t) { nuls += nul_count[t]; nls += nl_count[t]; }
+    const bool last_open = nbytes && T[nbytes - 1] != '\n';
+    const size_t nlines = nls + (last_open ? 1 : 0);
+    if (nuls) return -1;
+    std::unique_ptr<size_t[]> start(new size_t[nlines + 1]);
+    {
+        std::vector<size_t> base(threads + 1, 0);
+        for (int t = 0; t < threads; ++t) base[t + 1] = base[t] + nl_count[t];
+        if (nlines) start[0] = 0;
+        parallel_ranges(nbytes, threads, [&](size_t b, size_t e, int t) {
+            size_t k = base[t];
+            for (const char* q = T + b; (q = (const char*)memchr(q, '\n', size_t(T + e - q))) != nullptr; ++q)
+                if (k + 1 <= nlines) start[++k] = size_t(q - T) + 1;
+        });
+        start[nlines] = nbytes + (last_open ? 1 : 0);   // one past the (virtual) newline
+    }
+    // line i: bytes [start[i], start[i+1] - 1) without its newline
+    auto line_len = [&](size_t i) { return start[i + 1] - 1 - start[i]; };
+    std::vector<size_t> hdr_count(threads + 1, 0), long_count(threads + 1, 0);
+    parallel_ranges(nlines, threads, [&](size_t b, size_t e, int t) {
+        size_t h = 0, lg = 0;
+        for (size_t i = b; i < e; ++i) {
+            h += line_len(i) > 0 && T[start[i]] == '>';
+            lg += line_len(i) >= 999;
+        }
+        hdr_count[t] = h;
+        long_count[t] = lg;
+    });
+    pq_index_type records = 0;
+    size_t longs = 0;
+    for (int t = 0; t <= threads; ++t) { records += pq_index_type(hdr_count[t]); longs += long_count[t]; }
+    if (longs) return -1;
+    // record i: header line 2i, sequence line 2i + 1; status 0 = ok, 1 = has N, 2 = error
+    const size_t pairs = (nlines + 1) / 2;
+    const pq_index_type m = records * (pq_index_type)bloom_m;
+    const int nf = std::max(0, std::min(n_hashfunc, 5));
+    // not zero-filled: each worker touches (and page-faults) only its own records
+    std::unique_ptr<uint8_t[]> status(new uint8_t[pairs ? pairs : 1]);
+    std::unique_ptr<pq_index_type[]> hfw(new pq_index_type[pairs * size_t(nf) + 1]);
+    std::unique_ptr<pq_index_type[]> hrc(new pq_index_type[pairs * size_t(nf) + 1]);
+    // the sequence line of record i (valid records only)
+    const size_t* __restrict__ const st = start.get();
+    auto seq_of = [st, T](size_t i) { return T + st[2 * i + 1]; };
+    parallel_ranges(pairs, threads, [&, st, T](size_t b, size_t e, int) {
+        // locals and restrict pointers: the character stores below may not alias anything else
+        const int RL = read_len, NF = nf;
+        const size_t NL = nlines;
+        const bool open_end = last_open;
+        const pq_index_type M = m;
+        uint8_t* __restrict__ const sta = status.get();
+        pq_index_type* __restrict__ const hf = hfw.get();
+        pq_index_type* __restrict__ const hr = hrc.get();
+        char fw[1000], rc[1000];                     // lines are shorter than 999 characters here
+        for (size_t i = b; i < e; ++i) {
+            const size_t h = 2 * i, q = h + 1;
+            const size_t hlen = st[h + 1] - 1 - st[h];
+            if (hlen == 0 || T[st[h]] != '>' || q >= NL) { sta[i] = 2; continue; }
+            // the reference drops the last character of the buffer: the newline, or the last
+            // base of a final line without one
+            const size_t slen = (st[q + 1] - 1 - st[q]) + (q + 1 == NL && open_end ? 0 : 1) - 1;
+            if (slen != size_t(RL)) { sta[i] = 2; continue; }
+            const unsigned char* sq = (const unsigned char*)(T + st[q]);
+            unsigned cls = 0;
+            for (int j = 0; j < RL; ++j) {
+                const unsigned char ch = sq[j];
+                fw[j] = char(kBases.fw[ch]);
+                rc[RL - 1 - j] = char(kBases.rc[ch]);
+                cls |= 1u << kBases.cls[ch];
+            }
+            if (cls & 4u) { sta[i] = 2; continue; }      // a byte that is no base and no N
+            sta[i] = (cls & 2u) ? 1 : 0;
+            if (cls & 2u) continue;
+            pq_index_type a5[5], r5[5];
+            hash_codes5(fw, RL, M, a5);
+            hash_codes5(rc, RL, M, r5);
+            for (int f = 0; f < NF; ++f) {
+                hf[i * NF + f] = a5[f];
+                hr[i * NF + f] = r5[f];
+            }
+        }
+    });
+    // the Bloom pass in input order (src/bloom.c:91-135), up to the first bad record
+    const size_t nbits_bytes = (size_t(m) + 7) / 8 + 1;
+    std::unique_ptr<unsigned char, decltype(&free)> bits_mem((unsigned char*)alloc_huge(nbits_bytes), &free);
+    if (!bits_mem) return PQ_ERR_NOMEM;
+    unsigned char* const bits = bits_mem.get();
+    memset(bits, 0, nbits_bytes);
+    std::vector<uint8_t> keep(pairs, 0);
+    pq_index_type kept = 0, removed = 0;
+    constexpr size_t kAhead = 16;
+    for (size_t i = 0; i < pairs; ++i) {
+        if (i + kAhead < pairs && status[i + kAhead] == 0) {
+            for (int f = 0; f < nf; ++f) {
+                __builtin_prefetch(&bits[hfw[(i + kAhead) * nf + f] / 8]);
+                __builtin_prefetch(&bits[hrc[(i + kAhead) * nf + f] / 8]);
+            }
+        }
+        if (status[i] == 2) {
+            snprintf(msg, sizeof msg, "incorrect reads file at line %llu.\n", (unsigned long long)(kept * 2 + 2));
+            g_import_err = msg;
+            if (err) *err = g_import_err.c_str();
+            return PQ_ERR_ARG;
+        }
+        if (status[i] == 1) { removed++; continue; }
+        const pq_index_type* hv = &hfw[i * nf];
+        bool all = true;
+        for (int f = 0; f < nf; ++f)
+            if (!bit_get(bits, hv[f])) all = false;
+        bool dup = true;
+        if (!all) {
+            for (int f = 0; f < nf; ++f) {
+                if (!bit_get(bits, hrc[i * nf + f])) {
+                    for (int j = 0; j < nf; ++j) bit_set(bits, hv[j]);
+                    dup = false;
+                    break;
+                }
+            }
+        }
+        if (dup) { removed++; continue; }
+        keep[i] = 1;
+        kept++;
+    }
+    // kept reads in input order
+    std::vector<size_t> kc(threads + 1, 0);
+    parallel_ranges(pairs, threads, [&](size_t b, size_t e, int t) {
+        size_t c = 0;
+        for (size_t i = b; i < e; ++i) c += keep[i];
+        kc[t] = c;
+    });
+    std::vector<size_t> kb(threads + 1, 0);
+    for (int t = 0; t < threads; ++t) kb[t + 1] = kb[t] + kc[t];
+    const size_t out_bytes = size_t(kept) * size_t(read_len);
+    uint8_t* buf = (uint8_t*)alloc_huge(out_bytes ? out_bytes : 1);
+    if (!buf) return PQ_ERR_NOMEM;
+    parallel_ranges(pairs, threads, [&](size_t b, size_t e, int t) {
+        const int RL = read_len;
+        uint8_t* __restrict__ o = buf + kb[t] * size_t(RL);
+        for (size_t i = b; i < e; ++i) {
+            if (!keep[i]) continue;
+            const unsigned char* sq = (const unsigned char*)seq_of(i);   // all bases (kept)
+            for (int j = 0; j < RL; ++j) o[j] = kBases.fw[sq[j]];
+            o += RL;
+        }
+    });
+    *reads_out = buf;
+    *num_reads_out = kept;
+    if (removed_out) *removed_out = removed;
+    return PQ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pq_import_fasta(const char* path, int read_len, int bloom_m, int n_hashfunc, uint8_t** reads_out,
+                    pq_index_type* num_reads_out, pq_index_type* removed_out, const char** err) {
+    const int rc = import_fasta_parallel(path, read_len, bloom_m, n_hashfunc, reads_out, num_reads_out, removed_out,
+                                         err);
+    if (rc >= 0) return rc;
+    return import_fasta_serial(path, read_len, bloom_m, n_hashfunc, reads_out, num_reads_out, removed_out, err);
 }
 
 pq_index_t* construct_index(char* single_file, char* pair_file1, char* pair_file2, char* mate_file1,

@@ -68,6 +68,58 @@ def test_import_errors(tmp_path):
     assert rc == 1 and "open reads file" in err
 
 
+@pytest.mark.parametrize("width", [32, 64])
+def test_import_line_semantics(tmp_path, width):
+    """The whole-file import keeps the line-by-line reading of the reference (fgets into 1000
+    bytes, last character of each sequence buffer dropped): a final line without a newline loses
+    its last character, N reads are dropped without touching the Bloom filter, an error names
+    line 2 * kept + 2, and lines of 999 or more characters take the line-by-line path."""
+    build.build()
+    f = tmp_path / "a.fa"
+    f.write_bytes(b">a\nACGT\n>b\nccgt\n>c\nACNT\n>d\nGGGTA")       # last line: 5 chars, no newline
+    rc, err, reads, removed = import_fasta(width, str(f), 4)
+    assert rc == 0, err
+    assert reads.tolist() == [[1, 2, 3, 4], [2, 2, 3, 4], [3, 3, 3, 4]] and removed == 1
+    f.write_bytes(b">a\nACGT\n>b\nACGT\n>c\nACGX\n")                # duplicate, then a bad base
+    rc, err, _, _ = import_fasta(width, str(f), 4)
+    assert rc == 1 and "at line 4." in err                             # one read kept before it
+    f.write_bytes(b">a\nACGT\nACGT\n>b\nACGT\n")                     # a sequence where a header belongs
+    rc, err, _, _ = import_fasta(width, str(f), 4)
+    assert rc == 1 and "at line 4." in err
+    f.write_bytes(b">a\nACGT\n>b\n")                                  # header without a sequence line
+    rc, err, _, _ = import_fasta(width, str(f), 4)
+    assert rc == 1 and "at line 4." in err
+    f.write_bytes(b">a\nACGT\r\n")                                    # CRLF: the CR is no base
+    rc, err, _, _ = import_fasta(width, str(f), 4)
+    assert rc == 1 and "at line 2." in err
+    f.write_bytes(b"")
+    rc, err, reads, removed = import_fasta(width, str(f), 4)
+    assert rc == 0 and reads.shape[0] == 0 and removed == 0
+    # a header of 1200 characters: fgets splits it, so its tail is read as the sequence line
+    f.write_bytes(b">" + b"x" * 1199 + b"\nACGT\n")
+    rc, err, _, _ = import_fasta(width, str(f), 4)
+    assert rc == 1 and "at line 2." in err
+
+
+def test_import_large_random_matches_line_by_line_rules(tmp_path):
+    """Many records with duplicates, reverse complements, N and lowercase: the kept set is the
+    reference's (golden import case) and equal for both index widths up to their own hashing."""
+    build.build()
+    z = np.load(os.path.join(GOLDEN, "import_L60.npz"))
+    with gzip.open(os.path.join(GOLDEN, "import_L60.fa.gz"), "rb") as fh:
+        text = fh.read()
+    # the same records without the final newline, and with the last sequence one base longer:
+    # the reference drops that base with the (absent) newline
+    lines = text.rstrip(b"\n").split(b"\n")
+    lines[-1] = lines[-1] + b"A"
+    f = tmp_path / "nolf.fa"
+    f.write_bytes(b"\n".join(lines))
+    for width in (32, 64):
+        rc, err, reads, removed = import_fasta(width, str(f), 60)
+        assert rc == 0, err
+        assert reads.shape[0] == int(z["kept%d" % width]) and sha(reads) == str(z["sha_reads%d" % width])
+
+
 LAYOUT_PROG = r"""
 #include <stdio.h>
 #include <stddef.h>
