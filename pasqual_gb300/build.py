@@ -17,7 +17,7 @@ OUT = os.path.join(HERE, "_build")
 ROOT = os.path.dirname(HERE)
 SOURCES = ["pq_index.cu", "pq_search.cu", "pq_sort.cu", "pq_api.cu", "pq_dropin.cu",
            "pq_sort_static.cu", "pq_learned.cu"]
-HEADERS = ["pq_common.cuh", "pq_index.cuh", "pq_sort.cuh", "pq_learned.cuh", "pq_learned_build.cuh"]
+HEADERS = ["pq_common.cuh", "pq_index.cuh", "pq_sort.cuh", "pq_learned.cuh", "pq_learned_build.cuh", "pq_slots.h"]
 PUBLIC = ["pasqual_gb300.h", "pasqual_gb300_dropin.h"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

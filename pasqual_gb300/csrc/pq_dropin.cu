@@ -23,6 +23,7 @@
 #include <thread>
 
 #include "pq_common.cuh"
+#include "pq_slots.h"
 #include "../../include/pasqual_gb300.h"
 #include "../../include/pasqual_gb300_dropin.h"
 
@@ -112,22 +113,6 @@ std::string g_import_err;
 std::mutex g_mu;
 std::unordered_map<const void*, pq_ctx*> g_ctx;
 
-// 1-3 base prefix rank with end-of-read lowest (the order of the reference's 85 "triplet"
-// codes): rank of the string s (|s| = 1..3) among all strings of length 1..3, 1-based.
-int prefix_rank(const int* s, int len) {
-    // enumerate strings in lexicographic order with shorter-prefix-first; rank = position
-    int r = 0;
-    // strings before s: for each position i, strings that share s[0..i) and then either end
-    // (counted once when i > 0 ... handled by ordering) or continue with a smaller base.
-    // Direct count: order is depth-first over the 4-ary tree of depth 3, a node before its
-    // children.
-    int sub[4] = {0, 21, 5, 1};   // size of the subtree below a node at depth d (incl. itself)
-    for (int i = 0; i < len; ++i) {
-        r += s[i] * sub[i + 1];    // whole subtrees of smaller siblings
-        r += 1;                    // the node itself (prefix s[0..i]) comes before its children
-    }
-    return r;                      // 1..84
-}
 
 }  // namespace
 
@@ -544,24 +529,11 @@ pq_index_t* construct_index(char* single_file, char* pair_file1, char* pair_file
             memcpy(dst[c], bm.data() + size_t(c) * rowlen, rowlen * sizeof(uint64_t));
         }
         // sort-slot sizes (src/sufsort.c:386-450): 5 slots of 17 first-prefix ranks
-        pq_index_type hist[85] = {0};
-        for (size_t r = 0; r < nr; ++r) {
-            const uint8_t* s = (const uint8_t*)ix->reads + r * read_len;
-            for (int j = 0; j < read_len; ++j) {
-                int q[3], len = std::min(3, read_len - j);
-                for (int a = 0; a < len; ++a) q[a] = (dir ? s[read_len - 1 - (j + a)] : s[j + a]) - 1;
-                hist[prefix_rank(q, len)]++;
-            }
-        }
         pq_index_type* size = dir ? ix->size_bw : ix->size_fw;
         pq_index_type* off = dir ? ix->offset_bw : ix->offset_fw;
         pq_index_type mx = 0;
-        for (int k = 0; k < 5; ++k) {
-            size[k] = 0;
-            for (int j = 0; j < 17; ++j) size[k] += hist[k * 17 + j];
-            off[k] = k ? off[k - 1] + size[k - 1] : 0;
-            mx = std::max(mx, size[k]);
-        }
+        pq_slots::slot_sizes<pq_index_type>((const uint8_t*)ix->reads, nr, read_len, dir, size, off, &mx,
+                                            int(std::max(1u, std::thread::hardware_concurrency())));
         if (dir) {
             ix->OCC_sample_bw = sample;
             ix->reads_index_bw = ri;
