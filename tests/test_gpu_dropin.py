@@ -81,6 +81,15 @@ def test_reference_entry_points(tmp_path, width):
     O = port.Port(width)
     oix = O.build_index(reads, t)
     assert list(ix.C) == [int(x) for x in oix["C"]]
+    # sort-slot sizes of both directions (5 slots of 17 first-prefix ranks)
+    from test_slot_sizes import direct_histogram
+    for d, (szf, off_f, mxf) in enumerate((("size_fw", "offset_fw", "max_size_fw"),
+                                           ("size_bw", "offset_bw", "max_size_bw"))):
+        h = direct_histogram(reads, d)
+        sizes = [int(h[17 * k:17 * k + 17].sum()) for k in range(5)]
+        assert list(getattr(ix, szf)) == sizes
+        assert list(getattr(ix, off_f)) == [sum(sizes[:k]) for k in range(5)]
+        assert int(getattr(ix, mxf)) == max(sizes)
     n = nr * L
     rowlen = n // 64 + 1
     for d, (bmf, smpf, rif) in enumerate((("OCC_bitmap", "OCC_sample", "reads_index"),
