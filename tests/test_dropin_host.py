@@ -175,3 +175,37 @@ def test_struct_layout_matches_reference(tmp_path, width):
                    ["pq_index_t", "pq_node_t", "pq_edge_t", "pq_path_t", "pq_path_q_t",
                     "pq_string_graph_t"], [os.path.join(ROOT, "include")], [])
     assert ref == mine
+
+
+@pytest.mark.parametrize("width", [32, 64])
+def test_reference_cli_links_and_imports(tmp_path, width):
+    """The reference's own CLI objects (test.o, assemble.o, common.o, compiled from its sources
+    by the oracle recipe where they are present) link against the library unchanged; run here,
+    the binary imports the reads through the library, then stops at the GPU step with the
+    reference's error convention (message on stderr, exit status 0) when no GPU is usable."""
+    from oracle import port
+    if not os.path.isdir(REF_SRC) or os.uname().machine != "x86_64" or not shutil.which("gcc"):
+        pytest.skip("reference sources (x86) not present")
+    build.build()
+    port.build(ref=True)
+    objdir = os.path.join(ROOT, "oracle", "_ref", "obj_u%d" % width)
+    objs = [os.path.join(objdir, o) for o in ("test.o", "assemble.o", "common.o")]
+    if not all(os.path.exists(o) for o in objs):
+        pytest.skip("reference objects not built")
+    libdir = os.path.dirname(pq.library_path(width))
+    exe = tmp_path / "pasqual_cli"
+    subprocess.run(["gcc", "-fopenmp", "-o", str(exe)] + objs +
+                   ["-L" + libdir, "-lpasqual_gb300_u%d" % width, "-Wl,-rpath," + libdir, "-lgomp", "-lm"],
+                   check=True)
+    fa = tmp_path / "r.fa"
+    with gzip.open(os.path.join(GOLDEN, "import_L60.fa.gz"), "rb") as f:
+        fa.write_bytes(f.read())
+    z = np.load(os.path.join(GOLDEN, "import_L60.npz"))
+    r = subprocess.run([str(exe), "--singlereads", str(fa), "-l", "60", "-t", "31"], cwd=str(tmp_path),
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0
+    assert "Importing reads from" in r.stdout
+    assert "has imported %d reads" % int(z["kept%d" % width]) in r.stdout
+    import torch
+    if not torch.cuda.is_available():
+        assert "no usable CUDA device" in r.stderr
