@@ -209,3 +209,35 @@ def test_reference_cli_links_and_imports(tmp_path, width):
     import torch
     if not torch.cuda.is_available():
         assert "no usable CUDA device" in r.stderr
+
+
+@pytest.mark.parametrize("width", [32, 64])
+def test_import_matches_reference_live(tmp_path, width):
+    """A larger generated read file (duplicates, reverse complements, N, lowercase; the Bloom
+    filter also drops some unique reads as false positives) imported by the reference itself and
+    by the library: the same kept reads, byte for byte."""
+    from oracle import port
+    from pasqual_gb300 import synth
+    if not os.path.isdir(REF_SRC) or os.uname().machine != "x86_64":
+        pytest.skip("reference sources (x86) not present")
+    port.build(ref=True)
+    build.build()
+    rng = np.random.default_rng(2024 + width)
+    g = synth.genome(400000, 0.45, 0.1, (0.01, 0.02), seed=99)
+    rd = synth.reads(g, 80, 40000, 0.01, seed=100)
+    seqs = [bytes(synth.ACGT[r]) for r in rd]
+    for i in rng.choice(len(seqs), 2000, replace=False):
+        seqs.append(bytes(synth.ACGT[synth.revcomp(rd[i])]))
+    for i in rng.choice(len(seqs), 1000, replace=False):
+        s = bytearray(seqs[i]); s[int(rng.integers(0, 80))] = ord("N"); seqs.append(bytes(s))
+    for i in rng.choice(len(seqs), 1000, replace=False):
+        seqs.append(seqs[i].lower())
+    order = rng.permutation(len(seqs))
+    fa = tmp_path / "live.fa"
+    fa.write_bytes(b"".join(b">r%d\n%s\n" % (k, seqs[j]) for k, j in enumerate(order)))
+    ref = port.run_ref_dump(str(fa), 80, 41, str(tmp_path / "ref"), width=width)
+    rc, err, reads, removed = import_fasta(width, str(fa), 80)
+    assert rc == 0, err
+    assert reads.shape[0] == ref["reads"].shape[0]
+    assert np.array_equal(reads, ref["reads"].reshape(reads.shape))
+    assert removed == len(seqs) - reads.shape[0]
