@@ -133,6 +133,24 @@ PQ_API pq_index_t *construct_index (char *single_file, char *pair_file1, char *p
  * from index->reads), then node_t construction as src/string_graph.c:832-1017. */
 PQ_API pq_string_graph_t *construct_string_graph (pq_index_t * index);
 
+/* Node construction only (src/string_graph.c:832-1017), the second half of
+ * construct_string_graph: the reference's string_graph_t built from a graph in the CSR form that
+ * pq_get_graph returns (per read num_B, num_F, olp_B, olp_F and edge_off[num_reads + 1]; per
+ * edge dest, len, type and trans).  The nodes are built on `threads` host threads (0 = one per
+ * core), as the reference builds them inside its parallel search loop; the result does not depend
+ * on the thread count.  path_q->max_F_trans / max_B_trans hold the running maximum of the trans
+ * values in read order (the reference's value with one thread).  average_overlap is the mean
+ * edge overlap length (NaN for a graph without edges, as in the reference).  Every node, edge
+ * list and path queue is malloc'd as the reference's are.  Returns NULL (nothing left allocated)
+ * when memory runs out. */
+PQ_API pq_string_graph_t *pq_string_graph_from_csr (pq_index_type num_reads, int read_len,
+                                                    int min_overlap, const uint16_t * num_B,
+                                                    const uint16_t * num_F, const int32_t * olp_B,
+                                                    const int32_t * olp_F, const uint64_t * edge_off,
+                                                    const pq_index_type * dest, const uint16_t * len,
+                                                    const uint8_t * type, const int32_t * trans,
+                                                    int threads);
+
 /* src/string_graph.h:142 — the reference's destroy_graph is empty; so is this one. */
 PQ_API void destroy_graph (pq_string_graph_t * graph);
 

@@ -39,7 +39,8 @@ EXPORTS = ["pq_idx_bytes", "pq_create", "pq_destroy", "pq_last_error", "pq_set_r
 
 
 # The reference's own entry points served by the same library (include/pasqual_gb300_dropin.h).
-DROPIN_EXPORTS = ["construct_index", "construct_string_graph", "destroy_graph", "pq_import_fasta"]
+DROPIN_EXPORTS = ["construct_index", "construct_string_graph", "destroy_graph", "pq_import_fasta",
+                  "pq_string_graph_from_csr"]
 
 
 class PQError(RuntimeError):

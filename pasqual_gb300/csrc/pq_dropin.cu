@@ -591,86 +591,173 @@ pq_string_graph_t* construct_string_graph(pq_index_t* ix) {
     uint64_t ne = 0;
     ck(pq_get_graph_sizes(ctx, &ne, nullptr, nullptr));
     const size_t nr = ix->num_reads;
-    std::vector<uint16_t> nB(nr + 1), nF(nr + 1);
-    std::vector<int32_t> oB(nr + 1), oF(nr + 1), trans(ne + 1);
-    std::vector<uint64_t> off(nr + 1);
-    std::vector<pq_index_type> dest(ne + 1);
-    std::vector<uint16_t> len(ne + 1);
-    std::vector<uint8_t> type(ne + 1);
-    ck(pq_get_graph(ctx, nB.data(), nF.data(), oB.data(), oF.data(), off.data(), dest.data(), len.data(), type.data(),
-                    trans.data()));
+    // uninitialised host arrays: pq_get_graph writes every entry
+    std::unique_ptr<uint16_t[]> nB(new uint16_t[nr + 1]), nF(new uint16_t[nr + 1]), len(new uint16_t[ne + 1]);
+    std::unique_ptr<int32_t[]> oB(new int32_t[nr + 1]), oF(new int32_t[nr + 1]), trans(new int32_t[ne + 1]);
+    std::unique_ptr<uint64_t[]> off(new uint64_t[nr + 1]);
+    std::unique_ptr<pq_index_type[]> dest(new pq_index_type[ne + 1]);
+    std::unique_ptr<uint8_t[]> type(new uint8_t[ne + 1]);
+    ck(pq_get_graph(ctx, nB.get(), nF.get(), oB.get(), oF.get(), off.get(), dest.get(), len.get(), type.get(),
+                    trans.get()));
     pq_destroy(ctx);
-
-    pq_string_graph_t* g = (pq_string_graph_t*)malloc(sizeof(pq_string_graph_t));
+    pq_string_graph_t* g = pq_string_graph_from_csr(ix->num_reads, ix->read_len, ix->min_overlap, nB.get(), nF.get(),
+                                                    oB.get(), oF.get(), off.get(), dest.get(), len.get(), type.get(),
+                                                    trans.get(), 0);
     if (!g) error_exit("out of memory.\n");
-    g->nodes = (pq_node_t*)calloc(nr ? nr : 1, sizeof(pq_node_t));
-    if (!g->nodes) error_exit("out of memory.\n");
-    g->num_reads = ix->num_reads;
-    g->read_len = ix->read_len;
-    g->min_overlap = ix->min_overlap;
-    const int L = ix->read_len;
-    const char ONE = 1, BRANCH = 2, ENDING = 4, REMOVED = 8, SUSPECT = 4, NONE = 0;
-    const char BB = 3, FB = 1;
-    pq_index_type run_max_F = 0, run_max_B = 0;   // I_F[1].uu / I_B[1].uu of one thread
-    double overlap_len = 0;
-    pq_index_type overlaps = 0;
-    for (size_t i = 0; i < nr; ++i) {
-        pq_node_t* nd = &g->nodes[i];
-        const int b = nB[i], f = nF[i];
-        const uint64_t e0 = off[i];
-        for (int j = 0; j < b; ++j) run_max_B = std::max(run_max_B, (pq_index_type)trans[e0 + j]);
-        for (int j = 0; j < f; ++j) run_max_F = std::max(run_max_F, (pq_index_type)trans[e0 + b + j]);
-        nd->max_B = nd->num_B = (uint16_t)b;
-        nd->max_F = nd->num_F = (uint16_t)f;
-        nd->status = 0;
-        nd->path_q = nullptr;
-        nd->edges = (pq_edge_t*)malloc((size_t(b) + f) * sizeof(pq_edge_t));
-        const int ob = oB[i], of = oF[i];
-        const int mx = std::max(ob, of);
-        double ratio = mx == 0 ? 0 : ((double)abs(ob - of)) / mx;
-        nd->marked = ratio > 0.6 ? SUSPECT : 0;
-        if (b || f) {
-            nd->B_type = b == 1 ? ONE : (b > 1 ? BRANCH : ENDING);
-            nd->F_type = f == 1 ? ONE : (f > 1 ? BRANCH : ENDING);
-        } else {
-            nd->B_type = nd->F_type = ENDING;
-            nd->status = REMOVED;
-        }
-        int olen = 0;
-        for (int j = 0; j < b + f; ++j) {
-            nd->edges[j].dest = dest[e0 + j];
-            nd->edges[j].overlap_len = len[e0 + j];
-            nd->edges[j].type = (char)type[e0 + j];
-            olen += len[e0 + j];
-        }
-        if ((nd->B_type == BRANCH && nd->F_type != ENDING) || (nd->F_type == BRANCH && nd->B_type != ENDING)) {
-            pq_path_q_t* q = (pq_path_q_t*)malloc(sizeof(pq_path_q_t));
-            q->max_B_endlen = q->max_F_endlen = q->max_B_len = q->max_F_len = 0;
-            q->path = (pq_path_t*)malloc(sizeof(pq_path_t) * (size_t(b) + f));
-            q->max_F_trans = (int)run_max_F;
-            q->max_B_trans = (int)run_max_B;
-            for (int j = 0; j < b + f; ++j) {
-                pq_path_t* p = &q->path[j];
-                const pq_edge_t* e = &nd->edges[j];
-                p->end = e->dest;
-                p->hop = e->dest;
-                p->len = 1;
-                p->end_len = (uint16_t)(L - e->overlap_len);
-                p->bubble_len = 0;
-                p->type = NONE;
-                p->updated = 0;
-                p->direction = j < b ? (e->type == BB ? 1 : 0) : (e->type == FB ? 1 : 0);
-                p->trans = trans[e0 + j];
-            }
-            nd->path_q = q;
-        }
-        overlaps += (pq_index_type)(b + f);
-        overlap_len += (double)olen;
-    }
     printf("  takes %.3lf ms\n", now_ms() - t0);
-    g->average_overlap = overlap_len / overlaps;
     printf("  average overlap length: %lf\n", g->average_overlap);
     fflush(stdout);
+    return g;
+}
+
+// Frees what pq_string_graph_from_csr allocated for the nodes [0, n).
+static void free_nodes(pq_node_t* nodes, size_t n) {
+    for (size_t i = 0; i < n; ++i) {
+        free(nodes[i].edges);
+        if (nodes[i].path_q) free(nodes[i].path_q->path);
+        free(nodes[i].path_q);
+    }
+}
+
+pq_string_graph_t* pq_string_graph_from_csr(pq_index_type num_reads, int read_len, int min_overlap,
+                                            const uint16_t* num_B, const uint16_t* num_F, const int32_t* olp_B,
+                                            const int32_t* olp_F, const uint64_t* edge_off, const pq_index_type* dest,
+                                            const uint16_t* len, const uint8_t* type, const int32_t* trans,
+                                            int threads) {
+    const size_t nr = num_reads;
+    pq_string_graph_t* g = (pq_string_graph_t*)malloc(sizeof(pq_string_graph_t));
+    if (!g) return nullptr;
+    g->nodes = (pq_node_t*)calloc(nr ? nr : 1, sizeof(pq_node_t));
+    if (!g->nodes) {
+        free(g);
+        return nullptr;
+    }
+    g->num_reads = num_reads;
+    g->read_len = (uint16_t)read_len;
+    g->min_overlap = (uint16_t)min_overlap;
+    if (threads <= 0) threads = std::max(1, int(std::thread::hardware_concurrency()));
+    threads = std::max(1, std::min<int>(threads, int((nr + 4095) / 4096)));
+    const size_t chunk = nr ? (nr + threads - 1) / threads : 0;
+
+    // The running maximum of trans in read order (I_F[1].uu / I_B[1].uu of one reference thread):
+    // each range's own maximum first, then every range starts from the maximum of those before it.
+    std::vector<pq_index_type> mx_B(threads, 0), mx_F(threads, 0);
+    std::vector<uint64_t> olen(threads, 0), cnt(threads, 0);   // integer sums: exact, any order
+    std::vector<char> oom(threads, 0);
+    auto run = [&](auto&& body) {
+        if (threads == 1) {
+            body(0);
+            return;
+        }
+        std::vector<std::thread> th;
+        for (int t = 0; t < threads; ++t) th.emplace_back([&, t] { body(t); });
+        for (auto& x : th) x.join();
+    };
+    run([&](int t) {
+        const size_t b = std::min(nr, size_t(t) * chunk), e = std::min(nr, b + chunk);
+        pq_index_type mB = 0, mF = 0;
+        for (size_t i = b; i < e; ++i) {
+            const uint64_t e0 = edge_off[i];
+            for (int j = 0; j < num_B[i]; ++j) mB = std::max(mB, (pq_index_type)trans[e0 + j]);
+            for (int j = 0; j < num_F[i]; ++j) mF = std::max(mF, (pq_index_type)trans[e0 + num_B[i] + j]);
+        }
+        mx_B[t] = mB;
+        mx_F[t] = mF;
+    });
+    {   // exclusive prefix maximum over the ranges
+        pq_index_type pB = 0, pF = 0;
+        for (int t = 0; t < threads; ++t) {
+            const pq_index_type rB = mx_B[t], rF = mx_F[t];
+            mx_B[t] = pB;
+            mx_F[t] = pF;
+            pB = std::max(pB, rB);
+            pF = std::max(pF, rF);
+        }
+    }
+    const char ONE = 1, BRANCH = 2, ENDING = 4, REMOVED = 8, SUSPECT = 4, NONE = 0;
+    const char BB = 3, FB = 1;
+    run([&](int t) {
+        const size_t b = std::min(nr, size_t(t) * chunk), e = std::min(nr, b + chunk);
+        pq_index_type run_max_B = mx_B[t], run_max_F = mx_F[t];
+        uint64_t sum_len = 0, sum_cnt = 0;
+        for (size_t i = b; i < e; ++i) {
+            pq_node_t* nd = &g->nodes[i];
+            const int nb = num_B[i], nf = num_F[i];
+            const uint64_t e0 = edge_off[i];
+            for (int j = 0; j < nb; ++j) run_max_B = std::max(run_max_B, (pq_index_type)trans[e0 + j]);
+            for (int j = 0; j < nf; ++j) run_max_F = std::max(run_max_F, (pq_index_type)trans[e0 + nb + j]);
+            nd->max_B = nd->num_B = (uint16_t)nb;
+            nd->max_F = nd->num_F = (uint16_t)nf;
+            nd->status = 0;
+            nd->path_q = nullptr;
+            nd->edges = (pq_edge_t*)malloc((size_t(nb) + nf) * sizeof(pq_edge_t));
+            if (!nd->edges && nb + nf) {
+                oom[t] = 1;
+                return;
+            }
+            const int ob = olp_B[i], of = olp_F[i];
+            const int mo = std::max(ob, of);
+            const double ratio = mo == 0 ? 0 : ((double)abs(ob - of)) / mo;
+            nd->marked = ratio > 0.6 ? SUSPECT : 0;
+            if (nb || nf) {
+                nd->B_type = nb == 1 ? ONE : (nb > 1 ? BRANCH : ENDING);
+                nd->F_type = nf == 1 ? ONE : (nf > 1 ? BRANCH : ENDING);
+            } else {
+                nd->B_type = nd->F_type = ENDING;
+                nd->status = REMOVED;
+            }
+            for (int j = 0; j < nb + nf; ++j) {
+                nd->edges[j].dest = dest[e0 + j];
+                nd->edges[j].overlap_len = len[e0 + j];
+                nd->edges[j].type = (char)type[e0 + j];
+                sum_len += len[e0 + j];
+            }
+            if ((nd->B_type == BRANCH && nd->F_type != ENDING) || (nd->F_type == BRANCH && nd->B_type != ENDING)) {
+                pq_path_q_t* q = (pq_path_q_t*)malloc(sizeof(pq_path_q_t));
+                pq_path_t* path = (pq_path_t*)malloc(sizeof(pq_path_t) * (size_t(nb) + nf));
+                if (!q || !path) {
+                    free(q);
+                    free(path);
+                    oom[t] = 1;
+                    return;
+                }
+                q->max_B_endlen = q->max_F_endlen = q->max_B_len = q->max_F_len = 0;
+                q->path = path;
+                q->max_F_trans = (int)run_max_F;
+                q->max_B_trans = (int)run_max_B;
+                for (int j = 0; j < nb + nf; ++j) {
+                    pq_path_t* p = &path[j];
+                    const pq_edge_t* ed = &nd->edges[j];
+                    p->end = ed->dest;
+                    p->hop = ed->dest;
+                    p->len = 1;
+                    p->end_len = (uint16_t)(read_len - ed->overlap_len);
+                    p->bubble_len = 0;
+                    p->type = NONE;
+                    p->updated = 0;
+                    p->direction = j < nb ? (ed->type == BB ? 1 : 0) : (ed->type == FB ? 1 : 0);
+                    p->trans = trans[e0 + j];
+                }
+                nd->path_q = q;
+            }
+            sum_cnt += uint64_t(nb + nf);
+        }
+        olen[t] = sum_len;
+        cnt[t] = sum_cnt;
+    });
+    double overlap_len = 0;
+    pq_index_type overlaps = 0;
+    for (int t = 0; t < threads; ++t) {
+        if (oom[t]) {
+            free_nodes(g->nodes, nr);
+            free(g->nodes);
+            free(g);
+            return nullptr;
+        }
+        overlap_len += (double)olen[t];
+        overlaps += (pq_index_type)cnt[t];
+    }
+    g->average_overlap = overlap_len / overlaps;
     return g;
 }
 
