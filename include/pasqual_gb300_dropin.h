@@ -156,7 +156,8 @@ PQ_API void destroy_graph (pq_string_graph_t * graph);
 
 /* Import only: the reads construct_index keeps (num_reads * read_len codes 1..4, malloc'd,
  * caller frees) and the number removed as duplicates.  Returns PQ_OK or PQ_ERR_ARG with the
- * reference's message in *err (static storage). */
+ * reference's message in *err (static storage): the CLI's argument checks (read_len in
+ * (0, 65535], n_hashfunc in [1, 5], bloom_m >= 1; src/test.c:300-320), then the import's own. */
 PQ_API int pq_import_fasta (const char *path, int read_len, int bloom_m, int n_hashfunc,
                             uint8_t ** reads_out, pq_index_type * num_reads_out,
                             pq_index_type * removed_out, const char **err);

@@ -223,11 +223,12 @@ def ref_available() -> bool:
     return os.path.exists(os.path.join(REF, "ref_dump_u32"))
 
 
-def run_ref_dump(fasta: str, L: int, t: int, outdir: str, width: int = 32, threads: int = 4):
+def run_ref_dump(fasta: str, L: int, t: int, outdir: str, width: int = 32, threads: int = 4,
+                 bloom_m: int = 36, n_hashfunc: int = 2):
     """Run the unmodified reference (oracle/_ref/ref_dump_uXX) on a FASTA; return its dump."""
     exe = os.path.join(REF, "ref_dump_u%d" % width)
-    subprocess.run([exe, fasta, str(L), str(t), outdir, str(threads)], check=True,
-                   stdout=subprocess.DEVNULL)
+    subprocess.run([exe, fasta, str(L), str(t), outdir, str(threads), str(bloom_m), str(n_hashfunc)],
+                   check=True, stdout=subprocess.DEVNULL)
     return load_dump(outdir)
 
 

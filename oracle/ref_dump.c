@@ -5,7 +5,7 @@
  *
  * Test infrastructure only: linked against the reference objects built by oracle/Makefile.
  *
- *   ref_dump READS.fa L T OUTDIR [THREADS]
+ *   ref_dump READS.fa L T OUTDIR [THREADS [BLOOM_M N_HASHFUNC]]   (Bloom defaults: 36, 2)
  *
  * Calls, in the order the reference's main() makes them (src/test.c:364-370):
  *   construct_index()        src/index.h:63-68   (run single-threaded: the canonical tie order)
@@ -82,17 +82,18 @@ main (int argc, char **argv)
 {
     if (argc < 5)
     {
-        fprintf (stderr, "usage: %s READS.fa L T OUTDIR [THREADS]\n", argv[0]);
+        fprintf (stderr, "usage: %s READS.fa L T OUTDIR [THREADS [BLOOM_M N_HASHFUNC]]\n", argv[0]);
         return 2;
     }
     const char *fa = argv[1];
     int L = atoi (argv[2]), t = atoi (argv[3]);
     const char *out = argv[4];
     int threads = argc > 5 ? atoi (argv[5]) : omp_get_max_threads ();
+    int bloom_m = argc > 7 ? atoi (argv[6]) : 36, n_hashfunc = argc > 7 ? atoi (argv[7]) : 2;
     mkdir (out, 0755);
 
     omp_set_num_threads (1);
-    index_t *idx = construct_index ((char *) fa, NULL, NULL, NULL, NULL, t, L, 36, 2);
+    index_t *idx = construct_index ((char *) fa, NULL, NULL, NULL, NULL, t, L, bloom_m, n_hashfunc);
     INDEX_TYPE_T nr = idx->num_reads, n = nr * (INDEX_TYPE_T) L;
     INDEX_TYPE_T rowlen = (n + 64) / 64;
 

@@ -21,6 +21,7 @@
 #include <string>
 #include <algorithm>
 #include <thread>
+#include <type_traits>
 
 #include "pq_common.cuh"
 #include "pq_slots.h"
@@ -186,25 +187,6 @@ int import_fasta_serial(const char* path, int read_len, int bloom_m, int n_hashf
     return PQ_OK;
 }
 
-// The five hashes of src/bloom.c over a read's codes (len bytes, no terminator needed), in
-// index-width arithmetic, all in one pass (five independent chains); out[f] = hash f mod m.
-void hash_codes5(const char* k, int len, pq_index_type m, pq_index_type (&out)[5]) {
-    pq_index_type h0 = 0, h1 = 0, h2 = 0, h3 = 0, h4 = 0;
-    for (int i = 0; i < len; ++i) {
-        const pq_index_type c = (unsigned char)k[i];
-        h0 ^= (h0 << 5) + (h0 >> 2) + c;
-        h1 = c + (h1 << 6) + (h1 << 16) - h1;
-        h2 += c;
-        h3 ^= c;
-        h4 = 33 * h4 + c;
-    }
-    out[0] = h0 % m;
-    out[1] = h1 % m;
-    out[2] = h2 % m;
-    out[3] = h3 % m;
-    out[4] = h4 % m;
-}
-
 // Base symbol -> code (A=1 C=2 G=3 T=4, either case), the code of its complement, and a class:
 // 0 = base, 1 = N (either case), 2 = any other byte.  Tables make the decode branch-free.
 struct BaseTables {
@@ -226,6 +208,36 @@ struct BaseTables {
     }
 };
 const BaseTables kBases;
+
+// The first NF string hashes of src/bloom.c over a record's base codes and over its reverse
+// complement's, read straight from the sequence line through the base tables (forward codes front
+// to back, complement codes back to front) in one pass of 2 * NF independent chains, in
+// index-width arithmetic; hf[f] / hr[f] = hash f mod m.  Returns the OR of (1 << class) over the
+// line's bytes; the hashes are stored only when no N and no other byte was seen.
+template <int NF>
+inline unsigned hash_line(const unsigned char* sq, int RL, pq_index_type m, pq_index_type* hf,
+                          pq_index_type* hr) {
+    pq_index_type a0 = 0, a1 = 0, a2 = 0, a3 = 0, a4 = 0, r0 = 0, r1 = 0, r2 = 0, r3 = 0, r4 = 0;
+    unsigned cls = 0;
+    for (int j = 0; j < RL; ++j) {
+        const unsigned char ch = sq[j];
+        cls |= 1u << kBases.cls[ch];
+        const pq_index_type c = kBases.fw[ch], d = kBases.rc[sq[RL - 1 - j]];
+        if (NF > 0) { a0 ^= (a0 << 5) + (a0 >> 2) + c; r0 ^= (r0 << 5) + (r0 >> 2) + d; }   // shift-xor
+        if (NF > 1) { a1 = c + (a1 << 6) + (a1 << 16) - a1; r1 = d + (r1 << 6) + (r1 << 16) - r1; }   // sdbm
+        if (NF > 2) { a2 += c; r2 += d; }                                                     // sum
+        if (NF > 3) { a3 ^= c; r3 ^= d; }                                                     // xor
+        if (NF > 4) { a4 = 33 * a4 + c; r4 = 33 * r4 + d; }                                 // times 33
+    }
+    if ((cls & 6u) == 0) {
+        const pq_index_type av[5] = {a0, a1, a2, a3, a4}, rv[5] = {r0, r1, r2, r3, r4};
+        for (int f = 0; f < NF; ++f) {
+            hf[f] = av[f] % m;
+            hr[f] = rv[f] % m;
+        }
+    }
+    return cls;
+}
 
 // malloc-compatible (free()-able) memory in 2 MB-aligned whole huge pages where the kernel
 // grants them on request: random accesses then miss the TLB far less often
@@ -344,44 +356,38 @@ int import_fasta_parallel(const char* path, int read_len, int bloom_m, int n_has
     // the sequence line of record i (valid records only)
     const size_t* __restrict__ const st = start.get();
     auto seq_of = [st, T](size_t i) { return T + st[2 * i + 1]; };
-    parallel_ranges(pairs, threads, [&, st, T](size_t b, size_t e, int) {
-        // locals and restrict pointers: the character stores below may not alias anything else
-        const int RL = read_len, NF = nf;
-        const size_t NL = nlines;
-        const bool open_end = last_open;
-        const pq_index_type M = m;
-        uint8_t* __restrict__ const sta = status.get();
-        pq_index_type* __restrict__ const hf = hfw.get();
-        pq_index_type* __restrict__ const hr = hrc.get();
-        char fw[1000], rc[1000];                     // lines are shorter than 999 characters here
-        for (size_t i = b; i < e; ++i) {
-            const size_t h = 2 * i, q = h + 1;
-            const size_t hlen = st[h + 1] - 1 - st[h];
-            if (hlen == 0 || T[st[h]] != '>' || q >= NL) { sta[i] = 2; continue; }
-            // the reference drops the last character of the buffer: the newline, or the last
-            // base of a final line without one
-            const size_t slen = (st[q + 1] - 1 - st[q]) + (q + 1 == NL && open_end ? 0 : 1) - 1;
-            if (slen != size_t(RL)) { sta[i] = 2; continue; }
-            const unsigned char* sq = (const unsigned char*)(T + st[q]);
-            unsigned cls = 0;
-            for (int j = 0; j < RL; ++j) {
-                const unsigned char ch = sq[j];
-                fw[j] = char(kBases.fw[ch]);
-                rc[RL - 1 - j] = char(kBases.rc[ch]);
-                cls |= 1u << kBases.cls[ch];
+    auto classify = [&, st, T](auto nf_tag) {
+        constexpr int NF = decltype(nf_tag)::value;
+        parallel_ranges(pairs, threads, [&, st, T](size_t b, size_t e, int) {
+            const int RL = read_len;
+            const size_t NL = nlines;
+            const bool open_end = last_open;
+            const pq_index_type M = m;
+            uint8_t* __restrict__ const sta = status.get();
+            pq_index_type* __restrict__ const hf = hfw.get();
+            pq_index_type* __restrict__ const hr = hrc.get();
+            for (size_t i = b; i < e; ++i) {
+                const size_t h = 2 * i, q = h + 1;
+                const size_t hlen = st[h + 1] - 1 - st[h];
+                if (hlen == 0 || T[st[h]] != '>' || q >= NL) { sta[i] = 2; continue; }
+                // the reference drops the last character of the buffer: the newline, or the last
+                // base of a final line without one
+                const size_t slen = (st[q + 1] - 1 - st[q]) + (q + 1 == NL && open_end ? 0 : 1) - 1;
+                if (slen != size_t(RL)) { sta[i] = 2; continue; }
+                const unsigned cls = hash_line<NF>((const unsigned char*)(T + st[q]), RL, M, hf + i * NF, hr + i * NF);
+                // a byte that is no base and no N: error; an N: dropped before the filter
+                sta[i] = (cls & 4u) ? 2 : ((cls & 2u) ? 1 : 0);
             }
-            if (cls & 4u) { sta[i] = 2; continue; }      // a byte that is no base and no N
-            sta[i] = (cls & 2u) ? 1 : 0;
-            if (cls & 2u) continue;
-            pq_index_type a5[5], r5[5];
-            hash_codes5(fw, RL, M, a5);
-            hash_codes5(rc, RL, M, r5);
-            for (int f = 0; f < NF; ++f) {
-                hf[i * NF + f] = a5[f];
-                hr[i * NF + f] = r5[f];
-            }
-        }
-    });
+        });
+    };
+    switch (nf) {
+        case 0: classify(std::integral_constant<int, 0>{}); break;
+        case 1: classify(std::integral_constant<int, 1>{}); break;
+        case 2: classify(std::integral_constant<int, 2>{}); break;
+        case 3: classify(std::integral_constant<int, 3>{}); break;
+        case 4: classify(std::integral_constant<int, 4>{}); break;
+        default: classify(std::integral_constant<int, 5>{}); break;
+    }
     // the Bloom pass in input order (src/bloom.c:91-135), up to the first bad record
     const size_t nbits_bytes = (size_t(m) + 7) / 8 + 1;
     std::unique_ptr<unsigned char, decltype(&free)> bits_mem((unsigned char*)alloc_huge(nbits_bytes), &free);
@@ -457,6 +463,23 @@ extern "C" {
 
 int pq_import_fasta(const char* path, int read_len, int bloom_m, int n_hashfunc, uint8_t** reads_out,
                     pq_index_type* num_reads_out, pq_index_type* removed_out, const char** err) {
+    // the CLI's own argument checks (src/test.c:300-320), which run before the reference imports
+    const char* bad = nullptr;
+    char msg[160];
+    if (read_len <= 0 || read_len > 65535) {
+        snprintf(msg, sizeof msg, "invalid read length (%d), valid range (0, 65535].\n", read_len);
+        bad = msg;
+    } else if (n_hashfunc < 1 || n_hashfunc > 5) {
+        snprintf(msg, sizeof msg, "invalid number of hash functions (%d), valid range [1, MAX_FUNC].\n", n_hashfunc);
+        bad = msg;
+    } else if (bloom_m < 1) {
+        bad = "length of bloom filter array must be larger than 1.\n";
+    }
+    if (bad || !path || !reads_out || !num_reads_out) {
+        g_import_err = bad ? bad : "invalid argument.\n";
+        if (err) *err = g_import_err.c_str();
+        return PQ_ERR_ARG;
+    }
     const int rc = import_fasta_parallel(path, read_len, bloom_m, n_hashfunc, reads_out, num_reads_out, removed_out,
                                          err);
     if (rc >= 0) return rc;

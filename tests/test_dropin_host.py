@@ -66,6 +66,13 @@ def test_import_errors(tmp_path):
     assert rc == 1 and "incorrect reads file" in err
     rc, err, _, _ = import_fasta(32, str(tmp_path / "missing.fa"), 4)
     assert rc == 1 and "open reads file" in err
+    # the reference CLI's argument checks (src/test.c:300-320), before any file access
+    for L, m, nf, msg in ((0, 36, 2, "invalid read length (0)"), (70000, 36, 2, "invalid read length"),
+                          (4, 36, 0, "invalid number of hash functions (0)"),
+                          (4, 36, 6, "invalid number of hash functions (6)"),
+                          (4, 0, 2, "length of bloom filter array")):
+        rc, err, _, _ = import_fasta(32, str(bad), L, m, nf)
+        assert rc == 1 and msg in err, (L, m, nf, err)
 
 
 @pytest.mark.parametrize("width", [32, 64])
@@ -211,11 +218,13 @@ def test_reference_cli_links_and_imports(tmp_path, width):
         assert "no usable CUDA device" in r.stderr
 
 
-@pytest.mark.parametrize("width", [32, 64])
-def test_import_matches_reference_live(tmp_path, width):
+@pytest.mark.parametrize("width,bloom_m,nfunc", [(32, 36, 2), (64, 36, 2), (32, 6, 1), (64, 10, 3),
+                                               (32, 12, 4), (64, 40, 5)])
+def test_import_matches_reference_live(tmp_path, width, bloom_m, nfunc):
     """A larger generated read file (duplicates, reverse complements, N, lowercase; the Bloom
-    filter also drops some unique reads as false positives) imported by the reference itself and
-    by the library: the same kept reads, byte for byte."""
+    filter also drops some unique reads as false positives, many with a short filter) imported by
+    the reference itself and by the library, for every number of hash functions: the same kept
+    reads, byte for byte."""
     from oracle import port
     from pasqual_gb300 import synth
     if not os.path.isdir(REF_SRC) or os.uname().machine != "x86_64":
@@ -235,8 +244,9 @@ def test_import_matches_reference_live(tmp_path, width):
     order = rng.permutation(len(seqs))
     fa = tmp_path / "live.fa"
     fa.write_bytes(b"".join(b">r%d\n%s\n" % (k, seqs[j]) for k, j in enumerate(order)))
-    ref = port.run_ref_dump(str(fa), 80, 41, str(tmp_path / "ref"), width=width)
-    rc, err, reads, removed = import_fasta(width, str(fa), 80)
+    ref = port.run_ref_dump(str(fa), 80, 41, str(tmp_path / "ref"), width=width, bloom_m=bloom_m,
+                            n_hashfunc=nfunc)
+    rc, err, reads, removed = import_fasta(width, str(fa), 80, bloom_m, nfunc)
     assert rc == 0, err
     assert reads.shape[0] == ref["reads"].shape[0]
     assert np.array_equal(reads, ref["reads"].reshape(reads.shape))
