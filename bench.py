@@ -63,6 +63,36 @@ def dist_env():
     return rank, world, local
 
 
+def _group_size() -> int:
+    import torch.distributed as dist
+    return dist.get_world_size() if dist.is_available() and dist.is_initialized() else 1
+
+
+def rank_barrier() -> None:
+    """Barrier over the replicas (the default process group); nothing with one rank."""
+    if _group_size() > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def rank_max(x: float, device="cpu") -> float:
+    """Maximum of x over the replicas (x itself with one rank).  `device` is where the reduction
+    tensor lives: the rank's GPU under NCCL, the CPU under gloo."""
+    if _group_size() == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    tt = torch.tensor([x], device=device, dtype=torch.float64)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def replica_throughput(reads_per_rank: int, world: int, slowest_ms: float) -> float:
+    """Whole-job reads/s of `world` replicas that each searched reads_per_rank reads, the slowest
+    in slowest_ms per step (weak scaling: every rank searches its own full read set)."""
+    return reads_per_rank * world / (slowest_ms * 1e-3)
+
+
 def workload_reads(name: str, scale: float):
     from pasqual_gb300 import synth
     _, rd, L, t = synth.make_workload(name, scale=scale)
@@ -300,17 +330,10 @@ def run_ours(args):
     P = pq.Pasqual(width, device=local, stream=stream.cuda_stream)
 
     def barrier():
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
+        rank_barrier()
 
     def max_over_ranks(x: float) -> float:
-        if world == 1:
-            return x
-        import torch.distributed as dist
-        tt = torch.tensor([x], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        return float(tt.item())
+        return rank_max(x, dev)
 
     # ---- index build (setup) and suffix-sort throughput
     P.set_reads(rd, t)
@@ -406,7 +429,7 @@ def run_ours(args):
     achieved = alg_bytes / (kms * 1e-3) / 1e9
     tpr = profile_figure("dram_bytes_per_read")
     out = {
-        "metric": METRIC, "value": nr * world / (step_ms * 1e-3), "unit": "reads/s",
+        "metric": METRIC, "value": replica_throughput(nr, world, step_ms), "unit": "reads/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "int%d-index" % width, "data": "synthetic",
@@ -426,7 +449,7 @@ def run_ours(args):
                      "probes_per_read": probes / max(nr, 1), "kernel_ms": kms,
                      "traffic": (tpr * nr) if tpr else None},
         "gpu_launches": int(l1 - l0),
-        "e2e": ({"value": nr / (e2e_ms_med * 1e-3), "unit": "reads/s",
+        "e2e": ({"value": replica_throughput(nr, world, e2e_ms_med), "unit": "reads/s",
                  "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                  "ms_per_step": e2e_ms_med, "parts_last_step": parts[-1]} if e2e_ms_med else None),
     }
