@@ -152,7 +152,9 @@ int import_fasta_serial(const char* path, int read_len, int bloom_m, int n_hashf
     while (fgets(line, 1000, fp)) {
         if (line[0] != '>') { fclose(fp); return bad(kept); }
         if (!fgets(line, 1000, fp)) { fclose(fp); return bad(kept); }
-        line[strlen(line) - 1] = '\0';
+        const size_t got = strlen(line);     // 0 when the line starts with a NUL byte
+        if (got == 0) { fclose(fp); return bad(kept); }   // the length check below fails then too
+        line[got - 1] = '\0';
         if ((int)strlen(line) != read_len) { fclose(fp); return bad(kept); }
         bool with_n = false;
         for (int i = 0; i < read_len; ++i) {

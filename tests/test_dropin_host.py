@@ -106,6 +106,13 @@ def test_import_line_semantics(tmp_path, width):
     f.write_bytes(b">" + b"x" * 1199 + b"\nACGT\n")
     rc, err, _, _ = import_fasta(width, str(f), 4)
     assert rc == 1 and "at line 2." in err
+    # NUL bytes (line by line): fgets stops nowhere special, but the C string ends at the NUL
+    f.write_bytes(b">a\nACGT\n>b\nAC\x00T\n")
+    rc, err, _, _ = import_fasta(width, str(f), 4)
+    assert rc == 1 and "at line 4." in err
+    f.write_bytes(b">a\nACGT\n>b\n\x00CGT\n")                        # a line that starts with NUL
+    rc, err, _, _ = import_fasta(width, str(f), 4)
+    assert rc == 1 and "at line 4." in err
 
 
 def test_import_large_random_matches_line_by_line_rules(tmp_path):
