@@ -142,7 +142,8 @@ PQ_API pq_string_graph_t *construct_string_graph (pq_index_t * index);
  * values in read order (the reference's value with one thread).  average_overlap is the mean
  * edge overlap length (NaN for a graph without edges, as in the reference).  Every node, edge
  * list and path queue is malloc'd as the reference's are.  Returns NULL (nothing left allocated)
- * when memory runs out. */
+ * when memory runs out, when read_len is outside (0, 65535], or when an array the graph needs is
+ * NULL (the per-edge arrays may be NULL for a graph without edges). */
 PQ_API pq_string_graph_t *pq_string_graph_from_csr (pq_index_type num_reads, int read_len,
                                                     int min_overlap, const uint16_t * num_B,
                                                     const uint16_t * num_F, const int32_t * olp_B,

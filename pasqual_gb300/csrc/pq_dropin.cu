@@ -650,6 +650,9 @@ pq_string_graph_t* pq_string_graph_from_csr(pq_index_type num_reads, int read_le
                                             const uint16_t* len, const uint8_t* type, const int32_t* trans,
                                             int threads) {
     const size_t nr = num_reads;
+    if (read_len <= 0 || read_len > 65535 || min_overlap < 0 || min_overlap > 65535) return nullptr;
+    if (nr && (!num_B || !num_F || !olp_B || !olp_F || !edge_off)) return nullptr;
+    if (nr && edge_off[nr] && (!dest || !len || !type || !trans)) return nullptr;
     pq_string_graph_t* g = (pq_string_graph_t*)malloc(sizeof(pq_string_graph_t));
     if (!g) return nullptr;
     g->nodes = (pq_node_t*)calloc(nr ? nr : 1, sizeof(pq_node_t));

@@ -125,3 +125,24 @@ def test_graph_without_edges():
     g0 = call(lib, 32, 80, 41, tuple(a[:0] if k < 4 else (a[:1] if k == 4 else a)
                                      for k, a in enumerate(csr)), 0)
     assert g0.num_reads == 0 and math.isnan(g0.average_overlap)
+
+
+def test_invalid_arguments_return_null():
+    lib = pq.load_library(32)
+    f = lib.pq_string_graph_from_csr
+    f.restype = ct.c_void_p
+    f.argtypes = [ct.c_uint32, ct.c_int, ct.c_int] + [ct.c_void_p] * 9 + [ct.c_int]
+    nb, nf, ob, of, off, dest, ln, et, trans = random_csr(100, 3)
+    dest = dest.astype(np.uint32)
+    p = lambda a: a.ctypes.data_as(ct.c_void_p)
+    good = [p(nb), p(nf), p(ob), p(of), p(off), p(dest), p(ln), p(et), p(trans)]
+    assert f(100, 100, 55, *good, 1)                    # leaks one small graph; fine in a test
+    assert not f(100, 0, 55, *good, 1)
+    assert not f(100, 70000, 55, *good, 1)
+    for k in range(9):
+        args = list(good)
+        args[k] = None
+        assert not f(100, 100, 55, *args, 1), k
+    z16, z32 = np.zeros(10, np.uint16), np.zeros(10, np.int32)
+    zoff = np.zeros(11, np.uint64)
+    assert f(10, 100, 55, p(z16), p(z16), p(z32), p(z32), p(zoff), None, None, None, None, 1)
