@@ -59,3 +59,20 @@ def test_create_without_gpu_fails_loudly(libs):
         pytest.skip("a GPU is present")
     with pytest.raises(pq.PQError):
         pq.Pasqual(32)
+
+
+@pytest.mark.parametrize("width", [32, 64])
+def test_product_never_links_the_oracle(libs, width):
+    """The library and its Python binding neither link, load nor import the oracle (the C
+    restatement or the reference build): no CPU fallback can stand in for the CUDA path."""
+    out = subprocess.run(["readelf", "-d", pq.library_path(width)], capture_output=True, text=True,
+                         check=True).stdout
+    needed = re.findall(r"\(NEEDED\)\s+Shared library: \[([^\]]+)\]", out)
+    assert needed and not [n for n in needed if "oracle" in n or "pasqual_ref" in n], needed
+    pkg = os.path.join(ROOT, "pasqual_gb300")
+    for dirpath, _, files in os.walk(pkg):
+        for fn in files:
+            if fn.endswith((".py", ".cu", ".cuh", ".h", ".cpp")):
+                txt = open(os.path.join(dirpath, fn)).read()
+                assert not re.search(r"^\s*(from|import)\s+oracle\b", txt, flags=re.M), fn
+                assert "pq_oracle" not in txt and "libpasqual_ref" not in txt, fn
