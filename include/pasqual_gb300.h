@@ -164,8 +164,8 @@ PQ_API int pq_get_stage_ms (pq_ctx * ctx, float *sort_ms, float *fm_ms, float *s
  * that cannot take cudaMalloc's implicit device-wide synchronisation.  It calls no cudaMalloc,
  * cudaFree or other allocating routine: the caller passes device pointers to the reads
  * (num_reads * read_len codes 1..4) and to the output suffix array (num_reads * read_len
- * entries), and the working memory is a fixed array inside this library (about 30 MB for the
- * 32-bit build, 38 MB for the 64-bit one) that every GPU which loads the library keeps until the
+ * entries), and the working memory is a fixed array inside this library (about 28 MB for the
+ * 32-bit build, 32 MB for the 64-bit one) that every GPU which loads the library keeps until the
  * process exits.  Sizes above PQ_STATIC_SORT_MAX_SUFFIXES return PQ_ERR_CAPACITY without doing
  * any work.  The first call on each device looks up the array's device address (once, with that
  * device current); make that first call before any stream capture.  All calls share the array:
