@@ -144,3 +144,43 @@ def test_import_fuzz_against_restatement(tmp_path, width):
             assert reads.shape == want[1].shape and np.array_equal(reads, want[1]), case
             assert removed == want[2], case
     assert n_ok > 300 and n_err > 300
+
+
+@pytest.mark.parametrize("width", [32, 64])
+def test_restatement_matches_reference(tmp_path, width):
+    """The restatement above pinned to the reference's own import (its construct_index, compiled
+    by the oracle recipe) on random edge-case files: the same error, or the same numbers of kept
+    and removed reads (and the same bytes where the reference's sort of so few reads completes)."""
+    import os
+    import subprocess
+    from oracle import port
+    if not os.path.isdir("/root/reference/src") or os.uname().machine != "x86_64":
+        pytest.skip("reference sources (x86) not present")
+    port.build(ref=True)
+    exe = os.path.join(port.REF, "ref_dump_u%d" % width)
+    rng = np.random.default_rng(77 + width)
+    f = tmp_path / "f.fa"
+    compared = 0
+    while compared < 40:
+        L = int(rng.choice([20, 60]))
+        bloom_m, nf = int(rng.choice([1, 2, 5, 36])), int(rng.integers(1, 6))
+        data = random_file(rng, L)
+        if b"\0" in data:
+            continue                  # the reference writes before its buffer on a NUL-led line
+        want = model_import(data, L, bloom_m, nf, width)
+        if want[0] == "ok" and want[1].shape[0] < 2:
+            continue                  # the reference's sort needs reads to sort
+        f.write_bytes(data)
+        out = tmp_path / ("d%d" % compared)
+        r = subprocess.run([exe, str(f), str(L), str(L - 5), str(out), "1", str(bloom_m), str(nf)],
+                           capture_output=True, text=True, timeout=120)
+        if want[0] == "err":
+            assert "incorrect reads file at line %d." % want[1] in r.stderr, (r.stderr, want)
+        else:
+            # the import's own report; the reference's sort may then fail on a few reads
+            assert "has imported %d reads (removed %d duplicate reads)" % (want[1].shape[0], want[2]) \
+                in r.stdout, (r.stdout, want[1].shape, want[2])
+            if r.returncode == 0:
+                got = np.fromfile(os.path.join(str(out), "reads.bin"), np.uint8)
+                assert np.array_equal(got, want[1].reshape(-1))
+        compared += 1
