@@ -9,6 +9,7 @@ import pytest
 
 import pasqual_gb300 as pq
 from pasqual_gb300 import graph
+from conftest import golden_cases, idx_dtype, load_golden, sha
 from test_gpu_dropin import structs
 
 
@@ -146,3 +147,37 @@ def test_invalid_arguments_return_null():
     z16, z32 = np.zeros(10, np.uint16), np.zeros(10, np.int32)
     zoff = np.zeros(11, np.uint64)
     assert f(10, 100, 55, p(z16), p(z16), p(z32), p(z32), p(zoff), None, None, None, None, 1)
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_nodes_match_reference_digests(name):
+    """The library's node build on the oracle's edge lists gives the reference's own node_t
+    array: node types, status, SUSPECT marks, edges and path trans (-1 where a node has no path
+    queue) hash to the digests the reference's construct_string_graph produced for the case."""
+    from oracle import port
+    port.build()
+    g = load_golden(name)
+    width, t = int(g["width"]), int(g["t"])
+    reads = g["reads"]
+    nr, L = reads.shape
+    O = port.Port(width)
+    ref = O.overlaps(O.build_index(reads, t, threads=4), threads=4)
+    csr = (ref.num_B, ref.num_F, ref.olp_B, ref.olp_F, ref.edge_off, ref.dest, ref.length,
+           ref.etype, ref.trans)
+    gr = call(pq.load_library(width), width, L, t, csr, 0)
+    node = np.zeros((nr, 4), np.uint8)
+    dest, length, etype, trans = [], [], [], []
+    for i in range(nr):
+        nd = gr.nodes[i]
+        node[i] = (nd.B_type, nd.F_type, nd.status, nd.marked)
+        for j in range(nd.num_B + nd.num_F):
+            e = nd.edges[j]
+            dest.append(int(e.dest))
+            length.append(e.overlap_len)
+            etype.append(ord(e.type))
+            trans.append(nd.path_q.contents.path[j].trans if nd.path_q else -1)
+    assert sha(node) == str(g["sha_node_types"])
+    assert sha(np.array(dest, idx_dtype(width))) == str(g["sha_dest"])
+    assert sha(np.array(length, np.uint16)) == str(g["sha_length"])
+    assert sha(np.array(etype, np.uint8)) == str(g["sha_etype"])
+    assert sha(np.array(trans, np.int64)) == str(g["sha_trans"])
