@@ -113,6 +113,18 @@ main (int argc, char **argv)
     for (int c = 0; c < 4; c++)
         fprintf (m, " %llu", (unsigned long long) idx->prefix_count[c]);
     fprintf (m, "\n");
+    /* the sort-slot bookkeeping initial_sort leaves in index_t (src/index.c:466-469, 519-522) */
+    const INDEX_TYPE_T *slot_f[4] = {idx->size_fw, idx->offset_fw, idx->size_bw, idx->offset_bw};
+    const char *slot_n[4] = {"size_fw", "offset_fw", "size_bw", "offset_bw"};
+    for (int k = 0; k < 4; k++)
+    {
+        fprintf (m, "%s", slot_n[k]);
+        for (int c = 0; c < 5; c++)
+            fprintf (m, " %llu", (unsigned long long) slot_f[k][c]);
+        fprintf (m, "\n");
+    }
+    fprintf (m, "max_size_fw %llu\nmax_size_bw %llu\n", (unsigned long long) idx->max_size_fw,
+             (unsigned long long) idx->max_size_bw);
 
     size_t isz = sizeof (INDEX_TYPE_T);
     dump (out, "reads.bin", idx->reads, n);

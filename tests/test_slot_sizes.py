@@ -86,3 +86,31 @@ def test_slot_histogram_matches_direct_count(harness, L, threads):
             assert sz == int(want[17 * k:17 * k + 17].sum())
             assert off == int(want[:17 * k].sum())
         assert int(out[90]) == max(s for s, _ in sizes)
+
+
+@pytest.mark.parametrize("name", ["iid8k_L50_t31_u32", "lowc12k_L150_t63_u64"])
+def test_slot_sizes_match_reference(harness, tmp_path, name):
+    """The same sizes the reference's own initial_sort leaves in index_t, on a golden case's
+    reads (fed back through the reference with a Bloom filter long enough to keep them all)."""
+    from conftest import GOLDEN
+    from oracle import port
+    from pasqual_gb300 import synth
+    if not os.path.isdir("/root/reference/src") or os.uname().machine != "x86_64":
+        pytest.skip("reference sources (x86) not present")
+    port.build(ref=True)
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    reads, t, width = z["reads"], int(z["t"]), int(z["width"])
+    fa = tmp_path / "r.fa"
+    synth.write_fasta(str(fa), reads)
+    d = port.run_ref_dump(str(fa), reads.shape[1], t, str(tmp_path / "d"), width=width, bloom_m=100000)
+    assert np.array_equal(d["reads"], reads)
+    exe, _ = harness
+    path = tmp_path / "r.bin"
+    path.write_bytes(reads.tobytes())
+    for dir_, tag in ((0, "fw"), (1, "bw")):
+        out = subprocess.run([exe, str(path), str(reads.shape[0]), str(reads.shape[1]), str(dir_), "4"],
+                             capture_output=True, text=True, check=True).stdout.split("\n")
+        sizes = [tuple(int(v) for v in ln.split()) for ln in out[85:90]]
+        assert [s for s, _ in sizes] == d["meta"]["size_" + tag]
+        assert [o for _, o in sizes] == d["meta"]["offset_" + tag]
+        assert int(out[90]) == d["meta"]["max_size_" + tag]
