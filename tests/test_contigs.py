@@ -15,16 +15,17 @@ from pasqual_gb300 import build, synth
 REF_SRC = "/root/reference/src"
 
 
-@pytest.mark.parametrize("width,L,t,glen,cov,seed", [(32, 100, 63, 300000, 20, 5),
-                                                    (64, 75, 41, 200000, 25, 6)])
-def test_contigs_match_reference(tmp_path, width, L, t, glen, cov, seed):
+@pytest.mark.parametrize("width,L,t,glen,cov,seed,lowc,err", [(32, 100, 63, 300000, 20, 5, 0.0, 0.003),
+                                                              (64, 75, 41, 200000, 25, 6, 0.0, 0.003),
+                                                              (32, 100, 55, 150000, 25, 9, 0.01, 0.01)])
+def test_contigs_match_reference(tmp_path, width, L, t, glen, cov, seed, lowc, err):
     from oracle import port
     if not os.path.isdir(REF_SRC) or os.uname().machine != "x86_64":
         pytest.skip("reference sources (x86) not present")
     build.build()
     port.build(ref=True)
-    g = synth.genome(glen, 0.42, 0.08, (0.01, 0.03), seed=seed)
-    rd = synth.reads_for_coverage(g, L, cov, 0.003, seed=seed + 1)
+    g = synth.genome(glen, 0.42, 0.08, (0.01, 0.03), lowc, seed=seed)
+    rd = synth.reads_for_coverage(g, L, cov, err, seed=seed + 1)
     fa = tmp_path / "reads.fa"
     synth.write_fasta(str(fa), rd)
     env = dict(os.environ, OMP_NUM_THREADS="1")
