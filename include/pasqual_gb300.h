@@ -170,9 +170,10 @@ PQ_API int pq_get_stage_ms (pq_ctx * ctx, float *sort_ms, float *fm_ms, float *s
  * any work.  The first call on each device looks up the array's device address (once, with that
  * device current); make that first call before any stream capture.  All calls share the array:
  * calls that overlap on the GPU (other streams, other host threads) race and must be ordered by
- * the caller.  Work is queued on `cuda_stream` (a cudaStream_t, NULL = the default stream) and
- * the call returns once the suffix array is written.  Returns PQ_OK, PQ_ERR_ARG, PQ_ERR_CAPACITY
- * or PQ_ERR_CUDA. */
+ * the caller.  Work runs on `cuda_stream` (a cudaStream_t, NULL = the default stream) and the
+ * call synchronises that stream before it returns, so the suffix array is complete on return and
+ * a kernel failure comes back as PQ_ERR_CUDA.  A read byte outside the codes 1..4 returns
+ * PQ_ERR_ARG before any sorting.  Returns PQ_OK, PQ_ERR_ARG, PQ_ERR_CAPACITY or PQ_ERR_CUDA. */
 PQ_API int pq_suffix_sort_static (const uint8_t * reads_dev, pq_idx num_reads, int read_len,
                                   int dir, pq_idx * sa_dev, void *cuda_stream);
 

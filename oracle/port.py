@@ -17,12 +17,22 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF = os.path.join(HERE, "_ref")
 
+# The reference checkout the recipes read (never written).  PASQUAL_REFERENCE overrides it; this
+# is the one place that names the default.
+REFERENCE = os.environ.get("PASQUAL_REFERENCE", "/root/reference")
+REFERENCE_SRC = os.path.join(REFERENCE, "src")
+
+
+def reference_buildable() -> bool:
+    """The reference's sources are present and this host can compile them (x86: SSE4.2)."""
+    return os.path.isdir(REFERENCE_SRC) and os.uname().machine == "x86_64"
+
 
 def build(ref: bool = False) -> None:
     """Compile the restatement (and, when asked and available, the reference)."""
     subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
     if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + REFERENCE], check=True)
 
 
 def np_idx(width: int):

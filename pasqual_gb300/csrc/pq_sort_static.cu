@@ -13,6 +13,12 @@
 // a device share it: calls whose work overlaps on the GPU (different streams, or different
 // host threads) race on it and must be ordered by the caller.  Every call writes all of the
 // scratch it reads back, and clears the histogram it accumulates, before use.
+//
+// Each call first counts the read bytes outside the base codes 1..4 (a count kept in a second
+// fixed device variable, cleared by the call) and refuses such input with PQ_ERR_ARG: the sort
+// packs 2 bits a base, so another byte would corrupt its neighbours' bits and give a wrong order.
+// The call synchronises its stream before it returns, so the suffix array is complete and any
+// kernel error is reported as PQ_ERR_CUDA.
 #include <cstdio>
 #include <mutex>
 
@@ -33,6 +39,18 @@ constexpr size_t kScratchBytes =
     al256(3 * (kMax / 2048 + 2) * sizeof(unsigned long long)) + al256(kMax) + 1024;
 
 __device__ __align__(256) unsigned char g_sort_scratch[kScratchBytes];
+__device__ unsigned long long g_bad_codes;
+
+__global__ void k_clear_bad_codes() { g_bad_codes = 0; }
+
+// Bytes of reads[0, n) that are not a base code 1..4, added to g_bad_codes.
+__global__ void k_count_bad_codes(const uint8_t* __restrict__ reads, size_t n) {
+    unsigned long long bad = 0;
+    for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
+        bad += unsigned(reads[i] - 1u) > 3u;
+    for (int o = 16; o; o >>= 1) bad += __shfl_xor_sync(0xffffffffu, bad, o);
+    if ((threadIdx.x & 31) == 0 && bad) atomicAdd(&g_bad_codes, bad);
+}
 
 // Device address of g_sort_scratch per device, looked up once per device with that device
 // current (host code must not pass the symbol itself: it is a host-side stand-in).
@@ -69,7 +87,16 @@ extern "C" int pq_suffix_sort_static(const uint8_t* reads_dev, pq_idx num_reads,
     int rc = scratch_address(&scratch);
     if (rc != PQ_OK) return rc;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(cuda_stream);
+    const size_t nn = size_t(n);
+    k_clear_bad_codes<<<1, 1, 0, st>>>();
+    k_count_bad_codes<<<unsigned((nn + 255) / 256 < 1024 ? (nn + 255) / 256 : 1024), 256, 0, st>>>(reads_dev, nn);
+    unsigned long long bad = 0;
+    if (cudaMemcpyFromSymbolAsync(&bad, g_bad_codes, sizeof bad, 0, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return PQ_ERR_CUDA;
+    if (bad) return PQ_ERR_ARG;
     int e = pq::suffix_sort(reads_dev, idx_t(num_reads), read_len, dir, reinterpret_cast<idx_t*>(sa_dev), scratch,
                             kScratchBytes, st);
-    return e == 0 ? PQ_OK : PQ_ERR_CUDA;
+    if (e != 0) return PQ_ERR_CUDA;
+    return cudaStreamSynchronize(st) == cudaSuccess && cudaGetLastError() == cudaSuccess ? PQ_OK : PQ_ERR_CUDA;
 }

@@ -12,7 +12,6 @@ import pytest
 from conftest import ROOT
 from pasqual_gb300 import build, synth
 
-REF_SRC = "/root/reference/src"
 
 
 @pytest.mark.parametrize("width,L,t,glen,cov,seed,lowc,err", [(32, 100, 63, 300000, 20, 5, 0.0, 0.003),
@@ -20,7 +19,7 @@ REF_SRC = "/root/reference/src"
                                                               (32, 100, 55, 150000, 25, 9, 0.01, 0.01)])
 def test_contigs_match_reference(tmp_path, width, L, t, glen, cov, seed, lowc, err):
     from oracle import port
-    if not os.path.isdir(REF_SRC) or os.uname().machine != "x86_64":
+    if not port.reference_buildable():
         pytest.skip("reference sources (x86) not present")
     build.build()
     port.build(ref=True)

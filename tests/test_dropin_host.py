@@ -12,8 +12,9 @@ import pytest
 from conftest import GOLDEN, ROOT, sha
 import pasqual_gb300 as pq
 from pasqual_gb300 import build
+from oracle import port as _port
 
-REF_SRC = "/root/reference/src"
+REF_SRC = _port.REFERENCE_SRC
 
 
 @pytest.fixture(scope="module")
@@ -198,7 +199,7 @@ def test_reference_cli_links_and_imports(tmp_path, width):
     the binary imports the reads through the library, then stops at the GPU step with the
     reference's error convention (message on stderr, exit status 0) when no GPU is usable."""
     from oracle import port
-    if not os.path.isdir(REF_SRC) or os.uname().machine != "x86_64" or not shutil.which("gcc"):
+    if not port.reference_buildable() or not shutil.which("gcc"):
         pytest.skip("reference sources (x86) not present")
     build.build()
     port.build(ref=True)
@@ -234,7 +235,7 @@ def test_import_matches_reference_live(tmp_path, width, bloom_m, nfunc):
     reads, byte for byte."""
     from oracle import port
     from pasqual_gb300 import synth
-    if not os.path.isdir(REF_SRC) or os.uname().machine != "x86_64":
+    if not port.reference_buildable():
         pytest.skip("reference sources (x86) not present")
     port.build(ref=True)
     build.build()

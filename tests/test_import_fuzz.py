@@ -154,7 +154,7 @@ def test_restatement_matches_reference(tmp_path, width):
     import os
     import subprocess
     from oracle import port
-    if not os.path.isdir("/root/reference/src") or os.uname().machine != "x86_64":
+    if not port.reference_buildable():
         pytest.skip("reference sources (x86) not present")
     port.build(ref=True)
     exe = os.path.join(port.REF, "ref_dump_u%d" % width)

@@ -74,7 +74,7 @@ def test_golden_fixture_is_the_reference_on_its_reads(tmp_path, name):
     the reference's import with a Bloom filter long enough that no read is lost to a false
     positive (the fixture's reads are already free of duplicates)."""
     import os
-    if not os.path.isdir("/root/reference/src") or os.uname().machine != "x86_64":
+    if not port.reference_buildable():
         pytest.skip("reference sources (x86) not present")
     sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
     import make_golden
@@ -94,7 +94,7 @@ def test_golden_generator_reproduces_fixture(tmp_path, name):
     repeats or low-complexity runs came from an earlier version of the genome generator; they are
     pinned by their stored reads above."""
     import os
-    if not os.path.isdir("/root/reference/src") or os.uname().machine != "x86_64":
+    if not port.reference_buildable():
         pytest.skip("reference sources (x86) not present")
     sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
     import make_golden

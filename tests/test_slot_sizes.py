@@ -95,7 +95,7 @@ def test_slot_sizes_match_reference(harness, tmp_path, name):
     from conftest import GOLDEN
     from oracle import port
     from pasqual_gb300 import synth
-    if not os.path.isdir("/root/reference/src") or os.uname().machine != "x86_64":
+    if not port.reference_buildable():
         pytest.skip("reference sources (x86) not present")
     port.build(ref=True)
     z = np.load(os.path.join(GOLDEN, name + ".npz"))
