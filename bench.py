@@ -1,19 +1,30 @@
 #!/usr/bin/env python
-"""Benchmark: overlap-search reads/s (and suffix-sort Msuffix/s) of PASQUAL's hot path.
+"""Benchmark: overlap-search reads/s and suffix-sort Msuffix/s of PASQUAL's hot path, the learned
+index with the batched (queued, graph-replayed) search against the plain GPU backward search.
 
-Workload (default): 50 Mbp synthetic genome, GC 41 %, 10 % repeat copies of 1-5 kbp segments at
-1 % divergence; 100 bp reads at 30x from both strands with 0.5 % substitution errors; t = 63;
-32-bit index.  Reads are de-duplicated (equal or reverse-complement reads dropped) before use.
+Workload (default): 250 Mbp synthetic genome, GC 42 %, 15 % repeat copies of 1-5 kbp segments at
+0.5-2 % divergence; 100 bp reads at 20x from both strands (50 M reads) with 0.5 % substitution
+errors; t = 55; 64-bit index, 4.8 G suffixes per index after de-duplication (equal or
+reverse-complement reads dropped), sorted in chunks.  Data is seeded synthetic.
 
 A step is one overlap search (find_intervals + transitive reduction + edge CSR) over every read,
-on indexes already resident in HBM.  ``value`` = reads searched / time, whole job.
+with both indexes resident in HBM, in the library's default seed mode (1: depth-t interval scan
+with sorted-continuation reduction).  ``value`` = reads searched / step time, whole job.
 
-``e2e`` runs the public API end to end each step: host reads (pinned) -> GPU suffix sorts and
-FM-indexes -> overlap search -> edges back to host, into host arrays allocated by the untimed
-first step and reused (as the pinned input buffer is).
+Beside it, on the same index: ``plain`` = the reference's method on the GPU (seed mode 0: walk
+and FM-index DFS), ``learned`` = seed mode 2 (learned-index windows), ``learned_batched`` = seed
+mode 2 through the queued persistent search replayed from a CUDA graph with the autotuned plan,
+``learned_batched_vs_plain`` = the ratio of the last two.  Every mode's edges are compared with
+the plain search's.  ``roofline`` is the dominant kernel's algorithmic traffic as the library
+counts it inside the kernels (32-byte sectors of index data loaded + result bytes written) over
+its CUDA-event time, against the measured HBM copy bandwidth; ``reference_probes_per_read`` is the
+reference method's work, which the GPU method avoids.
 
-``--impl reference`` times the reference's CPU algorithm for the same metric: the C restatement
-of the reference (oracle/), OpenMP over all host cores, on a bounded sample.
+``e2e`` runs the public API end to end each step: pinned host reads -> GPU suffix sorts and
+FM-indexes -> overlap search -> edges back to host arrays.
+
+``--impl reference`` times the reference's CPU algorithm for the same metric and workload: the C
+restatement of the reference (oracle/), OpenMP over all host cores, each step a bounded sample.
 """
 from __future__ import annotations
 
@@ -34,7 +45,7 @@ sys.path.insert(0, ROOT)
 import numpy as np  # noqa: E402
 
 METRIC = "overlap-search reads/s + sort Msuffix/s, learned vs plain GPU, bit-exact"
-WORKLOAD = "50Mbp_L100_30x_t63"
+WORKLOAD = "250Mbp_L100_20x_t55"
 
 
 def parse():
@@ -45,14 +56,16 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--scale", type=float, default=1.0, help="genome-size scale (1.0 = full)")
-    ap.add_argument("--cpu-scale", type=float, default=0.1,
-                    help="genome-size scale of the CPU-baseline sample")
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--cpu-scale", type=float, default=0.01,
+                    help="genome-size scale of the CPU-baseline sample's index")
+    ap.add_argument("--cpu-seconds", type=float, default=20.0,
+                    help="CPU work of the cpu_baseline sample (reference arm: of all steps together)")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-modes", action="store_true", help="skip the plain/learned comparison")
-    ap.add_argument("--batched-scale", type=float, default=0.25,
-                    help="genome scale of the queued-search workload (0 = skip)")
+    ap.add_argument("--batched-scale", type=float, default=0.1,
+                    help="genome scale of the mixed read-set queued workload (0 = skip)")
+    ap.add_argument("--detail", default="", help="also write every figure to this JSON file")
     return ap.parse_args()
 
 
@@ -99,6 +112,15 @@ def workload_reads(name: str, scale: float):
     return synth.dedup(rd), L, t
 
 
+def workload_config(name: str) -> dict:
+    """The workload as both arms report it (its definition, not quantities measured on it)."""
+    from pasqual_gb300 import synth
+    w = synth.WORKLOADS[name]
+    return {"workload": name, "genome_bp": w["genome"], "read_len": w["L"], "coverage": w["cov"],
+            "t": w["t"], "index": "U%d" % w.get("index", 32),
+            "l2": "inputs larger than L2 (both FM-indexes, suffix arrays and packed texts), no flush"}
+
+
 def measured_peak_hbm():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -108,15 +130,22 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def profile_figure(key: str):
-    """A figure recorded in the committed ncu summary of the search kernel ("key = value")."""
-    p = os.path.join(ROOT, "profiles", "k_search_lean.md")
+def profile_figure(name: str, key: str):
+    """A figure recorded in a committed ncu summary under profiles/ ("key = value")."""
+    p = os.path.join(ROOT, "profiles", name)
     try:
         txt = open(p).read()
     except OSError:
         return None
     m = re.search(re.escape(key) + r"\s*=\s*([0-9.]+)", txt)
     return float(m.group(1)) if m else None
+
+
+def r4(x):
+    """Four significant digits (keeps the JSON line short)."""
+    if x is None or isinstance(x, (bool, int)):
+        return x
+    return float("%.4g" % x)
 
 
 class Clocks:
@@ -178,140 +207,192 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(workload: str, scale: float, seconds: float, threads: int | None = None):
-    """The C restatement of the reference's overlap search on the host cores (OpenMP), timed on a
-    bounded sample: index of a genome scaled by `scale`, search over as many reads as fit in
-    about `seconds` seconds."""
-    from oracle import port
-    port.build()
-    rd, L, t = workload_reads(workload, scale)
-    threads = threads or os.cpu_count() or 1
-    P = port.Port(32)
-    ix = P.build_index(rd, t, threads=threads, seed_k=min(12, t))
-    seeds = (ix["seed0"], ix["seed1"])
-    nr = rd.shape[0]
-    probe = min(nr, 20000)
-    t0 = time.perf_counter()
-    P.overlaps(ix, 0, probe, threads=threads, seeds=seeds)
-    dt = time.perf_counter() - t0
-    count = int(min(nr, max(probe, probe * seconds / max(dt, 1e-6))))
-    t0 = time.perf_counter()
-    g = P.overlaps(ix, 0, count, threads=threads, seeds=seeds)
-    dt = time.perf_counter() - t0
-    return {"value": count / dt, "unit": "reads/s", "cores": threads, "kind": "port",
-            "sample": "%d of %d reads of the %s workload at genome scale %g (%d bp reads, t=%d), "
-                      "forward/backward seeds at depth 12 as the reference's sort records them; "
-                      "%.1f s" % (count, nr, workload, scale, L, t, dt),
-            "probes_per_read": g.probes / max(count, 1)}
+class CpuSample:
+    """The C restatement of the reference's overlap search on the host cores (OpenMP): the index
+    of the workload's genome scaled by `scale` (same read length, coverage, t and error rate),
+    built once, then searched read range by read range."""
+
+    def __init__(self, workload: str, scale: float, threads: int | None = None):
+        from oracle import port
+        port.build()
+        self.rd, self.L, self.t = workload_reads(workload, scale)
+        self.workload, self.scale = workload, scale
+        self.threads = threads or os.cpu_count() or 1
+        from pasqual_gb300 import synth
+        width = synth.WORKLOADS[workload].get("index", 32)
+        self.P = port.Port(width)
+        self.ix = self.P.build_index(self.rd, self.t, threads=self.threads, seed_k=min(12, self.t))
+        self.seeds = (self.ix["seed0"], self.ix["seed1"])
+        self.next = 0
+
+    def search(self, seconds: float):
+        """Search about `seconds` of reads (continuing where the last call stopped, wrapping
+        around); returns (reads, seconds, probes)."""
+        nr = self.rd.shape[0]
+        probe = min(nr, 4000)
+        t0 = time.perf_counter()
+        self._run(probe)
+        dt = time.perf_counter() - t0
+        count = int(min(nr, max(probe, probe * seconds / max(dt, 1e-6))))
+        t0 = time.perf_counter()
+        probes = self._run(count)
+        return count, time.perf_counter() - t0, probes
+
+    def _run(self, count: int) -> int:
+        nr = self.rd.shape[0]
+        first = self.next if self.next + count <= nr else 0
+        self.next = (first + count) % nr
+        g = self.P.overlaps(self.ix, first, count, threads=self.threads, seeds=self.seeds)
+        return g.probes
+
+    def describe(self, count: int, secs: float) -> str:
+        return ("%d reads of the %s workload's reads at genome scale %g (%d reads kept, %d bp, "
+                "t=%d), searched in %.1f s against their own index (seeds at depth 12)"
+                % (count, self.workload, self.scale, self.rd.shape[0], self.L, self.t, secs))
+
+
+def cpu_baseline(workload: str, scale: float, seconds: float):
+    cs = CpuSample(workload, scale)
+    n, secs, probes = cs.search(seconds)
+    return {"value": n / secs, "unit": "reads/s", "cores": cs.threads, "kind": "port",
+            "sample": cs.describe(n, secs), "probes_per_read": probes / max(n, 1)}
 
 
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    cb = cpu_baseline(args.workload, args.cpu_scale, args.cpu_seconds)
-    vals = [cb["value"]]
-    for _ in range(max(0, args.steps - 1)):
-        vals.append(cpu_baseline(args.workload, args.cpu_scale, args.cpu_seconds / 2)["value"])
+    cs = CpuSample(args.workload, args.cpu_scale)
+    per_step = max(0.5, args.cpu_seconds / max(1, args.steps))
+    for _ in range(args.warmup):
+        cs.search(per_step / 4)
+    vals, total_n, total_s = [], 0, 0.0
+    for _ in range(args.steps):
+        n, secs, _ = cs.search(per_step)
+        vals.append(n / secs)
+        total_n += n
+        total_s += secs
     v = statistics.median(vals)
-    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": "reads/s", "n_gpus": world,
+    out = {"impl": "reference", "metric": METRIC, "value": r4(v), "unit": "reads/s", "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "int32-index", "data": "synthetic",
-           "config": {"workload": args.workload, "index": "U32", "sample_scale": args.cpu_scale},
-           "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
-           "e2e": {"value": v, "unit": "reads/s", "h2d_bytes_per_step": 0,
-                   "d2h_bytes_per_step": 0}}
-    out["cpu_baseline"]["value"] = v
+           "scaling": "weak", "vs_baseline": None,
+           "dtype": "int%s-index" % workload_config(args.workload)["index"][1:],
+           "data": "synthetic", "config": workload_config(args.workload),
+           "cpu_baseline": {"value": r4(v), "unit": "reads/s", "cores": cs.threads, "kind": "port",
+                            "sample": "per step: " + cs.describe(total_n // max(1, args.steps),
+                                                                 total_s / max(1, args.steps))},
+           "e2e": {"value": r4(v), "unit": "reads/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
 
-def seed_modes(P, nr: int, steps: int):
-    """Plain backward search (mode 0), interval scan with the k-mer table (1) and with the learned
-    index (2) on the same index: search reads/s (whole pq_overlaps, CSR included), kernel time and
-    probes per read of each, plus the learned model's build figures."""
+def timed_mode(P, nr: int, steps: int, run, stream, device):
+    """Warm-up, then `steps` timed runs of one search configuration: search ms (CUDA events
+    around the whole call), kernel ms, probes and algorithmic bytes per read, the graph."""
+    import torch
+    run()
+    ms, kern = [], []
+    for _ in range(steps):
+        torch.cuda.synchronize(device)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        run()
+        e1.record(stream)
+        torch.cuda.synchronize(device)
+        ms.append(e0.elapsed_time(e1))
+        kern.append(P.kernel_stats()[0])
+    g = P.graph()
+    sec, outb = P.search_traffic()
+    return {"ms": statistics.median(ms), "kernel_ms": statistics.median(kern), "graph": g,
+            "probes_per_read": g.probes / max(nr, 1), "bytes": 32.0 * sec + outb}
+
+
+def modes_block(P, nr: int, steps: int, stream, device, peak: float, plain_ref):
+    """The reference's method (mode 0), learned windows (mode 2) and learned windows through the
+    queued search with graph replay, each on the same index, each with its edges compared with
+    the default mode's (which the caller has checked against its own search)."""
+    import pasqual_gb300 as pq
     out = {}
-    ref = None
+    ref_dest, ref_off = plain_ref
     P.learned_build(0, 400)
     P.learned_build(1, 400)
-    for name, mode in (("plain", 0), ("scan", 1), ("learned", 2)):
+    for name, mode, batched in (("plain", 0, False), ("learned", 2, False), ("learned_batched", 2, True)):
         P.set_seed_mode(mode)
-        P.overlaps()
-        search, kern = [], []
-        for _ in range(steps):
-            P.overlaps()
-            search.append(P.stage_ms()[2])
-            kern.append(P.kernel_stats()[0])
-        g = P.graph()
-        same = ref is None or (np.array_equal(g.dest, ref[0]) and np.array_equal(g.edge_off, ref[1]))
-        if ref is None:
-            ref = (g.dest.copy(), g.edge_off.copy())
-        out[name] = {"reads_per_s": nr / (statistics.median(search) * 1e-3),
-                     "search_ms": statistics.median(search), "kernel_ms": statistics.median(kern),
-                     "probes_per_read": g.probes / max(nr, 1), "edges_identical_to_plain": bool(same)}
+        if batched:
+            pq.autotune_batched([P], graph=True)
+            r = timed_mode(P, nr, steps, lambda: pq.overlaps_batched([P], graph=True), stream, device)
+        else:
+            r = timed_mode(P, nr, steps, P.overlaps, stream, device)
+        g = r["graph"]
+        same = bool(np.array_equal(g.dest, ref_dest) and np.array_equal(g.edge_off, ref_off))
+        out[name] = {"reads_per_s": r4(nr / (r["ms"] * 1e-3)), "ms": r4(r["ms"]),
+                     "kernel_ms": r4(r["kernel_ms"]), "probes_per_read": r4(r["probes_per_read"]),
+                     "bytes_per_read": r4(r["bytes"] / max(nr, 1)),
+                     "frac": r4(r["bytes"] / (r["kernel_ms"] * 1e-3) / 1e9 / peak),
+                     "edges_equal": same}
     lx = [P.learned_info(d) for d in (0, 1)]
     out["learned_model"] = {
-        "segments": lx[0]["segments"], "hidden": lx[0]["hidden"], "train_steps": lx[0]["steps"],
-        "distinct_keys": [x["num_keys"] for x in lx],
-        "build_ms": sum(x["keys_ms"] + x["train_ms"] + x["eval_ms"] for x in lx),
-        "train_ms": sum(x["train_ms"] for x in lx),
-        "mean_window_rows": [x["mean_window"] for x in lx],
-        "mean_window_rows_root_only": [x["mean_window_root"] for x in lx],
-        "window_misses": lx[0]["misses"], "window_queries": lx[0]["queries"]}
-    out["learned_vs_plain"] = out["learned"]["reads_per_s"] / out["plain"]["reads_per_s"]
-    out["scan_vs_plain"] = out["scan"]["reads_per_s"] / out["plain"]["reads_per_s"]
+        "train_ms": r4(sum(x["train_ms"] for x in lx)),
+        "build_ms": r4(sum(x["keys_ms"] + x["train_ms"] + x["eval_ms"] for x in lx)),
+        "window_rows": r4(statistics.mean(x["mean_window"] for x in lx)),
+        "window_rows_root": r4(statistics.mean(x["mean_window_root"] for x in lx)),
+        "misses": lx[0]["misses"]}
+    st = P.batch_stats()
+    out["learned_batched"]["plan"] = [st["ctas_per_sm"], st["groups_per_item"], st["edge_slots"]]
     P.set_seed_mode(1)
     return out
 
 
-def batched(scale: float, steps: int, device: int, stream):
-    """Queued search: several read sets (own L and t each) in one persistent kernel from a device
-    work queue, replayed from a CUDA graph with the autotuned plan, against one search launch per
-    read set."""
+def mixed_sets(scale: float, steps: int, device, stream):
+    """Several read sets of uneven read length and mixed t (100 Mbp genome scaled): one search
+    launch per set against the queued persistent search from a CUDA graph with the autotuned
+    plan, in seed mode 2; the edges must be each set's own."""
     import torch
     import pasqual_gb300 as pq
     from pasqual_gb300 import synth
     name = "100Mbp_L75-250_25x_batched"
     sets = synth.make_batches(name, scale=scale)
     ctxs = []
-    for rd, L, t in sets:
-        P = pq.Pasqual(32, device=device, stream=stream.cuda_stream)
-        P.set_reads(rd, t)
-        P.build_index()
-        ctxs.append(P)
-    total = sum(rd.shape[0] for rd, _, _ in sets)
+    try:
+        for rd, L, t in sets:
+            P = pq.Pasqual(32, device=device, stream=stream.cuda_stream)
+            P.set_reads(rd, t)
+            P.set_seed_mode(2)
+            P.build_index()
+            ctxs.append(P)
+        total = sum(rd.shape[0] for rd, _, _ in sets)
 
-    def timed(fn):
-        fn()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize(device)
-        e0.record(stream)
-        for _ in range(steps):
+        def timed(fn):
             fn()
-        e1.record(stream)
-        torch.cuda.synchronize(device)
-        return e0.elapsed_time(e1) / steps
+            torch.cuda.synchronize(device)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(steps):
+                fn()
+            e1.record(stream)
+            torch.cuda.synchronize(device)
+            return e0.elapsed_time(e1) / steps
 
-    seq_ms = timed(lambda: [P.overlaps() for P in ctxs])
-    ref = [(P.graph().dest.copy()) for P in ctxs]
-    tune_ms = pq.autotune_batched(ctxs, graph=True)
-    q_ms = timed(lambda: pq.overlaps_batched(ctxs, graph=True))
-    same = all(np.array_equal(P.graph().dest, r) for P, r in zip(ctxs, ref))
-    st = ctxs[0].batch_stats()
-    for P in ctxs:
-        P.close()
-    return {"workload": name, "genome_scale": scale,
-            "read_sets": [{"reads": int(rd.shape[0]), "read_len": L, "t": t} for rd, L, t in sets],
-            "reads": int(total), "sequential_reads_per_s": total / (seq_ms * 1e-3),
-            "queued_graph_reads_per_s": total / (q_ms * 1e-3), "queued_vs_sequential": seq_ms / q_ms,
-            "queued_kernel_ms": st["kernel_ms"], "autotuned_kernel_ms": tune_ms,
-            "plan": {k: st[k] for k in ("ctas_per_sm", "groups_per_item", "edge_slots")},
-            "graph": bool(st["graph_used"]), "edges_identical_to_sequential": bool(same)}
+        seq_ms = timed(lambda: [P.overlaps() for P in ctxs])
+        ref = [P.graph().dest.copy() for P in ctxs]
+        pq.autotune_batched(ctxs, graph=True)
+        q_ms = timed(lambda: pq.overlaps_batched(ctxs, graph=True))
+        same = all(np.array_equal(P.graph().dest, r) for P, r in zip(ctxs, ref))
+        return {"scale": scale, "sets": len(sets),
+                "L": [L for _, L, _ in sets], "t": [t for _, _, t in sets], "reads": int(total),
+                "seq_reads_per_s": r4(total / (seq_ms * 1e-3)),
+                "queued_reads_per_s": r4(total / (q_ms * 1e-3)), "queued_vs_seq": r4(seq_ms / q_ms),
+                "edges_equal": bool(same)}
+    finally:
+        for P in ctxs:
+            P.close()
 
 
 def run_ours(args):
     import torch
     import pasqual_gb300 as pq
+    from pasqual_gb300 import synth
 
     rank, world, local = dist_env()
     if world > 1:
@@ -324,18 +405,13 @@ def run_ours(args):
     nr = rd.shape[0]
     n = nr * L
     width = 32 if n < (1 << 32) else 64          # the reference's U32/U64 split by index size
-    from pasqual_gb300 import synth
     width = max(width, synth.WORKLOADS[args.workload].get("index", 32))
     stream = torch.cuda.Stream(device=dev)
     P = pq.Pasqual(width, device=local, stream=stream.cuda_stream)
+    peak, peak_kind = measured_peak_hbm()
+    detail = {}
 
-    def barrier():
-        rank_barrier()
-
-    def max_over_ranks(x: float) -> float:
-        return rank_max(x, dev)
-
-    # ---- index build (setup) and suffix-sort throughput
+    # ---- index build (setup) and suffix-sort throughput (suffix arrays only, both directions)
     P.set_reads(rd, t)
     P.build_index()                       # warm-up build
     sort_ms = []
@@ -352,14 +428,14 @@ def run_ours(args):
     P.build_index()                       # index for the search; sort scratch given back
     sort_ms_med = statistics.median(sort_ms)
 
-    # ---- overlap search: warm-up, then K timed steps (clock sampling runs through both)
+    # ---- overlap search in the default mode: warm-up, then K timed steps (clocks sampled)
     clocks = Clocks(local)
     clocks.start()
     for _ in range(args.warmup):
         P.overlaps()
     _, l0 = P.kernel_stats()
     kern_ms = []
-    barrier()
+    rank_barrier()
     torch.cuda.synchronize(dev)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -369,20 +445,23 @@ def run_ours(args):
         kern_ms.append(P.kernel_stats()[0])
     e1.record(stream)
     torch.cuda.synchronize(dev)
-    barrier()
+    rank_barrier()
     ck = clocks.stop()
     _, l1 = P.kernel_stats()
-    step_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
+    step_ms = rank_max(e0.elapsed_time(e1) / args.steps, dev)
     g = P.graph()
-    probes = g.probes
-    wide = g.wide_reads
-    ne = len(g.dest)
+    sec, outb = P.search_traffic()
+    ref_graph = (g.dest.copy(), g.edge_off.copy())
+    kms = statistics.median(kern_ms)
+    alg_bytes = 32.0 * sec + outb
+    achieved = alg_bytes / (kms * 1e-3) / 1e9
+    dram_per_read = profile_figure("k_search_lean_250Mbp_L100.md", "dram_bytes_per_read")
 
     # ---- end to end through the public API with host buffers
     pinned = torch.empty((nr, L), dtype=torch.uint8, pin_memory=True)
     pinned.numpy()[:] = rd
-    e2e_ms = []
-    parts = []
+    del rd
+    e2e_ms, parts = [], []
     h2d = nr * L
     d2h = 0
     gg = None                              # host output arrays, reused from step to step
@@ -396,7 +475,6 @@ def run_ours(args):
         P.overlaps()
         t3 = time.perf_counter()
         gg = P.graph(out=gg)
-        t3g = time.perf_counter()
         if s == 0:                         # page-locked host arrays of the graph's sizes, reused
             gg = pq.Graph(**{f: torch.empty(max(getattr(gg, f).nbytes, 1), dtype=torch.uint8, pin_memory=True)
                              .numpy()[:getattr(gg, f).nbytes].view(getattr(gg, f).dtype)
@@ -409,60 +487,67 @@ def run_ours(args):
         if s > 0:                          # first pass is a warm-up
             e2e_ms.append((t4 - t0) * 1e3)
             sm, fm, _ = P.stage_ms()
-            parts.append({"set_reads_ms": (t1 - t0) * 1e3, "build_index_ms": (t2 - t1) * 1e3,
-                          "sort_ms": sm, "fm_ms": fm, "search_ms": (t3 - t2) * 1e3,
-                          "graph_d2h_ms": (t4 - t3) * 1e3, "graph_call_ms": (t3g - t3) * 1e3})
-    e2e_ms_med = max_over_ranks(statistics.median(e2e_ms)) if e2e_ms else None
+            parts.append({"set_reads": r4((t1 - t0) * 1e3), "build_index": r4((t2 - t1) * 1e3),
+                          "sort": r4(sm), "fm": r4(fm), "search": r4((t3 - t2) * 1e3),
+                          "d2h": r4((t4 - t3) * 1e3)})
+    e2e_ms_med = rank_max(statistics.median(e2e_ms), dev) if e2e_ms else None
+    del pinned
 
     if rank != 0:
+        P.close()
         return
-    peak, peak_kind = measured_peak_hbm()
-    kms = statistics.median(kern_ms)
     cb = None
     if world == 1 and not args.no_cpu_baseline:
         cb = cpu_baseline(args.workload, args.cpu_scale, args.cpu_seconds)
-    # Algorithmic bytes: 32 B for every rank probe the reference's method takes on this workload
-    # shape (counted by the C restatement on the CPU sample, or the figure recorded beside the ncu
-    # summary), whatever the GPU kernels skip.
-    oracle_ppr = cb["probes_per_read"] if cb else profile_figure("oracle_probes_per_read")
-    alg_bytes = 32.0 * oracle_ppr * nr if oracle_ppr else 32.0 * probes
-    achieved = alg_bytes / (kms * 1e-3) / 1e9
-    tpr = profile_figure("dram_bytes_per_read")
+    ref_ppr = cb["probes_per_read"] if cb else profile_figure("k_search_lean_250Mbp_L100.md",
+                                                               "reference_probes_per_read")
     out = {
-        "metric": METRIC, "value": replica_throughput(nr, world, step_ms), "unit": "reads/s",
-        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
+        "metric": METRIC, "value": r4(replica_throughput(nr, world, step_ms)), "unit": "reads/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": r4(step_ms),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "int%d-index" % width, "data": "synthetic",
-        "config": {"workload": args.workload, "genome_scale": args.scale, "reads": nr,
-                   "read_len": L, "t": t, "index": "U%d" % width, "suffixes_per_index": n,
-                   "edges": ne, "wide_tier_reads": wide, "seed_k": min(12, t),
-                   "l2": "inputs larger than L2 (two FM-indexes %.2f GB + reads %.2f GB)"
-                         % (2 * (n // 64 + 1) * 32 / 1e9, n / 1e9),
-                   "parallelism": "replica per GPU" if world > 1 else "single GPU"},
-        "sort": {"value": 2 * n / (sort_ms_med * 1e-3) / 1e6, "unit": "Msuffix/s",
-                 "ms_fw_plus_bw": sort_ms_med},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_kind": peak_kind,
-                     "kernel": "k_search_lean (+ k_search_fast over handed-over reads)",
-                     "algorithmic_bytes_per_launch": alg_bytes,
-                     "reference_probes_per_read": oracle_ppr,
-                     "probes_per_read": probes / max(nr, 1), "kernel_ms": kms,
-                     "traffic": (tpr * nr) if tpr else None},
+        "config": workload_config(args.workload),
         "gpu_launches": int(l1 - l0),
-        "e2e": ({"value": replica_throughput(nr, world, e2e_ms_med), "unit": "reads/s",
-                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                 "ms_per_step": e2e_ms_med, "parts_last_step": parts[-1]} if e2e_ms_med else None),
+        "roofline": {"bound": "hbm", "achieved": r4(achieved), "peak": peak, "unit": "GB/s",
+                     "frac": r4(achieved / peak), "peak_kind": peak_kind,
+                     "kernel": "k_search_lean", "kernel_ms": r4(kms),
+                     "bytes_per_read": r4(alg_bytes / nr),
+                     "traffic": r4(dram_per_read * nr) if dram_per_read else None,
+                     "reference_probes_per_read": r4(ref_ppr), "probes_per_read": r4(g.probes / nr)},
+        "e2e": ({"value": r4(replica_throughput(nr, world, e2e_ms_med)), "unit": "reads/s",
+                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": r4(e2e_ms_med),
+                 "parts_ms": parts[-1]} if e2e_ms_med else None),
     }
     if ck:
         out["clocks"] = ck
-    if not args.no_modes:
-        out["seed_modes"] = seed_modes(P, nr, max(1, min(args.steps, 3)))
-    if args.batched_scale > 0:
-        out["batched"] = batched(args.batched_scale, max(1, min(args.steps, 3)), local, stream)
     if cb:
-        out["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
-    print(json.dumps(out), flush=True)
+        out["cpu_baseline"] = {k: (r4(cb[k]) if k == "value" else cb[k])
+                               for k in ("value", "unit", "cores", "kind", "sample")}
+    detail["reads"] = nr
+    detail["suffixes_per_index"] = n
+    detail["edges"] = len(g.dest)
+    detail["wide_tier_reads"] = g.wide_reads
+    if not args.no_modes:
+        m = modes_block(P, nr, max(1, min(args.steps, 3)), stream, dev, peak, ref_graph)
+        detail["modes"] = m
     P.close()
+    if args.batched_scale > 0:
+        detail["mixed_sets"] = mixed_sets(args.batched_scale, max(1, min(args.steps, 3)), local, stream)
+    if args.detail:
+        with open(args.detail, "w") as f:
+            json.dump({"line": out, "detail": detail}, f, indent=1)
+    # the figures read most often go last: a reader that keeps only the end of the line sees them
+    out["reads"] = nr
+    out["modes"] = detail.get("modes")
+    out["mixed_sets"] = detail.get("mixed_sets")
+    out["sort_msuffix_per_s"] = r4(2 * n / (sort_ms_med * 1e-3) / 1e6)
+    if "modes" in detail:
+        mo = detail["modes"]
+        out["plain_reads_per_s"] = mo["plain"]["reads_per_s"]
+        out["learned_batched_reads_per_s"] = mo["learned_batched"]["reads_per_s"]
+        out["learned_batched_vs_plain"] = r4(mo["learned_batched"]["reads_per_s"] / mo["plain"]["reads_per_s"])
+        out["edges_equal_all_modes"] = all(mo[k]["edges_equal"] for k in ("plain", "learned", "learned_batched"))
+    print(json.dumps(out, separators=(",", ":")), flush=True)
 
 
 def main():

@@ -142,6 +142,15 @@ PQ_API int pq_overlaps (pq_ctx * ctx);
 PQ_API int pq_get_graph_sizes (pq_ctx * ctx, uint64_t * num_edges, uint64_t * probes,
                         uint64_t * wide_reads);
 
+/* Memory traffic of the last pq_overlaps, as the method in use defines it: load_sectors = the
+ * 32-byte sectors of index data its kernels loaded (occurrence blocks, k-mer table, suffix-array
+ * and inverse-SA entries, packed-text words, reads_index entries, read bytes; every load counted
+ * where it is issued, so a sector loaded twice counts twice; tables that stay in L2 -- superblock
+ * counts, learned models -- and the kernels' own scratch are not counted); store_bytes = the
+ * bytes of per-read results and edges the search kernels write.  32 * load_sectors + store_bytes
+ * is the search's algorithmic traffic. */
+PQ_API int pq_get_search_traffic (pq_ctx * ctx, uint64_t * load_sectors, uint64_t * store_bytes);
+
 /* Copy the last pq_overlaps result to host arrays.  Per read: num_B, num_F (node_t.num_B/F),
  * olp_B, olp_F (overlaps_B/F of src/string_graph.c:807-808), edge_off[num_reads+1].  Per edge,
  * B edges then F edges of each read in the reference's DFS order: dest, overlap length, type

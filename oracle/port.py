@@ -32,7 +32,7 @@ def build(ref: bool = False) -> None:
     """Compile the restatement (and, when asked and available, the reference)."""
     subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
     if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + REFERENCE], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "stage", "REF=" + REFERENCE], check=True)
 
 
 def np_idx(width: int):

@@ -35,7 +35,7 @@ EXPORTS = ["pq_idx_bytes", "pq_create", "pq_destroy", "pq_last_error", "pq_set_r
            "pq_suffix_sort_static", "pq_learned_build", "pq_learned_get_info", "pq_learned_export",
            "pq_learned_predict", "pq_learned_keys", "pq_mlp_forward", "pq_mlp_backward",
            "pq_overlaps_batched", "pq_set_batch_plan", "pq_get_batch_stats", "pq_autotune_batched",
-           "pq_set_sort_chunk"]
+           "pq_set_sort_chunk", "pq_get_search_traffic"]
 
 
 # The reference's own entry points served by the same library (include/pasqual_gb300_dropin.h).
@@ -100,6 +100,7 @@ def load_library(width: int = 32) -> ct.CDLL:
         "pq_get_batch_stats": (c_int, [vp, vp, vp, vp, vp, vp]),
         "pq_autotune_batched": (c_int, [vp, c_int, c_int, vp]),
         "pq_set_sort_chunk": (c_int, [vp, ct.c_uint64]),
+        "pq_get_search_traffic": (c_int, [vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -340,6 +341,14 @@ class Pasqual:
     def construct_string_graph(self) -> Graph:
         self.overlaps()
         return self.graph()
+
+    def search_traffic(self):
+        """(32-byte sectors of index data the last overlap search loaded, bytes of results it
+        wrote): the search's algorithmic traffic is 32 * sectors + bytes."""
+        sec, out = ct.c_uint64(), ct.c_uint64()
+        self._ck(self.lib.pq_get_search_traffic(self.h, ct.byref(sec), ct.byref(out)),
+                 "pq_get_search_traffic")
+        return sec.value, out.value
 
     def kernel_stats(self):
         """(fast search kernel ms of the last overlap search, kernels launched so far)."""

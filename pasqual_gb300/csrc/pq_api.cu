@@ -107,7 +107,7 @@ struct pq_ctx {
     DevBuf off, g_dest, g_len, g_type, g_trans, asm_tmp, wide, warp_scratch, defer, heavy_scratch, ovf2;
     uint64_t heavy_reads = 0;
     bool graph_ok = false;
-    uint64_t num_edges = 0, probes = 0, wide_reads = 0;
+    uint64_t num_edges = 0, probes = 0, sectors = 0, wide_reads = 0;
 };
 
 static int fail(pq_ctx* c, int code, const std::string& msg) {
@@ -551,7 +551,8 @@ static int search_prepare(pq_ctx* ctx, pq::SearchArgs& A, pq::SearchOut& O) {
     // sorted continuations wherever those fit in 256 bases
     A.sorted_reduce = (ctx->seed_mode != 0 && ctx->L - ctx->t <= 256) ? 1 : 0;
 
-    unsigned long long* ctr = ctx->ctrs.as<unsigned long long>();   // [0] e_count [1] probes [2] ovf(u32)
+    // [0] e_count [1] probes [2] ovf (u32) [3] learned misses [4] defer (u32) [5] heavy ovf [6] sectors
+    unsigned long long* ctr = ctx->ctrs.as<unsigned long long>();
     O.num_B = ctx->nB.as<uint16_t>();
     O.num_F = ctx->nF.as<uint16_t>();
     O.olp_B = ctx->oB.as<int32_t>();
@@ -567,6 +568,7 @@ static int search_prepare(pq_ctx* ctx, pq::SearchArgs& A, pq::SearchOut& O) {
     O.ovf_list = ctx->ovf_list.as<idx_t>();
     O.ovf_count = reinterpret_cast<unsigned int*>(ctr + 2);
     O.probes = ctr + 1;
+    O.sectors = ctr + 6;
     A.lx_misses = ctr + 3;
     CK(ctx->defer.ensure((nr + 1) * sizeof(idx_t)));
     A.defer = ctx->defer.as<idx_t>();
@@ -697,12 +699,15 @@ static int search_finish(pq_ctx* ctx, pq::SearchArgs& A, pq::SearchOut& O) {
                            ctx->g_len.as<uint16_t>(), ctx->g_type.as<uint8_t>(), ctx->g_trans.as<int32_t>(), ctx->st));
     CK(cudaEventRecord(ctx->ev1, ctx->st));
     CK(cudaMemcpyAsync(hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, ctx->st));
+    unsigned long long sec = 0;
+    CK(cudaMemcpyAsync(&sec, ctr + 6, sizeof sec, cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaEventSynchronize(ctx->ev1));
     CK(cudaStreamSynchronize(ctx->st));
     cudaEventElapsedTime(&ctx->ms_search, ctx->ev0, ctx->ev1);
     cudaEventElapsedTime(&ctx->ms_fast, ctx->evk0, ctx->evk1);
     ctx->num_edges = total;
     ctx->probes = hc[1];
+    ctx->sectors = sec;
     ctx->graph_ok = true;
     return PQ_OK;
 }
@@ -744,6 +749,16 @@ int pq_get_graph_sizes(pq_ctx* ctx, uint64_t* num_edges, uint64_t* probes, uint6
     if (num_edges) *num_edges = ctx->num_edges;
     if (probes) *probes = ctx->probes;
     if (wide_reads) *wide_reads = ctx->wide_reads;
+    return PQ_OK;
+}
+
+int pq_get_search_traffic(pq_ctx* ctx, uint64_t* load_sectors, uint64_t* store_bytes) {
+    if (!ctx) return PQ_ERR_ARG;
+    if (!ctx->graph_ok) return fail(ctx, PQ_ERR_STATE, "pq_overlaps first");
+    if (load_sectors) *load_sectors = ctx->sectors;
+    // per read: num_B, num_F (2 + 2), olp_B, olp_F (4 + 4), edge-pool offset (8), status (1);
+    // per edge: dest, trans (4), length (2), type (1)
+    if (store_bytes) *store_bytes = uint64_t(ctx->num_reads) * 21 + ctx->num_edges * (sizeof(idx_t) + 7);
     return PQ_OK;
 }
 

@@ -42,6 +42,7 @@ struct SearchOut {
     idx_t* ovf_list;               // reads handed to the wide kernel
     unsigned int* ovf_count;
     unsigned long long* probes;    // total rank probes (one 32-byte sector each)
+    unsigned long long* sectors;   // total 32-byte sectors of index data loaded (see Tally)
 };
 
 struct SearchArgs {

@@ -46,6 +46,31 @@ struct EdgeRec {
     uint8_t type;
 };
 
+// Per-thread counters of a search: rank probes (one occurrence block each, the unit of the
+// reference's OCCx/search_* calls) and the 32-byte sectors of every global load of index data the
+// method issues -- occurrence blocks, k-mer table entries, suffix-array and inverse-SA entries,
+// packed-text words, reads_index entries and read bytes.  Tables that stay resident in L2 (the
+// superblock counts, learned models) and the search's own scratch are not counted.  `+= n` is n
+// rank probes, one sector each (an occurrence block is one aligned sector).
+struct Tally {
+    uint32_t probes{0}, sectors{0};
+    __device__ __forceinline__ Tally& operator+=(uint32_t n) {
+        probes += n;
+        sectors += n;
+        return *this;
+    }
+    __device__ __forceinline__ void add(uint32_t p, uint32_t s) {
+        probes += p;
+        sectors += s;
+    }
+};
+
+// 32-byte sectors spanned by `bytes` bytes at p
+__device__ __forceinline__ uint32_t sectors_of(const void* p, size_t bytes) {
+    const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+    return uint32_t(((a + bytes - 1) >> 5) - (a >> 5) + 1);
+}
+
 // ------------------------------------------------------------------------------ rank primitives
 
 __device__ __forceinline__ void ld_block(const OccBlock* p, uint64_t& lo, uint64_t& hi, uint64_t& dol,
@@ -116,7 +141,7 @@ __device__ __forceinline__ idx_t rank_dollar(const FmView& f, idx_t pos) {
 }
 
 // search_1: LF-map the closed interval [l, u] by base c
-__device__ __forceinline__ void lf_step(const FmView& f, int c, idx_t& l, idx_t& u, uint32_t& probes) {
+__device__ __forceinline__ void lf_step(const FmView& f, int c, idx_t& l, idx_t& u, Tally& probes) {
     idx_t ol = rank_c(f, c, l);
     idx_t ou = rank_c(f, c, u + 1);
     probes += 2;
@@ -127,7 +152,7 @@ __device__ __forceinline__ void lf_step(const FmView& f, int c, idx_t& l, idx_t&
 // search_2: step on this index by c, keep the other index's interval [ll, uu] in sync.
 // #symbols < c in [l, u] ($ included) = (pos - sum_{k>=c} rank_k) differences; fixes cancel.
 __device__ __forceinline__ void bi_step(const FmView& f, int c, idx_t& l, idx_t& u, idx_t& ll, idx_t& uu,
-                                        uint32_t& probes) {
+                                        Tally& probes) {
     idx_t vl = l, vu = u + 1;
     idx_t rl[4], ru[4];
     rank_all(f, vl, rl);
@@ -147,7 +172,7 @@ __device__ __forceinline__ void bi_step(const FmView& f, int c, idx_t& l, idx_t&
 }
 
 // search_3: (#$ in [l, u]) - 1, wrapping to all-ones at zero
-__device__ __forceinline__ idx_t dollars_m1(const FmView& f, idx_t l, idx_t u, uint32_t& probes) {
+__device__ __forceinline__ idx_t dollars_m1(const FmView& f, idx_t l, idx_t u, Tally& probes) {
     probes += 2;
     return rank_dollar(f, u + 1) - rank_dollar(f, l) - 1;
 }
@@ -176,7 +201,7 @@ __device__ __forceinline__ int pattern_at(const ReadView& rd, int L, int kind, i
 
 // exact SA interval of pattern pat(hi) pat(hi-1) ... pat(lo) (text order) from the k-mer table
 __device__ __forceinline__ void kmer_seed(const FmView& f, const ReadView& rd, int L, int kind, int first,
-                                          int last, int step, idx_t& l, idx_t& u, uint32_t& probes) {
+                                          int last, int step, idx_t& l, idx_t& u, Tally& probes) {
     uint32_t code = 0;
     for (int j = first;; j += step) {
         code = (code << 2) | uint32_t(pattern_at(rd, L, kind, j) - 1);
@@ -184,7 +209,7 @@ __device__ __forceinline__ void kmer_seed(const FmView& f, const ReadView& rd, i
     }
     l = __ldg(f.kstart + code);
     u = __ldg(f.kend + code);
-    probes += 1;
+    probes.add(1, 2);
 }
 
 struct ReadResult {
@@ -267,13 +292,14 @@ __device__ __forceinline__ uint64_t top_mask(int nbases) {      // 1 <= nbases <
 // the walked index at self * L + L - t for a strict kind, and the complement of the other index's
 // text there for FF and BB.
 __device__ __forceinline__ void pattern_words(const FmView* fm, int L, int t, int kind, idx_t self,
-                                              uint64_t (&P)[kScanWords]) {
+                                              uint64_t (&P)[kScanWords], Tally& probes) {
     const bool strict = kind == PQ_FB || kind == PQ_BF;
     const uint64_t* pk = fm[strict ? walked_index(kind) : 1 - walked_index(kind)].pk;
     const size_t pos = size_t(self) * L + size_t(L - t);
     const uint64_t flip = strict ? 0 : ~uint64_t(0);
     #pragma unroll
     for (int w = 0; w < kScanWords; ++w) P[w] = text_window(pk, pos + 32 * w) ^ flip;
+    probes.add(0, sectors_of(pk + (pos >> 5), 8 * (kScanWords + 1)));
 }
 
 // -1 / 0 / +1: the suffix at text position p (m bases to end-of-read) is below / starts with /
@@ -295,12 +321,17 @@ __device__ __forceinline__ int cmp_row(const uint64_t* __restrict__ pk, idx_t p,
     return m < t ? -1 : 0;
 }
 
+// sectors cmp_row loads for a suffix at text position p
+__device__ __forceinline__ uint32_t cmp_sectors(const uint64_t* pk, idx_t p) {
+    return sectors_of(pk + (size_t(p) >> 5), 24);
+}
+
 // Rows [first, end) of each chain's index that start with its pattern, searched within
 // [lo, hi): lower and upper bounds of both chains advance together (four independent searches).
 __device__ __forceinline__ void sa_bounds2(const FmView* f0, const FmView* f1, int L, const uint64_t (&P0)[kScanWords],
                                            const uint64_t (&P1)[kScanWords], int t, const idx_t (&lo)[2],
                                            const idx_t (&hi)[2], idx_t (&first)[2], idx_t (&end)[2],
-                                           uint32_t& probes) {
+                                           Tally& probes) {
     idx_t a0[2] = {lo[0], lo[1]}, a1[2] = {hi[0], hi[1]}, b0[2] = {lo[0], lo[1]}, b1[2] = {hi[0], hi[1]};
     const FmView* fq[2] = {f0, f1};
     while (a0[0] < a1[0] || b0[0] < b1[0] || a0[1] < a1[1] || b0[1] < b1[1]) {
@@ -318,14 +349,14 @@ __device__ __forceinline__ void sa_bounds2(const FmView* f0, const FmView* f1, i
                 const int c = cmp_row(fq[q]->pk, pa[q], L - int(pa[q] % idx_t(L)), P, t);
                 if (c < 0) a0[q] = ma + 1;
                 else a1[q] = ma;
-                probes += 2;
+                probes.add(2, 1 + cmp_sectors(fq[q]->pk, pa[q]));
             }
             if (b0[q] < b1[q]) {
                 const idx_t mb = b0[q] + (b1[q] - b0[q]) / 2;
                 const int c = cmp_row(fq[q]->pk, pb[q], L - int(pb[q] % idx_t(L)), P, t);
                 if (c <= 0) b0[q] = mb + 1;
                 else b1[q] = mb;
-                probes += 2;
+                probes.add(2, 1 + cmp_sectors(fq[q]->pk, pb[q]));
             }
         }
     }
@@ -336,16 +367,23 @@ __device__ __forceinline__ void sa_bounds2(const FmView* f0, const FmView* f1, i
 // `o` bases of the walked index's text at ra equal those of the pattern source at rs.  The
 // pattern P_d (d = t + o) of a strict kind is the read's own text in the walked index at
 // self * L + L - d; of FF and BB it is the complement of the other index's text there.
+// `sec` counts the sectors loaded from the walked text (the pattern source is the read's own text,
+// counted once by pattern_words).
 __device__ __forceinline__ bool prefix_matches(const uint64_t* __restrict__ pka, size_t ra,
-                                               const uint64_t* __restrict__ pks, size_t rs, int o, bool cmpl) {
-    for (int c = 0; c < o; c += 32) {
+                                               const uint64_t* __restrict__ pks, size_t rs, int o, bool cmpl,
+                                               uint32_t& sec) {
+    bool ok = true;
+    int c = 0;
+    for (; c < o && ok; c += 32) {
         const int m = o - c < 32 ? o - c : 32;
         const uint64_t x = text_window(pka, ra + c);
         uint64_t y = text_window(pks, rs + c);
         if (cmpl) y = ~y;
-        if ((x ^ y) & top_mask(m)) return false;
+        ok = ((x ^ y) & top_mask(m)) == 0;
     }
-    return true;
+    // windows at ra, ra + 32, ..., ra + c - 32: words (ra >> 5) .. ((ra + c - 32) >> 5) + 1
+    if (c > 0) sec += sectors_of(pka + (ra >> 5), 8 * ((((ra + c - 32) >> 5) - (ra >> 5)) + 2));
+    return ok;
 }
 
 // Slots of the level-0 candidates of the two chains of one side: q * M + i.
@@ -387,12 +425,12 @@ struct SlotsStack {    // wide tier: the slot's candidate stack
 // holds more than kScanMax rows, and the caller walks instead.
 template <class Slots>
 __device__ __forceinline__ bool scan_pair(const SearchArgs& A, const FmView* fm, idx_t self, int k0, int k1,
-                                          int (&n)[2], int32_t& olp, uint32_t& probes, const Slots& slots) {
+                                          int (&n)[2], int32_t& olp, Tally& probes, const Slots& slots) {
     const int L = A.L, t = A.t, k = A.seed_k, M = L - t;
     const int tb = t < 32 * kScanWords ? t : 32 * kScanWords;    // bases bisected; the rest checked per row
     uint64_t P0[kScanWords], P1[kScanWords];
-    pattern_words(fm, L, t, k0, self, P0);
-    pattern_words(fm, L, t, k1, self, P1);
+    pattern_words(fm, L, t, k0, self, P0, probes);
+    pattern_words(fm, L, t, k1, self, P1, probes);
     const FmView* f0 = fm + walked_index(k0);
     const FmView* f1 = fm + walked_index(k1);
     idx_t lo[2], hi[2], first[2], end[2];
@@ -416,7 +454,7 @@ __device__ __forceinline__ bool scan_pair(const SearchArgs& A, const FmView* fm,
         hi[0] = __ldg(f0->kend + c0) + 1;
         lo[1] = __ldg(f1->kstart + c1);
         hi[1] = __ldg(f1->kend + c1) + 1;
-        probes += 2;
+        probes.add(2, 4);
         if (hi[0] < lo[0]) hi[0] = lo[0];
         if (hi[1] < lo[1]) hi[1] = lo[1];
     }
@@ -433,12 +471,12 @@ __device__ __forceinline__ bool scan_pair(const SearchArgs& A, const FmView* fm,
             if (first[q] == lo[q] && lo[q] > 0) {
                 const idx_t p = __ldg(fa.sa + lo[q] - 1);
                 ok = ok && cmp_row(fa.pk, p, L - int(p % idx_t(L)), P, tb) < 0;
-                probes += 2;
+                probes.add(2, 1 + cmp_sectors(fa.pk, p));
             }
             if (end[q] == hi[q] && hi[q] < n_rows) {
                 const idx_t p = __ldg(fa.sa + hi[q]);
                 ok = ok && cmp_row(fa.pk, p, L - int(p % idx_t(L)), P, tb) > 0;
-                probes += 2;
+                probes.add(2, 1 + cmp_sectors(fa.pk, p));
             }
         }
         if (!ok) {
@@ -460,9 +498,10 @@ __device__ __forceinline__ bool scan_pair(const SearchArgs& A, const FmView* fm,
             const idx_t p = __ldg(fa.sa + row);
             const idx_t rp = p / idx_t(L);
             const int o = int(p - rp * idx_t(L));
-            probes += 2;
-            if (o >= M || !prefix_matches(fa.pk, size_t(rp) * L, pks, src - o, o, cmpl)) continue;
-            if (t > tb && !prefix_matches(fa.pk, size_t(p) + tb, pks, src + tb, t - tb, cmpl)) continue;
+            probes.add(2, 1);
+            if (o >= M || !prefix_matches(fa.pk, size_t(rp) * L, pks, src - o, o, cmpl, probes.sectors)) continue;
+            if (t > tb && !prefix_matches(fa.pk, size_t(p) + tb, pks, src + tb, t - tb, cmpl, probes.sectors))
+                continue;
             const uint64_t bit = uint64_t(1) << (o & 63);
             const int hw = o >> 6;
             const uint64_t cur = hw == 0 ? mk0 : hw == 1 ? mk1 : hw == 2 ? mk2 : mk3;
@@ -514,7 +553,7 @@ __device__ __forceinline__ bool scan_pair(const SearchArgs& A, const FmView* fm,
 // `need_read()` makes rd valid (the walk reads the read's bases; the scan reads the packed text).
 template <class Slots, class NeedRead>
 __device__ __forceinline__ void chain_pair(const SearchArgs& A, const FmView* fm, const ReadView& rd, idx_t self,
-                                           int k0, int k1, int (&n)[2], int32_t& olp, uint32_t& probes,
+                                           int k0, int k1, int (&n)[2], int32_t& olp, Tally& probes,
                                            const Slots& slots, NeedRead need_read) {
     const int L = A.L, t = A.t, k = A.seed_k;
     n[0] = n[1] = 0;
@@ -575,7 +614,7 @@ __device__ __forceinline__ void chain_pair(const SearchArgs& A, const FmView* fm
 // One side's candidates into the thread's stack: kind k0 then k1, the reference's order.
 __device__ __forceinline__ int side_candidates(const SearchArgs& A, const FmView* fm, const ReadView& rd, idx_t self,
                                                int k0, int k1, Cand* stk, int cap, int& n_out, int32_t& olp,
-                                               uint32_t& probes) {
+                                               Tally& probes) {
     const int M = A.L - A.t;
     if (2 * M > cap) return OVF_STACK;
     int n[2];
@@ -595,7 +634,7 @@ __device__ __forceinline__ int cand_index(int type) { return (type == PQ_FB || t
 // finds it empty, so the sets are the reference's.
 __device__ __forceinline__ int reduce_side(const SearchArgs& A, const FmView* fm, idx_t self, Cand* stk, int cap,
                                            int n0, Frame* fr, int frcap, EdgeRec* eb, int ebcap, int& ne,
-                                           int& side_count, uint32_t& probes) {
+                                           int& side_count, Tally& probes) {
     const int L = A.L;
     int level = 0;
     fr[0].pos = 0;
@@ -618,6 +657,7 @@ __device__ __forceinline__ int reduce_side(const SearchArgs& A, const FmView* fm
                     idx_t uuu = fo.Cf[0] + rank_dollar(fo, c.uu + 1) - 1;
                     probes += 2;
                     if (lll <= uuu) {
+                        probes.add(0, sectors_of(fo.reads_index + lll, size_t(uuu - lll + 1) * sizeof(idx_t)));
                         for (idx_t kk = lll; kk < uuu + 1; ++kk) {
                             idx_t r = __ldg(fo.reads_index + kk);
                             flag = true;
@@ -716,7 +756,7 @@ __device__ __forceinline__ int reduce_side(const SearchArgs& A, const FmView* fm
 
 __device__ __forceinline__ ReadResult search_read(const SearchArgs& A, const FmView* fm, idx_t self,
                                                   const ReadView& rd, Cand* stk, int cap, Frame* fr, int frcap,
-                                                  EdgeRec* eb, int ebcap, uint32_t& probes) {
+                                                  EdgeRec* eb, int ebcap, Tally& probes) {
     ReadResult R;
     R.status = OVF_NONE;
     R.nB = R.nF = 0;
@@ -740,8 +780,9 @@ __device__ __forceinline__ ReadResult search_read(const SearchArgs& A, const FmV
     return R;
 }
 
-__device__ __forceinline__ void load_read(const SearchArgs& A, idx_t r, uint32_t* w, int stride) {
+__device__ __forceinline__ void load_read(const SearchArgs& A, idx_t r, uint32_t* w, int stride, Tally& probes) {
     const uint8_t* src = A.reads + size_t(r) * A.L;
+    probes.add(0, sectors_of(src, size_t(A.L)));
     const int words = (A.L + 15) >> 4;
     for (int i = 0; i < words; ++i) {
         uint32_t v = 0;
@@ -785,11 +826,17 @@ __device__ __forceinline__ void publish(const SearchOut& O, idx_t r, const ReadR
     O.edge_src[r] = base;
 }
 
-__device__ __forceinline__ void add_probes(const SearchOut& O, uint32_t probes) {
-    unsigned long long v = probes;
+__device__ __forceinline__ void add_probes(const SearchOut& O, const Tally& t) {
+    unsigned long long v = t.probes, w = t.sectors;
     #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0 && v) atomicAdd(O.probes, v);
+    for (int o = 16; o > 0; o >>= 1) {
+        v += __shfl_down_sync(0xffffffffu, v, o);
+        w += __shfl_down_sync(0xffffffffu, w, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (v) atomicAdd(O.probes, v);
+        if (w) atomicAdd(O.sectors, w);
+    }
 }
 
 // ------------------------------------------------------------------------------ fast tier
@@ -924,20 +971,24 @@ __host__ __device__ constexpr int lam_words(int M) { return M <= 64 ? 2 : kLamWo
 
 // continuation of candidate r' at overlap d: L - d bases (at most 32 W) in ceil((L - d) / 32)
 // words, first base in the top bits, zero past the end; word w at out[w * plane]
+// (returns the 32-byte sectors of packed text it loaded)
 template <int W>
-__device__ __forceinline__ void continuation(const SearchArgs& A, int type, idx_t rp, int d, uint64_t* out,
-                                             size_t plane) {
+__device__ __forceinline__ uint32_t continuation(const SearchArgs& A, int type, idx_t rp, int d, uint64_t* out,
+                                                 size_t plane) {
     const int L = A.L, len = L - d;
     const bool fwd = cand_index(type) == 1;
     const uint64_t* pk = A.fm[fwd ? 0 : 1].pk;
     const size_t pos = size_t(rp) * L + size_t(d);
     const uint64_t flip = fwd ? 0 : ~uint64_t(0);
+    int nw = 0;
     #pragma unroll
     for (int w = 0; w < W; ++w) {
         const int left = len - 32 * w;
         if (left <= 0) break;
         out[w * plane] = (text_window(pk, pos + 32 * w) ^ flip) & top_mask(left < 32 ? left : 32);
+        nw = w + 1;
     }
+    return nw ? sectors_of(pk + (pos >> 5), 8 * ((((pos + 32 * (nw - 1)) >> 5) - (pos >> 5)) + 2)) : 0;
 }
 
 // the first n bases (1 <= n <= 32 W) of continuations a and b agree
@@ -973,7 +1024,7 @@ __device__ __forceinline__ int cmp_cont(const uint64_t* a, int la, const uint64_
 template <int W>
 __device__ __forceinline__ int reduce_sorted(const SearchArgs& A, const WarpScratch& S, idx_t self, int side,
                                              size_t cand, int na, int n0, size_t red, size_t eb, int& ne,
-                                             int& count, uint32_t& probes) {
+                                             int& count, Tally& probes) {
     const int L = A.L, M = L - A.t;
     const int first_kind = side ? PQ_FB : PQ_BF;
     int m = 0;
@@ -986,10 +1037,10 @@ __device__ __forceinline__ int reduce_sorted(const SearchArgs& A, const WarpScra
         for (idx_t row = ll; row <= uu; ++row) {
             const idx_t p = __ldg(fb.sa + row);
             const idx_t rp = p / idx_t(L);
-            continuation<W>(A, type, rp, d, S.r_k + red + m, S.r_plane);
+            const uint32_t sec = continuation<W>(A, type, rp, d, S.r_k + red + m, S.r_plane);
             S.r_id[red + m] = rp;
             S.r_meta[red + m] = mt;
-            probes += 2;
+            probes.add(2, 1 + sec);
             ++m;
         }
     }
@@ -1087,7 +1138,7 @@ __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A0, SearchOut
     const size_t mbase_w = gw * 32 * size_t(PMAX);            // emission bounds
     const size_t rbase_w = gw * 32 * size_t(kRedMax);          // sorted-reduction candidates
     TFrame* const frw = S.frames + gw * 32 * FRAMES;
-    uint32_t probes = 0;
+    Tally probes;
     int cur = -1;
     // reads of the current batch (or of the list of reads handed over by the lean tier)
     const size_t list_n = Q.read_list ? size_t(*Q.list_count) : 0;
@@ -1103,7 +1154,7 @@ __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A0, SearchOut
             gend = group + Q.groups_per_item;
             if (b != cur) {
                 if (cur >= 0) add_probes(O, probes);
-                probes = 0;
+                probes = Tally{};
                 __syncwarp();
                 load_batch(B, Q.batches + b, lane);
                 cur = b;
@@ -1123,7 +1174,7 @@ __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A0, SearchOut
         const idx_t self = idx_t(r);
         // ---- phase A
         if (have) {
-            load_read(A, idx_t(r), s_reads + threadIdx.x, blockDim.x);
+            load_read(A, idx_t(r), s_reads + threadIdx.x, blockDim.x, probes);
             ReadView rd{s_reads + threadIdx.x, int(blockDim.x)};
             const size_t cb = cbase_w + size_t(lane) * 4 * size_t(S.mstride);
             int nb[2], nf[2];
@@ -1300,6 +1351,7 @@ __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A0, SearchOut
                         const idx_t endk = uuu + 1;      // k < uuu + 1: no iteration when uuu + 1 wraps
                         const idx_t cnt = endk > lll ? endk - lll : 0;
                         const idx_t* rix = A.fm[cand_index(meta_type(hm))].reads_index;
+                        if (cnt > 0) probes.add(0, sectors_of(rix + lll, size_t(cnt) * sizeof(idx_t)));
                         for (idx_t k = 0; k < cnt; ++k) {
                             const idx_t rr = __ldg(rix + (lll + k));
                             if (rr == self) continue;
@@ -1452,7 +1504,7 @@ __global__ void __launch_bounds__(kLeanThreads, 8) k_search_lean(SearchArgs A0, 
     const size_t cb = tid * 4 * size_t(S.mstride);
     const size_t eb = tid * size_t(S.ebcap);
     const size_t red = tid * size_t(kRedMax);
-    uint32_t probes = 0;
+    Tally probes;
     int cur = -1;
     for (size_t iter = 0;; ++iter) {
         size_t group, gend;
@@ -1466,7 +1518,7 @@ __global__ void __launch_bounds__(kLeanThreads, 8) k_search_lean(SearchArgs A0, 
             gend = group + Q.groups_per_item;
             if (b != cur) {
                 if (cur >= 0) add_probes(O, probes);
-                probes = 0;
+                probes = Tally{};
                 __syncwarp();
                 load_batch(B, Q.batches + b, lane);
                 cur = b;
@@ -1484,7 +1536,7 @@ __global__ void __launch_bounds__(kLeanThreads, 8) k_search_lean(SearchArgs A0, 
             ReadView rd{s_reads + threadIdx.x, int(blockDim.x)};
             bool loaded = false;      // the read's bases are loaded only if a chain walks
             auto need_read = [&] {
-                if (!loaded) load_read(A, self, s_reads + threadIdx.x, blockDim.x);
+                if (!loaded) load_read(A, self, s_reads + threadIdx.x, blockDim.x, probes);
                 loaded = true;
             };
             int nb[2], nf[2];
@@ -1745,14 +1797,14 @@ __global__ void __launch_bounds__(64) k_search_wide(SearchArgs A, SearchOut O, c
     if (threadIdx.x < 2) s_fm[threadIdx.x] = A.fm[threadIdx.x];
     __syncthreads();
     const unsigned slot = blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t probes = 0;
+    Tally probes;
     if (slot < unsigned(W.slots)) {
         Cand* stk = reinterpret_cast<Cand*>(W.stack) + size_t(slot) * W.stack_cap;
         Frame* fr = reinterpret_cast<Frame*>(W.frames) + size_t(slot) * W.frame_cap;
         EdgeRec* eb = reinterpret_cast<EdgeRec*>(W.edges) + size_t(slot) * W.edge_cap;
         for (unsigned i = slot; i < count; i += unsigned(W.slots)) {
             idx_t r = list[i];
-            load_read(A, r, s_reads + threadIdx.x, blockDim.x);
+            load_read(A, r, s_reads + threadIdx.x, blockDim.x, probes);
             ReadView rd{s_reads + threadIdx.x, int(blockDim.x)};
             ReadResult R = search_read(A, s_fm, r, rd, stk, int(W.stack_cap), fr, int(W.frame_cap), eb,
                                        int(W.edge_cap), probes);
@@ -1781,7 +1833,8 @@ __global__ void __launch_bounds__(64) k_search_wide(SearchArgs A, SearchOut O, c
             O.edge_src[r] = base;
         }
     }
-    if (probes) atomicAdd(O.probes, (unsigned long long)probes);
+    if (probes.probes) atomicAdd(O.probes, (unsigned long long)probes.probes);
+    if (probes.sectors) atomicAdd(O.sectors, (unsigned long long)probes.sectors);
 }
 
 size_t wide_slot_bytes(int L) {

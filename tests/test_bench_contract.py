@@ -19,7 +19,7 @@ def test_reference_arm_prints_one_contract_line():
                 "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
         assert key in out, key
     assert out["impl"] == "reference" and out["unit"] == "reads/s" and out["value"] > 0
-    assert out["config"]["workload"] == "50Mbp_L100_30x_t63"
+    assert out["config"]["workload"] == "250Mbp_L100_20x_t55" and out["config"]["index"] == "U64"
     cb = out["cpu_baseline"]
     assert set(cb) >= {"value", "unit", "cores", "kind", "sample"} and cb["kind"] == "port"
     assert cb["value"] == out["value"] and cb["cores"] >= 1

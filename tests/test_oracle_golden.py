@@ -3,6 +3,7 @@
 Pins every array of the hot path: both suffix arrays (canonical single-thread order), both
 FM-indexes in the reference layout, and the per-read ordered edge lists with node fields.
 """
+import os
 import sys
 
 import numpy as np
@@ -103,3 +104,21 @@ def test_golden_generator_reproduces_fixture(tmp_path, name):
     z = np.load(os.path.join(GOLDEN, name + ".npz"))
     for k in z.files:
         assert np.array_equal(np.asarray(fresh[k]), z[k]), k
+
+
+def test_oracle_matches_reference_at_workload_size(tmp_path):
+    """The restatement at the full size of the 1 Mbp, 50 bp, 40x, t = 31 workload (800 K reads
+    generated, about 550 K kept by the library's import with the reference's Bloom filter):
+    both suffix arrays, both FM-indexes and every edge equal the reference's digests."""
+    from conftest import graph_digests_ok, large_kept_reads, load_large
+    g = load_large("c1_1Mbp_L50_40x_t31_u32")
+    reads, _ = large_kept_reads(g, tmp_path)
+    P = port.Port(32)
+    cores = os.cpu_count() or 1
+    ix = P.build_index(reads, int(g["t"]), threads=cores)
+    for d in (0, 1):
+        assert sha(ix["sa%d" % d]) == str(g["sha_sa%d" % d])
+        assert sha(ix["bitmap%d" % d]) == str(g["sha_bitmap%d" % d])
+        assert sha(ix["sample%d" % d]) == str(g["sha_sample%d" % d])
+        assert sha(ix["reads_index%d" % d]) == str(g["sha_reads_index%d" % d])
+    graph_digests_ok(P.overlaps(ix, threads=cores), g, "oracle")
