@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--scale", type=float, default=1.0, help="genome-size scale (1.0 = full)")
-    ap.add_argument("--cpu-scale", type=float, default=0.01,
+    ap.add_argument("--cpu-scale", type=float, default=0.05,
                     help="genome-size scale of the CPU-baseline sample's index")
     ap.add_argument("--cpu-seconds", type=float, default=20.0,
                     help="CPU work of the cpu_baseline sample (reference arm: of all steps together)")
@@ -226,24 +226,28 @@ class CpuSample:
         self.next = 0
 
     def search(self, seconds: float):
-        """Search about `seconds` of reads (continuing where the last call stopped, wrapping
-        around); returns (reads, seconds, probes)."""
+        """Search about `seconds` of reads, continuing where the last call stopped and wrapping
+        around the sample's reads as often as needed; returns (reads, seconds, probes)."""
         nr = self.rd.shape[0]
         probe = min(nr, 4000)
         t0 = time.perf_counter()
         self._run(probe)
         dt = time.perf_counter() - t0
-        count = int(min(nr, max(probe, probe * seconds / max(dt, 1e-6))))
+        count = int(max(probe, probe * seconds / max(dt, 1e-6)))
         t0 = time.perf_counter()
         probes = self._run(count)
         return count, time.perf_counter() - t0, probes
 
     def _run(self, count: int) -> int:
         nr = self.rd.shape[0]
-        first = self.next if self.next + count <= nr else 0
-        self.next = (first + count) % nr
-        g = self.P.overlaps(self.ix, first, count, threads=self.threads, seeds=self.seeds)
-        return g.probes
+        probes = 0
+        while count > 0:
+            take = min(count, nr - self.next)
+            g = self.P.overlaps(self.ix, self.next, take, threads=self.threads, seeds=self.seeds)
+            probes += g.probes
+            self.next = (self.next + take) % nr
+            count -= take
+        return probes
 
     def describe(self, count: int, secs: float) -> str:
         return ("%d reads of the %s workload's reads at genome scale %g (%d reads kept, %d bp, "

@@ -112,6 +112,15 @@ PQ_API int pq_get_index_ref (pq_ctx * ctx, int dir, uint64_t * bitmap, pq_idx * 
  * the exact SA interval of the read's last (dir 0) / first, reversed (dir 1) k bases. */
 PQ_API int pq_get_seeds (pq_ctx * ctx, int dir, pq_idx * start, pq_idx * size, uint16_t * depth);
 
+/* The seed intervals the reference's sort records for every read (index_t.interval_start,
+ * interval_end = the interval's size, interval_depth; src/sufsort.c:178-209, 322-334, starting from
+ * the depth-1 seeds of src/index.c:495-502): the deepest depth D in 9, 12, ..., t at which the
+ * reference's recursive bucket sort visits the bucket of the read's last (dir 0) / first, reversed
+ * (dir 1) D bases, with that bucket's first row and size; depth 1 and the interval of that one base
+ * by C[] when there is none.  Computed on the GPU from direction dir's suffix array (pq_sort or
+ * pq_build_index first); field for field the reference's arrays. */
+PQ_API int pq_get_sort_seeds (pq_ctx * ctx, int dir, pq_idx * start, pq_idx * size, uint16_t * depth);
+
 /* Seed depth k of the overlap search (1 <= k <= min(13, t)); default min(12, t). */
 PQ_API int pq_set_seed_k (pq_ctx * ctx, int k);
 

@@ -119,6 +119,41 @@ typedef struct pq_string_graph_t
     pq_node_t *nodes;
 } pq_string_graph_t;
 
+/* bucket_t (src/sufsort.h:17-23): per first-prefix rank (NUM_SLOTS = 85, src/common.h:50) the
+ * number of suffixes and their offset inside the rank's slot. */
+#define PQ_NUM_SLOTS 85
+typedef struct pq_bucket_t
+{
+    pq_index_type freqs[PQ_NUM_SLOTS];
+    pq_index_type offs[PQ_NUM_SLOTS];
+} pq_bucket_t;
+
+/* src/sufsort.h:32.  Recodes every read in place: byte j becomes the rank (0..84) of the read's bases
+ * j .. min(j + 2, L - 1) in the order of strings of up to 3 bases with a string before its
+ * extensions -- the reference's triplet code (src/sufsort.c:124-151), on every host core. */
+PQ_API void transform_to_triplet (char *reads, int read_len, pq_index_type num_reads);
+/* src/sufsort.h:35-36.  The same for every read reversed (src/sufsort.c:80-121). */
+PQ_API void transform_to_triplet_reverse (char *reads, int read_len, pq_index_type num_reads);
+/* src/sufsort.h:38-40.  Histogram of the recoded text's first-prefix ranks into bkt (frequencies,
+ * offsets restarting in each of the 5 slots of 17 ranks), slot sizes bsize[5], slot offsets
+ * boffset[5] and the largest slot *max_size (src/sufsort.c:386-450), on every host core. */
+PQ_API void initial_sort (char *reads, pq_index_type num_elems, pq_bucket_t * bkt, pq_index_type * bsize,
+                          pq_index_type * boffset, pq_index_type * max_size);
+/* src/sufsort.h:42-46.  Slot `slot` of the suffix array of the recoded text: writes its bsize[slot]
+ * rows (text positions, canonical order: suffix string with end-of-read lowest, then position) to
+ * sa[0 ..), advances new_idx over the slot's ranks as the reference's scatter does, and deepens
+ * interval_start / interval_end (the interval's size) / interval_depth with the seed records of the
+ * slot's sort buckets (src/sufsort.c:178-209, 322-334).  The sort runs on the GPU (device 0): the
+ * whole text is sorted on the first call and kept until a call brings another text (compared by
+ * address, size, read length, min overlap and a checksum of its bytes), so the five slot calls of
+ * one text sort once; the device memory stays held until the process exits or the next text.
+ * read_lock is ignored (the reference's OpenMP locks).  Errors print a message on stderr and exit
+ * with status 0, the reference's ERROR_EXIT convention. */
+PQ_API void suf_sort (pq_index_type * sa, char *reads, int slot, pq_index_type * new_idx, pq_bucket_t * bkt0,
+                      pq_index_type num_elems, int read_len, pq_index_type * interval_start,
+                      pq_index_type * interval_end, uint16_t * interval_depth, void *read_lock,
+                      pq_index_type bkt_offset, int min_overlap);
+
 /* src/index.h:63-68.  Reads the FASTA (import_singlereads + bloom_filter, src/index.c:145-405,
  * src/bloom.c:91-135, restated on the host), then sorts both texts and builds both FM-indexes on
  * the GPU and fills every host field of index_t in the reference's layout.  Paired-end and

@@ -35,12 +35,13 @@ EXPORTS = ["pq_idx_bytes", "pq_create", "pq_destroy", "pq_last_error", "pq_set_r
            "pq_suffix_sort_static", "pq_learned_build", "pq_learned_get_info", "pq_learned_export",
            "pq_learned_predict", "pq_learned_keys", "pq_mlp_forward", "pq_mlp_backward",
            "pq_overlaps_batched", "pq_set_batch_plan", "pq_get_batch_stats", "pq_autotune_batched",
-           "pq_set_sort_chunk", "pq_get_search_traffic"]
+           "pq_set_sort_chunk", "pq_get_search_traffic", "pq_get_sort_seeds"]
 
 
 # The reference's own entry points served by the same library (include/pasqual_gb300_dropin.h).
 DROPIN_EXPORTS = ["construct_index", "construct_string_graph", "destroy_graph", "pq_import_fasta",
-                  "pq_string_graph_from_csr"]
+                  "pq_string_graph_from_csr", "transform_to_triplet", "transform_to_triplet_reverse",
+                  "initial_sort", "suf_sort"]
 
 
 class PQError(RuntimeError):
@@ -101,6 +102,7 @@ def load_library(width: int = 32) -> ct.CDLL:
         "pq_autotune_batched": (c_int, [vp, c_int, c_int, vp]),
         "pq_set_sort_chunk": (c_int, [vp, ct.c_uint64]),
         "pq_get_search_traffic": (c_int, [vp, vp, vp]),
+        "pq_get_sort_seeds": (c_int, [vp, c_int, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -306,6 +308,15 @@ class Pasqual:
         z = np.empty(nr, self.dt)
         d = np.empty(nr, np.uint16)
         self._ck(self.lib.pq_get_seeds(self.h, direction, _p(s), _p(z), _p(d)), "pq_get_seeds")
+        return s[:self.num_reads], z[:self.num_reads], d[:self.num_reads]
+
+    def sort_seeds(self, direction: int):
+        """The seed intervals the reference's sort records: (start, size, depth) per read."""
+        nr = max(self.num_reads, 1)
+        s = np.empty(nr, self.dt)
+        z = np.empty(nr, self.dt)
+        d = np.empty(nr, np.uint16)
+        self._ck(self.lib.pq_get_sort_seeds(self.h, direction, _p(s), _p(z), _p(d)), "pq_get_sort_seeds")
         return s[:self.num_reads], z[:self.num_reads], d[:self.num_reads]
 
     # -- construct_string_graph ------------------------------------------------------------

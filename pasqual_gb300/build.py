@@ -16,7 +16,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 ROOT = os.path.dirname(HERE)
 SOURCES = ["pq_index.cu", "pq_search.cu", "pq_sort.cu", "pq_api.cu", "pq_dropin.cu",
-           "pq_sort_static.cu", "pq_learned.cu"]
+           "pq_sort_static.cu", "pq_learned.cu", "pq_seeds.cu",
+           "pq_sufsort.cu"]
 HEADERS = ["pq_common.cuh", "pq_index.cuh", "pq_sort.cuh", "pq_learned.cuh", "pq_learned_build.cuh", "pq_slots.h"]
 PUBLIC = ["pasqual_gb300.h", "pasqual_gb300_dropin.h"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")

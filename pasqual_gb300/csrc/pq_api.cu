@@ -357,6 +357,53 @@ int pq_get_sa(pq_ctx* ctx, int dir, pq_idx* sa_host) {
     return PQ_OK;
 }
 
+// Rows [first, first + count) of direction dir's suffix array into host memory (the slot a
+// drop-in suf_sort call returns).  Not part of the public header.
+int pq_get_sa_rows(pq_ctx* ctx, int dir, uint64_t first, uint64_t count, pq_idx* host) {
+    if (!ctx || (dir != 0 && dir != 1) || (count && !host)) return PQ_ERR_ARG;
+    if (!ctx->sa_ok[dir]) return fail(ctx, PQ_ERR_STATE, "no suffix array for this direction");
+    if (first > n_rows(ctx) || count > n_rows(ctx) - first) return fail(ctx, PQ_ERR_ARG, "rows out of range");
+    if (count)
+        CK(cudaMemcpyAsync(host, ctx->sa[dir].as<idx_t>() + first, count * sizeof(idx_t), cudaMemcpyDeviceToHost,
+                           ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return PQ_OK;
+}
+
+// The seed records of the sort buckets in rows [r0, r1) of direction dir applied to the host arrays
+// start/size/depth (one entry per read): a record replaces a read's seed when it is deeper, as in
+// src/sufsort.c:182-189.  Not part of the public header.
+int pq_apply_sort_seeds(pq_ctx* ctx, int dir, uint64_t r0, uint64_t r1, pq_idx* start, pq_idx* size,
+                        uint16_t* depth) {
+    if (!ctx || (dir != 0 && dir != 1) || !start || !size || !depth) return PQ_ERR_ARG;
+    if (!ctx->sa_ok[dir]) return fail(ctx, PQ_ERR_STATE, "no suffix array for this direction");
+    const size_t nr = ctx->num_reads, n = n_rows(ctx);
+    if (r0 > r1 || r1 > n) return fail(ctx, PQ_ERR_ARG, "rows out of range");
+    if (!nr || r0 == r1) return PQ_OK;
+    cudaSetDevice(ctx->device);
+    if (!ctx->pk_ok[dir]) {
+        CK(ctx->pk[dir].ensure((n / 32 + 4) * sizeof(uint64_t)));
+        CK(pq::pack_text(ctx->reads.as<uint8_t>(), n, idx_t(ctx->L), dir, ctx->pk[dir].as<uint64_t>(), ctx->st));
+        ctx->pk_ok[dir] = true;
+    }
+    DevBuf s, z, d, tmp;
+    CK(s.ensure(nr * sizeof(idx_t)));
+    CK(z.ensure(nr * sizeof(idx_t)));
+    CK(d.ensure(nr * sizeof(uint16_t)));
+    const size_t tb = pq::sort_seeds_tmp_bytes(size_t(r1 - r0));
+    CK(tmp.ensure(tb));
+    CK(cudaMemcpyAsync(s.p, start, nr * sizeof(idx_t), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(z.p, size, nr * sizeof(idx_t), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(d.p, depth, nr * sizeof(uint16_t), cudaMemcpyHostToDevice, ctx->st));
+    CK(pq::sort_seeds(ctx->sa[dir].as<idx_t>(), ctx->pk[dir].as<uint64_t>(), idx_t(ctx->L), ctx->t, size_t(r0),
+                      size_t(r1), d.as<uint16_t>(), s.as<idx_t>(), z.as<idx_t>(), tmp.p, tb, ctx->st));
+    CK(cudaMemcpyAsync(start, s.p, nr * sizeof(idx_t), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(size, z.p, nr * sizeof(idx_t), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(depth, d.p, nr * sizeof(uint16_t), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return PQ_OK;
+}
+
 int pq_set_seed_k(pq_ctx* ctx, int k) {
     if (!ctx) return PQ_ERR_ARG;
     if (k < 1 || k > 13) return fail(ctx, PQ_ERR_ARG, "seed depth must be in [1, 13]");
@@ -484,6 +531,34 @@ int pq_get_seeds(pq_ctx* ctx, int dir, pq_idx* start, pq_idx* size, uint16_t* de
     CK(cudaStreamSynchronize(ctx->st));
     if (depth)
         for (size_t i = 0; i < nr; ++i) depth[i] = uint16_t(ctx->fm_k[dir]);
+    return PQ_OK;
+}
+
+int pq_get_sort_seeds(pq_ctx* ctx, int dir, pq_idx* start, pq_idx* size, uint16_t* depth) {
+    if (!ctx || (dir != 0 && dir != 1)) return PQ_ERR_ARG;
+    if (!ctx->sa_ok[dir]) return fail(ctx, PQ_ERR_STATE, "no suffix array for this direction");
+    cudaSetDevice(ctx->device);
+    const size_t nr = ctx->num_reads, n = n_rows(ctx);
+    if (!nr) return PQ_OK;
+    if (!ctx->pk_ok[dir]) {
+        CK(ctx->pk[dir].ensure((n / 32 + 4) * sizeof(uint64_t)));
+        CK(pq::pack_text(ctx->reads.as<uint8_t>(), n, idx_t(ctx->L), dir, ctx->pk[dir].as<uint64_t>(), ctx->st));
+        ctx->pk_ok[dir] = true;
+    }
+    DevBuf s, z, d, tmp;
+    CK(s.ensure(nr * sizeof(idx_t)));
+    CK(z.ensure(nr * sizeof(idx_t)));
+    CK(d.ensure(nr * sizeof(uint16_t)));
+    const size_t tb = pq::sort_seeds_tmp_bytes(n);
+    CK(tmp.ensure(tb));
+    CK(pq::seed_init(ctx->reads.as<uint8_t>(), ctx->num_reads, idx_t(ctx->L), dir, ctx->C, d.as<uint16_t>(),
+                     s.as<idx_t>(), z.as<idx_t>(), ctx->st));
+    CK(pq::sort_seeds(ctx->sa[dir].as<idx_t>(), ctx->pk[dir].as<uint64_t>(), idx_t(ctx->L), ctx->t, 0, n,
+                      d.as<uint16_t>(), s.as<idx_t>(), z.as<idx_t>(), tmp.p, tb, ctx->st));
+    if (start) CK(cudaMemcpyAsync(start, s.p, nr * sizeof(idx_t), cudaMemcpyDeviceToHost, ctx->st));
+    if (size) CK(cudaMemcpyAsync(size, z.p, nr * sizeof(idx_t), cudaMemcpyDeviceToHost, ctx->st));
+    if (depth) CK(cudaMemcpyAsync(depth, d.p, nr * sizeof(uint16_t), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
     return PQ_OK;
 }
 

@@ -546,7 +546,7 @@ pq_index_t* construct_index(char* single_file, char* pair_file1, char* pair_file
         uint16_t* sd = (uint16_t*)malloc((nr ? nr : 1) * sizeof(uint16_t));
         if (!sample || !ri || !ss || !sz || !sd) error_exit("out of memory.\n");
         ck(pq_get_index_ref(ctx, dir, bm.data(), sample, ri));
-        ck(pq_get_seeds(ctx, dir, ss, sz, sd));
+        ck(pq_get_sort_seeds(ctx, dir, ss, sz, sd));
         uint64_t** dst = dir ? ix->OCC_bitmap_bw : ix->OCC_bitmap;
         for (int c = 0; c < 5; ++c) {
             dst[c] = (uint64_t*)malloc(rowlen * sizeof(uint64_t));

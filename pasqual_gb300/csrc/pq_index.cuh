@@ -21,6 +21,15 @@ cudaError_t build_kmer_table(const idx_t* sa, idx_t num_reads, idx_t L, int k, i
 // sort's BWT symbols, whose rows (symbol != 0xff) the sort has already entered, or null (all rows)
 cudaError_t build_isa(const idx_t* sa, size_t n, idx_t L, idx_t M, idx_t* isa, cudaStream_t st,
                       const uint8_t* hint = nullptr);
+// The per-read seed intervals the reference's sort records (index_t.interval_start/end/depth,
+// src/sufsort.c:178-209, 322-334) from a finished suffix array and the packed text of its
+// direction (pq_seeds.cu).  seed_init writes the depth-1 seeds build_idx starts from; sort_seeds
+// then deepens them with the records of the buckets in rows [r0, r1).
+cudaError_t seed_init(const uint8_t* reads, idx_t num_reads, idx_t L, int dir, const idx_t C[6], uint16_t* depth,
+                      idx_t* start, idx_t* size, cudaStream_t st);
+size_t sort_seeds_tmp_bytes(size_t rows);
+cudaError_t sort_seeds(const idx_t* sa, const uint64_t* pk, idx_t L, int t, size_t r0, size_t r1, uint16_t* depth,
+                       idx_t* start, idx_t* size, void* tmp, size_t tmp_bytes, cudaStream_t st);
 cudaError_t export_ref_layout(const OccBlock* blk, const idx_t* sb, idx_t num_reads, idx_t L,
                               const idx_t fix[4], uint64_t* bitmap, idx_t* sample, cudaStream_t st);
 
