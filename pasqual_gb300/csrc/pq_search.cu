@@ -1019,6 +1019,10 @@ __device__ __forceinline__ int cmp_cont(const uint64_t* a, int la, const uint64_
     return la == lb ? 0 : (la < lb ? -1 : 1);
 }
 
+template <int W>
+__device__ __forceinline__ int reduce_gathered(int L, const WarpScratch& S, idx_t self, int side, size_t red, int m,
+                                               size_t eb, int& ne, int& count);
+
 // Edges of one side of one read from its level-0 candidate groups (na of the first kind, then
 // n0 - na of the second) in the candidate scratch at `cand`; per-lane scratch at `red`.
 template <int W>
@@ -1026,7 +1030,6 @@ __device__ __forceinline__ int reduce_sorted(const SearchArgs& A, const WarpScra
                                              size_t cand, int na, int n0, size_t red, size_t eb, int& ne,
                                              int& count, Tally& probes) {
     const int L = A.L, M = L - A.t;
-    const int first_kind = side ? PQ_FB : PQ_BF;
     int m = 0;
     for (int g = 0; g < n0; ++g) {
         const size_t src = cand + (g < na ? size_t(2 * side) * M + g : size_t(2 * side + 1) * M + (g - na));
@@ -1044,6 +1047,16 @@ __device__ __forceinline__ int reduce_sorted(const SearchArgs& A, const WarpScra
             ++m;
         }
     }
+    return reduce_gathered<W>(L, S, self, side, red, m, eb, ne, count);
+}
+
+// The reduction of reduce_sorted over m gathered candidates: continuations in S.r_k (word w of
+// candidate i at r_k[w * r_plane + red + i]), read ids in S.r_id and (overlap, kind) in S.r_meta,
+// from red on.  Emitted edges go to the edge scratch at eb + ne, in DFS order.
+template <int W>
+__device__ __forceinline__ int reduce_gathered(int L, const WarpScratch& S, idx_t self, int side, size_t red, int m,
+                                               size_t eb, int& ne, int& count) {
+    const int first_kind = side ? PQ_FB : PQ_BF;
     int nemit = 0;
     for (int c = 0; c < m; ++c) {
         const uint64_t* kc = S.r_k + red + c;
@@ -1094,6 +1107,120 @@ __device__ __forceinline__ int reduce_sorted(const SearchArgs& A, const WarpScra
     }
     count = nemit;
     return OVF_NONE;
+}
+
+// ------------------------------------------------------------------------ lean tier: candidate scan
+//
+// The interval scan already yields every candidate of a side with its read id and overlap -- row
+// (r', o) of I_t is a candidate at depth t + o -- and its continuation is the rest of r' after the
+// overlap: the walked index's text right after the matched pattern, at the row's text position
+// plus t (complemented for the kinds walked on the backward index, B-F and F-F).  So the lean tier
+// gathers each side's candidates for reduce_gathered straight from the scan, without the
+// depth-indexed candidate slots, the inverse-SA load of every candidate depth and the suffix-array
+// reload of every candidate that the group form (scan_pair + reduce_sorted) needs.
+
+// Candidates of both kinds of one side, gathered for reduce_gathered at red + m: false when the
+// scan does not apply to this read (a depth-t interval of more than kScanMax rows, or a learned
+// window that missed) or the side has more than kRedMax candidates -- the fast tier then redoes
+// the read.
+template <int W>
+__device__ __forceinline__ bool scan_planes(const SearchArgs& A, const FmView* fm, idx_t self, int k0, int k1,
+                                            const WarpScratch& S, size_t red, int& m, int32_t& olp, Tally& probes) {
+    const int L = A.L, t = A.t, k = A.seed_k, M = L - t;
+    const int m0 = m;
+    const int tb = t < 32 * kScanWords ? t : 32 * kScanWords;
+    uint64_t P0[kScanWords], P1[kScanWords];
+    pattern_words(fm, L, t, k0, self, P0, probes);
+    pattern_words(fm, L, t, k1, self, P1, probes);
+    const FmView* f0 = fm + walked_index(k0);
+    const FmView* f1 = fm + walked_index(k1);
+    idx_t lo[2], hi[2], first[2], end[2];
+    if (A.sa_seed == 2) {
+        #pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const LearnedView& v = (q ? f1 : f0)->lx;
+            const uint32_t K = uint32_t((q ? P1 : P0)[0] >> 32);
+            const int sg = lx_segment(v, K);
+            const long long pr = lx_predict(v, sg, K);
+            const long long b0 = (long long)__ldg(v.base + sg), b1 = (long long)__ldg(v.base + sg + 1);
+            const long long a = pr - (long long)__ldg(v.err + 2 * sg), b = pr + (long long)__ldg(v.err + 2 * sg + 1);
+            lo[q] = idx_t(a > b0 ? a : b0);
+            hi[q] = idx_t(b < b1 ? b : b1);
+            if (hi[q] < lo[q]) hi[q] = lo[q];
+        }
+    } else {
+        const uint32_t c0 = uint32_t(P0[0] >> (64 - 2 * k)), c1 = uint32_t(P1[0] >> (64 - 2 * k));
+        lo[0] = __ldg(f0->kstart + c0);
+        hi[0] = __ldg(f0->kend + c0) + 1;
+        lo[1] = __ldg(f1->kstart + c1);
+        hi[1] = __ldg(f1->kend + c1) + 1;
+        probes.add(2, 4);
+        if (hi[0] < lo[0]) hi[0] = lo[0];
+        if (hi[1] < lo[1]) hi[1] = lo[1];
+    }
+    sa_bounds2(f0, f1, L, P0, P1, tb, lo, hi, first, end, probes);
+    if (A.sa_seed == 2) {
+        const idx_t n_rows = A.num_reads * idx_t(L);
+        bool ok = true;
+        #pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const FmView& fa = *(q ? f1 : f0);
+            const uint64_t (&P)[kScanWords] = q ? P1 : P0;
+            if (first[q] == lo[q] && lo[q] > 0) {
+                const idx_t p = __ldg(fa.sa + lo[q] - 1);
+                ok = ok && cmp_row(fa.pk, p, L - int(p % idx_t(L)), P, tb) < 0;
+                probes.add(2, 1 + cmp_sectors(fa.pk, p));
+            }
+            if (end[q] == hi[q] && hi[q] < n_rows) {
+                const idx_t p = __ldg(fa.sa + hi[q]);
+                ok = ok && cmp_row(fa.pk, p, L - int(p % idx_t(L)), P, tb) > 0;
+                probes.add(2, 1 + cmp_sectors(fa.pk, p));
+            }
+        }
+        if (!ok) {
+            atomicAdd(A.lx_misses, 1ull);
+            return false;
+        }
+    }
+    if (end[0] - first[0] > idx_t(kScanMax) || end[1] - first[1] > idx_t(kScanMax)) return false;
+    #pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const int kind = q ? k1 : k0;
+        const FmView& fa = *(q ? f1 : f0);
+        const FmView& fb = fm[1 - walked_index(kind)];
+        const bool cmpl = !(kind == PQ_FB || kind == PQ_BF);
+        const uint64_t* pks = cmpl ? fb.pk : fa.pk;
+        const uint64_t flip = walked_index(kind) ? ~uint64_t(0) : 0;
+        const size_t src = size_t(self) * L + size_t(L - t);
+        for (idx_t row = first[q]; row < end[q]; ++row) {
+            const idx_t p = __ldg(fa.sa + row);
+            const idx_t rp = p / idx_t(L);
+            const int o = int(p - rp * idx_t(L));
+            probes.add(2, 1);
+            if (o >= M || !prefix_matches(fa.pk, size_t(rp) * L, pks, src - o, o, cmpl, probes.sectors)) continue;
+            if (t > tb && !prefix_matches(fa.pk, size_t(p) + tb, pks, src + tb, t - tb, cmpl, probes.sectors))
+                continue;
+            if (m - m0 >= kRedMax) return false;
+            // the continuation: M - o bases of the walked text after the pattern
+            const int len = M - o;
+            const size_t pos = size_t(p) + size_t(t);
+            int nw = 0;
+            #pragma unroll
+            for (int w = 0; w < W; ++w) {
+                const int left = len - 32 * w;
+                if (left <= 0) break;
+                S.r_k[w * S.r_plane + red + m] =
+                    (text_window(fa.pk, pos + 32 * w) ^ flip) & top_mask(left < 32 ? left : 32);
+                nw = w + 1;
+            }
+            if (nw) probes.add(0, sectors_of(fa.pk + (pos >> 5), 8 * ((((pos + 32 * (nw - 1)) >> 5) - (pos >> 5)) + 2)));
+            S.r_id[red + m] = rp;
+            S.r_meta[red + m] = pack_meta(t + o, kind);
+            ++m;
+            olp = int32_t(uint32_t(olp) + 1u);
+        }
+    }
+    return true;
 }
 
 // warp-cooperative copy of one batch description into shared memory
@@ -1474,12 +1601,12 @@ __global__ void __launch_bounds__(128, 6) k_search_fast(SearchArgs A0, SearchOut
 
 // ------------------------------------------------------------------------------ lean tier
 //
-// One thread per read, no warp-level phases: candidates by the interval scan (or the walk where
-// the scan does not apply) and each side's edges by sorted continuations.  A read with more than
-// kRedMax candidates on a side is listed in `defer` for the fast tier (which runs the DFS there);
-// a read whose edges outgrow its edge slots goes to the wide tier like any other overflow.  With
-// no shared-memory DFS state and fewer registers, more warps stay resident to hide the latency of
-// the independent suffix-array and text loads.
+// One thread per read, no warp-level phases: each side's candidates by the interval scan as a list
+// of records, and its edges by sorted continuations.  A read the scan does not serve (a depth-t
+// interval beyond kScanMax rows, a learned window that missed) or with more than kRedMax
+// candidates on a side is listed in `defer` for the fast tier (which walks and runs the DFS there).
+// With no shared-memory DFS state and fewer registers, more warps stay resident to hide the latency
+// of the independent suffix-array and text loads.
 constexpr int kLeanThreads = 128;
 
 template <int W>
@@ -1501,7 +1628,6 @@ __global__ void __launch_bounds__(kLeanThreads, 8) k_search_lean(SearchArgs A0, 
         __syncwarp();
     }
     const size_t tid = gw * 32 + lane;
-    const size_t cb = tid * 4 * size_t(S.mstride);
     const size_t eb = tid * size_t(S.ebcap);
     const size_t red = tid * size_t(kRedMax);
     Tally probes;
@@ -1528,34 +1654,26 @@ __global__ void __launch_bounds__(kLeanThreads, 8) k_search_lean(SearchArgs A0, 
             gend = group + 1;
             if (group * 32 >= size_t(A.num_reads)) break;
         }
-        const int M = A.L - A.t;
         for (; group < gend && group * 32 < size_t(A.num_reads); ++group) {
             const size_t r = group * 32 + lane;
             if (r >= size_t(A.num_reads)) continue;
             const idx_t self = idx_t(r);
-            ReadView rd{s_reads + threadIdx.x, int(blockDim.x)};
-            bool loaded = false;      // the read's bases are loaded only if a chain walks
-            auto need_read = [&] {
-                if (!loaded) load_read(A, self, s_reads + threadIdx.x, blockDim.x, probes);
-                loaded = true;
-            };
-            int nb[2], nf[2];
+            // B side: B-F then B-B candidates, then extract_bw_edges (src/string_graph.c:824-825);
+            // then the F side: F-B, F-F, extract_fw_edges (:828-829)
             int32_t ob = 0, of = 0;
-            chain_pair(A, A.fm, rd, self, PQ_BF, PQ_BB, nb, ob, probes, SlotsFast{S.c_ll, S.c_uu, S.c_meta, cb, M},
-                       need_read);
-            chain_pair(A, A.fm, rd, self, PQ_FB, PQ_FF, nf, of, probes,
-                       SlotsFast{S.c_ll, S.c_uu, S.c_meta, cb + 2 * size_t(M), M}, need_read);
-            if (uint32_t(ob) > uint32_t(kRedMax) || uint32_t(of) > uint32_t(kRedMax)) {
+            int m = 0, ne = 0, count_b = 0, count_f = 0;
+            int status = OVF_NONE;
+            bool ok = scan_planes<W>(A, A.fm, self, PQ_BF, PQ_BB, S, red, m, ob, probes);
+            if (ok && ob != 0) status = reduce_gathered<W>(A.L, S, self, 0, red, m, eb, ne, count_b);
+            m = 0;
+            if (ok) ok = scan_planes<W>(A, A.fm, self, PQ_FB, PQ_FF, S, red, m, of, probes);
+            if (ok && of != 0 && status == OVF_NONE)
+                status = reduce_gathered<W>(A.L, S, self, 1, red, m, eb, ne, count_f);
+            if (!ok) {              // the fast tier redoes this read (walk, or more candidates)
                 const unsigned k = atomicAdd(A.defer_count, 1u);
                 A.defer[k] = self;
                 continue;
             }
-            int ne = 0, count_b = 0, count_f = 0;
-            int status = OVF_NONE;
-            if (ob != 0)     // src/string_graph.c:824
-                status = reduce_sorted<W>(A, S, self, 0, cb, nb[0], nb[0] + nb[1], red, eb, ne, count_b, probes);
-            if (status == OVF_NONE && of != 0)     // src/string_graph.c:828
-                status = reduce_sorted<W>(A, S, self, 1, cb, nf[0], nf[0] + nf[1], red, eb, ne, count_f, probes);
             if (status != OVF_NONE) {
                 O.status[r] = uint8_t(status);
                 const unsigned k = atomicAdd(O.ovf_count, 1u);
