@@ -80,6 +80,7 @@ struct pq_ctx {
     int fm_k[2] = {0, 0};
     DevBuf sort_tmp, counts;
     const uint32_t* sorted_keys[2] = {nullptr, nullptr};   // the last sort's keys, inside sort_tmp
+    int kmer_from_sort[2] = {0, 0};                         // k of the k-mer table a chunked sort entered
     const uint8_t* bwt_hint[2] = {nullptr, nullptr};       // the last sort's BWT symbols, inside sort_tmp
     bool pk_ok[2] = {false, false};                        // pk[dir] holds this read set's packed text
     uint64_t sort_chunk = 0;                                // suffixes per sort chunk (0: automatic)
@@ -279,9 +280,9 @@ int pq_get_counts(pq_ctx* ctx, pq_idx C[6], pq_idx suffix_count[4], pq_idx prefi
     return PQ_OK;
 }
 
-// side_outputs: also the BWT symbols and inverse-SA entries of the rows the group refinement
-// places (FM-index work done where the refinement leaves DRAM idle; pq_build_index asks for
-// them).  pq_sort itself computes the suffix array only.
+// side_outputs: also the BWT symbols of the rows the group refinement places (FM-index work done
+// where the refinement leaves DRAM idle; pq_build_index asks for them), and for a chunked sort the
+// k-mer table from its chunks' keys.  pq_sort itself computes the suffix array only.
 static int sort_dir(pq_ctx* ctx, int dir, bool side_outputs) {
     if (!ctx || (dir != 0 && dir != 1)) return PQ_ERR_ARG;
     if (!ctx->have_reads) return fail(ctx, PQ_ERR_STATE, "pq_set_reads first");
@@ -289,9 +290,6 @@ static int sort_dir(pq_ctx* ctx, int dir, bool side_outputs) {
     const size_t n = n_rows(ctx);
     CK(ctx->sa[dir].ensure(n * sizeof(idx_t) + 64));
     CK(ctx->pk[dir].ensure((n / 32 + 4) * sizeof(uint64_t)));
-    // the inverse SA (read offsets 1..L-t): the sort enters the rows its refinement places
-    const size_t isa_n = size_t(ctx->num_reads) * size_t(ctx->L - ctx->t);
-    CK(ctx->isa[dir].ensure(isa_n * sizeof(idx_t) + 64));
     // one pass below 2^31 suffixes (32-bit group ranks), else chunks of 6-base buckets
     const size_t one_pass_max = (size_t(1) << 31) - 1;
     const bool chunked = n > one_pass_max || (ctx->sort_chunk && n > ctx->sort_chunk);
@@ -302,11 +300,24 @@ static int sort_dir(pq_ctx* ctx, int dir, bool side_outputs) {
     ctx->sorted_keys[0] = ctx->sorted_keys[1] = nullptr;     // the scratch is about to be reused
     ctx->bwt_hint[0] = ctx->bwt_hint[1] = nullptr;
     const uint8_t** hint_out = side_outputs ? &ctx->bwt_hint[dir] : nullptr;
-    idx_t* isa_out = side_outputs ? ctx->isa[dir].as<idx_t>() : nullptr;
+    idx_t* isa_out = nullptr;       // the search needs no inverse suffix array
+    // a chunked index-build sort also enters the k-mer table from its chunks' keys (k >= 6: a
+    // k-mer's rows then lie in one 6-base bucket, so in one chunk)
+    ctx->kmer_from_sort[dir] = 0;
+    const int kk = ctx->seed_k;
+    const bool kmer_in_sort = side_outputs && chunked && kk >= 6 && kk <= pq::kSortKeyBases;
+    if (kmer_in_sort) {
+        const size_t nk = size_t(1) << (2 * kk);
+        CK(ctx->kstart[dir].ensure(nk * sizeof(idx_t)));
+        CK(ctx->kend[dir].ensure(nk * sizeof(idx_t)));
+        CK(pq::kmer_table_clear(kk, ctx->kstart[dir].as<idx_t>(), ctx->kend[dir].as<idx_t>(), ctx->st));
+    }
     int rc = chunked ? pq::suffix_sort_chunked(ctx->reads.as<uint8_t>(), ctx->num_reads, ctx->L, dir,
                                                ctx->sa[dir].as<idx_t>(), cap, ctx->sort_tmp.p, tmp_bytes, ctx->st,
                                                hint_out, ctx->pk[dir].as<uint64_t>(), isa_out,
-                                               idx_t(ctx->L - ctx->t))
+                                               idx_t(ctx->L - ctx->t),
+                                               kmer_in_sort ? ctx->kstart[dir].as<idx_t>() : nullptr,
+                                               kmer_in_sort ? ctx->kend[dir].as<idx_t>() : nullptr, kk)
                      : pq::suffix_sort(ctx->reads.as<uint8_t>(), ctx->num_reads, ctx->L, dir,
                                        ctx->sa[dir].as<idx_t>(), ctx->sort_tmp.p, tmp_bytes, ctx->st,
                                        &ctx->sorted_keys[dir], hint_out, ctx->pk[dir].as<uint64_t>(), isa_out,
@@ -318,6 +329,7 @@ static int sort_dir(pq_ctx* ctx, int dir, bool side_outputs) {
     CK(cudaEventRecord(ctx->ev1, ctx->st));
     CK(cudaEventSynchronize(ctx->ev1));
     cudaEventElapsedTime(&ctx->ms_sort, ctx->ev0, ctx->ev1);
+    if (kmer_in_sort) ctx->kmer_from_sort[dir] = kk;
     ctx->sa_ok[dir] = true;
     ctx->fm_ok[dir] = false;
     ctx->graph_ok = false;
@@ -342,6 +354,7 @@ int pq_set_sa(pq_ctx* ctx, int dir, const pq_idx* sa, int from_device) {
     CK(cudaStreamSynchronize(ctx->st));
     ctx->sorted_keys[dir] = nullptr;
     ctx->bwt_hint[dir] = nullptr;
+    ctx->kmer_from_sort[dir] = 0;
     ctx->sa_ok[dir] = true;
     ctx->fm_ok[dir] = false;
     ctx->graph_ok = false;
@@ -442,8 +455,7 @@ int pq_build_fm(pq_ctx* ctx, int dir) {
     CK(ctx->kstart[dir].ensure(nk * sizeof(idx_t)));
     CK(ctx->kend[dir].ensure(nk * sizeof(idx_t)));
     CK(ctx->pk[dir].ensure((n / 32 + 4) * sizeof(uint64_t)));
-    const size_t isa_n = size_t(ctx->num_reads) * size_t(ctx->L - ctx->t);
-    CK(ctx->isa[dir].ensure(isa_n * sizeof(idx_t) + 64));
+    ctx->isa[dir].release();
     CK(cudaEventRecord(ctx->ev0, ctx->st));
     if (!ctx->pk_ok[dir])
         CK(pq::pack_text(ctx->reads.as<uint8_t>(), n, idx_t(ctx->L), dir, ctx->pk[dir].as<uint64_t>(), ctx->st));
@@ -451,10 +463,11 @@ int pq_build_fm(pq_ctx* ctx, int dir) {
     CK(pq::build_occ(ctx->sa[dir].as<idx_t>(), ctx->reads.as<uint8_t>(), ctx->num_reads, idx_t(ctx->L), dir,
                      ctx->blk[dir].as<OccBlock>(), ctx->sb[dir].as<idx_t>(), ctx->ri[dir].as<idx_t>(), ctx->st,
                      ctx->pk[dir].as<uint64_t>(), ctx->bwt_hint[dir]));
-    CK(pq::build_kmer_table(ctx->sa[dir].as<idx_t>(), ctx->num_reads, idx_t(ctx->L), k, ctx->kstart[dir].as<idx_t>(),
-                            ctx->kend[dir].as<idx_t>(), ctx->st, ctx->sorted_keys[dir], ctx->pk[dir].as<uint64_t>()));
-    CK(pq::build_isa(ctx->sa[dir].as<idx_t>(), n, idx_t(ctx->L), idx_t(ctx->L - ctx->t), ctx->isa[dir].as<idx_t>(),
-                     ctx->st, ctx->bwt_hint[dir]));
+    if (ctx->kmer_from_sort[dir] != k)
+        CK(pq::build_kmer_table(ctx->sa[dir].as<idx_t>(), ctx->num_reads, idx_t(ctx->L), k,
+                                ctx->kstart[dir].as<idx_t>(), ctx->kend[dir].as<idx_t>(), ctx->st,
+                                ctx->sorted_keys[dir], ctx->pk[dir].as<uint64_t>()));
+    ctx->kmer_from_sort[dir] = 0;
     CK(cudaEventRecord(ctx->ev1, ctx->st));
     CK(cudaEventSynchronize(ctx->ev1));
     cudaEventElapsedTime(&ctx->ms_fm, ctx->ev0, ctx->ev1);
@@ -592,7 +605,7 @@ static int search_prepare(pq_ctx* ctx, pq::SearchArgs& A, pq::SearchOut& O) {
         f.kend = ctx->kend[d].as<idx_t>();
         f.sa = ctx->sa[d].as<idx_t>();
         f.pk = ctx->pk[d].as<uint64_t>();
-        f.isa = ctx->isa[d].as<idx_t>();
+        f.isa = nullptr;          // no inverse suffix array: reads the lean tier hands over walk
         const idx_t* fix = d == 0 ? ctx->sfx : ctx->pfx;
         f.Cf[0] = ctx->C[0];
         for (int c = 1; c <= 4; ++c) f.Cf[c] = ctx->C[c] + fix[c - 1];
@@ -600,6 +613,7 @@ static int search_prepare(pq_ctx* ctx, pq::SearchArgs& A, pq::SearchOut& O) {
     A.reads = ctx->reads.as<uint8_t>();
     A.num_reads = ctx->num_reads;
     A.L = ctx->L;
+    A.dl = make_divl(uint32_t(ctx->L));
     A.t = ctx->t;
     A.seed_k = ctx->fm_k[0];
     // Interval scan where depth-t intervals are small (4^min(t, 64) well above 64 n: chance hits

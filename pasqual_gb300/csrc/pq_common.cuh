@@ -69,6 +69,17 @@ struct FmView {
     idx_t Cf[5];              // Cf[0] = C[0]; Cf[c] = C[c] + fix[c]  (LF-mapping base)
 };
 
+// Division of a text position by the read length L without a 64-bit divide: with
+// m = floor((2^64 - 1) / L) + 1, floor(p / L) = high 64 bits of p * m for every p < 2^64 / L (so
+// for every position of an index below 2^48 suffixes, L <= 65535): the product's excess over p / L
+// is below p / 2^64 < 1 / L, too small to reach the next integer.
+struct DivL {
+    uint64_t m;
+    uint32_t L;
+};
+inline DivL make_divl(uint32_t L) { return DivL{~uint64_t(0) / L + 1, L}; }
+__device__ __forceinline__ uint64_t div_l(uint64_t p, const DivL& d) { return __umul64hi(p, d.m); }
+
 namespace pq {
 // Count of kernels this library has launched (reported through pq_get_kernel_stats).
 void note_launch();

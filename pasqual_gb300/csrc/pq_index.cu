@@ -307,9 +307,10 @@ __device__ __forceinline__ uint32_t key_code(uint32_t key, int k) {
 }
 
 // four rows a thread from one 16-byte load (the key array starts 16-byte aligned), plus the
-// neighbours on either side
+// neighbours on either side; key[i] is the key of row off + i (the keys of one chunk of a chunked
+// sort: for k >= 6 a k-mer's rows share one 6-base bucket of that sort, so never span two chunks)
 __global__ void k_kmer_bounds_keys(const uint32_t* __restrict__ key, idx_t n, int k, idx_t* __restrict__ kstart,
-                                   idx_t* __restrict__ kend) {
+                                   idx_t* __restrict__ kend, size_t off) {
     const size_t stride = size_t(gridDim.x) * blockDim.x;
     const size_t nn = size_t(n);
     for (size_t q = size_t(blockIdx.x) * blockDim.x + threadIdx.x; 4 * q < nn; q += stride) {
@@ -331,8 +332,8 @@ __global__ void k_kmer_bounds_keys(const uint32_t* __restrict__ key, idx_t n, in
         for (int u = 1; u <= 4; ++u) {
             const size_t r = r0 + u - 1;
             if (r >= nn || c[u] == 0xffffffffu) continue;
-            if (c[u - 1] != c[u]) kstart[c[u]] = idx_t(r);
-            if (c[u + 1] != c[u]) kend[c[u]] = idx_t(r);
+            if (c[u - 1] != c[u]) kstart[c[u]] = idx_t(off + r);
+            if (c[u + 1] != c[u]) kend[c[u]] = idx_t(off + r);
         }
     }
 }
@@ -433,14 +434,26 @@ cudaError_t read_counts(const uint8_t* reads, idx_t num_reads, idx_t L, unsigned
     return cudaGetLastError();
 }
 
-cudaError_t build_kmer_table(const idx_t* sa, idx_t num_reads, idx_t L, int k, idx_t* kstart, idx_t* kend,
-                             cudaStream_t st, const uint32_t* sorted_keys, const uint64_t* pk) {
-    const size_t n = size_t(num_reads) * L;
+cudaError_t kmer_table_clear(int k, idx_t* kstart, idx_t* kend, cudaStream_t st) {
     const size_t nk = size_t(1) << (2 * k);
     { k_fill_idx<<<grid_for(nk, 256), 256, 0, st>>>(kstart, nk, idx_t(1)); note_launch(); }
     { k_fill_idx<<<grid_for(nk, 256), 256, 0, st>>>(kend, nk, idx_t(0)); note_launch(); }
+    return cudaGetLastError();
+}
+
+cudaError_t kmer_table_from_keys(const uint32_t* keys, size_t m, size_t off, int k, idx_t* kstart, idx_t* kend,
+                                 cudaStream_t st) {
+    if (m) { k_kmer_bounds_keys<<<grid_for((m + 3) / 4, 256), 256, 0, st>>>(keys, idx_t(m), k, kstart, kend, off); note_launch(); }
+    return cudaGetLastError();
+}
+
+cudaError_t build_kmer_table(const idx_t* sa, idx_t num_reads, idx_t L, int k, idx_t* kstart, idx_t* kend,
+                             cudaStream_t st, const uint32_t* sorted_keys, const uint64_t* pk) {
+    const size_t n = size_t(num_reads) * L;
+    cudaError_t e = kmer_table_clear(k, kstart, kend, st);
+    if (e != cudaSuccess) return e;
     if (n && sorted_keys && k <= kSortKeyBases && reinterpret_cast<uintptr_t>(sorted_keys) % 16 == 0) {
-        { k_kmer_bounds_keys<<<grid_for((n + 3) / 4, 256), 256, 0, st>>>(sorted_keys, idx_t(n), k, kstart, kend); note_launch(); }
+        return kmer_table_from_keys(sorted_keys, n, 0, k, kstart, kend, st);
     } else if (n) {
         { k_kmer_bounds_pk<<<grid_for(n, 256), 256, 0, st>>>(sa, pk, n, L, k, kstart, kend); note_launch(); }
     }

@@ -17,6 +17,11 @@ cudaError_t read_counts(const uint8_t* reads, idx_t num_reads, idx_t L, unsigned
 // suffix array and the packed text pk (each one streaming pass)
 cudaError_t build_kmer_table(const idx_t* sa, idx_t num_reads, idx_t L, int k, idx_t* kstart, idx_t* kend,
                              cudaStream_t st, const uint32_t* sorted_keys, const uint64_t* pk);
+// The k-mer table in parts: cleared (every k-mer absent), then entered from runs of sorted keys
+// (rows off .. off + m - 1), as each chunk of a chunked sort finishes.
+cudaError_t kmer_table_clear(int k, idx_t* kstart, idx_t* kend, cudaStream_t st);
+cudaError_t kmer_table_from_keys(const uint32_t* keys, size_t m, size_t off, int k, idx_t* kstart, idx_t* kend,
+                                 cudaStream_t st);
 // rows of the suffixes at read offsets 1..M (isa[read * M + offset - 1]); M = L - t.  hint: the
 // sort's BWT symbols, whose rows (symbol != 0xff) the sort has already entered, or null (all rows)
 cudaError_t build_isa(const idx_t* sa, size_t n, idx_t L, idx_t M, idx_t* isa, cudaStream_t st,
@@ -60,6 +65,7 @@ struct SearchArgs {
     idx_t num_reads;
     int L;
     int t;
+    DivL dl;                    // division by L
     int seed_k;                 // k-mer seed depth (0 = start at depth 1 from C[])
     int sa_seed;                // 1: candidates by depth-t interval scan (needs fm[].sa/pk/isa),
                                 // 2: the same with learned windows (needs fm[].lx)

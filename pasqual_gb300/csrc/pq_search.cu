@@ -65,6 +65,12 @@ struct Tally {
     }
 };
 
+// bases from text position p to the end of its read, and the read of position p (DivL: no divide)
+__device__ __forceinline__ int suffix_len(idx_t p, const DivL& dl) {
+    return int(dl.L - uint32_t(uint64_t(p) - div_l(uint64_t(p), dl) * dl.L));
+}
+__device__ __forceinline__ idx_t read_of(idx_t p, const DivL& dl) { return idx_t(div_l(uint64_t(p), dl)); }
+
 // 32-byte sectors spanned by `bytes` bytes at p
 __device__ __forceinline__ uint32_t sectors_of(const void* p, size_t bytes) {
     const uintptr_t a = reinterpret_cast<uintptr_t>(p);
@@ -328,7 +334,8 @@ __device__ __forceinline__ uint32_t cmp_sectors(const uint64_t* pk, idx_t p) {
 
 // Rows [first, end) of each chain's index that start with its pattern, searched within
 // [lo, hi): lower and upper bounds of both chains advance together (four independent searches).
-__device__ __forceinline__ void sa_bounds2(const FmView* f0, const FmView* f1, int L, const uint64_t (&P0)[kScanWords],
+__device__ __forceinline__ void sa_bounds2(const FmView* f0, const FmView* f1, const DivL& dl,
+                                           const uint64_t (&P0)[kScanWords],
                                            const uint64_t (&P1)[kScanWords], int t, const idx_t (&lo)[2],
                                            const idx_t (&hi)[2], idx_t (&first)[2], idx_t (&end)[2],
                                            Tally& probes) {
@@ -346,14 +353,14 @@ __device__ __forceinline__ void sa_bounds2(const FmView* f0, const FmView* f1, i
             const uint64_t (&P)[kScanWords] = q ? P1 : P0;
             if (a0[q] < a1[q]) {
                 const idx_t ma = a0[q] + (a1[q] - a0[q]) / 2;
-                const int c = cmp_row(fq[q]->pk, pa[q], L - int(pa[q] % idx_t(L)), P, t);
+                const int c = cmp_row(fq[q]->pk, pa[q], suffix_len(pa[q], dl), P, t);
                 if (c < 0) a0[q] = ma + 1;
                 else a1[q] = ma;
                 probes.add(2, 1 + cmp_sectors(fq[q]->pk, pa[q]));
             }
             if (b0[q] < b1[q]) {
                 const idx_t mb = b0[q] + (b1[q] - b0[q]) / 2;
-                const int c = cmp_row(fq[q]->pk, pb[q], L - int(pb[q] % idx_t(L)), P, t);
+                const int c = cmp_row(fq[q]->pk, pb[q], suffix_len(pb[q], dl), P, t);
                 if (c <= 0) b0[q] = mb + 1;
                 else b1[q] = mb;
                 probes.add(2, 1 + cmp_sectors(fq[q]->pk, pb[q]));
@@ -426,6 +433,7 @@ struct SlotsStack {    // wide tier: the slot's candidate stack
 template <class Slots>
 __device__ __forceinline__ bool scan_pair(const SearchArgs& A, const FmView* fm, idx_t self, int k0, int k1,
                                           int (&n)[2], int32_t& olp, Tally& probes, const Slots& slots) {
+    if (!fm[0].isa || !fm[1].isa) return false;      // group intervals need the inverse SA: walk
     const int L = A.L, t = A.t, k = A.seed_k, M = L - t;
     const int tb = t < 32 * kScanWords ? t : 32 * kScanWords;    // bases bisected; the rest checked per row
     uint64_t P0[kScanWords], P1[kScanWords];
@@ -458,7 +466,7 @@ __device__ __forceinline__ bool scan_pair(const SearchArgs& A, const FmView* fm,
         if (hi[0] < lo[0]) hi[0] = lo[0];
         if (hi[1] < lo[1]) hi[1] = lo[1];
     }
-    sa_bounds2(f0, f1, L, P0, P1, tb, lo, hi, first, end, probes);
+    sa_bounds2(f0, f1, A.dl, P0, P1, tb, lo, hi, first, end, probes);
     if (A.sa_seed == 2) {
         // The window holds the answer for every key present in the index; for any other key it
         // is checked: the rows just outside the window must not start with P_t.
@@ -470,12 +478,12 @@ __device__ __forceinline__ bool scan_pair(const SearchArgs& A, const FmView* fm,
             const uint64_t (&P)[kScanWords] = q ? P1 : P0;
             if (first[q] == lo[q] && lo[q] > 0) {
                 const idx_t p = __ldg(fa.sa + lo[q] - 1);
-                ok = ok && cmp_row(fa.pk, p, L - int(p % idx_t(L)), P, tb) < 0;
+                ok = ok && cmp_row(fa.pk, p, suffix_len(p, A.dl), P, tb) < 0;
                 probes.add(2, 1 + cmp_sectors(fa.pk, p));
             }
             if (end[q] == hi[q] && hi[q] < n_rows) {
                 const idx_t p = __ldg(fa.sa + hi[q]);
-                ok = ok && cmp_row(fa.pk, p, L - int(p % idx_t(L)), P, tb) > 0;
+                ok = ok && cmp_row(fa.pk, p, suffix_len(p, A.dl), P, tb) > 0;
                 probes.add(2, 1 + cmp_sectors(fa.pk, p));
             }
         }
@@ -496,7 +504,7 @@ __device__ __forceinline__ bool scan_pair(const SearchArgs& A, const FmView* fm,
         uint64_t mk0 = 0, mk1 = 0, mk2 = 0, mk3 = 0;              // depths with candidates (o < 256)
         for (idx_t row = first[q]; row < end[q]; ++row) {
             const idx_t p = __ldg(fa.sa + row);
-            const idx_t rp = p / idx_t(L);
+            const idx_t rp = read_of(p, A.dl);
             const int o = int(p - rp * idx_t(L));
             probes.add(2, 1);
             if (o >= M || !prefix_matches(fa.pk, size_t(rp) * L, pks, src - o, o, cmpl, probes.sectors)) continue;
@@ -1039,7 +1047,7 @@ __device__ __forceinline__ int reduce_sorted(const SearchArgs& A, const WarpScra
         const FmView& fb = A.fm[cand_index(type)];
         for (idx_t row = ll; row <= uu; ++row) {
             const idx_t p = __ldg(fb.sa + row);
-            const idx_t rp = p / idx_t(L);
+            const idx_t rp = read_of(p, A.dl);
             const uint32_t sec = continuation<W>(A, type, rp, d, S.r_k + red + m, S.r_plane);
             S.r_id[red + m] = rp;
             S.r_meta[red + m] = mt;
@@ -1158,7 +1166,7 @@ __device__ __forceinline__ bool scan_planes(const SearchArgs& A, const FmView* f
         if (hi[0] < lo[0]) hi[0] = lo[0];
         if (hi[1] < lo[1]) hi[1] = lo[1];
     }
-    sa_bounds2(f0, f1, L, P0, P1, tb, lo, hi, first, end, probes);
+    sa_bounds2(f0, f1, A.dl, P0, P1, tb, lo, hi, first, end, probes);
     if (A.sa_seed == 2) {
         const idx_t n_rows = A.num_reads * idx_t(L);
         bool ok = true;
@@ -1168,12 +1176,12 @@ __device__ __forceinline__ bool scan_planes(const SearchArgs& A, const FmView* f
             const uint64_t (&P)[kScanWords] = q ? P1 : P0;
             if (first[q] == lo[q] && lo[q] > 0) {
                 const idx_t p = __ldg(fa.sa + lo[q] - 1);
-                ok = ok && cmp_row(fa.pk, p, L - int(p % idx_t(L)), P, tb) < 0;
+                ok = ok && cmp_row(fa.pk, p, suffix_len(p, A.dl), P, tb) < 0;
                 probes.add(2, 1 + cmp_sectors(fa.pk, p));
             }
             if (end[q] == hi[q] && hi[q] < n_rows) {
                 const idx_t p = __ldg(fa.sa + hi[q]);
-                ok = ok && cmp_row(fa.pk, p, L - int(p % idx_t(L)), P, tb) > 0;
+                ok = ok && cmp_row(fa.pk, p, suffix_len(p, A.dl), P, tb) > 0;
                 probes.add(2, 1 + cmp_sectors(fa.pk, p));
             }
         }
@@ -1194,7 +1202,7 @@ __device__ __forceinline__ bool scan_planes(const SearchArgs& A, const FmView* f
         const size_t src = size_t(self) * L + size_t(L - t);
         for (idx_t row = first[q]; row < end[q]; ++row) {
             const idx_t p = __ldg(fa.sa + row);
-            const idx_t rp = p / idx_t(L);
+            const idx_t rp = read_of(p, A.dl);
             const int o = int(p - rp * idx_t(L));
             probes.add(2, 1);
             if (o >= M || !prefix_matches(fa.pk, size_t(rp) * L, pks, src - o, o, cmpl, probes.sectors)) continue;

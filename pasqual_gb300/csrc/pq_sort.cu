@@ -17,6 +17,7 @@
 // 268 bases) are sorted by prefix doubling on 29-base 64-bit keys instead: ranks by
 // (rank(p), rank(p+h) or "empty" past the read end) for h = 29, 58, 116, ...
 #include "pq_sort.cuh"
+#include "pq_index.cuh"
 
 #include <algorithm>
 #include <vector>
@@ -1382,21 +1383,27 @@ constexpr int kBucketBases = 6;
 constexpr int kBuckets = (1 << (2 * kBucketBases)) * 8;
 constexpr int kCkTile = 4096;
 
-__device__ __forceinline__ uint32_t bucket_of(const uint64_t* __restrict__ pk, size_t p, idx_t L) {
-    const int m = int(L - idx_t(p % L));
+__device__ __forceinline__ uint32_t bucket_of(const uint64_t* __restrict__ pk, size_t p, const DivL& dl) {
+    const int m = int(dl.L - uint32_t(p - div_l(p, dl) * dl.L));
     const int w = m < kBucketBases ? m : kBucketBases;
     const uint32_t pre = uint32_t(window(pk, p) >> (64 - 2 * kBucketBases)) & (~0u << (2 * (kBucketBases - w)));
     return (pre << 3) | uint32_t(w);
 }
 
-__global__ void k_bucket_hist(const uint64_t* __restrict__ pk, size_t n, idx_t L, unsigned long long* __restrict__ hist) {
+// every position's bucket (kept for the chunk passes, which then read 2 bytes a position) and the
+// bucket histogram
+__global__ void k_bucket_hist(const uint64_t* __restrict__ pk, size_t n, DivL dl, uint16_t* __restrict__ bid,
+                              unsigned long long* __restrict__ hist) {
     const size_t stride = size_t(gridDim.x) * blockDim.x;
-    for (size_t p = size_t(blockIdx.x) * blockDim.x + threadIdx.x; p < n; p += stride)
-        atomicAdd(&hist[bucket_of(pk, p, L)], 1ull);
+    for (size_t p = size_t(blockIdx.x) * blockDim.x + threadIdx.x; p < n; p += stride) {
+        const uint32_t b = bucket_of(pk, p, dl);
+        bid[p] = uint16_t(b);
+        atomicAdd(&hist[b], 1ull);
+    }
 }
 
 // per tile of 4096 positions: how many fall in buckets [lo, hi)
-__global__ void __launch_bounds__(256) k_chunk_count(const uint64_t* __restrict__ pk, size_t n, idx_t L, uint32_t lo,
+__global__ void __launch_bounds__(256) k_chunk_count(const uint16_t* __restrict__ bid, size_t n, uint32_t lo,
                                                     uint32_t hi, unsigned long long* __restrict__ tcnt) {
     __shared__ unsigned red[8];
     const size_t t0 = size_t(blockIdx.x) * kCkTile;
@@ -1404,7 +1411,7 @@ __global__ void __launch_bounds__(256) k_chunk_count(const uint64_t* __restrict_
     for (int j = threadIdx.x; j < kCkTile; j += 256) {
         const size_t p = t0 + j;
         if (p < n) {
-            const uint32_t b = bucket_of(pk, p, L);
+            const uint32_t b = bid[p];
             c += (b >= lo && b < hi) ? 1u : 0u;
         }
     }
@@ -1420,7 +1427,7 @@ __global__ void __launch_bounds__(256) k_chunk_count(const uint64_t* __restrict_
 
 // the positions of a chunk in text order (tile offsets from the exclusive scan of the counts)
 template <class V>
-__global__ void __launch_bounds__(256) k_chunk_write(const uint64_t* __restrict__ pk, size_t n, idx_t L, uint32_t lo,
+__global__ void __launch_bounds__(256) k_chunk_write(const uint16_t* __restrict__ bid, size_t n, uint32_t lo,
                                                     uint32_t hi, const unsigned long long* __restrict__ toff,
                                                     V* __restrict__ list) {
     __shared__ unsigned wsum[8];
@@ -1433,7 +1440,7 @@ __global__ void __launch_bounds__(256) k_chunk_write(const uint64_t* __restrict_
         const size_t p = t0 + j0 + threadIdx.x;
         bool in = false;
         if (p < n) {
-            const uint32_t b = bucket_of(pk, p, L);
+            const uint32_t b = bid[p];
             in = b >= lo && b < hi;
         }
         const unsigned bal = __ballot_sync(0xffffffffu, in);
@@ -1452,16 +1459,16 @@ __global__ void __launch_bounds__(256) k_chunk_write(const uint64_t* __restrict_
 }
 
 template <class V>
-__global__ void k_init_keys_list(const uint64_t* __restrict__ pk, const V* __restrict__ list, size_t m, idx_t L,
+__global__ void k_init_keys_list(const uint64_t* __restrict__ pk, const V* __restrict__ list, size_t m, DivL dl,
                                  uint32_t* __restrict__ key) {
     const size_t stride = size_t(gridDim.x) * blockDim.x;
     for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < m; i += stride) {
         const size_t p = size_t(list[i]);
-        key[i] = make_key<uint32_t>(window(pk, p), int(L - idx_t(p % L)));
+        key[i] = make_key<uint32_t>(window(pk, p), int(dl.L - uint32_t(p - div_l(p, dl) * dl.L)));
     }
 }
 
-static size_t chunk_parts(size_t n, size_t cap, size_t (&b)[10]) {
+static size_t chunk_parts(size_t n, size_t cap, size_t (&b)[11]) {
     const size_t ntiles = (n + kCkTile - 1) / kCkTile;
     b[0] = cap * sizeof(uint64_t);                    // ka (32-bit head keys; 64-bit for big groups)
     b[1] = cap * sizeof(uint64_t);                    // kb (also the group lists)
@@ -1473,28 +1480,29 @@ static size_t chunk_parts(size_t n, size_t cap, size_t (&b)[10]) {
     b[7] = (ntiles + 1) * sizeof(unsigned long long); // tile counts / offsets
     b[8] = (size_t(kBuckets) + 8) * sizeof(unsigned long long);
     b[9] = n;                                         // BWT symbols of the refined rows
+    b[10] = n * sizeof(uint16_t);                     // every position's 6-base bucket
     size_t t = 0;
     for (size_t x : b) t += al(x);
     return t + 1024;
 }
 
 size_t suffix_sort_chunked_tmp_bytes(size_t n, size_t cap) {
-    size_t b[10];
+    size_t b[11];
     return chunk_parts(n, cap, b);
 }
 
 int suffix_sort_chunked(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa, size_t cap, void* tmp,
                         size_t tmp_bytes, cudaStream_t st, const uint8_t** bwt_out, uint64_t* pk_out,
-                        idx_t* isa_out, idx_t isa_m) {
+                        idx_t* isa_out, idx_t isa_m, idx_t* kstart, idx_t* kend, int kmer_k) {
     if (bwt_out) *bwt_out = nullptr;
     const size_t n = size_t(num_reads) * size_t(L);
     if (n == 0) return 0;
     if (cap < 2 || cap >= (size_t(1) << 31)) return int(cudaErrorInvalidValue);
-    size_t b[10];
+    size_t b[11];
     if (tmp_bytes < chunk_parts(n, cap, b)) return int(cudaErrorInvalidValue);
     char* q = static_cast<char*>(tmp);
-    char* part[10];
-    for (int i = 0; i < 10; ++i) {
+    char* part[11];
+    for (int i = 0; i < 11; ++i) {
         part[i] = q;
         q += al(b[i]);
     }
@@ -1509,11 +1517,13 @@ int suffix_sort_chunked(const uint8_t* reads, idx_t num_reads, int L, int dir, i
     unsigned long long* tcnt = reinterpret_cast<unsigned long long*>(part[7]);
     unsigned long long* hist = reinterpret_cast<unsigned long long*>(part[8]);
     unsigned long long* counters = hist + kBuckets;
+    uint16_t* bid = reinterpret_cast<uint16_t*>(part[10]);
+    const DivL dl = make_divl(uint32_t(L));
     const size_t nwords = n / 32 + 4;
     const size_t ntiles = (n + kCkTile - 1) / kCkTile;
     { k_pack_text<<<grid_for(nwords, 256), 256, 0, st>>>(reads, n, idx_t(L), dir, nwords, pk); note_launch(); }
     cudaMemsetAsync(hist, 0, size_t(kBuckets) * sizeof(unsigned long long), st);
-    { k_bucket_hist<<<grid_for(n, 256), 256, 0, st>>>(pk, n, idx_t(L), hist); note_launch(); }
+    { k_bucket_hist<<<grid_for(n, 256), 256, 0, st>>>(pk, n, dl, bid, hist); note_launch(); }
     std::vector<unsigned long long> h(kBuckets);
     cudaMemcpyAsync(h.data(), hist, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
     cudaError_t e = cudaStreamSynchronize(st);
@@ -1527,12 +1537,12 @@ int suffix_sort_chunked(const uint8_t* reads, idx_t num_reads, int L, int dir, i
         while (hi < uint32_t(kBuckets) && m + h[hi] <= cap) m += h[hi++];
         if (hi == lo) return int(cudaErrorNotSupported);          // one bucket larger than a chunk
         if (m) {
-            { k_chunk_count<<<unsigned(ntiles), 256, 0, st>>>(pk, n, idx_t(L), lo, hi, tcnt); note_launch(); }
+            { k_chunk_count<<<unsigned(ntiles), 256, 0, st>>>(bid, n, lo, hi, tcnt); note_launch(); }
             { k_scan_small<<<1, 1024, 0, st>>>(tcnt, ntiles); note_launch(); }
-            { k_chunk_write<idx_t><<<unsigned(ntiles), 256, 0, st>>>(pk, n, idx_t(L), lo, hi, tcnt, va0); note_launch(); }
+            { k_chunk_write<idx_t><<<unsigned(ntiles), 256, 0, st>>>(bid, n, lo, hi, tcnt, va0); note_launch(); }
             uint32_t* ka = reinterpret_cast<uint32_t*>(ka0);
             uint32_t* kb = reinterpret_cast<uint32_t*>(kb0);
-            { k_init_keys_list<idx_t><<<grid_for(m, 256), 256, 0, st>>>(pk, va0, m, idx_t(L), ka); note_launch(); }
+            { k_init_keys_list<idx_t><<<grid_for(m, 256), 256, 0, st>>>(pk, va0, m, dl, ka); note_launch(); }
             idx_t* va = va0;
             idx_t* vb = vb0;
             int rc = radix_sort_pairs<uint32_t, idx_t>(&ka, &va, &kb, &vb, m, 0, 32, rtmp, radix_tmp_bytes(m), st, false);
@@ -1547,6 +1557,12 @@ int suffix_sort_chunked(const uint8_t* reads, idx_t num_reads, int L, int dir, i
                 if (rc < 0) return int(cudaErrorNotSupported);      // would need prefix doubling
             }
             { k_copy_vals<idx_t><<<grid_for(m, 256), 256, 0, st>>>(va, m, sa + offset); note_launch(); }
+            // the chunk's keys are still sorted and aligned with its rows (the refinement only
+            // reorders rows of equal keys): its k-mers' row ranges
+            if (kstart && kmer_k >= 6 && kmer_k <= kSortKeyBases) {
+                const cudaError_t ek = kmer_table_from_keys(ka, m, offset, kmer_k, kstart, kend, st);
+                if (ek != cudaSuccess) return int(ek);
+            }
         }
         offset += m;
         lo = hi;

@@ -27,9 +27,12 @@ int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa
 // consecutive buckets sorted in chunks of at most cap (< 2^31) suffixes.  Returns
 // cudaErrorNotSupported if one bucket exceeds cap.  bwt_out and pk_out as for suffix_sort.
 size_t suffix_sort_chunked_tmp_bytes(size_t n, size_t cap);
+// kstart/kend (cleared by the caller), when given, receive the k-mer table (6 <= k <= 14) from each
+// chunk's sorted keys.
 int suffix_sort_chunked(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa, size_t cap, void* tmp,
                         size_t tmp_bytes, cudaStream_t st, const uint8_t** bwt_out = nullptr,
-                        uint64_t* pk_out = nullptr, idx_t* isa_out = nullptr, idx_t isa_m = 0);
+                        uint64_t* pk_out = nullptr, idx_t* isa_out = nullptr, idx_t isa_m = 0,
+                        idx_t* kstart = nullptr, idx_t* kend = nullptr, int kmer_k = 0);
 
 // Per-read seeds from a k-mer table (pq_index.cu).
 cudaError_t read_seeds(const uint8_t* reads, idx_t num_reads, int L, int dir, int k, const idx_t* kstart,
