@@ -244,6 +244,12 @@ PQ_API int pq_learned_keys (pq_ctx * ctx, int dir, uint32_t * keys, pq_idx * fir
  * These are the kernels the training runs. */
 PQ_API int pq_mlp_forward (const float *params, const float *x, int n, float *y);
 PQ_API int pq_mlp_backward (const float *params, const float *x, const float *dy, int n, float *grad);
+/* One step of the training's joint phase on one network (host arrays): the gradient of the mean
+ * squared error sum_i (mlp(x[i]) - target[i])^2 / n, then Adam (beta1 0.9, beta2 0.999, eps 1e-8,
+ * learning rate lr, bias correction for step number `step` >= 1) on all 193 parameters; params (one
+ * 196-float record) and the moment estimates m1, m2 (193 each) are updated in place. */
+PQ_API int pq_mlp_adam_step (float *params, float *m1, float *m2, const float *x, const float *target, int n,
+                             int step, float lr);
 
 /* ---- Queued search over several read sets (no counterpart in the reference) ----------------
  *

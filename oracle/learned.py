@@ -49,6 +49,25 @@ def mlp_backward(params: np.ndarray, x: np.ndarray, dy: np.ndarray) -> np.ndarra
     return np.concatenate([g_w1, g_b1, g_w2, [g_b2]])
 
 
+def adam_step(params: np.ndarray, m1: np.ndarray, m2: np.ndarray, x: np.ndarray, target: np.ndarray,
+              step: int, lr: float):
+    """One step of the learned index's joint training phase in float64: gradient of the mean squared
+    error sum_i (mlp(x_i) - target_i)^2 / n, then Adam (beta1 0.9, beta2 0.999, eps 1e-8, bias
+    correction for step number `step`) on the 193 parameters.  Returns (params, m1, m2)."""
+    p = np.asarray(params, np.float64).copy()
+    n = len(x)
+    y = mlp_forward(p, x)
+    dy = 2.0 * (y - np.asarray(target, np.float64)) / n
+    g = mlp_backward(p, x, dy)
+    k = 3 * HIDDEN + 1
+    a = 0.9 * np.asarray(m1, np.float64)[:k] + 0.1 * g
+    b = 0.999 * np.asarray(m2, np.float64)[:k] + 0.001 * g * g
+    mh = a / (1.0 - 0.9 ** step)
+    vh = b / (1.0 - 0.999 ** step)
+    p[:k] -= lr * mh / (np.sqrt(vh) + 1e-8)
+    return p, a, b
+
+
 def finite_difference(params: np.ndarray, x: np.ndarray, dy: np.ndarray, eps: float = 1e-6) -> np.ndarray:
     """Central differences of sum_i dy_i * mlp(x_i) with respect to the 193 parameters."""
     p = np.asarray(params, np.float64).copy()

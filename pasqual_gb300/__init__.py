@@ -22,7 +22,7 @@ import numpy as np
 from . import build as _build
 
 __all__ = ["Pasqual", "Graph", "PQError", "load_library", "library_path", "EXPORTS", "mlp_forward",
-           "mlp_backward", "LearnedInfo", "overlaps_batched", "autotune_batched"]
+           "mlp_backward", "mlp_adam_step", "LearnedInfo", "overlaps_batched", "autotune_batched"]
 
 PQ_ERRORS = {1: "PQ_ERR_ARG", 2: "PQ_ERR_CUDA", 3: "PQ_ERR_NOMEM", 4: "PQ_ERR_TOO_MANY_EDGES",
              5: "PQ_ERR_STATE", 6: "PQ_ERR_CAPACITY", 7: "PQ_ERR_INTERNAL"}
@@ -35,7 +35,7 @@ EXPORTS = ["pq_idx_bytes", "pq_create", "pq_destroy", "pq_last_error", "pq_set_r
            "pq_suffix_sort_static", "pq_learned_build", "pq_learned_get_info", "pq_learned_export",
            "pq_learned_predict", "pq_learned_keys", "pq_mlp_forward", "pq_mlp_backward",
            "pq_overlaps_batched", "pq_set_batch_plan", "pq_get_batch_stats", "pq_autotune_batched",
-           "pq_set_sort_chunk", "pq_get_search_traffic", "pq_get_sort_seeds"]
+           "pq_set_sort_chunk", "pq_get_search_traffic", "pq_get_sort_seeds", "pq_mlp_adam_step"]
 
 
 # The reference's own entry points served by the same library (include/pasqual_gb300_dropin.h).
@@ -103,6 +103,7 @@ def load_library(width: int = 32) -> ct.CDLL:
         "pq_set_sort_chunk": (c_int, [vp, ct.c_uint64]),
         "pq_get_search_traffic": (c_int, [vp, vp, vp]),
         "pq_get_sort_seeds": (c_int, [vp, c_int, vp, vp, vp]),
+        "pq_mlp_adam_step": (c_int, [vp, vp, vp, vp, vp, c_int, c_int, ct.c_float]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -153,6 +154,21 @@ def mlp_backward(params: np.ndarray, x: np.ndarray, dy: np.ndarray, width: int =
     if rc != 0:
         raise PQError(rc, "pq_mlp_backward")
     return g
+
+
+def mlp_adam_step(params: np.ndarray, m1: np.ndarray, m2: np.ndarray, x: np.ndarray, target: np.ndarray,
+                  step: int, lr: float, width: int = 32):
+    """One joint-phase training step of one network on the GPU; returns (params, m1, m2) updated."""
+    lib = load_library(width)
+    p = np.ascontiguousarray(params, np.float32).copy()
+    a = np.ascontiguousarray(m1, np.float32).copy()
+    b = np.ascontiguousarray(m2, np.float32).copy()
+    x = np.ascontiguousarray(x, np.float32)
+    t = np.ascontiguousarray(target, np.float32)
+    rc = lib.pq_mlp_adam_step(_p(p), _p(a), _p(b), _p(x), _p(t), len(x), int(step), float(lr))
+    if rc != 0:
+        raise PQError(rc, "pq_mlp_adam_step")
+    return p, a, b
 
 
 BATCH_GRAPH = 1

@@ -1060,6 +1060,33 @@ int pq_mlp_backward(const float* params, const float* x, const float* dy, int n,
     return rc;
 }
 
+int pq_mlp_adam_step(float* params, float* m1, float* m2, const float* x, const float* target, int n, int step,
+                     float lr) {
+    if (!params || !m1 || !m2 || n <= 0 || !x || !target || step < 1) return PQ_ERR_ARG;
+    DevBuf dp, dm1, dm2, dx, dt;
+    if (dp.ensure(pq::kLxStride * 4) || dm1.ensure(pq::kLxParams * 4) || dm2.ensure(pq::kLxParams * 4) ||
+        dx.ensure(size_t(n) * 4) || dt.ensure(size_t(n) * 4))
+        return PQ_ERR_NOMEM;
+    int rc = PQ_OK;
+    if (cudaMemcpy(dp.p, params, pq::kLxStride * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(dm1.p, m1, pq::kLxParams * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(dm2.p, m2, pq::kLxParams * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(dx.p, x, size_t(n) * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(dt.p, target, size_t(n) * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+        pq::mlp_adam_step(dp.as<float>(), dm1.as<float>(), dm2.as<float>(), dx.as<float>(), dt.as<float>(), n, step,
+                          lr, 0) != cudaSuccess ||
+        cudaMemcpy(params, dp.p, pq::kLxParams * 4, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(m1, dm1.p, pq::kLxParams * 4, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(m2, dm2.p, pq::kLxParams * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+        rc = PQ_ERR_CUDA;
+    dp.release();
+    dm1.release();
+    dm2.release();
+    dx.release();
+    dt.release();
+    return rc;
+}
+
 // ---------------------------------------------------------------------------- queued search
 
 static uint64_t fnv1a(const void* p, size_t n) {

@@ -31,6 +31,7 @@ static inline unsigned grid_cap(size_t work, int threads) {
 
 constexpr int kTileRows = 4096;      // 256 threads x 16 rows
 constexpr int kTrainThreads = 256;   // samples per training step
+constexpr float kJointLr = 1e-3f;    // learning rate of the joint phase (all parameters)
 
 // ---------------------------------------------------------------------------------- keys
 
@@ -204,6 +205,66 @@ __device__ __forceinline__ void mlp_backward_block(const float* w1, const float*
     __syncthreads();
 }
 
+// One Adam step (beta1 0.9, beta2 0.999, eps 1e-8) of the block on k parameters p with gradient g;
+// p1 = 0.9^t and p2 = 0.999^t for this step t (bias correction).
+__device__ __forceinline__ void adam_params(float* p, float* m1, float* m2, const float* g, int k, float lr, float p1,
+                                            float p2) {
+    for (int i = threadIdx.x; i < k; i += blockDim.x) {
+        const float gi = g[i];
+        m1[i] = 0.9f * m1[i] + 0.1f * gi;
+        m2[i] = 0.999f * m2[i] + 0.001f * gi * gi;
+        const float mh = m1[i] / (1.f - p1), vh = m2[i] / (1.f - p2);
+        p[i] -= lr * mh / (sqrtf(vh) + 1e-8f);
+    }
+}
+
+// Mean squared error of the network (parameters P in shared memory) on batches of 256 samples
+// (x, target): sg = d loss / d y of every sample, and the gradient of the loss in acc[0..192].
+__device__ __forceinline__ void mse_gradient(const float* P, const float* x, const float* tgt, int n, float* sx,
+                                             float* sg, float* acc, float (*part)[3][kLxHidden], float* red) {
+    const int tid = threadIdx.x;
+    if (tid < kLxParams) acc[tid] = 0.f;
+    __syncthreads();
+    for (int c = 0; c < n; c += 256) {
+        const int nb = n - c < 256 ? n - c : 256;
+        if (tid < nb) {
+            const float xi = x[c + tid];
+            const float y = mlp_forward_smem(P, P + kLxHidden, P + 2 * kLxHidden, P[3 * kLxHidden], xi);
+            sx[tid] = xi;
+            sg[tid] = 2.f * (y - tgt[c + tid]) / float(n);
+        }
+        __syncthreads();
+        mlp_backward_block(P, P + kLxHidden, P + 2 * kLxHidden, sx, sg, nb, acc, part, red);
+    }
+}
+
+// One training step of one network on its own (the step the joint phase of k_lx_train takes):
+// gradient of the mean squared error on (x, target), then Adam on all 193 parameters; par
+// (one kLxStride record), m1, m2 (193 each) are read and written; t is the 1-based step number.
+__global__ void __launch_bounds__(256) k_mlp_adam_step(float* __restrict__ par, float* __restrict__ m1g,
+                                                      float* __restrict__ m2g, const float* __restrict__ x,
+                                                      const float* __restrict__ tgt, int n, int t, float lr) {
+    __shared__ float P[kLxParams], m1[kLxParams], m2[kLxParams], acc[kLxParams];
+    __shared__ float sx[256], sg[256];
+    __shared__ float part[4][3][kLxHidden];
+    __shared__ float red[8];
+    const int tid = threadIdx.x;
+    if (tid < kLxParams) {
+        P[tid] = par[tid];
+        m1[tid] = m1g[tid];
+        m2[tid] = m2g[tid];
+    }
+    __syncthreads();
+    mse_gradient(P, x, tgt, n, sx, sg, acc, part, red);
+    adam_params(P, m1, m2, acc, kLxParams, lr, powf(0.9f, float(t)), powf(0.999f, float(t)));
+    __syncthreads();
+    if (tid < kLxParams) {
+        par[tid] = P[tid];
+        m1g[tid] = m1[tid];
+        m2g[tid] = m2[tid];
+    }
+}
+
 __global__ void k_mlp_forward(const float* __restrict__ par, const float* __restrict__ x, int n,
                               float* __restrict__ y) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -273,6 +334,9 @@ __global__ void __launch_bounds__(kTrainThreads) k_lx_train(const uint32_t* __re
     __shared__ float part[4][3][H];
     __shared__ float red[8];
     __shared__ float s_b2, s_sigma;
+    __shared__ float jp[kLxParams], jq[kLxParams], jm1[kLxParams], jm2[kLxParams];
+    __shared__ float ex[kTrainThreads], et[kTrainThreads];
+    __shared__ float s_loss0, s_loss1;
     const int s = blockIdx.x, tid = threadIdx.x;
     const unsigned long long ds = dsi[s], cnt = dsi[s + 1] - ds;
     SegData sd;
@@ -355,13 +419,70 @@ __global__ void __launch_bounds__(kTrainThreads) k_lx_train(const uint32_t* __re
         if (tid == 0) s_b2 = v[0];
         __syncthreads();
     }
+    // Joint phase: every parameter (knot slopes and offsets w1, b1 as well as w2, b2) by Adam on the
+    // same loss, from the knot-value solution; kept only if it lowers the squared error on an even
+    // sample of the segment's keys.
+    if (tid < H) {
+        jp[tid] = w1[tid];
+        jp[H + tid] = b1[tid];
+        jp[2 * H + tid] = w2[tid];
+    }
+    if (tid == 0) jp[3 * H] = s_b2;
+    if (tid < kLxParams) {
+        jq[tid] = 0.f;
+        jm1[tid] = 0.f;
+        jm2[tid] = 0.f;
+    }
+    if (cnt) {
+        const unsigned long long i = ds + ((unsigned long long)tid * cnt + cnt / 2) / kTrainThreads;
+        ex[tid] = sd.x_of(i);
+        et[tid] = sd.target(i, ex[tid]) * inv_sigma;
+    }
+    __syncthreads();
+    auto sample_loss = [&](float* out_loss) {
+        float q = 0.f;
+        if (cnt) {
+            const float y = mlp_forward_smem(jp, jp + H, jp + 2 * H, jp[3 * H], ex[tid]);
+            q = (y - et[tid]) * (y - et[tid]);
+        }
+        for (int o = 16; o > 0; o >>= 1) q += __shfl_down_sync(0xffffffffu, q, o);
+        if ((tid & 31) == 0) red[tid >> 5] = q;
+        __syncthreads();
+        if (tid == 0) {
+            float t = 0.f;
+            for (int w = 0; w < 8; ++w) t += red[w];
+            *out_loss = t;
+        }
+        __syncthreads();
+    };
+    sample_loss(&s_loss0);
+    if (tid < kLxParams) jq[tid] = jp[tid];
+    const int steps2 = steps / 2;
+    float q1 = 1.f, q2 = 1.f;
+    for (int step = 0; step < steps2 && cnt; ++step) {
+        const unsigned long long i = ds + mix32(~seed ^ mix32(uint32_t(s) * 0x2545f491u + uint32_t(step) * 0x9e3779b9u + uint32_t(tid))) % cnt;
+        const float x = sd.x_of(i);
+        sx[tid] = x;
+        const float y = mlp_forward_smem(jp, jp + H, jp + 2 * H, jp[3 * H], x);
+        sg[tid] = 2.f * (y - sd.target(i, x) * inv_sigma) / float(kTrainThreads);
+        if (tid < kLxParams) acc[tid] = 0.f;
+        __syncthreads();
+        mlp_backward_block(jp, jp + H, jp + 2 * H, sx, sg, kTrainThreads, acc, part, red);
+        q1 *= 0.9f;
+        q2 *= 0.999f;
+        adam_params(jp, jm1, jm2, acc, kLxParams, kJointLr * (1.f - float(step) / float(steps2)), q1, q2);
+        __syncthreads();
+    }
+    sample_loss(&s_loss1);
+    if (!(s_loss1 < s_loss0) && tid < kLxParams) jp[tid] = jq[tid];     // keep the knot-value solution
+    __syncthreads();
     float* out = par + size_t(s) * kLxStride;
     if (tid < H) {
-        out[tid] = w1[tid];
-        out[H + tid] = b1[tid];
-        out[2 * H + tid] = w2[tid] * s_sigma;
+        out[tid] = jp[tid];
+        out[H + tid] = jp[H + tid];
+        out[2 * H + tid] = jp[2 * H + tid] * s_sigma;
     }
-    if (tid == 0) out[3 * H] = s_b2 * s_sigma;
+    if (tid == 0) out[3 * H] = jp[3 * H] * s_sigma;
     if (tid >= kLxParams && tid < kLxStride) out[tid] = 0.f;
 }
 
@@ -495,6 +616,12 @@ cudaError_t mlp_forward(const float* par, const float* x, int n, float* y, cudaS
 
 cudaError_t mlp_backward(const float* par, const float* x, const float* dy, int n, float* grad, cudaStream_t st) {
     { k_mlp_backward<<<1, 256, 0, st>>>(par, x, dy, n, grad); note_launch(); }
+    return cudaGetLastError();
+}
+
+cudaError_t mlp_adam_step(float* par, float* m1, float* m2, const float* x, const float* tgt, int n, int t, float lr,
+                          cudaStream_t st) {
+    { k_mlp_adam_step<<<1, 256, 0, st>>>(par, m1, m2, x, tgt, n, t, lr); note_launch(); }
     return cudaGetLastError();
 }
 

@@ -36,5 +36,8 @@ cudaError_t lx_predict_keys(const LearnedView& v, const uint32_t* keys, size_t n
 // inputs, and the gradient of sum_i dy_i * y_i with respect to the 193 parameters.
 cudaError_t mlp_forward(const float* par, const float* x, int n, float* y, cudaStream_t st);
 cudaError_t mlp_backward(const float* par, const float* x, const float* dy, int n, float* grad, cudaStream_t st);
+// one training step of one network: Adam on the mean squared error of (x, tgt) (t = step number)
+cudaError_t mlp_adam_step(float* par, float* m1, float* m2, const float* x, const float* tgt, int n, int t, float lr,
+                          cudaStream_t st);
 
 }  // namespace pq

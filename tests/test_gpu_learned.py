@@ -37,6 +37,29 @@ def test_mlp_kernels_match_oracle(n):
     np.testing.assert_allclose(g, ref, rtol=GRAD_RTOL, atol=GRAD_RTOL * np.abs(ref).max())
 
 
+@pytest.mark.parametrize("step", [1, 7])
+def test_adam_step_matches_oracle(step):
+    """One step of the training's joint phase (all 193 parameters, w1 and b1 included): the GPU's
+    mean-squared-error gradient and Adam update against the float64 oracle, twice in a row."""
+    rng = np.random.default_rng(step)
+    p = _params(rng)
+    k = 3 * learned.HIDDEN + 1
+    m1 = rng.normal(0.0, 1e-3, k).astype(np.float32)
+    m2 = rng.uniform(1e-8, 1e-6, k).astype(np.float32)
+    x = rng.uniform(0.0, 1.0, 256).astype(np.float32)
+    tgt = rng.normal(0.0, 0.5, 256).astype(np.float32)
+    gp, ga, gb = p, m1, m2
+    rp, ra, rb = p.astype(np.float64), m1.astype(np.float64), m2.astype(np.float64)
+    for t in (step, step + 1):
+        gp, ga, gb = pq.mlp_adam_step(gp, ga, gb, x, tgt, t, 1e-3)
+        rp, ra, rb = learned.adam_step(rp, ra, rb, x, tgt, t, 1e-3)
+        np.testing.assert_allclose(ga, ra, rtol=GRAD_RTOL, atol=GRAD_RTOL * np.abs(ra).max())
+        np.testing.assert_allclose(gb, rb, rtol=1e-3, atol=1e-3 * np.abs(rb).max())
+        # parameters move by about lr a step: compare the moves
+        np.testing.assert_allclose(gp[:k] - p[:k], rp[:k] - p[:k].astype(np.float64), rtol=1e-2, atol=2e-5)
+    assert np.any(gp[:2 * learned.HIDDEN] != p[:2 * learned.HIDDEN])      # the first layer trains too
+
+
 @pytest.mark.parametrize("name", ["rep15k_L100_t63_u32", "lowc12k_L150_t63_u64"])
 def test_learned_keys_match_oracle(name):
     g = load_golden(name)
