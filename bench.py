@@ -329,7 +329,9 @@ def modes_block(P, nr: int, steps: int, stream, device, peak: float, plain_ref):
             r = timed_mode(P, nr, steps, P.overlaps, stream, device)
         g = r["graph"]
         same = bool(np.array_equal(g.dest, ref_dest) and np.array_equal(g.edge_off, ref_off))
+        tiers = P.tier_stats()
         out[name] = {"reads_per_s": r4(nr / (r["ms"] * 1e-3)), "ms": r4(r["ms"]),
+                     "handed_over": [tiers[k] for k in ("deferred", "block", "heavy", "wide")],
                      "kernel_ms": r4(r["kernel_ms"]), "probes_per_read": r4(r["probes_per_read"]),
                      "bytes_per_read": r4(r["bytes"] / max(nr, 1)),
                      "frac": r4(r["bytes"] / (r["kernel_ms"] * 1e-3) / 1e9 / peak),
@@ -462,6 +464,7 @@ def run_ours(args):
     step_ms = rank_max(e0.elapsed_time(e1) / args.steps, dev)
     g = P.graph()
     sec, outb = P.search_traffic()
+    detail["tiers"] = {k: r4(v) for k, v in P.tier_stats().items()}
     ref_graph = (g.dest.copy(), g.edge_off.copy())
     kms = statistics.median(kern_ms)
     alg_bytes = 32.0 * sec + outb

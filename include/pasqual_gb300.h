@@ -274,6 +274,15 @@ PQ_API int pq_get_batch_stats (pq_ctx * lead, float *kernel_ms, int *ctas_per_sm
  * lead's plan; *best_ms = its time.  The contexts hold the last run's (identical) results. */
 PQ_API int pq_autotune_batched (pq_ctx ** ctxs, int count, int flags, float *best_ms);
 
+/* How the last pq_overlaps divided its reads among its tiers: reads[0] = reads the lean tier (one
+ * thread a read, interval scan) handed to the fast tier (warp-level walk and DFS), reads[1] = reads
+ * the block tier (one CTA a read, all-pairs reduction in shared memory) finished of those the fast
+ * tier handed over, reads[2] = reads the heavy tier (the fast tier's DFS with larger capacities)
+ * took, reads[3] = reads the wide tier (the reference's own bounds) took; ms[0] = the lean and
+ * fast kernels (CUDA events), ms[1..3] = the block, heavy and wide tiers (host time, their
+ * synchronisations included).  Either pointer may be NULL. */
+PQ_API int pq_get_tier_stats (pq_ctx * ctx, uint64_t reads[4], float ms[4]);
+
 /* Duration (ms, CUDA events on the context stream) of the fast search kernel in the last
  * pq_overlaps, and the number of kernels this library has launched since it was loaded. */
 PQ_API int pq_get_kernel_stats (pq_ctx * ctx, float *search_kernel_ms,

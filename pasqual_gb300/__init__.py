@@ -35,7 +35,8 @@ EXPORTS = ["pq_idx_bytes", "pq_create", "pq_destroy", "pq_last_error", "pq_set_r
            "pq_suffix_sort_static", "pq_learned_build", "pq_learned_get_info", "pq_learned_export",
            "pq_learned_predict", "pq_learned_keys", "pq_mlp_forward", "pq_mlp_backward",
            "pq_overlaps_batched", "pq_set_batch_plan", "pq_get_batch_stats", "pq_autotune_batched",
-           "pq_set_sort_chunk", "pq_get_search_traffic", "pq_get_sort_seeds", "pq_mlp_adam_step"]
+           "pq_set_sort_chunk", "pq_get_search_traffic", "pq_get_sort_seeds", "pq_mlp_adam_step",
+           "pq_get_tier_stats"]
 
 
 # The reference's own entry points served by the same library (include/pasqual_gb300_dropin.h).
@@ -104,6 +105,7 @@ def load_library(width: int = 32) -> ct.CDLL:
         "pq_get_search_traffic": (c_int, [vp, vp, vp]),
         "pq_get_sort_seeds": (c_int, [vp, c_int, vp, vp, vp]),
         "pq_mlp_adam_step": (c_int, [vp, vp, vp, vp, vp, c_int, c_int, ct.c_float]),
+        "pq_get_tier_stats": (c_int, [vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -368,6 +370,14 @@ class Pasqual:
     def construct_string_graph(self) -> Graph:
         self.overlaps()
         return self.graph()
+
+    def tier_stats(self) -> dict:
+        """Reads the last overlap search handed from tier to tier, and each tier's time."""
+        n = (ct.c_uint64 * 4)()
+        ms = (ct.c_float * 4)()
+        self._ck(self.lib.pq_get_tier_stats(self.h, n, ms), "pq_get_tier_stats")
+        return {"deferred": n[0], "block": n[1], "heavy": n[2], "wide": n[3], "lean_fast_ms": ms[0],
+                "block_ms": ms[1], "heavy_ms": ms[2], "wide_ms": ms[3]}
 
     def search_traffic(self):
         """(32-byte sectors of index data the last overlap search loaded, bytes of results it

@@ -5,6 +5,7 @@
 #include <cstring>
 #include <string>
 #include <vector>
+#include <chrono>
 #include <algorithm>
 
 #include "pq_index.cuh"
@@ -105,8 +106,11 @@ struct pq_ctx {
 
     // overlap-search output
     DevBuf nB, nF, oB, oF, status, esrc, e_dest, e_trans, e_len, e_type, ctrs, ovf_list;
-    DevBuf off, g_dest, g_len, g_type, g_trans, asm_tmp, wide, warp_scratch, defer, heavy_scratch, ovf2;
-    uint64_t heavy_reads = 0;
+    DevBuf off, g_dest, g_len, g_type, g_trans, asm_tmp, wide, warp_scratch, defer, heavy_scratch, ovf2, ovf3;
+    uint64_t block_reads = 0;               // reads the block tier finished
+    float ms_block = 0;
+    uint64_t heavy_reads = 0, deferred_reads = 0;
+    float ms_heavy = 0, ms_wide = 0;        // host time of the heavy and wide tiers
     bool graph_ok = false;
     uint64_t num_edges = 0, probes = 0, sectors = 0, wide_reads = 0;
 };
@@ -183,7 +187,7 @@ void pq_destroy(pq_ctx* ctx) {
                       &ctx->oF, &ctx->status, &ctx->esrc, &ctx->e_dest, &ctx->e_trans, &ctx->e_len,
                       &ctx->e_type, &ctx->ctrs, &ctx->ovf_list, &ctx->off, &ctx->g_dest, &ctx->g_len,
                       &ctx->g_type, &ctx->g_trans, &ctx->asm_tmp, &ctx->wide, &ctx->warp_scratch, &ctx->defer,
-                      &ctx->heavy_scratch, &ctx->ovf2};
+                      &ctx->heavy_scratch, &ctx->ovf2, &ctx->ovf3};
     for (DevBuf* b : bufs) b->release();
     for (int d = 0; d < 2; ++d) {
         ctx->sa[d].release();
@@ -672,13 +676,41 @@ static int search_finish(pq_ctx* ctx, pq::SearchArgs& A, pq::SearchOut& O) {
     const size_t nr = ctx->num_reads;
     const size_t nrp = nr + 1;
     unsigned long long* ctr = ctx->ctrs.as<unsigned long long>();
-    unsigned long long hc[4];
+    unsigned long long hc[5];
     CK(cudaMemcpyAsync(hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
     ctx->lx_misses = hc[3];
+    ctx->deferred_reads = A.sorted_reduce ? (hc[4] & 0xffffffffu) : 0;
     unsigned ovf = unsigned(hc[2] & 0xffffffffu);
     const idx_t* ovf_src = ctx->ovf_list.as<idx_t>();
     ctx->heavy_reads = 0;
+    ctx->ms_heavy = ctx->ms_wide = 0;
+    auto wall_ms = [] {
+        return std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+    };
+    ctx->block_reads = 0;
+    ctx->ms_block = 0;
+    if (ovf && A.sorted_reduce) {
+        // block tier (one CTA a read, all-pairs reduction in shared memory) over the reads the fast
+        // tier could not hold; the ones it cannot hold either go on to the heavy tier.  Seed mode 0
+        // keeps the reference's DFS for every read and skips it.
+        const float tb0 = wall_ms();
+        CK(ctx->ovf3.ensure(nrp * sizeof(idx_t)));
+        CK(cudaMemsetAsync(ctr + 7, 0, sizeof(unsigned long long), ctx->st));
+        CK(pq::search_block(A, O, ctx->ovf_list.as<idx_t>(), reinterpret_cast<const unsigned*>(ctr + 2), ovf,
+                            ctx->ovf3.as<idx_t>(), reinterpret_cast<unsigned*>(ctr + 7), ctx->st));
+        unsigned long long h7 = 0;
+        CK(cudaMemcpyAsync(&h7, ctr + 7, sizeof h7, cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+        const unsigned left = unsigned(h7 & 0xffffffffu);
+        if (pq::block_tier_holds(ctx->L, ctx->t)) {
+            ctx->block_reads = ovf - left;
+            ovf = left;
+            ovf_src = ctx->ovf3.as<idx_t>();
+        }
+        ctx->ms_block = wall_ms() - tb0;
+    }
+    const float th0 = wall_ms();
     if (ovf) {
         // heavy tier (the fast kernel's DFS with larger capacities) over the reads the fast tier
         // could not hold; what it cannot hold either goes on to the wide tier
@@ -691,15 +723,18 @@ static int search_finish(pq_ctx* ctx, pq::SearchArgs& A, pq::SearchOut& O) {
         O2.ovf_list = ctx->ovf2.as<idx_t>();
         O2.ovf_count = reinterpret_cast<unsigned int*>(ctr + 5);
         CK(cudaMemsetAsync(ctr + 5, 0, sizeof(unsigned long long), ctx->st));
-        CK(pq::search_heavy(A, O2, ctx->ovf_list.as<idx_t>(), reinterpret_cast<const unsigned*>(ctr + 2), hblocks,
-                            ctx->heavy_scratch.p, hbytes, hebcap, ctx->st));
+        // the heavy tier's list: the block tier's leftovers (ctr[7]), or the fast tier's own (ctr[2])
+        const unsigned* hcount = reinterpret_cast<const unsigned*>(ovf_src == ctx->ovf3.as<idx_t>() ? ctr + 7 : ctr + 2);
+        CK(pq::search_heavy(A, O2, ovf_src, hcount, hblocks, ctx->heavy_scratch.p, hbytes, hebcap, ctx->st));
         unsigned long long h5 = 0;
         CK(cudaMemcpyAsync(&h5, ctr + 5, sizeof h5, cudaMemcpyDeviceToHost, ctx->st));
         CK(cudaStreamSynchronize(ctx->st));
         ctx->heavy_reads = ovf;
         ovf = unsigned(h5 & 0xffffffffu);
         ovf_src = ctx->ovf2.as<idx_t>();
+        ctx->ms_heavy = wall_ms() - th0;
     }
+    const float tw0 = wall_ms();
     ctx->wide_reads = ovf;
     if (ovf) {
         // wide tier over the overflow list; retried after growing the edge pool if needed
@@ -768,6 +803,7 @@ static int search_finish(pq_ctx* ctx, pq::SearchArgs& A, pq::SearchOut& O) {
         dlist.release();
         if (!list.empty()) return fail(ctx, PQ_ERR_INTERNAL, "edge pool retries exhausted");
     }
+    if (ctx->wide_reads) ctx->ms_wide = wall_ms() - tw0;
     // CSR in read order
     CK(ctx->off.ensure(nrp * 8));
     unsigned long long total = 0;
@@ -879,6 +915,24 @@ int pq_get_stage_ms(pq_ctx* ctx, float* sort_ms, float* fm_ms, float* search_ms)
     if (sort_ms) *sort_ms = ctx->ms_sort;
     if (fm_ms) *fm_ms = ctx->ms_fm;
     if (search_ms) *search_ms = ctx->ms_search;
+    return PQ_OK;
+}
+
+int pq_get_tier_stats(pq_ctx* ctx, uint64_t* reads, float* ms) {
+    if (!ctx) return PQ_ERR_ARG;
+    if (!ctx->graph_ok) return fail(ctx, PQ_ERR_STATE, "pq_overlaps first");
+    if (reads) {
+        reads[0] = ctx->deferred_reads;
+        reads[1] = ctx->block_reads;
+        reads[2] = ctx->heavy_reads;
+        reads[3] = ctx->wide_reads;
+    }
+    if (ms) {
+        ms[0] = ctx->ms_fast;
+        ms[1] = ctx->ms_block;
+        ms[2] = ctx->ms_heavy;
+        ms[3] = ctx->ms_wide;
+    }
     return PQ_OK;
 }
 

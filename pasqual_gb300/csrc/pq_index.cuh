@@ -130,6 +130,12 @@ int search_lean_blocks(int L, int M, int num_sms);
 size_t lean_scratch_bytes(int L, int t, int lean_blocks, int fast_blocks, int ebcap);
 cudaError_t search_lean(const SearchArgs& a, const SearchOut& o, int lean_blocks, int fast_blocks, void* scratch,
                         size_t scratch_bytes, int ebcap, cudaStream_t st);
+// Block tier over reads[0, *count) (count_host of them): one CTA a read, all-pairs reduction of each
+// side's candidates in shared memory; reads it cannot hold (or whose edges overflow the pool) are
+// appended to next_list for the heavy tier.
+cudaError_t search_block(const SearchArgs& a, const SearchOut& o, const idx_t* list, const unsigned* count,
+                         unsigned count_host, idx_t* next_list, unsigned* next_count, cudaStream_t st);
+bool block_tier_holds(int L, int t);      // false: reads of this L and t skip the block tier
 // Heavy tier over reads[0, *count) with a wider DFS (reads the fast tier could not hold).
 size_t heavy_scratch_bytes(int L, int t, int blocks, int ebcap);
 cudaError_t search_heavy(const SearchArgs& a, const SearchOut& o, const idx_t* list, const unsigned* count, int blocks,

@@ -1858,6 +1858,310 @@ size_t lean_scratch_bytes(int L, int t, int lean_blocks, int fast_blocks, int eb
     return scratch_layout(L - t, nwarps, ebcap, nullptr, nullptr);
 }
 
+// ------------------------------------------------------------------------------ block tier
+//
+// Reads the fast tier hands over are the ones with many candidates -- low-complexity sequence,
+// where a read's side can have thousands.  The block tier gives each such read one CTA: two
+// threads walk the two sides (chain_pair, from exact k-mer seeds, with the reference's depths),
+// the CTA expands every candidate group into its candidates (read id from the suffix array,
+// continuation from the packed text), and reduces each side as reduce_sorted does, with the
+// m x m ordered pairs of candidates spread over the CTA's threads: candidate c is covered when
+// another candidate's continuation is a proper prefix of its own, trans(c) counts the
+// continuations that start with c's, first_same(c) tells whether a candidate of the side's first
+// kind has exactly c's continuation.  The emitted candidates are then ranked in DFS order
+// (continuation, read id) by counting, again over pairs.  Everything lives in shared memory; a
+// side with more candidates than fit goes on to the heavy and wide tiers as before.
+
+constexpr int kBlockThreads = 256;
+constexpr size_t kBlockSmemBudget = 200 * 1024;     // dynamic shared memory of one block-tier CTA
+
+struct BlockSmem {      // the block tier's dynamic shared memory (offsets in bytes)
+    size_t words, ids, metas, cnts, elist, e_ids, e_metas, e_trans, groups, prefs, read, bytes;
+    int cap;            // candidates a side (and B-side edges kept while the F side is reduced)
+    int nw;             // continuation words per candidate
+};
+
+BlockSmem block_smem_layout(int L, int t, size_t budget) {
+    BlockSmem b{};
+    const int M = L - t;
+    b.nw = (M + 31) / 32;
+    const size_t groups = size_t(2) * size_t(2 * M) * sizeof(Cand);
+    const size_t prefs = size_t(2 * M + 1) * sizeof(unsigned);
+    const size_t read = size_t((L + 15) / 16) * sizeof(uint32_t);
+    const size_t per = size_t(b.nw) * 8 + sizeof(idx_t) + 4 + 4 + 4 + sizeof(idx_t) + 4 + 4;
+    const size_t fixed = groups + prefs + read + 16 * 16;
+    int cap = budget > fixed ? int((budget - fixed) / per) : 0;
+    cap = cap > 65535 ? 65535 : cap;
+    cap &= ~31;
+    b.cap = cap;
+    size_t o = 0;
+    auto take = [&](size_t n) {
+        const size_t r = o;
+        o += (n + 15) & ~size_t(15);
+        return r;
+    };
+    b.words = take(size_t(cap) * size_t(b.nw) * 8);
+    b.ids = take(size_t(cap) * sizeof(idx_t));
+    b.e_ids = take(size_t(cap) * sizeof(idx_t));
+    b.metas = take(size_t(cap) * 4);
+    b.cnts = take(size_t(cap) * 4);
+    b.elist = take(size_t(cap) * 4);
+    b.e_metas = take(size_t(cap) * 4);
+    b.e_trans = take(size_t(cap) * 4);
+    b.groups = take(groups);
+    b.prefs = take(prefs);
+    b.read = take(read);
+    b.bytes = o;
+    return b;
+}
+
+// the first n bases of continuations a and b (word k of candidate i at w[k * cap + i]) agree
+__device__ __forceinline__ bool block_same_prefix(const uint64_t* w, int cap, int a, int b, int n) {
+    for (int k = 0; n > 0; ++k, n -= 32) {
+        const uint64_t x = w[size_t(k) * cap + a] ^ w[size_t(k) * cap + b];
+        if (n < 32) return (x & top_mask(n)) == 0;
+        if (x) return false;
+    }
+    return true;
+}
+// order of two continuations that are equal or not prefixes of one another
+__device__ __forceinline__ int block_cmp(const uint64_t* w, int cap, int nw, int a, int la, int b, int lb) {
+    const int n = la < lb ? la : lb;
+    for (int k = 0; k < nw && 32 * k < n; ++k) {
+        const uint64_t x = w[size_t(k) * cap + a], y = w[size_t(k) * cap + b];
+        if (x != y) return x < y ? -1 : 1;
+    }
+    return la == lb ? 0 : (la < lb ? -1 : 1);
+}
+
+__global__ void __launch_bounds__(kBlockThreads) k_search_block(SearchArgs A, SearchOut O, const idx_t* list,
+                                                                const unsigned* list_count, BlockSmem lay,
+                                                                idx_t* next_list, unsigned* next_count) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint64_t* cw = reinterpret_cast<uint64_t*>(smem + lay.words);
+    idx_t* cid = reinterpret_cast<idx_t*>(smem + lay.ids);
+    uint32_t* cmeta = reinterpret_cast<uint32_t*>(smem + lay.metas);
+    uint32_t* ccnt = reinterpret_cast<uint32_t*>(smem + lay.cnts);
+    uint32_t* elist = reinterpret_cast<uint32_t*>(smem + lay.elist);
+    idx_t* e_id = reinterpret_cast<idx_t*>(smem + lay.e_ids);
+    uint32_t* e_meta = reinterpret_cast<uint32_t*>(smem + lay.e_metas);
+    int32_t* e_trans = reinterpret_cast<int32_t*>(smem + lay.e_trans);
+    Cand* grp = reinterpret_cast<Cand*>(smem + lay.groups);
+    unsigned* pref = reinterpret_cast<unsigned*>(smem + lay.prefs);
+    uint32_t* rdw = reinterpret_cast<uint32_t*>(smem + lay.read);
+    __shared__ int s_n[2][2];
+    __shared__ int32_t s_olp[2];
+    __shared__ int s_ok, s_ne, s_cnt[2];
+    __shared__ unsigned s_wsum[kBlockThreads / 32];
+    __shared__ unsigned long long s_base;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int L = A.L, M = L - A.t, cap = lay.cap, nw = lay.nw;
+    const unsigned count = *list_count;
+    Tally probes;
+    for (unsigned item = blockIdx.x; item < count; item += gridDim.x) {
+        const idx_t self = list[item];
+        if (tid == 0) {
+            load_read(A, self, rdw, 1, probes);
+            s_ok = 1;
+        }
+        __syncthreads();
+        // the candidate groups of side B (thread 0) and side F (thread 32)
+        if (tid == 0 || tid == 32) {
+            const int side = tid ? 1 : 0;
+            ReadView rd{rdw, 1};
+            int n[2];
+            int32_t olp = 0;
+            chain_pair(A, A.fm, rd, self, side ? PQ_FB : PQ_BF, side ? PQ_FF : PQ_BB, n, olp, probes,
+                       SlotsStack{grp + size_t(side) * 2 * M, M}, [] {});
+            s_n[side][0] = n[0];
+            s_n[side][1] = n[1];
+            s_olp[side] = olp;
+        }
+        __syncthreads();
+        for (int side = 0; side < 2; ++side) {
+            if (tid == 0) s_cnt[side] = 0;
+            if (s_olp[side] == 0) {      // src/string_graph.c:824, 828
+                __syncthreads();
+                continue;
+            }
+            const int n0 = s_n[side][0], ng = n0 + s_n[side][1];
+            const Cand* g = grp + size_t(side) * 2 * M;
+            if (tid == 0) {       // group sizes are index-wide: summed in 64 bits, stopped past cap
+                unsigned long long s = 0;
+                for (int i = 0; i < ng && s <= (unsigned long long)cap; ++i) {
+                    const Cand& c = g[i < n0 ? i : M + (i - n0)];
+                    pref[i] = unsigned(s);
+                    s += (unsigned long long)(c.uu - c.ll) + 1ull;
+                }
+                pref[ng] = unsigned(s);
+                if (s > (unsigned long long)cap) s_ok = 0;
+            }
+            __syncthreads();
+            if (!s_ok) break;
+            const int m = int(pref[ng]);
+            // every candidate's read id and continuation
+            for (int i = tid; i < m; i += kBlockThreads) {
+                int lo = 0, hi = ng - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (pref[mid] <= unsigned(i)) lo = mid;
+                    else hi = mid - 1;
+                }
+                const Cand& c = g[lo < n0 ? lo : M + (lo - n0)];
+                const idx_t row = c.ll + idx_t(unsigned(i) - pref[lo]);
+                const FmView& fb = A.fm[cand_index(c.type)];
+                const idx_t rp = read_of(__ldg(fb.sa + row), A.dl);
+                const int d = int(c.len), len = L - d;
+                const bool fwd = cand_index(c.type) == 1;
+                const uint64_t* pk = A.fm[fwd ? 0 : 1].pk;
+                const size_t pos = size_t(rp) * L + size_t(d);
+                const uint64_t flip = fwd ? 0 : ~uint64_t(0);
+                int used = 0;
+                for (int w = 0; w < nw; ++w) {
+                    const int left = len - 32 * w;
+                    uint64_t x = 0;
+                    if (left > 0) {
+                        x = (text_window(pk, pos + 32 * w) ^ flip) & top_mask(left < 32 ? left : 32);
+                        used = w + 1;
+                    }
+                    cw[size_t(w) * cap + i] = x;
+                }
+                probes.add(2, 1 + (used ? sectors_of(pk + (pos >> 5),
+                                                     8 * ((((pos + 32 * (used - 1)) >> 5) - (pos >> 5)) + 2))
+                                        : 0));
+                cid[i] = rp;
+                cmeta[i] = pack_meta(d, c.type);
+            }
+            __syncthreads();
+            // all pairs: covered (bit 0), first_same (bit 1), trans (bits 2..)
+            const int first_kind = side ? PQ_FB : PQ_BF;
+            for (int c = tid; c < m; c += kBlockThreads) {
+                const int lc = L - meta_len(cmeta[c]);
+                uint32_t v = 0;
+                for (int x = 0; x < m; ++x) {
+                    const uint32_t mx = cmeta[x];
+                    const int lx = L - meta_len(mx);
+                    if (!block_same_prefix(cw, cap, c, x, lx < lc ? lx : lc)) continue;
+                    if (lx < lc) {
+                        v |= 1u;
+                        break;
+                    }
+                    v += 4u;
+                    if (lx == lc && meta_type(mx) == first_kind) v |= 2u;
+                }
+                ccnt[c] = v;
+            }
+            if (tid == 0) s_ne = 0;
+            __syncthreads();
+            // the emitted candidates, listed (index | trans << 16) in candidate order
+            for (int c0 = 0; c0 < m; c0 += kBlockThreads) {
+                const int c = c0 + tid;
+                bool em = false;
+                if (c < m) {
+                    const uint32_t v = ccnt[c];
+                    em = !(v & 1u) && cid[c] != self && (meta_type(cmeta[c]) == first_kind || !(v & 2u));
+                }
+                const unsigned bal = __ballot_sync(0xffffffffu, em);
+                if (lane == 0) s_wsum[wid] = __popc(bal);
+                __syncthreads();
+                unsigned before = 0, all = 0;
+                for (int w = 0; w < kBlockThreads / 32; ++w) {
+                    before += w < wid ? s_wsum[w] : 0u;
+                    all += s_wsum[w];
+                }
+                if (em) elist[s_ne + int(before) + __popc(bal & ((1u << lane) - 1))] = uint32_t(c) | ((ccnt[c] >> 2) << 16);
+                __syncthreads();
+                if (tid == 0) s_ne += int(all);
+                __syncthreads();
+            }
+            const int ne = s_ne;
+            // DFS order: each emitted candidate's rank among the emitted ones; B-side edges are
+            // kept in place, F-side ranks wait in ccnt for the pool reservation
+            for (int i = tid; i < ne; i += kBlockThreads) {
+                const uint32_t v = elist[i];
+                const int c = int(v & 0xffff), lc = L - meta_len(cmeta[c]);
+                int rank = 0;
+                for (int j = 0; j < ne; ++j) {
+                    const int x = int(elist[j] & 0xffff);
+                    const int o = block_cmp(cw, cap, nw, x, L - meta_len(cmeta[x]), c, lc);
+                    rank += (o != 0 ? o < 0 : cid[x] < cid[c]) ? 1 : 0;
+                }
+                if (side == 0) {
+                    e_id[rank] = cid[c];
+                    e_meta[rank] = cmeta[c];
+                    e_trans[rank] = int32_t(v >> 16);
+                } else {
+                    ccnt[c] = uint32_t(rank);
+                }
+            }
+            if (tid == 0) s_cnt[side] = ne;
+            __syncthreads();
+        }
+        if (!s_ok) {             // more candidates than fit: the heavy tier
+            if (tid == 0) {
+                const unsigned k = atomicAdd(next_count, 1u);
+                next_list[k] = self;
+            }
+            __syncthreads();
+            continue;
+        }
+        const int nb = s_cnt[0], nf = s_cnt[1], ne = nb + nf;
+        if (tid == 0) {
+            s_base = ne ? atomicAdd(O.e_count, (unsigned long long)ne) : 0ull;
+            if (s_base + ne > O.e_cap) {         // edge pool full: the wide tier grows it
+                O.status[self] = OVF_POOL;
+                const unsigned k = atomicAdd(next_count, 1u);
+                next_list[k] = self;
+            } else {
+                O.status[self] = OVF_NONE;
+                O.num_B[self] = uint16_t(nb);
+                O.num_F[self] = uint16_t(nf);
+                O.olp_B[self] = s_olp[0];
+                O.olp_F[self] = s_olp[1];
+                O.edge_src[self] = s_base;
+            }
+        }
+        __syncthreads();
+        const unsigned long long base = s_base;
+        if (base + ne <= O.e_cap) {
+            for (int e = tid; e < nb; e += kBlockThreads) {
+                O.e_dest[base + e] = e_id[e];
+                O.e_trans[base + e] = e_trans[e];
+                O.e_len[base + e] = uint16_t(meta_len(e_meta[e]));
+                O.e_type[base + e] = uint8_t(meta_type(e_meta[e]));
+            }
+            for (int i = tid; i < nf; i += kBlockThreads) {       // the F side's candidates are still in place
+                const uint32_t v = elist[i];
+                const int c = int(v & 0xffff);
+                const unsigned long long q = base + nb + ccnt[c];
+                O.e_dest[q] = cid[c];
+                O.e_trans[q] = int32_t(v >> 16);
+                O.e_len[q] = uint16_t(meta_len(cmeta[c]));
+                O.e_type[q] = uint8_t(meta_type(cmeta[c]));
+            }
+        }
+        __syncthreads();
+    }
+    add_probes(O, probes);
+}
+
+bool block_tier_holds(int L, int t) { return block_smem_layout(L, t, kBlockSmemBudget).cap >= 128; }
+
+cudaError_t search_block(const SearchArgs& a, const SearchOut& o, const idx_t* list, const unsigned* count,
+                         unsigned count_host, idx_t* next_list, unsigned* next_count, cudaStream_t st) {
+    const BlockSmem lay = block_smem_layout(a.L, a.t, kBlockSmemBudget);
+    if (lay.cap < 128 || !count_host) return cudaSuccess;     // nothing this tier can hold
+    cudaError_t e = cudaFuncSetAttribute(k_search_block, cudaFuncAttributeMaxDynamicSharedMemorySize, int(lay.bytes));
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const unsigned blocks = count_host < unsigned(sms) ? count_host : unsigned(sms);
+    k_search_block<<<blocks, kBlockThreads, lay.bytes, st>>>(a, o, list, count, lay, next_list, next_count);
+    note_launch();
+    return cudaGetLastError();
+}
+
 // Heavy tier: the fast kernel's DFS with 32 times the stack, 4 times the level width and 256
 // levels, over a list of reads (the ones the fast tier could not hold: low-complexity sequence
 // gives thousands of candidates a side).  Its own overflow goes to the wide tier.

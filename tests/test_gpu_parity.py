@@ -126,14 +126,21 @@ def test_seed_modes_agree(name):
     assert probes[1] < probes[0]
 
 
-def test_wide_tier_used_and_exact():
-    """Dinucleotide runs give reads with many edges: some must go through the wide kernel."""
-    g = load_golden("dinuc6k_L60_t20_u32")
-    with gpu_ctx(32) as P:
+@pytest.mark.parametrize("name", ["dinuc6k_L60_t20_u32", "lowc12k_L150_t63_u64"])
+def test_handed_over_tiers_used_and_exact(name):
+    """Dinucleotide runs give reads with hundreds of candidates on a side: the lean tier hands them
+    to the fast tier, which hands the largest to the block tier (one CTA a read); the edges stay
+    the reference's."""
+    g = load_golden(name)
+    with gpu_ctx(int(g["width"])) as P:
         P.construct_index(g["reads"], int(g["t"]))
         out = P.construct_string_graph()
-    assert out.wide_reads > 0
-    assert sha(out.dest.astype(np.uint32)) == str(g["sha_dest"])
+        tiers = P.tier_stats()
+    assert tiers["deferred"] > 0
+    assert tiers["block"] + tiers["heavy"] + tiers["wide"] > 0, tiers
+    assert sha(out.dest.astype(idx_dtype(g["width"]))) == str(g["sha_dest"])
+    assert sha(out.num_B) == str(g["sha_num_B"]) and sha(out.num_F) == str(g["sha_num_F"])
+    assert sha(graph.trans_with_mask(out.num_B, out.num_F, out.edge_off, out.trans)) == str(g["sha_trans"])
 
 
 def _oracle_run(reads, t, width):
