@@ -66,6 +66,8 @@ def parse():
     ap.add_argument("--batched-scale", type=float, default=0.1,
                     help="genome scale of the mixed read-set queued workload (0 = skip)")
     ap.add_argument("--detail", default="", help="also write every figure to this JSON file")
+    ap.add_argument("--seed-mode", type=int, default=1, choices=[0, 1, 2],
+                    help="seed mode of the timed search (0: the reference's walk and DFS, k_search_fast)")
     return ap.parse_args()
 
 
@@ -422,6 +424,7 @@ def run_ours(args):
     width = max(width, synth.WORKLOADS[args.workload].get("index", 32))
     stream = torch.cuda.Stream(device=dev)
     P = pq.Pasqual(width, device=local, stream=stream.cuda_stream)
+    P.set_seed_mode(args.seed_mode)
     peak, peak_kind = measured_peak_hbm()
 
     # ---- index build (setup) and suffix-sort throughput (suffix arrays only, both directions)
@@ -541,9 +544,9 @@ def run_ours(args):
         "gpu_launches": int(l1 - l0),
         "roofline": {"bound": "hbm", "achieved": r4(achieved), "peak": peak, "unit": "GB/s",
                      "frac": r4(achieved / peak), "peak_kind": peak_kind,
-                     "kernel": "k_search_lean", "kernel_ms": r4(kms),
+                     "kernel": "k_search_fast" if args.seed_mode == 0 else "k_search_lean", "kernel_ms": r4(kms),
                      "bytes_per_read": r4(alg_bytes / nr),
-                     "traffic": r4(dram_per_read * nr) if dram_per_read else None,
+                     "traffic": r4(dram_per_read * nr) if dram_per_read and args.seed_mode == 1 else None,
                      "reference_probes_per_read": r4(ref_ppr), "probes_per_read": r4(g.probes / nr)},
         "e2e": ({"value": r4(replica_throughput(nr, world, e2e_ms_med)), "unit": "reads/s",
                  "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": r4(e2e_ms_med),

@@ -106,7 +106,7 @@ struct pq_ctx {
 
     // overlap-search output
     DevBuf nB, nF, oB, oF, status, esrc, e_dest, e_trans, e_len, e_type, ctrs, ovf_list;
-    DevBuf off, g_dest, g_len, g_type, g_trans, asm_tmp, wide, warp_scratch, defer, heavy_scratch, ovf2, ovf3;
+    DevBuf off, g_dest, g_len, g_type, g_trans, asm_tmp, wide, warp_scratch, defer, heavy_scratch, ovf2, ovf3, ovf4, block_scratch;
     uint64_t block_reads = 0;               // reads the block tier finished
     float ms_block = 0;
     uint64_t heavy_reads = 0, deferred_reads = 0;
@@ -187,7 +187,7 @@ void pq_destroy(pq_ctx* ctx) {
                       &ctx->oF, &ctx->status, &ctx->esrc, &ctx->e_dest, &ctx->e_trans, &ctx->e_len,
                       &ctx->e_type, &ctx->ctrs, &ctx->ovf_list, &ctx->off, &ctx->g_dest, &ctx->g_len,
                       &ctx->g_type, &ctx->g_trans, &ctx->asm_tmp, &ctx->wide, &ctx->warp_scratch, &ctx->defer,
-                      &ctx->heavy_scratch, &ctx->ovf2, &ctx->ovf3};
+                      &ctx->heavy_scratch, &ctx->ovf2, &ctx->ovf3, &ctx->ovf4, &ctx->block_scratch};
     for (DevBuf* b : bufs) b->release();
     for (int d = 0; d < 2; ++d) {
         ctx->sa[d].release();
@@ -593,7 +593,7 @@ static int search_prepare(pq_ctx* ctx, pq::SearchArgs& A, pq::SearchOut& O) {
     CK(ctx->status.ensure(nrp));
     CK(ctx->esrc.ensure(nrp * 8));
     CK(ctx->ovf_list.ensure(nrp * sizeof(idx_t)));
-    CK(ctx->ctrs.ensure(64));
+    CK(ctx->ctrs.ensure(128));
     size_t ecap = std::max<size_t>(ctx->e_dest.bytes / sizeof(idx_t), nr * 6 + 4096);
     CK(ctx->e_dest.ensure(ecap * sizeof(idx_t)));
     CK(ctx->e_trans.ensure(ecap * 4));
@@ -683,6 +683,7 @@ static int search_finish(pq_ctx* ctx, pq::SearchArgs& A, pq::SearchOut& O) {
     ctx->deferred_reads = A.sorted_reduce ? (hc[4] & 0xffffffffu) : 0;
     unsigned ovf = unsigned(hc[2] & 0xffffffffu);
     const idx_t* ovf_src = ctx->ovf_list.as<idx_t>();
+    const unsigned* ovf_cnt = reinterpret_cast<const unsigned*>(ctr + 2);     // device count of ovf_src
     ctx->heavy_reads = 0;
     ctx->ms_heavy = ctx->ms_wide = 0;
     auto wall_ms = [] {
@@ -707,6 +708,26 @@ static int search_finish(pq_ctx* ctx, pq::SearchArgs& A, pq::SearchOut& O) {
             ctx->block_reads = ovf - left;
             ovf = left;
             ovf_src = ctx->ovf3.as<idx_t>();
+            ovf_cnt = reinterpret_cast<const unsigned*>(ctr + 7);
+            if (ovf) {
+                // the same tier with its candidate arrays in global memory, for sides of up to
+                // 32768 candidates
+                const int gb = pq::block_global_blocks(ovf);
+                const size_t gbytes = pq::block_global_bytes(ctx->L, ctx->t, gb);
+                CK(ctx->block_scratch.ensure(gbytes));
+                CK(ctx->ovf4.ensure(nrp * sizeof(idx_t)));
+                CK(cudaMemsetAsync(ctr + 8, 0, sizeof(unsigned long long), ctx->st));
+                CK(pq::search_block_global(A, O, ovf_src, ovf_cnt, ovf, gb, ctx->block_scratch.p, gbytes,
+                                           ctx->ovf4.as<idx_t>(), reinterpret_cast<unsigned*>(ctr + 8), ctx->st));
+                unsigned long long h8 = 0;
+                CK(cudaMemcpyAsync(&h8, ctr + 8, sizeof h8, cudaMemcpyDeviceToHost, ctx->st));
+                CK(cudaStreamSynchronize(ctx->st));
+                const unsigned left2 = unsigned(h8 & 0xffffffffu);
+                ctx->block_reads += ovf - left2;
+                ovf = left2;
+                ovf_src = ctx->ovf4.as<idx_t>();
+                ovf_cnt = reinterpret_cast<const unsigned*>(ctr + 8);
+            }
         }
         ctx->ms_block = wall_ms() - tb0;
     }
@@ -723,9 +744,8 @@ static int search_finish(pq_ctx* ctx, pq::SearchArgs& A, pq::SearchOut& O) {
         O2.ovf_list = ctx->ovf2.as<idx_t>();
         O2.ovf_count = reinterpret_cast<unsigned int*>(ctr + 5);
         CK(cudaMemsetAsync(ctr + 5, 0, sizeof(unsigned long long), ctx->st));
-        // the heavy tier's list: the block tier's leftovers (ctr[7]), or the fast tier's own (ctr[2])
-        const unsigned* hcount = reinterpret_cast<const unsigned*>(ovf_src == ctx->ovf3.as<idx_t>() ? ctr + 7 : ctr + 2);
-        CK(pq::search_heavy(A, O2, ovf_src, hcount, hblocks, ctx->heavy_scratch.p, hbytes, hebcap, ctx->st));
+        // the heavy tier's list: the block tiers' leftovers, or the fast tier's own
+        CK(pq::search_heavy(A, O2, ovf_src, ovf_cnt, hblocks, ctx->heavy_scratch.p, hbytes, hebcap, ctx->st));
         unsigned long long h5 = 0;
         CK(cudaMemcpyAsync(&h5, ctr + 5, sizeof h5, cudaMemcpyDeviceToHost, ctx->st));
         CK(cudaStreamSynchronize(ctx->st));

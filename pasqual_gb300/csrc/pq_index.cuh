@@ -136,6 +136,13 @@ cudaError_t search_lean(const SearchArgs& a, const SearchOut& o, int lean_blocks
 cudaError_t search_block(const SearchArgs& a, const SearchOut& o, const idx_t* list, const unsigned* count,
                          unsigned count_host, idx_t* next_list, unsigned* next_count, cudaStream_t st);
 bool block_tier_holds(int L, int t);      // false: reads of this L and t skip the block tier
+// The block tier with each CTA's candidate arrays in its own region of a global scratch buffer
+// (block_global_bytes for `blocks` CTAs): sides of up to 32768 candidates.
+int block_global_blocks(unsigned count);
+size_t block_global_bytes(int L, int t, int blocks);
+cudaError_t search_block_global(const SearchArgs& a, const SearchOut& o, const idx_t* list, const unsigned* count,
+                                unsigned count_host, int blocks, void* scratch, size_t scratch_bytes,
+                                idx_t* next_list, unsigned* next_count, cudaStream_t st);
 // Heavy tier over reads[0, *count) with a wider DFS (reads the fast tier could not hold).
 size_t heavy_scratch_bytes(int L, int t, int blocks, int ebcap);
 cudaError_t search_heavy(const SearchArgs& a, const SearchOut& o, const idx_t* list, const unsigned* count, int blocks,

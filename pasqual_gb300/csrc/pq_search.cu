@@ -1881,6 +1881,17 @@ struct BlockSmem {      // the block tier's dynamic shared memory (offsets in by
     int nw;             // continuation words per candidate
 };
 
+// bytes a candidate takes (continuation words, read id, meta, counter, emitted list, B-side edge)
+// and the fixed part (both sides' candidate groups, their prefix sums, the read)
+size_t block_per_cand(int L, int t) {
+    return size_t((L - t + 31) / 32) * 8 + sizeof(idx_t) + 4 + 4 + 4 + sizeof(idx_t) + 4 + 4;
+}
+size_t block_fixed(int L, int t) {
+    const int M = L - t;
+    return size_t(2) * size_t(2 * M) * sizeof(Cand) + size_t(2 * M + 1) * sizeof(unsigned) +
+           size_t((L + 15) / 16) * sizeof(uint32_t) + 16 * 16;
+}
+
 BlockSmem block_smem_layout(int L, int t, size_t budget) {
     BlockSmem b{};
     const int M = L - t;
@@ -1888,10 +1899,9 @@ BlockSmem block_smem_layout(int L, int t, size_t budget) {
     const size_t groups = size_t(2) * size_t(2 * M) * sizeof(Cand);
     const size_t prefs = size_t(2 * M + 1) * sizeof(unsigned);
     const size_t read = size_t((L + 15) / 16) * sizeof(uint32_t);
-    const size_t per = size_t(b.nw) * 8 + sizeof(idx_t) + 4 + 4 + 4 + sizeof(idx_t) + 4 + 4;
-    const size_t fixed = groups + prefs + read + 16 * 16;
-    int cap = budget > fixed ? int((budget - fixed) / per) : 0;
-    cap = cap > 65535 ? 65535 : cap;
+    const size_t per = block_per_cand(L, t);
+    const size_t fixed = block_fixed(L, t);
+    int cap = budget > fixed ? int(std::min<size_t>((budget - fixed) / per, 65535)) : 0;
     cap &= ~31;
     b.cap = cap;
     size_t o = 0;
@@ -1934,10 +1944,15 @@ __device__ __forceinline__ int block_cmp(const uint64_t* w, int cap, int nw, int
     return la == lb ? 0 : (la < lb ? -1 : 1);
 }
 
+// kGlobal: the candidate arrays live in a per-CTA region of `scratch` (global memory, cached in
+// L1/L2) instead of shared memory, for sides with more candidates than shared memory holds.
+template <bool kGlobal>
 __global__ void __launch_bounds__(kBlockThreads) k_search_block(SearchArgs A, SearchOut O, const idx_t* list,
                                                                 const unsigned* list_count, BlockSmem lay,
-                                                                idx_t* next_list, unsigned* next_count) {
-    extern __shared__ __align__(16) unsigned char smem[];
+                                                                idx_t* next_list, unsigned* next_count,
+                                                                unsigned char* scratch) {
+    extern __shared__ __align__(16) unsigned char smem_dyn[];
+    unsigned char* smem = kGlobal ? scratch + size_t(blockIdx.x) * lay.bytes : smem_dyn;
     uint64_t* cw = reinterpret_cast<uint64_t*>(smem + lay.words);
     idx_t* cid = reinterpret_cast<idx_t*>(smem + lay.ids);
     uint32_t* cmeta = reinterpret_cast<uint32_t*>(smem + lay.metas);
@@ -2151,13 +2166,45 @@ cudaError_t search_block(const SearchArgs& a, const SearchOut& o, const idx_t* l
                          unsigned count_host, idx_t* next_list, unsigned* next_count, cudaStream_t st) {
     const BlockSmem lay = block_smem_layout(a.L, a.t, kBlockSmemBudget);
     if (lay.cap < 128 || !count_host) return cudaSuccess;     // nothing this tier can hold
-    cudaError_t e = cudaFuncSetAttribute(k_search_block, cudaFuncAttributeMaxDynamicSharedMemorySize, int(lay.bytes));
+    cudaError_t e = cudaFuncSetAttribute(k_search_block<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         int(lay.bytes));
     if (e != cudaSuccess) return e;
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const unsigned blocks = count_host < unsigned(sms) ? count_host : unsigned(sms);
-    k_search_block<<<blocks, kBlockThreads, lay.bytes, st>>>(a, o, list, count, lay, next_list, next_count);
+    k_search_block<false><<<blocks, kBlockThreads, lay.bytes, st>>>(a, o, list, count, lay, next_list, next_count,
+                                                                    nullptr);
+    note_launch();
+    return cudaGetLastError();
+}
+
+// The same tier with the candidate arrays in global memory: kBlockGlobalCap candidates a side, one
+// region of block_global_bytes / blocks bytes per CTA.
+constexpr int kBlockGlobalCap = 32768;
+
+int block_global_blocks(unsigned count) {
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const unsigned most = unsigned(sms) * 2;
+    return int(count < most ? count : most);
+}
+
+BlockSmem block_global_layout(int L, int t) {
+    return block_smem_layout(L, t, block_per_cand(L, t) * kBlockGlobalCap + block_fixed(L, t));
+}
+
+size_t block_global_bytes(int L, int t, int blocks) { return size_t(blocks) * block_global_layout(L, t).bytes; }
+
+cudaError_t search_block_global(const SearchArgs& a, const SearchOut& o, const idx_t* list, const unsigned* count,
+                                unsigned count_host, int blocks, void* scratch, size_t scratch_bytes,
+                                idx_t* next_list, unsigned* next_count, cudaStream_t st) {
+    if (!count_host || blocks <= 0) return cudaSuccess;
+    const BlockSmem lay = block_global_layout(a.L, a.t);
+    if (scratch_bytes < size_t(blocks) * lay.bytes) return cudaErrorInvalidValue;
+    k_search_block<true><<<blocks, kBlockThreads, 0, st>>>(a, o, list, count, lay, next_list, next_count,
+                                                           static_cast<unsigned char*>(scratch));
     note_launch();
     return cudaGetLastError();
 }
