@@ -65,6 +65,17 @@ PQ_API int pq_create (pq_ctx ** out, int device, void *cuda_stream);
 PQ_API void pq_destroy (pq_ctx * ctx);
 PQ_API const char *pq_last_error (const pq_ctx * ctx);
 
+/* Page-locked host memory for the buffers that cross to and from the device (reads in, graphs
+ * out).  The region is mapped on huge-page boundaries, advised for transparent huge pages
+ * (madvise; small pages where the kernel has none), touched, and registered with CUDA.  A copy
+ * from it then needs one address translation per huge page.  Copies from small-page pinned
+ * memory (cudaHostAlloc) were measured on GB300 at 11-17 GB/s when they followed a suffix sort
+ * or a search, whose random accesses over most of device memory had evicted the translations,
+ * against 210 GB/s from this memory in the same place.  *out is aligned to the huge-page size;
+ * pq_host_free releases it.  PQ_ERR_NOMEM when the memory cannot be mapped or registered. */
+PQ_API int pq_host_alloc (size_t bytes, void **out);
+PQ_API int pq_host_free (void *p);
+
 /* Reads after import and de-duplication: num_reads * read_len base codes 1..4 (A,C,G,T), the
  * layout of index_t.reads after import_singlereads (src/index.c:145-405).  min_overlap is the
  * -t of the CLI, with SEQ_DEPTH(9) < min_overlap < read_len (src/test.c:306-311).

@@ -15,6 +15,7 @@ from __future__ import annotations
 
 import ctypes as ct
 import os
+import weakref
 from dataclasses import dataclass
 
 import numpy as np
@@ -22,7 +23,8 @@ import numpy as np
 from . import build as _build
 
 __all__ = ["Pasqual", "Graph", "PQError", "load_library", "library_path", "EXPORTS", "mlp_forward",
-           "mlp_backward", "mlp_adam_step", "LearnedInfo", "overlaps_batched", "autotune_batched"]
+           "mlp_backward", "mlp_adam_step", "LearnedInfo", "overlaps_batched", "autotune_batched",
+           "host_empty"]
 
 PQ_ERRORS = {1: "PQ_ERR_ARG", 2: "PQ_ERR_CUDA", 3: "PQ_ERR_NOMEM", 4: "PQ_ERR_TOO_MANY_EDGES",
              5: "PQ_ERR_STATE", 6: "PQ_ERR_CAPACITY", 7: "PQ_ERR_INTERNAL"}
@@ -36,7 +38,7 @@ EXPORTS = ["pq_idx_bytes", "pq_create", "pq_destroy", "pq_last_error", "pq_set_r
            "pq_learned_predict", "pq_learned_keys", "pq_mlp_forward", "pq_mlp_backward",
            "pq_overlaps_batched", "pq_set_batch_plan", "pq_get_batch_stats", "pq_autotune_batched",
            "pq_set_sort_chunk", "pq_get_search_traffic", "pq_get_sort_seeds", "pq_mlp_adam_step",
-           "pq_get_tier_stats"]
+           "pq_get_tier_stats", "pq_host_alloc", "pq_host_free"]
 
 
 # The reference's own entry points served by the same library (include/pasqual_gb300_dropin.h).
@@ -106,6 +108,8 @@ def load_library(width: int = 32) -> ct.CDLL:
         "pq_get_sort_seeds": (c_int, [vp, c_int, vp, vp, vp]),
         "pq_mlp_adam_step": (c_int, [vp, vp, vp, vp, vp, c_int, c_int, ct.c_float]),
         "pq_get_tier_stats": (c_int, [vp, vp, vp]),
+        "pq_host_alloc": (c_int, [ct.c_size_t, ct.POINTER(vp)]),
+        "pq_host_free": (c_int, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -171,6 +175,24 @@ def mlp_adam_step(params: np.ndarray, m1: np.ndarray, m2: np.ndarray, x: np.ndar
     if rc != 0:
         raise PQError(rc, "pq_mlp_adam_step")
     return p, a, b
+
+
+def host_empty(shape, dtype=np.uint8, width: int = 32) -> np.ndarray:
+    """A host array in page-locked, huge-page-backed memory (pq_host_alloc), for the buffers that
+    cross to the device and back: copies from it keep their full rate after a sort or search,
+    where copies from small-page pinned memory slow down ten-fold.  Released when the array and
+    every view of it are gone."""
+    lib = load_library(width)
+    dt = np.dtype(dtype)
+    count = int(np.prod(shape, dtype=np.int64))
+    nbytes = max(count * dt.itemsize, 1)
+    ptr = ct.c_void_p()
+    rc = lib.pq_host_alloc(nbytes, ct.byref(ptr))
+    if rc != 0:
+        raise PQError(rc, "pq_host_alloc(%d bytes)" % nbytes)
+    buf = (ct.c_uint8 * nbytes).from_address(ptr.value)
+    weakref.finalize(buf, lib.pq_host_free, ptr.value)
+    return np.frombuffer(buf, dtype=dt, count=count).reshape(shape)
 
 
 BATCH_GRAPH = 1

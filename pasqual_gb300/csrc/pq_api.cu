@@ -16,6 +16,13 @@
 static_assert(sizeof(pq_idx) == sizeof(idx_t), "pq_idx and idx_t must agree");
 
 #include <atomic>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <sys/mman.h>
+#ifndef MADV_COLLAPSE
+#define MADV_COLLAPSE 25
+#endif
 namespace pq {
 static std::atomic<unsigned long long> g_launches{0};
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
@@ -150,6 +157,80 @@ static LearnedView lx_view(const pq_ctx* c, int d) {
 extern "C" {
 
 int pq_idx_bytes(void) { return int(sizeof(idx_t)); }
+
+namespace {
+// Host regions handed out by pq_host_alloc: aligned address -> the mapping it lies in.
+struct HostRegion {
+    void* base;
+    size_t total;
+};
+std::mutex g_host_mu;
+std::unordered_map<void*, HostRegion> g_host;
+
+size_t huge_page_bytes() {
+    unsigned long long v = 0;
+    if (FILE* f = fopen("/sys/kernel/mm/transparent_hugepage/hpage_pmd_size", "r")) {
+        if (fscanf(f, "%llu", &v) != 1) v = 0;
+        fclose(f);
+    }
+    return (v >= 4096 && (v & (v - 1)) == 0) ? size_t(v) : (size_t(2) << 20);
+}
+}  // namespace
+
+int pq_host_alloc(size_t bytes, void** out) {
+    if (!out) return PQ_ERR_ARG;
+    *out = nullptr;
+    // The device's context first: registered as the process's first CUDA call (the context
+    // created inside cudaHostRegister), a region was measured to lose some of its huge pages and
+    // to copy at a half to a twentieth of the rate of one registered afterwards.
+    if (cudaFree(nullptr) != cudaSuccess) {
+        cudaGetLastError();
+        return PQ_ERR_CUDA;
+    }
+    const size_t hp = huge_page_bytes();
+    const size_t size = (std::max<size_t>(bytes, 1) + hp - 1) / hp * hp;
+    const size_t total = size + hp;
+    void* base = mmap(nullptr, total, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
+    if (base == MAP_FAILED) return PQ_ERR_NOMEM;
+    char* p = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(base) + hp - 1) / hp * hp);
+    madvise(p, size, MADV_HUGEPAGE);      // advice only: small pages where there are no huge ones
+    // fault the pages in (huge pages are zeroed by the kernel), one huge page per step, in parallel
+    const size_t pages = size / hp;
+    const size_t nth = std::max<size_t>(1, std::min<size_t>(pages, std::max(1u, std::thread::hardware_concurrency())));
+    std::vector<std::thread> th;
+    for (size_t t = 0; t < nth; ++t)
+        th.emplace_back([=] {
+            for (size_t i = t; i < pages; i += nth) memset(p + i * hp, 0, hp);
+        });
+    for (auto& x : th) x.join();
+    // where a fault found no free huge page (a fragmented host), ask once more, synchronously:
+    // MADV_COLLAPSE compacts and rebuilds the range in huge pages (Linux 6.1+; an error is ignored)
+    madvise(p, size, MADV_COLLAPSE);
+    if (cudaHostRegister(p, size, cudaHostRegisterDefault) != cudaSuccess) {
+        cudaGetLastError();
+        munmap(base, total);
+        return PQ_ERR_NOMEM;
+    }
+    std::lock_guard<std::mutex> g(g_host_mu);
+    g_host[p] = HostRegion{base, total};
+    *out = p;
+    return PQ_OK;
+}
+
+int pq_host_free(void* p) {
+    if (!p) return PQ_OK;
+    HostRegion r{};
+    {
+        std::lock_guard<std::mutex> g(g_host_mu);
+        auto it = g_host.find(p);
+        if (it == g_host.end()) return PQ_ERR_ARG;
+        r = it->second;
+        g_host.erase(it);
+    }
+    cudaHostUnregister(p);
+    munmap(r.base, r.total);
+    return PQ_OK;
+}
 
 int pq_create(pq_ctx** out, int device, void* cuda_stream) {
     if (!out) return PQ_ERR_ARG;
