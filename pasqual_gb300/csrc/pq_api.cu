@@ -320,9 +320,19 @@ int pq_set_reads(pq_ctx* ctx, const uint8_t* reads, pq_idx num_reads, int read_l
     ctx->seed_k = std::min(ctx->seed_k, min_overlap);
     size_t bytes = size_t(num_reads) * read_len;
     CK(ctx->reads.ensure(bytes + 64));
-    if (bytes)
-        CK(cudaMemcpyAsync(ctx->reads.p, reads, bytes, from_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
-                           ctx->st));
+    if (bytes) {
+        // page-locked host memory (cudaHostAlloc'd or registered) is read by the upload kernel;
+        // pageable memory goes through cudaMemcpy
+        cudaPointerAttributes pa{};
+        const bool pinned = !from_device && cudaPointerGetAttributes(&pa, reads) == cudaSuccess &&
+                            pa.type == cudaMemoryTypeHost && pa.devicePointer != nullptr;
+        cudaGetLastError();
+        if (pinned)
+            CK(pq::upload(ctx->reads.as<uint8_t>(), static_cast<const uint8_t*>(pa.devicePointer), bytes, ctx->st));
+        else
+            CK(cudaMemcpyAsync(ctx->reads.p, reads, bytes,
+                               from_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, ctx->st));
+    }
     CK(ctx->counts.ensure(13 * sizeof(unsigned long long)));
     CK(pq::read_counts(ctx->reads.as<uint8_t>(), num_reads, idx_t(read_len),
                        ctx->counts.as<unsigned long long>(), ctx->st));

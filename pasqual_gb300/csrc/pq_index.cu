@@ -427,6 +427,49 @@ cudaError_t build_occ(const idx_t* sa, const uint8_t* reads, idx_t num_reads, id
     return cudaGetLastError();
 }
 
+// Host -> device copy of n bytes by a kernel that reads page-locked host memory directly: four
+// independent 16-byte loads a thread, 32 CTAs per SM.  So many loads in flight keep the copy at
+// the link's rate even when the GPU's cached translations of the host pages were evicted by a sort
+// or a search over most of device memory (a copy-engine cudaMemcpy from the same buffer then fell
+// to ~10 GB/s).  Bytes before the first 16-byte boundary and after the last are copied one by one;
+// when source and destination are not equally aligned the whole copy goes byte by byte.
+__global__ void __launch_bounds__(256) k_upload(uint8_t* __restrict__ dst, const uint8_t* __restrict__ src,
+                                                size_t n) {
+    const size_t tid = size_t(blockIdx.x) * blockDim.x + threadIdx.x, stride = size_t(gridDim.x) * blockDim.x;
+    const size_t mis = reinterpret_cast<uintptr_t>(src) & 15;
+    if (mis != (reinterpret_cast<uintptr_t>(dst) & 15)) {
+        for (size_t i = tid; i < n; i += stride) dst[i] = src[i];
+        return;
+    }
+    const size_t head = mis ? (16 - mis < n ? 16 - mis : n) : 0;
+    const size_t n16 = (n - head) / 16, tail = head + n16 * 16;
+    if (tid < head) dst[tid] = src[tid];
+    if (tid < n - tail) dst[tail + tid] = src[tail + tid];
+    uint4* d = reinterpret_cast<uint4*>(dst + head);
+    const uint4* s = reinterpret_cast<const uint4*>(src + head);
+    size_t i = tid;
+    for (; i + 3 * stride < n16; i += 4 * stride) {
+        const uint4 a = s[i], b = s[i + stride], c = s[i + 2 * stride], e = s[i + 3 * stride];
+        d[i] = a;
+        d[i + stride] = b;
+        d[i + 2 * stride] = c;
+        d[i + 3 * stride] = e;
+    }
+    for (; i < n16; i += stride) d[i] = s[i];
+}
+
+cudaError_t upload(uint8_t* dst, const uint8_t* src, size_t n, cudaStream_t st) {
+    if (!n) return cudaSuccess;
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const size_t want = (n / 16 + 255) / 256;
+    const unsigned blocks = unsigned(std::max<size_t>(1, std::min<size_t>(want, size_t(sms) * 32)));
+    k_upload<<<blocks, 256, 0, st>>>(dst, src, n);
+    note_launch();
+    return cudaGetLastError();
+}
+
 cudaError_t read_counts(const uint8_t* reads, idx_t num_reads, idx_t L, unsigned long long* out13,
                         cudaStream_t st) {
     cudaMemsetAsync(out13, 0, 13 * sizeof(unsigned long long), st);

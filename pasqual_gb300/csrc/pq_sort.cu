@@ -1381,7 +1381,7 @@ int suffix_sort(const uint8_t* reads, idx_t num_reads, int L, int dir, idx_t* sa
 
 constexpr int kBucketBases = 6;
 constexpr int kBuckets = (1 << (2 * kBucketBases)) * 8;
-constexpr int kCkTile = 4096;
+constexpr int kCkTile = 8192;
 
 __device__ __forceinline__ uint32_t bucket_of(const uint64_t* __restrict__ pk, size_t p, const DivL& dl) {
     const int m = int(dl.L - uint32_t(p - div_l(p, dl) * dl.L));
@@ -1391,81 +1391,134 @@ __device__ __forceinline__ uint32_t bucket_of(const uint64_t* __restrict__ pk, s
 }
 
 // every position's bucket (kept for the chunk passes, which then read 2 bytes a position) and the
-// bucket histogram
-__global__ void k_bucket_hist(const uint64_t* __restrict__ pk, size_t n, DivL dl, uint16_t* __restrict__ bid,
-                              unsigned long long* __restrict__ hist) {
+// bucket histogram, counted in shared memory (kBuckets 32-bit counters, one CTA per SM) and added
+// to the global histogram once per CTA
+constexpr int kHistThreads = 1024;
+__global__ void __launch_bounds__(kHistThreads) k_bucket_hist(const uint64_t* __restrict__ pk, size_t n, DivL dl,
+                                                              uint16_t* __restrict__ bid,
+                                                              unsigned long long* __restrict__ hist) {
+    extern __shared__ unsigned s_hist[];
+    for (int i = threadIdx.x; i < kBuckets; i += blockDim.x) s_hist[i] = 0;
+    __syncthreads();
     const size_t stride = size_t(gridDim.x) * blockDim.x;
     for (size_t p = size_t(blockIdx.x) * blockDim.x + threadIdx.x; p < n; p += stride) {
         const uint32_t b = bucket_of(pk, p, dl);
         bid[p] = uint16_t(b);
-        atomicAdd(&hist[b], 1ull);
+        atomicAdd(&s_hist[b], 1u);
     }
-}
-
-// per tile of 4096 positions: how many fall in buckets [lo, hi)
-__global__ void __launch_bounds__(256) k_chunk_count(const uint16_t* __restrict__ bid, size_t n, uint32_t lo,
-                                                    uint32_t hi, unsigned long long* __restrict__ tcnt) {
-    __shared__ unsigned red[8];
-    const size_t t0 = size_t(blockIdx.x) * kCkTile;
-    unsigned c = 0;
-    for (int j = threadIdx.x; j < kCkTile; j += 256) {
-        const size_t p = t0 + j;
-        if (p < n) {
-            const uint32_t b = bid[p];
-            c += (b >= lo && b < hi) ? 1u : 0u;
-        }
-    }
-    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = c;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned t = 0;
-        for (int w = 0; w < 8; ++w) t += red[w];
-        tcnt[blockIdx.x] = t;
+    for (int i = threadIdx.x; i < kBuckets; i += blockDim.x)
+        if (s_hist[i]) atomicAdd(&hist[i], (unsigned long long)s_hist[i]);
+}
+
+// Chunk passes over tiles of kCkTile positions; warp w of a tile takes its positions
+// [w * kCkSpan, (w + 1) * kCkSpan), 32 consecutive ones a step.  A bucket's chunk comes from a
+// kBuckets-byte map (chunk numbers below kNoChunk).
+constexpr int kCkThreads = 256;
+constexpr int kCkWarps = kCkThreads / 32;
+constexpr int kCkSpan = kCkTile / kCkWarps;
+constexpr int kMaxChunks = 255;
+constexpr unsigned kNoChunk = 0xffu;
+
+// per tile and chunk: how many of the tile's positions fall in the chunk, into
+// tcnt[chunk * ntiles + tile]
+__global__ void __launch_bounds__(kCkThreads) k_chunk_tiles(const uint16_t* __restrict__ bid, size_t n,
+                                                            const uint8_t* __restrict__ cmap, int nchunks,
+                                                            size_t ntiles, unsigned long long* __restrict__ tcnt) {
+    __shared__ uint8_t s_map[kBuckets];
+    __shared__ unsigned s_cnt[kMaxChunks];
+    for (int i = threadIdx.x; i < kBuckets; i += blockDim.x) s_map[i] = cmap[i];
+    for (int c = threadIdx.x; c < nchunks; c += blockDim.x) s_cnt[c] = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    for (size_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const size_t t0 = tile * kCkTile;
+        #pragma unroll 4
+        for (int j = threadIdx.x; j < kCkTile; j += kCkThreads) {
+            const size_t p = t0 + size_t(j);
+            const unsigned c = p < n ? unsigned(s_map[bid[p]]) : kNoChunk;
+            const unsigned peers = __match_any_sync(0xffffffffu, c);
+            if (c != kNoChunk && lane == __ffs(peers) - 1) atomicAdd(&s_cnt[c], unsigned(__popc(peers)));
+        }
+        __syncthreads();
+        for (int c = threadIdx.x; c < nchunks; c += blockDim.x) {
+            tcnt[size_t(c) * ntiles + tile] = s_cnt[c];
+            s_cnt[c] = 0;
+        }
+        __syncthreads();
     }
 }
 
-// the positions of a chunk in text order (tile offsets from the exclusive scan of the counts)
+// Every position into its chunk's slice of `out`, in text order within the chunk.  toff is the
+// exclusive scan of tcnt in chunk-major order: the chunk's slice start plus the tile's place in
+// it.  A first walk over the tile counts each warp's positions per chunk, the warps' starts follow
+// from those counts, and a second walk (over the same bytes, from L1) writes, each warp keeping a
+// running offset per chunk.
 template <class V>
-__global__ void __launch_bounds__(256) k_chunk_write(const uint16_t* __restrict__ bid, size_t n, uint32_t lo,
-                                                    uint32_t hi, const unsigned long long* __restrict__ toff,
-                                                    V* __restrict__ list) {
-    __shared__ unsigned wsum[8];
-    __shared__ unsigned long long run;
-    const size_t t0 = size_t(blockIdx.x) * kCkTile;
+__global__ void __launch_bounds__(kCkThreads) k_chunk_scatter(const uint16_t* __restrict__ bid, size_t n,
+                                                              const uint8_t* __restrict__ cmap, int nchunks,
+                                                              size_t ntiles,
+                                                              const unsigned long long* __restrict__ toff,
+                                                              V* __restrict__ out) {
+    __shared__ uint8_t s_map[kBuckets];
+    __shared__ unsigned s_run[kCkWarps][kMaxChunks];     // per warp and chunk: place within the tile
+    __shared__ unsigned long long s_base[kMaxChunks];    // per chunk: the tile's start in `out`
+    for (int i = threadIdx.x; i < kBuckets; i += blockDim.x) s_map[i] = cmap[i];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (threadIdx.x == 0) run = toff[blockIdx.x];
-    __syncthreads();
-    for (int j0 = 0; j0 < kCkTile; j0 += 256) {
-        const size_t p = t0 + j0 + threadIdx.x;
-        bool in = false;
-        if (p < n) {
-            const uint32_t b = bid[p];
-            in = b >= lo && b < hi;
-        }
-        const unsigned bal = __ballot_sync(0xffffffffu, in);
-        if (lane == 0) wsum[warp] = __popc(bal);
+    const unsigned below = (1u << lane) - 1u;
+    for (size_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const size_t w0 = tile * kCkTile + size_t(warp) * kCkSpan;
+        for (int c = lane; c < nchunks; c += 32) s_run[warp][c] = 0;
         __syncthreads();
-        unsigned before = 0, all = 0;
-        for (int w = 0; w < 8; ++w) {
-            before += w < warp ? wsum[w] : 0u;
-            all += wsum[w];
+        for (int k = 0; k < kCkSpan; k += 32) {
+            const size_t p = w0 + size_t(k + lane);
+            const unsigned c = p < n ? unsigned(s_map[bid[p]]) : kNoChunk;
+            const unsigned peers = __match_any_sync(0xffffffffu, c);
+            if (c != kNoChunk && lane == __ffs(peers) - 1) s_run[warp][c] += unsigned(__popc(peers));
+            __syncwarp();
         }
-        if (in) list[run + before + __popc(bal & ((1u << lane) - 1))] = V(p);
         __syncthreads();
-        if (threadIdx.x == 0) run += all;
+        for (int c = threadIdx.x; c < nchunks; c += blockDim.x) {
+            s_base[c] = toff[size_t(c) * ntiles + tile];
+            unsigned run = 0;
+            for (int w = 0; w < kCkWarps; ++w) {
+                const unsigned x = s_run[w][c];
+                s_run[w][c] = run;
+                run += x;
+            }
+        }
+        __syncthreads();
+        for (int k = 0; k < kCkSpan; k += 32) {
+            const size_t p = w0 + size_t(k + lane);
+            const unsigned c = p < n ? unsigned(s_map[bid[p]]) : kNoChunk;
+            const unsigned peers = __match_any_sync(0xffffffffu, c);
+            if (c != kNoChunk) out[s_base[c] + s_run[warp][c] + __popc(peers & below)] = V(p);
+            __syncwarp();
+            if (c != kNoChunk && lane == __ffs(peers) - 1) s_run[warp][c] += unsigned(__popc(peers));
+            __syncwarp();
+        }
         __syncthreads();
     }
 }
 
+// the chunk's keys, and its positions copied from their slice of the suffix array into the radix
+// sort's value buffer (which starts 16-byte aligned, as the sort's staged tiles want)
 template <class V>
 __global__ void k_init_keys_list(const uint64_t* __restrict__ pk, const V* __restrict__ list, size_t m, DivL dl,
-                                 uint32_t* __restrict__ key) {
+                                 uint32_t* __restrict__ key, V* __restrict__ val) {
     const size_t stride = size_t(gridDim.x) * blockDim.x;
     for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < m; i += stride) {
-        const size_t p = size_t(list[i]);
+        const V v = list[i];
+        const size_t p = size_t(v);
         key[i] = make_key<uint32_t>(window(pk, p), int(dl.L - uint32_t(p - div_l(p, dl) * dl.L)));
+        val[i] = v;
     }
+}
+
+// chunks a greedy packing of buckets into `cap` can make: every chunk but the last is over half
+// full or ends before a bucket of more than half a chunk, so at most 2 n / cap + 2
+static size_t chunk_bound(size_t n, size_t cap) {
+    return std::min<size_t>(size_t(kMaxChunks), 2 * ((n + cap - 1) / cap) + 2);
 }
 
 static size_t chunk_parts(size_t n, size_t cap, size_t (&b)[11]) {
@@ -1477,8 +1530,8 @@ static size_t chunk_parts(size_t n, size_t cap, size_t (&b)[11]) {
     b[4] = cap * sizeof(uint32_t);                    // rank
     b[5] = (n / 32 + 4) * sizeof(uint64_t);           // packed text
     b[6] = radix_tmp_bytes(cap);
-    b[7] = (ntiles + 1) * sizeof(unsigned long long); // tile counts / offsets
-    b[8] = (size_t(kBuckets) + 8) * sizeof(unsigned long long);
+    b[7] = (chunk_bound(n, cap) * ntiles + 1) * sizeof(unsigned long long);   // tile counts / offsets
+    b[8] = (size_t(kBuckets) + 8) * sizeof(unsigned long long) + size_t(kBuckets);   // histogram, counters, map
     b[9] = n;                                         // BWT symbols of the refined rows
     b[10] = n * sizeof(uint16_t);                     // every position's 6-base bucket
     size_t t = 0;
@@ -1518,31 +1571,59 @@ int suffix_sort_chunked(const uint8_t* reads, idx_t num_reads, int L, int dir, i
     unsigned long long* hist = reinterpret_cast<unsigned long long*>(part[8]);
     unsigned long long* counters = hist + kBuckets;
     uint16_t* bid = reinterpret_cast<uint16_t*>(part[10]);
+    uint8_t* cmap = reinterpret_cast<uint8_t*>(counters + 8);
     const DivL dl = make_divl(uint32_t(L));
     const size_t nwords = n / 32 + 4;
     const size_t ntiles = (n + kCkTile - 1) / kCkTile;
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     { k_pack_text<<<grid_for(nwords, 256), 256, 0, st>>>(reads, n, idx_t(L), dir, nwords, pk); note_launch(); }
     cudaMemsetAsync(hist, 0, size_t(kBuckets) * sizeof(unsigned long long), st);
-    { k_bucket_hist<<<grid_for(n, 256), 256, 0, st>>>(pk, n, dl, bid, hist); note_launch(); }
+    const size_t hsm = size_t(kBuckets) * sizeof(unsigned);
+    cudaFuncSetAttribute(k_bucket_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, int(hsm));
+    { k_bucket_hist<<<unsigned(sms), kHistThreads, hsm, st>>>(pk, n, dl, bid, hist); note_launch(); }
     std::vector<unsigned long long> h(kBuckets);
     cudaMemcpyAsync(h.data(), hist, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
     cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return int(e);
-    size_t offset = 0;
-    uint32_t lo = 0;
-    while (lo < uint32_t(kBuckets)) {
-        // the next run of buckets that fits the chunk capacity
-        uint32_t hi = lo;
-        size_t m = 0;
-        while (hi < uint32_t(kBuckets) && m + h[hi] <= cap) m += h[hi++];
-        if (hi == lo) return int(cudaErrorNotSupported);          // one bucket larger than a chunk
-        if (m) {
-            { k_chunk_count<<<unsigned(ntiles), 256, 0, st>>>(bid, n, lo, hi, tcnt); note_launch(); }
-            { k_scan_small<<<1, 1024, 0, st>>>(tcnt, ntiles); note_launch(); }
-            { k_chunk_write<idx_t><<<unsigned(ntiles), 256, 0, st>>>(bid, n, lo, hi, tcnt, va0); note_launch(); }
+    // chunks: runs of consecutive buckets that fit the capacity, each a slice of the suffix array
+    std::vector<uint8_t> map(kBuckets, uint8_t(kNoChunk));
+    struct Chunk {
+        size_t offset, m;
+    };
+    std::vector<Chunk> chunks;
+    {
+        size_t offset = 0;
+        uint32_t lo = 0;
+        while (lo < uint32_t(kBuckets)) {
+            uint32_t hi = lo;
+            size_t m = 0;
+            while (hi < uint32_t(kBuckets) && m + h[hi] <= cap) m += h[hi++];
+            if (hi == lo) return int(cudaErrorNotSupported);          // one bucket larger than a chunk
+            if (m) {
+                if (chunks.size() >= chunk_bound(n, cap)) return int(cudaErrorNotSupported);
+                for (uint32_t b = lo; b < hi; ++b) map[b] = uint8_t(chunks.size());
+                chunks.push_back({offset, m});
+            }
+            offset += m;
+            lo = hi;
+        }
+    }
+    const int nchunks = int(chunks.size());
+    cudaMemcpyAsync(cmap, map.data(), map.size(), cudaMemcpyHostToDevice, st);
+    // every position into its chunk's slice of the suffix array, in text order: tile counts per
+    // chunk, their scan in chunk-major order (the slices' starts included), the scatter
+    const unsigned cgrid = unsigned(std::min<size_t>(ntiles, size_t(sms) * 8));
+    { k_chunk_tiles<<<cgrid, kCkThreads, 0, st>>>(bid, n, cmap, nchunks, ntiles, tcnt); note_launch(); }
+    { k_scan_small<<<1, 1024, 0, st>>>(tcnt, size_t(nchunks) * ntiles); note_launch(); }
+    { k_chunk_scatter<idx_t><<<cgrid, kCkThreads, 0, st>>>(bid, n, cmap, nchunks, ntiles, tcnt, sa); note_launch(); }
+    for (const Chunk& ck : chunks) {
+        const size_t offset = ck.offset, m = ck.m;
+        {
             uint32_t* ka = reinterpret_cast<uint32_t*>(ka0);
             uint32_t* kb = reinterpret_cast<uint32_t*>(kb0);
-            { k_init_keys_list<idx_t><<<grid_for(m, 256), 256, 0, st>>>(pk, va0, m, dl, ka); note_launch(); }
+            { k_init_keys_list<idx_t><<<grid_for(m, 256), 256, 0, st>>>(pk, sa + offset, m, dl, ka, va0); note_launch(); }
             idx_t* va = va0;
             idx_t* vb = vb0;
             int rc = radix_sort_pairs<uint32_t, idx_t>(&ka, &va, &kb, &vb, m, 0, 32, rtmp, radix_tmp_bytes(m), st, false);
@@ -1564,8 +1645,6 @@ int suffix_sort_chunked(const uint8_t* reads, idx_t num_reads, int L, int dir, i
                 if (ek != cudaSuccess) return int(ek);
             }
         }
-        offset += m;
-        lo = hi;
     }
     if (bwt_out) *bwt_out = bwt;
     return int(cudaGetLastError());
