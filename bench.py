@@ -143,26 +143,6 @@ def profile_figure(name: str, key: str):
     return float(m.group(1)) if m else None
 
 
-def huge_page_share(addr: int) -> float | None:
-    """Share of the host mapping holding `addr` that transparent huge pages back (/proc/self/smaps)."""
-    try:
-        size = huge = None
-        inside = False
-        for line in open("/proc/self/smaps"):
-            head = line.split()
-            if head and "-" in head[0] and len(head) > 4:
-                lo, hi = (int(x, 16) for x in head[0].split("-"))
-                inside = lo <= addr < hi
-            elif inside and line.startswith("Rss:"):
-                size = int(head[1])
-            elif inside and line.startswith("AnonHugePages:"):
-                huge = int(head[1])
-                break
-        return huge / size if size else None
-    except (OSError, ValueError):
-        return None
-
-
 def r4(x):
     """Four significant digits (keeps the JSON line short)."""
     if x is None or isinstance(x, (bool, int)):
@@ -431,8 +411,8 @@ def run_ours(args):
     dev = torch.device("cuda", local)
 
     t_start = time.time()
-    # the end-to-end steps' input buffer: page-locked and backed by huge pages (pq_host_alloc),
-    # so that its copy keeps its rate after the sorts and the search
+    # the end-to-end steps' input buffer: page-locked (pq_host_alloc), which pq_set_reads copies
+    # with a kernel that keeps the link's rate after the sorts and the search
     w = synth.WORKLOADS[args.workload]
     raw_reads = int(max(int(w["genome"] * args.scale), 4 * w["L"]) * w["cov"] // w["L"])
     pinned_all = torch.from_numpy(pq.host_empty((raw_reads, w["L"]), np.uint8))
@@ -509,7 +489,6 @@ def run_ours(args):
     c1.record(stream)
     torch.cuda.synchronize(dev)
     detail["h2d_copy_gbs"] = r4(nr * L / (c0.elapsed_time(c1) * 1e-3) / 1e9)
-    detail["host_huge_page_share"] = huge_page_share(pinned.numpy().ctypes.data)
     del probe
     e2e_ms, parts = [], []
     h2d = nr * L

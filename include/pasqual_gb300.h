@@ -65,14 +65,15 @@ PQ_API int pq_create (pq_ctx ** out, int device, void *cuda_stream);
 PQ_API void pq_destroy (pq_ctx * ctx);
 PQ_API const char *pq_last_error (const pq_ctx * ctx);
 
-/* Page-locked host memory for the buffers that cross to and from the device (reads in, graphs
- * out).  The region is mapped on huge-page boundaries, advised for transparent huge pages
- * (madvise; small pages where the kernel has none), touched, and registered with CUDA.  A copy
- * from it then needs one address translation per huge page.  Copies from small-page pinned
- * memory (cudaHostAlloc) were measured on GB300 at 11-17 GB/s when they followed a suffix sort
- * or a search, whose random accesses over most of device memory had evicted the translations,
- * against 210 GB/s from this memory in the same place.  *out is aligned to the huge-page size;
- * pq_host_free releases it.  PQ_ERR_NOMEM when the memory cannot be mapped or registered. */
+/* Page-locked host memory (cudaHostAlloc) for the buffers that cross to and from the device:
+ * reads in (pq_set_reads) and graphs out (pq_get_graph).  Both calls copy page-locked buffers with
+ * a copy kernel that reads or writes them directly, many accesses in flight: that keeps the
+ * link's rate (about 210 GB/s on GB300) right after a suffix sort or a search, where copy-engine
+ * copies (cudaMemcpy) from such memory were measured at 10-17 GB/s, and from cudaHostRegister'ed
+ * small-page memory at 2-35 GB/s even by kernel.  Allocate these buffers once, before the loop that
+ * reuses them.  pq_host_free releases a buffer from pq_host_alloc (PQ_ERR_ARG for any other
+ * pointer).  PQ_ERR_NOMEM when the memory cannot be allocated, PQ_ERR_CUDA when there is no usable
+ * device. */
 PQ_API int pq_host_alloc (size_t bytes, void **out);
 PQ_API int pq_host_free (void *p);
 
@@ -81,7 +82,8 @@ PQ_API int pq_host_free (void *p);
  * -t of the CLI, with SEQ_DEPTH(9) < min_overlap < read_len (src/test.c:306-311).
  * from_device != 0: `reads` is a device pointer.  PQ_ERR_ARG if any byte is not a base code
  * (the reference's import drops reads with N and rejects other symbols, src/index.c:304-318);
- * the context then holds no reads. */
+ * the context then holds no reads.  Page-locked host reads (cudaHostAlloc, pq_host_alloc,
+ * cudaHostRegister) are copied by a kernel that reads them directly; pageable ones by cudaMemcpy. */
 PQ_API int pq_set_reads (pq_ctx * ctx, const uint8_t * reads, pq_idx num_reads, int read_len,
                   int min_overlap, int from_device);
 
@@ -175,8 +177,9 @@ PQ_API int pq_get_search_traffic (pq_ctx * ctx, uint64_t * load_sectors, uint64_
  * olp_B, olp_F (overlaps_B/F of src/string_graph.c:807-808), edge_off[num_reads+1].  Per edge,
  * B edges then F edges of each read in the reference's DFS order: dest, overlap length, type
  * (BF=0 FB=1 FF=2 BB=3) and the path_t.trans value (src/string_graph.c:940, 970).  Any pointer
- * may be NULL (that array is skipped).  Page-locked or already-touched host arrays copy at link
- * speed; freshly allocated pageable ones pay their first-touch page faults inside this call. */
+ * may be NULL (that array is skipped).  Page-locked host arrays (pq_host_alloc, cudaHostAlloc) are
+ * written by a copy kernel at link speed; freshly allocated pageable ones pay their first-touch
+ * page faults inside this call. */
 PQ_API int pq_get_graph (pq_ctx * ctx, uint16_t * num_B, uint16_t * num_F, int32_t * olp_B,
                   int32_t * olp_F, uint64_t * edge_off, pq_idx * dest, uint16_t * len,
                   uint8_t * type, int32_t * trans);

@@ -178,10 +178,9 @@ def mlp_adam_step(params: np.ndarray, m1: np.ndarray, m2: np.ndarray, x: np.ndar
 
 
 def host_empty(shape, dtype=np.uint8, width: int = 32) -> np.ndarray:
-    """A host array in page-locked, huge-page-backed memory (pq_host_alloc), for the buffers that
-    cross to the device and back: copies from it keep their full rate after a sort or search,
-    where copies from small-page pinned memory slow down ten-fold.  Released when the array and
-    every view of it are gone."""
+    """A host array in page-locked memory (pq_host_alloc), for the buffers that cross to the device
+    and back: pq_set_reads and pq_get_graph copy such buffers with a kernel that keeps the link's
+    rate after a sort or search.  Released when the array and every view of it are gone."""
     lib = load_library(width)
     dt = np.dtype(dtype)
     count = int(np.prod(shape, dtype=np.int64))

@@ -19,10 +19,6 @@ static_assert(sizeof(pq_idx) == sizeof(idx_t), "pq_idx and idx_t must agree");
 #include <mutex>
 #include <thread>
 #include <unordered_map>
-#include <sys/mman.h>
-#ifndef MADV_COLLAPSE
-#define MADV_COLLAPSE 25
-#endif
 namespace pq {
 static std::atomic<unsigned long long> g_launches{0};
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
@@ -159,77 +155,44 @@ extern "C" {
 int pq_idx_bytes(void) { return int(sizeof(idx_t)); }
 
 namespace {
-// Host regions handed out by pq_host_alloc: aligned address -> the mapping it lies in.
-struct HostRegion {
-    void* base;
-    size_t total;
-};
+// Host buffers handed out by pq_host_alloc (pq_host_free accepts only these).
 std::mutex g_host_mu;
-std::unordered_map<void*, HostRegion> g_host;
-
-size_t huge_page_bytes() {
-    unsigned long long v = 0;
-    if (FILE* f = fopen("/sys/kernel/mm/transparent_hugepage/hpage_pmd_size", "r")) {
-        if (fscanf(f, "%llu", &v) != 1) v = 0;
-        fclose(f);
-    }
-    return (v >= 4096 && (v & (v - 1)) == 0) ? size_t(v) : (size_t(2) << 20);
-}
+std::unordered_map<void*, size_t> g_host;
 }  // namespace
 
 int pq_host_alloc(size_t bytes, void** out) {
     if (!out) return PQ_ERR_ARG;
     *out = nullptr;
-    // The device's context first: registered as the process's first CUDA call (the context
-    // created inside cudaHostRegister), a region was measured to lose some of its huge pages and
-    // to copy at a half to a twentieth of the rate of one registered afterwards.
-    if (cudaFree(nullptr) != cudaSuccess) {
+    void* p = nullptr;
+    const cudaError_t e = cudaHostAlloc(&p, std::max<size_t>(bytes, 1), cudaHostAllocDefault);
+    if (e != cudaSuccess) {
         cudaGetLastError();
-        return PQ_ERR_CUDA;
-    }
-    const size_t hp = huge_page_bytes();
-    const size_t size = (std::max<size_t>(bytes, 1) + hp - 1) / hp * hp;
-    const size_t total = size + hp;
-    void* base = mmap(nullptr, total, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
-    if (base == MAP_FAILED) return PQ_ERR_NOMEM;
-    char* p = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(base) + hp - 1) / hp * hp);
-    madvise(p, size, MADV_HUGEPAGE);      // advice only: small pages where there are no huge ones
-    // fault the pages in (huge pages are zeroed by the kernel), one huge page per step, in parallel
-    const size_t pages = size / hp;
-    const size_t nth = std::max<size_t>(1, std::min<size_t>(pages, std::max(1u, std::thread::hardware_concurrency())));
-    std::vector<std::thread> th;
-    for (size_t t = 0; t < nth; ++t)
-        th.emplace_back([=] {
-            for (size_t i = t; i < pages; i += nth) memset(p + i * hp, 0, hp);
-        });
-    for (auto& x : th) x.join();
-    // where a fault found no free huge page (a fragmented host), ask once more, synchronously:
-    // MADV_COLLAPSE compacts and rebuilds the range in huge pages (Linux 6.1+; an error is ignored)
-    madvise(p, size, MADV_COLLAPSE);
-    if (cudaHostRegister(p, size, cudaHostRegisterDefault) != cudaSuccess) {
-        cudaGetLastError();
-        munmap(base, total);
-        return PQ_ERR_NOMEM;
+        return e == cudaErrorMemoryAllocation ? PQ_ERR_NOMEM : PQ_ERR_CUDA;
     }
     std::lock_guard<std::mutex> g(g_host_mu);
-    g_host[p] = HostRegion{base, total};
+    g_host[p] = bytes;
     *out = p;
     return PQ_OK;
 }
 
 int pq_host_free(void* p) {
     if (!p) return PQ_OK;
-    HostRegion r{};
     {
         std::lock_guard<std::mutex> g(g_host_mu);
         auto it = g_host.find(p);
         if (it == g_host.end()) return PQ_ERR_ARG;
-        r = it->second;
         g_host.erase(it);
     }
-    cudaHostUnregister(p);
-    munmap(r.base, r.total);
-    return PQ_OK;
+    return cudaFreeHost(p) == cudaSuccess ? PQ_OK : PQ_ERR_CUDA;
+}
+
+// The device-accessible address of page-locked host memory (cudaHostAlloc'd or registered), or
+// null for pageable memory.
+static void* locked_device_ptr(const void* host) {
+    cudaPointerAttributes pa{};
+    const bool ok = cudaPointerGetAttributes(&pa, host) == cudaSuccess && pa.type == cudaMemoryTypeHost;
+    cudaGetLastError();
+    return ok ? pa.devicePointer : nullptr;
 }
 
 int pq_create(pq_ctx** out, int device, void* cuda_stream) {
@@ -321,14 +284,11 @@ int pq_set_reads(pq_ctx* ctx, const uint8_t* reads, pq_idx num_reads, int read_l
     size_t bytes = size_t(num_reads) * read_len;
     CK(ctx->reads.ensure(bytes + 64));
     if (bytes) {
-        // page-locked host memory (cudaHostAlloc'd or registered) is read by the upload kernel;
+        // page-locked host memory (cudaHostAlloc'd or registered) is read by the copy kernel;
         // pageable memory goes through cudaMemcpy
-        cudaPointerAttributes pa{};
-        const bool pinned = !from_device && cudaPointerGetAttributes(&pa, reads) == cudaSuccess &&
-                            pa.type == cudaMemoryTypeHost && pa.devicePointer != nullptr;
-        cudaGetLastError();
-        if (pinned)
-            CK(pq::upload(ctx->reads.as<uint8_t>(), static_cast<const uint8_t*>(pa.devicePointer), bytes, ctx->st));
+        const void* locked = from_device ? nullptr : locked_device_ptr(reads);
+        if (locked)
+            CK(pq::kernel_copy(ctx->reads.p, locked, bytes, ctx->st));
         else
             CK(cudaMemcpyAsync(ctx->reads.p, reads, bytes,
                                from_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, ctx->st));
@@ -818,6 +778,39 @@ static int search_finish(pq_ctx* ctx, pq::SearchArgs& A, pq::SearchOut& O) {
                 ovf = left2;
                 ovf_src = ctx->ovf4.as<idx_t>();
                 ovf_cnt = reinterpret_cast<const unsigned*>(ctr + 8);
+                // reads that found the edge pool full: grow it past everything reserved so far
+                // (twice that covers every failed reservation made again) and run them once more
+                unsigned long long reserved = 0;
+                if (ovf) {
+                    CK(cudaMemcpyAsync(&reserved, ctr + 0, sizeof reserved, cudaMemcpyDeviceToHost, ctx->st));
+                    CK(cudaStreamSynchronize(ctx->st));
+                }
+                if (ovf && reserved > O.e_cap) {
+                    const size_t need = size_t(2 * reserved + 4096), keep = O.e_cap;
+                    CK(ctx->e_dest.grow(need * sizeof(idx_t), keep * sizeof(idx_t), ctx->st));
+                    CK(ctx->e_trans.grow(need * 4, keep * 4, ctx->st));
+                    CK(ctx->e_len.grow(need * 2, keep * 2, ctx->st));
+                    CK(ctx->e_type.grow(need, keep, ctx->st));
+                    O.e_dest = ctx->e_dest.as<idx_t>();
+                    O.e_trans = ctx->e_trans.as<int32_t>();
+                    O.e_len = ctx->e_len.as<uint16_t>();
+                    O.e_type = ctx->e_type.as<uint8_t>();
+                    O.e_cap = need;
+                    const int gb2 = pq::block_global_blocks(ovf);
+                    const size_t gbytes2 = pq::block_global_bytes(ctx->L, ctx->t, gb2);
+                    CK(ctx->block_scratch.ensure(gbytes2));
+                    CK(cudaMemsetAsync(ctr + 7, 0, sizeof(unsigned long long), ctx->st));
+                    CK(pq::search_block_global(A, O, ovf_src, ovf_cnt, ovf, gb2, ctx->block_scratch.p, gbytes2,
+                                               ctx->ovf3.as<idx_t>(), reinterpret_cast<unsigned*>(ctr + 7), ctx->st));
+                    unsigned long long h7b = 0;
+                    CK(cudaMemcpyAsync(&h7b, ctr + 7, sizeof h7b, cudaMemcpyDeviceToHost, ctx->st));
+                    CK(cudaStreamSynchronize(ctx->st));
+                    const unsigned left3 = unsigned(h7b & 0xffffffffu);
+                    ctx->block_reads += ovf - left3;
+                    ovf = left3;
+                    ovf_src = ctx->ovf3.as<idx_t>();
+                    ovf_cnt = reinterpret_cast<const unsigned*>(ctr + 7);
+                }
             }
         }
         ctx->ms_block = wall_ms() - tb0;
@@ -1004,8 +997,10 @@ int pq_get_graph(pq_ctx* ctx, uint16_t* num_B, uint16_t* num_F, int32_t* olp_B, 
     if (!ctx->graph_ok) return fail(ctx, PQ_ERR_STATE, "pq_overlaps first");
     const size_t nr = ctx->num_reads, ne = ctx->num_edges;
     cudaStream_t s = ctx->st;
+    // page-locked destinations are written by the copy kernel, pageable ones by cudaMemcpy
     auto d2h = [&](void* h, const DevBuf& b, size_t bytes) -> cudaError_t {
         if (!h || !bytes) return cudaSuccess;
+        if (void* locked = locked_device_ptr(h)) return pq::kernel_copy(locked, b.p, bytes, s);
         return cudaMemcpyAsync(h, b.p, bytes, cudaMemcpyDeviceToHost, s);
     };
     CK(d2h(num_B, ctx->nB, nr * 2));

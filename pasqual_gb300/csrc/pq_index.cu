@@ -427,14 +427,15 @@ cudaError_t build_occ(const idx_t* sa, const uint8_t* reads, idx_t num_reads, id
     return cudaGetLastError();
 }
 
-// Host -> device copy of n bytes by a kernel that reads page-locked host memory directly: four
-// independent 16-byte loads a thread, 32 CTAs per SM.  So many loads in flight keep the copy at
-// the link's rate even when the GPU's cached translations of the host pages were evicted by a sort
-// or a search over most of device memory (a copy-engine cudaMemcpy from the same buffer then fell
-// to ~10 GB/s).  Bytes before the first 16-byte boundary and after the last are copied one by one;
-// when source and destination are not equally aligned the whole copy goes byte by byte.
-__global__ void __launch_bounds__(256) k_upload(uint8_t* __restrict__ dst, const uint8_t* __restrict__ src,
-                                                size_t n) {
+// Copy of n bytes between page-locked host memory and device memory by a kernel (either side may
+// be the host's, at its device-accessible address): four independent 16-byte accesses a thread,
+// 32 CTAs per SM.  So many accesses in flight keep the copy at the link's rate right after a sort
+// or a search over most of device memory, where a copy-engine cudaMemcpy from the same
+// (cudaHostAlloc'd) buffer was measured at ~10 GB/s.  Bytes before the first 16-byte boundary
+// and after the last go one by one; when the two sides are not equally aligned the whole copy
+// goes byte by byte.
+__global__ void __launch_bounds__(256) k_copy_bytes(uint8_t* __restrict__ dst, const uint8_t* __restrict__ src,
+                                                    size_t n) {
     const size_t tid = size_t(blockIdx.x) * blockDim.x + threadIdx.x, stride = size_t(gridDim.x) * blockDim.x;
     const size_t mis = reinterpret_cast<uintptr_t>(src) & 15;
     if (mis != (reinterpret_cast<uintptr_t>(dst) & 15)) {
@@ -458,14 +459,14 @@ __global__ void __launch_bounds__(256) k_upload(uint8_t* __restrict__ dst, const
     for (; i < n16; i += stride) d[i] = s[i];
 }
 
-cudaError_t upload(uint8_t* dst, const uint8_t* src, size_t n, cudaStream_t st) {
+cudaError_t kernel_copy(void* dst, const void* src, size_t n, cudaStream_t st) {
     if (!n) return cudaSuccess;
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const size_t want = (n / 16 + 255) / 256;
     const unsigned blocks = unsigned(std::max<size_t>(1, std::min<size_t>(want, size_t(sms) * 32)));
-    k_upload<<<blocks, 256, 0, st>>>(dst, src, n);
+    k_copy_bytes<<<blocks, 256, 0, st>>>(static_cast<uint8_t*>(dst), static_cast<const uint8_t*>(src), n);
     note_launch();
     return cudaGetLastError();
 }

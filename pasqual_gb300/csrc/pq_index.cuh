@@ -11,8 +11,9 @@ cudaError_t build_occ(const idx_t* sa, const uint8_t* reads, idx_t num_reads, id
                       OccBlock* blk, idx_t* sb, idx_t* reads_index, cudaStream_t st, const uint64_t* pk = nullptr,
                       const uint8_t* hint = nullptr);
 // out13: base counts [4], last-base counts [4], first-base counts [4], bytes outside 1..4
-// n bytes from page-locked host memory (a device-accessible address) to device memory, by a kernel
-cudaError_t upload(uint8_t* dst, const uint8_t* src, size_t n, cudaStream_t st);
+// n bytes between device memory and page-locked host memory (at its device-accessible address),
+// copied by a kernel
+cudaError_t kernel_copy(void* dst, const void* src, size_t n, cudaStream_t st);
 cudaError_t read_counts(const uint8_t* reads, idx_t num_reads, idx_t L, unsigned long long* out13,
                         cudaStream_t st);
 // k-mer table of direction dir: from the sort's keys when sorted_keys is given, else from the

@@ -1877,14 +1877,16 @@ constexpr size_t kBlockSmemBudget = 200 * 1024;     // dynamic shared memory of 
 
 struct BlockSmem {      // the block tier's dynamic shared memory (offsets in bytes)
     size_t words, ids, metas, cnts, elist, e_ids, e_metas, e_trans, groups, prefs, read, bytes;
+    size_t perm0, perm1, info;      // the sorted reduction's order and walk arrays (global variant)
     int cap;            // candidates a side (and B-side edges kept while the F side is reduced)
     int nw;             // continuation words per candidate
 };
 
-// bytes a candidate takes (continuation words, read id, meta, counter, emitted list, B-side edge)
-// and the fixed part (both sides' candidate groups, their prefix sums, the read)
-size_t block_per_cand(int L, int t) {
-    return size_t((L - t + 31) / 32) * 8 + sizeof(idx_t) + 4 + 4 + 4 + sizeof(idx_t) + 4 + 4;
+// bytes a candidate takes (continuation words, read id, meta, counter, emitted list, B-side edge;
+// with `sorted`, two order arrays and the walk's array) and the fixed part (both sides' candidate
+// groups, their prefix sums, the read)
+size_t block_per_cand(int L, int t, bool sorted = false) {
+    return size_t((L - t + 31) / 32) * 8 + sizeof(idx_t) + 4 + 4 + 4 + sizeof(idx_t) + 4 + 4 + (sorted ? 12 : 0);
 }
 size_t block_fixed(int L, int t) {
     const int M = L - t;
@@ -1892,14 +1894,14 @@ size_t block_fixed(int L, int t) {
            size_t((L + 15) / 16) * sizeof(uint32_t) + 16 * 16;
 }
 
-BlockSmem block_smem_layout(int L, int t, size_t budget) {
+BlockSmem block_smem_layout(int L, int t, size_t budget, bool sorted = false) {
     BlockSmem b{};
     const int M = L - t;
     b.nw = (M + 31) / 32;
     const size_t groups = size_t(2) * size_t(2 * M) * sizeof(Cand);
     const size_t prefs = size_t(2 * M + 1) * sizeof(unsigned);
     const size_t read = size_t((L + 15) / 16) * sizeof(uint32_t);
-    const size_t per = block_per_cand(L, t);
+    const size_t per = block_per_cand(L, t, sorted);
     const size_t fixed = block_fixed(L, t);
     int cap = budget > fixed ? int(std::min<size_t>((budget - fixed) / per, 65535)) : 0;
     cap &= ~31;
@@ -1921,6 +1923,12 @@ BlockSmem block_smem_layout(int L, int t, size_t budget) {
     b.groups = take(groups);
     b.prefs = take(prefs);
     b.read = take(read);
+    b.perm0 = b.perm1 = b.info = 0;
+    if (sorted) {
+        b.perm0 = take(size_t(cap) * 4);
+        b.perm1 = take(size_t(cap) * 4);
+        b.info = take(size_t(cap) * 4);
+    }
     b.bytes = o;
     return b;
 }
@@ -1944,8 +1952,143 @@ __device__ __forceinline__ int block_cmp(const uint64_t* w, int cap, int nw, int
     return la == lb ? 0 : (la < lb ? -1 : 1);
 }
 
+// 4-bit digit q (0 = least significant) of candidate c's sort key: the continuation words (word 0
+// most significant), then the continuation length (16 bits), then the read id.
+__device__ __forceinline__ unsigned block_digit(const uint64_t* cw, int cap, int nw, const idx_t* cid,
+                                                const uint32_t* cmeta, int L, int c, int q) {
+    constexpr int kIdDigits = 2 * int(sizeof(idx_t));
+    if (q < kIdDigits) return unsigned(uint64_t(cid[c]) >> (4 * q)) & 15u;
+    q -= kIdDigits;
+    if (q < 4) return (unsigned(L - meta_len(cmeta[c])) >> (4 * q)) & 15u;
+    q -= 4;
+    return unsigned(cw[size_t(nw - 1 - q / 16) * cap + c] >> (4 * (q % 16))) & 15u;
+}
+
+// One side's reduction by sorting, for the global-memory block tier (m up to 32768 candidates,
+// where the m x m pair tests cost too much).  The candidates are ordered by (continuation, read id)
+// with a stable LSD radix sort on 4-bit digits of (continuation words, length, read id): each
+// thread counts and then places one contiguous run of the current order, and a digit that is the
+// same for every candidate skips its placing.  Comparing the words (zero past each continuation's
+// end) and then the length is the order in which a continuation precedes its extensions, so the
+// candidates whose continuation starts with a given one follow it contiguously.  One walk then
+// decides what the pair tests decide: a run of equal continuations with no earlier prefix among
+// them is uncovered, the candidates after it that extend it are covered, trans = the run plus its
+// extensions, and the run's second-kind candidates yield when a first-kind one is in it.  The
+// emitted candidates come out in sorted order, which is the DFS order; they are written as the
+// pair version writes them (B side: e_id/e_meta/e_trans by rank; F side: elist by rank, ccnt[c] =
+// rank).  Returns the number emitted (in thread 0).
+__device__ int block_sorted_side(int m, int L, int nw, int cap, const uint64_t* cw, const idx_t* cid,
+                                 const uint32_t* cmeta, uint32_t* perm0, uint32_t* perm1, uint32_t* info,
+                                 unsigned* scnt, unsigned* s_misc, int first_kind, idx_t self, int side,
+                                 idx_t* e_id, uint32_t* e_meta, int32_t* e_trans, uint32_t* elist, uint32_t* ccnt) {
+    constexpr int T = kBlockThreads;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int per = (m + T - 1) / T;
+    const int b0 = min(m, tid * per), b1 = min(m, b0 + per);
+    for (int i = tid; i < m; i += T) perm0[i] = uint32_t(i);
+    uint32_t* src = perm0;
+    uint32_t* dst = perm1;
+    const int digits = 2 * int(sizeof(idx_t)) + 4 + 16 * nw;
+    unsigned* s_wsum = s_misc;             // [T / 32]
+    unsigned* s_dstart = s_misc + 8;       // [17]
+    __syncthreads();
+    for (int q = 0; q < digits; ++q) {
+        #pragma unroll
+        for (int d = 0; d < 16; ++d) scnt[d * T + tid] = 0;
+        for (int e = b0; e < b1; ++e) ++scnt[block_digit(cw, cap, nw, cid, cmeta, L, int(src[e]), q) * T + tid];
+        __syncthreads();
+        // exclusive scan of the 16 x T counts, digit-major: thread tid owns entries [16 tid, 16 tid + 16)
+        unsigned mine = 0;
+        #pragma unroll
+        for (int j = 0; j < 16; ++j) mine += scnt[16 * tid + j];
+        unsigned x = mine;
+        #pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) s_wsum[wid] = x;
+        __syncthreads();
+        unsigned run = x - mine;
+        for (int w = 0; w < wid; ++w) run += s_wsum[w];
+        #pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            const unsigned v = scnt[16 * tid + j];
+            scnt[16 * tid + j] = run;
+            run += v;
+        }
+        if ((16 * tid) % T == 0) s_dstart[(16 * tid) / T] = run - mine;   // the digit's first place
+        if (tid == 0) s_dstart[16] = unsigned(m);
+        __syncthreads();
+        bool trivial = false;
+        #pragma unroll
+        for (int d = 0; d < 16; ++d) trivial |= s_dstart[d + 1] - s_dstart[d] == unsigned(m);
+        if (!trivial) {
+            for (int e = b0; e < b1; ++e) {
+                const uint32_t c = src[e];
+                dst[scnt[block_digit(cw, cap, nw, cid, cmeta, L, int(c), q) * T + tid]++] = c;
+            }
+            uint32_t* tmp = src;
+            src = dst;
+            dst = tmp;
+        }
+        __syncthreads();
+    }
+    // per position of the order: common prefix with the previous candidate (bases, capped at both
+    // lengths) and the continuation length
+    for (int k = tid; k < m; k += T) {
+        const int c = int(src[k]);
+        const int lc = L - meta_len(cmeta[c]);
+        int lcp = 0;
+        if (k > 0) {
+            const int a = int(src[k - 1]);
+            const int la = L - meta_len(cmeta[a]);
+            lcp = 32 * nw;
+            for (int w = 0; w < nw; ++w) {
+                const uint64_t z = cw[size_t(w) * cap + a] ^ cw[size_t(w) * cap + c];
+                if (z) {
+                    lcp = 32 * w + (__clzll(z) >> 1);
+                    break;
+                }
+            }
+            lcp = min(lcp, min(la, lc));
+        }
+        info[k] = uint32_t(lcp) | (uint32_t(lc) << 16);
+    }
+    __syncthreads();
+    int ne = 0;
+    if (tid == 0) {
+        for (int i = 0; i < m;) {
+            const int lr = int(info[i] >> 16);
+            int k = i + 1;
+            while (k < m && int(info[k] & 0xffffu) >= lr && int(info[k] >> 16) == lr) ++k;
+            const int eq_end = k;
+            while (k < m && int(info[k] & 0xffffu) >= lr) ++k;
+            const int32_t trans = int32_t(k - i);
+            bool first_same = false;
+            for (int j = i; j < eq_end; ++j) first_same |= meta_type(cmeta[src[j]]) == first_kind;
+            for (int j = i; j < eq_end; ++j) {
+                const int c = int(src[j]);
+                if (cid[c] == self || (meta_type(cmeta[c]) != first_kind && first_same)) continue;
+                if (side == 0) {
+                    e_id[ne] = cid[c];
+                    e_meta[ne] = cmeta[c];
+                    e_trans[ne] = trans;
+                } else {
+                    elist[ne] = uint32_t(c) | (uint32_t(trans) << 16);
+                    ccnt[c] = uint32_t(ne);
+                }
+                ++ne;
+            }
+            i = k;
+        }
+    }
+    return ne;
+}
+
 // kGlobal: the candidate arrays live in a per-CTA region of `scratch` (global memory, cached in
-// L1/L2) instead of shared memory, for sides with more candidates than shared memory holds.
+// L1/L2) instead of shared memory, for sides with more candidates than shared memory holds; each
+// side is then reduced by sorting (block_sorted_side) instead of by pair tests.
 template <bool kGlobal>
 __global__ void __launch_bounds__(kBlockThreads) k_search_block(SearchArgs A, SearchOut O, const idx_t* list,
                                                                 const unsigned* list_count, BlockSmem lay,
@@ -1954,6 +2097,11 @@ __global__ void __launch_bounds__(kBlockThreads) k_search_block(SearchArgs A, Se
     extern __shared__ __align__(16) unsigned char smem_dyn[];
     unsigned char* smem = kGlobal ? scratch + size_t(blockIdx.x) * lay.bytes : smem_dyn;
     uint64_t* cw = reinterpret_cast<uint64_t*>(smem + lay.words);
+    uint32_t* perm0 = reinterpret_cast<uint32_t*>(smem + lay.perm0);
+    uint32_t* perm1 = reinterpret_cast<uint32_t*>(smem + lay.perm1);
+    uint32_t* sinfo = reinterpret_cast<uint32_t*>(smem + lay.info);
+    unsigned* scnt = reinterpret_cast<unsigned*>(smem_dyn);              // global variant: 16 x 256 counts
+    unsigned* smisc = scnt + 16 * kBlockThreads;
     idx_t* cid = reinterpret_cast<idx_t*>(smem + lay.ids);
     uint32_t* cmeta = reinterpret_cast<uint32_t*>(smem + lay.metas);
     uint32_t* ccnt = reinterpret_cast<uint32_t*>(smem + lay.cnts);
@@ -2048,8 +2196,15 @@ __global__ void __launch_bounds__(kBlockThreads) k_search_block(SearchArgs A, Se
                 cmeta[i] = pack_meta(d, c.type);
             }
             __syncthreads();
-            // all pairs: covered (bit 0), first_same (bit 1), trans (bits 2..)
             const int first_kind = side ? PQ_FB : PQ_BF;
+            if constexpr (kGlobal) {
+                const int nsorted = block_sorted_side(m, L, nw, cap, cw, cid, cmeta, perm0, perm1, sinfo, scnt, smisc,
+                                                      first_kind, self, side, e_id, e_meta, e_trans, elist, ccnt);
+                if (tid == 0) s_cnt[side] = nsorted;
+                __syncthreads();
+                continue;
+            }
+            // all pairs: covered (bit 0), first_same (bit 1), trans (bits 2..)
             for (int c = tid; c < m; c += kBlockThreads) {
                 const int lc = L - meta_len(cmeta[c]);
                 uint32_t v = 0;
@@ -2192,8 +2347,11 @@ int block_global_blocks(unsigned count) {
 }
 
 BlockSmem block_global_layout(int L, int t) {
-    return block_smem_layout(L, t, block_per_cand(L, t) * kBlockGlobalCap + block_fixed(L, t));
+    return block_smem_layout(L, t, block_per_cand(L, t, true) * kBlockGlobalCap + block_fixed(L, t), true);
 }
+// the global variant's dynamic shared memory: the sort's 16 x kBlockThreads digit counts and a
+// few words of scan state
+constexpr size_t kBlockSortSmem = (16 * kBlockThreads + 32) * sizeof(unsigned);
 
 size_t block_global_bytes(int L, int t, int blocks) { return size_t(blocks) * block_global_layout(L, t).bytes; }
 
@@ -2203,8 +2361,8 @@ cudaError_t search_block_global(const SearchArgs& a, const SearchOut& o, const i
     if (!count_host || blocks <= 0) return cudaSuccess;
     const BlockSmem lay = block_global_layout(a.L, a.t);
     if (scratch_bytes < size_t(blocks) * lay.bytes) return cudaErrorInvalidValue;
-    k_search_block<true><<<blocks, kBlockThreads, 0, st>>>(a, o, list, count, lay, next_list, next_count,
-                                                           static_cast<unsigned char*>(scratch));
+    k_search_block<true><<<blocks, kBlockThreads, kBlockSortSmem, st>>>(a, o, list, count, lay, next_list, next_count,
+                                                                        static_cast<unsigned char*>(scratch));
     note_launch();
     return cudaGetLastError();
 }

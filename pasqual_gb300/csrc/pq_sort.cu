@@ -427,12 +427,21 @@ int radix_sort_pairs(K** k0, V** v0, K** k1, V** v1, size_t n, int lo_bit, int h
         if (e != cudaSuccess) return int(e);
     }
     size_t tiles = (n + RS_TILE_MAX - 1) / RS_TILE_MAX;
-    // one wave of resident CTAs
-    size_t ctas = std::min<size_t>(tiles, std::min<size_t>(RS_MAX_CTAS, size_t(152) * RsCfg<K, V>::min_blocks));
-    size_t part = ((tiles + ctas - 1) / ctas) * RS_TILE_MAX;
-    ctas = (n + part - 1) / part;
+    // one wave of resident CTAs: as many per SM as the downsweep's shared memory and registers
+    // allow (a grid sized for more ran a second, partial wave on a fraction of the SMs)
     const size_t smem = rs_down_smem<K, V>();
     cudaFuncSetAttribute(k_rs_downsweep<K, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    int dev = 0, sms = 152, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rs_downsweep<K, V>, RsCfg<K, V>::threads, smem) !=
+            cudaSuccess || per_sm < 1) {
+        cudaGetLastError();
+        per_sm = 1;
+    }
+    size_t ctas = std::min<size_t>(tiles, std::min<size_t>(RS_MAX_CTAS, size_t(sms) * size_t(per_sm)));
+    size_t part = ((tiles + ctas - 1) / ctas) * RS_TILE_MAX;
+    ctas = (n + part - 1) / part;
     for (int d = lo_bit / 8; d * 8 < hi_bit; ++d) {
         bool trivial = false;
         for (int b = 0; b < 256; ++b)

@@ -143,6 +143,28 @@ def test_handed_over_tiers_used_and_exact(name):
     assert sha(graph.trans_with_mask(out.num_B, out.num_F, out.edge_off, out.trans)) == str(g["sha_trans"])
 
 
+def test_block_tier_in_global_memory_matches_reference_method():
+    """The 200 Mbp, 150 bp workload (2 % dinucleotide runs) at 1/100 genome: its run reads have
+    thousands of candidates a side, more than the block tier holds in shared memory, so they are
+    reduced by the global-memory block tier (sorted reduction).  Every edge field equals the
+    reference's method on the GPU (seed mode 0: walk + FM-index DFS, no block tier), and no read
+    reaches the heavy or wide tier."""
+    _, rd, L, t = synth.make_workload("200Mbp_L150_20x_t63", scale=0.01)
+    rd = synth.dedup(rd)
+    out, tiers = {}, None
+    for mode in (0, 1):
+        with gpu_ctx(64) as P:
+            P.set_reads(rd, t)
+            P.set_seed_mode(mode)
+            P.build_index()
+            out[mode] = P.construct_string_graph()
+            if mode == 1:
+                tiers = P.tier_stats()
+    assert tiers["block"] > 1000 and tiers["heavy"] == 0 and tiers["wide"] == 0, tiers
+    for f in ("edge_off", "dest", "length", "etype", "trans", "num_B", "num_F", "olp_B", "olp_F"):
+        assert np.array_equal(getattr(out[0], f), getattr(out[1], f)), f
+
+
 def _oracle_run(reads, t, width):
     from oracle import port
     P = port.Port(width)
