@@ -1409,11 +1409,35 @@ __global__ void __launch_bounds__(kHistThreads) k_bucket_hist(const uint64_t* __
     extern __shared__ unsigned s_hist[];
     for (int i = threadIdx.x; i < kBuckets; i += blockDim.x) s_hist[i] = 0;
     __syncthreads();
+    // eight consecutive positions a thread a step: their windows come from the same two words of
+    // the packed text (the first position is a multiple of 8), their read offsets from one
+    // multiply-high, their buckets go out in one 16-byte store
+    const size_t groups = (n + 7) / 8;
     const size_t stride = size_t(gridDim.x) * blockDim.x;
-    for (size_t p = size_t(blockIdx.x) * blockDim.x + threadIdx.x; p < n; p += stride) {
-        const uint32_t b = bucket_of(pk, p, dl);
-        bid[p] = uint16_t(b);
-        atomicAdd(&s_hist[b], 1u);
+    for (size_t g = size_t(blockIdx.x) * blockDim.x + threadIdx.x; g < groups; g += stride) {
+        const size_t p0 = g * 8;
+        const uint64_t a = pk[p0 >> 5], b = pk[(p0 >> 5) + 1];
+        const int s0 = int(p0 & 31);
+        int off = int(uint32_t(p0 - div_l(p0, dl) * dl.L));
+        uint32_t v[8];
+        #pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int sh = 2 * (s0 + j);
+            const uint64_t x = sh ? ((a << sh) | (b >> (64 - sh))) : a;
+            const int m = int(dl.L) - off;
+            const int w = m < kBucketBases ? m : kBucketBases;
+            const uint32_t pre = uint32_t(x >> (64 - 2 * kBucketBases)) & (~0u << (2 * (kBucketBases - w)));
+            v[j] = (pre << 3) | uint32_t(w);
+            if (p0 + size_t(j) < n) atomicAdd(&s_hist[v[j]], 1u);
+            off = off + 1 == int(dl.L) ? 0 : off + 1;
+        }
+        if (p0 + 8 <= n) {
+            *reinterpret_cast<uint4*>(bid + p0) =
+                make_uint4(v[0] | (v[1] << 16), v[2] | (v[3] << 16), v[4] | (v[5] << 16), v[6] | (v[7] << 16));
+        } else {
+            for (int j = 0; j < 8; ++j)
+                if (p0 + size_t(j) < n) bid[p0 + j] = uint16_t(v[j]);
+        }
     }
     __syncthreads();
     for (int i = threadIdx.x; i < kBuckets; i += blockDim.x)
@@ -1505,6 +1529,68 @@ __global__ void __launch_bounds__(kCkThreads) k_chunk_scatter(const uint16_t* __
             __syncwarp();
             if (c != kNoChunk && lane == __ffs(peers) - 1) s_run[warp][c] += unsigned(__popc(peers));
             __syncwarp();
+        }
+        __syncthreads();
+    }
+}
+
+// The counting pass for at most kFewChunks chunks (every index up to 8 G suffixes at the default
+// capacity), without __match_any_sync: thread tid of a tile takes its 32 consecutive positions
+// [tile * kCkTile + 32 tid, + 32) in four 16-byte loads, and keeps one counter per chunk in its own
+// column of a shared array (no atomics, no bank conflicts): 3.3 times faster than k_chunk_tiles.
+// (Scatters built the same way -- per-thread runs, or per-chunk ballots over 32 consecutive
+// positions -- measured slower than k_chunk_scatter's __match_any_sync groups.)
+constexpr int kFewChunks = 16;
+constexpr int kCkPer = kCkTile / kCkThreads;          // 32 positions a thread
+
+__device__ __forceinline__ void load_bids32(const uint16_t* __restrict__ bid, size_t p0, size_t n, uint32_t (&w)[16]) {
+    if (p0 + kCkPer <= n) {
+        #pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint4 x = *reinterpret_cast<const uint4*>(bid + p0 + 8 * q);
+            w[4 * q] = x.x;
+            w[4 * q + 1] = x.y;
+            w[4 * q + 2] = x.z;
+            w[4 * q + 3] = x.w;
+        }
+    } else {
+        #pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            const uint32_t lo = p0 + 2 * q < n ? bid[p0 + 2 * q] : 0xffffu;
+            const uint32_t hi = p0 + 2 * q + 1 < n ? bid[p0 + 2 * q + 1] : 0xffffu;
+            w[q] = lo | (hi << 16);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kCkThreads) k_chunk_tiles_few(const uint16_t* __restrict__ bid, size_t n,
+                                                                const uint8_t* __restrict__ cmap, int nchunks,
+                                                                size_t ntiles, unsigned long long* __restrict__ tcnt) {
+    __shared__ uint8_t s_map[kBuckets + 1];
+    __shared__ unsigned s_cnt[kFewChunks][kCkThreads];
+    for (int i = threadIdx.x; i < kBuckets; i += blockDim.x) s_map[i] = cmap[i];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (size_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        #pragma unroll
+        for (int c = 0; c < kFewChunks; ++c) s_cnt[c][tid] = 0;
+        __syncthreads();
+        const size_t p0 = tile * kCkTile + size_t(tid) * kCkPer;
+        if (p0 < n) {
+            uint32_t w[16];
+            load_bids32(bid, p0, n, w);
+            #pragma unroll
+            for (int j = 0; j < kCkPer; ++j) {
+                const uint32_t b = (w[j >> 1] >> (16 * (j & 1))) & 0xffffu;
+                if (b != 0xffffu) ++s_cnt[s_map[b]][tid];
+            }
+        }
+        __syncthreads();
+        for (int c = warp; c < nchunks; c += kCkWarps) {
+            unsigned sum = 0;
+            for (int i = lane; i < kCkThreads; i += 32) sum += s_cnt[c][i];
+            #pragma unroll
+            for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+            if (lane == 0) tcnt[size_t(c) * ntiles + tile] = sum;
         }
         __syncthreads();
     }
@@ -1624,7 +1710,12 @@ int suffix_sort_chunked(const uint8_t* reads, idx_t num_reads, int L, int dir, i
     // every position into its chunk's slice of the suffix array, in text order: tile counts per
     // chunk, their scan in chunk-major order (the slices' starts included), the scatter
     const unsigned cgrid = unsigned(std::min<size_t>(ntiles, size_t(sms) * 8));
-    { k_chunk_tiles<<<cgrid, kCkThreads, 0, st>>>(bid, n, cmap, nchunks, ntiles, tcnt); note_launch(); }
+    if (nchunks <= kFewChunks) {
+        k_chunk_tiles_few<<<cgrid, kCkThreads, 0, st>>>(bid, n, cmap, nchunks, ntiles, tcnt);
+    } else {
+        k_chunk_tiles<<<cgrid, kCkThreads, 0, st>>>(bid, n, cmap, nchunks, ntiles, tcnt);
+    }
+    note_launch();
     { k_scan_small<<<1, 1024, 0, st>>>(tcnt, size_t(nchunks) * ntiles); note_launch(); }
     { k_chunk_scatter<idx_t><<<cgrid, kCkThreads, 0, st>>>(bid, n, cmap, nchunks, ntiles, tcnt, sa); note_launch(); }
     for (const Chunk& ck : chunks) {

@@ -95,6 +95,20 @@ def test_chunked_sort_matches_reference(name):
     assert sha(out.length) == str(g["sha_length"])
 
 
+@pytest.mark.parametrize("parts", [3, 40])
+def test_chunk_counts_both_paths(parts):
+    """Chunked sorts with up to 16 chunks count their positions per tile with per-thread counters,
+    with more with per-warp groups of equal chunks: both give the reference's suffix arrays."""
+    g = load_golden("rep20k_L100_t63_u64")
+    n = g["reads"].shape[0] * g["reads"].shape[1]
+    with gpu_ctx(int(g["width"])) as P:
+        P.set_reads(g["reads"], int(g["t"]))
+        P.set_sort_chunk(max(n // parts, 2))
+        for d in (0, 1):
+            P.sort(d)
+            assert sha(P.get_sa(d)) == str(g["sha_sa%d" % d])
+
+
 @pytest.mark.parametrize("k", [1, 5, 10])
 def test_seed_depth_does_not_change_edges(k):
     g = load_golden("rep15k_L100_t63_u32")
