@@ -1952,6 +1952,11 @@ __device__ __forceinline__ int block_cmp(const uint64_t* w, int cap, int nw, int
     return la == lb ? 0 : (la < lb ? -1 : 1);
 }
 
+constexpr int kBlockMaxWords = 8;       // continuation words a candidate (L - t <= 256)
+// the digit counts' index with one pad word after every 16, so that a thread summing 16
+// consecutive counts and its neighbours hit different banks
+__device__ __forceinline__ int block_pad(int f) { return f + (f >> 4); }
+
 // 4-bit digit q (0 = least significant) of candidate c's sort key: the continuation words (word 0
 // most significant), then the continuation length (16 bits), then the read id.
 __device__ __forceinline__ unsigned block_digit(const uint64_t* cw, int cap, int nw, const idx_t* cid,
@@ -1991,16 +1996,51 @@ __device__ int block_sorted_side(int m, int L, int nw, int cap, const uint64_t* 
     const int digits = 2 * int(sizeof(idx_t)) + 4 + 16 * nw;
     unsigned* s_wsum = s_misc;             // [T / 32]
     unsigned* s_dstart = s_misc + 8;       // [17]
+    // which key bits differ between candidates: each key XOR candidate 0's, OR-reduced (id, length,
+    // words); a digit whose bits never differ needs no pass at all
+    unsigned long long* s_diff = reinterpret_cast<unsigned long long*>(s_misc + 26);   // [2 + nw]
+    if (tid < 2 + nw) s_diff[tid] = 0;
+    __syncthreads();
+    {
+        unsigned long long did = 0, dlen = 0, dw[kBlockMaxWords];
+        #pragma unroll
+        for (int w = 0; w < kBlockMaxWords; ++w) dw[w] = 0;
+        const unsigned long long id0 = uint64_t(cid[0]), len0 = unsigned(L - meta_len(cmeta[0]));
+        for (int c = tid; c < m; c += T) {
+            did |= uint64_t(cid[c]) ^ id0;
+            dlen |= unsigned(L - meta_len(cmeta[c])) ^ len0;
+            #pragma unroll
+            for (int w = 0; w < kBlockMaxWords; ++w)
+                if (w < nw) dw[w] |= cw[size_t(w) * cap + c] ^ cw[size_t(w) * cap];
+        }
+        if (did) atomicOr(&s_diff[0], did);
+        if (dlen) atomicOr(&s_diff[1], dlen);
+        #pragma unroll
+        for (int w = 0; w < kBlockMaxWords; ++w)
+            if (w < nw && dw[w]) atomicOr(&s_diff[2 + w], dw[w]);
+    }
     __syncthreads();
     for (int q = 0; q < digits; ++q) {
+        {   // the digit's bits in the OR of differences: zero means every candidate has the same digit
+            constexpr int kIdDigits = 2 * int(sizeof(idx_t));
+            unsigned long long bits;
+            if (q < kIdDigits) bits = s_diff[0] >> (4 * q);
+            else if (q < kIdDigits + 4) bits = s_diff[1] >> (4 * (q - kIdDigits));
+            else {
+                const int r = q - kIdDigits - 4;
+                bits = s_diff[2 + nw - 1 - r / 16] >> (4 * (r % 16));
+            }
+            if ((bits & 15ull) == 0) continue;
+        }
         #pragma unroll
-        for (int d = 0; d < 16; ++d) scnt[d * T + tid] = 0;
-        for (int e = b0; e < b1; ++e) ++scnt[block_digit(cw, cap, nw, cid, cmeta, L, int(src[e]), q) * T + tid];
+        for (int d = 0; d < 16; ++d) scnt[block_pad(d * T + tid)] = 0;
+        for (int e = b0; e < b1; ++e)
+            ++scnt[block_pad(block_digit(cw, cap, nw, cid, cmeta, L, int(src[e]), q) * T + tid)];
         __syncthreads();
         // exclusive scan of the 16 x T counts, digit-major: thread tid owns entries [16 tid, 16 tid + 16)
         unsigned mine = 0;
         #pragma unroll
-        for (int j = 0; j < 16; ++j) mine += scnt[16 * tid + j];
+        for (int j = 0; j < 16; ++j) mine += scnt[block_pad(16 * tid + j)];
         unsigned x = mine;
         #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -2013,8 +2053,8 @@ __device__ int block_sorted_side(int m, int L, int nw, int cap, const uint64_t* 
         for (int w = 0; w < wid; ++w) run += s_wsum[w];
         #pragma unroll
         for (int j = 0; j < 16; ++j) {
-            const unsigned v = scnt[16 * tid + j];
-            scnt[16 * tid + j] = run;
+            const unsigned v = scnt[block_pad(16 * tid + j)];
+            scnt[block_pad(16 * tid + j)] = run;
             run += v;
         }
         if ((16 * tid) % T == 0) s_dstart[(16 * tid) / T] = run - mine;   // the digit's first place
@@ -2026,7 +2066,7 @@ __device__ int block_sorted_side(int m, int L, int nw, int cap, const uint64_t* 
         if (!trivial) {
             for (int e = b0; e < b1; ++e) {
                 const uint32_t c = src[e];
-                dst[scnt[block_digit(cw, cap, nw, cid, cmeta, L, int(c), q) * T + tid]++] = c;
+                dst[scnt[block_pad(block_digit(cw, cap, nw, cid, cmeta, L, int(c), q) * T + tid)]++] = c;
             }
             uint32_t* tmp = src;
             src = dst;
@@ -2100,8 +2140,8 @@ __global__ void __launch_bounds__(kBlockThreads) k_search_block(SearchArgs A, Se
     uint32_t* perm0 = reinterpret_cast<uint32_t*>(smem + lay.perm0);
     uint32_t* perm1 = reinterpret_cast<uint32_t*>(smem + lay.perm1);
     uint32_t* sinfo = reinterpret_cast<uint32_t*>(smem + lay.info);
-    unsigned* scnt = reinterpret_cast<unsigned*>(smem_dyn);              // global variant: 16 x 256 counts
-    unsigned* smisc = scnt + 16 * kBlockThreads;
+    unsigned* scnt = reinterpret_cast<unsigned*>(smem_dyn);              // global variant: 16 x 256 counts, padded
+    unsigned* smisc = scnt + 16 * kBlockThreads + 16 * kBlockThreads / 16;
     idx_t* cid = reinterpret_cast<idx_t*>(smem + lay.ids);
     uint32_t* cmeta = reinterpret_cast<uint32_t*>(smem + lay.metas);
     uint32_t* ccnt = reinterpret_cast<uint32_t*>(smem + lay.cnts);
@@ -2351,7 +2391,7 @@ BlockSmem block_global_layout(int L, int t) {
 }
 // the global variant's dynamic shared memory: the sort's 16 x kBlockThreads digit counts and a
 // few words of scan state
-constexpr size_t kBlockSortSmem = (16 * kBlockThreads + 32) * sizeof(unsigned);
+constexpr size_t kBlockSortSmem = (16 * kBlockThreads + 16 * kBlockThreads / 16 + 64) * sizeof(unsigned);
 
 size_t block_global_bytes(int L, int t, int blocks) { return size_t(blocks) * block_global_layout(L, t).bytes; }
 
