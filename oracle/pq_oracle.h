@@ -1,6 +1,6 @@
 /*
- * pq_oracle — CPU restatement of PASQUAL's hot path, used ONLY as a checker by tests/, by
- * __graft_entry__.smoke() and by bench.py's CPU-baseline leg.  It is never linked into, called
+ * pq_oracle — CPU restatement of PASQUAL's hot path: test infrastructure, the oracle of tests/ and
+ * __graft_entry__.smoke() and the timed CPU baseline of bench.py.  It is never linked into, called
  * by, or substituted for the CUDA library (pasqual_gb300/), which fails loudly instead.
  *
  * Parity of this restatement is pinned against the unmodified reference (oracle/ref_dump.c,
