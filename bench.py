@@ -473,6 +473,11 @@ def run_ours(args):
     alg_bytes = 32.0 * sec + outb
     achieved = alg_bytes / (kms * 1e-3) / 1e9
     dram_per_read = profile_figure("k_search_lean_250Mbp_L100.md", "dram_bytes_per_read")
+    # the committed capture describes this launch only if its kernel did the same work per read
+    # (same algorithmic bytes, within 5 %): otherwise no traffic figure is claimed
+    cap_alg = profile_figure("k_search_lean_250Mbp_L100.md", "algorithmic_bytes_per_read")
+    traffic_applies = bool(dram_per_read and cap_alg and args.seed_mode == 1 and
+                           abs(alg_bytes / nr - cap_alg) <= 0.05 * cap_alg)
 
     # ---- end to end through the public API with host buffers
     pinned = pinned_all[:nr]
@@ -544,7 +549,7 @@ def run_ours(args):
                      "frac": r4(achieved / peak), "peak_kind": peak_kind,
                      "kernel": "k_search_fast" if args.seed_mode == 0 else "k_search_lean", "kernel_ms": r4(kms),
                      "bytes_per_read": r4(alg_bytes / nr),
-                     "traffic": r4(dram_per_read * nr) if dram_per_read and args.seed_mode == 1 else None,
+                     "traffic": r4(dram_per_read * nr) if traffic_applies else None,
                      "reference_probes_per_read": r4(ref_ppr), "probes_per_read": r4(g.probes / nr)},
         "e2e": ({"value": r4(replica_throughput(nr, world, e2e_ms_med)), "unit": "reads/s",
                  "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": r4(e2e_ms_med),

@@ -134,7 +134,10 @@ PQ_API int pq_get_seeds (pq_ctx * ctx, int dir, pq_idx * start, pq_idx * size, u
  * pq_build_index first); field for field the reference's arrays. */
 PQ_API int pq_get_sort_seeds (pq_ctx * ctx, int dir, pq_idx * start, pq_idx * size, uint16_t * depth);
 
-/* Seed depth k of the overlap search (1 <= k <= min(13, t)); default min(12, t). */
+/* Seed depth k of the overlap search (1 <= k <= min(14, t)): the k-mer table of 4^k entries per
+ * index that seeds the walks and narrows the interval scans.  Default, per read set: 14 from 2^32
+ * suffixes per index, 13 from 2^30, else 12, never above t; a value set here is kept for later
+ * read sets. */
 PQ_API int pq_set_seed_k (pq_ctx * ctx, int k);
 
 /* How the candidates of each read are found.  0 walks from the depth-k seed to depth L with one

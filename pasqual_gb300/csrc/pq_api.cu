@@ -73,6 +73,7 @@ struct pq_ctx {
     idx_t num_reads = 0;
     int L = 0, t = 0;
     int seed_k = 0;
+    int seed_k_user = 0;      // set by pq_set_seed_k: kept for every later read set
     int seed_mode = 1;        // 1: candidates by depth-t interval scan, 0: walk from the k-mer seed
     DevBuf reads;
     idx_t C[6] = {0}, sfx[4] = {0}, pfx[4] = {0};
@@ -279,7 +280,13 @@ int pq_set_reads(pq_ctx* ctx, const uint8_t* reads, pq_idx num_reads, int read_l
     ctx->num_reads = num_reads;
     ctx->L = read_len;
     ctx->t = min_overlap;
-    if (!ctx->seed_k) ctx->seed_k = std::min(12, min_overlap);
+    // default seed depth by index size: a k-mer's rows number about n / 4^k, and each halving of
+    // them saves a bisection step of every interval scan (the 250 Mbp workload's search: 189 ms at
+    // k = 12, 166 at 13, 148 at 14), for 4^k table entries (2 per index, IDX bytes each)
+    if (!ctx->seed_k_user) {
+        const unsigned long long n_sfx = (unsigned long long)num_reads * (unsigned)read_len;
+        ctx->seed_k = n_sfx >= (1ull << 32) ? 14 : (n_sfx >= (1ull << 30) ? 13 : 12);
+    }
     ctx->seed_k = std::min(ctx->seed_k, min_overlap);
     size_t bytes = size_t(num_reads) * read_len;
     CK(ctx->reads.ensure(bytes + 64));
@@ -474,9 +481,10 @@ int pq_apply_sort_seeds(pq_ctx* ctx, int dir, uint64_t r0, uint64_t r1, pq_idx* 
 
 int pq_set_seed_k(pq_ctx* ctx, int k) {
     if (!ctx) return PQ_ERR_ARG;
-    if (k < 1 || k > 13) return fail(ctx, PQ_ERR_ARG, "seed depth must be in [1, 13]");
+    if (k < 1 || k > pq::kSortKeyBases) return fail(ctx, PQ_ERR_ARG, "seed depth must be in [1, 14]");
     if (ctx->have_reads && k > ctx->t) return fail(ctx, PQ_ERR_ARG, "seed depth must not exceed t");
     ctx->seed_k = k;
+    ctx->seed_k_user = 1;
     return PQ_OK;
 }
 

@@ -109,7 +109,7 @@ def test_chunk_counts_both_paths(parts):
             assert sha(P.get_sa(d)) == str(g["sha_sa%d" % d])
 
 
-@pytest.mark.parametrize("k", [1, 5, 10])
+@pytest.mark.parametrize("k", [1, 5, 10, 14])
 def test_seed_depth_does_not_change_edges(k):
     g = load_golden("rep15k_L100_t63_u32")
     with gpu_ctx(32) as P:
