@@ -579,6 +579,15 @@ def run_ours(args):
     out["modes"] = detail.get("modes")
     out["mixed_sets"] = detail.get("mixed_sets")
     out["sort_msuffix_per_s"] = r4(2 * n / (sort_ms_med * 1e-3) / 1e6)
+    # the sort against its algorithmic bytes: per suffix, the 2-bit text of the prefix that tells
+    # it apart from its neighbours plus one suffix-array entry (measured on the oracle's suffix
+    # arrays of a sample of this workload, recorded with the launch list)
+    sbytes = (profile_figure("launches_250Mbp_L100_full.md", "sort_bytes_per_suffix")
+              if args.workload == "250Mbp_L100_20x_t55" else None)
+    if sbytes:
+        sach = sbytes * 2 * n / (sort_ms_med * 1e-3) / 1e9
+        out["sort_roofline"] = {"bound": "hbm", "achieved": r4(sach), "peak": peak, "unit": "GB/s",
+                                "frac": r4(sach / peak), "bytes_per_suffix": sbytes}
     if "modes" in detail:
         mo = detail["modes"]
         out["plain_reads_per_s"] = mo["plain"]["reads_per_s"]
