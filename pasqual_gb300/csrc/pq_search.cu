@@ -1864,13 +1864,15 @@ size_t lean_scratch_bytes(int L, int t, int lean_blocks, int fast_blocks, int eb
 // where a read's side can have thousands.  The block tier gives each such read one CTA: two
 // threads walk the two sides (chain_pair, from exact k-mer seeds, with the reference's depths),
 // the CTA expands every candidate group into its candidates (read id from the suffix array,
-// continuation from the packed text), and reduces each side as reduce_sorted does, with the
+// continuation from the packed text), and reduces each side as reduce_gathered does, with the
 // m x m ordered pairs of candidates spread over the CTA's threads: candidate c is covered when
 // another candidate's continuation is a proper prefix of its own, trans(c) counts the
 // continuations that start with c's, first_same(c) tells whether a candidate of the side's first
 // kind has exactly c's continuation.  The emitted candidates are then ranked in DFS order
-// (continuation, read id) by counting, again over pairs.  Everything lives in shared memory; a
-// side with more candidates than fit goes on to the heavy and wide tiers as before.
+// (continuation, read id) by counting, again over pairs.  In this variant everything lives in
+// shared memory; a side with more candidates than fit goes to the variant with its arrays in
+// global memory, which reduces by sorting (block_sorted_side), and only a side beyond that one's
+// capacity goes on to the heavy and wide tiers.
 
 constexpr int kBlockThreads = 256;
 constexpr size_t kBlockSmemBudget = 200 * 1024;     // dynamic shared memory of one block-tier CTA
@@ -2307,7 +2309,7 @@ __global__ void __launch_bounds__(kBlockThreads) k_search_block(SearchArgs A, Se
             if (tid == 0) s_cnt[side] = ne;
             __syncthreads();
         }
-        if (!s_ok) {             // more candidates than fit: the heavy tier
+        if (!s_ok) {             // more candidates than fit: the next tier
             if (tid == 0) {
                 const unsigned k = atomicAdd(next_count, 1u);
                 next_list[k] = self;
@@ -2318,7 +2320,7 @@ __global__ void __launch_bounds__(kBlockThreads) k_search_block(SearchArgs A, Se
         const int nb = s_cnt[0], nf = s_cnt[1], ne = nb + nf;
         if (tid == 0) {
             s_base = ne ? atomicAdd(O.e_count, (unsigned long long)ne) : 0ull;
-            if (s_base + ne > O.e_cap) {         // edge pool full: the wide tier grows it
+            if (s_base + ne > O.e_cap) {         // edge pool full: the host grows it, runs the read again
                 O.status[self] = OVF_POOL;
                 const unsigned k = atomicAdd(next_count, 1u);
                 next_list[k] = self;
